@@ -1,0 +1,352 @@
+"""Benchmark: converged MLWF solves/s on one GB300 (replicas over N GPUs).
+
+Workload (default ``fcc10_w32``): seeded tight-binding problem, fcc a = 6 A, 10x10x10
+k-mesh (1000 k), nntot = 8, num_wann = 32, hopping range 3 cells, gauge noise 0.3,
+run to convergence (conv_tol = 1e-10 A^2 over conv_window = 5).  One *step* is one
+full wann_main solve starting from the Loewdin-projected M^(0), U^(0).
+
+value : solves/s with M^(0), U^(0) resident in HBM (device-pointer entry point);
+        M (131 MB) plus the solver state exceed the 129 MB L2, so no flush is needed.
+e2e   : solves/s through the reference-named C ABI (cwannierise) with host buffers:
+        per step H2D of M and U, D2H of the rotated M and final U.
+roofline: dominant kernel, timed live with CUDA events on its launch stream
+        (profiling pass of the engine), algorithmic FLOPs per launch.
+cpu_baseline: the NumPy oracle (CPU restatement of wann_main) on the host cores, one
+        process per core over the same problem, a bounded number of iterations,
+        converted to solves/s with the GPU's iteration count per solve.
+
+``--impl reference`` times that CPU restatement alone (the reference wannier90.x is
+Fortran and cannot be built in this image), printing the same metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "converged MLWF solves/s"
+WORKLOADS = {
+    "fcc10_w32": dict(cfg="fcc10_w32", conv_tol=1e-10, conv_window=5, num_iter=20000),
+    "sc4_w8": dict(cfg="sc4_w8", conv_tol=1e-10, conv_window=-1, num_iter=200),
+}
+
+
+def _env_rank():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0")),
+            int(os.environ.get("WORLD_SIZE", "1")))
+
+
+# ----------------------------------------------------------------------------------
+# CPU restatement timing (oracle) -- used by the cpu_baseline leg and --impl reference
+# ----------------------------------------------------------------------------------
+def _cpu_worker(args):
+    wl, seed, iters = args
+    os.environ["OPENBLAS_NUM_THREADS"] = "1"
+    os.environ["OMP_NUM_THREADS"] = "1"
+    import numpy as np  # noqa: F401
+
+    from oracle import w90_oracle as O
+    from wannier90_gb300 import synth
+
+    p = synth.make_problem(**synth.CONFIGS[wl["cfg"]], seed=seed)
+    M = synth.to_math_m(p.m)
+    A = synth.to_math_u(p.a)
+    km = O.kmesh_get(p.real_lattice, p.kpoints)
+    U0, M0 = O.overlap_project(M, A, km["nnlist"])
+    ctl = O.WannControl(num_iter=iters, conv_tol=wl["conv_tol"], conv_window=-1)
+    t = time.perf_counter()
+    r = O.wann_main(M0, U0, km, ctl, record=False)
+    dt = time.perf_counter() - t
+    return dt / max(r.niter, 1)
+
+
+def cpu_seconds_per_iteration(wl, iters, procs):
+    ctx = mp.get_context("spawn")
+    env_old = os.environ.get("OPENBLAS_NUM_THREADS")
+    os.environ["OPENBLAS_NUM_THREADS"] = "1"
+    try:
+        with ctx.Pool(procs) as pool:
+            per = pool.map(_cpu_worker, [(wl, 0, iters)] * procs)
+    finally:
+        if env_old is None:
+            os.environ.pop("OPENBLAS_NUM_THREADS", None)
+        else:
+            os.environ["OPENBLAS_NUM_THREADS"] = env_old
+    return statistics.mean(per)
+
+
+# ----------------------------------------------------------------------------------
+# clocks sampling during the timed region
+# ----------------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            p = [x.strip() for x in l.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------------
+def run_reference_arm(args, wl):
+    rank, _, world = _env_rank()
+    if rank != 0:
+        return 0
+    procs = os.cpu_count() or 1
+    iters = args.cpu_iters
+    spi = cpu_seconds_per_iteration(wl, iters, procs)
+    niter = args.assume_iters
+    # each step: a bounded sample (iters iterations on every core); solves/s extrapolated
+    t_steps = []
+    for _ in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        s = cpu_seconds_per_iteration(wl, max(2, iters // 2), procs)
+        t_steps.append(time.perf_counter() - t0)
+        spi = 0.5 * (spi + s)
+    value = procs / (spi * niter)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(t_steps[args.warmup:]),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded tight-binding generator)",
+        "config": {"workload": args.workload, "note": "CPU restatement of wann_main (NumPy/LAPACK), "
+                   "not wannier90.x: no Fortran compiler in the image"},
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": procs, "kind": "port",
+                         "sample": "%d iterations per core of the %s solve (1 process per core, 1 BLAS thread), "
+                                   "solves/s = cores / (s_per_iter * %d iterations per solve)"
+                                   % (iters, args.workload, niter)},
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="fcc10_w32", choices=sorted(WORKLOADS))
+    ap.add_argument("--cpu-iters", type=int, default=4)
+    ap.add_argument("--assume-iters", type=int, default=0,
+                    help="iterations per solve for the reference arm (0: measured by the GPU arm's table)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-iters", type=int, default=6)
+    ap.add_argument("--e2e-steps", type=int, default=1)
+    args = ap.parse_args()
+    wl = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        if args.assume_iters <= 0:
+            args.assume_iters = KNOWN_ITERS.get(args.workload, 1000)
+        return run_reference_arm(args, wl)
+
+    rank, local_rank, world = _env_rank()
+    import numpy as np
+    import torch
+
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA GPU")
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    from wannier90_gb300 import library as w90
+    from wannier90_gb300 import synth
+    from wannier90_gb300._native import lib
+
+    # problem (replicas: every rank solves its own copy of the same seeded problem)
+    p = synth.make_problem(**synth.CONFIGS[wl["cfg"]], seed=0)
+    W, K, B = p.num_wann, len(p.kpoints), p.nntot
+    opts = dict(num_iter=wl["num_iter"], conv_tol=wl["conv_tol"], conv_window=wl["conv_window"], iprint=0)
+    h = w90.setup(kpoints=p.kpoints, unit_cell_cart=p.real_lattice, num_wann=W, **opts)
+    stream = torch.cuda.Stream()
+    w90.w90_set_stream(h, stream.cuda_stream)
+    # Loewdin projection on the device -> resident M0, U0
+    m_dev = torch.from_numpy(p.m.reshape(-1, order="F").view(np.float64).copy()).cuda()
+    u_dev = torch.from_numpy(p.a.reshape(-1, order="F").view(np.float64).copy()).cuda()
+    torch.cuda.synchronize()
+    w90.check(h, w90.w90_project_overlap_device(h, m_dev.data_ptr(), u_dev.data_ptr()), "project")
+    torch.cuda.synchronize()
+    m0, u0 = m_dev.clone(), u_dev.clone()
+    m_work, u_work = torch.empty_like(m0), torch.empty_like(u0)
+
+    def device_step():
+        with torch.cuda.stream(stream):
+            m_work.copy_(m0)
+            u_work.copy_(u0)
+        ierr = w90.w90_wannierise_device(h, m_work.data_ptr(), u_work.data_ptr())
+        if ierr > 0:
+            raise RuntimeError(h.last_error())
+
+    for _ in range(args.warmup):
+        device_step()
+    torch.cuda.synchronize()
+    log = w90.w90_get_log(h, wl["num_iter"] + 1)
+    niter = int(log[-1][0])
+    launches = w90.w90_kernel_launches(h)
+    clocks = ClockSampler(local_rank)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        device_step()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    if dist:
+        dist.barrier()
+    ms = ev0.elapsed_time(ev1)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / args.steps
+    value = world * 1e3 / ms_per_step
+
+    # e2e through the reference-named C ABI with host buffers (pinned)
+    m_host0 = torch.from_numpy(m0.cpu().numpy()).pin_memory()
+    u_host0 = torch.from_numpy(u0.cpu().numpy()).pin_memory()
+    m_host = torch.empty_like(m_host0).pin_memory()
+    u_host = torch.empty_like(u_host0).pin_memory()
+    L = lib()
+    import ctypes as C
+    uopt = np.asfortranarray(np.broadcast_to(np.eye(W, dtype=np.complex128)[:, :, None], (W, W, K)).copy())
+    L.cset_u_opt(h.handle, uopt.ctypes.data)
+    L.cset_m_local(h.handle, C.c_void_p(m_host.data_ptr()))
+    L.cset_u_matrix(h.handle, C.c_void_p(u_host.data_ptr()))
+
+    def e2e_step():
+        m_host.copy_(m_host0)
+        u_host.copy_(u_host0)
+        ierr = C.c_int(0)
+        t0 = time.perf_counter()
+        L.cwannierise(h.handle, C.byref(ierr))
+        dt = time.perf_counter() - t0
+        if ierr.value > 0:
+            raise RuntimeError(h.last_error())
+        return dt
+
+    e2e_t = [e2e_step() for _ in range(max(1, args.e2e_steps))]
+    e2e_value = world / statistics.mean(e2e_t)
+    bytes_m = W * W * B * K * 16
+    bytes_u = W * W * K * 16
+
+    # roofline of the dominant kernel (profiling pass, CUDA events on the launch stream)
+    msk = (C.c_double * 8)()
+    cnt = (C.c_int * 8)()
+    with torch.cuda.stream(stream):
+        m_work.copy_(m0)
+        u_work.copy_(u0)
+    torch.cuda.synchronize()
+    ierr = L.w90g_profile_device(h.handle, C.c_void_p(m_work.data_ptr()), C.c_void_p(u_work.data_ptr()),
+                                 args.profile_iters, msk, cnt)
+    names = [L.w90g_profile_kernel_name(i).decode() for i in range(8)]
+    per_kernel = {n: {"ms_total": msk[i], "launches": cnt[i],
+                      "ms_avg": (msk[i] / cnt[i]) if cnt[i] else None} for i, n in enumerate(names)}
+    fp64_peak = L.w90g_measure_fp64_peak()
+    dom = "k_m_update"
+    avg = per_kernel[dom]["ms_avg"]
+    flops_launch = 2 * 8.0 * W ** 3 * K * B   # two complex W^3 GEMMs per (k,b)
+    achieved = flops_launch / (avg * 1e-3) / 1e12 if avg else None
+    roof = {"bound": "fp64", "kernel": dom, "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+            "frac": (achieved / fp64_peak) if (achieved and fp64_peak > 0) else None, "traffic": None,
+            "peak_source": "FP64 FMA probe measured in this run (MEASURED_PEAKS.json has no FP64 figure)",
+            "algorithmic_flops_per_launch": flops_launch, "per_kernel": per_kernel}
+
+    # CPU baseline (oracle on host cores, bounded sample)
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        procs = os.cpu_count() or 1
+        spi = cpu_seconds_per_iteration(wl, args.cpu_iters, procs)
+        cpu = {"value": procs / (spi * niter), "unit": "solves/s", "cores": procs, "kind": "port",
+               "sample": "%d iterations of the %s solve on each of %d cores (1 process per core, 1 BLAS "
+                         "thread); solves/s = cores / (%.3f s/iter * %d iter/solve)"
+                         % (args.cpu_iters, args.workload, procs, spi, niter)}
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded tight-binding generator)",
+            "config": {"workload": args.workload, "lattice": synth.CONFIGS[wl["cfg"]]["kind"],
+                       "num_kpts": K, "nntot": B, "num_wann": W, "conv_tol": wl["conv_tol"],
+                       "conv_window": wl["conv_window"], "iterations_per_solve": niter,
+                       "precision": "fp64", "l2": "inputs larger than L2 (M = %d MB)" % (bytes_m >> 20),
+                       "parallelism": "replicas" if world > 1 else "single"},
+            "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": bytes_m + bytes_u,
+                    "d2h_bytes_per_step": bytes_m + bytes_u},
+            "gpu_launches": int(launches) * args.steps,
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "clocks": clk,
+        }
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+# iterations per solve of each workload as measured by the GPU arm (FP64 engine)
+KNOWN_ITERS = {"fcc10_w32": 1824, "sc4_w8": 200}
+
+if __name__ == "__main__":
+    sys.exit(main())

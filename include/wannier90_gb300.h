@@ -1,0 +1,141 @@
+/*
+ * wannier90_gb300.h -- C ABI of the GB300 MLWF (wann_main) engine.
+ *
+ * The first group of entry points carries the names, argument order and meaning of
+ * Wannier90's own C binding of its library (src/c_interface.F90, prototypes in
+ * src/wannier90.hh), so a code that drives Wannier90 through `w90_create`/`cset_*`/
+ * `cinput_setopt`/`cwannierise`/`cget_*` can link this library instead for the
+ * wannierisation step.  Differences, all at the type level:
+ *   - keywords and seednames are NUL-terminated `const char*` (the reference passes a
+ *     Fortran CFI descriptor built by the std::string helpers of wannier90.hh; the
+ *     same helper overloads are provided below for C++ callers);
+ *   - `int&` out-arguments are `int*` (identical calling convention);
+ *   - complex arrays are `double*` pointing at interleaved (re, im) pairs, i.e. the
+ *     memory of `std::complex<double>` / Fortran `complex(8)` arrays;
+ *   - the MPI communicator argument of cinput_setopt is accepted and ignored (one
+ *     process drives one GPU; k-points are never distributed).
+ *
+ * Array layouts are the reference's (Fortran column-major):
+ *   m matrix   [nk][nntot][nb][nb]   element (m,n,b,k) at m + nb*(n + nb*(b + nntot*k))
+ *   u matrix   [nk][nw][nw]          element (m,n,k)  at m + nw*(n + nw*k)
+ *   u_opt      [nk][nw][nb]
+ *   eigval     [nk][nb]
+ *   nnkp       [nntot][nk] int32, 1-based k+b indices (cget_nnkp)
+ *   centres    [nw][3], spreads [nw]
+ * Error convention (src/error.F90:25-35): ierr = 0 ok; >0 error (1 fatal, 2 alloc,
+ * 5 input/unsupported option, 6 file); <0 warning (-1 not converged).
+ *
+ * The engine never aborts the process; CUDA errors map to ierr = 1, device OOM to 2.
+ */
+#ifndef WANNIER90_GB300_H
+#define WANNIER90_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- handle lifecycle: src/c_interface.F90:10-25 ------------------------------- */
+void* w90_create(void);
+void w90_delete(void* handle);
+
+/* ---- options: src/c_interface.F90:179-247 (cset_option_*), library keywords of
+ *      w90_set_option (src/library_interface.F90:667-808) ---------------------------- */
+void cset_option_int(void* handle, const char* keyword, int value);
+void cset_option_int3(void* handle, const char* keyword, const int* value3);
+void cset_option_intx(void* handle, const char* keyword, const int* values, int count);
+void cset_option_float(void* handle, const char* keyword, double value);
+/* value: double[3][3] row-major, row i = a_i (Angstrom) for unit_cell_cart */
+void cset_option_float33(void* handle, const char* keyword, const double* value33);
+/* value: double[x][y] row-major (e.g. kpoints: x = num_kpts, y = 3) */
+void cset_option_floatxy(void* handle, const char* keyword, const double* values, int x, int y);
+
+/* ---- process options, build the k-mesh: src/c_interface.F90:49-68 ---------------- */
+void cinput_setopt(void* handle, const char* seedname, int* ierr, int comm);
+
+/* ---- data pointers (caller keeps ownership): src/c_interface.F90:82-127 ----------- */
+void cset_eigval(void* handle, double* eigval);
+void cset_m_local(void* handle, double* m_matrix);
+void cset_u_matrix(void* handle, double* u_matrix);
+void cset_u_opt(void* handle, double* u_opt);
+
+/* ---- work: src/c_interface.F90:38-47 (cwannierise -> w90_wannierise ->
+ *      wann_main, src/library_interface.F90:464-530) ----------------------------------
+ * On entry m holds the projected M^(0) and u the initial U (after cproject_overlap);
+ * on exit u holds the final U and m is rotated in place to the final gauge. */
+void cwannierise(void* handle, int* ierr);
+
+/* ---- getters: src/c_interface.F90:129-177 ------------------------------------------ */
+void cget_nn(void* handle, int* nntot);
+void cget_nnkp(void* handle, int* nnkp);
+void cget_centres(void* handle, double* centres);
+void cget_spreads(void* handle, double* spreads);
+
+/* ---- additions the isolated-band C path needs -----------------------------------
+ * cproject_overlap: Loewdin initialisation w90_project_overlap -> overlap_project
+ *   (src/library_interface.F90:422-462, src/overlap.F90:758-952), which the reference
+ *   exports to Fortran only.  On entry u holds A(k) (num_wann x num_wann), m the raw
+ *   overlaps; on exit u = Z V^dagger and m = U^dagger M U(k+b).
+ * cget_omega: (Omega_I, Omega_D, Omega_OD, Omega_total) of the last wannierisation
+ *   (common_data%omega / wann_spread, src/wannierise.F90:457-470). */
+void cproject_overlap(void* handle, int* ierr);
+void cget_omega(void* handle, double* omega4);
+/* cget_gkpb: nncell of kmesh_info ([nntot][nk][3] int32), the G offsets of k+b
+ *   (w90_get_gkpb, src/library_interface.F90:866-900) */
+void cget_gkpb(void* handle, int* gkpb);
+
+/* ---- engine extensions (no counterpart in the reference) ---------------------------- */
+/* Last error message ("" when none). */
+const char* w90g_last_error(void* handle);
+/* Per-iteration record of the last wannierisation: rows of 10 doubles
+ *   (iter, delta Omega, RMS gradient, Omega_total, Omega_D, Omega_OD, lquad, alphamin,
+ *    device timestamp ns, 0) for iter = 0 (initial state) .. niter.
+ * Returns the number of rows written (<= max_rows). */
+int w90g_get_log(void* handle, double* rows, int max_rows);
+/* centres/spreads per iteration: rows of 4*num_wann doubles (x[W], y[W], z[W], spread[W]) */
+int w90g_get_log_centres(void* handle, double* rows, int max_rows);
+/* Same as cwannierise / cproject_overlap but m and u are DEVICE pointers (CUDA memory of
+ * the current device, same layouts); results are written back to them on the device. */
+void w90g_wannierise_device(void* handle, double* d_m_matrix, double* d_u_matrix, int* ierr);
+void w90g_project_overlap_device(void* handle, double* d_m_matrix, double* d_u_matrix, int* ierr);
+/* Run the engine's work on a caller-provided cudaStream_t (NULL = the engine's own). */
+void w90g_set_stream(void* handle, void* cuda_stream);
+/* Number of engine kernels launched by the last call on this handle. */
+long long w90g_kernel_launches(void* handle);
+/* Profiling run of wannierise on device buffers: every kernel launched alone and timed
+ * with CUDA events on the launching stream (at most max_iters iterations).  ms[i] and
+ * counts[i] (w90g_profile_kernel_name(i), i < 8) receive total time and launches that
+ * did work.  Returns ierr.  The per-kernel sequence and arithmetic equal cwannierise's. */
+int w90g_profile_device(void* handle, double* d_m_matrix, double* d_u_matrix, int max_iters,
+                        double* ms, int* counts);
+const char* w90g_profile_kernel_name(int i);
+/* FP64 FMA throughput of the current device in TFLOP/s (dependent-chain probe). */
+double w90g_measure_fp64_peak(void);
+
+#ifdef __cplusplus
+}  /* extern "C" */
+
+#include <complex>
+#include <string>
+/* std::string helpers with the reference's names and argument lists (src/wannier90.hh:43-99) */
+inline void cinput_setopt(void* blob, std::string seed, int& ierr, int comm = 0) {
+  cinput_setopt(blob, seed.c_str(), &ierr, comm);
+}
+inline void cset_option(void* blob, std::string key, int x) { cset_option_int(blob, key.c_str(), x); }
+inline void cset_option(void* blob, std::string key, int x[3]) { cset_option_int3(blob, key.c_str(), x); }
+inline void cset_option(void* blob, std::string key, int* x, int y) { cset_option_intx(blob, key.c_str(), x, y); }
+inline void cset_option(void* blob, std::string key, double x[][3]) {
+  cset_option_float33(blob, key.c_str(), &x[0][0]);
+}
+inline void cset_option(void* blob, std::string key, double x) { cset_option_float(blob, key.c_str(), x); }
+inline void cset_option(void* blob, std::string key, double* x, int i1, int i2) {
+  cset_option_floatxy(blob, key.c_str(), x, i1, i2);
+}
+inline void cwannierise(void* blob, int& ierr) { cwannierise(blob, &ierr); }
+inline void cproject_overlap(void* blob, int& ierr) { cproject_overlap(blob, &ierr); }
+inline void cget_nn(void* blob, int& n) { cget_nn(blob, &n); }
+inline void cset_m_local(void* blob, std::complex<double>* m) { cset_m_local(blob, reinterpret_cast<double*>(m)); }
+inline void cset_u_matrix(void* blob, std::complex<double>* u) { cset_u_matrix(blob, reinterpret_cast<double*>(u)); }
+inline void cset_u_opt(void* blob, std::complex<double>* u) { cset_u_opt(blob, reinterpret_cast<double*>(u)); }
+#endif
+
+#endif /* WANNIER90_GB300_H */

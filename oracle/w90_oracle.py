@@ -1,0 +1,543 @@
+"""CPU oracle for the MLWF spread-minimisation path (test infrastructure only).
+
+This module is a plain NumPy/SciPy restatement of Wannier90's ``wann_main``
+path and of the set-up steps that feed it.  It exists so that the tests, the
+``smoke()`` entry and the ``cpu_baseline`` leg of ``bench.py`` can check and
+time the CUDA engine.  Nothing in the product (``wannier90_gb300``) imports it;
+the engine never falls back to it.
+
+Every function cites the reference routine it follows (paths are relative to
+the Wannier90 source tree).  Arithmetic is FP64 / complex128 throughout, as in
+the reference (``src/constants.F90`` ``dp``).  LAPACK ``zheev`` and ``zgesvd``
+are called through ``scipy.linalg.lapack`` (same LAPACK routines the reference
+links; bundled OpenBLAS build).
+
+Parity pin: ``tests/test_oracle_golden.py`` runs this oracle on the reference's
+own regression inputs (Pb, GaAs, diamond, basic1; fixtures under
+``tests/golden/``) and compares every printed ``<-- CONV`` spread (10 decimals),
+the final centres/spreads and the b-vector tables with the reference's
+benchmark outputs.
+
+Array conventions (oracle-internal, "math" layout):
+  M[k, b, m, n]  = M_mn^{(k,b)}     complex128  (K, B, W, W)
+  U[k, m, n]     = U_mn^{(k)}       complex128  (K, W, W)
+  bk[k, b, :]    = b-vector (Cartesian, 1/Angstrom)
+  nnlist[k, b]   = 0-based index of k+b
+The reference stores the same data Fortran column-major, i.e. ``m_matrix(m,n,b,k)``;
+``from_fortran_m``/``to_fortran_m`` convert.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+from scipy.linalg import lapack
+
+# src/constants.F90:109 (CODATA 2006, the default build)
+BOHR_ANGSTROM = 0.52917720859
+TWOPI = 2.0 * math.pi
+EPS_DP = np.finfo(np.float64).eps      # Fortran epsilon(1.0_dp)
+TINY_DP = np.finfo(np.float64).tiny    # Fortran tiny(1.0_dp)
+EPS5 = 1.0e-5
+EPS6 = 1.0e-6
+EPS8 = 1.0e-8
+
+
+# ---------------------------------------------------------------------------
+# layout helpers
+# ---------------------------------------------------------------------------
+def from_fortran_m(flat, W, B, K):
+    """Fortran ``m_matrix(W,W,B,K)`` buffer -> M[k,b,m,n]."""
+    a = np.asarray(flat).reshape(K, B, W, W)  # [k][b][n][m]
+    return np.ascontiguousarray(a.transpose(0, 1, 3, 2))
+
+
+def to_fortran_m(M):
+    return np.ascontiguousarray(M.transpose(0, 1, 3, 2)).reshape(-1)
+
+
+def from_fortran_u(flat, W, K):
+    a = np.asarray(flat).reshape(K, W, W)
+    return np.ascontiguousarray(a.transpose(0, 2, 1))
+
+
+def to_fortran_u(U):
+    return np.ascontiguousarray(U.transpose(0, 2, 1)).reshape(-1)
+
+
+# ---------------------------------------------------------------------------
+# lattice helpers  (src/utility.F90:233-336, :426-446)
+# ---------------------------------------------------------------------------
+def recip_lattice(real_lattice):
+    """utility_recip_lattice_base: rows b_i = 2*pi (a_j x a_k)/det."""
+    a = np.asarray(real_lattice, dtype=np.float64)
+    cof = np.empty((3, 3))
+    cof[0] = np.cross(a[1], a[2])
+    cof[1] = np.cross(a[2], a[0])
+    cof[2] = np.cross(a[0], a[1])
+    det = float(np.dot(a[0], cof[0]))
+    return TWOPI * cof / det, abs(det)
+
+
+def frac_to_cart(frac, lattice):
+    return np.asarray(frac) @ np.asarray(lattice)
+
+
+# ---------------------------------------------------------------------------
+# k-mesh  (src/kmesh.F90:61-740, :984-1104, :1107-1432)
+# ---------------------------------------------------------------------------
+NSUPCELL = 5  # src/kmesh.F90:55
+
+
+def _supercell_sort(recip):
+    """kmesh_supercell_sort (src/kmesh.F90:984-1038) incl. internal_maxloc tie rule."""
+    n = NSUPCELL
+    lmn = [(0, 0, 0)]
+    for l in range(-n, n + 1):
+        for m in range(-n, n + 1):
+            for nn in range(-n, n + 1):
+                if l == 0 and m == 0 and nn == 0:
+                    continue
+                lmn.append((l, m, nn))
+    lmn = np.array(lmn, dtype=np.int64)
+    dist = np.sqrt(((lmn @ recip) ** 2).sum(axis=1))
+    N = len(lmn)
+    out = np.empty_like(lmn)
+    d = dist.copy()
+    alive = np.ones(N, dtype=bool)
+    for pos in range(N - 1, -1, -1):
+        mx = np.max(np.where(alive, d, -1.0))
+        # lowest index among (near-)degenerate maxima  (internal_maxloc, :1866-1883)
+        g = int(np.argmax(np.where(alive, d, -1.0)))
+        cand = np.where(alive & (np.abs(d - d[g]) < EPS8))[0]
+        idx = int(cand.min()) if len(cand) else g
+        del mx
+        out[pos] = lmn[idx]
+        alive[idx] = False
+        d[idx] = -1.0
+    return out
+
+
+def _get_bvectors(kpt_cart, recip, lmn, shell_dist, multi, tol):
+    """kmesh_get_bvectors (src/kmesh.F90:1041-1104) for origin k-point 1."""
+    bvec = []
+    for cell in lmn:
+        vkpp2 = cell @ recip
+        for nkp2 in range(len(kpt_cart)):
+            vkpp = vkpp2 + kpt_cart[nkp2]
+            dist = np.sqrt(((kpt_cart[0] - vkpp) ** 2).sum())
+            if shell_dist * (1.0 - tol) <= dist <= shell_dist * (1.0 + tol):
+                bvec.append(vkpp - kpt_cart[0])
+            if len(bvec) == multi:
+                return np.array(bvec)
+    return np.array(bvec)
+
+
+def kmesh_get(real_lattice, kpt_latt, search_shells=36, tol=1.0e-6):
+    """Restatement of kmesh_get (src/kmesh.F90:61-740), automatic shells only.
+
+    Returns dict(nntot, nnlist[K,B] (0-based), nncell[K,B,3], wb[B], bk[K,B,3],
+    wbtot, shells, dnn, multi).
+    """
+    recip, _ = recip_lattice(real_lattice)
+    lmn = _supercell_sort(recip)
+    kpt_latt = np.asarray(kpt_latt, dtype=np.float64)
+    K = len(kpt_latt)
+    kpt_cart = kpt_latt @ recip
+    eta = 99999999.0
+
+    # shell distances / multiplicities (src/kmesh.F90:129-158); the reference scans
+    # |k + G| over all k-points and cells, keeping the smallest distance above the
+    # previous shell and counting its multiplicity
+    cell_cart = lmn @ recip
+    alld = np.sqrt(((kpt_cart[:, None, :] + cell_cart[None, :, :]) ** 2).sum(axis=2)).reshape(-1)
+    dnn, multi = [], []
+    dnn0 = 0.0
+    for _ in range(search_shells):
+        cand = alld[(alld > tol) & (alld > dnn0 + tol)]
+        if len(cand) == 0:
+            dnn.append(eta)
+            multi.append(0)
+            dnn0 = eta
+            continue
+        dnn1 = float(cand.min())
+        counter = int(((cand > dnn1 - tol) & (cand < dnn1 + tol)).sum())
+        dnn.append(dnn1)
+        multi.append(counter)
+        dnn0 = dnn1
+    # kmesh_shell_automatic (src/kmesh.F90:1107-1432)
+    target = np.array([1.0, 1.0, 1.0, 0.0, 0.0, 0.0])
+    shell_list, shell_bvecs = [], []
+    bweight = None
+    for shell in range(search_shells):
+        bv = _get_bvectors(kpt_cart, recip, lmn, dnn[shell], multi[shell], tol)
+        lpar = False
+        for b1 in bv:
+            for prev in shell_bvecs:
+                for b2 in prev:
+                    delta = np.dot(b1, b2) / math.sqrt(np.dot(b1, b1) * np.dot(b2, b2))
+                    if abs(abs(delta) - 1.0) < EPS6:
+                        lpar = True
+        if lpar:
+            continue
+        shell_list.append(shell)
+        shell_bvecs.append(bv)
+        ns = len(shell_list)
+        amat = np.zeros((6, ns))
+        for s, b in enumerate(shell_bvecs):
+            amat[0, s] = (b[:, 0] * b[:, 0]).sum()
+            amat[1, s] = (b[:, 1] * b[:, 1]).sum()
+            amat[2, s] = (b[:, 2] * b[:, 2]).sum()
+            amat[3, s] = (b[:, 0] * b[:, 1]).sum()
+            amat[4, s] = (b[:, 1] * b[:, 2]).sum()
+            amat[5, s] = (b[:, 2] * b[:, 0]).sum()
+        u, sv, vt = np.linalg.svd(amat, full_matrices=True)
+        if np.any(np.abs(sv) < EPS5):
+            if ns == 1:
+                raise RuntimeError("kmesh_shell_automatic: very small singular value")
+            shell_list.pop()
+            shell_bvecs.pop()
+            continue
+        w = vt.T @ ((u.T @ target)[:ns] / sv)
+        b1sat = True
+        for i in range(3):
+            for j in range(i, 3):
+                delta = sum(w[s] * (b[:, i] * b[:, j]).sum() for s, b in enumerate(shell_bvecs))
+                if i == j and abs(delta - 1.0) > tol:
+                    b1sat = False
+                if i != j and abs(delta) > tol:
+                    b1sat = False
+        if b1sat:
+            bweight = w
+            break
+    if bweight is None:
+        raise RuntimeError("Unable to satisfy B1 with the searched shells")
+
+    nntot = sum(multi[s] for s in shell_list)
+    wb = np.concatenate([[bweight[i]] * multi[s] for i, s in enumerate(shell_list)])
+
+    # neighbour lists (src/kmesh.F90:362-390): cells in sorted order, k2 ascending,
+    # stop at the shell multiplicity (vectorised over k2 within one cell)
+    nnlist = np.zeros((K, nntot), dtype=np.int64)
+    nncell = np.zeros((K, nntot, 3), dtype=np.int64)
+    bk = np.zeros((K, nntot, 3))
+    for nkp in range(K):
+        nnx = 0
+        for s in shell_list:
+            cnt = 0
+            lo, hi = dnn[s] * (1 - tol), dnn[s] * (1 + tol)
+            for ci, cell in enumerate(lmn):
+                vkpp = cell_cart[ci] + kpt_cart                  # (K,3)
+                dist = np.sqrt(((kpt_cart[nkp] - vkpp) ** 2).sum(axis=1))
+                hits = np.nonzero((dist >= lo) & (dist <= hi))[0]
+                for nkp2 in hits:
+                    nnlist[nkp, nnx] = nkp2
+                    nncell[nkp, nnx] = cell
+                    bk[nkp, nnx] = vkpp[nkp2] - kpt_cart[nkp]
+                    nnx += 1
+                    cnt += 1
+                    if cnt == multi[s]:
+                        break
+                if cnt == multi[s]:
+                    break
+    wbtot = float(wb.sum())
+    return dict(nntot=nntot, nnlist=nnlist, nncell=nncell, wb=wb, bk=bk, wbtot=wbtot,
+                shells=[s + 1 for s in shell_list], dnn=np.array(dnn), multi=np.array(multi))
+
+
+# ---------------------------------------------------------------------------
+# overlap_project (Loewdin)  (src/overlap.F90:758-952)
+# ---------------------------------------------------------------------------
+def overlap_project(M, A, nnlist):
+    """U(k) = Z V^dagger from zgesvd of A(k); M(k,b) <- U(k)^dag M(k,b) U(k+b)."""
+    K, B, W, _ = M.shape
+    U = np.empty((K, W, W), dtype=np.complex128)
+    for k in range(K):
+        z, s, vh, info = lapack.zgesvd(A[k], full_matrices=1, compute_uv=1)[:4]
+        if info != 0:
+            raise RuntimeError("zgesvd failed in overlap_project")
+        U[k] = z @ vh
+        chk = U[k].conj().T @ U[k]
+        if np.max(np.abs(chk - np.eye(W))) > EPS5:
+            raise RuntimeError("unitarity of initial U")
+    Mout = np.conj(U)[:, None].transpose(0, 1, 3, 2) @ M @ U[nnlist]
+    return U, Mout
+
+
+# ---------------------------------------------------------------------------
+# wann_omega / wann_domega  (src/wannierise.F90:1979-2284, :2287-2569)
+# ---------------------------------------------------------------------------
+@dataclass
+class Spread:
+    """localisation_vars_type (src/wannierise.F90:35-43)."""
+    om_i: float = 0.0
+    om_d: float = 0.0
+    om_od: float = 0.0
+    om_tot: float = 0.0
+
+    def copy(self):
+        return Spread(self.om_i, self.om_d, self.om_od, self.om_tot)
+
+
+def wann_omega(M, km, omega_invariant=None):
+    """Returns (Spread, rave[3,W], r2ave[W], rave2[W]).
+
+    ``omega_invariant`` None reproduces the ``first_pass`` branch (:2214-2239).
+    """
+    K, B, W, _ = M.shape
+    wb, bk = km["wb"], km["bk"]
+    diag = np.diagonal(M, axis1=2, axis2=3)           # (K,B,W)
+    ln = np.angle(diag)                               # aimag(log(.)) :2034-2043
+    rave = -np.einsum("b,kbi,kbn->in", wb, bk, ln) / K          # :2045-2061
+    rave2 = (rave * rave).sum(axis=0)
+    mnn2 = (diag * diag.conj()).real
+    r2ave = np.einsum("b,kbn->n", wb, 1.0 - mnn2 + ln ** 2) / K  # :2076-2090
+    absm2 = (M * M.conj()).real
+    if omega_invariant is None:
+        summ = absm2.sum(axis=(2, 3))                  # (K,B)
+        om_i = float(np.einsum("b,kb->", wb, W - summ) / K)
+    else:
+        om_i = omega_invariant
+    offd = absm2.sum(axis=(2, 3)) - mnn2.sum(axis=2)  # (K,B)
+    om_od = float(np.einsum("b,kb->", wb, offd) / K)  # :2241-2258
+    brn = np.einsum("kbi,in->kbn", bk, rave)
+    om_d = float(np.einsum("b,kbn->", wb, (ln + brn) ** 2) / K)  # :2260-2275
+    sp = Spread(om_i, om_d, om_od, om_i + om_d + om_od)
+    return sp, rave, r2ave, rave2
+
+
+def wann_domega(M, km):
+    """Gradient cdodq(m,n,k) (src/wannierise.F90:2287-2569, non-SLWF branch)."""
+    K, B, W, _ = M.shape
+    wb, bk = km["wb"], km["bk"]
+    diag = np.diagonal(M, axis1=2, axis2=3)
+    lnw = wb[None, :, None] * np.angle(diag)           # :2366-2375
+    rave = -np.einsum("kbi,kbn->in", bk, lnw) / K      # :2378-2391
+    rnkb = np.einsum("kbi,in->kbn", bk, rave)          # :2409-2417
+    crt = M / diag[:, :, None, :]
+    cr = M * np.conj(diag)[:, :, None, :]
+    G = np.zeros((K, W, W), dtype=np.complex128)
+    H = lambda X: np.conj(np.swapaxes(X, -1, -2))
+    w = wb[None, :, None, None]
+    G += (w * 0.5 * (cr - H(cr))).sum(axis=1)          # :2511-2515
+    T = crt * lnw[:, :, None, :]
+    G -= ((T + H(T)) * (-0.5j)).sum(axis=1)            # :2516-2520
+    R = crt * rnkb[:, :, None, :]
+    G -= (w * (R + H(R)) * (-0.5j)).sum(axis=1)        # :2521-2524
+    return G * (4.0 / K)                               # :2531
+
+
+# ---------------------------------------------------------------------------
+# wann_main  (src/wannierise.F90:48-1752)
+# ---------------------------------------------------------------------------
+@dataclass
+class WannControl:
+    """wann_control_type defaults (src/wannier90_types.F90:170-192)."""
+    num_iter: int = 100
+    num_cg_steps: int = 5
+    conv_tol: float = 1.0e-10
+    conv_window: int = -1
+    trial_step: float = 2.0
+    fixed_step: float = -999.0
+    lfixstep: bool = False
+    conv_noise_amp: float = -1.0
+    conv_noise_num: int = 3
+
+
+@dataclass
+class IterRecord:
+    iter: int
+    delta: float
+    rms_grad: float
+    spread: Spread
+    centres: np.ndarray
+    spreads: np.ndarray
+    lquad: bool
+    alphamin: float
+
+
+@dataclass
+class WannResult:
+    U: np.ndarray
+    M: np.ndarray
+    spread: Spread
+    centres: np.ndarray
+    spreads: np.ndarray
+    iters: list = field(default_factory=list)
+    initial: IterRecord | None = None
+    converged: bool = False
+    niter: int = 0
+
+
+def new_u_and_m(cdq, U, M, nnlist):
+    """internal_new_u_and_m (src/wannierise.F90:1599-1751): zheev of i*cdq, dU=V e^{-i l} V^dag."""
+    K, W, _ = cdq.shape
+    dU = np.empty_like(cdq)
+    for k in range(K):
+        w, v, info = lapack.zheev(1j * cdq[k], compute_v=1, lower=0)
+        if info != 0:
+            raise RuntimeError("zheev failed in internal_new_u_and_m")
+        dU[k] = (v * np.exp(-1j * w)[None, :]) @ v.conj().T
+    Unew = U @ dU                                                     # :1728-1733
+    Mnew = np.conj(np.swapaxes(dU, 1, 2))[:, None] @ M @ dU[nnlist]  # :1736-1748
+    return Unew, Mnew
+
+
+def wann_main(M, U, km, ctl: WannControl, record=True):
+    """Restatement of wann_main for precond=F, guiding_centres=F, SLWF=F, no sitesym."""
+    M = M.copy()
+    U = U.copy()
+    K, B, W, _ = M.shape
+    nnlist = km["nnlist"]
+    wbtot = km["wbtot"]
+
+    wann_spread, rave, r2ave, rave2 = wann_omega(M, km)          # :452-457
+    om_invariant = wann_spread.om_i
+    res = WannResult(U, M, wann_spread, rave, r2ave - rave2)
+    res.initial = IterRecord(0, wann_spread.om_tot, 0.0, wann_spread.copy(), rave.copy(),
+                             r2ave - rave2, False, 0.0)
+    old_spread = Spread()
+    ncg = 0
+    gcnorm0 = gcnorm1 = 0.0
+    cdqkeep = np.zeros((K, W, W), dtype=np.complex128)
+    history = np.zeros(max(ctl.conv_window, 1))
+    conv_count = 0
+    noise_count = 0
+    lconverged = False
+    lrandom = False
+    lfirst = True
+    save_spread = 0.0
+    lquad = False
+    alphamin = 0.0
+    it = 0
+    for it in range(1, ctl.num_iter + 1):
+        cdodq = wann_domega(M, km)                                    # :566-571
+        # internal_search_direction (:1371-1525)
+        gcnorm1 = float(np.vdot(cdodq, cdodq).real)
+        if it == 1 or ncg >= ctl.num_cg_steps:
+            gcfac = 0.0
+            ncg = 0
+        else:
+            if gcnorm0 > EPS_DP:
+                gcfac = gcnorm1 / gcnorm0
+                if gcfac > 3.0:
+                    gcfac = 0.0
+                    ncg = 0
+                else:
+                    ncg += 1
+            else:
+                gcfac = 0.0
+                ncg = 0
+        gcnorm0 = gcnorm1
+        cdq = cdodq + cdqkeep * gcfac
+        if lrandom:
+            raise NotImplementedError("conv_noise_amp > 0 is not restated in the oracle")
+        doda0 = -float(np.vdot(cdodq, cdq).real) / (4.0 * wbtot)
+        if doda0 > 0.0:
+            if ncg > 0:
+                cdq = cdodq.copy()
+                ncg = 0
+                gcfac = 0.0
+                doda0 = -float(np.vdot(cdodq, cdq).real) / (4.0 * wbtot)
+                if doda0 > 0.0:
+                    cdq = -cdq
+                    doda0 = -doda0
+            else:
+                cdq = -cdq
+                doda0 = -doda0
+        lrandom = False
+        cdqkeep = cdq.copy()                                          # :595
+
+        if ctl.lfixstep:
+            alphamin = ctl.fixed_step
+            lquad = False
+        else:
+            cdq_t = cdqkeep * (ctl.trial_step / (4.0 * wbtot))        # :605
+            U0, M0 = U, M
+            U, M = new_u_and_m(cdq_t, U0, M0, nnlist)
+            trial_spread, rave, r2ave, rave2 = wann_omega(M, km, om_invariant)
+            # internal_optimal_step (:1528-1596)
+            fac = trial_spread.om_tot - wann_spread.om_tot
+            if abs(fac) > TINY_DP:
+                fac = 1.0 / fac
+                shift = 1.0
+            else:
+                fac = 1.0e6
+                shift = fac * trial_spread.om_tot - fac * wann_spread.om_tot
+            eqb = fac * doda0
+            eqa = shift - eqb * ctl.trial_step
+            if abs(eqa / (fac * wann_spread.om_tot)) > EPS_DP:
+                lquad = True
+                alphamin = -0.5 * eqb / eqa * (ctl.trial_step ** 2)
+            else:
+                lquad = False
+                alphamin = ctl.trial_step
+            if doda0 * alphamin > 0.0:
+                lquad = False
+                alphamin = ctl.trial_step
+
+        if ctl.lfixstep or lquad:
+            cdq_a = cdqkeep * (alphamin / (4.0 * wbtot))              # :665
+            if not ctl.lfixstep:
+                U, M = U0, M0
+            U, M = new_u_and_m(cdq_a, U, M, nnlist)
+            old_spread = wann_spread.copy()
+            wann_spread, rave, r2ave, rave2 = wann_omega(M, km, om_invariant)
+        else:
+            old_spread = wann_spread.copy()
+            wann_spread = trial_spread.copy()
+
+        if record:
+            res.iters.append(IterRecord(it, wann_spread.om_tot - old_spread.om_tot,
+                                        math.sqrt(abs(gcnorm1)), wann_spread.copy(),
+                                        rave.copy(), r2ave - rave2, lquad, alphamin))
+
+        if ctl.conv_window > 1:                                       # :799-805
+            # internal_test_convergence (:1076-1164)
+            delta = wann_spread.om_tot - old_spread.om_tot
+            if it <= ctl.conv_window:
+                history[it - 1] = delta
+            else:
+                history = np.concatenate([history[1:], [delta]])
+            conv_count += 1
+            if conv_count >= ctl.conv_window and np.all(np.abs(history) <= ctl.conv_tol):
+                if ctl.conv_noise_amp > 0.0 and noise_count < ctl.conv_noise_num:
+                    if lfirst:
+                        lfirst = False
+                        save_spread = wann_spread.om_tot
+                        lrandom = True
+                        conv_count = 0
+                    else:
+                        if abs(save_spread - wann_spread.om_tot) < ctl.conv_tol:
+                            lconverged = True
+                        else:
+                            save_spread = wann_spread.om_tot
+                            lrandom = True
+                            conv_count = 0
+                    if lrandom:
+                        noise_count += 1
+                else:
+                    lconverged = True
+        if lconverged:
+            break
+
+    res.U, res.M = U, M
+    res.spread = wann_spread
+    res.centres = rave
+    res.spreads = r2ave - rave2
+    res.converged = lconverged
+    res.niter = it
+    check_unitarity(U)
+    return res
+
+
+def check_unitarity(U, tol=EPS5):
+    """wann_check_unitarity (src/wannierise.F90:2594-2661)."""
+    K, W, _ = U.shape
+    eye = np.eye(W)
+    a = U @ np.conj(np.swapaxes(U, 1, 2))
+    b = np.conj(np.swapaxes(U, 1, 2)) @ U
+    if np.max(np.abs(a - eye)) > tol or np.max(np.abs(b - eye)) > tol:
+        raise RuntimeError("wann_check_unitarity: U not unitary")
+    return True

@@ -1,0 +1,176 @@
+"""Build the golden fixtures under tests/golden/ from Wannier90's regression inputs.
+
+Run once in a checkout that has the Wannier90 source tree:
+
+    python tests/golden/make_fixtures.py /path/to/wannier90
+
+For each isolated-band ``wann_main`` regression case of the reference test suite
+(test-suite/tests/testw90_example02 Pb, testw90_example01 GaAs,
+testw90_example05 diamond, testw90_basic1) it stores, in one ``.npz``:
+
+* the inputs exactly as the reference reads them: lattice (Angstrom), k-points,
+  the raw ``.mmn`` blocks with their ``(k, k2, G)`` headers, the raw ``.amn``;
+* the wannierise keywords of the ``.win`` file;
+* the golden outputs parsed from the reference's ``benchmark.out`` file: every
+  ``<-- CONV`` line (iteration, delta, RMS gradient, spread), the initial and
+  final centres/spreads, the final Omega_I/Omega_D/Omega_OD/Omega_total and the
+  b-vector/weight table.
+
+The parser here is deliberately independent of the package's own file readers.
+"""
+from __future__ import annotations
+
+import os
+import re
+import sys
+
+import numpy as np
+
+BOHR_ANGSTROM = 0.52917720859  # src/constants.F90:109 (CODATA 2006 default)
+
+CASES = {
+    "pb": ("test-suite/tests/testw90_example02", "lead"),
+    "gaas": ("test-suite/tests/testw90_example01", "gaas"),
+    "diamond": ("test-suite/tests/testw90_example05", "diamond"),
+    "basic1": ("test-suite/tests/testw90_basic1", "wannier"),
+}
+
+
+def _strip(line):
+    for c in "!#":
+        if c in line:
+            line = line[: line.index(c)]
+    return line.strip()
+
+
+def parse_win(path):
+    lines = [_strip(l) for l in open(path)]
+    lines = [l for l in lines if l]
+    kw, blocks = {}, {}
+    i = 0
+    while i < len(lines):
+        low = lines[i].lower()
+        if low.startswith("begin"):
+            name = low.split()[1]
+            body = []
+            i += 1
+            while not lines[i].lower().startswith("end"):
+                body.append(lines[i])
+                i += 1
+            blocks[name] = body
+        else:
+            m = re.match(r"([A-Za-z_0-9]+)\s*[=:\s]\s*(.*)", lines[i])
+            if m:
+                kw[m.group(1).lower()] = m.group(2).strip()
+        i += 1
+    cell = blocks["unit_cell_cart"]
+    scale = 1.0
+    if cell[0].lower().startswith(("bohr", "ang")):
+        scale = BOHR_ANGSTROM if cell[0].lower().startswith("bohr") else 1.0
+        cell = cell[1:]
+    real_lattice = np.array([[float(x) for x in r.split()[:3]] for r in cell]) * scale
+    kpts = np.array([[float(x) for x in r.split()[:3]] for r in blocks["kpoints"]])
+    return kw, real_lattice, kpts
+
+
+def parse_mmn(path):
+    with open(path) as f:
+        f.readline()
+        nb, nk, nntot = (int(x) for x in f.readline().split())
+        heads = np.zeros((nk * nntot, 5), dtype=np.int64)
+        blocks = np.zeros((nk * nntot, nb, nb), dtype=np.complex128)  # [ncount][m][n]
+        for c in range(nk * nntot):
+            heads[c] = [int(x) for x in f.readline().split()]
+            for n in range(nb):
+                for m in range(nb):
+                    re_, im_ = (float(x) for x in f.readline().split())
+                    blocks[c, m, n] = re_ + 1j * im_
+    return nb, nk, nntot, heads, blocks
+
+
+def parse_amn(path):
+    with open(path) as f:
+        f.readline()
+        nb, nk, npj = (int(x) for x in f.readline().split())
+        A = np.zeros((nk, nb, npj), dtype=np.complex128)
+        for _ in range(nb * npj * nk):
+            p = f.readline().split()
+            m, n, k = int(p[0]), int(p[1]), int(p[2])
+            A[k - 1, m - 1, n - 1] = float(p[3]) + 1j * float(p[4])
+    return A
+
+
+def parse_benchmark(path):
+    txt = open(path).read().splitlines()
+    conv = []
+    for l in txt:
+        if l.rstrip().endswith("<-- CONV") and not l.strip().startswith(("+", "|")):
+            p = l.split()
+            conv.append([int(p[0]), float(p[1]), float(p[2]), float(p[3])])
+    conv = np.array(conv)
+
+    def centres_after(tag):
+        idx = next(i for i, l in enumerate(txt) if l.strip() == tag)
+        out = []
+        for l in txt[idx + 1:]:
+            if "WF centre and spread" in l:
+                m = re.search(r"\(\s*([-\d.]+),\s*([-\d.]+),\s*([-\d.]+)\s*\)\s+([-\d.]+)", l)
+                out.append([float(m.group(i)) for i in range(1, 5)])
+            elif out:
+                break
+        return np.array(out)
+
+    final = centres_after("Final State")
+    initial = centres_after("Initial State")
+    om = {}
+    for l in txt:
+        for key, tag in (("om_i", "Omega I"), ("om_d", "Omega D"), ("om_od", "Omega OD"),
+                         ("om_tot", "Omega Total")):
+            if tag + " " in l and "=" in l:
+                om[key] = float(l.split("=")[-1])
+    bvec = []
+    in_tab = False
+    for l in txt:
+        if "b_k Vectors" in l:
+            in_tab = True
+            continue
+        if in_tab:
+            p = l.replace("|", " ").split()
+            if len(p) == 5 and p[0].isdigit():
+                bvec.append([float(x) for x in p[1:]])
+            elif bvec and l.strip().startswith("+"):
+                break
+    return conv, initial, final, om, np.array(bvec)
+
+
+def build(ref_root, out_dir):
+    for name, (sub, seed) in CASES.items():
+        d = os.path.join(ref_root, sub)
+        kw, real_lattice, kpts = parse_win(os.path.join(d, seed + ".win"))
+        nb, nk, nntot, heads, blocks = parse_mmn(os.path.join(d, seed + ".mmn"))
+        A = parse_amn(os.path.join(d, seed + ".amn"))
+        bench = os.path.join(d, "benchmark.out.default.inp=%s.win" % seed)
+        conv, initial, final, om, bvec = parse_benchmark(bench)
+        knobs = dict(num_wann=int(kw["num_wann"]), num_iter=int(kw.get("num_iter", 100)),
+                     num_cg_steps=int(kw.get("num_cg_steps", 5)),
+                     conv_tol=float(kw.get("conv_tol", "1e-10").replace("d", "e")),
+                     conv_window=int(kw.get("conv_window", -1)),
+                     trial_step=float(kw.get("trial_step", 2.0)),
+                     search_shells=int(kw.get("search_shells", 36)))
+        np.savez_compressed(
+            os.path.join(out_dir, name + ".npz"),
+            real_lattice=real_lattice, kpt_latt=kpts,
+            mp_grid=np.array([int(x) for x in kw["mp_grid"].split()[:3]]),
+            num_bands=nb, num_kpts=nk, nntot=nntot,
+            mmn_heads=heads, mmn_blocks=blocks, amn=A,
+            knobs=np.array([knobs[k] for k in sorted(knobs)], dtype=np.float64),
+            knob_names=np.array(sorted(knobs)),
+            conv=conv, centres_initial=initial, centres_final=final,
+            omega_final=np.array([om["om_i"], om["om_d"], om["om_od"], om["om_tot"]]),
+            bvec_table=bvec)
+        print(name, nb, nk, nntot, conv.shape, final.shape, om)
+
+
+if __name__ == "__main__":
+    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    build(root, os.path.dirname(os.path.abspath(__file__)))

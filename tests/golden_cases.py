@@ -1,0 +1,40 @@
+"""Helpers that turn the golden fixtures (tests/golden/*.npz) into engine/oracle inputs."""
+import os
+
+import numpy as np
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+CASES = ["pb", "gaas", "diamond", "basic1"]
+
+
+def load(name):
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    d = {k: z[k] for k in z.files}
+    d["knobs"] = dict(zip([str(x) for x in z["knob_names"]], z["knobs"]))
+    return d
+
+
+def assemble_m(d, nnlist, nncell):
+    """Place the .mmn blocks at (k, nn) by matching (k2, G) against the k-mesh tables,
+    as overlap_read does (src/overlap.F90:270-300).  Returns M[k,b,m,n]."""
+    K = int(d["num_kpts"])
+    B = nnlist.shape[1]
+    W = int(d["num_bands"])
+    M = np.zeros((K, B, W, W), dtype=np.complex128)
+    filled = np.zeros((K, B), dtype=bool)
+    for h, blk in zip(d["mmn_heads"], d["mmn_blocks"]):
+        k, k2 = int(h[0]) - 1, int(h[1]) - 1
+        hit = [b for b in range(B) if nnlist[k, b] == k2 and tuple(nncell[k, b]) == tuple(h[2:])]
+        assert len(hit) == 1, (h, hit)
+        M[k, hit[0]] = blk
+        filled[k, hit[0]] = True
+    assert filled.all()
+    return M
+
+
+def control(d):
+    from oracle import w90_oracle as O
+    kn = d["knobs"]
+    return O.WannControl(num_iter=int(kn["num_iter"]), num_cg_steps=int(kn["num_cg_steps"]),
+                         conv_tol=float(kn["conv_tol"]), conv_window=int(kn["conv_window"]),
+                         trial_step=float(kn["trial_step"]))

@@ -1,0 +1,41 @@
+"""The oracle against the reference's own regression outputs (parity pin of the oracle).
+
+Inputs and expected values are the reference test suite's (test-suite/tests/testw90_example02,
+_example01, _example05, _basic1), packed by tests/golden/make_fixtures.py.  Every printed
+<-- CONV spread (10 decimals) must match to 2e-10 A^2 (RMS gradient to 1e-3 relative above a 1e-6 roundoff floor), final centres to 1e-6 A (printed to
+6 decimals), spreads to 1e-7 A^2 and the b-vector / weight table to 1e-6.
+"""
+import numpy as np
+import pytest
+
+from oracle import w90_oracle as O
+from tests import golden_cases as G
+
+
+@pytest.mark.parametrize("name", G.CASES)
+def test_oracle_reproduces_reference_trajectory(name):
+    d = G.load(name)
+    kn = d["knobs"]
+    km = O.kmesh_get(d["real_lattice"], d["kpt_latt"], int(kn["search_shells"]))
+    # b-vectors and weights in the reference's order (benchmark table)
+    tab = d["bvec_table"]
+    assert km["nntot"] == len(tab)
+    np.testing.assert_allclose(km["bk"][0], tab[:, :3], atol=1e-6)
+    np.testing.assert_allclose(km["wb"], tab[:, 3], atol=1e-6)
+    M = G.assemble_m(d, km["nnlist"], km["nncell"])
+    U0, M0 = O.overlap_project(M, d["amn"], km["nnlist"])
+    r = O.wann_main(M0, U0, km, G.control(d))
+    rec = {0: r.initial}
+    rec.update({it.iter: it for it in r.iters})
+    for it, delta, rms, spread in d["conv"]:
+        got = rec[int(it)]
+        assert abs(got.spread.om_tot - spread) < 2e-10, (it, got.spread.om_tot, spread)
+        # the gradient norm near the minimum is a small difference of O(1) terms whose
+        # roundoff floor (different BLAS, summation order) is ~1e-6
+        assert abs(got.rms_grad - rms) < 1e-6 + 1e-3 * rms
+    fin = d["centres_final"]
+    np.testing.assert_allclose(r.centres.T, fin[:, :3], atol=1.01e-6)
+    np.testing.assert_allclose(r.spreads, fin[:, 3], atol=1.01e-8)
+    om = d["omega_final"]
+    got = [r.spread.om_i, r.spread.om_d, r.spread.om_od, r.spread.om_tot]
+    np.testing.assert_allclose(got, om, atol=1.01e-9)

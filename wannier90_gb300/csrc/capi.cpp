@@ -1,0 +1,530 @@
+// C ABI of the GB300 MLWF engine (declared in include/wannier90_gb300.h).
+//
+// Mirrors Wannier90's library flow (src/library_interface.F90, src/c_interface.F90):
+//   w90_create -> cset_option_* -> cinput_setopt (parse options, build the k-mesh)
+//   -> cget_nn / cget_nnkp -> cset_m_local / cset_u_matrix / cset_u_opt
+//   -> cproject_overlap -> cwannierise -> cget_centres / cget_spreads -> w90_delete
+// All compute of cproject_overlap / cwannierise runs in the CUDA engine (engine.cu);
+// there is no host compute path.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/wannier90_gb300.h"
+#include "engine.h"
+#include "kmesh.h"
+
+namespace {
+
+using w90g::Control;
+using w90g::Engine;
+using w90g::KmeshInfo;
+using w90g::ProblemSpec;
+
+struct Opt {
+  std::vector<double> v;
+  int rows = 1, cols = 1;
+  bool is_int = false;
+};
+
+struct Handle {
+  std::map<std::string, Opt> opts;
+  bool setup_complete = false;
+  // system
+  int num_wann = 0, num_bands = 0, num_kpts = 0;
+  int mp_grid[3] = {0, 0, 0};
+  double real_lattice[9] = {0};
+  std::vector<double> kpt_latt;
+  // knobs
+  Control ctl{};
+  int iprint = 1, num_print_cycles = 1, timing_level = 1;
+  int search_shells = 36;
+  double kmesh_tol = 1.0e-6;
+  KmeshInfo km;
+  // caller data
+  double* m_local = nullptr;
+  double* u_matrix = nullptr;
+  double* u_opt = nullptr;
+  double* eigval = nullptr;
+  // results
+  bool have_result = false;
+  double omega[4] = {0, 0, 0, 0};
+  std::vector<double> centres, spreads, log, log_centres;
+  int niter = 0;
+  // engine
+  std::unique_ptr<Engine> eng;
+  cudaStream_t stream = nullptr;
+  std::string last_error;
+};
+
+std::string lower(std::string s) {
+  for (auto& c : s) c = (char)std::tolower((unsigned char)c);
+  return s;
+}
+
+Handle* H(void* h) { return static_cast<Handle*>(h); }
+
+void set_opt(void* h, const char* key, const double* v, int rows, int cols, bool is_int) {
+  if (!h || !key) return;
+  Opt o;
+  o.v.assign(v, v + (size_t)rows * cols);
+  o.rows = rows;
+  o.cols = cols;
+  o.is_int = is_int;
+  H(h)->opts[lower(key)] = o;
+}
+
+bool get_num(const Handle* h, const char* k, double& out) {
+  auto it = h->opts.find(k);
+  if (it == h->opts.end() || it->second.v.empty()) return false;
+  out = it->second.v[0];
+  return true;
+}
+
+// Fortran Ew.d edit descriptor (mantissa in [0.1, 1))
+std::string fort_e(double v, int w, int d) {
+  char buf[64];
+  if (v == 0.0 || !std::isfinite(v)) {
+    if (!std::isfinite(v)) {
+      std::snprintf(buf, sizeof buf, "%*s", w, "NaN");
+      return buf;
+    }
+    std::string m = "0." + std::string(d, '0') + "E+00";
+    std::snprintf(buf, sizeof buf, "%*s", w, m.c_str());
+    return buf;
+  }
+  const double a = std::fabs(v);
+  int e = (int)std::floor(std::log10(a)) + 1;
+  double mant = a / std::pow(10.0, e);
+  double scale = std::pow(10.0, d);
+  double r = std::round(mant * scale) / scale;
+  if (r >= 1.0) {
+    e += 1;
+    r = std::round(a / std::pow(10.0, e) * scale) / scale;
+  } else if (r < 0.1) {
+    e -= 1;
+    r = std::round(a / std::pow(10.0, e) * scale) / scale;
+  }
+  char mbuf[48];
+  std::snprintf(mbuf, sizeof mbuf, "%.*f", d, r);
+  char out[64];
+  std::snprintf(out, sizeof out, "%s%sE%c%02d", v < 0 ? "-" : "", mbuf, e < 0 ? '-' : '+', std::abs(e));
+  std::snprintf(buf, sizeof buf, "%*s", w, out);
+  return buf;
+}
+
+void print_centres(const Handle* h, const double* cen4) {
+  const int W = h->num_wann;
+  double sx = 0, sy = 0, sz = 0, ss = 0;
+  for (int n = 0; n < W; ++n) {
+    std::printf("  WF centre and spread%5d  (%10.6f,%10.6f,%10.6f )%15.8f\n", n + 1, cen4[n], cen4[W + n],
+                cen4[2 * W + n], cen4[3 * W + n]);
+    sx += cen4[n];
+    sy += cen4[W + n];
+    sz += cen4[2 * W + n];
+    ss += cen4[3 * W + n];
+  }
+  std::printf("  Sum of centres and spreads (%10.6f,%10.6f,%10.6f )%15.8f\n\n", sx, sy, sz, ss);
+}
+
+// .wout blocks of wann_main (src/wannierise.F90:451-545, :704-756, :838-880)
+void print_wout(const Handle* h, const w90g::ProblemResult& r) {
+  const int W = h->num_wann;
+  const int rows = (int)(r.log.size() / w90g::kLogStride);
+  std::printf("\n *------------------------------- WANNIERISE ---------------------------------*\n");
+  std::printf(" +--------------------------------------------------------------------+<-- CONV\n");
+  std::printf(" | Iter  Delta Spread     RMS Gradient      Spread (Ang^2)      Time  |<-- CONV\n");
+  std::printf(" +--------------------------------------------------------------------+<-- CONV\n\n");
+  const double t0 = r.log.empty() ? 0.0 : r.log[8];
+  for (int i = 0; i < rows; ++i) {
+    const double* lg = &r.log[(size_t)i * w90g::kLogStride];
+    const int it = (int)lg[0];
+    const bool lprint = (it == 0) || (it % h->num_print_cycles == 0) || it == 1 || it == h->ctl.num_iter ||
+                        i == rows - 1;
+    if (!lprint) continue;
+    if (it == 0) {
+      std::printf(" %s\n", std::string(78, '-').c_str());
+      std::printf(" Initial State\n");
+    } else {
+      std::printf(" Cycle: %6d\n", it);
+    }
+    print_centres(h, &r.log_centres[(size_t)i * 4 * W]);
+    const double tsec = (lg[8] - t0) * 1e-9;
+    std::printf(" %6d  %s  %15.10f  %18.10f   %8.2f  <-- CONV\n", it, fort_e(lg[1], 12, 3).c_str(), lg[2], lg[3],
+                tsec);
+    std::printf("        O_D=%15.7f O_OD=%15.7f O_TOT=%15.7f <-- SPRD\n", lg[4], lg[5], lg[3]);
+    if (it > 0) {
+      const double* pv = &r.log[(size_t)(i - 1) * w90g::kLogStride];
+      std::printf(" Delta: O_D=%s O_OD=%s O_TOT=%s <-- DLTA\n", fort_e(lg[4] - pv[4], 15, 7).c_str(),
+                  fort_e(lg[5] - pv[5], 15, 7).c_str(), fort_e(lg[3] - pv[3], 15, 7).c_str());
+    }
+    std::printf(" %s\n", std::string(78, '-').c_str());
+  }
+  if (r.converged) {
+    std::printf("\n             <<<     Delta <%s  over %2d iterations     >>>\n",
+                fort_e(h->ctl.conv_tol, 10, 3).c_str(), h->ctl.conv_window);
+    std::printf("             <<< Wannierisation convergence criteria satisfied >>>\n\n");
+  }
+  std::printf(" Final State\n");
+  std::vector<double> cen4(4 * W);
+  for (int n = 0; n < W; ++n) {
+    for (int i = 0; i < 3; ++i) cen4[i * W + n] = r.centres[n * 3 + i];
+    cen4[3 * W + n] = r.spreads[n];
+  }
+  print_centres(h, cen4.data());
+  std::printf("        Spreads (Ang^2)       Omega I      = %15.9f\n", r.spread.om_i);
+  std::printf("        ================       Omega D      = %15.9f\n", r.spread.om_d);
+  std::printf("                               Omega OD     = %15.9f\n", r.spread.om_od);
+  std::printf("    Final Spread (Ang^2)       Omega Total  = %15.9f\n", r.spread.om_tot);
+  std::printf(" %s\n", std::string(78, '-').c_str());
+  std::fflush(stdout);
+}
+
+int fail(Handle* h, int code, const std::string& msg) {
+  h->last_error = msg;
+  if (h->iprint > 0 || code > 0) std::fprintf(stderr, "Exiting....... \n%s\n", msg.c_str());
+  return code;
+}
+
+int build_spec(Handle* h, ProblemSpec& s) {
+  s.W = h->num_wann;
+  s.K = h->num_kpts;
+  s.B = h->km.nntot;
+  s.wbtot = h->km.wbtot;
+  s.nnlist = h->km.nnlist;
+  s.bk = h->km.bk;
+  s.wb = h->km.wb;
+  s.ctl = h->ctl;
+  return 0;
+}
+
+Engine* engine(Handle* h) {
+  if (!h->eng) h->eng.reset(new Engine());
+  h->eng->set_stream(h->stream);
+  return h->eng.get();
+}
+
+int do_project(Handle* h, double* m, double* u, cudaMemcpyKind in, cudaMemcpyKind out) {
+  if (!h->setup_complete) return fail(h, 1, "cinput_setopt must be called before cproject_overlap");
+  if (!m) return fail(h, 1, "m_matrix_local not set for projovlp call");
+  if (!u) return fail(h, 1, "u_matrix not set for projovlp call");
+  if (h->num_bands != h->num_wann) return fail(h, 5, "cproject_overlap: disentanglement (num_bands > num_wann) is not supported by the GPU engine");
+  ProblemSpec s;
+  build_spec(h, s);
+  std::string err;
+  Engine* e = engine(h);
+  int rc = e->setup({s}, err);
+  if (!rc) rc = e->load(0, m, u, in, err);
+  if (!rc) rc = e->project(err);
+  if (!rc) rc = e->store(0, m, u, out, err);
+  if (rc) return fail(h, rc, err);
+  return 0;
+}
+
+int do_wannierise(Handle* h, double* m, double* u, cudaMemcpyKind in, cudaMemcpyKind out) {
+  if (!h->setup_complete) return fail(h, 1, "cinput_setopt must be called before cwannierise");
+  if (!m) return fail(h, 1, "m_matrix_local not set for wannierise");
+  if (!u) return fail(h, 1, "u_matrix not set for wannierise");
+  if (h->num_bands != h->num_wann) return fail(h, 5, "wannierise: disentanglement (num_bands > num_wann) is not supported by the GPU engine");
+  ProblemSpec s;
+  build_spec(h, s);
+  std::string err;
+  Engine* e = engine(h);
+  int rc = e->setup({s}, err);
+  if (!rc) rc = e->load(0, m, u, in, err);
+  if (!rc) rc = e->wannierise(err);
+  const int solve_rc = rc;
+  if (rc == 0 || rc == 1) {
+    std::string err2;
+    int rc2 = e->store(0, m, u, out, err2);
+    if (rc2 && !rc) {
+      rc = rc2;
+      err = err2;
+    }
+  }
+  if (rc && solve_rc != 1) return fail(h, rc, err);
+  const auto& r = e->result(0);
+  h->omega[0] = r.spread.om_i;
+  h->omega[1] = r.spread.om_d;
+  h->omega[2] = r.spread.om_od;
+  h->omega[3] = r.spread.om_tot;
+  h->centres = r.centres;
+  h->spreads = r.spreads;
+  h->log = r.log;
+  h->log_centres = r.log_centres;
+  h->niter = r.niter;
+  h->have_result = true;
+  if (h->iprint > 0) print_wout(h, r);
+  if (rc) return fail(h, rc, err);
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+void* w90_create(void) { return new Handle(); }
+
+void w90_delete(void* h) { delete H(h); }
+
+void cset_option_int(void* h, const char* key, int value) {
+  double v = value;
+  set_opt(h, key, &v, 1, 1, true);
+}
+
+void cset_option_int3(void* h, const char* key, const int* value3) {
+  double v[3] = {(double)value3[0], (double)value3[1], (double)value3[2]};
+  set_opt(h, key, v, 1, 3, true);
+}
+
+void cset_option_intx(void* h, const char* key, const int* values, int count) {
+  std::vector<double> v(values, values + count);
+  set_opt(h, key, v.data(), 1, count, true);
+}
+
+void cset_option_float(void* h, const char* key, double value) { set_opt(h, key, &value, 1, 1, false); }
+
+void cset_option_float33(void* h, const char* key, const double* value33) {
+  set_opt(h, key, value33, 3, 3, false);
+}
+
+void cset_option_floatxy(void* h, const char* key, const double* values, int x, int y) {
+  set_opt(h, key, values, x, y, false);
+}
+
+// w90_input_setopt (src/library_interface.F90:161-292) restricted to what wann_main uses;
+// keyword defaults of src/wannier90_types.F90:170-192 and src/wannier90_readwrite.F90:647-754.
+void cinput_setopt(void* hv, const char* seedname, int* ierr, int comm) {
+  (void)seedname;
+  (void)comm;
+  Handle* h = H(hv);
+  *ierr = 0;
+  if (!h) {
+    *ierr = 1;
+    return;
+  }
+  if (h->opts.empty()) {
+    *ierr = fail(h, 1, " input_setopt called with no input");
+    return;
+  }
+  double v;
+  h->num_wann = get_num(h, "num_wann", v) ? (int)v : 0;
+  if (h->num_wann <= 0) {
+    *ierr = fail(h, 5, "Error: num_wann must be greater than zero");
+    return;
+  }
+  h->num_bands = get_num(h, "num_bands", v) ? (int)v : h->num_wann;
+  auto kit = h->opts.find("kpoints");
+  if (kit == h->opts.end() || kit->second.cols != 3) {
+    *ierr = fail(h, 5, "Error: Did not find the kpoint information in the input file");
+    return;
+  }
+  h->kpt_latt = kit->second.v;
+  h->num_kpts = kit->second.rows;
+  if (get_num(h, "num_kpts", v) && (int)v != h->num_kpts) {
+    *ierr = fail(h, 5, "Error: num_kpts does not match the number of kpoints given");
+    return;
+  }
+  auto cit = h->opts.find("unit_cell_cart");
+  if (cit == h->opts.end() || cit->second.v.size() != 9) {
+    *ierr = fail(h, 5, "Error: Did not find the cell information in the input file");
+    return;
+  }
+  std::memcpy(h->real_lattice, cit->second.v.data(), 9 * sizeof(double));
+  auto mit = h->opts.find("mp_grid");
+  if (mit != h->opts.end() && mit->second.v.size() == 3)
+    for (int i = 0; i < 3; ++i) h->mp_grid[i] = (int)mit->second.v[i];
+  Control& c = h->ctl;
+  c.num_iter = get_num(h, "num_iter", v) ? (int)v : 100;
+  c.num_cg_steps = get_num(h, "num_cg_steps", v) ? (int)v : 5;
+  c.conv_tol = get_num(h, "conv_tol", v) ? v : 1.0e-10;
+  c.conv_noise_amp = get_num(h, "conv_noise_amp", v) ? v : -1.0;
+  c.conv_window = (c.conv_noise_amp > 0.0) ? 5 : -1;
+  if (get_num(h, "conv_window", v)) c.conv_window = (int)v;
+  c.conv_noise_num = get_num(h, "conv_noise_num", v) ? (int)v : 3;
+  c.fixed_step = -999.0;
+  c.lfixstep = 0;
+  if (get_num(h, "fixed_step", v)) {
+    if (v < 0.0) {
+      *ierr = fail(h, 5, "Error: fixed_step must be > 0");
+      return;
+    }
+    c.fixed_step = v;
+    if (v > 0.0) c.lfixstep = 1;
+  }
+  c.trial_step = 2.0;
+  if (get_num(h, "trial_step", v)) {
+    if (c.lfixstep) {
+      *ierr = fail(h, 5, "Error: cannot specify both fixed_step and trial_step");
+      return;
+    }
+    c.trial_step = v;
+  }
+  if (c.num_iter < 0 || c.num_cg_steps < 0 || c.conv_tol < 0.0 || c.conv_noise_num < 0) {
+    *ierr = fail(h, 5, "Error: wannierise keyword out of range");
+    return;
+  }
+  h->iprint = get_num(h, "iprint", v) ? (int)v : 1;
+  h->num_print_cycles = get_num(h, "num_print_cycles", v) ? std::max(1, (int)v) : 1;
+  h->timing_level = get_num(h, "timing_level", v) ? (int)v : 1;
+  h->search_shells = get_num(h, "search_shells", v) ? (int)v : 36;
+  h->kmesh_tol = get_num(h, "kmesh_tol", v) ? v : 1.0e-6;
+  // options on wann_main's code path that the engine does not implement
+  const char* unsupported[] = {"precond", "guiding_centres", "slwf_num", "slwf_constrain", "site_symmetry",
+                               "gamma_only"};
+  for (const char* k : unsupported) {
+    if (get_num(h, k, v)) {
+      const bool active = (std::string(k) == "slwf_num") ? ((int)v != h->num_wann) : (v != 0.0);
+      if (active) {
+        *ierr = fail(h, 5, std::string("Option '") + k + "' is not supported by the GPU engine");
+        return;
+      }
+    }
+  }
+  if (c.conv_noise_amp > 0.0) {
+    *ierr = fail(h, 5, "Option 'conv_noise_amp' > 0 is not supported by the GPU engine");
+    return;
+  }
+  std::string err;
+  int rc = w90g::kmesh_get(h->real_lattice, h->kpt_latt.data(), h->num_kpts, h->search_shells, h->kmesh_tol,
+                           h->km, err);
+  if (rc) {
+    *ierr = fail(h, rc, err);
+    return;
+  }
+  h->centres.assign(3 * h->num_wann, 0.0);
+  h->spreads.assign(h->num_wann, 0.0);
+  h->setup_complete = true;
+  h->opts.clear();   // src/library_interface.F90:284-290 clears the settings after use
+}
+
+void cset_eigval(void* h, double* eigval) { H(h)->eigval = eigval; }
+void cset_m_local(void* h, double* m) { H(h)->m_local = m; }
+void cset_u_matrix(void* h, double* u) { H(h)->u_matrix = u; }
+void cset_u_opt(void* h, double* u) { H(h)->u_opt = u; }
+
+void cwannierise(void* hv, int* ierr) {
+  Handle* h = H(hv);
+  // w90_wannierise requires u_opt as well (src/library_interface.F90:480-486)
+  if (!h->u_opt) {
+    *ierr = fail(h, 1, "u_opt not set for wannierise");
+    return;
+  }
+  *ierr = do_wannierise(h, h->m_local, h->u_matrix, cudaMemcpyHostToDevice, cudaMemcpyDeviceToHost);
+}
+
+void cproject_overlap(void* hv, int* ierr) {
+  Handle* h = H(hv);
+  *ierr = do_project(h, h->m_local, h->u_matrix, cudaMemcpyHostToDevice, cudaMemcpyDeviceToHost);
+}
+
+void w90g_wannierise_device(void* hv, double* d_m, double* d_u, int* ierr) {
+  *ierr = do_wannierise(H(hv), d_m, d_u, cudaMemcpyDeviceToDevice, cudaMemcpyDeviceToDevice);
+}
+
+void w90g_project_overlap_device(void* hv, double* d_m, double* d_u, int* ierr) {
+  *ierr = do_project(H(hv), d_m, d_u, cudaMemcpyDeviceToDevice, cudaMemcpyDeviceToDevice);
+}
+
+void cget_nn(void* hv, int* nn) {
+  Handle* h = H(hv);
+  *nn = h->setup_complete ? h->km.nntot : 0;
+}
+
+void cget_nnkp(void* hv, int* nnkp) {
+  // w90_get_nnkp: nnlist(nk, nntot), 1-based, Fortran column-major (k fastest)
+  Handle* h = H(hv);
+  if (!h->setup_complete) return;
+  const int K = h->num_kpts, B = h->km.nntot;
+  for (int b = 0; b < B; ++b)
+    for (int k = 0; k < K; ++k) nnkp[b * K + k] = h->km.nnlist[(size_t)k * B + b] + 1;
+}
+
+void cget_gkpb(void* hv, int* gkpb) {
+  // nncell(3, nk, nntot), Fortran column-major
+  Handle* h = H(hv);
+  if (!h->setup_complete) return;
+  const int K = h->num_kpts, B = h->km.nntot;
+  for (int b = 0; b < B; ++b)
+    for (int k = 0; k < K; ++k)
+      for (int i = 0; i < 3; ++i) gkpb[(b * K + k) * 3 + i] = h->km.nncell[((size_t)k * B + b) * 3 + i];
+}
+
+void cget_centres(void* hv, double* centres) {
+  Handle* h = H(hv);
+  std::copy(h->centres.begin(), h->centres.end(), centres);
+}
+
+void cget_spreads(void* hv, double* spreads) {
+  Handle* h = H(hv);
+  std::copy(h->spreads.begin(), h->spreads.end(), spreads);
+}
+
+void cget_omega(void* hv, double* omega4) {
+  Handle* h = H(hv);
+  std::copy(h->omega, h->omega + 4, omega4);
+}
+
+const char* w90g_last_error(void* hv) { return H(hv)->last_error.c_str(); }
+
+int w90g_get_log(void* hv, double* rows, int max_rows) {
+  Handle* h = H(hv);
+  const int n = std::min(max_rows, (int)(h->log.size() / w90g::kLogStride));
+  std::copy(h->log.begin(), h->log.begin() + (size_t)n * w90g::kLogStride, rows);
+  return n;
+}
+
+int w90g_get_log_centres(void* hv, double* rows, int max_rows) {
+  Handle* h = H(hv);
+  const size_t stride = 4 * (size_t)h->num_wann;
+  if (!stride) return 0;
+  const int n = std::min(max_rows, (int)(h->log_centres.size() / stride));
+  std::copy(h->log_centres.begin(), h->log_centres.begin() + (size_t)n * stride, rows);
+  return n;
+}
+
+void w90g_set_stream(void* hv, void* cuda_stream) {
+  Handle* h = H(hv);
+  h->stream = (cudaStream_t)cuda_stream;
+  if (h->eng) h->eng->set_stream(h->stream);
+}
+
+int w90g_profile_device(void* hv, double* d_m, double* d_u, int max_iters, double* ms, int* counts) {
+  Handle* h = H(hv);
+  if (!h->setup_complete) return fail(h, 1, "cinput_setopt must be called before w90g_profile_device");
+  ProblemSpec s;
+  build_spec(h, s);
+  std::string err;
+  Engine* e = engine(h);
+  int rc = e->setup({s}, err);
+  if (!rc) rc = e->load(0, d_m, d_u, cudaMemcpyDeviceToDevice, err);
+  if (!rc) rc = e->wannierise_profiled(max_iters, ms, counts, err);
+  if (rc) return fail(h, rc, err);
+  return 0;
+}
+
+const char* w90g_profile_kernel_name(int i) {
+  return (i >= 0 && i < w90g::kPNum) ? w90g::kProfNames[i] : "";
+}
+
+double w90g_measure_fp64_peak(void) {
+  double t = 0.0;
+  std::string err;
+  if (w90g::measure_fp64_peak(&t, err)) return -1.0;
+  return t;
+}
+
+long long w90g_kernel_launches(void* hv) {
+  Handle* h = H(hv);
+  return h->eng ? h->eng->launches() : 0;
+}
+
+}  // extern "C"

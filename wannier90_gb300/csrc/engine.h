@@ -1,0 +1,97 @@
+// Host orchestration of the GB300 MLWF engine: device arena, launch sequence,
+// CUDA-graph replay of the iteration, result download.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "w90g.cuh"
+
+namespace w90g {
+
+struct ProblemSpec {
+  int W = 0, K = 0, B = 0;
+  double wbtot = 0.0;
+  std::vector<int> nnlist;   // [k][b] 0-based
+  std::vector<double> bk;    // [k][b][3]
+  std::vector<double> wb;    // [b]
+  Control ctl{};
+};
+
+struct ProblemResult {
+  int niter = 0;
+  int converged = 0;
+  int error = 0;
+  Spread spread{};
+  std::vector<double> centres;   // [W][3]
+  std::vector<double> spreads;   // [W]
+  std::vector<double> log;       // (niter+1) x kLogStride
+  std::vector<double> log_centres;  // (niter+1) x 4W
+  double unitarity_err = 0.0;
+};
+
+enum ProfKernel {
+  kPGrad = 0, kPCtrlSearch, kPExpU, kPMUpdate, kPOmega, kPCtrlStep, kPCtrlEnd, kPInit, kPNum
+};
+extern const char* kProfNames[kPNum];
+
+class Engine {
+ public:
+  Engine();
+  ~Engine();
+  Engine(const Engine&) = delete;
+  Engine& operator=(const Engine&) = delete;
+
+  // (Re)allocate for a batch of problems; reuses the arena when the shapes match.
+  int setup(const std::vector<ProblemSpec>& specs, std::string& err);
+  // Copy M (m_matrix layout) and U into buffer 0 of problem p.
+  int load(int p, const void* M, const void* U, cudaMemcpyKind kind, std::string& err);
+  // Copy the accepted M and U of problem p out.
+  int store(int p, void* M, void* U, cudaMemcpyKind kind, std::string& err);
+  // Loewdin projection on every problem (U holds A on entry).
+  int project(std::string& err);
+  // wann_main on every problem; results via result().
+  int wannierise(std::string& err);
+  // wann_main with each kernel launched individually and timed with CUDA events on the
+  // launching stream; ms[i] / cnt[i] accumulate per kernel kind (kProfNames order);
+  // only launches that did work are counted (skipped second passes are excluded).
+  int wannierise_profiled(int max_iters, double* ms, int* cnt, std::string& err);
+  const ProblemResult& result(int p) const { return results_[p]; }
+  int nprob() const { return (int)specs_.size(); }
+
+  void set_stream(cudaStream_t s) { user_stream_ = s; }
+  cudaStream_t stream() const { return user_stream_ ? user_stream_ : own_stream_; }
+  long long launches() const { return launches_; }
+
+ private:
+  int alloc(std::string& err);
+  void release();
+  void launch_iteration(cudaStream_t s);
+  int init_states(std::string& err);
+
+  std::vector<ProblemSpec> specs_;
+  std::vector<Problem> hprobs_;
+  std::vector<ProblemResult> results_;
+  void* arena_ = nullptr;
+  size_t arena_bytes_ = 0;
+  Problem* dprobs_ = nullptr;
+  int* d_offs_k_ = nullptr;
+  int* d_offs_kb_ = nullptr;
+  int* d_offs_grad_ = nullptr;
+  int* d_status_ = nullptr;
+  double* d_unit_ = nullptr;
+  int n_k_ = 0, n_kb_ = 0, n_grad_ = 0;
+  int maxW_small_ = 0;   // largest W <= 32 in the batch (shared-memory kernels)
+  int max_iter_ = 0;
+  cudaStream_t own_stream_ = nullptr;
+  cudaStream_t user_stream_ = nullptr;
+  cudaGraphExec_t graph_exec_ = nullptr;
+  cudaStream_t graph_stream_ = nullptr;
+  std::string layout_key_;
+  long long launches_ = 0;
+};
+
+int measure_fp64_peak(double* tflops, std::string& err);
+
+}  // namespace w90g

@@ -1,0 +1,965 @@
+// FP64 kernels of the GB300 MLWF engine (the plain FP64 path).
+//
+// One iteration of wann_main (src/wannierise.F90:534-816) is the fixed launch sequence
+//   k_grad -> k_ctrl_search -> k_exp_u(0) -> k_m_update(0) -> k_omega(0) -> k_ctrl_step
+//   -> k_exp_u(1) -> k_m_update(1) -> k_omega(1) -> k_ctrl_end
+// All data-dependent decisions of the reference (CG reset, uphill reversal, parabolic
+// line search, convergence) are taken on the device by the k_ctrl_* kernels, so the
+// sequence never needs the host and can be replayed (or graph-captured) blindly:
+// kernels whose work is not needed (second update when the parabola was rejected,
+// anything after convergence) return at entry.
+//
+// GB300's FP64 pipe is ~1/64 of its FP32 rate, so these kernels are FP64-issue bound
+// for W >= 8; they are written to minimise FP64 instructions (reciprocals of M_nn
+// precomputed, exp(X) by an optimised Taylor scheme instead of an eigensolver) and keep
+// W <= 32 operands in shared memory.
+#include "w90g.cuh"
+
+namespace w90g {
+
+constexpr int kSmemW = 32;   // W <= kSmemW: all per-matrix operands live in shared memory
+
+// ----------------------------------------------------------------------------
+// CTA-wide helpers
+// ----------------------------------------------------------------------------
+__device__ __forceinline__ double block_sum(double v, double* red) {
+  // deterministic tree reduction over blockDim.x (power of two, <= 1024)
+  int t = threadIdx.x;
+  red[t] = v;
+  __syncthreads();
+  for (int s = blockDim.x >> 1; s > 0; s >>= 1) {
+    if (t < s) red[t] += red[t + s];
+    __syncthreads();
+  }
+  double r = red[0];
+  __syncthreads();
+  return r;
+}
+
+__device__ __forceinline__ double block_max(double v, double* red) {
+  int t = threadIdx.x;
+  red[t] = v;
+  __syncthreads();
+  for (int s = blockDim.x >> 1; s > 0; s >>= 1) {
+    if (t < s) red[t] = fmax(red[t], red[t + s]);
+    __syncthreads();
+  }
+  double r = red[0];
+  __syncthreads();
+  return r;
+}
+
+// C = op(A) * B for W x W column-major matrices (generic pointers: shared or global).
+// CA: op(A) = A^H (A read as conj(A[i*lda+l])), else op(A) = A.
+// Each thread computes a 2x2 micro-tile of C.  C must not alias A or B.
+template <bool CA>
+__device__ void cta_gemm(double2* __restrict__ C, int ldc, const double2* __restrict__ A, int lda,
+                         const double2* __restrict__ B, int ldb, int W) {
+  const int nb = (W + 1) >> 1;
+  for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) {
+    const int i0 = (t % nb) * 2, j0 = (t / nb) * 2;
+    const bool i1 = (i0 + 1) < W, j1 = (j0 + 1) < W;
+    double2 c00 = cmk(0, 0), c01 = cmk(0, 0), c10 = cmk(0, 0), c11 = cmk(0, 0);
+    const double2 z = cmk(0, 0);
+#pragma unroll 4
+    for (int l = 0; l < W; ++l) {
+      double2 a0, a1;
+      if (CA) {
+        a0 = cconj(A[i0 * lda + l]);
+        a1 = i1 ? cconj(A[(i0 + 1) * lda + l]) : z;
+      } else {
+        a0 = A[l * lda + i0];
+        a1 = i1 ? A[l * lda + i0 + 1] : z;
+      }
+      const double2 b0 = B[j0 * ldb + l];
+      const double2 b1 = j1 ? B[(j0 + 1) * ldb + l] : z;
+      cfma(c00, a0, b0);
+      cfma(c10, a1, b0);
+      cfma(c01, a0, b1);
+      cfma(c11, a1, b1);
+    }
+    C[j0 * ldc + i0] = c00;
+    if (i1) C[j0 * ldc + i0 + 1] = c10;
+    if (j1) {
+      C[(j0 + 1) * ldc + i0] = c01;
+      if (i1) C[(j0 + 1) * ldc + i0 + 1] = c11;
+    }
+  }
+}
+
+// Per-block statistics of one M(k,b): Im ln M_nn, |M_nn|^2, sum_{m!=n}|M_mn|^2.
+// (the quantities wann_omega reads, src/wannierise.F90:2034-2043, :2076-2090, :2241-2258)
+__device__ void block_stats(const double2* Mb, int ld, int W, double* ln_out, double* abs2_out,
+                            double* offd_out, double* red) {
+  double off = 0.0;
+  for (int e = threadIdx.x; e < W * W; e += blockDim.x) {
+    const int m = e % W, n = e / W;
+    const double2 v = Mb[n * ld + m];
+    if (m != n) off += cabs2(v);
+  }
+  for (int n = threadIdx.x; n < W; n += blockDim.x) {
+    const double2 d = Mb[n * ld + n];
+    ln_out[n] = atan2(d.y, d.x);
+    abs2_out[n] = d.x * d.x + d.y * d.y;
+  }
+  const double tot = block_sum(off, red);
+  if (threadIdx.x == 0) *offd_out = tot;
+}
+
+// ----------------------------------------------------------------------------
+// k_mdiag: statistics of every block of M[cur] (initial spread, after projection)
+// grid: one CTA per (problem, k*B+b), 128 threads
+// ----------------------------------------------------------------------------
+__global__ void k_mdiag(const Problem* __restrict__ probs, WorkMap wm) {
+  __shared__ double red[128];
+  int local;
+  const int p = locate(wm, blockIdx.x, local);
+  const Problem& P = probs[p];
+  const int W = P.W;
+  const double2* Mb = P.M[P.st->cur] + (size_t)local * W * W;
+  block_stats(Mb, W, W, P.diag_ln + (size_t)local * W, P.diag_abs2 + (size_t)local * W,
+              P.offd + local, red);
+}
+
+// ----------------------------------------------------------------------------
+// k_omega: wann_omega (src/wannierise.F90:1979-2284), non-SLWF branch.
+// One CTA (512 threads) per problem.  slot: 0 trial, 1 optimal step, 2 initial.
+// Deterministic: fixed (n, chunk) ownership and fixed-order tree reductions.
+// ----------------------------------------------------------------------------
+constexpr int kOmegaThreads = 512;
+
+__global__ void __launch_bounds__(kOmegaThreads) k_omega(const Problem* __restrict__ probs, int slot) {
+  __shared__ double red[kOmegaThreads];
+  __shared__ double s_rave[3 * 512];
+  const Problem& P = probs[blockIdx.x];
+  CtrlState* st = P.st;
+  if (slot < 2) {
+    if (st->done) return;
+    if (slot == 1 && !st->do_second) return;
+  }
+  const int W = P.W, K = P.K, B = P.B;
+  const int KB = K * B;
+  const int t = threadIdx.x;
+  // thread (n, chunk) ownership; W <= 512 so at least one chunk of 512 threads
+  const int nch = kOmegaThreads / W;   // chunks
+  const int n = t % W, ch = t / W;
+  const bool act = ch < nch;
+  double r0 = 0, r1 = 0, r2 = 0, q = 0;
+  if (act) {
+    for (int kb = ch; kb < KB; kb += nch) {
+      const int b = kb % B;
+      const double w = P.wb[b];
+      const double l = P.diag_ln[(size_t)kb * W + n];
+      const double a = P.diag_abs2[(size_t)kb * W + n];
+      const double* bv = P.bk + (size_t)kb * 3;
+      const double wl = w * l;
+      r0 = fma(wl, bv[0], r0);
+      r1 = fma(wl, bv[1], r1);
+      r2 = fma(wl, bv[2], r2);
+      q += w * (1.0 - a + l * l);
+    }
+  }
+  // reduce over chunks for each n: red layout [ch][n]
+  double* rv = s_rave;  // rave(3, n) stored as s_rave[i*W+n]
+  double vals[4] = {r0, r1, r2, q};
+  double r2ave_n = 0.0;
+  for (int c = 0; c < 4; ++c) {
+    red[t] = act ? vals[c] : 0.0;
+    __syncthreads();
+    if (t < W) {
+      double s = 0.0;
+      for (int cc = 0; cc < nch; ++cc) s += red[cc * W + t];
+      if (c < 3) rv[c * W + t] = -s / (double)K;
+      else r2ave_n = s / (double)K;
+    }
+    __syncthreads();
+  }
+  // scalar sums over (k,b): Omega_OD and first-pass Omega_I
+  double od = 0.0, oi = 0.0;
+  const bool first = (slot == 2) && st->first_pass;
+  for (int kb = t; kb < KB; kb += kOmegaThreads) {
+    const double w = P.wb[kb % B];
+    const double o = P.offd[kb];
+    od += w * o;
+    if (first) {
+      double sd = 0.0;
+      for (int m = 0; m < W; ++m) sd += P.diag_abs2[(size_t)kb * W + m];
+      oi += w * ((double)W - (o + sd));
+    }
+  }
+  od = block_sum(od, red) / (double)K;
+  if (first) oi = block_sum(oi, red) / (double)K;
+  // Omega_D = (1/K) sum wb (ln + b.rave_n)^2   (second pass, needs rave)
+  double dd = 0.0;
+  if (act) {
+    const double x0 = rv[n], x1 = rv[W + n], x2 = rv[2 * W + n];
+    for (int kb = ch; kb < KB; kb += nch) {
+      const double w = P.wb[kb % B];
+      const double* bv = P.bk + (size_t)kb * 3;
+      const double brn = bv[0] * x0 + bv[1] * x1 + bv[2] * x2;
+      const double l = P.diag_ln[(size_t)kb * W + n] + brn;
+      dd = fma(w * l, l, dd);
+    }
+  }
+  dd = block_sum(dd, red) / (double)K;
+  // outputs
+  double* cen = P.centres + (size_t)slot * 4 * W;
+  if (t < W) {
+    const double x0 = rv[t], x1 = rv[W + t], x2 = rv[2 * W + t];
+    cen[t] = x0;
+    cen[W + t] = x1;
+    cen[2 * W + t] = x2;
+    cen[3 * W + t] = r2ave_n - (x0 * x0 + x1 * x1 + x2 * x2);
+  }
+  if (t == 0) {
+    if (first) {
+      st->om_invariant = oi;
+      st->first_pass = 0;
+    }
+    Spread s;
+    s.om_i = st->om_invariant;
+    s.om_d = dd;
+    s.om_od = od;
+    s.om_tot = s.om_i + s.om_d + s.om_od;
+    if (slot == 2) {
+      st->wann = s;
+    } else {
+      st->slot[slot] = s;
+    }
+    if (!isfinite(s.om_tot)) {
+      st->error = 1;
+      st->done = 1;
+    }
+  }
+}
+
+// ----------------------------------------------------------------------------
+// k_grad: wann_domega (src/wannierise.F90:2287-2569), non-SLWF branch, fused with the
+// per-k partial dot products of internal_search_direction (:1424-1431).
+// grid: one CTA per (problem, k, tile_i, tile_j) of 32x32 tiles; 256 threads.
+// rave is the one computed by the preceding k_omega on the same M (the reference
+// recomputes it from the same data, :2378-2393).
+// ----------------------------------------------------------------------------
+constexpr int kTile = 32;
+
+__global__ void __launch_bounds__(256) k_grad(const Problem* __restrict__ probs, WorkMap wm) {
+  __shared__ double2 sA[kTile * (kTile + 1)];   // A[j*(33)+i] = M(r0+i, c0+j)
+  __shared__ double2 sT[kTile * (kTile + 1)];   // T[i*(33)+j] = M(c0+j, r0+i)
+  __shared__ double2 sdm[kTile], sdn[kTile];     // diag, rows / cols range
+  __shared__ double2 sim[kTile], sin_[kTile];    // 1/M_nn
+  __shared__ double sqm[kTile], sqn[kTile];      // q = wb*(ln + b.rave)
+  __shared__ double red[256];
+  int local;
+  const int p = locate(wm, blockIdx.x, local);
+  const Problem& P = probs[p];
+  const CtrlState* st = P.st;
+  if (st->done) return;
+  const int W = P.W, B = P.B, K = P.K;
+  const int nt = (W + kTile - 1) / kTile;
+  const int k = local / (nt * nt);
+  const int tt = local % (nt * nt);
+  const int r0 = (tt % nt) * kTile, c0 = (tt / nt) * kTile;
+  const int nr = min(kTile, W - r0), nc = min(kTile, W - c0);
+  const double* rave = P.centres + (size_t)2 * 4 * W;  // accepted slot
+  const double2* Mk = P.M[st->cur] + (size_t)k * B * W * W;
+  const int t = threadIdx.x;
+
+  double2 acc[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) acc[q] = cmk(0, 0);
+
+  for (int b = 0; b < B; ++b) {
+    const double2* Mb = Mk + (size_t)b * W * W;
+    const double w = P.wb[b];
+    const double* bv = P.bk + ((size_t)k * B + b) * 3;
+    __syncthreads();
+    for (int e = t; e < kTile * kTile; e += 256) {
+      const int i = e % kTile, j = e / kTile;
+      if (i < nr && j < nc) sA[j * (kTile + 1) + i] = Mb[(size_t)(c0 + j) * W + r0 + i];
+      // transposed tile: rows c0.., cols r0..; coalesced over the row index
+      const int jj = e % kTile, ii = e / kTile;
+      if (jj < nc && ii < nr) sT[ii * (kTile + 1) + jj] = Mb[(size_t)(r0 + ii) * W + c0 + jj];
+    }
+    if (t < kTile) {
+      if (t < nr) {
+        const int m = r0 + t;
+        const double2 d = Mb[(size_t)m * W + m];
+        sdm[t] = d;
+        const double inv = 1.0 / (d.x * d.x + d.y * d.y);
+        sim[t] = cmk(d.x * inv, -d.y * inv);
+        const double brn = bv[0] * rave[m] + bv[1] * rave[W + m] + bv[2] * rave[2 * W + m];
+        sqm[t] = w * (atan2(d.y, d.x) + brn);
+      }
+    } else if (t < 2 * kTile) {
+      const int u = t - kTile;
+      if (u < nc) {
+        const int n = c0 + u;
+        const double2 d = Mb[(size_t)n * W + n];
+        sdn[u] = d;
+        const double inv = 1.0 / (d.x * d.x + d.y * d.y);
+        sin_[u] = cmk(d.x * inv, -d.y * inv);
+        const double brn = bv[0] * rave[n] + bv[1] * rave[W + n] + bv[2] * rave[2 * W + n];
+        sqn[u] = w * (atan2(d.y, d.x) + brn);
+      }
+    }
+    __syncthreads();
+    const double hw = 0.5 * w;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int e = t + 256 * q;
+      const int i = e % kTile, j = e / kTile;
+      if (i < nr && j < nc) {
+        const double2 mmn = sA[j * (kTile + 1) + i];    // M_mn
+        const double2 mnm = sT[i * (kTile + 1) + j];    // M_nm
+        // cr_mn = M_mn conj(M_nn); cr_nm = M_nm conj(M_mm)
+        const double2 cr_mn = cmulc(mmn, sdn[j]);
+        const double2 cr_nm = cmulc(mnm, sdm[i]);
+        // crt_mn = M_mn / M_nn ; crt_nm = M_nm / M_mm
+        const double2 crt_mn = cmul(mmn, sin_[j]);
+        const double2 crt_nm = cmul(mnm, sim[i]);
+        // A[R]:  wb/2 (cr_mn - conj(cr_nm))
+        double gx = hw * (cr_mn.x - cr_nm.x);
+        double gy = hw * (cr_mn.y + cr_nm.y);
+        // -S[T]: (i/2) (crt_mn q_n + conj(crt_nm) q_m)
+        const double qn = sqn[j], qm = sqm[i];
+        const double sx = crt_mn.x * qn + crt_nm.x * qm;
+        const double sy = crt_mn.y * qn - crt_nm.y * qm;
+        gx -= 0.5 * sy;
+        gy += 0.5 * sx;
+        acc[q].x += gx;
+        acc[q].y += gy;
+      }
+    }
+  }
+  // scale, store, partial dot products
+  const double fac = 4.0 / (double)K;
+  double g2 = 0.0, gd = 0.0;
+  double2* Gk = P.G + (size_t)k * W * W;
+  const double2* Dk = P.D + (size_t)k * W * W;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int e = t + 256 * q;
+    const int i = e % kTile, j = e / kTile;
+    if (i < nr && j < nc) {
+      const double2 g = cscale(acc[q], fac);
+      const size_t off = (size_t)(c0 + j) * W + r0 + i;
+      Gk[off] = g;
+      const double2 d = Dk[off];
+      g2 += g.x * g.x + g.y * g.y;
+      gd += g.x * d.x + g.y * d.y;
+    }
+  }
+  g2 = block_sum(g2, red);
+  gd = block_sum(gd, red);
+  if (t == 0) {
+    P.gpart[(size_t)local * 2] = g2;
+    P.gpart[(size_t)local * 2 + 1] = gd;
+  }
+}
+
+// ----------------------------------------------------------------------------
+// k_ctrl_search: internal_search_direction (src/wannierise.F90:1371-1525) as scalars.
+// D = G + gcfac*D_prev is never formed here: the coefficients (coefG, coefD) are
+// handed to k_exp_u, and <G,D> = |G|^2 + gcfac*<G,D_prev> comes from k_grad's partials.
+// One CTA (256 threads) per problem.
+// ----------------------------------------------------------------------------
+__global__ void k_ctrl_search(const Problem* __restrict__ probs) {
+  __shared__ double red[256];
+  const Problem& P = probs[blockIdx.x];
+  CtrlState* st = P.st;
+  if (st->done) return;
+  const int nt = (P.W + kTile - 1) / kTile;
+  const int n = P.K * nt * nt;
+  double g2 = 0.0, gd = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    g2 += P.gpart[(size_t)i * 2];
+    gd += P.gpart[(size_t)i * 2 + 1];
+  }
+  g2 = block_sum(g2, red);
+  gd = block_sum(gd, red);
+  if (threadIdx.x != 0) return;
+  const Control& c = P.ctl;
+  const int iter = st->iter + 1;
+  const double gcnorm1 = g2;
+  double gcfac;
+  int ncg = st->ncg;
+  if (iter == 1 || ncg >= c.num_cg_steps) {
+    gcfac = 0.0;
+    ncg = 0;
+  } else {
+    if (st->gcnorm0 > 2.220446049250313e-16) {   // epsilon(1.0_dp)
+      gcfac = gcnorm1 / st->gcnorm0;
+      if (gcfac > 3.0) {
+        gcfac = 0.0;
+        ncg = 0;
+      } else {
+        ncg = ncg + 1;
+      }
+    } else {
+      gcfac = 0.0;
+      ncg = 0;
+    }
+  }
+  st->gcnorm0 = gcnorm1;
+  st->gcnorm1 = gcnorm1;
+  const double fw = 4.0 * P.wbtot;
+  double coefG = 1.0, coefD = gcfac;
+  double doda0 = -(g2 + gcfac * gd) / fw;
+  if (doda0 > 0.0) {
+    if (ncg > 0) {
+      coefD = 0.0;
+      ncg = 0;
+      gcfac = 0.0;
+      doda0 = -g2 / fw;
+      if (doda0 > 0.0) {
+        coefG = -coefG;
+        doda0 = -doda0;
+      }
+    } else {
+      coefG = -coefG;
+      coefD = -coefD;
+      doda0 = -doda0;
+    }
+  }
+  st->ncg = ncg;
+  st->gcfac = gcfac;
+  st->doda0 = doda0;
+  st->coefG = coefG;
+  st->coefD = coefD;
+  if (c.lfixstep) {
+    st->alphamin = c.fixed_step;
+    st->s_trial = c.fixed_step / fw;
+  } else {
+    st->s_trial = c.trial_step / fw;
+  }
+  st->do_second = 0;
+}
+
+// ----------------------------------------------------------------------------
+// exp(X) for anti-Hermitian X (W x W), scaling and squaring with a degree-16 Taylor
+// polynomial evaluated by the Paterson-Stockmeyer scheme (p = 4): Y2, Y3, Y4 and
+// three Horner steps in Y4 = 6 matrix products, then j squarings.  ||Y||_1 <= 0.8
+// bounds the truncation term 0.8^17/17! < 1.1e-16 (||e^Y||_2 = 1 for anti-Hermitian Y).
+// exp(s*D) equals the reference's V e^{-i s lambda} V^dagger with (V, lambda) the
+// eigenpairs of i*D (src/wannierise.F90:1655-1690) in exact arithmetic.
+// Buffers: X (input, scaled in place), Y2, Y3, Y4, R, T  (6 * W*W).  Result in *out.
+// ----------------------------------------------------------------------------
+__device__ const double kInvFact[17] = {
+    1.0, 1.0, 0.5, 1.6666666666666666e-01, 4.1666666666666664e-02, 8.3333333333333332e-03,
+    1.3888888888888889e-03, 1.9841269841269841e-04, 2.4801587301587302e-05,
+    2.7557319223985893e-06, 2.7557319223985888e-07, 2.5052108385441720e-08,
+    2.0876756987868100e-09, 1.6059043836821613e-10, 1.1470745597729725e-11,
+    7.6471637318198164e-13, 4.7794773323873853e-14};
+
+__device__ double2* cta_expm(double2* X, double2* Y2, double2* Y3, double2* Y4, double2* R,
+                             double2* T, int W, double* red) {
+  const int WW = W * W;
+  // ||X||_1 = max column sum
+  double colmax = 0.0;
+  for (int j = threadIdx.x; j < W; j += blockDim.x) {
+    double s = 0.0;
+    for (int i = 0; i < W; ++i) s += sqrt(cabs2(X[j * W + i]));
+    colmax = fmax(colmax, s);
+  }
+  double nrm = block_max(colmax, red);
+  int js = 0;
+  while (nrm > 0.8 && js < 60) {
+    nrm *= 0.5;
+    ++js;
+  }
+  const double sc = ldexp(1.0, -js);
+  for (int e = threadIdx.x; e < WW; e += blockDim.x) X[e] = cscale(X[e], sc);
+  __syncthreads();
+  cta_gemm<false>(Y2, W, X, W, X, W, W);
+  __syncthreads();
+  cta_gemm<false>(Y3, W, Y2, W, X, W, W);
+  cta_gemm<false>(Y4, W, Y2, W, Y2, W, W);
+  __syncthreads();
+  // R = B3 + c16*Y4, with B_q = c_{4q} I + c_{4q+1} Y + c_{4q+2} Y2 + c_{4q+3} Y3
+  for (int e = threadIdx.x; e < WW; e += blockDim.x) {
+    const int i = e % W, j = e / W;
+    double2 v = cscale(Y4[e], kInvFact[16]);
+    v = cadd(v, cscale(X[e], kInvFact[13]));
+    v = cadd(v, cscale(Y2[e], kInvFact[14]));
+    v = cadd(v, cscale(Y3[e], kInvFact[15]));
+    if (i == j) v.x += kInvFact[12];
+    R[e] = v;
+  }
+  __syncthreads();
+  for (int q = 2; q >= 0; --q) {
+    cta_gemm<false>(T, W, Y4, W, R, W, W);
+    __syncthreads();
+    const double c0 = kInvFact[4 * q], c1 = kInvFact[4 * q + 1], c2 = kInvFact[4 * q + 2],
+                 c3 = kInvFact[4 * q + 3];
+    for (int e = threadIdx.x; e < WW; e += blockDim.x) {
+      const int i = e % W, j = e / W;
+      double2 v = T[e];
+      v = cadd(v, cscale(X[e], c1));
+      v = cadd(v, cscale(Y2[e], c2));
+      v = cadd(v, cscale(Y3[e], c3));
+      if (i == j) v.x += c0;
+      R[e] = v;
+    }
+    __syncthreads();
+  }
+  double2* a = R;
+  double2* b = T;
+  for (int s = 0; s < js; ++s) {
+    cta_gemm<false>(b, W, a, W, a, W, W);
+    __syncthreads();
+    double2* tmp = a;
+    a = b;
+    b = tmp;
+  }
+  return a;
+}
+
+// ----------------------------------------------------------------------------
+// k_exp_u: one CTA per (problem, k).  which = 0: trial step (also forms D),
+// which = 1: optimal step.  dU(k) = exp(s*D(k));  U[cur^1](k) = U[cur](k) dU(k)
+// (src/wannierise.F90:1655-1733).
+// ----------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_exp_u(const Problem* __restrict__ probs, WorkMap wm, int which) {
+  extern __shared__ double2 smem[];
+  __shared__ double red[256];
+  int k;
+  const int p = locate(wm, blockIdx.x, k);
+  const Problem& P = probs[p];
+  CtrlState* st = P.st;
+  if (st->done) return;
+  if (which == 1 && !st->do_second) return;
+  const int W = P.W, WW = W * W;
+  double2* buf = (W <= kSmemW) ? smem : (P.work + (size_t)k * 6 * WW);
+  double2 *X = buf, *Y2 = buf + WW, *Y3 = buf + 2 * WW, *Y4 = buf + 3 * WW, *R = buf + 4 * WW,
+          *T = buf + 5 * WW;
+  double2* Dk = P.D + (size_t)k * WW;
+  const double s = (which == 0) ? st->s_trial : st->s_second;
+  if (which == 0) {
+    const double cg = st->coefG, cd = st->coefD;
+    const double2* Gk = P.G + (size_t)k * WW;
+    for (int e = threadIdx.x; e < WW; e += blockDim.x) {
+      const double2 d = cadd(cscale(Gk[e], cg), cscale(Dk[e], cd));
+      Dk[e] = d;
+      X[e] = cscale(d, s);
+    }
+  } else {
+    for (int e = threadIdx.x; e < WW; e += blockDim.x) X[e] = cscale(Dk[e], s);
+  }
+  __syncthreads();
+  double2* E = cta_expm(X, Y2, Y3, Y4, R, T, W, red);
+  // E is R or T; reuse X/Y2 for U
+  double2* dUk = P.dU + (size_t)k * WW;
+  const int cur = st->cur;
+  const double2* Uk = P.U[cur] + (size_t)k * WW;
+  for (int e = threadIdx.x; e < WW; e += blockDim.x) {
+    dUk[e] = E[e];
+    X[e] = Uk[e];
+  }
+  __syncthreads();
+  cta_gemm<false>(Y2, W, X, W, E, W, W);
+  __syncthreads();
+  double2* Un = P.U[cur ^ 1] + (size_t)k * WW;
+  for (int e = threadIdx.x; e < WW; e += blockDim.x) Un[e] = Y2[e];
+}
+
+// ----------------------------------------------------------------------------
+// k_m_update: M(k,b) <- dU(k)^H M(k,b) dU(nnlist(k,b))   (src/wannierise.F90:1736-1748)
+// mode 0: step update, reads M[cur], writes M[cur^1] (which selects trial/optimal pass)
+// mode 1: projection (src/overlap.F90:909-923): rotation U[cur], in place on M[cur].
+// Epilogue: block statistics for k_omega.  One CTA (256 threads) per (problem, k*B+b).
+// ----------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_m_update(const Problem* __restrict__ probs, WorkMap wm,
+                                                  int mode, int which) {
+  extern __shared__ double2 smem[];
+  __shared__ double red[256];
+  int kb;
+  const int p = locate(wm, blockIdx.x, kb);
+  const Problem& P = probs[p];
+  CtrlState* st = P.st;
+  if (mode == 0) {
+    if (st->done) return;
+    if (which == 1 && !st->do_second) return;
+  }
+  const int W = P.W, WW = W * W, B = P.B;
+  const int k = kb / B;
+  const int k2 = P.nnlist[kb];
+  const int cur = st->cur;
+  const double2* rot = (mode == 0) ? P.dU : P.U[cur];
+  const double2* Rk = rot + (size_t)k * WW;
+  const double2* Rk2 = rot + (size_t)k2 * WW;
+  const double2* Min = P.M[cur] + (size_t)kb * WW;
+  double2* Mout = P.M[mode == 0 ? (cur ^ 1) : cur] + (size_t)kb * WW;
+  if (W <= kSmemW) {
+    double2 *sR = smem, *sM = smem + WW, *sR2 = smem + 2 * WW, *sT = smem + 3 * WW;
+    for (int e = threadIdx.x; e < WW; e += blockDim.x) {
+      sR[e] = Rk[e];
+      sM[e] = Min[e];
+      sR2[e] = Rk2[e];
+    }
+    __syncthreads();
+    cta_gemm<true>(sT, W, sR, W, sM, W, W);
+    __syncthreads();
+    cta_gemm<false>(sM, W, sT, W, sR2, W, W);
+    __syncthreads();
+    for (int e = threadIdx.x; e < WW; e += blockDim.x) Mout[e] = sM[e];
+    block_stats(sM, W, W, P.diag_ln + (size_t)kb * W, P.diag_abs2 + (size_t)kb * W, P.offd + kb, red);
+  } else {
+    // operands stay in global memory (L1/L2-resident); T = R(k)^H M(k,b) in tbuf
+    double2* Tg = P.tbuf + (size_t)kb * WW;
+    cta_gemm<true>(Tg, W, Rk, W, Min, W, W);
+    __syncthreads();
+    cta_gemm<false>(Mout, W, Tg, W, Rk2, W, W);
+    __syncthreads();
+    block_stats(Mout, W, W, P.diag_ln + (size_t)kb * W, P.diag_abs2 + (size_t)kb * W, P.offd + kb, red);
+  }
+}
+
+// ----------------------------------------------------------------------------
+// k_ctrl_step: internal_optimal_step (src/wannierise.F90:1528-1596).  One thread per problem.
+// ----------------------------------------------------------------------------
+__global__ void k_ctrl_step(const Problem* __restrict__ probs, int nprob) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= nprob) return;
+  const Problem& P = probs[p];
+  CtrlState* st = P.st;
+  if (st->done) return;
+  const Control& c = P.ctl;
+  if (c.lfixstep) {
+    st->lquad = 0;
+    st->do_second = 0;
+    return;
+  }
+  const double trial = st->slot[0].om_tot, cur = st->wann.om_tot;
+  double fac = trial - cur, shift;
+  if (fabs(fac) > 2.2250738585072014e-308) {   // tiny(1.0_dp)
+    fac = 1.0 / fac;
+    shift = 1.0;
+  } else {
+    fac = 1.0e6;
+    shift = fac * trial - fac * cur;
+  }
+  const double eqb = fac * st->doda0;
+  const double eqa = shift - eqb * c.trial_step;
+  int lquad;
+  double alphamin, falphamin;
+  if (fabs(eqa / (fac * cur)) > 2.220446049250313e-16) {
+    lquad = 1;
+    alphamin = -0.5 * eqb / eqa * (c.trial_step * c.trial_step);
+    falphamin = cur - 0.25 * eqb * eqb / (fac * eqa) * (c.trial_step * c.trial_step);
+  } else {
+    lquad = 0;
+    alphamin = c.trial_step;
+    falphamin = trial;
+  }
+  if (st->doda0 * alphamin > 0.0) {
+    lquad = 0;
+    alphamin = c.trial_step;
+    falphamin = trial;
+  }
+  st->lquad = lquad;
+  st->alphamin = alphamin;
+  st->falphamin = falphamin;
+  st->do_second = lquad;
+  st->s_second = alphamin / (4.0 * P.wbtot);
+}
+
+// ----------------------------------------------------------------------------
+// k_ctrl_end: spread bookkeeping, log line, convergence (internal_test_convergence,
+// src/wannierise.F90:1076-1164), buffer flip.  One CTA (128 threads) per problem.
+// ----------------------------------------------------------------------------
+__global__ void k_ctrl_end(const Problem* __restrict__ probs) {
+  const Problem& P = probs[blockIdx.x];
+  CtrlState* st = P.st;
+  if (st->done) return;
+  const int W = P.W;
+  const int acc = st->do_second ? 1 : 0;
+  // accepted centres -> slot 2
+  const double* src = P.centres + (size_t)acc * 4 * W;
+  double* dst = P.centres + (size_t)2 * 4 * W;
+  double* lgc = P.log_centres + (size_t)(st->iter + 1) * 4 * W;
+  for (int i = threadIdx.x; i < 4 * W; i += blockDim.x) {
+    dst[i] = src[i];
+    lgc[i] = src[i];
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  const Control& c = P.ctl;
+  st->old = st->wann;
+  st->wann = st->slot[acc];
+  st->cur ^= 1;
+  const int iter = st->iter + 1;
+  st->iter = iter;
+  double* lg = P.log + (size_t)iter * kLogStride;
+  lg[0] = iter;
+  lg[1] = st->wann.om_tot - st->old.om_tot;
+  lg[2] = sqrt(fabs(st->gcnorm1));
+  lg[3] = st->wann.om_tot;
+  lg[4] = st->wann.om_d;
+  lg[5] = st->wann.om_od;
+  lg[6] = st->lquad;
+  lg[7] = st->alphamin;
+  unsigned long long tns;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(tns));
+  lg[8] = (double)tns;
+  if (c.conv_window > 1) {
+    const double delta = st->wann.om_tot - st->old.om_tot;
+    const int cw = c.conv_window;
+    if (iter <= cw) {
+      st->history[iter - 1] = delta;
+    } else {
+      for (int j = 0; j < cw - 1; ++j) st->history[j] = st->history[j + 1];
+      st->history[cw - 1] = delta;
+    }
+    st->conv_count += 1;
+    if (st->conv_count >= cw) {
+      bool ok = true;
+      for (int j = 0; j < cw; ++j)
+        if (fabs(st->history[j]) > c.conv_tol) ok = false;
+      if (ok) st->lconverged = 1;   // conv_noise_amp > 0 is rejected on the host
+    }
+  }
+  if (st->lconverged || iter >= c.num_iter) st->done = 1;
+  if (!isfinite(st->wann.om_tot)) {
+    st->error = 1;
+    st->done = 1;
+  }
+}
+
+// ----------------------------------------------------------------------------
+// k_log_init: log row 0 = the "Initial State" block (src/wannierise.F90:479-520).
+// ----------------------------------------------------------------------------
+__global__ void k_log_init(const Problem* __restrict__ probs) {
+  const Problem& P = probs[blockIdx.x];
+  const int W = P.W;
+  const double* src = P.centres + (size_t)2 * 4 * W;
+  for (int i = threadIdx.x; i < 4 * W; i += blockDim.x) P.log_centres[i] = src[i];
+  if (threadIdx.x == 0) {
+    const CtrlState* st = P.st;
+    double* lg = P.log;
+    lg[0] = 0;
+    lg[1] = st->wann.om_tot;
+    lg[2] = 0.0;
+    lg[3] = st->wann.om_tot;
+    lg[4] = st->wann.om_d;
+    lg[5] = st->wann.om_od;
+    lg[6] = 0;
+    lg[7] = 0;
+    unsigned long long tns;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(tns));
+    lg[8] = (double)tns;
+  }
+}
+
+// ----------------------------------------------------------------------------
+// Parallel-ordered cyclic Jacobi eigensolver for a Hermitian W x W matrix H (generic
+// pointer, overwritten by its near-diagonal form); V receives the eigenvectors
+// (columns).  Rotation for pair (p,q):  J = [[c, s e^{i phi}], [-s e^{-i phi}, c]],
+// phi = arg(H_pq), (c, s) the real Jacobi rotation of [[H_pp, |H_pq|], [|H_pq|, H_qq]].
+// Returns the number of sweeps used (or -1 when not converged within max_sweeps).
+// ----------------------------------------------------------------------------
+__device__ int cta_jacobi(double2* H, double2* V, int W, int max_sweeps, double* red,
+                          double* rc, double2* rse, int* rp, int* rq) {
+  const int WW = W * W;
+  for (int e = threadIdx.x; e < WW; e += blockDim.x) {
+    V[e] = cmk((e % W) == (e / W) ? 1.0 : 0.0, 0.0);
+  }
+  const int n = (W + 1) & ~1;     // even number of players (one dummy when W is odd)
+  const int npair = n / 2;
+  __syncthreads();
+  for (int sweep = 0; sweep <= max_sweeps; ++sweep) {
+    double off = 0.0, fro = 0.0;
+    for (int e = threadIdx.x; e < WW; e += blockDim.x) {
+      const double a = cabs2(H[e]);
+      fro += a;
+      if ((e % W) != (e / W)) off += a;
+    }
+    off = block_sum(off, red);
+    fro = block_sum(fro, red);
+    if (off <= 1.0e-30 * fro || off == 0.0) return sweep;
+    if (sweep == max_sweeps) break;
+    for (int r = 0; r < n - 1; ++r) {
+      for (int t = threadIdx.x; t < npair; t += blockDim.x) {
+        int p, q;
+        if (t == 0) {
+          p = r;
+          q = n - 1;
+        } else {
+          p = (r + t) % (n - 1);
+          q = (r - t + (n - 1)) % (n - 1);
+        }
+        if (p > q) {
+          const int x = p;
+          p = q;
+          q = x;
+        }
+        double c = 1.0;
+        double2 se = cmk(0, 0);
+        if (q < W) {
+          const double2 b = H[q * W + p];
+          const double ab = sqrt(cabs2(b));
+          if (ab > 1.0e-300) {
+            const double a = H[p * W + p].x, d = H[q * W + q].x;
+            const double th = (d - a) / (2.0 * ab);
+            const double tt = (th >= 0.0 ? 1.0 : -1.0) / (fabs(th) + sqrt(1.0 + th * th));
+            c = 1.0 / sqrt(1.0 + tt * tt);
+            const double s = tt * c;
+            se = cmk(s * b.x / ab, s * b.y / ab);
+          }
+        }
+        rp[t] = p;
+        rq[t] = q;
+        rc[t] = c;
+        rse[t] = se;
+      }
+      __syncthreads();
+      // columns: H <- H J, V <- V J
+      for (int e = threadIdx.x; e < W * npair; e += blockDim.x) {
+        const int i = e % W, t = e / W;
+        const int p = rp[t], q = rq[t];
+        if (q >= W) continue;
+        const double c = rc[t];
+        const double2 se = rse[t];
+        const double2 hp = H[p * W + i], hq = H[q * W + i];
+        // (HJ)_ip = c H_ip - conj(se) H_iq ; (HJ)_iq = se H_ip + c H_iq
+        H[p * W + i] = csub(cscale(hp, c), cmul(cconj(se), hq));
+        H[q * W + i] = cadd(cmul(se, hp), cscale(hq, c));
+        const double2 vp = V[p * W + i], vq = V[q * W + i];
+        V[p * W + i] = csub(cscale(vp, c), cmul(cconj(se), vq));
+        V[q * W + i] = cadd(cmul(se, vp), cscale(vq, c));
+      }
+      __syncthreads();
+      // rows: H <- J^H H
+      for (int e = threadIdx.x; e < W * npair; e += blockDim.x) {
+        const int j = e % W, t = e / W;
+        const int p = rp[t], q = rq[t];
+        if (q >= W) continue;
+        const double c = rc[t];
+        const double2 se = rse[t];
+        const double2 hp = H[j * W + p], hq = H[j * W + q];
+        // (J^H H)_pj = c H_pj - se H_qj ; (J^H H)_qj = conj(se) H_pj + c H_qj
+        H[j * W + p] = csub(cscale(hp, c), cmul(se, hq));
+        H[j * W + q] = cadd(cmul(cconj(se), hp), cscale(hq, c));
+      }
+      __syncthreads();
+    }
+  }
+  return -1;
+}
+
+// ----------------------------------------------------------------------------
+// k_lowdin: overlap_project's U(k) = Z V^dagger from A(k) = Z S V^dagger
+// (src/overlap.F90:842-860), computed as U = A (A^H A)^{-1/2} = A V L^{-1/2} V^H with the
+// Jacobi eigenpairs (V, L) of A^H A: the same unitary polar factor for full-rank A.
+// Input A(k) in U[cur](k) (the reference reads A into u_matrix, src/wannier_prog.F90:523-529);
+// output U overwrites it.  One CTA (256 threads) per (problem, k).
+// Status per k: 0 ok, 1 rank deficient, 2 Jacobi not converged.
+// ----------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_lowdin(const Problem* __restrict__ probs, WorkMap wm,
+                                                int* __restrict__ status) {
+  extern __shared__ double2 smem[];
+  __shared__ double red[256];
+  __shared__ double rc[128];
+  __shared__ double2 rse[128];
+  __shared__ int rp[128], rq[128];
+  int k;
+  const int p = locate(wm, blockIdx.x, k);
+  const Problem& P = probs[p];
+  const int W = P.W, WW = W * W;
+  double2* buf = (W <= kSmemW) ? smem : (P.work + (size_t)k * 6 * WW);
+  double2 *A = buf, *S = buf + WW, *V = buf + 2 * WW, *T = buf + 3 * WW;
+  double2* Uk = P.U[P.st->cur] + (size_t)k * WW;
+  for (int e = threadIdx.x; e < WW; e += blockDim.x) A[e] = Uk[e];
+  __syncthreads();
+  cta_gemm<true>(S, W, A, W, A, W, W);
+  __syncthreads();
+  const int sweeps = cta_jacobi(S, V, W, 60, red, rc, rse, rp, rq);
+  // V' = V diag(lambda^{-1/2}) into T
+  __shared__ int bad;
+  if (threadIdx.x == 0) bad = (sweeps < 0) ? 2 : 0;
+  __syncthreads();
+  for (int e = threadIdx.x; e < WW; e += blockDim.x) {
+    const int j = e / W;
+    const double l = S[j * W + j].x;
+    if (!(l > 0.0)) bad = 1;
+    T[e] = cscale(V[e], 1.0 / sqrt(l));
+  }
+  __syncthreads();
+  cta_gemm<false>(S, W, A, W, T, W, W);      // S <- A V L^{-1/2}
+  __syncthreads();
+  // U = S V^H : compute via (V S^H)^H  -> use conj-transposed product with A := V
+  // U_ij = sum_l S_il conj(V_jl)
+  for (int e = threadIdx.x; e < WW; e += blockDim.x) {
+    const int i = e % W, j = e / W;
+    double2 acc = cmk(0, 0);
+    for (int l = 0; l < W; ++l) {
+      const double2 s = S[l * W + i];
+      const double2 v = V[l * W + j];
+      acc = cadd(acc, cmulc(s, v));
+    }
+    Uk[e] = acc;
+  }
+  if (threadIdx.x == 0) status[blockIdx.x] = bad;
+}
+
+// ----------------------------------------------------------------------------
+// k_unitarity: wann_check_unitarity (src/wannierise.F90:2594-2661); writes
+// max(|U U^H - I|, |U^H U - I|) per (problem, k).  One CTA (128 threads) per item.
+// ----------------------------------------------------------------------------
+__global__ void k_unitarity(const Problem* __restrict__ probs, WorkMap wm, double* __restrict__ out) {
+  __shared__ double red[128];
+  int k;
+  const int p = locate(wm, blockIdx.x, k);
+  const Problem& P = probs[p];
+  const int W = P.W;
+  const double2* U = P.U[P.st->cur] + (size_t)k * W * W;
+  double mx = 0.0;
+  for (int e = threadIdx.x; e < W * W; e += blockDim.x) {
+    const int i = e % W, j = e / W;
+    double2 a = cmk(0, 0), b = cmk(0, 0);
+    for (int m = 0; m < W; ++m) {
+      a = cadd(a, cmulc(U[m * W + i], U[m * W + j]));      // (U U^H)_ij
+      b = cadd(b, cmulc(U[j * W + m], U[i * W + m]));      // (U^H U)_ij
+    }
+    if (i == j) {
+      a.x -= 1.0;
+      b.x -= 1.0;
+    }
+    mx = fmax(mx, fmax(sqrt(cabs2(a)), sqrt(cabs2(b))));
+  }
+  mx = block_max(mx, red);
+  if (threadIdx.x == 0) out[blockIdx.x] = mx;
+}
+
+// ----------------------------------------------------------------------------
+// k_all_done: *out = 1 when every problem of the batch has finished.
+// ----------------------------------------------------------------------------
+__global__ void k_all_done(const Problem* __restrict__ probs, int nprob, int* __restrict__ out) {
+  __shared__ int active;
+  if (threadIdx.x == 0) active = 0;
+  __syncthreads();
+  for (int p = threadIdx.x; p < nprob; p += blockDim.x)
+    if (!probs[p].st->done) active = 1;
+  __syncthreads();
+  if (threadIdx.x == 0) *out = active ? 0 : 1;
+}
+
+// ----------------------------------------------------------------------------
+// k_fp64_peak: FP64 FMA throughput probe (8 independent dependency chains per thread).
+// Used to state the FP64-pipe roofline, which the measured-peaks file does not carry.
+// ----------------------------------------------------------------------------
+__global__ void k_fp64_peak(double* __restrict__ out, int iters, double seed) {
+  double a[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) a[i] = seed + threadIdx.x * 1e-9 + i;
+  const double m = 0.999999999, c = 1e-12;
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) a[i] = fma(a[i], m, c);
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) s += a[i];
+  if (s == 12345.678) out[0] = s;   // keeps the chains live; never true for these inputs
+}
+
+}  // namespace w90g

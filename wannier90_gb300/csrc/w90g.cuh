@@ -1,0 +1,147 @@
+// Shared device-side definitions of the GB300 MLWF engine.
+//
+// Layout in HBM (one "problem" = one wann_main solve):
+//   M[buf][k][b]  W x W complex128 block, column-major (element (m,n) at n*W+m),
+//                 exactly the reference's m_matrix_loc(W,W,B,K) layout.
+//   U[buf][k]     W x W complex128, column-major (u_matrix(W,W,K)).
+//   G[k], D[k]    gradient (cdodq) and kept search direction (cdqkeep).
+//   dU[k]         the rotation exp(s*D(k)) of the current step.
+//   diag_ln, diag_abs2 [k][b][n], offd [k][b]  per-block statistics written by the
+//                 M-update epilogue and read by the spread reduction.
+// Two buffers of M and U are kept: `st->cur` selects the accepted state; every update
+// reads buffer cur and writes buffer cur^1, so the line-search "restore" of the
+// reference (src/wannierise.F90:608-615, :668-675) never copies memory.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace w90g {
+
+// ----------------------------------------------------------------------------
+// complex helpers (double2 = re, im)
+// ----------------------------------------------------------------------------
+__host__ __device__ __forceinline__ double2 cmk(double r, double i) { return make_double2(r, i); }
+__host__ __device__ __forceinline__ double2 cadd(double2 a, double2 b) { return cmk(a.x + b.x, a.y + b.y); }
+__host__ __device__ __forceinline__ double2 csub(double2 a, double2 b) { return cmk(a.x - b.x, a.y - b.y); }
+__host__ __device__ __forceinline__ double2 cscale(double2 a, double s) { return cmk(a.x * s, a.y * s); }
+__host__ __device__ __forceinline__ double2 cconj(double2 a) { return cmk(a.x, -a.y); }
+__host__ __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return cmk(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
+}
+// a * conj(b)
+__host__ __device__ __forceinline__ double2 cmulc(double2 a, double2 b) {
+  return cmk(fma(a.x, b.x, a.y * b.y), fma(a.y, b.x, -a.x * b.y));
+}
+#ifdef __CUDACC__
+// acc += a * b
+__device__ __forceinline__ void cfma(double2& acc, double2 a, double2 b) {
+  acc.x = fma(a.x, b.x, acc.x);
+  acc.x = fma(-a.y, b.y, acc.x);
+  acc.y = fma(a.x, b.y, acc.y);
+  acc.y = fma(a.y, b.x, acc.y);
+}
+// acc += conj(a) * b
+__device__ __forceinline__ void cfmac(double2& acc, double2 a, double2 b) {
+  acc.x = fma(a.x, b.x, acc.x);
+  acc.x = fma(a.y, b.y, acc.x);
+  acc.y = fma(a.x, b.y, acc.y);
+  acc.y = fma(-a.y, b.x, acc.y);
+}
+__host__ __device__ __forceinline__ double cabs2(double2 a) { return a.x * a.x + a.y * a.y; }
+__device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
+  // plain a*conj(b)/|b|^2, as Fortran complex division of well-scaled operands
+  double d = b.x * b.x + b.y * b.y;
+  double2 n = cmulc(a, b);
+  return cmk(n.x / d, n.y / d);
+}
+#endif
+
+// ----------------------------------------------------------------------------
+// controller state of one problem (device memory, one per problem)
+// Mirrors the scalar locals of wann_main (src/wannierise.F90:150-175).
+// ----------------------------------------------------------------------------
+constexpr int kMaxConvWindow = 64;
+
+struct Spread {
+  double om_i, om_d, om_od, om_tot;
+};
+
+struct CtrlState {
+  // loop bookkeeping
+  int iter;            // iterations completed
+  int done;            // 1 => no further work (converged, num_iter reached or error)
+  int cur;             // accepted buffer index (0/1)
+  int error;           // 0 ok, >0 engine error code
+  int ncg;
+  int lquad;
+  int do_second;       // second update (parabolic optimum) required this iteration
+  int conv_count, noise_count, lrandom, lfirst, lconverged;
+  int first_pass;
+  int pad0;
+  // CG
+  double gcnorm0, gcnorm1, gcfac, doda0;
+  double coefG, coefD;   // D <- coefG*G + coefD*D_prev
+  double s_trial;        // X = s*D for the trial step
+  double s_second;       // X = s*D for the optimal step
+  double alphamin, falphamin;
+  double save_spread;
+  double om_invariant;
+  Spread wann, old, slot[2];   // slot[0] = trial spread, slot[1] = optimal-step spread
+  double history[kMaxConvWindow];
+};
+
+// wann_control_type subset used on device (src/wannier90_types.F90:170-192)
+struct Control {
+  int num_iter, num_cg_steps, conv_window, conv_noise_num;
+  int lfixstep, pad;
+  double conv_tol, trial_step, fixed_step, conv_noise_amp;
+};
+
+// per-iteration record (the <-- CONV / <-- SPRD lines, src/wannierise.F90:704-756)
+constexpr int kLogStride = 10;  // iter, delta, rms_grad, om_tot, om_d, om_od, lquad, alphamin, t_ns, pad
+
+struct Problem {
+  int W, K, B, nthr_pad;
+  double wbtot;
+  double2* M[2];
+  double2* U[2];
+  double2* G;
+  double2* D;
+  double2* dU;
+  double2* work;        // exp / eig workspace (W > 32): 6*W*W per k
+  double2* tbuf;        // M-update intermediate (W > 32): W*W per (k,b)
+  const int* nnlist;    // [k][b] 0-based
+  const double* bk;     // [k][b][3]
+  const double* wb;     // [b]
+  double* diag_ln;      // [k][b][n]  Im ln M_nn
+  double* diag_abs2;    // [k][b][n]  |M_nn|^2
+  double* offd;         // [k][b]     sum_{m!=n} |M_mn|^2
+  double* gpart;        // [k][2]     sum |G|^2, sum Re conj(G) D_prev  (per k)
+  double* centres;      // [slot][4][W]: rave(3,W) + r2ave-rave2 (W) per spread slot; slot 2 = accepted
+  double* log;          // [num_iter+1][kLogStride]
+  double* log_centres;  // [num_iter+1][4][W]
+  CtrlState* st;
+  Control ctl;
+  int max_exp_squarings;
+  int pad2;
+};
+
+// Work map: blockIdx.x -> (problem, local index) over a prefix sum.
+struct WorkMap {
+  const int* offs;  // nprob+1 prefix sums of work items per problem
+  int nprob;
+};
+
+#ifdef __CUDACC__
+__device__ __forceinline__ int locate(const WorkMap& wm, int item, int& local) {
+  int lo = 0, hi = wm.nprob - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (__ldg(wm.offs + mid) <= item) lo = mid; else hi = mid - 1;
+  }
+  local = item - __ldg(wm.offs + lo);
+  return lo;
+}
+#endif
+
+}  // namespace w90g

@@ -1,0 +1,249 @@
+"""Python mirror of Wannier90's library interface for the wannierisation path.
+
+The reference exposes ``w90_library`` (src/library_interface.F90) to Python through
+f90wrap (wrap/Makefile.serial:52-71): a ``lib_common_type`` object plus module
+functions ``w90_set_option``, ``w90_input_setopt``, ``w90_get_nn``, ``w90_get_nnkp``,
+``w90_set_m_local``, ``w90_set_u_matrix``, ``w90_set_u_opt``, ``w90_project_overlap``,
+``w90_wannierise``, ``w90_get_centres``, ``w90_get_spreads``.  This module provides the
+same names and argument meaning on top of the engine's C ABI
+(include/wannier90_gb300.h).  Arrays are NumPy arrays in Fortran order, exactly the
+reference's shapes:
+
+    m_matrix  complex128 (num_bands, num_bands, nntot, num_kpts)
+    u_matrix  complex128 (num_wann, num_wann, num_kpts)
+    u_opt     complex128 (num_bands, num_wann, num_kpts)
+
+Status: functions return ``ierr`` like the Fortran library (0 ok, >0 error, <0 warning).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from ._native import lib
+
+
+class W90Error(RuntimeError):
+    def __init__(self, ierr, msg):
+        super().__init__("ierr=%d: %s" % (ierr, msg))
+        self.ierr = ierr
+
+
+def _cplx(a, shape=None):
+    a = np.asarray(a)
+    if a.dtype != np.complex128 or not a.flags.f_contiguous:
+        raise TypeError("expected a Fortran-ordered complex128 array")
+    if shape is not None and a.shape != tuple(shape):
+        raise ValueError("array shape %s, expected %s" % (a.shape, tuple(shape)))
+    return a
+
+
+class LibCommon:
+    """Counterpart of ``lib_common_type`` (src/library_interface.F90:27-99)."""
+
+    def __init__(self):
+        self._L = lib()
+        self._h = self._L.w90_create()
+        self._keep = {}      # arrays whose pointers the library holds
+        self.num_wann = self.num_bands = self.num_kpts = 0
+        self.nntot = 0
+
+    def __del__(self):
+        try:
+            if self._h:
+                self._L.w90_delete(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def last_error(self):
+        return self._L.w90g_last_error(self._h).decode()
+
+
+def w90_create():
+    return LibCommon()
+
+
+def w90_set_option(common: LibCommon, keyword: str, value):
+    """w90_set_option (src/library_interface.F90:667-808): int, bool, real, 1-D int,
+    2-D real (kpoints: shape (num_kpts, 3); unit_cell_cart: rows a_1..a_3 in Angstrom)."""
+    L, h, key = common._L, common._h, keyword.encode()
+    if isinstance(value, (bool, np.bool_)):
+        L.cset_option_int(h, key, int(bool(value)))
+    elif isinstance(value, (int, np.integer)):
+        L.cset_option_int(h, key, int(value))
+    elif isinstance(value, (float, np.floating)):
+        L.cset_option_float(h, key, float(value))
+    else:
+        a = np.asarray(value)
+        if a.dtype.kind in "iu":
+            a = np.ascontiguousarray(a, dtype=np.int32).reshape(-1)
+            if a.size == 3 and keyword.lower() == "mp_grid":
+                L.cset_option_int3(h, key, a.ctypes.data_as(C.POINTER(C.c_int)))
+            else:
+                L.cset_option_intx(h, key, a.ctypes.data_as(C.POINTER(C.c_int)), a.size)
+        else:
+            a = np.ascontiguousarray(a, dtype=np.float64)
+            if a.ndim == 1:
+                a = a.reshape(1, -1)
+            if a.shape == (3, 3) and keyword.lower() == "unit_cell_cart":
+                L.cset_option_float33(h, key, a.ctypes.data_as(C.POINTER(C.c_double)))
+            else:
+                L.cset_option_floatxy(h, key, a.ctypes.data_as(C.POINTER(C.c_double)),
+                                      a.shape[0], a.shape[1])
+
+
+def w90_input_setopt(common: LibCommon, seedname: str = "wannier", comm: int = 0) -> int:
+    """w90_input_setopt (src/library_interface.F90:161-292): process options, build the k-mesh."""
+    ierr = C.c_int(0)
+    common._L.cinput_setopt(common._h, seedname.encode(), C.byref(ierr), int(comm))
+    if ierr.value == 0:
+        nn = C.c_int(0)
+        common._L.cget_nn(common._h, C.byref(nn))
+        common.nntot = nn.value
+    return ierr.value
+
+
+def w90_get_nn(common: LibCommon) -> int:
+    nn = C.c_int(0)
+    common._L.cget_nn(common._h, C.byref(nn))
+    return nn.value
+
+
+def w90_get_nnkp(common: LibCommon, num_kpts: int) -> np.ndarray:
+    """nnlist as (num_kpts, nntot) int32, 1-based (w90_get_nnkp)."""
+    B = w90_get_nn(common)
+    out = np.zeros((num_kpts, B), dtype=np.int32, order="F")
+    common._L.cget_nnkp(common._h, out.ctypes.data_as(C.POINTER(C.c_int)))
+    return out
+
+
+def w90_get_gkpb(common: LibCommon, num_kpts: int) -> np.ndarray:
+    """nncell as (3, num_kpts, nntot) int32 (w90_get_gkpb)."""
+    B = w90_get_nn(common)
+    out = np.zeros((3, num_kpts, B), dtype=np.int32, order="F")
+    common._L.cget_gkpb(common._h, out.ctypes.data_as(C.POINTER(C.c_int)))
+    return out
+
+
+def w90_set_m_local(common: LibCommon, m):
+    common._keep["m"] = _cplx(m)
+    common._L.cset_m_local(common._h, common._keep["m"].ctypes.data)
+
+
+def w90_set_u_matrix(common: LibCommon, u):
+    common._keep["u"] = _cplx(u)
+    common._L.cset_u_matrix(common._h, common._keep["u"].ctypes.data)
+
+
+def w90_set_u_opt(common: LibCommon, u_opt):
+    common._keep["u_opt"] = _cplx(u_opt)
+    common._L.cset_u_opt(common._h, common._keep["u_opt"].ctypes.data)
+
+
+def w90_set_eigval(common: LibCommon, eigval):
+    e = np.asarray(eigval, dtype=np.float64)
+    if not e.flags.f_contiguous:
+        raise TypeError("expected a Fortran-ordered float64 array")
+    common._keep["eig"] = e
+    common._L.cset_eigval(common._h, e.ctypes.data)
+
+
+def w90_project_overlap(common: LibCommon) -> int:
+    """Loewdin initialisation (src/library_interface.F90:422-462) on the GPU."""
+    ierr = C.c_int(0)
+    common._L.cproject_overlap(common._h, C.byref(ierr))
+    return ierr.value
+
+
+def w90_wannierise(common: LibCommon) -> int:
+    """wann_main (src/library_interface.F90:464-530) on the GPU; U and M updated in place."""
+    ierr = C.c_int(0)
+    common._L.cwannierise(common._h, C.byref(ierr))
+    return ierr.value
+
+
+def w90_wannierise_device(common: LibCommon, m_ptr: int, u_ptr: int) -> int:
+    """wann_main with M and U already resident in device memory (raw CUDA pointers)."""
+    ierr = C.c_int(0)
+    common._L.w90g_wannierise_device(common._h, C.c_void_p(m_ptr), C.c_void_p(u_ptr), C.byref(ierr))
+    return ierr.value
+
+
+def w90_project_overlap_device(common: LibCommon, m_ptr: int, u_ptr: int) -> int:
+    ierr = C.c_int(0)
+    common._L.w90g_project_overlap_device(common._h, C.c_void_p(m_ptr), C.c_void_p(u_ptr), C.byref(ierr))
+    return ierr.value
+
+
+def w90_get_centres(common: LibCommon, num_wann: int) -> np.ndarray:
+    """Wannier centres as (3, num_wann) (Fortran layout, Angstrom)."""
+    out = np.zeros((3, num_wann), dtype=np.float64, order="F")
+    common._L.cget_centres(common._h, out.ctypes.data_as(C.POINTER(C.c_double)))
+    return out
+
+
+def w90_get_spreads(common: LibCommon, num_wann: int) -> np.ndarray:
+    out = np.zeros(num_wann, dtype=np.float64)
+    common._L.cget_spreads(common._h, out.ctypes.data_as(C.POINTER(C.c_double)))
+    return out
+
+
+def w90_get_omega(common: LibCommon) -> np.ndarray:
+    """(Omega_I, Omega_D, Omega_OD, Omega_total)."""
+    out = np.zeros(4, dtype=np.float64)
+    common._L.cget_omega(common._h, out.ctypes.data_as(C.POINTER(C.c_double)))
+    return out
+
+
+def w90_get_log(common: LibCommon, max_rows: int) -> np.ndarray:
+    """Per-iteration record: columns iter, dOmega, rms_grad, Omega, Omega_D, Omega_OD,
+    lquad, alphamin, device time (ns), 0."""
+    out = np.zeros((max_rows, 10), dtype=np.float64)
+    n = common._L.w90g_get_log(common._h, out.ctypes.data_as(C.POINTER(C.c_double)), max_rows)
+    return out[:n]
+
+
+def w90_get_log_centres(common: LibCommon, max_rows: int, num_wann: int) -> np.ndarray:
+    out = np.zeros((max_rows, 4 * num_wann), dtype=np.float64)
+    n = common._L.w90g_get_log_centres(common._h, out.ctypes.data_as(C.POINTER(C.c_double)), max_rows)
+    return out[:n].reshape(n, 4, num_wann)
+
+
+def w90_set_stream(common: LibCommon, cuda_stream: int):
+    common._L.w90g_set_stream(common._h, C.c_void_p(cuda_stream))
+
+
+def w90_kernel_launches(common: LibCommon) -> int:
+    return int(common._L.w90g_kernel_launches(common._h))
+
+
+def check(common: LibCommon, ierr: int, what: str):
+    if ierr > 0:
+        raise W90Error(ierr, "%s: %s" % (what, common.last_error()))
+    return ierr
+
+
+def setup(*, kpoints, unit_cell_cart, num_wann, num_bands=None, mp_grid=None, **options) -> LibCommon:
+    """wannier_setup-style helper (test-suite/libv2-demo/*/wannier.cc:5-34)."""
+    c = w90_create()
+    kp = np.asarray(kpoints, dtype=np.float64)
+    w90_set_option(c, "kpoints", kp)
+    w90_set_option(c, "num_kpts", int(kp.shape[0]))
+    w90_set_option(c, "num_wann", int(num_wann))
+    w90_set_option(c, "num_bands", int(num_bands or num_wann))
+    w90_set_option(c, "unit_cell_cart", np.asarray(unit_cell_cart, dtype=np.float64))
+    if mp_grid is not None:
+        w90_set_option(c, "mp_grid", np.asarray(mp_grid, dtype=np.int32))
+    for k, v in options.items():
+        w90_set_option(c, k, v)
+    check(c, w90_input_setopt(c), "w90_input_setopt")
+    c.num_wann = int(num_wann)
+    c.num_bands = int(num_bands or num_wann)
+    c.num_kpts = int(kp.shape[0])
+    return c
