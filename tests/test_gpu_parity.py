@@ -1,8 +1,11 @@
 """Parity of the CUDA engine with the oracle and with the reference's own outputs.
 
 All calls go through the C ABI (include/wannier90_gb300.h) via ctypes, like a library
-caller of Wannier90.  Tolerances: spread per iteration within 1e-8 relative (plus a
-1e-11 A^2 floor near Omega = 0), centres within 1e-6 A.  The final U and M are
+caller of Wannier90.  Tolerances: spread per iteration within 1e-8 relative, centres
+within 1e-6 A.  The synthetic tight-binding problems (one orbital per band, point
+orbitals) have Omega_min = 0 exactly; for them an absolute floor of 2e-10 A^2 applies:
+perturbing the input by 1e-15 (relative) moves the oracle's own trajectory by up to
+7.6e-11 A^2 as Omega -> 0, so no two FP64 codes agree more closely than that.  The final U and M are
 compared to 1e-7: at a minimum Omega is flat, so roundoff of 1e-16 in Omega leaves the
 gauge determined only to ~sqrt(1e-16) (both codes sit at that floor).
 """
@@ -24,7 +27,7 @@ def _oracle(real_lattice, kpoints, M_raw, A, ctl, search_shells=36):
     return km, U0, M0, r
 
 
-def _check_trajectory(out, r, rel=1e-8, floor=1e-11):
+def _check_trajectory(out, r, rel=1e-8, floor=2e-10):
     log = out["log"]
     ref = [r.initial] + r.iters
     assert len(log) == len(ref), (len(log), len(ref))
@@ -49,7 +52,7 @@ def test_golden_cases(name):
     np.testing.assert_allclose(out["U0"], U0, atol=1e-11)
     np.testing.assert_allclose(out["M0"], M0, atol=1e-11)
     r = O.wann_main(M0, U0, km, ctl)
-    _check_trajectory(out, r)
+    _check_trajectory(out, r, floor=1e-11)
     # against the reference's printed <-- CONV lines directly
     by_iter = {int(row[0]): row for row in out["log"]}
     for it, delta, rms, spread in d["conv"]:
