@@ -110,6 +110,21 @@ int w90g_profile_device(void* handle, double* d_m_matrix, double* d_u_matrix, in
 const char* w90g_profile_kernel_name(int i);
 /* FP64 FMA throughput of the current device in TFLOP/s (dependent-chain probe). */
 double w90g_measure_fp64_peak(void);
+/* Loewdin projection (as w90g_project_overlap_device) that allocates no device memory.
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc where they
+ * project: e.g. a DFT code whose device memory all belongs to its own pool allocator.
+ * d_m_matrix / d_u_matrix are the caller's device buffers (layouts as above; u holds
+ * A(k) on entry), updated in place; nnkp is the host array cget_nnkp returns
+ * ([nntot][num_kpts], 1-based).  Scratch lives in a file-scope device array of about
+ * 4.3 MB that every GPU loading the library keeps until exit; limits num_wann <= 32,
+ * num_kpts <= 4096, num_kpts*nntot <= 8192 (larger sizes return 5 without GPU work).
+ * The first call on a device resolves that array's address (cudaGetSymbolAddress) and
+ * sets kernel attributes, so make it before any stream capture.  Calls share the array:
+ * calls whose GPU work overlaps (other streams or threads) race.  cuda_stream may be
+ * NULL (legacy default stream).  Returns 0 ok, 1 CUDA error / rank-deficient A(k),
+ * 5 sizes out of range.  Synchronises the stream before returning. */
+int w90g_project_overlap_noalloc(int num_wann, int num_kpts, int nntot, const int* nnkp,
+                                 double* d_m_matrix, double* d_u_matrix, void* cuda_stream);
 
 #ifdef __cplusplus
 }  /* extern "C" */

@@ -13,6 +13,7 @@
 // reference (src/wannierise.F90:608-615, :668-675) never copies memory.
 #pragma once
 #include <cuda_runtime.h>
+#include <math.h>
 #include <stdint.h>
 
 namespace w90g {
