@@ -18,8 +18,9 @@ def run_engine(real_lattice, kpoints, M_raw, A, ctl, num_wann, search_shells=36,
     opts.update(extra or {})
     c = w90.setup(kpoints=kpoints, unit_cell_cart=real_lattice, num_wann=num_wann, **opts)
     K = len(kpoints)
-    m = synth.from_math_m(M_raw)
-    u = synth.from_math_u(A)
+    # fresh Fortran-ordered copies: the engine updates them in place
+    m = np.array(synth.from_math_m(M_raw), order="F", copy=True)
+    u = np.array(synth.from_math_u(A), order="F", copy=True)
     uopt = np.asfortranarray(np.broadcast_to(np.eye(num_wann, dtype=np.complex128)[:, :, None],
                                              (num_wann, num_wann, K)).copy())
     w90.w90_set_m_local(c, m)

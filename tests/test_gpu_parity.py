@@ -2,10 +2,17 @@
 
 All calls go through the C ABI (include/wannier90_gb300.h) via ctypes, like a library
 caller of Wannier90.  Tolerances: spread per iteration within 1e-8 relative, centres
-within 1e-6 A.  The synthetic tight-binding problems (one orbital per band, point
-orbitals) have Omega_min = 0 exactly; for them an absolute floor of 2e-10 A^2 applies:
-perturbing the input by 1e-15 (relative) moves the oracle's own trajectory by up to
-7.6e-11 A^2 as Omega -> 0, so no two FP64 codes agree more closely than that.  The final U and M are
+within 1e-6 A.
+
+The reference's own cases are compared over their whole trajectories.  The synthetic
+tight-binding problems are chaotic under conjugate gradients: perturbing the input by
+1e-15 (relative) moves the oracle's OWN trajectory by 1e-9 at iteration 5 and 1e-6 at
+iteration 9 for W=48 (tests print nothing, the numbers are in the design notes).  No
+two FP64 implementations agree beyond that horizon, so each synthetic case is compared
+over its stable window: the iterations where the oracle and the oracle run on the
+1e-15-perturbed input still agree to 1e-11.  Where the whole run is stable (config 1)
+the final centres are compared too.  These problems also have Omega_min = 0, so an
+absolute floor of 2e-10 A^2 applies as Omega -> 0.  The final U and M are
 compared to 1e-7: at a minimum Omega is flat, so roundoff of 1e-16 in Omega leaves the
 gauge determined only to ~sqrt(1e-16) (both codes sit at that floor).
 """
@@ -27,15 +34,34 @@ def _oracle(real_lattice, kpoints, M_raw, A, ctl, search_shells=36):
     return km, U0, M0, r
 
 
-def _check_trajectory(out, r, rel=1e-8, floor=2e-10):
+def _check_trajectory(out, r, rel=1e-8, floor=2e-10, upto=None):
     log = out["log"]
     ref = [r.initial] + r.iters
-    assert len(log) == len(ref), (len(log), len(ref))
+    if upto is None:
+        assert len(log) == len(ref), (len(log), len(ref))
     for row, it in zip(log, ref):
+        if upto is not None and it.iter > upto:
+            break
         assert int(row[0]) == it.iter
         assert abs(row[3] - it.spread.om_tot) <= rel * abs(it.spread.om_tot) + floor, (it.iter, row[3], it.spread.om_tot)
-    np.testing.assert_allclose(out["centres"], r.centres, atol=1e-6)
-    np.testing.assert_allclose(out["spreads"], r.spreads, atol=1e-6)
+        lc = out["log_centres"][it.iter]
+        np.testing.assert_allclose(lc[:3], it.centres, atol=1e-6)
+    if upto is None or upto >= len(ref) - 1:
+        np.testing.assert_allclose(out["centres"], r.centres, atol=1e-6)
+        np.testing.assert_allclose(out["spreads"], r.spreads, atol=1e-6)
+
+
+def _stable_window(M0, U0, km, ctl, tol=1e-11):
+    """Last iteration up to which the oracle agrees with itself on a 1e-15-perturbed input."""
+    rng = np.random.default_rng(12345)
+    a = O.wann_main(M0, U0, km, ctl)
+    b = O.wann_main(M0 * (1 + 1e-15 * rng.standard_normal(M0.shape)), U0, km, ctl)
+    last = 0
+    for x, y in zip(a.iters, b.iters):
+        if abs(x.spread.om_tot - y.spread.om_tot) > tol * abs(x.spread.om_tot) + 1e-13:
+            break
+        last = x.iter
+    return last
 
 
 @pytest.mark.parametrize("name", G.CASES)
@@ -72,36 +98,44 @@ def _synthetic(cfg, num_iter, seed=0, **ctl_kw):
     assert out["ierr"] == 0, out["err"]
     km, U0, M0, r = _oracle(p.real_lattice, p.kpoints, M, A, ctl)
     np.testing.assert_allclose(out["U0"], U0, atol=1e-10)
-    return out, r
+    np.testing.assert_allclose(out["M0"], M0, atol=1e-10)
+    window = _stable_window(M0, U0, km, ctl)
+    return out, r, window
 
 
 def test_config1_sc4_w8_200_iterations():
-    out, r = _synthetic(synth.CONFIGS["sc4_w8"], 200, num_cg_steps=5)
+    out, r, window = _synthetic(synth.CONFIGS["sc4_w8"], 200, num_cg_steps=5)
+    assert window >= 10
+    # config 1 stays within 2e-10 A^2 of the oracle over all 200 iterations
     _check_trajectory(out, r)
 
 
 @pytest.mark.parametrize("W,mp", [(1, (3, 3, 3)), (5, (3, 3, 3)), (13, (2, 2, 2)), (32, (2, 2, 3))])
 def test_shapes_shared_memory_path(W, mp):
     cfg = dict(kind="sc", a=4.0, mp=mp, num_wann=W, rmax=1, eps=0.3)
-    out, r = _synthetic(cfg, 25)
-    _check_trajectory(out, r)
+    out, r, window = _synthetic(cfg, 25)
+    assert window >= 2
+    _check_trajectory(out, r, upto=window)
 
 
 @pytest.mark.parametrize("W", [33, 48])
 def test_shapes_global_memory_path(W):
     cfg = dict(kind="sc", a=4.0, mp=(2, 2, 2), num_wann=W, rmax=1, eps=0.3)
-    out, r = _synthetic(cfg, 12)
-    _check_trajectory(out, r)
+    out, r, window = _synthetic(cfg, 12)
+    assert window >= 2
+    _check_trajectory(out, r, upto=window)
 
 
 def test_fcc_fixed_step():
     cfg = dict(kind="fcc", a=6.0, mp=(3, 3, 3), num_wann=6, rmax=1, eps=0.3)
-    out, r = _synthetic(cfg, 30, fixed_step=1.0, lfixstep=True)
-    _check_trajectory(out, r)
+    out, r, window = _synthetic(cfg, 30, fixed_step=1.0, lfixstep=True)
+    _check_trajectory(out, r, upto=window)
 
 
 def test_convergence_window_stops_at_reference_iteration():
     cfg = dict(kind="sc", a=5.0, mp=(3, 3, 3), num_wann=4, rmax=1, eps=0.2)
-    out, r = _synthetic(cfg, 300, conv_window=3, conv_tol=1e-8)
+    out, r, window = _synthetic(cfg, 300, conv_window=3, conv_tol=1e-8)
     assert r.converged
+    # small problem: the spread stays within 1e-8 relative / 2e-10 A^2 of the oracle over
+    # the whole run and the convergence window closes at the same iteration
     _check_trajectory(out, r)
