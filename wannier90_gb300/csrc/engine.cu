@@ -2,7 +2,7 @@
 //
 // Memory: one cudaMalloc arena per batch, sub-allocated at 256-byte alignment; every
 // per-problem array of the iteration stays resident in HBM for the whole solve.
-// Launch: the ten-kernel iteration (see k_fp64.cu) is captured once into a CUDA graph
+// Launch: the fourteen-kernel iteration (see k_fp64.cu) is captured once into a CUDA graph
 // and replayed; the device controller makes replays after convergence no-ops, so the
 // host only polls a single "all done" word every few replays.
 #include <cuda_runtime.h>
@@ -18,7 +18,9 @@ namespace w90g {
 
 // kernels (k_fp64.cu)
 __global__ void k_mdiag(const Problem* probs, WorkMap wm);
-__global__ void k_omega(const Problem* probs, int slot);
+__global__ void k_omega_p1(const Problem* probs, WorkMap wm, int slot);
+__global__ void k_omega_p2(const Problem* probs, WorkMap wm, int slot);
+__global__ void k_omega_p3(const Problem* probs, int slot);
 __global__ void k_grad(const Problem* probs, WorkMap wm);
 __global__ void k_ctrl_search(const Problem* probs);
 __global__ void k_exp_u(const Problem* probs, WorkMap wm, int which);
@@ -106,14 +108,14 @@ int Engine::alloc(std::string& err) {
   if (!own_stream_) W90G_CHECK(cudaStreamCreateWithFlags(&own_stream_, cudaStreamNonBlocking));
   // sizes
   struct Sizes {
-    size_t M, U, KWW, work, tbuf, diag, offd, gpart, cen, log, logc, nn, bk, wb, st;
+    size_t M, U, KWW, work, tbuf, diag, offd, gpart, cen, log, logc, nn, bk, wb, st, op1, op2;
   };
   std::vector<Sizes> sz(np);
   size_t total = 0;
   n_k_ = n_kb_ = n_grad_ = 0;
   maxW_small_ = 0;
   max_iter_ = 0;
-  std::vector<int> offs_k(np + 1, 0), offs_kb(np + 1, 0), offs_grad(np + 1, 0);
+  std::vector<int> offs_k(np + 1, 0), offs_kb(np + 1, 0), offs_grad(np + 1, 0), offs_chunk(np + 1, 0);
   for (int p = 0; p < np; ++p) {
     const auto& s = specs_[p];
     const size_t W = s.W, K = s.K, B = s.B;
@@ -135,18 +137,23 @@ int Engine::alloc(std::string& err) {
     z.bk = align_up(K * B * 3 * 8);
     z.wb = align_up(B * 8);
     z.st = align_up(sizeof(CtrlState));
+    const size_t nch = (K * B + 63) / 64;
+    z.op1 = align_up(nch * (4 * W + 2) * 8);
+    z.op2 = align_up(nch * 8);
     total += 2 * z.M + 2 * z.U + 3 * z.KWW + z.work + z.tbuf + 2 * z.diag + z.offd + z.gpart + z.cen +
-             z.log + z.logc + z.nn + z.bk + z.wb + z.st;
+             z.log + z.logc + z.nn + z.bk + z.wb + z.st + z.op1 + z.op2;
     offs_k[p + 1] = offs_k[p] + s.K;
     offs_kb[p + 1] = offs_kb[p] + s.K * s.B;
     offs_grad[p + 1] = offs_grad[p] + s.K * nt * nt;
+    offs_chunk[p + 1] = offs_chunk[p] + (s.K * s.B + 63) / 64;
     if (s.W <= 32) maxW_small_ = std::max(maxW_small_, s.W);
     max_iter_ = std::max(max_iter_, s.ctl.num_iter);
   }
   n_k_ = offs_k[np];
   n_kb_ = offs_kb[np];
   n_grad_ = offs_grad[np];
-  const size_t hdr = align_up(np * sizeof(Problem)) + 3 * align_up((np + 1) * sizeof(int)) +
+  n_chunk_ = offs_chunk[np];
+  const size_t hdr = align_up(np * sizeof(Problem)) + 4 * align_up((np + 1) * sizeof(int)) +
                      align_up(n_k_ * sizeof(int)) + align_up(n_k_ * sizeof(double)) + align_up(sizeof(int));
   total += hdr;
   W90G_CHECK(cudaMalloc(&arena_, total));
@@ -161,6 +168,7 @@ int Engine::alloc(std::string& err) {
   d_offs_k_ = (int*)take(align_up((np + 1) * sizeof(int)));
   d_offs_kb_ = (int*)take(align_up((np + 1) * sizeof(int)));
   d_offs_grad_ = (int*)take(align_up((np + 1) * sizeof(int)));
+  d_offs_chunk_ = (int*)take(align_up((np + 1) * sizeof(int)));
   d_status_ = (int*)take(align_up(n_k_ * sizeof(int)));
   d_unit_ = (double*)take(align_up(n_k_ * sizeof(double)));
   int* d_alldone = (int*)take(align_up(sizeof(int)));
@@ -195,6 +203,9 @@ int Engine::alloc(std::string& err) {
     double* bk = (double*)take(z.bk);
     double* wb = (double*)take(z.wb);
     P.st = (CtrlState*)take(z.st);
+    P.opart1 = (double*)take(z.op1);
+    P.opart2 = (double*)take(z.op2);
+    P.nchunk = (s.K * s.B + 63) / 64;
     P.ctl = s.ctl;
     W90G_CHECK(cudaMemcpy(nn, s.nnlist.data(), s.nnlist.size() * sizeof(int), cudaMemcpyHostToDevice));
     W90G_CHECK(cudaMemcpy(bk, s.bk.data(), s.bk.size() * sizeof(double), cudaMemcpyHostToDevice));
@@ -207,6 +218,7 @@ int Engine::alloc(std::string& err) {
   W90G_CHECK(cudaMemcpy(d_offs_k_, offs_k.data(), (np + 1) * sizeof(int), cudaMemcpyHostToDevice));
   W90G_CHECK(cudaMemcpy(d_offs_kb_, offs_kb.data(), (np + 1) * sizeof(int), cudaMemcpyHostToDevice));
   W90G_CHECK(cudaMemcpy(d_offs_grad_, offs_grad.data(), (np + 1) * sizeof(int), cudaMemcpyHostToDevice));
+  W90G_CHECK(cudaMemcpy(d_offs_chunk_, offs_chunk.data(), (np + 1) * sizeof(int), cudaMemcpyHostToDevice));
   // dynamic shared memory limits of the shared-memory kernels
   const int ws = std::max(maxW_small_, 1);
   W90G_CHECK(cudaFuncSetAttribute(k_exp_u, cudaFuncAttributeMaxDynamicSharedMemorySize, 6 * ws * ws * 16));
@@ -282,6 +294,14 @@ int Engine::project(std::string& err) {
   return 0;
 }
 
+void Engine::launch_omega(cudaStream_t s, int slot) {
+  const int np = nprob();
+  const WorkMap wmc{d_offs_chunk_, np};
+  k_omega_p1<<<n_chunk_, 256, 0, s>>>(dprobs_, wmc, slot);
+  k_omega_p2<<<n_chunk_, 256, 0, s>>>(dprobs_, wmc, slot);
+  k_omega_p3<<<np, 256, 0, s>>>(dprobs_, slot);
+}
+
 void Engine::launch_iteration(cudaStream_t s) {
   const int np = nprob();
   const int ws = std::max(maxW_small_, 1);
@@ -294,11 +314,11 @@ void Engine::launch_iteration(cudaStream_t s) {
   k_ctrl_search<<<np, 256, 0, s>>>(dprobs_);
   k_exp_u<<<n_k_, 256, sm_exp, s>>>(dprobs_, wmk, 0);
   k_m_update<<<n_kb_, 256, sm_mu, s>>>(dprobs_, wmkb, 0, 0);
-  k_omega<<<np, 512, 0, s>>>(dprobs_, 0);
+  launch_omega(s, 0);
   k_ctrl_step<<<(np + 127) / 128, 128, 0, s>>>(dprobs_, np);
   k_exp_u<<<n_k_, 256, sm_exp, s>>>(dprobs_, wmk, 1);
   k_m_update<<<n_kb_, 256, sm_mu, s>>>(dprobs_, wmkb, 0, 1);
-  k_omega<<<np, 512, 0, s>>>(dprobs_, 1);
+  launch_omega(s, 1);
   k_ctrl_end<<<np, 128, 0, s>>>(dprobs_);
 }
 
@@ -311,10 +331,10 @@ int Engine::wannierise(std::string& err) {
   const WorkMap wmk{d_offs_k_, np};
   // initial spread (src/wannierise.F90:452-470)
   k_mdiag<<<n_kb_, 128, 0, st>>>(dprobs_, wmkb);
-  k_omega<<<np, 512, 0, st>>>(dprobs_, 2);
+  launch_omega(st, 2);
   k_log_init<<<np, 128, 0, st>>>(dprobs_);
   W90G_CHECK(cudaGetLastError());
-  launches_ += 3;
+  launches_ += 5;
   // capture one iteration into a graph (re-captured when the stream changes)
   if (!graph_exec_) {
     if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
@@ -339,7 +359,7 @@ int Engine::wannierise(std::string& err) {
   while (done_iters < max_iter_) {
     const int n = std::min(chunk, max_iter_ - done_iters);
     for (int i = 0; i < n; ++i) W90G_CHECK(cudaGraphLaunch(graph_exec_, st));
-    launches_ += 10LL * n;
+    launches_ += 14LL * n;
     done_iters += n;
     if (any_window && done_iters < max_iter_) {
       k_all_done<<<1, 256, 0, st>>>(dprobs_, np, d_alldone);
@@ -435,7 +455,7 @@ int Engine::wannierise_profiled(int max_iters, double* ms, int* cnt, std::string
   int rc = 0;
   rc |= timed(kPInit, [&] {
     k_mdiag<<<n_kb_, 128, 0, st>>>(dprobs_, wmkb);
-    k_omega<<<np, 512, 0, st>>>(dprobs_, 2);
+    launch_omega(st, 2);
     k_log_init<<<np, 128, 0, st>>>(dprobs_);
   });
   CtrlState hs;
@@ -445,13 +465,13 @@ int Engine::wannierise_profiled(int max_iters, double* ms, int* cnt, std::string
     rc |= timed(kPCtrlSearch, [&] { k_ctrl_search<<<np, 256, 0, st>>>(dprobs_); });
     rc |= timed(kPExpU, [&] { k_exp_u<<<n_k_, 256, sm_exp, st>>>(dprobs_, wmk, 0); });
     rc |= timed(kPMUpdate, [&] { k_m_update<<<n_kb_, 256, sm_mu, st>>>(dprobs_, wmkb, 0, 0); });
-    rc |= timed(kPOmega, [&] { k_omega<<<np, 512, 0, st>>>(dprobs_, 0); });
+    rc |= timed(kPOmega, [&] { launch_omega(st, 0); });
     rc |= timed(kPCtrlStep, [&] { k_ctrl_step<<<(np + 127) / 128, 128, 0, st>>>(dprobs_, np); });
     W90G_CHECK(cudaMemcpy(&hs, hprobs_[0].st, sizeof(CtrlState), cudaMemcpyDeviceToHost));
     if (hs.do_second) {
       rc |= timed(kPExpU, [&] { k_exp_u<<<n_k_, 256, sm_exp, st>>>(dprobs_, wmk, 1); });
       rc |= timed(kPMUpdate, [&] { k_m_update<<<n_kb_, 256, sm_mu, st>>>(dprobs_, wmkb, 0, 1); });
-      rc |= timed(kPOmega, [&] { k_omega<<<np, 512, 0, st>>>(dprobs_, 1); });
+      rc |= timed(kPOmega, [&] { launch_omega(st, 1); });
     }
     rc |= timed(kPCtrlEnd, [&] { k_ctrl_end<<<np, 128, 0, st>>>(dprobs_); });
     W90G_CHECK(cudaMemcpy(&hs, hprobs_[0].st, sizeof(CtrlState), cudaMemcpyDeviceToHost));

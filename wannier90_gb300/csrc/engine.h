@@ -68,6 +68,7 @@ class Engine {
   int alloc(std::string& err);
   void release();
   void launch_iteration(cudaStream_t s);
+  void launch_omega(cudaStream_t s, int slot);
   int init_states(std::string& err);
 
   std::vector<ProblemSpec> specs_;
@@ -79,9 +80,10 @@ class Engine {
   int* d_offs_k_ = nullptr;
   int* d_offs_kb_ = nullptr;
   int* d_offs_grad_ = nullptr;
+  int* d_offs_chunk_ = nullptr;
   int* d_status_ = nullptr;
   double* d_unit_ = nullptr;
-  int n_k_ = 0, n_kb_ = 0, n_grad_ = 0;
+  int n_k_ = 0, n_kb_ = 0, n_grad_ = 0, n_chunk_ = 0;
   int maxW_small_ = 0;   // largest W <= 32 in the batch (shared-memory kernels)
   int max_iter_ = 0;
   cudaStream_t own_stream_ = nullptr;

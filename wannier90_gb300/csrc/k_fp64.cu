@@ -1,8 +1,9 @@
 // FP64 kernels of the GB300 MLWF engine (the plain FP64 path).
 //
 // One iteration of wann_main (src/wannierise.F90:534-816) is the fixed launch sequence
-//   k_grad -> k_ctrl_search -> k_exp_u(0) -> k_m_update(0) -> k_omega(0) -> k_ctrl_step
-//   -> k_exp_u(1) -> k_m_update(1) -> k_omega(1) -> k_ctrl_end
+//   k_grad -> k_ctrl_search -> k_exp_u(0) -> k_m_update(0) -> spread(0) -> k_ctrl_step
+//   -> k_exp_u(1) -> k_m_update(1) -> spread(1) -> k_ctrl_end
+// where spread(slot) = k_omega_p1 -> k_omega_p2 -> k_omega_p3.
 // All data-dependent decisions of the reference (CG reset, uphill reversal, parabolic
 // line search, convergence) are taken on the device by the k_ctrl_* kernels, so the
 // sequence never needs the host and can be replayed (or graph-captured) blindly:
@@ -122,33 +123,44 @@ __global__ void k_mdiag(const Problem* __restrict__ probs, WorkMap wm) {
 }
 
 // ----------------------------------------------------------------------------
-// k_omega: wann_omega (src/wannierise.F90:1979-2284), non-SLWF branch.
-// One CTA (512 threads) per problem.  slot: 0 trial, 1 optimal step, 2 initial.
-// Deterministic: fixed (n, chunk) ownership and fixed-order tree reductions.
+// wann_omega (src/wannierise.F90:1979-2284), non-SLWF branch, as a deterministic
+// three-pass reduction over chunks of kOmegaChunk (k,b) blocks:
+//   p1: per chunk  P_n = sum wb b ln_n (3W), q_n = sum wb (1 - |M_nn|^2 + ln_n^2) (W),
+//       sum wb offd, and (first pass only) sum wb (W - sum|M|^2)
+//   p2: rave = -(1/K) sum_chunks P (same fixed order in every CTA), then the chunk's
+//       part of sum wb (ln_n + b.rave_n)^2
+//   p3: one CTA per problem: totals, centres, spreads, Omega terms.
+// slot: 0 trial, 1 optimal step, 2 initial (accepted).  Fixed thread ownership and
+// fixed-order reductions make the result independent of scheduling.
 // ----------------------------------------------------------------------------
-constexpr int kOmegaThreads = 512;
+constexpr int kOmegaChunk = 64;
 
-__global__ void __launch_bounds__(kOmegaThreads) k_omega(const Problem* __restrict__ probs, int slot) {
-  __shared__ double red[kOmegaThreads];
-  __shared__ double s_rave[3 * 512];
-  const Problem& P = probs[blockIdx.x];
-  CtrlState* st = P.st;
+__device__ __forceinline__ bool omega_skip(const CtrlState* st, int slot) {
   if (slot < 2) {
-    if (st->done) return;
-    if (slot == 1 && !st->do_second) return;
+    if (st->done) return true;
+    if (slot == 1 && !st->do_second) return true;
   }
-  const int W = P.W, K = P.K, B = P.B;
-  const int KB = K * B;
+  return false;
+}
+
+__global__ void __launch_bounds__(256) k_omega_p1(const Problem* __restrict__ probs, WorkMap wm, int slot) {
+  __shared__ double red[256];
+  int ch;
+  const int p = locate(wm, blockIdx.x, ch);
+  const Problem& P = probs[p];
+  const CtrlState* st = P.st;
+  if (omega_skip(st, slot)) return;
+  const int W = P.W, B = P.B;
+  const int KB = P.K * B;
+  const int kb0 = ch * kOmegaChunk, kb1 = min(KB, kb0 + kOmegaChunk);
   const int t = threadIdx.x;
-  // thread (n, chunk) ownership; W <= 512 so at least one chunk of 512 threads
-  const int nch = kOmegaThreads / W;   // chunks
-  const int n = t % W, ch = t / W;
-  const bool act = ch < nch;
+  const int nsub = blockDim.x / W;           // W <= 256
+  const int n = t % W, sub = t / W;
+  const bool act = sub < nsub;
   double r0 = 0, r1 = 0, r2 = 0, q = 0;
   if (act) {
-    for (int kb = ch; kb < KB; kb += nch) {
-      const int b = kb % B;
-      const double w = P.wb[b];
+    for (int kb = kb0 + sub; kb < kb1; kb += nsub) {
+      const double w = P.wb[kb % B];
       const double l = P.diag_ln[(size_t)kb * W + n];
       const double a = P.diag_abs2[(size_t)kb * W + n];
       const double* bv = P.bk + (size_t)kb * 3;
@@ -159,25 +171,21 @@ __global__ void __launch_bounds__(kOmegaThreads) k_omega(const Problem* __restri
       q += w * (1.0 - a + l * l);
     }
   }
-  // reduce over chunks for each n: red layout [ch][n]
-  double* rv = s_rave;  // rave(3, n) stored as s_rave[i*W+n]
-  double vals[4] = {r0, r1, r2, q};
-  double r2ave_n = 0.0;
+  double* out = P.opart1 + (size_t)ch * (4 * W + 2);
+  const double vals[4] = {r0, r1, r2, q};
   for (int c = 0; c < 4; ++c) {
     red[t] = act ? vals[c] : 0.0;
     __syncthreads();
     if (t < W) {
-      double s = 0.0;
-      for (int cc = 0; cc < nch; ++cc) s += red[cc * W + t];
-      if (c < 3) rv[c * W + t] = -s / (double)K;
-      else r2ave_n = s / (double)K;
+      double sacc = 0.0;
+      for (int u = 0; u < nsub; ++u) sacc += red[u * W + t];
+      out[c * W + t] = sacc;
     }
     __syncthreads();
   }
-  // scalar sums over (k,b): Omega_OD and first-pass Omega_I
-  double od = 0.0, oi = 0.0;
   const bool first = (slot == 2) && st->first_pass;
-  for (int kb = t; kb < KB; kb += kOmegaThreads) {
+  double od = 0.0, oi = 0.0;
+  for (int kb = kb0 + t; kb < kb1; kb += blockDim.x) {
     const double w = P.wb[kb % B];
     const double o = P.offd[kb];
     od += w * o;
@@ -187,57 +195,106 @@ __global__ void __launch_bounds__(kOmegaThreads) k_omega(const Problem* __restri
       oi += w * ((double)W - (o + sd));
     }
   }
-  od = block_sum(od, red) / (double)K;
-  if (first) oi = block_sum(oi, red) / (double)K;
-  // Omega_D = (1/K) sum wb (ln + b.rave_n)^2   (second pass, needs rave)
+  od = block_sum(od, red);
+  oi = block_sum(oi, red);
+  if (t == 0) {
+    out[4 * W] = od;
+    out[4 * W + 1] = oi;
+  }
+}
+
+// rave(3,W) from the pass-1 partials, summed over chunks in index order
+__device__ void omega_rave(const Problem& P, double* s_rave) {
+  const int W = P.W;
+  const int stride = 4 * W + 2;
+  for (int i = threadIdx.x; i < 3 * W; i += blockDim.x) {
+    double sacc = 0.0;
+    for (int c = 0; c < P.nchunk; ++c) sacc += P.opart1[(size_t)c * stride + i];
+    s_rave[i] = -sacc / (double)P.K;
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(256) k_omega_p2(const Problem* __restrict__ probs, WorkMap wm, int slot) {
+  __shared__ double red[256];
+  __shared__ double s_rave[3 * 256];
+  int ch;
+  const int p = locate(wm, blockIdx.x, ch);
+  const Problem& P = probs[p];
+  if (omega_skip(P.st, slot)) return;
+  omega_rave(P, s_rave);
+  const int W = P.W, B = P.B;
+  const int KB = P.K * B;
+  const int kb0 = ch * kOmegaChunk, kb1 = min(KB, kb0 + kOmegaChunk);
+  const int t = threadIdx.x;
+  const int nsub = blockDim.x / W;
+  const int n = t % W, sub = t / W;
   double dd = 0.0;
-  if (act) {
-    const double x0 = rv[n], x1 = rv[W + n], x2 = rv[2 * W + n];
-    for (int kb = ch; kb < KB; kb += nch) {
+  if (sub < nsub) {
+    const double x0 = s_rave[n], x1 = s_rave[W + n], x2 = s_rave[2 * W + n];
+    for (int kb = kb0 + sub; kb < kb1; kb += nsub) {
       const double w = P.wb[kb % B];
       const double* bv = P.bk + (size_t)kb * 3;
-      const double brn = bv[0] * x0 + bv[1] * x1 + bv[2] * x2;
-      const double l = P.diag_ln[(size_t)kb * W + n] + brn;
+      const double l = P.diag_ln[(size_t)kb * W + n] + (bv[0] * x0 + bv[1] * x1 + bv[2] * x2);
       dd = fma(w * l, l, dd);
     }
   }
-  dd = block_sum(dd, red) / (double)K;
-  // outputs
+  dd = block_sum(dd, red);
+  if (t == 0) P.opart2[ch] = dd;
+}
+
+__global__ void __launch_bounds__(256) k_omega_p3(const Problem* __restrict__ probs, int slot) {
+  __shared__ double red[256];
+  __shared__ double s_rave[3 * 256];
+  const Problem& P = probs[blockIdx.x];
+  CtrlState* st = P.st;
+  if (omega_skip(st, slot)) return;
+  omega_rave(P, s_rave);
+  const int W = P.W, K = P.K;
+  const int stride = 4 * W + 2;
+  const int t = threadIdx.x;
   double* cen = P.centres + (size_t)slot * 4 * W;
-  if (t < W) {
-    const double x0 = rv[t], x1 = rv[W + t], x2 = rv[2 * W + t];
-    cen[t] = x0;
-    cen[W + t] = x1;
-    cen[2 * W + t] = x2;
-    cen[3 * W + t] = r2ave_n - (x0 * x0 + x1 * x1 + x2 * x2);
+  for (int i = t; i < W; i += blockDim.x) {
+    double q = 0.0;
+    for (int c = 0; c < P.nchunk; ++c) q += P.opart1[(size_t)c * stride + 3 * W + i];
+    const double x0 = s_rave[i], x1 = s_rave[W + i], x2 = s_rave[2 * W + i];
+    cen[i] = x0;
+    cen[W + i] = x1;
+    cen[2 * W + i] = x2;
+    cen[3 * W + i] = q / (double)K - (x0 * x0 + x1 * x1 + x2 * x2);
   }
+  double od = 0.0, oi = 0.0, dd = 0.0;
   if (t == 0) {
+    for (int c = 0; c < P.nchunk; ++c) {
+      od += P.opart1[(size_t)c * stride + 4 * W];
+      oi += P.opart1[(size_t)c * stride + 4 * W + 1];
+      dd += P.opart2[c];
+    }
+    const bool first = (slot == 2) && st->first_pass;
     if (first) {
-      st->om_invariant = oi;
+      st->om_invariant = oi / (double)K;
       st->first_pass = 0;
     }
-    Spread s;
-    s.om_i = st->om_invariant;
-    s.om_d = dd;
-    s.om_od = od;
-    s.om_tot = s.om_i + s.om_d + s.om_od;
-    if (slot == 2) {
-      st->wann = s;
-    } else {
-      st->slot[slot] = s;
-    }
-    if (!isfinite(s.om_tot)) {
+    Spread sp;
+    sp.om_i = st->om_invariant;
+    sp.om_d = dd / (double)K;
+    sp.om_od = od / (double)K;
+    sp.om_tot = sp.om_i + sp.om_d + sp.om_od;
+    if (slot == 2) st->wann = sp;
+    else st->slot[slot] = sp;
+    if (!isfinite(sp.om_tot)) {
       st->error = 1;
       st->done = 1;
     }
   }
+  (void)red;
 }
 
 // ----------------------------------------------------------------------------
 // k_grad: wann_domega (src/wannierise.F90:2287-2569), non-SLWF branch, fused with the
 // per-k partial dot products of internal_search_direction (:1424-1431).
 // grid: one CTA per (problem, k, tile_i, tile_j) of 32x32 tiles; 256 threads.
-// rave is the one computed by the preceding k_omega on the same M (the reference
+// rave is the one computed by the preceding spread pass on the same M (the reference
 // recomputes it from the same data, :2378-2393).
 // ----------------------------------------------------------------------------
 constexpr int kTile = 32;
@@ -566,7 +623,7 @@ __global__ void __launch_bounds__(256) k_exp_u(const Problem* __restrict__ probs
 // k_m_update: M(k,b) <- dU(k)^H M(k,b) dU(nnlist(k,b))   (src/wannierise.F90:1736-1748)
 // mode 0: step update, reads M[cur], writes M[cur^1] (which selects trial/optimal pass)
 // mode 1: projection (src/overlap.F90:909-923): rotation U[cur], in place on M[cur].
-// Epilogue: block statistics for k_omega.  One CTA (256 threads) per (problem, k*B+b).
+// Epilogue: block statistics for the spread passes.  One CTA (256 threads) per (problem, k*B+b).
 // ----------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_m_update(const Problem* __restrict__ probs, WorkMap wm,
                                                   int mode, int which) {

@@ -121,6 +121,10 @@ struct Problem {
   double* centres;      // [slot][4][W]: rave(3,W) + r2ave-rave2 (W) per spread slot; slot 2 = accepted
   double* log;          // [num_iter+1][kLogStride]
   double* log_centres;  // [num_iter+1][4][W]
+  double* opart1;       // [nchunk][4W+2] spread partials (pass 1)
+  double* opart2;       // [nchunk]       Omega_D partials (pass 2)
+  int nchunk;           // ceil(K*B / 64)
+  int pad3;
   CtrlState* st;
   Control ctl;
   int max_exp_squarings;
