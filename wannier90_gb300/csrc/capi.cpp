@@ -48,6 +48,7 @@ struct Handle {
   int iprint = 1, num_print_cycles = 1, timing_level = 1;
   int search_shells = 36;
   double kmesh_tol = 1.0e-6;
+  int gpu_tensor = 0;   // M update on tensor cores (W <= 32)
   KmeshInfo km;
   // caller data
   double* m_local = nullptr;
@@ -203,6 +204,7 @@ int build_spec(Handle* h, ProblemSpec& s) {
   s.bk = h->km.bk;
   s.wb = h->km.wb;
   s.ctl = h->ctl;
+  s.tensor = h->gpu_tensor;
   return 0;
 }
 
@@ -377,6 +379,8 @@ void cinput_setopt(void* hv, const char* seedname, int* ierr, int comm) {
   h->timing_level = get_num(h, "timing_level", v) ? (int)v : 1;
   h->search_shells = get_num(h, "search_shells", v) ? (int)v : 36;
   h->kmesh_tol = get_num(h, "kmesh_tol", v) ? v : 1.0e-6;
+  // engine key: gpu_tensor = 1 computes M(k,b) = U^H M0 U' on tensor cores (W <= 32)
+  h->gpu_tensor = get_num(h, "gpu_tensor", v) ? (int)v : 0;
   // options on wann_main's code path that the engine does not implement
   const char* unsupported[] = {"precond", "guiding_centres", "slwf_num", "slwf_constrain", "site_symmetry",
                                "gamma_only"};

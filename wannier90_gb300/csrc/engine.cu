@@ -32,6 +32,12 @@ __global__ void k_lowdin(const Problem* probs, WorkMap wm, int* status);
 __global__ void k_unitarity(const Problem* probs, WorkMap wm, double* out);
 __global__ void k_all_done(const Problem* probs, int nprob, int* out);
 __global__ void k_fp64_peak(double* out, int iters, double seed);
+__global__ void k_u_final(const Problem* probs, WorkMap wm);
+__global__ void k_u_identity(const Problem* probs, WorkMap wm);
+__global__ void k_frob0(const Problem* probs, WorkMap wm);
+cudaError_t oz_launch(int wp, int step, const Problem* probs, WorkMap wm, int which, int grid,
+                      cudaStream_t s);
+cudaError_t oz_set_attributes(int wp);
 
 const char* kProfNames[kPNum] = {"k_grad", "k_ctrl_search", "k_exp_u", "k_m_update",
                                  "k_omega", "k_ctrl_step", "k_ctrl_end", "init"};
@@ -82,7 +88,7 @@ int Engine::setup(const std::vector<ProblemSpec>& specs, std::string& err) {
   }
   // layout key: reuse the arena when the problem shapes are unchanged
   std::ostringstream key;
-  for (const auto& s : specs) key << s.W << ',' << s.K << ',' << s.B << ',' << s.ctl.num_iter << ';';
+  for (const auto& s : specs) key << s.W << ',' << s.K << ',' << s.B << ',' << s.ctl.num_iter << ',' << s.tensor << ';';
   specs_ = specs;
   if (arena_ && key.str() == layout_key_) {
     // refresh the read-only tables (they may differ at equal shapes)
@@ -105,10 +111,26 @@ int Engine::setup(const std::vector<ProblemSpec>& specs, std::string& err) {
 
 int Engine::alloc(std::string& err) {
   const int np = (int)specs_.size();
+  // tensor-core M update: every problem asks for it, W <= 32, and every k' has exactly
+  // B predecessors (k,b) (true on Monkhorst-Pack meshes)
+  tensor_wp_ = 0;
+  {
+    bool ok = np > 0;
+    int wmax = 0;
+    for (const auto& s : specs_) {
+      ok = ok && s.tensor && s.W <= 32;
+      wmax = std::max(wmax, s.W);
+      if (!ok) break;
+      std::vector<int> cnt(s.K, 0);
+      for (int v : s.nnlist) cnt[v]++;
+      for (int c : cnt) ok = ok && (c == s.B);
+    }
+    if (ok) tensor_wp_ = wmax <= 8 ? 8 : (wmax <= 16 ? 16 : 32);
+  }
   if (!own_stream_) W90G_CHECK(cudaStreamCreateWithFlags(&own_stream_, cudaStreamNonBlocking));
   // sizes
   struct Sizes {
-    size_t M, U, KWW, work, tbuf, diag, offd, gpart, cen, log, logc, nn, bk, wb, st, op1, op2;
+    size_t M, U, KWW, work, tbuf, diag, offd, gpart, cen, log, logc, nn, bk, wb, st, op1, op2, m0, u0, inv, fr;
   };
   std::vector<Sizes> sz(np);
   size_t total = 0;
@@ -126,7 +148,11 @@ int Engine::alloc(std::string& err) {
     z.U = align_up(K * WW * 16);
     z.KWW = align_up(K * WW * 16);
     z.work = s.W > 32 ? align_up(K * 6 * WW * 16) : 0;
-    z.tbuf = s.W > 32 ? align_up(K * B * WW * 16) : 0;
+    z.tbuf = (s.W > 32 || tensor_wp_) ? align_up(K * B * WW * 16) : 0;
+    z.m0 = tensor_wp_ ? align_up(K * B * WW * 16) : 0;
+    z.u0 = tensor_wp_ ? align_up(K * WW * 16) : 0;
+    z.inv = tensor_wp_ ? align_up(K * B * 4) : 0;
+    z.fr = tensor_wp_ ? align_up(K * B * 8) : 0;
     z.diag = align_up(K * B * W * 8);
     z.offd = align_up(K * B * 8);
     z.gpart = align_up(K * nt * nt * 2 * 8);
@@ -141,7 +167,7 @@ int Engine::alloc(std::string& err) {
     z.op1 = align_up(nch * (4 * W + 2) * 8);
     z.op2 = align_up(nch * 8);
     total += 2 * z.M + 2 * z.U + 3 * z.KWW + z.work + z.tbuf + 2 * z.diag + z.offd + z.gpart + z.cen +
-             z.log + z.logc + z.nn + z.bk + z.wb + z.st + z.op1 + z.op2;
+             z.log + z.logc + z.nn + z.bk + z.wb + z.st + z.op1 + z.op2 + z.m0 + z.u0 + z.inv + z.fr;
     offs_k[p + 1] = offs_k[p] + s.K;
     offs_kb[p + 1] = offs_kb[p] + s.K * s.B;
     offs_grad[p + 1] = offs_grad[p] + s.K * nt * nt;
@@ -203,6 +229,20 @@ int Engine::alloc(std::string& err) {
     double* bk = (double*)take(z.bk);
     double* wb = (double*)take(z.wb);
     P.st = (CtrlState*)take(z.st);
+    P.M0 = z.m0 ? (double2*)take(z.m0) : nullptr;
+    P.U0 = z.u0 ? (double2*)take(z.u0) : nullptr;
+    int* inv = z.inv ? (int*)take(z.inv) : nullptr;
+    P.inv_nnlist = inv;
+    P.tensor = tensor_wp_ ? 1 : 0;
+    P.frob0 = z.fr ? (double*)take(z.fr) : nullptr;
+    if (inv) {
+      std::vector<int> h_inv((size_t)s.K * s.B), fill(s.K, 0);
+      for (int kb = 0; kb < s.K * s.B; ++kb) {
+        const int k2 = s.nnlist[kb];
+        h_inv[(size_t)k2 * s.B + fill[k2]++] = kb;
+      }
+      W90G_CHECK(cudaMemcpy(inv, h_inv.data(), h_inv.size() * sizeof(int), cudaMemcpyHostToDevice));
+    }
     P.opart1 = (double*)take(z.op1);
     P.opart2 = (double*)take(z.op2);
     P.nchunk = (s.K * s.B + 63) / 64;
@@ -222,8 +262,10 @@ int Engine::alloc(std::string& err) {
   // dynamic shared memory limits of the shared-memory kernels
   const int ws = std::max(maxW_small_, 1);
   W90G_CHECK(cudaFuncSetAttribute(k_exp_u, cudaFuncAttributeMaxDynamicSharedMemorySize, 6 * ws * ws * 16));
+  W90G_CHECK(cudaFuncSetAttribute(k_u_final, cudaFuncAttributeMaxDynamicSharedMemorySize, 3 * ws * ws * 16));
   W90G_CHECK(cudaFuncSetAttribute(k_m_update, cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * ws * ws * 16));
   W90G_CHECK(cudaFuncSetAttribute(k_lowdin, cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * ws * ws * 16));
+  if (tensor_wp_) W90G_CHECK(oz_set_attributes(tensor_wp_));
   return 0;
 }
 
@@ -302,6 +344,38 @@ void Engine::launch_omega(cudaStream_t s, int slot) {
   k_omega_p3<<<np, 256, 0, s>>>(dprobs_, slot);
 }
 
+// tensor path: keep the entry M and U, iterate on R = U0^H U starting from identity
+int Engine::prepare_tensor(cudaStream_t st, std::string& err) {
+  if (!tensor_wp_) return 0;
+  for (int p = 0; p < nprob(); ++p) {
+    const auto& s = specs_[p];
+    const size_t WW = (size_t)s.W * s.W;
+    W90G_CHECK(cudaMemcpyAsync(hprobs_[p].M0, hprobs_[p].M[0], (size_t)s.K * s.B * WW * 16,
+                               cudaMemcpyDeviceToDevice, st));
+    W90G_CHECK(cudaMemcpyAsync(hprobs_[p].U0, hprobs_[p].U[0], (size_t)s.K * WW * 16, cudaMemcpyDeviceToDevice, st));
+  }
+  const WorkMap wmk{d_offs_k_, nprob()};
+  const WorkMap wmkb{d_offs_kb_, nprob()};
+  k_u_identity<<<n_k_, 256, 0, st>>>(dprobs_, wmk);
+  k_frob0<<<n_kb_, 128, 0, st>>>(dprobs_, wmkb);
+  W90G_CHECK(cudaGetLastError());
+  launches_ += 2;
+  return 0;
+}
+
+void Engine::launch_mupdate(cudaStream_t s, int which) {
+  const int np = nprob();
+  const WorkMap wmk{d_offs_k_, np};
+  const WorkMap wmkb{d_offs_kb_, np};
+  if (tensor_wp_) {
+    oz_launch(tensor_wp_, 1, dprobs_, wmk, which, n_k_, s);
+    oz_launch(tensor_wp_, 2, dprobs_, wmk, which, n_k_, s);
+  } else {
+    const int ws = std::max(maxW_small_, 1);
+    k_m_update<<<n_kb_, 256, (size_t)4 * ws * ws * 16, s>>>(dprobs_, wmkb, 0, which);
+  }
+}
+
 void Engine::launch_iteration(cudaStream_t s) {
   const int np = nprob();
   const int ws = std::max(maxW_small_, 1);
@@ -313,11 +387,11 @@ void Engine::launch_iteration(cudaStream_t s) {
   k_grad<<<n_grad_, 256, 0, s>>>(dprobs_, wmg);
   k_ctrl_search<<<np, 256, 0, s>>>(dprobs_);
   k_exp_u<<<n_k_, 256, sm_exp, s>>>(dprobs_, wmk, 0);
-  k_m_update<<<n_kb_, 256, sm_mu, s>>>(dprobs_, wmkb, 0, 0);
+  launch_mupdate(s, 0);
   launch_omega(s, 0);
   k_ctrl_step<<<(np + 127) / 128, 128, 0, s>>>(dprobs_, np);
   k_exp_u<<<n_k_, 256, sm_exp, s>>>(dprobs_, wmk, 1);
-  k_m_update<<<n_kb_, 256, sm_mu, s>>>(dprobs_, wmkb, 0, 1);
+  launch_mupdate(s, 1);
   launch_omega(s, 1);
   k_ctrl_end<<<np, 128, 0, s>>>(dprobs_);
 }
@@ -329,6 +403,7 @@ int Engine::wannierise(std::string& err) {
   if (init_states(err)) return 1;
   const WorkMap wmkb{d_offs_kb_, np};
   const WorkMap wmk{d_offs_k_, np};
+  if (int rc0 = prepare_tensor(st, err)) return rc0;
   // initial spread (src/wannierise.F90:452-470)
   k_mdiag<<<n_kb_, 128, 0, st>>>(dprobs_, wmkb);
   launch_omega(st, 2);
@@ -369,6 +444,11 @@ int Engine::wannierise(std::string& err) {
       if (hdone) break;
       chunk = std::min(chunk * 2, 32);
     }
+  }
+  if (tensor_wp_) {
+    const int ws = std::max(maxW_small_, 1);
+    k_u_final<<<n_k_, 256, (size_t)3 * ws * ws * 16, st>>>(dprobs_, wmk);
+    launches_ += 1;
   }
   // final unitarity check (src/wannierise.F90:890-892)
   k_unitarity<<<n_k_, 128, 0, st>>>(dprobs_, wmk, d_unit_);
@@ -426,6 +506,7 @@ int Engine::wannierise_profiled(int max_iters, double* ms, int* cnt, std::string
   launches_ = 0;
   const int np = nprob();
   if (int rc0 = init_states(err)) return rc0;
+  if (int rc0 = prepare_tensor(st, err)) return rc0;
   for (int i = 0; i < kPNum; ++i) {
     ms[i] = 0.0;
     cnt[i] = 0;
@@ -464,13 +545,13 @@ int Engine::wannierise_profiled(int max_iters, double* ms, int* cnt, std::string
     rc |= timed(kPGrad, [&] { k_grad<<<n_grad_, 256, 0, st>>>(dprobs_, wmg); });
     rc |= timed(kPCtrlSearch, [&] { k_ctrl_search<<<np, 256, 0, st>>>(dprobs_); });
     rc |= timed(kPExpU, [&] { k_exp_u<<<n_k_, 256, sm_exp, st>>>(dprobs_, wmk, 0); });
-    rc |= timed(kPMUpdate, [&] { k_m_update<<<n_kb_, 256, sm_mu, st>>>(dprobs_, wmkb, 0, 0); });
+    rc |= timed(kPMUpdate, [&] { launch_mupdate(st, 0); });
     rc |= timed(kPOmega, [&] { launch_omega(st, 0); });
     rc |= timed(kPCtrlStep, [&] { k_ctrl_step<<<(np + 127) / 128, 128, 0, st>>>(dprobs_, np); });
     W90G_CHECK(cudaMemcpy(&hs, hprobs_[0].st, sizeof(CtrlState), cudaMemcpyDeviceToHost));
     if (hs.do_second) {
       rc |= timed(kPExpU, [&] { k_exp_u<<<n_k_, 256, sm_exp, st>>>(dprobs_, wmk, 1); });
-      rc |= timed(kPMUpdate, [&] { k_m_update<<<n_kb_, 256, sm_mu, st>>>(dprobs_, wmkb, 0, 1); });
+      rc |= timed(kPMUpdate, [&] { launch_mupdate(st, 1); });
       rc |= timed(kPOmega, [&] { launch_omega(st, 1); });
     }
     rc |= timed(kPCtrlEnd, [&] { k_ctrl_end<<<np, 128, 0, st>>>(dprobs_); });

@@ -17,6 +17,7 @@ struct ProblemSpec {
   std::vector<double> bk;    // [k][b][3]
   std::vector<double> wb;    // [b]
   Control ctl{};
+  int tensor = 0;            // request the tensor-core M update (W <= 32)
 };
 
 struct ProblemResult {
@@ -69,6 +70,8 @@ class Engine {
   void release();
   void launch_iteration(cudaStream_t s);
   void launch_omega(cudaStream_t s, int slot);
+  void launch_mupdate(cudaStream_t s, int which);
+  int prepare_tensor(cudaStream_t st, std::string& err);
   int init_states(std::string& err);
 
   std::vector<ProblemSpec> specs_;
@@ -85,6 +88,7 @@ class Engine {
   double* d_unit_ = nullptr;
   int n_k_ = 0, n_kb_ = 0, n_grad_ = 0, n_chunk_ = 0;
   int maxW_small_ = 0;   // largest W <= 32 in the batch (shared-memory kernels)
+  int tensor_wp_ = 0;    // > 0: tensor M update with padded width 8/16/32 for the whole batch
   int max_iter_ = 0;
   cudaStream_t own_stream_ = nullptr;
   cudaStream_t user_stream_ = nullptr;
@@ -95,5 +99,6 @@ class Engine {
 };
 
 int measure_fp64_peak(double* tflops, std::string& err);
+size_t oz_smem_bytes(int wp);
 
 }  // namespace w90g

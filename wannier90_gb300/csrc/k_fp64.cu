@@ -187,7 +187,16 @@ __global__ void __launch_bounds__(256) k_omega_p1(const Problem* __restrict__ pr
   double od = 0.0, oi = 0.0;
   for (int kb = kb0 + t; kb < kb1; kb += blockDim.x) {
     const double w = P.wb[kb % B];
-    const double o = P.offd[kb];
+    double o;
+    if (P.tensor && slot < 2) {
+      // tensor path: |M(k,b)|_F^2 is invariant under the unitary rotation, so the
+      // off-diagonal sum is |M0(k,b)|_F^2 minus the diagonal (src/wannierise.F90:2214-2258)
+      double sd = 0.0;
+      for (int m = 0; m < W; ++m) sd += P.diag_abs2[(size_t)kb * W + m];
+      o = P.frob0[kb] - sd;
+    } else {
+      o = P.offd[kb];
+    }
     od += w * o;
     if (first) {
       double sd = 0.0;
@@ -1017,6 +1026,57 @@ __global__ void k_fp64_peak(double* __restrict__ out, int iters, double seed) {
 #pragma unroll
   for (int i = 0; i < 8; ++i) s += a[i];
   if (s == 12345.678) out[0] = s;   // keeps the chains live; never true for these inputs
+}
+
+// ----------------------------------------------------------------------------
+// Tensor-path bookkeeping: during the loop U[] holds R = U0^H U (identity at entry),
+// M is always recomputed from the entry overlaps M0; at the end U = U0 R.
+// k_u_identity: U[0](k) = I.   k_u_final: U[cur](k) <- U0(k) U[cur](k).
+// One CTA (256 threads) per (problem, k).
+// ----------------------------------------------------------------------------
+__global__ void k_u_identity(const Problem* __restrict__ probs, WorkMap wm) {
+  int k;
+  const int p = locate(wm, blockIdx.x, k);
+  const Problem& P = probs[p];
+  const int W = P.W;
+  double2* U = P.U[0] + (size_t)k * W * W;
+  for (int e = threadIdx.x; e < W * W; e += blockDim.x) U[e] = cmk((e % W) == (e / W) ? 1.0 : 0.0, 0.0);
+}
+
+__global__ void __launch_bounds__(256) k_u_final(const Problem* __restrict__ probs, WorkMap wm) {
+  extern __shared__ double2 smem[];
+  int k;
+  const int p = locate(wm, blockIdx.x, k);
+  const Problem& P = probs[p];
+  const int W = P.W, WW = W * W;
+  double2* R = P.U[P.st->cur] + (size_t)k * WW;
+  const double2* U0 = P.U0 + (size_t)k * WW;
+  double2* buf = (W <= kSmemW) ? smem : (P.work + (size_t)k * 6 * WW);
+  double2 *sA = buf, *sR = buf + WW, *sC = buf + 2 * WW;
+  for (int e = threadIdx.x; e < WW; e += blockDim.x) {
+    sA[e] = U0[e];
+    sR[e] = R[e];
+  }
+  __syncthreads();
+  cta_gemm<false>(sC, W, sA, W, sR, W, W);
+  __syncthreads();
+  for (int e = threadIdx.x; e < WW; e += blockDim.x) R[e] = sC[e];
+}
+
+// ----------------------------------------------------------------------------
+// k_frob0: |M0(k,b)|_F^2 per block (tensor path, once per solve).  One CTA per (k,b).
+// ----------------------------------------------------------------------------
+__global__ void k_frob0(const Problem* __restrict__ probs, WorkMap wm) {
+  __shared__ double red[128];
+  int kb;
+  const int p = locate(wm, blockIdx.x, kb);
+  const Problem& P = probs[p];
+  const int W = P.W;
+  const double2* Mb = P.M0 + (size_t)kb * W * W;
+  double acc = 0.0;
+  for (int e = threadIdx.x; e < W * W; e += blockDim.x) acc += cabs2(Mb[e]);
+  acc = block_sum(acc, red);
+  if (threadIdx.x == 0) P.frob0[kb] = acc;
 }
 
 }  // namespace w90g

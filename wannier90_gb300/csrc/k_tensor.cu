@@ -1,0 +1,466 @@
+// Tensor-core M update: M(k,b) = U(k)^H M0(k,b) U(k+b) with FP64-level accuracy from
+// BF16 tcgen05 MMAs (Ozaki-style exact slicing).
+//
+// Every complex product is computed through its real embedding
+//     [C_r C_i] = [A_r A_i] [[B_r, B_i], [-B_i, B_r]]      (K = N = 2*WP real)
+// Each operand is scaled per row (A) / per column (B) by a power of two and split into
+// S = 7 signed 7-bit digits (x_1 in [-128,128], x_t in [-64,64] for t > 1), each an exact
+// BF16 value.  For every digit pair (t,u) with t+u <= S+1 the MMA A^(t) B^(u) over the
+// K = 2*WP reduction is exact in the FP32 accumulator (every partial sum is an integer
+// below 2^22), so the pairs of one diagonal d = t+u share one TMEM accumulator.  The
+// epilogue recombines the 7 diagonals exactly in int64 and converts once to FP64.
+// Truncation error: ~2^-49 relative to (row scale x column scale) per product term.
+//
+// The product is batched as tall-skinny GEMMs (B*WP rows sharing one WP x WP operand):
+//   step 1 (group k):  rows (b, n):  Z(k,b)^T = M0(k,b)^T conj(U(k))   -> Z row-major
+//   step 2 (group k'): rows of Z(k,b) for the B pairs with nnlist(k,b) = k':
+//                      M(k,b) = Z(k,b) U(k')  -> M column-major + block statistics
+// One CTA per group; 128-row tiles; operands sliced by all 256 threads into shared
+// memory (canonical K-major, no swizzle); one thread issues the MMAs; warps 0-3 read
+// the accumulators (TMEM lanes = rows).
+#include <cuda_bf16.h>
+
+#include "w90g.cuh"
+
+namespace w90g {
+
+namespace {
+
+constexpr int kS = 7;            // digits per operand
+constexpr int kDiag = kS;        // diagonals d = 2 .. S+1
+constexpr int kTileRows = 128;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// shared-memory matrix descriptor: canonical K-major layout, no swizzle
+//   start address, LBO = byte stride between core matrices along K,
+//   SBO = byte stride between 8-row groups, version 1 (bit 46), layout 0
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr >> 4) & 0x3FFF);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+  d |= (uint64_t)1 << 46;
+  return d;
+}
+
+// instruction descriptor, kind::f16: D = F32, A = B = BF16, both K-major, N, M = 128
+__host__ __device__ constexpr uint32_t idesc_bf16(int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(kTileRows >> 4) << 24);
+}
+
+// element (row, k) of a K-major tile with K_real columns, in bytes
+__device__ __forceinline__ uint32_t kmaj_off(int row, int k, int kreal) {
+  return (uint32_t)((row >> 3) * (kreal >> 3) * 128 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
+}
+
+// exact BF16 bits of a small integer (|x| < 2^22): 1.5*2^23 magic, top 16 bits
+__device__ __forceinline__ uint16_t int_to_bf16(int x) {
+  const float f = __int_as_float(0x4B400000 + x) - 12582912.0f;
+  return (uint16_t)(__float_as_uint(f) >> 16);
+}
+
+// exact integer value of an integer-valued float with |f| < 2^22
+__device__ __forceinline__ int float_to_int_exact(float f) {
+  return __float_as_int(f + 12582912.0f) - 0x4B400000;
+}
+
+// |v| as an ordered integer (non-negative doubles compare like their bit patterns)
+__device__ __forceinline__ unsigned long long abs_bits(double v) {
+  return (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
+}
+
+// exponent e with |v| < 2^e from the bits of |v| (0 for v == 0); integer ops only
+__device__ __forceinline__ int exp_above_bits(unsigned long long ab) {
+  return ab ? (int)(ab >> 52) - 1022 : 0;
+}
+
+// N = round(v * 2^(49 - e)) as a signed integer (|N| <= 2^49), integer ops only
+__device__ __forceinline__ long long scaled_int(double v, int e) {
+  const long long bits = __double_as_longlong(v);
+  const int be = (int)((bits >> 52) & 0x7FF);
+  if (be == 0) return 0;   // zero / subnormal
+  const long long mant = (bits & 0x000FFFFFFFFFFFFFLL) | 0x0010000000000000LL;
+  // v = mant * 2^(be - 1075);  v * 2^(49-e) = mant * 2^(be - 1026 - e)
+  const int sh = 1026 + e - be;    // right shift >= 3 since |v| < 2^e
+  long long n;
+  if (sh >= 62) n = 0;
+  else n = (mant + (1LL << (sh - 1))) >> sh;
+  return (bits < 0) ? -n : n;
+}
+
+// signed 7-bit digits of N (|N| <= 2^49), extracted from the bottom:
+// x_7..x_2 in [-64, 63], x_1 the remaining top part (|x_1| <= 128); N = sum_t x_t 2^(7(7-t))
+__device__ __forceinline__ void digits7(long long n, int x[kS]) {
+#pragma unroll
+  for (int t = kS - 1; t > 0; --t) {
+    const int lo = (int)n & 127;
+    const int d = lo - ((lo & 64) << 1);     // centred in [-64, 63]
+    x[t] = d;
+    n = (n - d) >> 7;
+  }
+  x[0] = (int)n;
+}
+
+// exact double of S * 2^sc (|S| < 2^63) with integer ops only (round to nearest even)
+__device__ __forceinline__ double int64_scaled_to_double(long long S, int sc) {
+  if (S == 0) return 0.0;
+  const unsigned long long sign = (S < 0) ? 0x8000000000000000ull : 0ull;
+  unsigned long long a = (S < 0) ? (unsigned long long)(-S) : (unsigned long long)S;
+  const int lz = __clzll(a);
+  a <<= lz;                                   // leading 1 at bit 63
+  // keep 53 bits: round to nearest even on the 11 dropped bits
+  unsigned long long m = a >> 11;
+  const unsigned long long rem = a & 0x7FFull;
+  if (rem > 0x400ull || (rem == 0x400ull && (m & 1ull))) m += 1ull;
+  int ex = 63 - lz + sc;                      // value = m * 2^(ex - 52)
+  if (m >> 53) {                              // rounding carried into a new bit
+    m >>= 1;
+    ex += 1;
+  }
+  const unsigned long long bits = sign | ((unsigned long long)(ex + 1023) << 52) | (m & 0x000FFFFFFFFFFFFFull);
+  return __longlong_as_double((long long)bits);
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t parity) {
+  for (int it = 0; it < (1 << 20); ++it) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(addr), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
+template <int WP>
+struct TileSmem {
+  static constexpr int KR = 2 * WP;                 // real K
+  static constexpr int NR = 2 * WP;                 // real N
+  static constexpr int A_BYTES = kTileRows * KR * 2;
+  static constexpr int B_BYTES = NR * KR * 2;
+  static constexpr int TMEM_COLS = (kDiag * NR <= 128) ? 128 : ((kDiag * NR <= 256) ? 256 : 512);
+  static constexpr size_t BYTES = (size_t)kS * A_BYTES + (size_t)kS * B_BYTES + 1024;
+};
+
+}  // namespace
+
+// STEP 1: group = k.  STEP 2: group = k'.  which: 0 trial, 1 optimal-step pass.
+template <int WP, int STEP>
+__global__ void __launch_bounds__(256, 1) k_oz_mupdate(const Problem* __restrict__ probs, WorkMap wm, int which) {
+  using L = TileSmem<WP>;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  unsigned char* sA = base;                                   // kS slices of A
+  unsigned char* sB = base + (size_t)kS * L::A_BYTES;          // kS slices of B
+  __shared__ __align__(8) uint64_t mbar;
+  __shared__ uint32_t tmem_base_slot;
+  __shared__ int s_rowexp[kTileRows];
+  __shared__ int s_colexp[2 * WP];
+  __shared__ int s_bad;
+
+  int g;
+  const int p = locate(wm, blockIdx.x, g);
+  const Problem& P = probs[p];
+  CtrlState* st = P.st;
+  if (st->done) return;
+  if (which == 1 && !st->do_second) return;
+  const int W = P.W, B = P.B, WW = W * W;
+  const int cur = st->cur;
+  const double2* Unew = P.U[cur ^ 1];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  constexpr int KR = L::KR, NR = L::NR;
+
+  // ---- TMEM allocation (warp 0) and barrier init
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                 :: "r"(smem_u32(&tmem_base_slot)), "r"((uint32_t)L::TMEM_COLS) : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&mbar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    s_bad = 0;
+  }
+
+  // ---- B operand of the group: step 1 conj(U(k)), step 2 U(k')
+  const double2* Ug = Unew + (size_t)g * WW;
+  // column scales: column c (and c+WP) of the real embedding = complex column c
+  for (int c = tid; c < WP; c += blockDim.x) {
+    unsigned long long mx = 0ull;
+    if (c < W)
+      for (int m = 0; m < W; ++m) {
+        const double2 u = Ug[(size_t)c * W + m];
+        mx = max(mx, max(abs_bits(u.x), abs_bits(u.y)));
+      }
+    const int e = exp_above_bits(mx);
+    s_colexp[c] = e;
+    s_colexp[c + WP] = e;
+  }
+  __syncthreads();
+  // B^T is stored K-major: row = real output column n (0..NR), k = real K index
+  for (int e = tid; e < NR * KR; e += blockDim.x) {
+    const int ln = e & 31, wi = e >> 5;
+    const int kgroups = KR / 8;
+    const int n = (wi / kgroups) * 4 + (ln >> 3);
+    const int kk = (wi % kgroups) * 8 + (ln & 7);
+    const int cc = n % WP;           // complex column
+    const int mm = kk % WP;          // complex row (K index)
+    double val = 0.0;
+    if (cc < W && mm < W) {
+      const double2 u = Ug[(size_t)cc * W + mm];
+      // B = U (step 2) or conj(U) (step 1): B_r = Re U, B_i = +/- Im U
+      const double br = u.x, bi = (STEP == 1) ? -u.y : u.y;
+      const bool kre = kk < WP, nre = n < WP;
+      if (kre && nre) val = br;            // [B_r   B_i]
+      else if (kre && !nre) val = bi;
+      else if (!kre && nre) val = -bi;     // [-B_i  B_r]
+      else val = br;
+    }
+    int x[kS];
+    digits7(scaled_int(val, s_colexp[n]), x);
+    const uint32_t off = kmaj_off(n, kk, KR);
+#pragma unroll
+    for (int t = 0; t < kS; ++t) *(uint16_t*)(sB + (size_t)t * L::B_BYTES + off) = int_to_bf16(x[t]);
+  }
+
+  const int rows_group = B * WP;
+  const int ntiles = (rows_group + kTileRows - 1) / kTileRows;
+  __syncthreads();
+  const uint32_t tmem = tmem_base_slot;
+  const uint32_t idesc = idesc_bf16(NR);
+  uint32_t phase = 0;
+
+  for (int tile = 0; tile < ntiles; ++tile) {
+    // ---- A rows of this tile: row r -> block i = row/WP (pair index), n/m = row%WP
+    // row scales (one thread per row pair of halves: 2 threads per row)
+    {
+      const int r = tid >> 1, half = tid & 1;
+      const int row = tile * kTileRows + r;
+      const int bi = row / WP, rr = row % WP;
+      unsigned long long mx = 0ull;
+      const double2* src = nullptr;
+      size_t stride = 0;
+      if (bi < B && rr < W) {
+        if (STEP == 1) {
+          // A(row=(b,n), kk) = M0(k,b)(m=kk, n): column n of block (k,b), contiguous in m
+          src = P.M0 + ((size_t)g * B + bi) * WW + (size_t)rr * W;
+          stride = 1;
+        } else {
+          // A(row=((k,b),m), kk) = Z(k,b)(m, j=kk): Z row-major, contiguous in j
+          const int kb = P.inv_nnlist[(size_t)g * B + bi];
+          src = P.tbuf + (size_t)kb * WW + (size_t)rr * W;
+          stride = 1;
+        }
+        for (int m = half; m < W; m += 2) {
+          const double2 a = src[m * stride];
+          mx = max(mx, max(abs_bits(a.x), abs_bits(a.y)));
+        }
+      }
+      mx = max(mx, (unsigned long long)__shfl_xor_sync(0xffffffffu, (long long)mx, 1));
+      if (half == 0) s_rowexp[r] = exp_above_bits(mx);
+    }
+    __syncthreads();
+    for (int e = tid; e < kTileRows * WP; e += blockDim.x) {
+      // lane -> (row r within 4, m within 8): a warp writes 4 consecutive 16-byte core rows
+      const int ln = e & 31, wi = e >> 5;
+      const int mgroups = WP / 8;
+      const int r = (wi / mgroups) * 4 + (ln >> 3);
+      const int m = (wi % mgroups) * 8 + (ln & 7);
+      const int row = tile * kTileRows + r;
+      const int bi = row / WP, rr = row % WP;
+      double2 a = make_double2(0.0, 0.0);
+      if (bi < B && rr < W && m < W) {
+        if (STEP == 1) {
+          a = P.M0[((size_t)g * B + bi) * WW + (size_t)rr * W + m];
+        } else {
+          const int kb = P.inv_nnlist[(size_t)g * B + bi];
+          a = P.tbuf[(size_t)kb * WW + (size_t)rr * W + m];
+        }
+      }
+      const int ex = s_rowexp[r];
+      int xr[kS], xi[kS];
+      digits7(scaled_int(a.x, ex), xr);
+      digits7(scaled_int(a.y, ex), xi);
+      const uint32_t o_re = kmaj_off(r, m, KR), o_im = kmaj_off(r, m + WP, KR);
+#pragma unroll
+      for (int t = 0; t < kS; ++t) {
+        *(uint16_t*)(sA + (size_t)t * L::A_BYTES + o_re) = int_to_bf16(xr[t]);
+        *(uint16_t*)(sA + (size_t)t * L::A_BYTES + o_im) = int_to_bf16(xi[t]);
+      }
+    }
+    // make the generic-proxy smem writes visible to the tensor core (async proxy)
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+
+    // ---- MMAs: pairs (t,u), t+u <= S+1 (1-based), diagonal d = t+u -> accumulator d-2
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      bool first[kDiag];
+#pragma unroll
+      for (int d = 0; d < kDiag; ++d) first[d] = true;
+      for (int t = 0; t < kS; ++t) {
+        for (int u = 0; u + t <= kS - 1; ++u) {
+          const int d = t + u;   // 0-based diagonal index (t+u+2 in 1-based digits)
+          const uint32_t dtm = tmem + (uint32_t)(d * NR);
+          const uint32_t a0 = smem_u32(sA + (size_t)t * L::A_BYTES);
+          const uint32_t b0 = smem_u32(sB + (size_t)u * L::B_BYTES);
+#pragma unroll
+          for (int ks = 0; ks < KR / 16; ++ks) {
+            const uint64_t ad = smem_desc(a0 + ks * 256, 128, (KR / 8) * 128);
+            const uint64_t bd = smem_desc(b0 + ks * 256, 128, (KR / 8) * 128);
+            const uint32_t acc = (first[d] && ks == 0) ? 0u : 1u;
+            asm volatile(
+                "{\n\t.reg .pred p;\n\t"
+                "setp.ne.b32 p, %4, 0;\n\t"
+                "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+                :: "r"(dtm), "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+                : "memory");
+          }
+          first[d] = false;
+        }
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                   :: "r"(smem_u32(&mbar)) : "memory");
+    }
+    const bool ok_mine = mbar_wait(smem_u32(&mbar), phase);
+    phase ^= 1u;
+    if (!ok_mine) s_bad = 1;
+    __syncthreads();
+    const bool ok = (s_bad == 0);   // uniform across the CTA
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+
+    // ---- epilogue: all 8 warps; warp w reads TMEM lanes 32*(w%4).. (its sub-partition),
+    // warps w and w+4 take the lower / upper half of the complex output columns
+    if (ok) {
+      const int wq = warp & 3, half = warp >> 2;
+      const int r = wq * 32 + lane;
+      const int row = tile * kTileRows + r;
+      const int bi = row / WP, rr = row % WP;
+      const bool valid = (bi < B) && (rr < W);
+      const int erow = s_rowexp[r];
+      const uint32_t lane_base = (uint32_t)(wq * 32) << 16;
+      int kb_out = 0;
+      if (STEP == 2 && bi < B) kb_out = P.inv_nnlist[(size_t)g * B + bi];
+      const int cbeg = half * (WP / 2), cend = cbeg + WP / 2;
+      double dre = 0.0, dim = 0.0;   // this row's diagonal element, if in this half
+      bool has_diag = false;
+      // complex output column c: real part at real column c, imaginary part at c + WP
+#pragma unroll 1
+      for (int c0 = cbeg; c0 < cend; c0 += 4) {
+        uint32_t q[kDiag][4], s4[kDiag][4];
+#pragma unroll
+        for (int d = 0; d < kDiag; ++d) {
+          const uint32_t ta = tmem + lane_base + (uint32_t)(d * NR + c0);
+          const uint32_t tb = tmem + lane_base + (uint32_t)(d * NR + WP + c0);
+          asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+                       : "=r"(q[d][0]), "=r"(q[d][1]), "=r"(q[d][2]), "=r"(q[d][3])
+                       : "r"(ta));
+          asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+                       : "=r"(s4[d][0]), "=r"(s4[d][1]), "=r"(s4[d][2]), "=r"(s4[d][3])
+                       : "r"(tb));
+        }
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const int c = c0 + j;
+          // S = sum_d D_d 2^(7(6-d)) by Horner in int64 (exact, |S| < 2^63)
+          long long sr = float_to_int_exact(__uint_as_float(q[0][j]));
+          long long si = float_to_int_exact(__uint_as_float(s4[0][j]));
+#pragma unroll
+          for (int d = 1; d < kDiag; ++d) {
+            sr = (sr << 7) + float_to_int_exact(__uint_as_float(q[d][j]));
+            si = (si << 7) + float_to_int_exact(__uint_as_float(s4[d][j]));
+          }
+          // value = S * 2^(erow + ecol - 56)
+          const int sc = erow + s_colexp[c] - 56;
+          const double re = int64_scaled_to_double(sr, sc);
+          const double im = int64_scaled_to_double(si, sc);
+          if (valid && c < W) {
+            if (STEP == 1) {
+              // Z(k,b) row-major: element (j=c, n=rr) at c*W + rr
+              P.tbuf[((size_t)g * B + bi) * WW + (size_t)c * W + rr] = make_double2(re, im);
+            } else {
+              // M(k,b) column-major: element (m=rr, c) at c*W + rr
+              P.M[cur ^ 1][(size_t)kb_out * WW + (size_t)c * W + rr] = make_double2(re, im);
+              if (c == rr) {
+                dre = re;
+                dim = im;
+                has_diag = true;
+              }
+            }
+          }
+        }
+      }
+      if (STEP == 2 && has_diag) {
+        // diagonal statistics (once per row); the off-diagonal sum follows from the
+        // invariant |M(k,b)|_F^2 = |M0(k,b)|_F^2 in the spread pass
+        P.diag_ln[(size_t)kb_out * W + rr] = atan2(dim, dre);
+        P.diag_abs2[(size_t)kb_out * W + rr] = dre * dre + dim * dim;
+      }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (s_bad) break;
+  }
+  if (s_bad && tid == 0) {
+    st->error = 2;
+    st->done = 1;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;"
+                 :: "r"(tmem), "r"((uint32_t)L::TMEM_COLS) : "memory");
+  }
+}
+
+// host-side launchers (the template kernels stay private to this translation unit)
+template <int WP>
+static cudaError_t oz_launch_wp(int step, const Problem* probs, WorkMap wm, int which, int grid,
+                                cudaStream_t s) {
+  const size_t sm = TileSmem<WP>::BYTES;
+  if (step == 1) k_oz_mupdate<WP, 1><<<grid, 256, sm, s>>>(probs, wm, which);
+  else k_oz_mupdate<WP, 2><<<grid, 256, sm, s>>>(probs, wm, which);
+  return cudaGetLastError();
+}
+
+cudaError_t oz_launch(int wp, int step, const Problem* probs, WorkMap wm, int which, int grid,
+                      cudaStream_t s) {
+  switch (wp) {
+    case 8: return oz_launch_wp<8>(step, probs, wm, which, grid, s);
+    case 16: return oz_launch_wp<16>(step, probs, wm, which, grid, s);
+    default: return oz_launch_wp<32>(step, probs, wm, which, grid, s);
+  }
+}
+
+template <int WP>
+static cudaError_t oz_attr_wp() {
+  const int sm = (int)TileSmem<WP>::BYTES;
+  cudaError_t e = cudaFuncSetAttribute(k_oz_mupdate<WP, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_oz_mupdate<WP, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+}
+
+cudaError_t oz_set_attributes(int wp) {
+  switch (wp) {
+    case 8: return oz_attr_wp<8>();
+    case 16: return oz_attr_wp<16>();
+    default: return oz_attr_wp<32>();
+  }
+}
+
+size_t oz_smem_bytes(int wp) {
+  switch (wp) {
+    case 8: return TileSmem<8>::BYTES;
+    case 16: return TileSmem<16>::BYTES;
+    default: return TileSmem<32>::BYTES;
+  }
+}
+
+}  // namespace w90g

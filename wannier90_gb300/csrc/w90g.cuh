@@ -121,10 +121,14 @@ struct Problem {
   double* centres;      // [slot][4][W]: rave(3,W) + r2ave-rave2 (W) per spread slot; slot 2 = accepted
   double* log;          // [num_iter+1][kLogStride]
   double* log_centres;  // [num_iter+1][4][W]
+  double2* M0;          // tensor path: M at entry (never modified)
+  double2* U0;          // tensor path: U at entry; U[] then holds R = U0^H U
+  const int* inv_nnlist;  // tensor path: [k'][i] = k*B+b with nnlist(k,b) = k'
+  double* frob0;        // tensor path: |M0(k,b)|_F^2
   double* opart1;       // [nchunk][4W+2] spread partials (pass 1)
   double* opart2;       // [nchunk]       Omega_D partials (pass 2)
   int nchunk;           // ceil(K*B / 64)
-  int pad3;
+  int tensor;           // 1: M update on tensor cores (tcgen05, exact BF16 slicing)
   CtrlState* st;
   Control ctl;
   int max_exp_squarings;
