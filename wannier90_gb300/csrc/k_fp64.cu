@@ -502,13 +502,67 @@ __global__ void k_ctrl_search(const Problem* __restrict__ probs) {
 }
 
 // ----------------------------------------------------------------------------
-// exp(X) for anti-Hermitian X (W x W), scaling and squaring with a degree-16 Taylor
-// polynomial evaluated by the Paterson-Stockmeyer scheme (p = 4): Y2, Y3, Y4 and
-// three Horner steps in Y4 = 6 matrix products, then j squarings.  ||Y||_1 <= 0.8
-// bounds the truncation term 0.8^17/17! < 1.1e-16 (||e^Y||_2 = 1 for anti-Hermitian Y).
-// exp(s*D) equals the reference's V e^{-i s lambda} V^dagger with (V, lambda) the
-// eigenpairs of i*D (src/wannierise.F90:1655-1690) in exact arithmetic.
-// Buffers: X (input, scaled in place), Y2, Y3, Y4, R, T  (6 * W*W).  Result in *out.
+// C = A * B where the product is known to be Hermitian (sign = +1) or anti-Hermitian
+// (sign = -1): only the upper-triangular 2x2 tiles are computed (whole warps skip the
+// rest), then the lower triangle is mirrored.  Caller synchronises before reading C.
+// ----------------------------------------------------------------------------
+__device__ void cta_gemm_sym(double2* __restrict__ C, const double2* __restrict__ A,
+                             const double2* __restrict__ B, int W, double sign) {
+  const int nb = (W + 1) >> 1;
+  const int ntri = nb * (nb + 1) / 2;
+  for (int t = threadIdx.x; t < ntri; t += blockDim.x) {
+    int bi = 0, rem = t;
+    while (rem >= nb - bi) {
+      rem -= nb - bi;
+      ++bi;
+    }
+    const int bj = bi + rem;
+    const int i0 = bi * 2, j0 = bj * 2;
+    const bool i1 = (i0 + 1) < W, j1 = (j0 + 1) < W;
+    double2 c00 = cmk(0, 0), c01 = cmk(0, 0), c10 = cmk(0, 0), c11 = cmk(0, 0);
+    const double2 z = cmk(0, 0);
+#pragma unroll 4
+    for (int l = 0; l < W; ++l) {
+      const double2 a0 = A[l * W + i0];
+      const double2 a1 = i1 ? A[l * W + i0 + 1] : z;
+      const double2 b0 = B[j0 * W + l];
+      const double2 b1 = j1 ? B[(j0 + 1) * W + l] : z;
+      cfma(c00, a0, b0);
+      cfma(c10, a1, b0);
+      cfma(c01, a0, b1);
+      cfma(c11, a1, b1);
+    }
+    C[j0 * W + i0] = c00;
+    if (i1) C[j0 * W + i0 + 1] = c10;
+    if (j1) {
+      C[(j0 + 1) * W + i0] = c01;
+      if (i1) C[(j0 + 1) * W + i0 + 1] = c11;
+    }
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < W * W; e += blockDim.x) {
+    const int i = e % W, j = e / W;
+    if (i > j) {
+      const double2 u = C[i * W + j];   // C(j,i), upper triangle
+      C[e] = cmk(sign * u.x, -sign * u.y);
+    } else if (i == j) {
+      const double2 d = C[e];
+      C[e] = (sign > 0) ? cmk(d.x, 0.0) : cmk(0.0, d.y);
+    }
+  }
+}
+
+// ----------------------------------------------------------------------------
+// exp(X) for anti-Hermitian X (W x W): scaling and squaring with a Taylor polynomial
+// of degree m evaluated by Paterson-Stockmeyer in powers up to X^p.  Per matrix the
+// cheapest (m, squarings j) is chosen such that ||X / 2^j||_1 <= theta_m, where
+// theta_m^(m+1) / (m+1)! <= 2^-53 bounds the truncation (||e^Y||_2 = 1 for
+// anti-Hermitian Y):  (m, p, theta_m, cost in W^3 products) =
+//   (4,4,1.6e-3,1.5) (6,3,1.7e-2,2.0) (8,4,6.6e-2,2.5) (12,4,0.32,3.5) (16,4,0.78,4.5)
+// X^2 and X^4 are Hermitian and X^3 anti-Hermitian, so those powers cost half a
+// product.  exp(s*D) equals the reference's V e^{-i s lambda} V^dagger with (V, lambda)
+// the eigenpairs of i*D (src/wannierise.F90:1655-1690) in exact arithmetic.
+// Buffers: X (input, scaled in place), Y2, Y3, Y4, R, T (6 * W*W).  Returns the result.
 // ----------------------------------------------------------------------------
 __device__ const double kInvFact[17] = {
     1.0, 1.0, 0.5, 1.6666666666666666e-01, 4.1666666666666664e-02, 8.3333333333333332e-03,
@@ -520,52 +574,77 @@ __device__ const double kInvFact[17] = {
 __device__ double2* cta_expm(double2* X, double2* Y2, double2* Y3, double2* Y4, double2* R,
                              double2* T, int W, double* red) {
   const int WW = W * W;
-  // ||X||_1 = max column sum
   double colmax = 0.0;
   for (int j = threadIdx.x; j < W; j += blockDim.x) {
     double s = 0.0;
     for (int i = 0; i < W; ++i) s += sqrt(cabs2(X[j * W + i]));
     colmax = fmax(colmax, s);
   }
-  double nrm = block_max(colmax, red);
-  int js = 0;
-  while (nrm > 0.8 && js < 60) {
-    nrm *= 0.5;
-    ++js;
+  const double nrm = block_max(colmax, red);
+  // candidate degrees (theta_m with a 5% margin for the tail of the series)
+  const int cand_m[5] = {4, 6, 8, 12, 16};
+  const int cand_p[5] = {4, 3, 4, 4, 4};
+  const double cand_theta[5] = {1.6e-3, 1.68e-2, 6.6e-2, 0.32, 0.78};
+  const double cand_cost[5] = {1.5, 2.0, 2.5, 3.5, 4.5};
+  int m = 16, p = 4, js = 0;
+  double best = 1e300;
+  for (int c = 0; c < 5; ++c) {
+    int j = 0;
+    double v = nrm;
+    while (v > cand_theta[c] && j < 60) {
+      v *= 0.5;
+      ++j;
+    }
+    const double cost = cand_cost[c] + j;
+    if (cost < best) {
+      best = cost;
+      m = cand_m[c];
+      p = cand_p[c];
+      js = j;
+    }
   }
   const double sc = ldexp(1.0, -js);
   for (int e = threadIdx.x; e < WW; e += blockDim.x) X[e] = cscale(X[e], sc);
   __syncthreads();
-  cta_gemm<false>(Y2, W, X, W, X, W, W);
+  // powers: Y2 Hermitian, Y3 = Y2 X anti-Hermitian, Y4 = Y2 Y2 Hermitian
+  cta_gemm_sym(Y2, X, X, W, 1.0);
   __syncthreads();
-  cta_gemm<false>(Y3, W, Y2, W, X, W, W);
-  cta_gemm<false>(Y4, W, Y2, W, Y2, W, W);
+  cta_gemm_sym(Y3, Y2, X, W, -1.0);
+  if (p >= 4) cta_gemm_sym(Y4, Y2, Y2, W, 1.0);
   __syncthreads();
-  // R = B3 + c16*Y4, with B_q = c_{4q} I + c_{4q+1} Y + c_{4q+2} Y2 + c_{4q+3} Y3
-  for (int e = threadIdx.x; e < WW; e += blockDim.x) {
+  const double2* Yp = (p == 4) ? Y4 : Y3;
+  const int nblk = (m + p) / p;   // blocks B_0 .. B_{nblk-1}, B_q = sum_r c_{pq+r} Y^r
+  // element e of B_q
+  auto blk = [&](int q, int e) -> double2 {
     const int i = e % W, j = e / W;
-    double2 v = cscale(Y4[e], kInvFact[16]);
-    v = cadd(v, cscale(X[e], kInvFact[13]));
-    v = cadd(v, cscale(Y2[e], kInvFact[14]));
-    v = cadd(v, cscale(Y3[e], kInvFact[15]));
-    if (i == j) v.x += kInvFact[12];
-    R[e] = v;
+    double2 v = cmk(0.0, 0.0);
+    for (int r = 0; r < p; ++r) {
+      const int deg = p * q + r;
+      if (deg > m) break;
+      const double c = kInvFact[deg];
+      if (r == 0) {
+        if (i == j) v.x += c;
+      } else {
+        const double2 y = (r == 1) ? X[e] : ((r == 2) ? Y2[e] : Y3[e]);
+        v = cadd(v, cscale(y, c));
+      }
+    }
+    return v;
+  };
+  int q = nblk - 1;
+  // R = B_top; when B_top is c_m I alone, fold the first Horner step into a scaled copy
+  if (p * q == m) {
+    const double cm = kInvFact[m];
+    for (int e = threadIdx.x; e < WW; e += blockDim.x) R[e] = cadd(cscale(Yp[e], cm), blk(q - 1, e));
+    q -= 1;
+  } else {
+    for (int e = threadIdx.x; e < WW; e += blockDim.x) R[e] = blk(q, e);
   }
   __syncthreads();
-  for (int q = 2; q >= 0; --q) {
-    cta_gemm<false>(T, W, Y4, W, R, W, W);
+  for (q = q - 1; q >= 0; --q) {
+    cta_gemm<false>(T, W, Yp, W, R, W, W);
     __syncthreads();
-    const double c0 = kInvFact[4 * q], c1 = kInvFact[4 * q + 1], c2 = kInvFact[4 * q + 2],
-                 c3 = kInvFact[4 * q + 3];
-    for (int e = threadIdx.x; e < WW; e += blockDim.x) {
-      const int i = e % W, j = e / W;
-      double2 v = T[e];
-      v = cadd(v, cscale(X[e], c1));
-      v = cadd(v, cscale(Y2[e], c2));
-      v = cadd(v, cscale(Y3[e], c3));
-      if (i == j) v.x += c0;
-      R[e] = v;
-    }
+    for (int e = threadIdx.x; e < WW; e += blockDim.x) R[e] = cadd(T[e], blk(q, e));
     __syncthreads();
   }
   double2* a = R;
