@@ -36,6 +36,10 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 METRIC = "converged MLWF solves/s"
+try:
+    MEASURED = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+except Exception:
+    MEASURED = {}
 WORKLOADS = {
     "fcc10_w32": dict(cfg="fcc10_w32", conv_tol=1e-10, conv_window=5, num_iter=20000),
     "sc4_w8": dict(cfg="sc4_w8", conv_tol=1e-10, conv_window=-1, num_iter=200),
@@ -187,6 +191,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-iters", type=int, default=6)
     ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--precision", default="tensor", choices=["tensor", "fp64"],
+                    help="tensor: M update on tcgen05 tensor cores (exact BF16 slicing, FP64-accurate); "
+                         "fp64: every product on the FP64 pipe")
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":
@@ -213,7 +220,8 @@ def main():
     # problem (replicas: every rank solves its own copy of the same seeded problem)
     p = synth.make_problem(**synth.CONFIGS[wl["cfg"]], seed=0)
     W, K, B = p.num_wann, len(p.kpoints), p.nntot
-    opts = dict(num_iter=wl["num_iter"], conv_tol=wl["conv_tol"], conv_window=wl["conv_window"], iprint=0)
+    opts = dict(num_iter=wl["num_iter"], conv_tol=wl["conv_tol"], conv_window=wl["conv_window"], iprint=0,
+                gpu_tensor=1 if args.precision == "tensor" else 0)
     h = w90.setup(kpoints=p.kpoints, unit_cell_cart=p.real_lattice, num_wann=W, **opts)
     stream = torch.cuda.Stream()
     w90.w90_set_stream(h, stream.cuda_stream)
@@ -302,15 +310,45 @@ def main():
     names = [L.w90g_profile_kernel_name(i).decode() for i in range(8)]
     per_kernel = {n: {"ms_total": msk[i], "launches": cnt[i],
                       "ms_avg": (msk[i] / cnt[i]) if cnt[i] else None} for i, n in enumerate(names)}
+    exp_products = L.w90g_profile_exp_products(h.handle)
     fp64_peak = L.w90g_measure_fp64_peak()
-    dom = "k_m_update"
+    tot = sum(v["ms_total"] for v in per_kernel.values())
+    for v in per_kernel.values():
+        v["share"] = v["ms_total"] / tot if tot else None
+    dom = max(("k_m_update", "k_exp_u", "k_grad"), key=lambda n: per_kernel[n]["ms_total"])
     avg = per_kernel[dom]["ms_avg"]
-    flops_launch = 2 * 8.0 * W ** 3 * K * B   # two complex W^3 GEMMs per (k,b)
-    achieved = flops_launch / (avg * 1e-3) / 1e12 if avg else None
-    roof = {"bound": "fp64", "kernel": dom, "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
-            "frac": (achieved / fp64_peak) if (achieved and fp64_peak > 0) else None, "traffic": None,
-            "peak_source": "FP64 FMA probe measured in this run (MEASURED_PEAKS.json has no FP64 figure)",
-            "algorithmic_flops_per_launch": flops_launch, "per_kernel": per_kernel}
+    useful_mupdate = 2 * 8.0 * W ** 3 * K * B          # two complex W^3 GEMMs per (k,b)
+    if dom == "k_m_update" and args.precision == "tensor":
+        # BF16 MMA work actually issued: 28 digit pairs of (128 x 2WP x 2WP) per 128-row tile
+        wp = 8 if W <= 8 else (16 if W <= 16 else 32)
+        tiles = 2 * K * -(-(B * wp) // 128)
+        flops = 28 * 2.0 * 128 * (2 * wp) * (2 * wp) * tiles
+        achieved = flops / (avg * 1e-3) / 1e12
+        peak = float(MEASURED.get("bf16_tflops", 1900.0))
+        peak_src = ("bf16_tflops of MEASURED_PEAKS.json (burst), of measured" if "bf16_tflops" in MEASURED
+                    else "1.9 PFLOP/s bf16 burst, of fallback")
+        roof = {"bound": "tensor", "kernel": dom + " (tcgen05, 2 launches)", "achieved": achieved, "peak": peak,
+                "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                "peak_source": peak_src,
+                "algorithmic_flops_per_launch": flops,
+                "fp64_equivalent": {"flops_per_launch": useful_mupdate,
+                                    "tflops": useful_mupdate / (avg * 1e-3) / 1e12,
+                                    "fp64_pipe_peak_tflops": fp64_peak}}
+    else:
+        if dom == "k_exp_u":
+            cnt_exp = max(per_kernel["k_exp_u"]["launches"], 1)
+            flops = exp_products / cnt_exp * 8.0 * W ** 3
+        elif dom == "k_grad":
+            flops = 16.0 * K * B * W * W
+        else:
+            flops = useful_mupdate
+        achieved = flops / (avg * 1e-3) / 1e12
+        roof = {"bound": "fp64", "kernel": dom, "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                "frac": achieved / fp64_peak if fp64_peak > 0 else None, "traffic": None,
+                "peak_source": "FP64 FMA probe measured in this run (MEASURED_PEAKS.json has no FP64 figure)",
+                "algorithmic_flops_per_launch": flops}
+    roof["per_kernel"] = per_kernel
+    roof["profiled_iterations"] = args.profile_iters
 
     # CPU baseline (oracle on host cores, bounded sample)
     cpu = None
@@ -330,7 +368,10 @@ def main():
             "config": {"workload": args.workload, "lattice": synth.CONFIGS[wl["cfg"]]["kind"],
                        "num_kpts": K, "nntot": B, "num_wann": W, "conv_tol": wl["conv_tol"],
                        "conv_window": wl["conv_window"], "iterations_per_solve": niter,
-                       "precision": "fp64", "l2": "inputs larger than L2 (M = %d MB)" % (bytes_m >> 20),
+                       "precision": ("tensor: M(k,b) = U^H M0 U on tcgen05 BF16 MMAs with exact 7-digit "
+                                     "slicing (FP64-accurate); exp, gradient, spread on the FP64 pipe"
+                                     if args.precision == "tensor" else "fp64"),
+                       "l2": "inputs larger than L2 (M = %d MB)" % (bytes_m >> 20),
                        "parallelism": "replicas" if world > 1 else "single"},
             "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": bytes_m + bytes_u,
                     "d2h_bytes_per_step": bytes_m + bytes_u},
@@ -346,7 +387,7 @@ def main():
 
 
 # iterations per solve of each workload as measured by the GPU arm (FP64 engine)
-KNOWN_ITERS = {"fcc10_w32": 1824, "sc4_w8": 200}
+KNOWN_ITERS = {"fcc10_w32": 1834, "sc4_w8": 200}
 
 if __name__ == "__main__":
     sys.exit(main())

@@ -108,6 +108,9 @@ long long w90g_kernel_launches(void* handle);
 int w90g_profile_device(void* handle, double* d_m_matrix, double* d_u_matrix, int max_iters,
                         double* ms, int* counts);
 const char* w90g_profile_kernel_name(int i);
+/* W^3 complex products spent by exp(s D) and U dU during the last profiling run (the
+ * per-matrix Taylor degree and squarings are data dependent). */
+double w90g_profile_exp_products(void* handle);
 /* FP64 FMA throughput of the current device in TFLOP/s (dependent-chain probe). */
 double w90g_measure_fp64_peak(void);
 /* Loewdin projection (as w90g_project_overlap_device) that allocates no device memory.

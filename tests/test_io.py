@@ -1,0 +1,78 @@
+"""Wannier90 file formats (no GPU): .win/.mmn/.amn/.eig round trips, the reference's own
+.mmn/.amn read through the k-mesh tables, and the unformatted .chk layout."""
+import os
+import struct
+
+import numpy as np
+import pytest
+
+from tests import golden_cases as G
+from wannier90_gb300 import library as w90
+from wannier90_gb300 import synth, w90io
+
+REF = "/root/reference/test-suite/tests/testw90_example02"
+
+
+def _small():
+    return synth.make_problem(kind="fcc", a=6.0, mp=(3, 3, 3), num_wann=5, rmax=1, eps=0.3, seed=4)
+
+
+def test_mmn_amn_eig_roundtrip(tmp_path):
+    p = _small()
+    f = str(tmp_path / "x")
+    w90io.write_mmn(f + ".mmn", p.m, p.nnlist, p.nncell)
+    w90io.write_amn(f + ".amn", p.a)
+    eig = np.asfortranarray(np.arange(5 * 27, dtype=float).reshape(5, 27, order="F") * 0.1)
+    w90io.write_eig(f + ".eig", eig)
+    m = w90io.read_mmn(f + ".mmn", p.nnlist, p.nncell)
+    a = w90io.read_amn(f + ".amn")
+    np.testing.assert_allclose(m, p.m, atol=1e-11)
+    np.testing.assert_allclose(a, p.a, atol=1e-11)
+    np.testing.assert_allclose(w90io.read_eig(f + ".eig", 5, 27), eig, atol=1e-11)
+
+
+def test_win_roundtrip(tmp_path):
+    p = _small()
+    f = str(tmp_path / "x.win")
+    w90io.write_win(f, p.real_lattice, p.kpoints, p.mp_grid, 5, num_iter=40, conv_tol="1d-9", precond=".false.")
+    lat, kp, opts = w90io.win_system(f)
+    np.testing.assert_allclose(lat, p.real_lattice, atol=1e-12)
+    np.testing.assert_allclose(kp, p.kpoints, atol=1e-12)
+    assert opts["num_wann"] == 5 and opts["num_iter"] == 40 and abs(opts["conv_tol"] - 1e-9) < 1e-24
+    assert opts["precond"] == 0 and list(opts["mp_grid"]) == [3, 3, 3]
+
+
+@pytest.mark.skipif(not os.path.isdir(REF), reason="Wannier90 source tree not present")
+def test_reads_reference_inputs():
+    d = G.load("pb")
+    lat, kp, opts = w90io.win_system(os.path.join(REF, "lead.win"))
+    np.testing.assert_allclose(lat, d["real_lattice"], atol=1e-12)
+    c = w90.setup(kpoints=kp, unit_cell_cart=lat, num_wann=4, iprint=0, search_shells=12)
+    K = len(kp)
+    nnkp = w90.w90_get_nnkp(c, K) - 1
+    gkpb = np.transpose(w90.w90_get_gkpb(c, K), (1, 2, 0))
+    m = w90io.read_mmn(os.path.join(REF, "lead.mmn"), nnkp, gkpb)
+    M = G.assemble_m(d, nnkp, gkpb)           # independent parser of the same file
+    np.testing.assert_array_equal(synth.to_math_m(m), M)
+    a = w90io.read_amn(os.path.join(REF, "lead.amn"))
+    np.testing.assert_array_equal(a.transpose(2, 0, 1), d["amn"])
+
+
+def test_chk_layout(tmp_path):
+    p = _small()
+    u = np.asfortranarray(np.broadcast_to(np.eye(5, dtype=complex)[:, :, None], (5, 5, 27)).copy())
+    cen = np.asfortranarray(np.arange(15, dtype=float).reshape(3, 5))
+    f = str(tmp_path / "x.chk")
+    w90io.write_chk(f, num_bands=5, lattice=p.real_lattice, kpts=p.kpoints, mp_grid=(3, 3, 3), nntot=p.nntot,
+                    num_wann=5, u=u, m=p.m, centres=cen, spreads=np.ones(5))
+    r = w90io.read_chk(f)
+    assert r["num_bands"] == 5 and r["num_kpts"] == 27 and r["nntot"] == p.nntot and r["num_wann"] == 5
+    assert r["checkpoint"] == "postwann"
+    np.testing.assert_allclose(r["real_lattice"], p.real_lattice)
+    np.testing.assert_allclose(r["recip_lattice"] @ p.real_lattice.T, 2 * np.pi * np.eye(3), atol=1e-12)
+    np.testing.assert_array_equal(r["m"], p.m)
+    np.testing.assert_array_equal(r["u"], u)
+    np.testing.assert_array_equal(r["centres"], cen)
+    # first record: 4-byte marker 33, 33-byte header, marker 33 (Fortran sequential)
+    raw = open(f, "rb").read(41)
+    assert struct.unpack("<i", raw[:4])[0] == 33 and struct.unpack("<i", raw[37:41])[0] == 33

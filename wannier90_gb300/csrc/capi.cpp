@@ -515,6 +515,11 @@ int w90g_profile_device(void* hv, double* d_m, double* d_u, int max_iters, doubl
   return 0;
 }
 
+double w90g_profile_exp_products(void* hv) {
+  Handle* h = H(hv);
+  return h->eng ? h->eng->last_exp_products() : 0.0;
+}
+
 const char* w90g_profile_kernel_name(int i) {
   return (i >= 0 && i < w90g::kPNum) ? w90g::kProfNames[i] : "";
 }

@@ -560,6 +560,8 @@ int Engine::wannierise_profiled(int max_iters, double* ms, int* cnt, std::string
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  W90G_CHECK(cudaMemcpy(&hs, hprobs_[0].st, sizeof(CtrlState), cudaMemcpyDeviceToHost));
+  last_exp_products_ = hs.exp_products;
   return rc;
 }
 

@@ -64,6 +64,7 @@ class Engine {
   void set_stream(cudaStream_t s) { user_stream_ = s; }
   cudaStream_t stream() const { return user_stream_ ? user_stream_ : own_stream_; }
   long long launches() const { return launches_; }
+  double last_exp_products() const { return last_exp_products_; }
 
  private:
   int alloc(std::string& err);
@@ -96,6 +97,7 @@ class Engine {
   cudaStream_t graph_stream_ = nullptr;
   std::string layout_key_;
   long long launches_ = 0;
+  double last_exp_products_ = 0.0;
 };
 
 int measure_fp64_peak(double* tflops, std::string& err);

@@ -311,9 +311,8 @@ constexpr int kTile = 32;
 __global__ void __launch_bounds__(256) k_grad(const Problem* __restrict__ probs, WorkMap wm) {
   __shared__ double2 sA[kTile * (kTile + 1)];   // A[j*(33)+i] = M(r0+i, c0+j)
   __shared__ double2 sT[kTile * (kTile + 1)];   // T[i*(33)+j] = M(c0+j, r0+i)
-  __shared__ double2 sdm[kTile], sdn[kTile];     // diag, rows / cols range
-  __shared__ double2 sim[kTile], sin_[kTile];    // 1/M_nn
-  __shared__ double sqm[kTile], sqn[kTile];      // q = wb*(ln + b.rave)
+  // per-column / per-row coefficients of the factored gradient (see below)
+  __shared__ double2 s_alpha[kTile], s_beta[kTile];
   __shared__ double red[256];
   int local;
   const int p = locate(wm, blockIdx.x, local);
@@ -346,54 +345,42 @@ __global__ void __launch_bounds__(256) k_grad(const Problem* __restrict__ probs,
       const int jj = e % kTile, ii = e / kTile;
       if (jj < nc && ii < nr) sT[ii * (kTile + 1) + jj] = Mb[(size_t)(r0 + ii) * W + c0 + jj];
     }
+    // G_mn += wb/2 (M_mn conj(M_nn) - conj(M_nm) M_mm) + (i/2)(M_mn q_n / M_nn + conj(M_nm) q_m / conj(M_mm))
+    //       = M_mn alpha_n + conj(M_nm) beta_m,
+    // alpha_n =  wb/2 conj(M_nn) + (i/2) q_n / M_nn,   beta_m = -wb/2 M_mm + (i/2) q_m / conj(M_mm)
+    // with q = wb (Im ln M_nn + b.rave_n)  (src/wannierise.F90:2366-2375, :2409-2417, :2499-2527)
     if (t < kTile) {
       if (t < nr) {
         const int m = r0 + t;
         const double2 d = Mb[(size_t)m * W + m];
-        sdm[t] = d;
         const double inv = 1.0 / (d.x * d.x + d.y * d.y);
-        sim[t] = cmk(d.x * inv, -d.y * inv);
         const double brn = bv[0] * rave[m] + bv[1] * rave[W + m] + bv[2] * rave[2 * W + m];
-        sqm[t] = w * (atan2(d.y, d.x) + brn);
+        const double q = w * (atan2(d.y, d.x) + brn);
+        // conj(1/M_mm) = d * inv ;  (i/2) q conj(1/M_mm) = (i/2) q inv (d.x + i d.y)
+        s_beta[t] = cmk(-0.5 * w * d.x - 0.5 * q * inv * d.y, -0.5 * w * d.y + 0.5 * q * inv * d.x);
       }
     } else if (t < 2 * kTile) {
       const int u = t - kTile;
       if (u < nc) {
         const int n = c0 + u;
         const double2 d = Mb[(size_t)n * W + n];
-        sdn[u] = d;
         const double inv = 1.0 / (d.x * d.x + d.y * d.y);
-        sin_[u] = cmk(d.x * inv, -d.y * inv);
         const double brn = bv[0] * rave[n] + bv[1] * rave[W + n] + bv[2] * rave[2 * W + n];
-        sqn[u] = w * (atan2(d.y, d.x) + brn);
+        const double q = w * (atan2(d.y, d.x) + brn);
+        // 1/M_nn = (d.x - i d.y) inv ;  (i/2) q / M_nn = (q inv / 2)(d.y + i d.x)
+        s_alpha[u] = cmk(0.5 * w * d.x + 0.5 * q * inv * d.y, -0.5 * w * d.y + 0.5 * q * inv * d.x);
       }
     }
     __syncthreads();
-    const double hw = 0.5 * w;
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int e = t + 256 * q;
+    for (int qq = 0; qq < 4; ++qq) {
+      const int e = t + 256 * qq;
       const int i = e % kTile, j = e / kTile;
       if (i < nr && j < nc) {
         const double2 mmn = sA[j * (kTile + 1) + i];    // M_mn
         const double2 mnm = sT[i * (kTile + 1) + j];    // M_nm
-        // cr_mn = M_mn conj(M_nn); cr_nm = M_nm conj(M_mm)
-        const double2 cr_mn = cmulc(mmn, sdn[j]);
-        const double2 cr_nm = cmulc(mnm, sdm[i]);
-        // crt_mn = M_mn / M_nn ; crt_nm = M_nm / M_mm
-        const double2 crt_mn = cmul(mmn, sin_[j]);
-        const double2 crt_nm = cmul(mnm, sim[i]);
-        // A[R]:  wb/2 (cr_mn - conj(cr_nm))
-        double gx = hw * (cr_mn.x - cr_nm.x);
-        double gy = hw * (cr_mn.y + cr_nm.y);
-        // -S[T]: (i/2) (crt_mn q_n + conj(crt_nm) q_m)
-        const double qn = sqn[j], qm = sqm[i];
-        const double sx = crt_mn.x * qn + crt_nm.x * qm;
-        const double sy = crt_mn.y * qn - crt_nm.y * qm;
-        gx -= 0.5 * sy;
-        gy += 0.5 * sx;
-        acc[q].x += gx;
-        acc[q].y += gy;
+        cfma(acc[qq], mmn, s_alpha[j]);
+        cfmac(acc[qq], mnm, s_beta[i]);
       }
     }
   }
@@ -572,7 +559,7 @@ __device__ const double kInvFact[17] = {
     7.6471637318198164e-13, 4.7794773323873853e-14};
 
 __device__ double2* cta_expm(double2* X, double2* Y2, double2* Y3, double2* Y4, double2* R,
-                             double2* T, int W, double* red) {
+                             double2* T, int W, double* red, double* cost_out) {
   const int WW = W * W;
   double colmax = 0.0;
   for (int j = threadIdx.x; j < W; j += blockDim.x) {
@@ -603,6 +590,7 @@ __device__ double2* cta_expm(double2* X, double2* Y2, double2* Y3, double2* Y4, 
       js = j;
     }
   }
+  *cost_out = best;
   const double sc = ldexp(1.0, -js);
   for (int e = threadIdx.x; e < WW; e += blockDim.x) X[e] = cscale(X[e], sc);
   __syncthreads();
@@ -691,7 +679,9 @@ __global__ void __launch_bounds__(256) k_exp_u(const Problem* __restrict__ probs
     for (int e = threadIdx.x; e < WW; e += blockDim.x) X[e] = cscale(Dk[e], s);
   }
   __syncthreads();
-  double2* E = cta_expm(X, Y2, Y3, Y4, R, T, W, red);
+  double cost = 0.0;
+  double2* E = cta_expm(X, Y2, Y3, Y4, R, T, W, red, &cost);
+  if (threadIdx.x == 0) atomicAdd(&st->exp_products, cost + 1.0);
   // E is R or T; reuse X/Y2 for U
   double2* dUk = P.dU + (size_t)k * WW;
   const int cur = st->cur;

@@ -89,6 +89,7 @@ struct CtrlState {
   double om_invariant;
   Spread wann, old, slot[2];   // slot[0] = trial spread, slot[1] = optimal-step spread
   double history[kMaxConvWindow];
+  double exp_products;   // W^3 complex products spent in exp(s D) and U dU (work counter)
 };
 
 // wann_control_type subset used on device (src/wannier90_types.F90:170-192)

@@ -1,0 +1,273 @@
+"""Wannier90 file formats used around the wannierisation path.
+
+Readers: ``.win`` (keywords and blocks; src/readwrite.F90 tokenizer conventions),
+``.mmn`` / ``.amn`` (src/overlap.F90:234-366), ``.eig``; writers for the same (used
+to export synthetic problems that the reference ``wannier90.x`` can read) and the
+unformatted checkpoint ``.chk`` (src/wannier90_readwrite.F90:2278-2373).
+
+Arrays follow the library layouts (Fortran order):
+  m   complex128 (num_bands, num_bands, nntot, num_kpts)
+  a   complex128 (num_bands, num_proj, num_kpts)
+  u   complex128 (num_wann, num_wann, num_kpts)
+  eig float64    (num_bands, num_kpts)
+"""
+from __future__ import annotations
+
+import datetime
+import math
+import re
+import struct
+
+import numpy as np
+
+# src/constants.F90:109 (CODATA 2006, the default build)
+BOHR_ANGSTROM = 0.52917720859
+
+
+# --------------------------------------------------------------------------------
+# .win
+# --------------------------------------------------------------------------------
+def _strip(line):
+    for c in "!#":
+        if c in line:
+            line = line[: line.index(c)]
+    return line.strip()
+
+
+def read_win(path):
+    """Return (keywords: dict[str, str], blocks: dict[str, list[str]]), keys lower-case."""
+    lines = [_strip(l) for l in open(path)]
+    lines = [l for l in lines if l]
+    kw, blocks = {}, {}
+    i = 0
+    while i < len(lines):
+        low = lines[i].lower()
+        if low.startswith("begin"):
+            name = low.split()[1]
+            body = []
+            i += 1
+            while i < len(lines) and not lines[i].lower().startswith("end"):
+                body.append(lines[i])
+                i += 1
+            blocks[name] = body
+        else:
+            m = re.match(r"([A-Za-z_0-9]+)\s*[=:\s]\s*(.*)", lines[i])
+            if m:
+                kw[m.group(1).lower()] = m.group(2).strip()
+        i += 1
+    return kw, blocks
+
+
+def _fnum(s):
+    return float(s.lower().replace("d", "e"))
+
+
+def _flag(s):
+    return s.strip().lower().lstrip(".").startswith("t")
+
+
+def win_system(path):
+    """Lattice (rows a_i, Angstrom), k-points (fractional), mp_grid and the wannierise
+    keywords of a .win file, as library options."""
+    kw, blocks = read_win(path)
+    cell = blocks["unit_cell_cart"]
+    scale = 1.0
+    if cell[0].lower().startswith(("bohr", "ang")):
+        scale = BOHR_ANGSTROM if cell[0].lower().startswith("bohr") else 1.0
+        cell = cell[1:]
+    lattice = np.array([[_fnum(x) for x in r.split()[:3]] for r in cell]) * scale
+    kpts = np.array([[_fnum(x) for x in r.split()[:3]] for r in blocks["kpoints"]])
+    opts = {}
+    ints = ("num_wann", "num_bands", "num_iter", "num_cg_steps", "conv_window", "search_shells",
+            "iprint", "num_print_cycles", "conv_noise_num")
+    reals = ("conv_tol", "trial_step", "fixed_step", "conv_noise_amp", "kmesh_tol")
+    bools = ("precond", "guiding_centres", "gamma_only")
+    for k in ints:
+        if k in kw:
+            opts[k] = int(kw[k].split()[0])
+    for k in reals:
+        if k in kw:
+            opts[k] = _fnum(kw[k].split()[0])
+    for k in bools:
+        if k in kw:
+            opts[k] = int(_flag(kw[k]))
+    if "mp_grid" in kw:
+        opts["mp_grid"] = np.array([int(x) for x in re.split(r"[\s,]+", kw["mp_grid"])[:3]], dtype=np.int32)
+    return lattice, kpts, opts
+
+
+def write_win(path, lattice, kpts, mp_grid, num_wann, num_bands=None, **keywords):
+    with open(path, "w") as f:
+        f.write("num_wann = %d\n" % num_wann)
+        f.write("num_bands = %d\n" % (num_bands or num_wann))
+        for k, v in keywords.items():
+            f.write("%s = %s\n" % (k, v))
+        f.write("mp_grid : %d %d %d\n" % tuple(mp_grid))
+        f.write("begin unit_cell_cart\nang\n")
+        for r in lattice:
+            f.write("  %.12f %.12f %.12f\n" % tuple(r))
+        f.write("end unit_cell_cart\nbegin kpoints\n")
+        for k in kpts:
+            f.write("  %.12f %.12f %.12f\n" % tuple(k))
+        f.write("end kpoints\n")
+
+
+# --------------------------------------------------------------------------------
+# .mmn / .amn / .eig   (src/overlap.F90:234-366)
+# --------------------------------------------------------------------------------
+def read_mmn(path, nnlist, nncell):
+    """Overlaps placed at (k, nn) by matching each block's (k2, G) with the k-mesh tables,
+    as overlap_read does.  nnlist (K,B) 0-based, nncell (K,B,3)."""
+    nnlist = np.asarray(nnlist)
+    nncell = np.asarray(nncell)
+    with open(path) as f:
+        f.readline()
+        nb, nk, nntot = (int(x) for x in f.readline().split())
+        if nnlist.shape != (nk, nntot):
+            raise ValueError(".mmn has not the right number of k-points / nearest neighbours")
+        m = np.zeros((nb, nb, nntot, nk), dtype=np.complex128, order="F")
+        data = np.loadtxt(f, ndmin=2) if False else None
+        for _ in range(nk * nntot):
+            head = f.readline().split()
+            k, k2 = int(head[0]) - 1, int(head[1]) - 1
+            g = tuple(int(x) for x in head[2:5])
+            vals = np.array([[float(x) for x in f.readline().split()[:2]] for _ in range(nb * nb)])
+            blk = (vals[:, 0] + 1j * vals[:, 1]).reshape(nb, nb, order="F")   # (m, n), m fastest
+            hit = [b for b in range(nntot) if nnlist[k, b] == k2 and tuple(nncell[k, b]) == g]
+            if len(hit) != 1:
+                raise ValueError("Error reading %s: neighbour not found / not unique" % path)
+            m[:, :, hit[0], k] = blk
+    return m
+
+
+def write_mmn(path, m, nnlist, nncell, comment="written by wannier90_gb300"):
+    nb, _, nntot, nk = m.shape
+    with open(path, "w") as f:
+        f.write(comment[:60] + "\n")
+        f.write("%12d%12d%12d\n" % (nb, nk, nntot))
+        for k in range(nk):
+            for b in range(nntot):
+                g = nncell[k, b]
+                f.write("%5d%5d%5d%5d%5d\n" % (k + 1, nnlist[k, b] + 1, g[0], g[1], g[2]))
+                blk = m[:, :, b, k].reshape(-1, order="F")
+                for z in blk:
+                    f.write("%18.12f%18.12f\n" % (z.real, z.imag))
+
+
+def read_amn(path):
+    with open(path) as f:
+        f.readline()
+        nb, nk, npj = (int(x) for x in f.readline().split())
+        a = np.zeros((nb, npj, nk), dtype=np.complex128, order="F")
+        for _ in range(nb * npj * nk):
+            p = f.readline().split()
+            a[int(p[0]) - 1, int(p[1]) - 1, int(p[2]) - 1] = float(p[3]) + 1j * float(p[4])
+    return a
+
+
+def write_amn(path, a, comment="written by wannier90_gb300"):
+    nb, npj, nk = a.shape
+    with open(path, "w") as f:
+        f.write(comment[:60] + "\n")
+        f.write("%12d%12d%12d\n" % (nb, nk, npj))
+        for k in range(nk):
+            for n in range(npj):
+                for mm in range(nb):
+                    z = a[mm, n, k]
+                    f.write("%5d%5d%5d%18.12f%18.12f\n" % (mm + 1, n + 1, k + 1, z.real, z.imag))
+
+
+def read_eig(path, num_bands, num_kpts):
+    e = np.zeros((num_bands, num_kpts), order="F")
+    for line in open(path):
+        p = line.split()
+        if len(p) >= 3:
+            e[int(p[0]) - 1, int(p[1]) - 1] = float(p[2])
+    return e
+
+
+def write_eig(path, eig):
+    nb, nk = eig.shape
+    with open(path, "w") as f:
+        for k in range(nk):
+            for n in range(nb):
+                f.write("%5d%5d%18.12f\n" % (n + 1, k + 1, eig[n, k]))
+
+
+# --------------------------------------------------------------------------------
+# .chk  (unformatted sequential records, 4-byte record markers as gfortran writes them;
+# src/wannier90_readwrite.F90:2336-2366)
+# --------------------------------------------------------------------------------
+def _rec(f, payload: bytes):
+    n = struct.pack("<i", len(payload))
+    f.write(n + payload + n)
+
+
+def recip_lattice(lattice):
+    a = np.asarray(lattice, dtype=np.float64)
+    cof = np.stack([np.cross(a[1], a[2]), np.cross(a[2], a[0]), np.cross(a[0], a[1])])
+    return 2.0 * math.pi * cof / float(np.dot(a[0], cof[0]))
+
+
+def write_chk(path, *, num_bands, lattice, kpts, mp_grid, nntot, num_wann, u, m, centres, spreads,
+              exclude_bands=(), checkpoint="postwann", header=None):
+    """centres (3, num_wann) Angstrom; u (nw,nw,nk); m (nw,nw,nntot,nk)."""
+    if header is None:
+        now = datetime.datetime.now()
+        header = "written on " + now.strftime("%d%b%Y") + " at " + now.strftime("%H:%M:%S")
+    header = header.ljust(33)[:33]
+    lat = np.asarray(lattice, dtype=np.float64)
+    with open(path, "wb") as f:
+        _rec(f, header.encode())
+        _rec(f, struct.pack("<i", num_bands))
+        _rec(f, struct.pack("<i", len(exclude_bands)))
+        _rec(f, np.asarray(exclude_bands, dtype="<i4").tobytes())
+        _rec(f, np.asarray(lat, dtype="<f8").reshape(-1, order="F").tobytes())      # real_lattice(i,j) i fastest
+        _rec(f, np.asarray(recip_lattice(lat), dtype="<f8").reshape(-1, order="F").tobytes())
+        _rec(f, struct.pack("<i", len(kpts)))
+        _rec(f, np.asarray(mp_grid, dtype="<i4").tobytes())
+        _rec(f, np.asarray(kpts, dtype="<f8").reshape(-1).tobytes())                # kpt_latt(3, nk)
+        _rec(f, struct.pack("<i", nntot))
+        _rec(f, struct.pack("<i", num_wann))
+        _rec(f, checkpoint.ljust(20)[:20].encode())
+        _rec(f, struct.pack("<i", 0))                                               # have_disentangled = F
+        _rec(f, np.asarray(u, dtype="<c16").reshape(-1, order="F").tobytes())
+        _rec(f, np.asarray(m, dtype="<c16").reshape(-1, order="F").tobytes())
+        _rec(f, np.asarray(centres, dtype="<f8").reshape(-1, order="F").tobytes())
+        _rec(f, np.asarray(spreads, dtype="<f8").tobytes())
+
+
+def read_chk(path):
+    """Parse a .chk written by write_chk (or by wannier90.x for isolated bands)."""
+    recs = []
+    with open(path, "rb") as f:
+        while True:
+            h = f.read(4)
+            if not h:
+                break
+            (n,) = struct.unpack("<i", h)
+            recs.append(f.read(n))
+            f.read(4)
+    i = 0
+    out = {"header": recs[0].decode(errors="replace")}
+    out["num_bands"] = struct.unpack("<i", recs[1])[0]
+    nex = struct.unpack("<i", recs[2])[0]
+    out["exclude_bands"] = np.frombuffer(recs[3], "<i4").copy()
+    i = 4
+    out["real_lattice"] = np.frombuffer(recs[i], "<f8").reshape(3, 3, order="F").copy(); i += 1
+    out["recip_lattice"] = np.frombuffer(recs[i], "<f8").reshape(3, 3, order="F").copy(); i += 1
+    nk = struct.unpack("<i", recs[i])[0]; i += 1
+    out["mp_grid"] = np.frombuffer(recs[i], "<i4").copy(); i += 1
+    out["kpts"] = np.frombuffer(recs[i], "<f8").reshape(nk, 3).copy(); i += 1
+    nntot = struct.unpack("<i", recs[i])[0]; i += 1
+    nw = struct.unpack("<i", recs[i])[0]; i += 1
+    out["checkpoint"] = recs[i].decode().strip(); i += 1
+    have_dis = struct.unpack("<i", recs[i])[0]; i += 1
+    if have_dis:
+        raise ValueError("disentangled checkpoints are not supported")
+    out["u"] = np.frombuffer(recs[i], "<c16").reshape(nw, nw, nk, order="F").copy(); i += 1
+    out["m"] = np.frombuffer(recs[i], "<c16").reshape(nw, nw, nntot, nk, order="F").copy(); i += 1
+    out["centres"] = np.frombuffer(recs[i], "<f8").reshape(3, nw, order="F").copy(); i += 1
+    out["spreads"] = np.frombuffer(recs[i], "<f8").copy()
+    out.update(num_kpts=nk, nntot=nntot, num_wann=nw, num_exclude=nex)
+    return out
