@@ -191,6 +191,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-iters", type=int, default=6)
     ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--profile-case", type=int, default=0,
+                    help="run one solve capped at this many iterations and exit (small case for ncu)")
     ap.add_argument("--precision", default="tensor", choices=["tensor", "fp64"],
                     help="tensor: M update on tcgen05 tensor cores (exact BF16 slicing, FP64-accurate); "
                          "fp64: every product on the FP64 pipe")
@@ -233,6 +235,15 @@ def main():
     torch.cuda.synchronize()
     m0, u0 = m_dev.clone(), u_dev.clone()
     m_work, u_work = torch.empty_like(m0), torch.empty_like(u0)
+
+    if args.profile_case > 0:
+        hp = w90.setup(kpoints=p.kpoints, unit_cell_cart=p.real_lattice, num_wann=W,
+                       **dict(opts, num_iter=args.profile_case))
+        w90.check(hp, w90.w90_wannierise_device(hp, m0.clone().data_ptr(), u0.clone().data_ptr()), "profile case")
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": args.profile_case, "workload": args.workload,
+                          "spread": float(w90.w90_get_log(hp, args.profile_case + 1)[-1][3])}))
+        return 0
 
     def device_step():
         with torch.cuda.stream(stream):
