@@ -43,7 +43,27 @@ except Exception:
 WORKLOADS = {
     "fcc10_w32": dict(cfg="fcc10_w32", conv_tol=1e-10, conv_window=5, num_iter=20000),
     "sc4_w8": dict(cfg="sc4_w8", conv_tol=1e-10, conv_window=-1, num_iter=200),
+    # 256 independent problems, W ~ U{4,8,...,64}, k-mesh ~ U{3^3,4^3,6^3,8^3}, sc a ~ U[3,7] A,
+    # nntot 6, 300 iterations each, solved together
+    "batch256": dict(cfg=None, conv_tol=1e-10, conv_window=-1, num_iter=300, nprob=256),
 }
+
+
+def batch_params(i):
+    """Shape of problem i of the batched workload (seeded by its index)."""
+    import numpy as np
+    rng = np.random.Generator(np.random.PCG64(1000003 * (i + 1)))
+    W = int(rng.choice(np.arange(4, 65, 4)))
+    n = int(rng.choice([3, 4, 6, 8]))
+    a = float(rng.uniform(3.0, 7.0))
+    return dict(kind="sc", a=a, mp=(n, n, n), num_wann=W, rmax=2, eps=0.3)
+
+
+def _gen_batch_problem(i):
+    os.environ["OPENBLAS_NUM_THREADS"] = "1"
+    from wannier90_gb300 import synth
+    p = synth.make_problem(**batch_params(i), seed=i)
+    return i, p
 
 
 def _env_rank():
@@ -178,6 +198,92 @@ def run_reference_arm(args, wl):
     return 0
 
 
+def run_batch(args, wl):
+    """Batched workload: all problems solved together in one engine launch sequence per
+    M-update variant; one step = one batch solve (300 iterations of every problem)."""
+    import numpy as np
+    import torch
+
+    from wannier90_gb300 import autotune
+    from wannier90_gb300 import library as w90
+
+    torch.cuda.set_device(0)
+    n = args.batch_size or wl["nprob"]
+    procs = min(os.cpu_count() or 1, 16)
+    with mp.get_context("spawn").Pool(procs) as pool:
+        probs = [p for _, p in sorted(pool.map(_gen_batch_problem, range(n)))]
+    tune = {} if args.precision == "fp64" else autotune.table([p.num_wann for p in probs])
+    handles, m0s, u0s = [], [], []
+    for p in probs:
+        tensor = 0 if args.precision == "fp64" else tune[p.num_wann]["tensor"]
+        h = w90.setup(kpoints=p.kpoints, unit_cell_cart=p.real_lattice, num_wann=p.num_wann,
+                      num_iter=wl["num_iter"], conv_window=-1, iprint=0, gpu_tensor=tensor)
+        m = torch.from_numpy(p.m.reshape(-1, order="F").view(np.float64).copy()).cuda()
+        u = torch.from_numpy(p.a.reshape(-1, order="F").view(np.float64).copy()).cuda()
+        w90.check(h, w90.w90_project_overlap_device(h, m.data_ptr(), u.data_ptr()), "projection")
+        handles.append(h)
+        m0s.append(m)
+        u0s.append(u)
+    torch.cuda.synchronize()
+    mw = [torch.empty_like(m) for m in m0s]
+    uw = [torch.empty_like(u) for u in u0s]
+
+    def step():
+        for a, b in zip(mw, m0s):
+            a.copy_(b)
+        for a, b in zip(uw, u0s):
+            a.copy_(b)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        ierr = w90.w90_wannierise_batch_device(handles, [x.data_ptr() for x in mw], [x.data_ptr() for x in uw])
+        torch.cuda.synchronize()
+        if any(e > 0 for e in ierr):
+            raise RuntimeError("batch failed: %s" % [h.last_error() for h in handles if h.last_error()])
+        return time.perf_counter() - t
+
+    for _ in range(args.warmup):
+        step()
+    clocks = ClockSampler(0)
+    clocks.start()
+    ts = [step() for _ in range(args.steps)]
+    clk = clocks.stop()
+    t_step = statistics.mean(ts)
+    # e2e: host buffers, H2D of every problem's M and U, D2H of the results
+    mh = [x.cpu().pin_memory() for x in m0s]
+    uh = [x.cpu().pin_memory() for x in u0s]
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for a, b in zip(mw, mh):
+        a.copy_(b, non_blocking=True)
+    for a, b in zip(uw, uh):
+        a.copy_(b, non_blocking=True)
+    torch.cuda.synchronize()
+    w90.w90_wannierise_batch_device(handles, [x.data_ptr() for x in mw], [x.data_ptr() for x in uw])
+    for a, b in zip(mh, mw):
+        a.copy_(b, non_blocking=True)
+    for a, b in zip(uh, uw):
+        a.copy_(b, non_blocking=True)
+    torch.cuda.synchronize()
+    t_e2e = time.perf_counter() - t
+    nbytes = sum(x.numel() * 8 for x in m0s) + sum(x.numel() * 8 for x in u0s)
+    ws = [p.num_wann for p in probs]
+    line = {
+        "metric": METRIC, "value": n / t_step, "unit": "solves/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded tight-binding generator)",
+        "config": {"workload": args.workload, "problems": n, "iterations_each": wl["num_iter"],
+                   "num_wann": "U{4,...,64}", "kmesh": "U{3^3,4^3,6^3,8^3}", "lattice": "sc a~U[3,7]",
+                   "tensor_problems": sum(1 for p in probs if tune.get(p.num_wann, {}).get("tensor", 0)),
+                   "autotune": {str(k): v["tensor"] for k, v in tune.items()},
+                   "total_state_MB": nbytes >> 20, "l2": "inputs larger than L2"},
+        "e2e": {"value": n / t_e2e, "unit": "solves/s", "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
+        "gpu_launches": None, "roofline": None, "cpu_baseline": None, "clocks": clk,
+        "widths": {"min": min(ws), "max": max(ws), "mean": float(np.mean(ws))},
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -191,6 +297,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-iters", type=int, default=6)
     ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--batch-size", type=int, default=0, help="problems in the batched workload (default 256)")
     ap.add_argument("--profile-case", type=int, default=0,
                     help="run one solve capped at this many iterations and exit (small case for ncu)")
     ap.add_argument("--precision", default="tensor", choices=["tensor", "fp64"],
@@ -203,6 +310,8 @@ def main():
             args.assume_iters = KNOWN_ITERS.get(args.workload, 1000)
         return run_reference_arm(args, wl)
 
+    if wl.get("nprob"):
+        return run_batch(args, wl)
     rank, local_rank, world = _env_rank()
     import numpy as np
     import torch

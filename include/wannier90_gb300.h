@@ -97,6 +97,14 @@ int w90g_get_log_centres(void* handle, double* rows, int max_rows);
  * the current device, same layouts); results are written back to them on the device. */
 void w90g_wannierise_device(void* handle, double* d_m_matrix, double* d_u_matrix, int* ierr);
 void w90g_project_overlap_device(void* handle, double* d_m_matrix, double* d_u_matrix, int* ierr);
+/* Batched form: nprob independent problems, each set up on its own handle
+ * (cinput_setopt), with device buffers d_m[i], d_u[i] (layouts as above), solved together:
+ * problems are grouped by M-update variant (tensor path at padded width 8/16/32 when the
+ * handle sets gpu_tensor and num_wann <= 32, FP64 path otherwise); each group runs as one
+ * engine whose captured iteration covers all its problems, groups run concurrently on
+ * their own streams.  Per-problem status in ierr[i]; results via the handles' getters.
+ * No counterpart in the reference (which solves one problem per library call). */
+void w90g_wannierise_batch_device(void** handles, int nprob, double** d_m, double** d_u, int* ierr);
 /* Run the engine's work on a caller-provided cudaStream_t (NULL = the engine's own). */
 void w90g_set_stream(void* handle, void* cuda_stream);
 /* Number of engine kernels launched by the last call on this handle. */

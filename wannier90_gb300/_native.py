@@ -42,6 +42,8 @@ SIGNATURES = [
     ("w90g_wannierise_device", None, [C.c_void_p, C.c_void_p, C.c_void_p, _c_int_p]),
     ("w90g_project_overlap_device", None, [C.c_void_p, C.c_void_p, C.c_void_p, _c_int_p]),
     ("w90g_set_stream", None, [C.c_void_p, C.c_void_p]),
+    ("w90g_wannierise_batch_device", None,
+     [C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), _c_int_p]),
     ("w90g_kernel_launches", C.c_longlong, [C.c_void_p]),
     ("w90g_profile_device", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, _c_double_p, _c_int_p]),
     ("w90g_profile_kernel_name", C.c_char_p, [C.c_int]),

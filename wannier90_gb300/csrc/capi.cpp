@@ -16,6 +16,7 @@
 #include <map>
 #include <memory>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/wannier90_gb300.h"
@@ -529,6 +530,90 @@ double w90g_measure_fp64_peak(void) {
   std::string err;
   if (w90g::measure_fp64_peak(&t, err)) return -1.0;
   return t;
+}
+
+// Batched form: independent problems (each set up on its own handle) solved together.
+// Problems are grouped by the M-update variant their width selects (tensor path with
+// padded width 8 / 16 / 32 when requested and W <= 32, FP64 path otherwise); each group
+// is one engine whose iteration graph covers all of its problems, and the groups run
+// concurrently on their own streams.
+void w90g_wannierise_batch_device(void** handles, int nprob, double** d_m, double** d_u, int* ierr) {
+  struct Group {
+    std::vector<int> idx;
+    std::vector<ProblemSpec> specs;
+    std::unique_ptr<Engine> eng;
+    cudaStream_t stream = nullptr;
+    int rc = 0;
+    std::string err;
+  };
+  std::map<int, Group> groups;   // key: 0 fp64, 8/16/32 tensor width class
+  for (int i = 0; i < nprob; ++i) {
+    Handle* h = H(handles[i]);
+    ierr[i] = 0;
+    if (!h->setup_complete || !d_m[i] || !d_u[i]) {
+      ierr[i] = fail(h, 1, "batch: handle not set up or buffers missing");
+      continue;
+    }
+    ProblemSpec s;
+    build_spec(h, s);
+    int key = 0;
+    if (s.tensor && s.W <= 32) key = s.W <= 8 ? 8 : (s.W <= 16 ? 16 : 32);
+    groups[key].idx.push_back(i);
+    groups[key].specs.push_back(s);
+  }
+  std::vector<std::thread> threads;
+  for (auto& kv : groups) {
+    Group* g = &kv.second;
+    threads.emplace_back([g, d_m, d_u]() {
+      g->eng.reset(new Engine());
+      if (cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        g->rc = 1;
+        g->err = "batch: stream creation failed";
+        return;
+      }
+      g->eng->set_stream(g->stream);
+      g->rc = g->eng->setup(g->specs, g->err);
+      for (size_t j = 0; j < g->idx.size() && !g->rc; ++j)
+        g->rc = g->eng->load((int)j, d_m[g->idx[j]], d_u[g->idx[j]], cudaMemcpyDeviceToDevice, g->err);
+      if (!g->rc) g->rc = g->eng->wannierise(g->err);
+      if (g->rc == 0 || g->rc == 1) {
+        for (size_t j = 0; j < g->idx.size(); ++j) {
+          std::string e2;
+          int rc2 = g->eng->store((int)j, d_m[g->idx[j]], d_u[g->idx[j]], cudaMemcpyDeviceToDevice, e2);
+          if (rc2 && !g->rc) {
+            g->rc = rc2;
+            g->err = e2;
+          }
+        }
+      }
+    });
+  }
+  for (auto& t : threads) t.join();
+  for (auto& kv : groups) {
+    Group& g = kv.second;
+    for (size_t j = 0; j < g.idx.size(); ++j) {
+      Handle* h = H(handles[g.idx[j]]);
+      if (g.rc && g.rc != 1) {
+        ierr[g.idx[j]] = fail(h, g.rc, g.err);
+        continue;
+      }
+      const auto& r = g.eng->result((int)j);
+      h->omega[0] = r.spread.om_i;
+      h->omega[1] = r.spread.om_d;
+      h->omega[2] = r.spread.om_od;
+      h->omega[3] = r.spread.om_tot;
+      h->centres = r.centres;
+      h->spreads = r.spreads;
+      h->log = r.log;
+      h->log_centres = r.log_centres;
+      h->niter = r.niter;
+      h->have_result = true;
+      if (r.error) ierr[g.idx[j]] = fail(h, 1, "non-finite spread in the engine");
+      else if (!(r.unitarity_err <= 1e-5)) ierr[g.idx[j]] = fail(h, 1, "wann_check_unitarity: unitariety of final U violated");
+    }
+    g.eng.reset();
+    if (g.stream) cudaStreamDestroy(g.stream);
+  }
 }
 
 long long w90g_kernel_launches(void* hv) {

@@ -181,6 +181,19 @@ def w90_project_overlap_device(common: LibCommon, m_ptr: int, u_ptr: int) -> int
     return ierr.value
 
 
+def w90_wannierise_batch_device(commons, m_ptrs, u_ptrs):
+    """Solve several problems (one LibCommon each) together on the GPU; device buffers.
+    Returns the list of per-problem ierr."""
+    n = len(commons)
+    L = commons[0]._L
+    hs = (C.c_void_p * n)(*[c._h for c in commons])
+    ms = (C.c_void_p * n)(*[C.c_void_p(p) for p in m_ptrs])
+    us = (C.c_void_p * n)(*[C.c_void_p(p) for p in u_ptrs])
+    ierr = (C.c_int * n)()
+    L.w90g_wannierise_batch_device(hs, n, ms, us, ierr)
+    return list(ierr)
+
+
 def w90_get_centres(common: LibCommon, num_wann: int) -> np.ndarray:
     """Wannier centres as (3, num_wann) (Fortran layout, Angstrom)."""
     out = np.zeros((3, num_wann), dtype=np.float64, order="F")
