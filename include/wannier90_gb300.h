@@ -99,8 +99,8 @@ void w90g_wannierise_device(void* handle, double* d_m_matrix, double* d_u_matrix
 void w90g_project_overlap_device(void* handle, double* d_m_matrix, double* d_u_matrix, int* ierr);
 /* Batched form: nprob independent problems, each set up on its own handle
  * (cinput_setopt), with device buffers d_m[i], d_u[i] (layouts as above), solved together:
- * problems are grouped by M-update variant (tensor path at padded width 8/16/32 when the
- * handle sets gpu_tensor and num_wann <= 32, FP64 path otherwise); each group runs as one
+ * problems are grouped by M-update variant (tensor path at padded width 8/16/32/64/128 when
+ * the handle sets gpu_tensor, FP64 path otherwise); each group runs as one
  * engine whose captured iteration covers all its problems, groups run concurrently on
  * their own streams.  Per-problem status in ierr[i]; results via the handles' getters.
  * No counterpart in the reference (which solves one problem per library call). */
@@ -121,6 +121,14 @@ const char* w90g_profile_kernel_name(int i);
 double w90g_profile_exp_products(void* handle);
 /* FP64 FMA throughput of the current device in TFLOP/s (dependent-chain probe). */
 double w90g_measure_fp64_peak(void);
+/* Wigner-Seitz points of the Born-von Karman supercell used by the preconditioner
+ * (replaces hamiltonian_wigner_seitz, src/hamiltonian.F90:689-853, as called from
+ * hamiltonian_setup for wann_main, src/wannierise.F90:269-274).  Host only.
+ * real_lattice33: rows a_1..a_3 (Angstrom); search_size3: ws_search_size (default 2);
+ * irvec_out [max_pts][3], ndegen_out [max_pts].  Returns nrpts (> max_pts: only the count
+ * is returned), or -1 when the sum rule fails. */
+int w90g_ws_vectors(const double* real_lattice33, const int* mp_grid3, const int* search_size3,
+                    double ws_distance_tol, int* irvec_out, int* ndegen_out, int max_pts);
 /* Loewdin projection (as w90g_project_overlap_device) that allocates no device memory.
  * No counterpart in the reference.  For callers that cannot call cudaMalloc where they
  * project: e.g. a DFT code whose device memory all belongs to its own pool allocator.

@@ -329,6 +329,64 @@ def wann_domega(M, km):
 
 
 # ---------------------------------------------------------------------------
+# preconditioner (src/wannierise.F90:1256-1368) and its Wigner-Seitz grid
+# ---------------------------------------------------------------------------
+def ws_vectors(real_lattice, mp_grid, ws_search_size=(2, 2, 2), ws_distance_tol=1.0e-5):
+    """hamiltonian_wigner_seitz (src/hamiltonian.F90:689-853): lattice points n of the
+    Born-von Karman supercell's Wigner-Seitz cell, in the reference's loop order
+    (n1 outer, n3 inner), with degeneracies.  Returns (irvec[nrpts,3] int, ndegen[nrpts])."""
+    A = np.asarray(real_lattice, dtype=np.float64)
+    metric = A @ A.T                                         # utility_metric
+    mp = np.asarray(mp_grid, dtype=np.int64)
+    s = np.asarray(ws_search_size, dtype=np.int64)
+    rng = [np.arange(-s[i] * mp[i], s[i] * mp[i] + 1) for i in range(3)]
+    n = np.stack(np.meshgrid(*rng, indexing="ij"), axis=-1).reshape(-1, 3)
+    sh = [np.arange(-s[i] - 1, s[i] + 2) for i in range(3)]
+    shifts = np.stack(np.meshgrid(*sh, indexing="ij"), axis=-1).reshape(-1, 3)
+    centre = (len(shifts) - 1) // 2                          # i1 = i2 = i3 = 0
+    tol2 = ws_distance_tol ** 2
+    irvec, ndegen = [], []
+    for c0 in range(0, len(n), 4096):
+        nd = (n[c0:c0 + 4096, None, :] - shifts[None, :, :] * mp).astype(np.float64)
+        dist = np.einsum("psi,ij,psj->ps", nd, metric, nd)
+        dmin = dist.min(axis=1)
+        keep = np.abs(dist[:, centre] - dmin) < tol2
+        deg = (np.abs(dist - dmin[:, None]) < tol2).sum(axis=1)
+        irvec.append(n[c0:c0 + 4096][keep])
+        ndegen.append(deg[keep])
+    irvec = np.concatenate(irvec).astype(np.int64)
+    ndegen = np.concatenate(ndegen).astype(np.int64)
+    tot = float(np.sum(1.0 / ndegen))                        # sum rule (:829-852)
+    if abs(tot - float(np.prod(mp))) > EPS8:
+        raise RuntimeError("hamiltonian_wigner_seitz: error in finding Wigner-Seitz points")
+    return irvec, ndegen
+
+
+def precond_setup(real_lattice, kpt_latt, mp_grid):
+    """The tables wann_main builds for precond=T (src/wannierise.F90:269-300):
+    irvec/ndegen from hamiltonian_setup and k_to_r(k, R) = exp(-i 2pi k.R)."""
+    irvec, ndegen = ws_vectors(real_lattice, mp_grid)
+    rdotk = TWOPI * np.asarray(kpt_latt, dtype=np.float64) @ irvec.T.astype(np.float64)
+    # the filter's |R|^2 uses matmul(real_lattice, irvec) exactly as the reference
+    # (:1341), i.e. (a_1.n, a_2.n, a_3.n) with a_i the rows of real_lattice
+    rvec = irvec.astype(np.float64) @ np.asarray(real_lattice, dtype=np.float64).T
+    return {"irvec": irvec, "ndegen": ndegen, "k_to_r": np.exp(-1j * rdotk),
+            "r2": (rvec * rvec).sum(axis=1)}
+
+
+def precond_search_direction(cdodq, om_tot, pc):
+    """precond_search_direction, optimisation >= 3 form (src/wannierise.F90:1256-1368):
+    k -> R, filter by 1/(1 + R^2/alpha) with alpha = 10*om_tot/num_wann, R -> k."""
+    K, W, _ = cdodq.shape
+    k_to_r = pc["k_to_r"]
+    cr = np.einsum("kmn,kr->rmn", cdodq, k_to_r) / K         # :1317-1320
+    alpha = 10.0 * om_tot / W                                # :1339
+    cr = cr * (1.0 / (1.0 + pc["r2"] / alpha))[:, None, None]
+    cr = cr / pc["ndegen"][:, None, None].astype(np.float64)  # :1347-1349
+    return np.einsum("rmn,kr->kmn", cr, k_to_r.conj())       # :1350-1351
+
+
+# ---------------------------------------------------------------------------
 # wann_main  (src/wannierise.F90:48-1752)
 # ---------------------------------------------------------------------------
 @dataclass
@@ -343,6 +401,7 @@ class WannControl:
     lfixstep: bool = False
     conv_noise_amp: float = -1.0
     conv_noise_num: int = 3
+    precond: bool = False
 
 
 @dataclass
@@ -384,8 +443,11 @@ def new_u_and_m(cdq, U, M, nnlist):
     return Unew, Mnew
 
 
-def wann_main(M, U, km, ctl: WannControl, record=True):
-    """Restatement of wann_main for precond=F, guiding_centres=F, SLWF=F, no sitesym."""
+def wann_main(M, U, km, ctl: WannControl, record=True, precond=None):
+    """Restatement of wann_main for guiding_centres=F, SLWF=F, no sitesym.
+    ``precond``: the tables of :func:`precond_setup` when ``ctl.precond``."""
+    if ctl.precond and precond is None:
+        raise ValueError("precond=T needs the precond_setup tables")
     M = M.copy()
     U = U.copy()
     K, B, W, _ = M.shape
@@ -413,8 +475,12 @@ def wann_main(M, U, km, ctl: WannControl, record=True):
     it = 0
     for it in range(1, ctl.num_iter + 1):
         cdodq = wann_domega(M, km)                                    # :566-571
+        if ctl.precond:                                               # :577-581
+            cdodq_p = precond_search_direction(cdodq, wann_spread.om_tot, precond)
+        else:
+            cdodq_p = cdodq
         # internal_search_direction (:1371-1525)
-        gcnorm1 = float(np.vdot(cdodq, cdodq).real)
+        gcnorm1 = float(np.vdot(cdodq_p, cdodq).real)
         if it == 1 or ncg >= ctl.num_cg_steps:
             gcfac = 0.0
             ncg = 0
@@ -430,7 +496,7 @@ def wann_main(M, U, km, ctl: WannControl, record=True):
                 gcfac = 0.0
                 ncg = 0
         gcnorm0 = gcnorm1
-        cdq = cdodq + cdqkeep * gcfac
+        cdq = cdodq_p + cdqkeep * gcfac
         if lrandom:
             raise NotImplementedError("conv_noise_amp > 0 is not restated in the oracle")
         doda0 = -float(np.vdot(cdodq, cdq).real) / (4.0 * wbtot)

@@ -6,7 +6,8 @@ Run once in a checkout that has the Wannier90 source tree:
 
 For each isolated-band ``wann_main`` regression case of the reference test suite
 (test-suite/tests/testw90_example02 Pb, testw90_example01 GaAs,
-testw90_example05 diamond, testw90_basic1) it stores, in one ``.npz``:
+testw90_example05 diamond, testw90_basic1, and the preconditioned GaAs runs
+testw90_precond_1 / _2) it stores, in one ``.npz``:
 
 * the inputs exactly as the reference reads them: lattice (Angstrom), k-points,
   the raw ``.mmn`` blocks with their ``(k, k2, G)`` headers, the raw ``.amn``;
@@ -33,6 +34,8 @@ CASES = {
     "gaas": ("test-suite/tests/testw90_example01", "gaas"),
     "diamond": ("test-suite/tests/testw90_example05", "diamond"),
     "basic1": ("test-suite/tests/testw90_basic1", "wannier"),
+    "precond1": ("test-suite/tests/testw90_precond_1", "gaas1"),
+    "precond2": ("test-suite/tests/testw90_precond_2", "gaas2"),
 }
 
 
@@ -156,7 +159,9 @@ def build(ref_root, out_dir):
                      conv_tol=float(kw.get("conv_tol", "1e-10").replace("d", "e")),
                      conv_window=int(kw.get("conv_window", -1)),
                      trial_step=float(kw.get("trial_step", 2.0)),
-                     search_shells=int(kw.get("search_shells", 36)))
+                     search_shells=int(kw.get("search_shells", 36)),
+                     precond=int(kw.get("precond", "f").strip(".").lower().startswith("t")),
+                     optimisation=int(kw.get("optimisation", 3)))
         np.savez_compressed(
             os.path.join(out_dir, name + ".npz"),
             real_lattice=real_lattice, kpt_latt=kpts,

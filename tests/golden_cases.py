@@ -4,7 +4,7 @@ import os
 import numpy as np
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-CASES = ["pb", "gaas", "diamond", "basic1"]
+CASES = ["pb", "gaas", "diamond", "basic1", "precond1", "precond2"]
 
 
 def load(name):
@@ -37,4 +37,12 @@ def control(d):
     kn = d["knobs"]
     return O.WannControl(num_iter=int(kn["num_iter"]), num_cg_steps=int(kn["num_cg_steps"]),
                          conv_tol=float(kn["conv_tol"]), conv_window=int(kn["conv_window"]),
-                         trial_step=float(kn["trial_step"]))
+                         trial_step=float(kn["trial_step"]), precond=bool(kn.get("precond", 0)))
+
+
+def precond_tables(d):
+    """irvec / ndegen / k_to_r of a preconditioned case (None otherwise)."""
+    from oracle import w90_oracle as O
+    if not d["knobs"].get("precond", 0):
+        return None
+    return O.precond_setup(d["real_lattice"], d["kpt_latt"], d["mp_grid"])

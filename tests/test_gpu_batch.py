@@ -50,6 +50,7 @@ def test_batch_members_equal_standalone_runs():
     for i, h in enumerate(handles):
         m_a, u_a, log_a = alone[i]
         log_b = w90.w90_get_log(h, 16)
+        assert log_b.shape == log_a.shape, (i, log_b.shape)
         np.testing.assert_array_equal(log_b[:, :8], log_a[:, :8])   # same trajectory, bit for bit
         np.testing.assert_array_equal(ms[i].cpu().numpy(), m_a)
         np.testing.assert_array_equal(us[i].cpu().numpy(), u_a)

@@ -27,10 +27,10 @@ from wannier90_gb300 import synth
 pytestmark = pytest.mark.gpu
 
 
-def _oracle(real_lattice, kpoints, M_raw, A, ctl, search_shells=36):
+def _oracle(real_lattice, kpoints, M_raw, A, ctl, search_shells=36, precond=None):
     km = O.kmesh_get(real_lattice, kpoints, search_shells)
     U0, M0 = O.overlap_project(M_raw, A, km["nnlist"])
-    r = O.wann_main(M0, U0, km, ctl)
+    r = O.wann_main(M0, U0, km, ctl, precond=precond)
     return km, U0, M0, r
 
 
@@ -51,13 +51,13 @@ def _check_trajectory(out, r, rel=1e-8, floor=2e-10, upto=None):
         np.testing.assert_allclose(out["spreads"], r.spreads, atol=1e-6)
 
 
-def _stable_window(M0, U0, km, ctl, tol=1e-11, noise=1e-15):
+def _stable_window(M0, U0, km, ctl, tol=1e-11, noise=1e-15, precond=None):
     """Last iteration up to which the oracle agrees with itself on an input perturbed by
     `noise` (relative): 1e-15 for the FP64 engine, 1e-13 for the tensor engine, whose
     per-step roundoff (Ozaki slicing, ~2^-49 of the row x column scales) is larger."""
     rng = np.random.default_rng(12345)
-    a = O.wann_main(M0, U0, km, ctl)
-    b = O.wann_main(M0 * (1 + noise * rng.standard_normal(M0.shape)), U0, km, ctl)
+    a = O.wann_main(M0, U0, km, ctl, precond=precond)
+    b = O.wann_main(M0 * (1 + noise * rng.standard_normal(M0.shape)), U0, km, ctl, precond=precond)
     last = 0
     for x, y in zip(a.iters, b.iters):
         if abs(x.spread.om_tot - y.spread.om_tot) > tol * abs(x.spread.om_tot) + 1e-13:
@@ -75,13 +75,16 @@ def test_golden_cases(name, tensor):
     km = O.kmesh_get(d["real_lattice"], d["kpt_latt"], ss)
     M = G.assemble_m(d, km["nnlist"], km["nncell"])
     A = np.ascontiguousarray(d["amn"])
-    out = run_engine(d["real_lattice"], d["kpt_latt"], M, A, ctl, int(d["num_bands"]), ss,
-                     extra={"gpu_tensor": tensor})
+    extra = {"gpu_tensor": tensor}
+    if ctl.precond:
+        extra.update(precond=1, mp_grid=np.asarray(d["mp_grid"], dtype=np.int32),
+                     optimisation=int(d["knobs"]["optimisation"]))
+    out = run_engine(d["real_lattice"], d["kpt_latt"], M, A, ctl, int(d["num_bands"]), ss, extra=extra)
     assert out["ierr"] == 0, out["err"]
     U0, M0 = O.overlap_project(M, A, km["nnlist"])
     np.testing.assert_allclose(out["U0"], U0, atol=1e-11)
     np.testing.assert_allclose(out["M0"], M0, atol=1e-11)
-    r = O.wann_main(M0, U0, km, ctl)
+    r = O.wann_main(M0, U0, km, ctl, precond=G.precond_tables(d))
     _check_trajectory(out, r, floor=1e-11)
     # against the reference's printed <-- CONV lines directly
     by_iter = {int(row[0]): row for row in out["log"]}
@@ -133,10 +136,11 @@ def test_shapes_shared_memory_path(W, mp, tensor):
     _check_trajectory(out, r, upto=window)
 
 
+@pytest.mark.parametrize("tensor", [0, 1], ids=["fp64", "tensor"])
 @pytest.mark.parametrize("W", [33, 48])
-def test_shapes_global_memory_path(W):
+def test_shapes_global_memory_path(W, tensor):
     cfg = dict(kind="sc", a=4.0, mp=(2, 2, 2), num_wann=W, rmax=1, eps=0.3)
-    out, r, window = _synthetic(cfg, 12)
+    out, r, window = _synthetic(cfg, 12, tensor=tensor)
     assert window >= 2
     _check_trajectory(out, r, upto=window)
 
@@ -154,3 +158,41 @@ def test_convergence_window_stops_at_reference_iteration():
     # small problem: the spread stays within 1e-8 relative / 2e-10 A^2 of the oracle over
     # the whole run and the convergence window closes at the same iteration
     _check_trajectory(out, r)
+
+
+@pytest.mark.parametrize("tensor", [0, 1], ids=["fp64", "tensor"])
+@pytest.mark.parametrize("kind,W,mp", [("sc", 8, (4, 4, 4)), ("fcc", 20, (3, 3, 3)), ("sc", 33, (2, 3, 2))])
+def test_precond_synthetic(kind, W, mp, tensor):
+    """precond = T on meshes whose k -> R transform spans several 16-wide tiles in both
+    directions (nrpts 27..125, num_kpts 12..64, W^2 up to 17 element tiles)."""
+    cfg = dict(kind=kind, a=5.0, mp=mp, num_wann=W, rmax=1, eps=0.3)
+    p = synth.make_problem(**cfg, seed=3)
+    M = synth.to_math_m(p.m)
+    A = synth.to_math_u(p.a)
+    ctl = O.WannControl(num_iter=30, precond=True)
+    out = run_engine(p.real_lattice, p.kpoints, M, A, ctl, W,
+                     extra={"gpu_tensor": tensor, "precond": 1, "mp_grid": np.asarray(mp, dtype=np.int32)})
+    assert out["ierr"] == 0, out["err"]
+    pc = O.precond_setup(p.real_lattice, p.kpoints, mp)
+    km, U0, M0, r = _oracle(p.real_lattice, p.kpoints, M, A, ctl, precond=pc)
+    window = _stable_window(M0, U0, km, ctl, noise=1e-13 if tensor else 1e-15, precond=pc)
+    assert window >= 2
+    _check_trajectory(out, r, upto=window)
+
+
+@pytest.mark.parametrize("W,mp", [(8, (3, 3, 3)), (20, (2, 2, 2)), (32, (2, 2, 2)), (40, (2, 2, 2)),
+                                  (64, (2, 2, 2)), (100, (2, 2, 2))])
+def test_tensor_matches_fp64_first_iterations(W, mp):
+    """Before chaos amplifies roundoff, the tensor path (all tile widths 8..128) and the FP64
+    path give the same spreads to 1e-12 relative and the same rotations to 1e-11."""
+    cfg = dict(kind="sc", a=4.0, mp=mp, num_wann=W, rmax=1, eps=0.3)
+    p = synth.make_problem(**cfg, seed=5)
+    M = synth.to_math_m(p.m)
+    A = synth.to_math_u(p.a)
+    ctl = O.WannControl(num_iter=2)
+    a = run_engine(p.real_lattice, p.kpoints, M, A, ctl, W, extra={"gpu_tensor": 0})
+    b = run_engine(p.real_lattice, p.kpoints, M, A, ctl, W, extra={"gpu_tensor": 1})
+    assert a["ierr"] == 0 and b["ierr"] == 0, (a["err"], b["err"])
+    np.testing.assert_allclose(b["log"][:, 3], a["log"][:, 3], rtol=1e-12)
+    np.testing.assert_allclose(b["U"], a["U"], atol=1e-11)
+    np.testing.assert_allclose(b["M"], a["M"], atol=1e-11)

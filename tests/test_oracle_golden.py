@@ -1,7 +1,7 @@
 """The oracle against the reference's own regression outputs (parity pin of the oracle).
 
 Inputs and expected values are the reference test suite's (test-suite/tests/testw90_example02,
-_example01, _example05, _basic1), packed by tests/golden/make_fixtures.py.  Every printed
+_example01, _example05, _basic1, and the preconditioned _precond_1 / _precond_2), packed by tests/golden/make_fixtures.py.  Every printed
 <-- CONV spread (10 decimals) must match to 2e-10 A^2 (RMS gradient to 1e-3 relative above a 1e-6 roundoff floor), final centres to 1e-6 A (printed to
 6 decimals), spreads to 1e-7 A^2 and the b-vector / weight table to 1e-6.
 """
@@ -24,7 +24,7 @@ def test_oracle_reproduces_reference_trajectory(name):
     np.testing.assert_allclose(km["wb"], tab[:, 3], atol=1e-6)
     M = G.assemble_m(d, km["nnlist"], km["nncell"])
     U0, M0 = O.overlap_project(M, d["amn"], km["nnlist"])
-    r = O.wann_main(M0, U0, km, G.control(d))
+    r = O.wann_main(M0, U0, km, G.control(d), precond=G.precond_tables(d))
     rec = {0: r.initial}
     rec.update({it.iter: it for it in r.iters})
     for it, delta, rms, spread in d["conv"]:

@@ -49,6 +49,7 @@ SIGNATURES = [
     ("w90g_profile_kernel_name", C.c_char_p, [C.c_int]),
     ("w90g_profile_exp_products", C.c_double, [C.c_void_p]),
     ("w90g_measure_fp64_peak", C.c_double, []),
+    ("w90g_ws_vectors", C.c_int, [_c_double_p, _c_int_p, _c_int_p, C.c_double, _c_int_p, _c_int_p, C.c_int]),
     ("w90g_project_overlap_noalloc", C.c_int,
      [C.c_int, C.c_int, C.c_int, _c_int_p, C.c_void_p, C.c_void_p, C.c_void_p]),
 ]

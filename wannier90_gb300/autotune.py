@@ -1,6 +1,6 @@
 """Autotuner keyed on num_wann: picks the M-update variant for each width.
 
-Variants: the tensor-core M update at padded tile width 8 / 16 / 32 (W <= 32) and the
+Variants: the tensor-core M update at padded tile width 8 / 16 / 32 / 64 / 128 and the
 FP64 shared-/global-memory kernels.  For each W the tuner times a few iterations of a
 seeded tight-binding probe (sc lattice, 4x4x4 k-mesh, nntot 6) in both variants on the
 current GPU and keeps the faster.  Results are cached per process and, optionally, in a
@@ -45,8 +45,8 @@ def tune(num_wann: int, iters: int = 12, mp=(4, 4, 4)) -> dict:
     W = int(num_wann)
     if W in _CACHE:
         return _CACHE[W]
-    if W > 32:
-        res = {"tensor": 0, "t_fp64": None, "t_tensor": None, "reason": "W > 32: FP64 kernels only"}
+    if W > 128:
+        res = {"tensor": 0, "t_fp64": None, "t_tensor": None, "reason": "W > 128: FP64 kernels only"}
     else:
         p = synth.make_problem(kind="sc", a=5.0, mp=mp, num_wann=W, rmax=1, eps=0.3, seed=12345)
         t0 = _time_variant(p, 0, iters)

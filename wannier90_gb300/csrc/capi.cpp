@@ -49,8 +49,12 @@ struct Handle {
   int iprint = 1, num_print_cycles = 1, timing_level = 1;
   int search_shells = 36;
   double kmesh_tol = 1.0e-6;
-  int gpu_tensor = 0;   // M update on tensor cores (W <= 32)
+  int gpu_tensor = 0;   // M update on tensor cores (W <= 128)
   KmeshInfo km;
+  // preconditioner tables (precond = T), built at cinput_setopt like wann_main's
+  // hamiltonian_setup / k_to_r (src/wannierise.F90:269-300)
+  int precond = 0, nrpts = 0;
+  std::vector<double> pc_kr, pc_r2, pc_ndeg;
   // caller data
   double* m_local = nullptr;
   double* u_matrix = nullptr;
@@ -206,6 +210,11 @@ int build_spec(Handle* h, ProblemSpec& s) {
   s.wb = h->km.wb;
   s.ctl = h->ctl;
   s.tensor = h->gpu_tensor;
+  s.precond = h->precond;
+  s.nrpts = h->nrpts;
+  s.pc_kr = h->pc_kr;
+  s.pc_r2 = h->pc_r2;
+  s.pc_ndeg = h->pc_ndeg;
   return 0;
 }
 
@@ -244,17 +253,16 @@ int do_wannierise(Handle* h, double* m, double* u, cudaMemcpyKind in, cudaMemcpy
   int rc = e->setup({s}, err);
   if (!rc) rc = e->load(0, m, u, in, err);
   if (!rc) rc = e->wannierise(err);
-  const int solve_rc = rc;
-  if (rc == 0 || rc == 1) {
-    std::string err2;
-    int rc2 = e->store(0, m, u, out, err2);
-    if (rc2 && !rc) {
-      rc = rc2;
-      err = err2;
-    }
-  }
-  if (rc && solve_rc != 1) return fail(h, rc, err);
+  if (!rc) rc = e->store(0, m, u, out, err);
+  if (rc) return fail(h, rc, err);
   const auto& r = e->result(0);
+  if (r.error) {
+    rc = 1;
+    err = "non-finite spread in the engine";
+  } else if (!(r.unitarity_err <= 1e-5)) {
+    rc = 1;
+    err = "wann_check_unitarity: unitariety of final U violated";
+  }
   h->omega[0] = r.spread.om_i;
   h->omega[1] = r.spread.om_d;
   h->omega[2] = r.spread.om_od;
@@ -380,10 +388,10 @@ void cinput_setopt(void* hv, const char* seedname, int* ierr, int comm) {
   h->timing_level = get_num(h, "timing_level", v) ? (int)v : 1;
   h->search_shells = get_num(h, "search_shells", v) ? (int)v : 36;
   h->kmesh_tol = get_num(h, "kmesh_tol", v) ? v : 1.0e-6;
-  // engine key: gpu_tensor = 1 computes M(k,b) = U^H M0 U' on tensor cores (W <= 32)
+  // engine key: gpu_tensor = 1 computes M(k,b) = U^H M0 U' on tensor cores (W <= 128)
   h->gpu_tensor = get_num(h, "gpu_tensor", v) ? (int)v : 0;
   // options on wann_main's code path that the engine does not implement
-  const char* unsupported[] = {"precond", "guiding_centres", "slwf_num", "slwf_constrain", "site_symmetry",
+  const char* unsupported[] = {"guiding_centres", "slwf_num", "slwf_constrain", "site_symmetry",
                                "gamma_only"};
   for (const char* k : unsupported) {
     if (get_num(h, k, v)) {
@@ -404,6 +412,54 @@ void cinput_setopt(void* hv, const char* seedname, int* ierr, int comm) {
   if (rc) {
     *ierr = fail(h, rc, err);
     return;
+  }
+  h->precond = get_num(h, "precond", v) ? (v != 0.0) : 0;
+  h->nrpts = 0;
+  h->pc_kr.clear();
+  h->pc_r2.clear();
+  h->pc_ndeg.clear();
+  if (h->precond) {
+    if (h->mp_grid[0] < 1 || h->mp_grid[1] < 1 || h->mp_grid[2] < 1) {
+      *ierr = fail(h, 5, "Error: precond = T needs mp_grid");
+      return;
+    }
+    int ws[3] = {2, 2, 2};   // ws_search_size default (src/types.F90:78)
+    auto wit = h->opts.find("ws_search_size");
+    if (wit != h->opts.end()) {
+      for (int i = 0; i < 3; ++i) ws[i] = (int)wit->second.v[wit->second.v.size() == 3 ? i : 0];
+    }
+    const double wtol = get_num(h, "ws_distance_tol", v) ? v : 1.0e-5;
+    std::vector<int> irvec, ndegen;
+    rc = w90g::ws_vectors(h->real_lattice, h->mp_grid, ws, wtol, irvec, ndegen, err);
+    if (rc) {
+      *ierr = fail(h, rc, err);
+      return;
+    }
+    const int NR = (int)ndegen.size(), K = h->num_kpts;
+    h->nrpts = NR;
+    h->pc_kr.resize((size_t)2 * K * NR);
+    h->pc_r2.resize(NR);
+    h->pc_ndeg.resize(NR);
+    const double twopi = 6.283185307179586476925287;
+    for (int r = 0; r < NR; ++r) {
+      const double n[3] = {(double)irvec[3 * r], (double)irvec[3 * r + 1], (double)irvec[3 * r + 2]};
+      // rvec_cart = matmul(real_lattice, irvec) exactly as the reference forms it
+      // (src/wannierise.F90:1341): component i is a_i . n
+      double r2 = 0.0;
+      for (int i = 0; i < 3; ++i) {
+        const double x = h->real_lattice[i * 3] * n[0] + h->real_lattice[i * 3 + 1] * n[1] +
+                         h->real_lattice[i * 3 + 2] * n[2];
+        r2 += x * x;
+      }
+      h->pc_r2[r] = r2;
+      h->pc_ndeg[r] = (double)ndegen[r];
+      for (int k = 0; k < K; ++k) {
+        const double* kp = &h->kpt_latt[(size_t)3 * k];
+        const double rdotk = twopi * (kp[0] * n[0] + kp[1] * n[1] + kp[2] * n[2]);
+        h->pc_kr[((size_t)k * NR + r) * 2] = std::cos(rdotk);
+        h->pc_kr[((size_t)k * NR + r) * 2 + 1] = -std::sin(rdotk);
+      }
+    }
   }
   h->centres.assign(3 * h->num_wann, 0.0);
   h->spreads.assign(h->num_wann, 0.0);
@@ -525,6 +581,19 @@ const char* w90g_profile_kernel_name(int i) {
   return (i >= 0 && i < w90g::kPNum) ? w90g::kProfNames[i] : "";
 }
 
+int w90g_ws_vectors(const double* real_lattice33, const int* mp_grid3, const int* search_size3,
+                    double ws_distance_tol, int* irvec_out, int* ndegen_out, int max_pts) {
+  std::vector<int> irvec, ndegen;
+  std::string err;
+  if (w90g::ws_vectors(real_lattice33, mp_grid3, search_size3, ws_distance_tol, irvec, ndegen, err)) return -1;
+  const int n = (int)ndegen.size();
+  if (n <= max_pts) {
+    std::copy(irvec.begin(), irvec.end(), irvec_out);
+    std::copy(ndegen.begin(), ndegen.end(), ndegen_out);
+  }
+  return n;
+}
+
 double w90g_measure_fp64_peak(void) {
   double t = 0.0;
   std::string err;
@@ -534,7 +603,7 @@ double w90g_measure_fp64_peak(void) {
 
 // Batched form: independent problems (each set up on its own handle) solved together.
 // Problems are grouped by the M-update variant their width selects (tensor path with
-// padded width 8 / 16 / 32 when requested and W <= 32, FP64 path otherwise); each group
+// padded width 8 / 16 / 32 / 64 / 128 when requested, FP64 path otherwise); each group
 // is one engine whose iteration graph covers all of its problems, and the groups run
 // concurrently on their own streams.
 void w90g_wannierise_batch_device(void** handles, int nprob, double** d_m, double** d_u, int* ierr) {
@@ -557,7 +626,7 @@ void w90g_wannierise_batch_device(void** handles, int nprob, double** d_m, doubl
     ProblemSpec s;
     build_spec(h, s);
     int key = 0;
-    if (s.tensor && s.W <= 32) key = s.W <= 8 ? 8 : (s.W <= 16 ? 16 : 32);
+    if (s.tensor && s.W <= 128) key = s.W <= 8 ? 8 : (s.W <= 16 ? 16 : (s.W <= 32 ? 32 : (s.W <= 64 ? 64 : 128)));
     groups[key].idx.push_back(i);
     groups[key].specs.push_back(s);
   }
@@ -576,16 +645,8 @@ void w90g_wannierise_batch_device(void** handles, int nprob, double** d_m, doubl
       for (size_t j = 0; j < g->idx.size() && !g->rc; ++j)
         g->rc = g->eng->load((int)j, d_m[g->idx[j]], d_u[g->idx[j]], cudaMemcpyDeviceToDevice, g->err);
       if (!g->rc) g->rc = g->eng->wannierise(g->err);
-      if (g->rc == 0 || g->rc == 1) {
-        for (size_t j = 0; j < g->idx.size(); ++j) {
-          std::string e2;
-          int rc2 = g->eng->store((int)j, d_m[g->idx[j]], d_u[g->idx[j]], cudaMemcpyDeviceToDevice, e2);
-          if (rc2 && !g->rc) {
-            g->rc = rc2;
-            g->err = e2;
-          }
-        }
-      }
+      for (size_t j = 0; j < g->idx.size() && !g->rc; ++j)
+        g->rc = g->eng->store((int)j, d_m[g->idx[j]], d_u[g->idx[j]], cudaMemcpyDeviceToDevice, g->err);
     });
   }
   for (auto& t : threads) t.join();
@@ -593,7 +654,7 @@ void w90g_wannierise_batch_device(void** handles, int nprob, double** d_m, doubl
     Group& g = kv.second;
     for (size_t j = 0; j < g.idx.size(); ++j) {
       Handle* h = H(handles[g.idx[j]]);
-      if (g.rc && g.rc != 1) {
+      if (g.rc) {
         ierr[g.idx[j]] = fail(h, g.rc, g.err);
         continue;
       }

@@ -2,7 +2,8 @@
 //
 // Memory: one cudaMalloc arena per batch, sub-allocated at 256-byte alignment; every
 // per-problem array of the iteration stays resident in HBM for the whole solve.
-// Launch: the fourteen-kernel iteration (see k_fp64.cu) is captured once into a CUDA graph
+// Launch: the 14-kernel iteration (16 with the tensor-core M update, +2 with the
+// preconditioner; see k_fp64.cu) is captured once into a CUDA graph
 // and replayed; the device controller makes replays after convergence no-ops, so the
 // host only polls a single "all done" word every few replays.
 #include <cuda_runtime.h>
@@ -35,12 +36,13 @@ __global__ void k_fp64_peak(double* out, int iters, double seed);
 __global__ void k_u_final(const Problem* probs, WorkMap wm);
 __global__ void k_u_identity(const Problem* probs, WorkMap wm);
 __global__ void k_frob0(const Problem* probs, WorkMap wm);
+__global__ void k_precond(const Problem* probs, int dir);
 cudaError_t oz_launch(int wp, int step, const Problem* probs, WorkMap wm, int which, int grid,
                       cudaStream_t s);
 cudaError_t oz_set_attributes(int wp);
 
 const char* kProfNames[kPNum] = {"k_grad", "k_ctrl_search", "k_exp_u", "k_m_update",
-                                 "k_omega", "k_ctrl_step", "k_ctrl_end", "init"};
+                                 "k_omega", "k_ctrl_step", "k_ctrl_end", "init", "k_precond"};
 
 namespace {
 constexpr size_t kAlign = 256;
@@ -85,10 +87,17 @@ int Engine::setup(const std::vector<ProblemSpec>& specs, std::string& err) {
       err = "conv_window larger than the engine maximum (64)";
       return 5;
     }
+    if (s.precond && (s.nrpts < 1 || s.pc_kr.size() != (size_t)2 * s.K * s.nrpts ||
+                      s.pc_r2.size() != (size_t)s.nrpts || s.pc_ndeg.size() != (size_t)s.nrpts)) {
+      err = "precond: Wigner-Seitz tables missing or inconsistent";
+      return 5;
+    }
   }
   // layout key: reuse the arena when the problem shapes are unchanged
   std::ostringstream key;
-  for (const auto& s : specs) key << s.W << ',' << s.K << ',' << s.B << ',' << s.ctl.num_iter << ',' << s.tensor << ';';
+  for (const auto& s : specs)
+    key << s.W << ',' << s.K << ',' << s.B << ',' << s.ctl.num_iter << ',' << s.tensor << ',' << s.precond << ','
+        << s.nrpts << ';';
   specs_ = specs;
   if (arena_ && key.str() == layout_key_) {
     // refresh the read-only tables (they may differ at equal shapes)
@@ -98,6 +107,11 @@ int Engine::setup(const std::vector<ProblemSpec>& specs, std::string& err) {
       W90G_CHECK(cudaMemcpy((void*)P.nnlist, s.nnlist.data(), s.nnlist.size() * sizeof(int), cudaMemcpyHostToDevice));
       W90G_CHECK(cudaMemcpy((void*)P.bk, s.bk.data(), s.bk.size() * sizeof(double), cudaMemcpyHostToDevice));
       W90G_CHECK(cudaMemcpy((void*)P.wb, s.wb.data(), s.wb.size() * sizeof(double), cudaMemcpyHostToDevice));
+      if (s.precond) {
+        W90G_CHECK(cudaMemcpy((void*)P.pc_kr, s.pc_kr.data(), s.pc_kr.size() * 8, cudaMemcpyHostToDevice));
+        W90G_CHECK(cudaMemcpy((void*)P.pc_r2, s.pc_r2.data(), s.pc_r2.size() * 8, cudaMemcpyHostToDevice));
+        W90G_CHECK(cudaMemcpy((void*)P.pc_ndeg, s.pc_ndeg.data(), s.pc_ndeg.size() * 8, cudaMemcpyHostToDevice));
+      }
       hprobs_[p].ctl = s.ctl;
       hprobs_[p].wbtot = s.wbtot;
     }
@@ -111,30 +125,32 @@ int Engine::setup(const std::vector<ProblemSpec>& specs, std::string& err) {
 
 int Engine::alloc(std::string& err) {
   const int np = (int)specs_.size();
-  // tensor-core M update: every problem asks for it, W <= 32, and every k' has exactly
+  // tensor-core M update: every problem asks for it, W <= 128, and every k' has exactly
   // B predecessors (k,b) (true on Monkhorst-Pack meshes)
   tensor_wp_ = 0;
   {
     bool ok = np > 0;
     int wmax = 0;
     for (const auto& s : specs_) {
-      ok = ok && s.tensor && s.W <= 32;
+      ok = ok && s.tensor && s.W <= 128;
       wmax = std::max(wmax, s.W);
       if (!ok) break;
       std::vector<int> cnt(s.K, 0);
       for (int v : s.nnlist) cnt[v]++;
       for (int c : cnt) ok = ok && (c == s.B);
     }
-    if (ok) tensor_wp_ = wmax <= 8 ? 8 : (wmax <= 16 ? 16 : 32);
+    if (ok) tensor_wp_ = wmax <= 8 ? 8 : (wmax <= 16 ? 16 : (wmax <= 32 ? 32 : (wmax <= 64 ? 64 : 128)));
   }
   if (!own_stream_) W90G_CHECK(cudaStreamCreateWithFlags(&own_stream_, cudaStreamNonBlocking));
   // sizes
   struct Sizes {
     size_t M, U, KWW, work, tbuf, diag, offd, gpart, cen, log, logc, nn, bk, wb, st, op1, op2, m0, u0, inv, fr;
+    size_t pkr, pr2, pgr, pgp, ppart;
   };
   std::vector<Sizes> sz(np);
   size_t total = 0;
   n_k_ = n_kb_ = n_grad_ = 0;
+  pc_tiles_ = 0;
   maxW_small_ = 0;
   max_iter_ = 0;
   std::vector<int> offs_k(np + 1, 0), offs_kb(np + 1, 0), offs_grad(np + 1, 0), offs_chunk(np + 1, 0);
@@ -166,8 +182,20 @@ int Engine::alloc(std::string& err) {
     const size_t nch = (K * B + 63) / 64;
     z.op1 = align_up(nch * (4 * W + 2) * 8);
     z.op2 = align_up(nch * 8);
+    z.pkr = z.pr2 = z.pgr = z.pgp = z.ppart = 0;
+    if (s.precond) {
+      const size_t NR = s.nrpts;
+      const size_t te = (WW + 63) / 64;
+      z.pkr = align_up(K * NR * 16);
+      z.pr2 = align_up(NR * 8);
+      z.pgr = align_up(NR * WW * 16);
+      z.pgp = align_up(K * WW * 16);
+      z.ppart = align_up(te * ((K + 15) / 16) * 8);
+      pc_tiles_ = std::max(pc_tiles_, (int)(te * ((std::max(K, NR) + 15) / 16)));
+    }
     total += 2 * z.M + 2 * z.U + 3 * z.KWW + z.work + z.tbuf + 2 * z.diag + z.offd + z.gpart + z.cen +
-             z.log + z.logc + z.nn + z.bk + z.wb + z.st + z.op1 + z.op2 + z.m0 + z.u0 + z.inv + z.fr;
+             z.log + z.logc + z.nn + z.bk + z.wb + z.st + z.op1 + z.op2 + z.m0 + z.u0 + z.inv + z.fr +
+             z.pkr + 2 * z.pr2 + z.pgr + z.pgp + z.ppart;
     offs_k[p + 1] = offs_k[p] + s.K;
     offs_kb[p + 1] = offs_kb[p] + s.K * s.B;
     offs_grad[p + 1] = offs_grad[p] + s.K * nt * nt;
@@ -253,18 +281,36 @@ int Engine::alloc(std::string& err) {
     P.nnlist = nn;
     P.bk = bk;
     P.wb = wb;
+    P.precond = s.precond;
+    P.nrpts = s.precond ? s.nrpts : 0;
+    if (s.precond) {
+      double* kr = (double*)take(z.pkr);
+      double* r2 = (double*)take(z.pr2);
+      double* nd = (double*)take(z.pr2);
+      W90G_CHECK(cudaMemcpy(kr, s.pc_kr.data(), s.pc_kr.size() * 8, cudaMemcpyHostToDevice));
+      W90G_CHECK(cudaMemcpy(r2, s.pc_r2.data(), s.pc_r2.size() * 8, cudaMemcpyHostToDevice));
+      W90G_CHECK(cudaMemcpy(nd, s.pc_ndeg.data(), s.pc_ndeg.size() * 8, cudaMemcpyHostToDevice));
+      P.pc_kr = (const double2*)kr;
+      P.pc_r2 = r2;
+      P.pc_ndeg = nd;
+      P.pc_gr = (double2*)take(z.pgr);
+      P.pc_gp = (double2*)take(z.pgp);
+      P.pc_part = (double*)take(z.ppart);
+    }
   }
   W90G_CHECK(cudaMemcpy(dprobs_, hprobs_.data(), np * sizeof(Problem), cudaMemcpyHostToDevice));
   W90G_CHECK(cudaMemcpy(d_offs_k_, offs_k.data(), (np + 1) * sizeof(int), cudaMemcpyHostToDevice));
   W90G_CHECK(cudaMemcpy(d_offs_kb_, offs_kb.data(), (np + 1) * sizeof(int), cudaMemcpyHostToDevice));
   W90G_CHECK(cudaMemcpy(d_offs_grad_, offs_grad.data(), (np + 1) * sizeof(int), cudaMemcpyHostToDevice));
   W90G_CHECK(cudaMemcpy(d_offs_chunk_, offs_chunk.data(), (np + 1) * sizeof(int), cudaMemcpyHostToDevice));
-  // dynamic shared memory limits of the shared-memory kernels
-  const int ws = std::max(maxW_small_, 1);
-  W90G_CHECK(cudaFuncSetAttribute(k_exp_u, cudaFuncAttributeMaxDynamicSharedMemorySize, 6 * ws * ws * 16));
-  W90G_CHECK(cudaFuncSetAttribute(k_u_final, cudaFuncAttributeMaxDynamicSharedMemorySize, 3 * ws * ws * 16));
-  W90G_CHECK(cudaFuncSetAttribute(k_m_update, cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * ws * ws * 16));
-  W90G_CHECK(cudaFuncSetAttribute(k_lowdin, cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * ws * ws * 16));
+  // dynamic shared memory limits of the shared-memory kernels: a function attribute is
+  // process wide, so every engine sets the same value, the maximum for W <= 32 (engines
+  // of different widths may run concurrently in the batched form)
+  constexpr int wmax = 32;
+  W90G_CHECK(cudaFuncSetAttribute(k_exp_u, cudaFuncAttributeMaxDynamicSharedMemorySize, 6 * wmax * wmax * 16));
+  W90G_CHECK(cudaFuncSetAttribute(k_u_final, cudaFuncAttributeMaxDynamicSharedMemorySize, 3 * wmax * wmax * 16));
+  W90G_CHECK(cudaFuncSetAttribute(k_m_update, cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * wmax * wmax * 16));
+  W90G_CHECK(cudaFuncSetAttribute(k_lowdin, cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * wmax * wmax * 16));
   if (tensor_wp_) W90G_CHECK(oz_set_attributes(tensor_wp_));
   return 0;
 }
@@ -385,6 +431,10 @@ void Engine::launch_iteration(cudaStream_t s) {
   const size_t sm_exp = (size_t)6 * ws * ws * 16;
   const size_t sm_mu = (size_t)4 * ws * ws * 16;
   k_grad<<<n_grad_, 256, 0, s>>>(dprobs_, wmg);
+  if (pc_tiles_) {
+    k_precond<<<dim3(pc_tiles_, np), 256, 0, s>>>(dprobs_, 0);
+    k_precond<<<dim3(pc_tiles_, np), 256, 0, s>>>(dprobs_, 1);
+  }
   k_ctrl_search<<<np, 256, 0, s>>>(dprobs_);
   k_exp_u<<<n_k_, 256, sm_exp, s>>>(dprobs_, wmk, 0);
   launch_mupdate(s, 0);
@@ -434,7 +484,8 @@ int Engine::wannierise(std::string& err) {
   while (done_iters < max_iter_) {
     const int n = std::min(chunk, max_iter_ - done_iters);
     for (int i = 0; i < n; ++i) W90G_CHECK(cudaGraphLaunch(graph_exec_, st));
-    launches_ += 14LL * n;
+    // grad, search, 2 x (exp, M update, 3 spread passes), step, end (+ 2 precond)
+    launches_ += (10LL + 2 * (tensor_wp_ ? 2 : 1) + (pc_tiles_ ? 2 : 0)) * n;
     done_iters += n;
     if (any_window && done_iters < max_iter_) {
       k_all_done<<<1, 256, 0, st>>>(dprobs_, np, d_alldone);
@@ -489,15 +540,9 @@ int Engine::wannierise(std::string& err) {
     double ue = 0.0;
     for (int k = offs_k[p]; k < offs_k[p + 1]; ++k) ue = std::max(ue, unit[k]);
     R.unitarity_err = ue;
-    if (S.error && !rc) {
-      err = "non-finite spread in the engine (problem " + std::to_string(p) + ")";
-      rc = 1;
-    }
-    if (!(ue <= 1e-5) && !rc) {
-      err = "wann_check_unitarity: unitariety of final U violated (problem " + std::to_string(p) + ")";
-      rc = 1;
-    }
   }
+  // per-problem failures (non-finite spread, unitarity) are reported through result(p);
+  // a non-zero return means the engine itself failed (CUDA error or allocation)
   return rc;
 }
 
@@ -543,6 +588,10 @@ int Engine::wannierise_profiled(int max_iters, double* ms, int* cnt, std::string
   const int iters = std::min(max_iters, max_iter_);
   for (int it = 0; it < iters && !rc; ++it) {
     rc |= timed(kPGrad, [&] { k_grad<<<n_grad_, 256, 0, st>>>(dprobs_, wmg); });
+    if (pc_tiles_) {
+      rc |= timed(kPPrecond, [&] { k_precond<<<dim3(pc_tiles_, np), 256, 0, st>>>(dprobs_, 0); });
+      rc |= timed(kPPrecond, [&] { k_precond<<<dim3(pc_tiles_, np), 256, 0, st>>>(dprobs_, 1); });
+    }
     rc |= timed(kPCtrlSearch, [&] { k_ctrl_search<<<np, 256, 0, st>>>(dprobs_); });
     rc |= timed(kPExpU, [&] { k_exp_u<<<n_k_, 256, sm_exp, st>>>(dprobs_, wmk, 0); });
     rc |= timed(kPMUpdate, [&] { launch_mupdate(st, 0); });

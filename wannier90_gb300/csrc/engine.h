@@ -17,7 +17,12 @@ struct ProblemSpec {
   std::vector<double> bk;    // [k][b][3]
   std::vector<double> wb;    // [b]
   Control ctl{};
-  int tensor = 0;            // request the tensor-core M update (W <= 32)
+  int tensor = 0;            // request the tensor-core M update (W <= 128)
+  // preconditioner (precond = T): Wigner-Seitz points R_r of the Born-von Karman
+  // supercell, exp(-i 2 pi k.R) table [k][r] (re, im interleaved), |R|^2, degeneracies
+  int precond = 0;
+  int nrpts = 0;
+  std::vector<double> pc_kr, pc_r2, pc_ndeg;
 };
 
 struct ProblemResult {
@@ -33,7 +38,7 @@ struct ProblemResult {
 };
 
 enum ProfKernel {
-  kPGrad = 0, kPCtrlSearch, kPExpU, kPMUpdate, kPOmega, kPCtrlStep, kPCtrlEnd, kPInit, kPNum
+  kPGrad = 0, kPCtrlSearch, kPExpU, kPMUpdate, kPOmega, kPCtrlStep, kPCtrlEnd, kPInit, kPPrecond, kPNum
 };
 extern const char* kProfNames[kPNum];
 
@@ -88,6 +93,7 @@ class Engine {
   int* d_status_ = nullptr;
   double* d_unit_ = nullptr;
   int n_k_ = 0, n_kb_ = 0, n_grad_ = 0, n_chunk_ = 0;
+  int pc_tiles_ = 0;     // > 0: some problem is preconditioned; CTAs per problem of k_precond
   int maxW_small_ = 0;   // largest W <= 32 in the batch (shared-memory kernels)
   int tensor_wp_ = 0;    // > 0: tensor M update with padded width 8/16/32 for the whole batch
   int max_iter_ = 0;

@@ -1,7 +1,7 @@
 // FP64 kernels of the GB300 MLWF engine (the plain FP64 path).
 //
 // One iteration of wann_main (src/wannierise.F90:534-816) is the fixed launch sequence
-//   k_grad -> k_ctrl_search -> k_exp_u(0) -> k_m_update(0) -> spread(0) -> k_ctrl_step
+//   k_grad [-> k_precond(0) -> k_precond(1)] -> k_ctrl_search -> k_exp_u(0) -> k_m_update(0) -> spread(0) -> k_ctrl_step
 //   -> k_exp_u(1) -> k_m_update(1) -> spread(1) -> k_ctrl_end
 // where spread(slot) = k_omega_p1 -> k_omega_p2 -> k_omega_p3.
 // All data-dependent decisions of the reference (CG reset, uphill reversal, parabolic
@@ -411,6 +411,98 @@ __global__ void __launch_bounds__(256) k_grad(const Problem* __restrict__ probs,
 }
 
 // ----------------------------------------------------------------------------
+// k_precond: precond_search_direction (src/wannierise.F90:1256-1368), its GEMM form
+// (optimisation >= 3, :1314-1320 and :1345-1352):
+//   dir 0:  Gr(R) = sum_k G(k) exp(-i 2pi k.R)                          (k -> R)
+//   dir 1:  Gp(k) = sum_R f_R Gr(R) exp(+i 2pi k.R),
+//           f_R = 1 / (num_kpts * ndegen_R * (1 + |R|^2 / alpha)),  alpha = 10 Omega / W
+// Each is a complex GEMM (W^2 x n_out x n_red).  Tile: 64 matrix elements x 16 outputs
+// per CTA (256 threads, 4 outputs each), reduction in chunks of 16 through shared memory.
+// dir 1 also writes the tile's partial of Re <Gp, G> (gcnorm1 of :1426-1428).
+// grid: (CTAs per problem, problems); CTAs beyond a problem's tile count return.
+// ----------------------------------------------------------------------------
+constexpr int kPcE = 64, kPcO = 16, kPcC = 16;
+
+__global__ void __launch_bounds__(256) k_precond(const Problem* __restrict__ probs, int dir) {
+  __shared__ double2 sX[kPcC][kPcE];
+  __shared__ double2 sP[kPcC][kPcO];
+  __shared__ double sf[kPcC];
+  __shared__ double red[256];
+  const Problem& P = probs[blockIdx.y];
+  const CtrlState* st = P.st;
+  if (!P.precond || st->done) return;
+  const int WW = P.W * P.W, K = P.K, NR = P.nrpts;
+  const int n_out = dir == 0 ? NR : K;
+  const int n_red = dir == 0 ? K : NR;
+  const int te = (WW + kPcE - 1) / kPcE;
+  const int to = (n_out + kPcO - 1) / kPcO;
+  const int local = blockIdx.x;
+  if (local >= te * to) return;
+  const int e0 = (local % te) * kPcE, o0 = (local / te) * kPcO;
+  const int t = threadIdx.x;
+  const int e = t % kPcE, og = (t / kPcE) * 4;
+  const double2* X = dir == 0 ? P.G : P.pc_gr;
+  const double alpha = 10.0 * st->wann.om_tot / (double)P.W;
+  double2 acc[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) acc[q] = cmk(0, 0);
+  for (int c0 = 0; c0 < n_red; c0 += kPcC) {
+    __syncthreads();
+    if (dir == 1 && t < kPcC) {
+      const int r = c0 + t;
+      sf[t] = r < NR ? 1.0 / ((double)K * P.pc_ndeg[r] * (1.0 + P.pc_r2[r] / alpha)) : 0.0;
+    }
+    for (int i = t; i < kPcC * kPcO; i += 256) {
+      const int j = i / kPcO, o = i % kPcO;
+      double2 v = cmk(0, 0);
+      if (c0 + j < n_red && o0 + o < n_out) {
+        v = dir == 0 ? P.pc_kr[(size_t)(c0 + j) * NR + o0 + o]
+                     : cconj(P.pc_kr[(size_t)(o0 + o) * NR + c0 + j]);
+      }
+      sP[j][o] = v;
+    }
+    __syncthreads();
+    for (int i = t; i < kPcC * kPcE; i += 256) {
+      const int j = i / kPcE, ee = i % kPcE;
+      double2 v = cmk(0, 0);
+      if (c0 + j < n_red && e0 + ee < WW) {
+        v = X[(size_t)(c0 + j) * WW + e0 + ee];
+        if (dir == 1) v = cscale(v, sf[j]);
+      }
+      sX[j][ee] = v;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int j = 0; j < kPcC; ++j) {
+      const double2 x = sX[j][e];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) cfma(acc[q], x, sP[j][og + q]);
+    }
+  }
+  double part = 0.0;
+  if (e0 + e < WW) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int o = o0 + og + q;
+      if (o >= n_out) continue;
+      if (dir == 0) {
+        // the 1/num_kpts of :1320 is folded into f_R
+        P.pc_gr[(size_t)o * WW + e0 + e] = acc[q];
+      } else {
+        const size_t off = (size_t)o * WW + e0 + e;
+        P.pc_gp[off] = acc[q];
+        const double2 g = P.G[off];
+        part += acc[q].x * g.x + acc[q].y * g.y;
+      }
+    }
+  }
+  if (dir == 1) {
+    part = block_sum(part, red);
+    if (t == 0) P.pc_part[local] = part;
+  }
+}
+
+// ----------------------------------------------------------------------------
 // k_ctrl_search: internal_search_direction (src/wannierise.F90:1371-1525) as scalars.
 // D = G + gcfac*D_prev is never formed here: the coefficients (coefG, coefD) are
 // handed to k_exp_u, and <G,D> = |G|^2 + gcfac*<G,D_prev> comes from k_grad's partials.
@@ -430,10 +522,19 @@ __global__ void k_ctrl_search(const Problem* __restrict__ probs) {
   }
   g2 = block_sum(g2, red);
   gd = block_sum(gd, red);
+  // precond: gcnorm1 = Re <Gp, G> (:1426-1428) from k_precond's partials
+  double gpg = g2;
+  if (P.precond) {
+    const int te = (P.W * P.W + kPcE - 1) / kPcE;
+    const int np = te * ((P.K + kPcO - 1) / kPcO);
+    double a = 0.0;
+    for (int i = threadIdx.x; i < np; i += blockDim.x) a += P.pc_part[i];
+    gpg = block_sum(a, red);
+  }
   if (threadIdx.x != 0) return;
   const Control& c = P.ctl;
   const int iter = st->iter + 1;
-  const double gcnorm1 = g2;
+  const double gcnorm1 = gpg;
   double gcfac;
   int ncg = st->ncg;
   if (iter == 1 || ncg >= c.num_cg_steps) {
@@ -456,11 +557,15 @@ __global__ void k_ctrl_search(const Problem* __restrict__ probs) {
   st->gcnorm0 = gcnorm1;
   st->gcnorm1 = gcnorm1;
   const double fw = 4.0 * P.wbtot;
+  // D = (Gp or G) + gcfac D_prev; <G, Gp> = gcnorm1 (:1460-1464, :1475-1481)
   double coefG = 1.0, coefD = gcfac;
-  double doda0 = -(g2 + gcfac * gd) / fw;
+  int use_gp = P.precond;
+  double doda0 = -(gpg + gcfac * gd) / fw;
   if (doda0 > 0.0) {
     if (ncg > 0) {
+      // reset to the plain gradient, also under precond (:1488)
       coefD = 0.0;
+      use_gp = 0;
       ncg = 0;
       gcfac = 0.0;
       doda0 = -g2 / fw;
@@ -479,6 +584,7 @@ __global__ void k_ctrl_search(const Problem* __restrict__ probs) {
   st->doda0 = doda0;
   st->coefG = coefG;
   st->coefD = coefD;
+  st->use_gp = use_gp;
   if (c.lfixstep) {
     st->alphamin = c.fixed_step;
     st->s_trial = c.fixed_step / fw;
@@ -669,7 +775,7 @@ __global__ void __launch_bounds__(256) k_exp_u(const Problem* __restrict__ probs
   const double s = (which == 0) ? st->s_trial : st->s_second;
   if (which == 0) {
     const double cg = st->coefG, cd = st->coefD;
-    const double2* Gk = P.G + (size_t)k * WW;
+    const double2* Gk = (st->use_gp ? P.pc_gp : P.G) + (size_t)k * WW;
     for (int e = threadIdx.x; e < WW; e += blockDim.x) {
       const double2 d = cadd(cscale(Gk[e], cg), cscale(Dk[e], cd));
       Dk[e] = d;

@@ -10,6 +10,7 @@
 // below 2^22), so the pairs of one diagonal d = t+u share one TMEM accumulator.  The
 // epilogue recombines the 7 diagonals exactly in int64 and converts once to FP64.
 // Truncation error: ~2^-49 relative to (row scale x column scale) per product term.
+// Widths up to 128 are handled by chunking K and N in 32-complex-column pieces.
 //
 // The product is batched as tall-skinny GEMMs (B*WP rows sharing one WP x WP operand):
 //   step 1 (group k):  rows (b, n):  Z(k,b)^T = M0(k,b)^T conj(U(k))   -> Z row-major
@@ -139,14 +140,21 @@ __device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t parity) {
   return false;
 }
 
+// Tile geometry.  Complex dimensions are processed in chunks of CW = min(WP, 32) complex
+// indices; a chunk's real index l < CW is the real part of complex index chunk*CW + l and
+// l >= CW its imaginary part.  KC = NC = 2*CW real entries per chunk, NCH chunks along K
+// and along N (W up to 128).  Shared memory holds the S digit slices of one A chunk
+// (128 x KC) and one B chunk (NC x KC); TMEM holds the S diagonals of one N chunk.
 template <int WP>
 struct TileSmem {
-  static constexpr int KR = 2 * WP;                 // real K
-  static constexpr int NR = 2 * WP;                 // real N
-  static constexpr int A_BYTES = kTileRows * KR * 2;
-  static constexpr int B_BYTES = NR * KR * 2;
-  static constexpr int TMEM_COLS = (kDiag * NR <= 128) ? 128 : ((kDiag * NR <= 256) ? 256 : 512);
-  static constexpr size_t BYTES = (size_t)kS * A_BYTES + (size_t)kS * B_BYTES + 1024;
+  static constexpr int CW = WP < 32 ? WP : 32;
+  static constexpr int KC = 2 * CW;
+  static constexpr int NC = 2 * CW;
+  static constexpr int NCH = WP / CW;
+  static constexpr int A_BYTES = kTileRows * KC * 2;
+  static constexpr int B_BYTES = NC * KC * 2;
+  static constexpr int TMEM_COLS = (kDiag * NC <= 128) ? 128 : ((kDiag * NC <= 256) ? 256 : 512);
+  static constexpr size_t BYTES = (size_t)kS * (A_BYTES + B_BYTES) + 1024;
 };
 
 }  // namespace
@@ -155,14 +163,15 @@ struct TileSmem {
 template <int WP, int STEP>
 __global__ void __launch_bounds__(256, 1) k_oz_mupdate(const Problem* __restrict__ probs, WorkMap wm, int which) {
   using L = TileSmem<WP>;
+  constexpr int CW = L::CW, KC = L::KC, NC = L::NC, NCH = L::NCH;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  unsigned char* sA = base;                                   // kS slices of A
-  unsigned char* sB = base + (size_t)kS * L::A_BYTES;          // kS slices of B
+  unsigned char* sA = base;                                   // kS slices of an A chunk
+  unsigned char* sB = base + (size_t)kS * L::A_BYTES;          // kS slices of a B chunk
   __shared__ __align__(8) uint64_t mbar;
   __shared__ uint32_t tmem_base_slot;
   __shared__ int s_rowexp[kTileRows];
-  __shared__ int s_colexp[2 * WP];
+  __shared__ int s_colexp[WP];
   __shared__ int s_bad;
 
   int g;
@@ -175,7 +184,6 @@ __global__ void __launch_bounds__(256, 1) k_oz_mupdate(const Problem* __restrict
   const int cur = st->cur;
   const double2* Unew = P.U[cur ^ 1];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  constexpr int KR = L::KR, NR = L::NR;
 
   // ---- TMEM allocation (warp 0) and barrier init
   if (warp == 0) {
@@ -189,9 +197,8 @@ __global__ void __launch_bounds__(256, 1) k_oz_mupdate(const Problem* __restrict
     s_bad = 0;
   }
 
-  // ---- B operand of the group: step 1 conj(U(k)), step 2 U(k')
+  // ---- B operand of the group: step 1 conj(U(k)), step 2 U(k'); B(K=m, N=c) = (conj) U(m, c)
   const double2* Ug = Unew + (size_t)g * WW;
-  // column scales: column c (and c+WP) of the real embedding = complex column c
   for (int c = tid; c < WP; c += blockDim.x) {
     unsigned long long mx = 0ull;
     if (c < W)
@@ -199,214 +206,199 @@ __global__ void __launch_bounds__(256, 1) k_oz_mupdate(const Problem* __restrict
         const double2 u = Ug[(size_t)c * W + m];
         mx = max(mx, max(abs_bits(u.x), abs_bits(u.y)));
       }
-    const int e = exp_above_bits(mx);
-    s_colexp[c] = e;
-    s_colexp[c + WP] = e;
+    s_colexp[c] = exp_above_bits(mx);
   }
-  __syncthreads();
-  // B^T is stored K-major: row = real output column n (0..NR), k = real K index
-  for (int e = tid; e < NR * KR; e += blockDim.x) {
-    const int ln = e & 31, wi = e >> 5;
-    const int kgroups = KR / 8;
-    const int n = (wi / kgroups) * 4 + (ln >> 3);
-    const int kk = (wi % kgroups) * 8 + (ln & 7);
-    const int cc = n % WP;           // complex column
-    const int mm = kk % WP;          // complex row (K index)
-    double val = 0.0;
-    if (cc < W && mm < W) {
-      const double2 u = Ug[(size_t)cc * W + mm];
-      // B = U (step 2) or conj(U) (step 1): B_r = Re U, B_i = +/- Im U
-      const double br = u.x, bi = (STEP == 1) ? -u.y : u.y;
-      const bool kre = kk < WP, nre = n < WP;
-      if (kre && nre) val = br;            // [B_r   B_i]
-      else if (kre && !nre) val = bi;
-      else if (!kre && nre) val = -bi;     // [-B_i  B_r]
-      else val = br;
-    }
-    int x[kS];
-    digits7(scaled_int(val, s_colexp[n]), x);
-    const uint32_t off = kmaj_off(n, kk, KR);
+
+  // slice the (nc, kc) chunk of B^T (K-major: rows = real N index within the chunk)
+  auto slice_b = [&](int nc, int kc) {
+    for (int e = tid; e < NC * KC; e += blockDim.x) {
+      const int ln = e & 31, wi = e >> 5;
+      constexpr int kgroups = KC / 8;
+      const int n = (wi / kgroups) * 4 + (ln >> 3);
+      const int kk = (wi % kgroups) * 8 + (ln & 7);
+      const bool nre = n < CW, kre = kk < CW;
+      const int cc = nc * CW + (nre ? n : n - CW);    // complex column
+      const int mm = kc * CW + (kre ? kk : kk - CW);  // complex row (K index)
+      double val = 0.0;
+      if (cc < W && mm < W) {
+        const double2 u = Ug[(size_t)cc * W + mm];
+        const double br = u.x, bi = (STEP == 1) ? -u.y : u.y;
+        if (kre && nre) val = br;            // [B_r   B_i]
+        else if (kre && !nre) val = bi;
+        else if (!kre && nre) val = -bi;     // [-B_i  B_r]
+        else val = br;
+      }
+      int x[kS];
+      digits7(scaled_int(val, s_colexp[cc < WP ? cc : 0]), x);
+      const uint32_t off = kmaj_off(n, kk, KC);
 #pragma unroll
-    for (int t = 0; t < kS; ++t) *(uint16_t*)(sB + (size_t)t * L::B_BYTES + off) = int_to_bf16(x[t]);
-  }
+      for (int t = 0; t < kS; ++t) *(uint16_t*)(sB + (size_t)t * L::B_BYTES + off) = int_to_bf16(x[t]);
+    }
+  };
 
   const int rows_group = B * WP;
   const int ntiles = (rows_group + kTileRows - 1) / kTileRows;
   __syncthreads();
+  if (NCH == 1) slice_b(0, 0);
   const uint32_t tmem = tmem_base_slot;
-  const uint32_t idesc = idesc_bf16(NR);
+  const uint32_t idesc = idesc_bf16(NC);
   uint32_t phase = 0;
 
+  // A element (row, complex K index m) of this tile
+  auto a_elem = [&](int row, int m) -> double2 {
+    const int bi = row / WP, rr = row % WP;
+    if (bi >= B || rr >= W || m >= W) return make_double2(0.0, 0.0);
+    if (STEP == 1) return P.M0[((size_t)g * B + bi) * WW + (size_t)rr * W + m];   // M0(k,b)(m, n=rr)
+    const int kb = P.inv_nnlist[(size_t)g * B + bi];
+    return P.tbuf[(size_t)kb * WW + (size_t)rr * W + m];                          // Z(k,b)(m=rr, j=m), row-major
+  };
+
   for (int tile = 0; tile < ntiles; ++tile) {
-    // ---- A rows of this tile: row r -> block i = row/WP (pair index), n/m = row%WP
-    // row scales (one thread per row pair of halves: 2 threads per row)
+    // ---- row scales over the full row (2 threads per row)
     {
       const int r = tid >> 1, half = tid & 1;
       const int row = tile * kTileRows + r;
-      const int bi = row / WP, rr = row % WP;
       unsigned long long mx = 0ull;
-      const double2* src = nullptr;
-      size_t stride = 0;
-      if (bi < B && rr < W) {
-        if (STEP == 1) {
-          // A(row=(b,n), kk) = M0(k,b)(m=kk, n): column n of block (k,b), contiguous in m
-          src = P.M0 + ((size_t)g * B + bi) * WW + (size_t)rr * W;
-          stride = 1;
-        } else {
-          // A(row=((k,b),m), kk) = Z(k,b)(m, j=kk): Z row-major, contiguous in j
-          const int kb = P.inv_nnlist[(size_t)g * B + bi];
-          src = P.tbuf + (size_t)kb * WW + (size_t)rr * W;
-          stride = 1;
-        }
-        for (int m = half; m < W; m += 2) {
-          const double2 a = src[m * stride];
-          mx = max(mx, max(abs_bits(a.x), abs_bits(a.y)));
-        }
+      for (int m = half; m < W; m += 2) {
+        const double2 a = a_elem(row, m);
+        mx = max(mx, max(abs_bits(a.x), abs_bits(a.y)));
       }
       mx = max(mx, (unsigned long long)__shfl_xor_sync(0xffffffffu, (long long)mx, 1));
       if (half == 0) s_rowexp[r] = exp_above_bits(mx);
     }
     __syncthreads();
-    for (int e = tid; e < kTileRows * WP; e += blockDim.x) {
-      // lane -> (row r within 4, m within 8): a warp writes 4 consecutive 16-byte core rows
-      const int ln = e & 31, wi = e >> 5;
-      const int mgroups = WP / 8;
-      const int r = (wi / mgroups) * 4 + (ln >> 3);
-      const int m = (wi % mgroups) * 8 + (ln & 7);
-      const int row = tile * kTileRows + r;
-      const int bi = row / WP, rr = row % WP;
-      double2 a = make_double2(0.0, 0.0);
-      if (bi < B && rr < W && m < W) {
-        if (STEP == 1) {
-          a = P.M0[((size_t)g * B + bi) * WW + (size_t)rr * W + m];
-        } else {
-          const int kb = P.inv_nnlist[(size_t)g * B + bi];
-          a = P.tbuf[(size_t)kb * WW + (size_t)rr * W + m];
-        }
-      }
-      const int ex = s_rowexp[r];
-      int xr[kS], xi[kS];
-      digits7(scaled_int(a.x, ex), xr);
-      digits7(scaled_int(a.y, ex), xi);
-      const uint32_t o_re = kmaj_off(r, m, KR), o_im = kmaj_off(r, m + WP, KR);
+    for (int nc = 0; nc < NCH; ++nc) {
+      bool ok = true;
+      for (int kc = 0; kc < NCH; ++kc) {
+        // ---- slice the kc chunk of A: a warp writes 4 consecutive 16-byte core rows
+        for (int e = tid; e < kTileRows * CW; e += blockDim.x) {
+          const int ln = e & 31, wi = e >> 5;
+          constexpr int mgroups = CW / 8;
+          const int r = (wi / mgroups) * 4 + (ln >> 3);
+          const int l = (wi % mgroups) * 8 + (ln & 7);
+          const double2 a = a_elem(tile * kTileRows + r, kc * CW + l);
+          const int ex = s_rowexp[r];
+          int xr[kS], xi[kS];
+          digits7(scaled_int(a.x, ex), xr);
+          digits7(scaled_int(a.y, ex), xi);
+          const uint32_t o_re = kmaj_off(r, l, KC), o_im = kmaj_off(r, l + CW, KC);
 #pragma unroll
-      for (int t = 0; t < kS; ++t) {
-        *(uint16_t*)(sA + (size_t)t * L::A_BYTES + o_re) = int_to_bf16(xr[t]);
-        *(uint16_t*)(sA + (size_t)t * L::A_BYTES + o_im) = int_to_bf16(xi[t]);
-      }
-    }
-    // make the generic-proxy smem writes visible to the tensor core (async proxy)
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    __syncthreads();
-
-    // ---- MMAs: pairs (t,u), t+u <= S+1 (1-based), diagonal d = t+u -> accumulator d-2
-    if (tid == 0) {
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      bool first[kDiag];
-#pragma unroll
-      for (int d = 0; d < kDiag; ++d) first[d] = true;
-      for (int t = 0; t < kS; ++t) {
-        for (int u = 0; u + t <= kS - 1; ++u) {
-          const int d = t + u;   // 0-based diagonal index (t+u+2 in 1-based digits)
-          const uint32_t dtm = tmem + (uint32_t)(d * NR);
-          const uint32_t a0 = smem_u32(sA + (size_t)t * L::A_BYTES);
-          const uint32_t b0 = smem_u32(sB + (size_t)u * L::B_BYTES);
-#pragma unroll
-          for (int ks = 0; ks < KR / 16; ++ks) {
-            const uint64_t ad = smem_desc(a0 + ks * 256, 128, (KR / 8) * 128);
-            const uint64_t bd = smem_desc(b0 + ks * 256, 128, (KR / 8) * 128);
-            const uint32_t acc = (first[d] && ks == 0) ? 0u : 1u;
-            asm volatile(
-                "{\n\t.reg .pred p;\n\t"
-                "setp.ne.b32 p, %4, 0;\n\t"
-                "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
-                :: "r"(dtm), "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
-                : "memory");
+          for (int t = 0; t < kS; ++t) {
+            *(uint16_t*)(sA + (size_t)t * L::A_BYTES + o_re) = int_to_bf16(xr[t]);
+            *(uint16_t*)(sA + (size_t)t * L::A_BYTES + o_im) = int_to_bf16(xi[t]);
           }
-          first[d] = false;
         }
+        if (NCH > 1) slice_b(nc, kc);
+        // generic-proxy smem writes -> visible to the tensor core (async proxy)
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        // ---- MMAs: digit pairs (t,u), t+u <= S-1 (0-based) -> accumulator of diagonal t+u
+        if (tid == 0) {
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          for (int t = 0; t < kS; ++t) {
+            for (int u = 0; u + t <= kS - 1; ++u) {
+              const int d = t + u;
+              const uint32_t dtm = tmem + (uint32_t)(d * NC);
+              const uint32_t a0 = smem_u32(sA + (size_t)t * L::A_BYTES);
+              const uint32_t b0 = smem_u32(sB + (size_t)u * L::B_BYTES);
+              // the first write of every diagonal d in this N chunk is pair (0, d) of chunk kc = 0
+              const bool first_pair = (kc == 0) && (t == 0);
+#pragma unroll
+              for (int ks = 0; ks < KC / 16; ++ks) {
+                const uint64_t ad = smem_desc(a0 + ks * 256, 128, (KC / 8) * 128);
+                const uint64_t bd = smem_desc(b0 + ks * 256, 128, (KC / 8) * 128);
+                const uint32_t acc = (first_pair && ks == 0) ? 0u : 1u;
+                asm volatile(
+                    "{\n\t.reg .pred p;\n\t"
+                    "setp.ne.b32 p, %4, 0;\n\t"
+                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+                    :: "r"(dtm), "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+                    : "memory");
+              }
+            }
+          }
+          asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                       :: "r"(smem_u32(&mbar)) : "memory");
+        }
+        const bool ok_mine = mbar_wait(smem_u32(&mbar), phase);
+        phase ^= 1u;
+        if (!ok_mine) s_bad = 1;
+        __syncthreads();
+        ok = (s_bad == 0);   // uniform across the CTA
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        if (!ok) break;
       }
-      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
-                   :: "r"(smem_u32(&mbar)) : "memory");
-    }
-    const bool ok_mine = mbar_wait(smem_u32(&mbar), phase);
-    phase ^= 1u;
-    if (!ok_mine) s_bad = 1;
-    __syncthreads();
-    const bool ok = (s_bad == 0);   // uniform across the CTA
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-
-    // ---- epilogue: all 8 warps; warp w reads TMEM lanes 32*(w%4).. (its sub-partition),
-    // warps w and w+4 take the lower / upper half of the complex output columns
-    if (ok) {
-      const int wq = warp & 3, half = warp >> 2;
-      const int r = wq * 32 + lane;
-      const int row = tile * kTileRows + r;
-      const int bi = row / WP, rr = row % WP;
-      const bool valid = (bi < B) && (rr < W);
-      const int erow = s_rowexp[r];
-      const uint32_t lane_base = (uint32_t)(wq * 32) << 16;
-      int kb_out = 0;
-      if (STEP == 2 && bi < B) kb_out = P.inv_nnlist[(size_t)g * B + bi];
-      const int cbeg = half * (WP / 2), cend = cbeg + WP / 2;
-      double dre = 0.0, dim = 0.0;   // this row's diagonal element, if in this half
-      bool has_diag = false;
-      // complex output column c: real part at real column c, imaginary part at c + WP
+      // ---- epilogue for N chunk nc: all 8 warps; warp w reads TMEM lanes 32*(w%4)..,
+      // warps w and w+4 take the lower / upper half of the chunk's CW complex columns
+      if (ok) {
+        const int wq = warp & 3, half = warp >> 2;
+        const int r = wq * 32 + lane;
+        const int row = tile * kTileRows + r;
+        const int bi = row / WP, rr = row % WP;
+        const bool valid = (bi < B) && (rr < W);
+        const int erow = s_rowexp[r];
+        const uint32_t lane_base = (uint32_t)(wq * 32) << 16;
+        int kb_out = 0;
+        if (STEP == 2 && bi < B) kb_out = P.inv_nnlist[(size_t)g * B + bi];
+        const int jbeg = half * (CW / 2), jend = jbeg + CW / 2;
+        double dre = 0.0, dim = 0.0;
+        bool has_diag = false;
 #pragma unroll 1
-      for (int c0 = cbeg; c0 < cend; c0 += 4) {
-        uint32_t q[kDiag][4], s4[kDiag][4];
+        for (int j0 = jbeg; j0 < jend; j0 += 4) {
+          uint32_t q[kDiag][4], s4[kDiag][4];
 #pragma unroll
-        for (int d = 0; d < kDiag; ++d) {
-          const uint32_t ta = tmem + lane_base + (uint32_t)(d * NR + c0);
-          const uint32_t tb = tmem + lane_base + (uint32_t)(d * NR + WP + c0);
-          asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
-                       : "=r"(q[d][0]), "=r"(q[d][1]), "=r"(q[d][2]), "=r"(q[d][3])
-                       : "r"(ta));
-          asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
-                       : "=r"(s4[d][0]), "=r"(s4[d][1]), "=r"(s4[d][2]), "=r"(s4[d][3])
-                       : "r"(tb));
-        }
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          const int c = c0 + j;
-          // S = sum_d D_d 2^(7(6-d)) by Horner in int64 (exact, |S| < 2^63)
-          long long sr = float_to_int_exact(__uint_as_float(q[0][j]));
-          long long si = float_to_int_exact(__uint_as_float(s4[0][j]));
-#pragma unroll
-          for (int d = 1; d < kDiag; ++d) {
-            sr = (sr << 7) + float_to_int_exact(__uint_as_float(q[d][j]));
-            si = (si << 7) + float_to_int_exact(__uint_as_float(s4[d][j]));
+          for (int d = 0; d < kDiag; ++d) {
+            const uint32_t ta = tmem + lane_base + (uint32_t)(d * NC + j0);
+            const uint32_t tb = tmem + lane_base + (uint32_t)(d * NC + CW + j0);
+            asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+                         : "=r"(q[d][0]), "=r"(q[d][1]), "=r"(q[d][2]), "=r"(q[d][3])
+                         : "r"(ta));
+            asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+                         : "=r"(s4[d][0]), "=r"(s4[d][1]), "=r"(s4[d][2]), "=r"(s4[d][3])
+                         : "r"(tb));
           }
-          // value = S * 2^(erow + ecol - 56)
-          const int sc = erow + s_colexp[c] - 56;
-          const double re = int64_scaled_to_double(sr, sc);
-          const double im = int64_scaled_to_double(si, sc);
-          if (valid && c < W) {
-            if (STEP == 1) {
-              // Z(k,b) row-major: element (j=c, n=rr) at c*W + rr
-              P.tbuf[((size_t)g * B + bi) * WW + (size_t)c * W + rr] = make_double2(re, im);
-            } else {
-              // M(k,b) column-major: element (m=rr, c) at c*W + rr
-              P.M[cur ^ 1][(size_t)kb_out * WW + (size_t)c * W + rr] = make_double2(re, im);
-              if (c == rr) {
-                dre = re;
-                dim = im;
-                has_diag = true;
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const int c = nc * CW + j0 + j;   // complex output column
+            // S = sum_d D_d 2^(7(6-d)) by Horner in int64 (exact, |S| < 2^63)
+            long long sr = float_to_int_exact(__uint_as_float(q[0][j]));
+            long long si = float_to_int_exact(__uint_as_float(s4[0][j]));
+#pragma unroll
+            for (int d = 1; d < kDiag; ++d) {
+              sr = (sr << 7) + float_to_int_exact(__uint_as_float(q[d][j]));
+              si = (si << 7) + float_to_int_exact(__uint_as_float(s4[d][j]));
+            }
+            const int sc = erow + s_colexp[c < WP ? c : 0] - 56;   // value = S 2^(erow + ecol - 56)
+            const double re = int64_scaled_to_double(sr, sc);
+            const double im = int64_scaled_to_double(si, sc);
+            if (valid && c < W) {
+              if (STEP == 1) {
+                // Z(k,b) row-major: element (j=c, n=rr) at c*W + rr
+                P.tbuf[((size_t)g * B + bi) * WW + (size_t)c * W + rr] = make_double2(re, im);
+              } else {
+                // M(k,b) column-major: element (m=rr, c) at c*W + rr
+                P.M[cur ^ 1][(size_t)kb_out * WW + (size_t)c * W + rr] = make_double2(re, im);
+                if (c == rr) {
+                  dre = re;
+                  dim = im;
+                  has_diag = true;
+                }
               }
             }
           }
         }
+        if (STEP == 2 && has_diag) {
+          // diagonal statistics (once per row); the off-diagonal sum follows from the
+          // invariant |M(k,b)|_F^2 = |M0(k,b)|_F^2 in the spread pass
+          P.diag_ln[(size_t)kb_out * W + rr] = atan2(dim, dre);
+          P.diag_abs2[(size_t)kb_out * W + rr] = dre * dre + dim * dim;
+        }
       }
-      if (STEP == 2 && has_diag) {
-        // diagonal statistics (once per row); the off-diagonal sum follows from the
-        // invariant |M(k,b)|_F^2 = |M0(k,b)|_F^2 in the spread pass
-        P.diag_ln[(size_t)kb_out * W + rr] = atan2(dim, dre);
-        P.diag_abs2[(size_t)kb_out * W + rr] = dre * dre + dim * dim;
-      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncthreads();
+      if (s_bad) break;
     }
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
     if (s_bad) break;
   }
   if (s_bad && tid == 0) {
@@ -435,7 +427,9 @@ cudaError_t oz_launch(int wp, int step, const Problem* probs, WorkMap wm, int wh
   switch (wp) {
     case 8: return oz_launch_wp<8>(step, probs, wm, which, grid, s);
     case 16: return oz_launch_wp<16>(step, probs, wm, which, grid, s);
-    default: return oz_launch_wp<32>(step, probs, wm, which, grid, s);
+    case 32: return oz_launch_wp<32>(step, probs, wm, which, grid, s);
+    case 64: return oz_launch_wp<64>(step, probs, wm, which, grid, s);
+    default: return oz_launch_wp<128>(step, probs, wm, which, grid, s);
   }
 }
 
@@ -451,7 +445,9 @@ cudaError_t oz_set_attributes(int wp) {
   switch (wp) {
     case 8: return oz_attr_wp<8>();
     case 16: return oz_attr_wp<16>();
-    default: return oz_attr_wp<32>();
+    case 32: return oz_attr_wp<32>();
+    case 64: return oz_attr_wp<64>();
+    default: return oz_attr_wp<128>();
   }
 }
 
@@ -459,7 +455,9 @@ size_t oz_smem_bytes(int wp) {
   switch (wp) {
     case 8: return TileSmem<8>::BYTES;
     case 16: return TileSmem<16>::BYTES;
-    default: return TileSmem<32>::BYTES;
+    case 32: return TileSmem<32>::BYTES;
+    case 64: return TileSmem<64>::BYTES;
+    default: return TileSmem<128>::BYTES;
   }
 }
 

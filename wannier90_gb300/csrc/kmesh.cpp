@@ -309,4 +309,55 @@ int kmesh_get(const double real_lattice[9], const double* kpt_latt, int K, int s
   return 0;
 }
 
+int ws_vectors(const double real_lattice[9], const int mp_grid[3], const int search_size[3],
+               double dist_tol, std::vector<int>& irvec, std::vector<int>& ndegen, std::string& err) {
+  // metric g_ij = a_i . a_j (utility_metric, src/utility.F90:397-423)
+  double g[9];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double a = 0.0;
+      for (int l = 0; l < 3; ++l) a += real_lattice[i * 3 + l] * real_lattice[j * 3 + l];
+      g[i * 3 + j] = a;
+    }
+  const int s1 = search_size[0], s2 = search_size[1], s3 = search_size[2];
+  const int ndist = (2 * (s1 + 1) + 1) * (2 * (s2 + 1) + 1) * (2 * (s3 + 1) + 1);
+  const int centre = (ndist - 1) / 2;   // i1 = i2 = i3 = 0
+  const double tol2 = dist_tol * dist_tol;
+  std::vector<double> dist(ndist);
+  irvec.clear();
+  ndegen.clear();
+  for (int n1 = -s1 * mp_grid[0]; n1 <= s1 * mp_grid[0]; ++n1)
+    for (int n2 = -s2 * mp_grid[1]; n2 <= s2 * mp_grid[1]; ++n2)
+      for (int n3 = -s3 * mp_grid[2]; n3 <= s3 * mp_grid[2]; ++n3) {
+        int c = 0;
+        double dmin = 1e300;
+        for (int i1 = -s1 - 1; i1 <= s1 + 1; ++i1)
+          for (int i2 = -s2 - 1; i2 <= s2 + 1; ++i2)
+            for (int i3 = -s3 - 1; i3 <= s3 + 1; ++i3) {
+              const double d[3] = {(double)(n1 - i1 * mp_grid[0]), (double)(n2 - i2 * mp_grid[1]),
+                                   (double)(n3 - i3 * mp_grid[2])};
+              double x = 0.0;
+              for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) x += d[i] * g[i * 3 + j] * d[j];
+              dist[c++] = x;
+              dmin = std::min(dmin, x);
+            }
+        if (std::fabs(dist[centre] - dmin) < tol2) {
+          int deg = 0;
+          for (int i = 0; i < ndist; ++i) deg += (std::fabs(dist[i] - dmin) < tol2) ? 1 : 0;
+          irvec.push_back(n1);
+          irvec.push_back(n2);
+          irvec.push_back(n3);
+          ndegen.push_back(deg);
+        }
+      }
+  double tot = 0.0;
+  for (int d : ndegen) tot += 1.0 / (double)d;
+  if (std::fabs(tot - (double)mp_grid[0] * mp_grid[1] * mp_grid[2]) > 1e-8) {
+    err = "hamiltonian_wigner_seitz: error in finding Wigner-Seitz points";
+    return 1;
+  }
+  return 0;
+}
+
 }  // namespace w90g

@@ -22,4 +22,10 @@ void recip_lattice(const double a[9], double b[9], double* volume);
 int kmesh_get(const double real_lattice[9], const double* kpt_latt, int K, int search_shells,
               double tol, KmeshInfo& out, std::string& err);
 
+// Wigner-Seitz points of the Born-von Karman supercell (hamiltonian_wigner_seitz,
+// src/hamiltonian.F90:689-853): irvec [nrpts][3] in the reference's loop order and the
+// degeneracies ndegen [nrpts].  Fails when the sum rule sum 1/ndegen = prod mp_grid breaks.
+int ws_vectors(const double real_lattice[9], const int mp_grid[3], const int search_size[3],
+               double dist_tol, std::vector<int>& irvec, std::vector<int>& ndegen, std::string& err);
+
 }  // namespace w90g

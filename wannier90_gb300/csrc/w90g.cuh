@@ -78,7 +78,7 @@ struct CtrlState {
   int do_second;       // second update (parabolic optimum) required this iteration
   int conv_count, noise_count, lrandom, lfirst, lconverged;
   int first_pass;
-  int pad0;
+  int use_gp;          // precond: the search direction starts from the preconditioned gradient
   // CG
   double gcnorm0, gcnorm1, gcfac, doda0;
   double coefG, coefD;   // D <- coefG*G + coefD*D_prev
@@ -133,7 +133,15 @@ struct Problem {
   CtrlState* st;
   Control ctl;
   int max_exp_squarings;
-  int pad2;
+  int precond;          // 1: precond_search_direction (src/wannierise.F90:1256-1368)
+  int nrpts;            // Wigner-Seitz points of the preconditioner
+  int pad3;
+  const double2* pc_kr;   // [k][r] exp(-i 2 pi k.R_r)
+  const double* pc_r2;    // [r] |R_r|^2 as the reference forms it
+  const double* pc_ndeg;  // [r] degeneracy of R_r
+  double2* pc_gr;         // [r][W*W] gradient in real space
+  double2* pc_gp;         // [k][W*W] preconditioned gradient
+  double* pc_part;        // [tile] Re <Gp, G> partials of the back transform
 };
 
 // Work map: blockIdx.x -> (problem, local index) over a prefix sum.

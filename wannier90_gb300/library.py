@@ -228,6 +228,24 @@ def w90_get_log_centres(common: LibCommon, max_rows: int, num_wann: int) -> np.n
     return out[:n].reshape(n, 4, num_wann)
 
 
+def ws_vectors(real_lattice, mp_grid, ws_search_size=(2, 2, 2), ws_distance_tol=1.0e-5):
+    """Wigner-Seitz points of the Born-von Karman supercell (host): (irvec[n,3], ndegen[n])."""
+    L = lib()
+    a = np.ascontiguousarray(real_lattice, dtype=np.float64)
+    mp = np.ascontiguousarray(mp_grid, dtype=np.int32)
+    ss = np.ascontiguousarray(np.broadcast_to(ws_search_size, (3,)), dtype=np.int32)
+    args = (a.ctypes.data_as(C.POINTER(C.c_double)), mp.ctypes.data_as(C.POINTER(C.c_int)),
+            ss.ctypes.data_as(C.POINTER(C.c_int)), float(ws_distance_tol))
+    n = L.w90g_ws_vectors(*args, None, None, 0)
+    if n < 0:
+        raise W90Error(1, "hamiltonian_wigner_seitz: error in finding Wigner-Seitz points")
+    irvec = np.zeros((n, 3), dtype=np.int32)
+    ndegen = np.zeros(n, dtype=np.int32)
+    L.w90g_ws_vectors(*args, irvec.ctypes.data_as(C.POINTER(C.c_int)),
+                      ndegen.ctypes.data_as(C.POINTER(C.c_int)), n)
+    return irvec, ndegen
+
+
 def w90_set_stream(common: LibCommon, cuda_stream: int):
     common._L.w90g_set_stream(common._h, C.c_void_p(cuda_stream))
 
