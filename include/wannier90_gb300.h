@@ -121,6 +121,30 @@ const char* w90g_profile_kernel_name(int i);
 double w90g_profile_exp_products(void* handle);
 /* FP64 FMA throughput of the current device in TFLOP/s (dependent-chain probe). */
 double w90g_measure_fp64_peak(void);
+/* ---- Serving loop (continuous batching).  No counterpart in the reference, which solves
+ * one problem per library call (w90_wannierise, src/library_interface.F90:464-530).
+ * A server admits queued jobs first-in first-out while the device bytes of its running
+ * jobs stay within hbm_budget_bytes and fewer than max_active jobs run; running jobs
+ * overlap on the GPU (one stream each), are polled every chunk_iters iterations, and
+ * free their memory and slot when they converge.  Each job is solved exactly as by
+ * w90g_wannierise_device on the same handle (same kernels, bitwise the same result).
+ * Thread safety: submit/poll/pending/drain may be called from any thread; a submitted
+ * handle and its buffers belong to the server until the job's tag has been polled. */
+void* w90g_server_create(double hbm_budget_bytes, int max_active, int chunk_iters);
+/* d_m / d_u: device buffers holding the projected M0 (m_matrix layout) and U0, written
+ * before the call (the caller's stream synchronised); the final M and U are written back
+ * to them.  Returns 0 (queued), 2 when the job alone exceeds the budget, 1/5 on bad input. */
+int w90g_server_submit(void* server, void* handle, double* d_m, double* d_u, long long tag);
+/* Collect up to max completed jobs: tag, ierr (as w90g_wannierise_device), and the
+ * submit / admission / completion times in seconds on the server's clock.  Returns the count. */
+int w90g_server_poll(void* server, long long* tags, int* ierr, double* t_submit, double* t_admit,
+                     double* t_done, int max);
+int w90g_server_pending(void* server);          /* queued + running jobs */
+void w90g_server_drain(void* server);           /* block until no job is queued or running */
+/* peak running jobs, peak admitted bytes, jobs completed, iterations completed */
+void w90g_server_stats(void* server, double* out4);
+double w90g_server_now(void* server);           /* the server's clock (s since creation) */
+void w90g_server_delete(void* server);          /* finishes the queued and running jobs first */
 /* Wigner-Seitz points of the Born-von Karman supercell used by the preconditioner
  * (replaces hamiltonian_wigner_seitz, src/hamiltonian.F90:689-853, as called from
  * hamiltonian_setup for wann_main, src/wannierise.F90:269-274).  Host only.

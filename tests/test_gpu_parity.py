@@ -51,6 +51,15 @@ def _check_trajectory(out, r, rel=1e-8, floor=2e-10, upto=None):
         np.testing.assert_allclose(out["spreads"], r.spreads, atol=1e-6)
 
 
+def _sensitivity(M0, U0, km, ctl, noise, precond=None):
+    """|Omega(iter)| change of the oracle's trajectory when M0 is perturbed by `noise`
+    (relative), per iteration (0 = initial spread)."""
+    rng = np.random.default_rng(12345)
+    a = O.wann_main(M0, U0, km, ctl, precond=precond)
+    b = O.wann_main(M0 * (1 + noise * rng.standard_normal(M0.shape)), U0, km, ctl, precond=precond)
+    return {x.iter: abs(x.spread.om_tot - y.spread.om_tot) for x, y in zip([a.initial] + a.iters, [b.initial] + b.iters)}
+
+
 def _stable_window(M0, U0, km, ctl, tol=1e-11, noise=1e-15, precond=None):
     """Last iteration up to which the oracle agrees with itself on an input perturbed by
     `noise` (relative): 1e-15 for the FP64 engine, 1e-13 for the tensor engine, whose
@@ -84,20 +93,31 @@ def test_golden_cases(name, tensor):
     U0, M0 = O.overlap_project(M, A, km["nnlist"])
     np.testing.assert_allclose(out["U0"], U0, atol=1e-11)
     np.testing.assert_allclose(out["M0"], M0, atol=1e-11)
-    r = O.wann_main(M0, U0, km, ctl, precond=G.precond_tables(d))
+    pc = G.precond_tables(d)
+    r = O.wann_main(M0, U0, km, ctl, precond=pc)
     _check_trajectory(out, r, floor=1e-11)
-    # against the reference's printed <-- CONV lines directly
+    # against the reference's printed <-- CONV lines directly: 2e-10 A^2 wherever the
+    # trajectory is insensitive to the Loewdin step's roundoff, which is amplified by
+    # cond(A^H A) (1e0..1e2 for Pb/GaAs/diamond/basic1, 5.8e5 for the precond cases,
+    # whose middle iterations then move by up to 1e-8 A^2 between equally valid
+    # projections); elsewhere the metric's 1e-8 relative
+    cond = max(np.linalg.cond(a) ** 2 for a in A)
+    sens = _sensitivity(M0, U0, km, ctl, noise=max(1e-15, 1e-16 * cond), precond=pc)
     by_iter = {int(row[0]): row for row in out["log"]}
     for it, delta, rms, spread in d["conv"]:
-        assert abs(by_iter[int(it)][3] - spread) < 2e-10
+        tol = 2e-10 if sens.get(int(it), 0.0) < 2e-11 else 1e-8 * spread
+        assert abs(by_iter[int(it)][3] - spread) < tol, (int(it), by_iter[int(it)][3], spread, tol)
     np.testing.assert_allclose(out["centres"].T, d["centres_final"][:, :3], atol=1.01e-6)
     # Omega_I and Omega_total are stationary at the minimum and match the printed 9
     # decimals; the Omega_D / Omega_OD split moves with the sqrt(eps)-level gauge freedom
     om = out["omega"]
     np.testing.assert_allclose(om[[0, 3]], d["omega_final"][[0, 3]], atol=1.01e-9)
     np.testing.assert_allclose(om[[1, 2]], d["omega_final"][[1, 2]], atol=5e-9)
-    np.testing.assert_allclose(out["U"], r.U, atol=1e-7)
-    np.testing.assert_allclose(out["M"], r.M, atol=1e-7)
+    # the gauge at the minimum is fixed only to ~sqrt(eps), more loosely when the
+    # projection is ill-conditioned (precond cases, cond(A^H A) = 5.8e5)
+    utol = 1e-7 if cond < 1e3 else 1e-6
+    np.testing.assert_allclose(out["U"], r.U, atol=utol)
+    np.testing.assert_allclose(out["M"], r.M, atol=utol)
 
 
 def _synthetic(cfg, num_iter, seed=0, tensor=0, **ctl_kw):
@@ -196,3 +216,27 @@ def test_tensor_matches_fp64_first_iterations(W, mp):
     np.testing.assert_allclose(b["log"][:, 3], a["log"][:, 3], rtol=1e-12)
     np.testing.assert_allclose(b["U"], a["U"], atol=1e-11)
     np.testing.assert_allclose(b["M"], a["M"], atol=1e-11)
+
+
+@pytest.mark.parametrize("W,mp", [(8, (3, 3, 3)), (32, (3, 3, 3)), (64, (2, 2, 2)), (100, (2, 2, 2))])
+def test_tensor_exp_matches_fp64_exp(W, mp):
+    """exp(s D) and U dU on the tensor cores (gpu_tensor_exp = 1, the default) against
+    the same tensor M update with the FP64 exp: spreads to 1e-10 relative over the
+    oracle's stable window for 1e-13 input noise (the two exps pick different Taylor
+    degrees and squarings, each FP64-accurate), and U as unitary as with FP64 products."""
+    cfg = dict(kind="sc", a=4.0, mp=mp, num_wann=W, rmax=1, eps=0.3)
+    p = synth.make_problem(**cfg, seed=1)
+    M = synth.to_math_m(p.m)
+    A = synth.to_math_u(p.a)
+    ctl = O.WannControl(num_iter=8)
+    a = run_engine(p.real_lattice, p.kpoints, M, A, ctl, W, extra={"gpu_tensor": 1, "gpu_tensor_exp": 0})
+    b = run_engine(p.real_lattice, p.kpoints, M, A, ctl, W, extra={"gpu_tensor": 1, "gpu_tensor_exp": 1})
+    assert a["ierr"] == 0 and b["ierr"] == 0, (a["err"], b["err"])
+    km, U0, M0, r = _oracle(p.real_lattice, p.kpoints, M, A, ctl)
+    window = _stable_window(M0, U0, km, ctl, noise=1e-13)
+    assert window >= 1
+    np.testing.assert_allclose(b["log"][: window + 1, 3], a["log"][: window + 1, 3], rtol=1e-10)
+
+    def unitarity(U):
+        return max(np.abs(U[k] @ U[k].conj().T - np.eye(W)).max() for k in range(len(U)))
+    assert unitarity(b["U"]) < max(1e-13, 4 * unitarity(a["U"]))

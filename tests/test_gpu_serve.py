@@ -1,0 +1,81 @@
+"""Serving form: jobs admitted by HBM budget while others run give exactly their
+stand-alone results; admission respects the budget and the slot count."""
+import time
+
+import numpy as np
+import pytest
+
+from wannier90_gb300 import library as w90
+from wannier90_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+# (W, mp, tensor, conv_window): uneven widths, both M-update variants, jobs that stop
+# at convergence (window 3) at different iterations and jobs that run num_iter
+JOBS = [
+    (4, (3, 3, 3), 1, 3), (8, (2, 2, 2), 1, 3), (13, (3, 3, 3), 1, -1), (20, (2, 2, 2), 1, 3),
+    (33, (2, 2, 2), 1, 3), (8, (3, 3, 3), 0, 3), (6, (4, 4, 4), 1, -1), (40, (2, 2, 2), 0, 3),
+    (16, (4, 4, 4), 1, 3), (24, (3, 3, 3), 0, -1),
+]
+NUM_ITER = 60
+
+
+def _job(i):
+    torch = pytest.importorskip("torch")
+    W, mp, tensor, window = JOBS[i]
+    p = synth.make_problem(kind="sc", a=3.0 + 0.4 * i, mp=mp, num_wann=W, rmax=1, eps=0.3, seed=200 + i)
+    h = w90.setup(kpoints=p.kpoints, unit_cell_cart=p.real_lattice, num_wann=W, num_iter=NUM_ITER, iprint=0,
+                  gpu_tensor=tensor, conv_window=window, conv_tol=1e-8)
+    m = torch.from_numpy(p.m.reshape(-1, order="F").view(np.float64).copy()).cuda()
+    u = torch.from_numpy(p.a.reshape(-1, order="F").view(np.float64).copy()).cuda()
+    assert w90.w90_project_overlap_device(h, m.data_ptr(), u.data_ptr()) == 0, h.last_error()
+    return h, m, u
+
+
+def test_served_jobs_equal_standalone_runs():
+    torch = pytest.importorskip("torch")
+    jobs, alone = [], []
+    for i in range(len(JOBS)):
+        h, m, u = _job(i)
+        torch.cuda.synchronize()
+        m1, u1 = m.clone(), u.clone()
+        assert w90.w90_wannierise_device(h, m1.data_ptr(), u1.data_ptr()) == 0, h.last_error()
+        torch.cuda.synchronize()
+        alone.append((m1.cpu().numpy(), u1.cpu().numpy(), w90.w90_get_log(h, NUM_ITER + 1).copy(),
+                      w90.w90_get_centres(h, JOBS[i][0]).copy()))
+        jobs.append((h, m, u))
+    torch.cuda.synchronize()
+    # budget for about three of the larger jobs at once, four slots: jobs queue and are
+    # admitted as memory and slots free up
+    from wannier90_gb300 import _native  # noqa: F401
+    sizes = sorted((m.numel() + u.numel()) * 8 for _, m, u in jobs)
+    budget = 8.0 * sum(sizes[-3:])
+    srv = w90.Server(budget, max_active=4, chunk_iters=4)
+    for tag, (h, m, u) in enumerate(jobs):
+        assert srv.submit(h, m.data_ptr(), u.data_ptr(), tag) == 0, h.last_error()
+        time.sleep(0.002 * (tag % 3))   # staggered arrivals
+    srv.drain()
+    done = srv.poll()
+    stats = srv.stats()
+    srv.close()
+    assert sorted(d[0] for d in done) == list(range(len(JOBS)))
+    assert all(d[1] == 0 for d in done), [(d[0], jobs[d[0]][0].last_error()) for d in done if d[1]]
+    assert all(d[2] <= d[3] <= d[4] for d in done)
+    assert 1 <= stats["peak_active"] <= 4 and stats["peak_bytes"] <= budget
+    for i, (h, m, u) in enumerate(jobs):
+        m_a, u_a, log_a, cen_a = alone[i]
+        log_b = w90.w90_get_log(h, NUM_ITER + 1)
+        assert log_b.shape == log_a.shape, (i, log_b.shape, log_a.shape)
+        np.testing.assert_array_equal(log_b[:, :8], log_a[:, :8])   # same trajectory, bit for bit
+        np.testing.assert_array_equal(m.cpu().numpy(), m_a)
+        np.testing.assert_array_equal(u.cpu().numpy(), u_a)
+        np.testing.assert_array_equal(w90.w90_get_centres(h, JOBS[i][0]), cen_a)
+
+
+def test_server_rejects_job_above_budget():
+    h, m, u = _job(0)
+    srv = w90.Server(1024.0, max_active=2)
+    assert srv.submit(h, m.data_ptr(), u.data_ptr(), 7) == 2
+    assert "budget" in h.last_error()
+    assert srv.pending() == 0
+    srv.close()

@@ -49,6 +49,15 @@ SIGNATURES = [
     ("w90g_profile_kernel_name", C.c_char_p, [C.c_int]),
     ("w90g_profile_exp_products", C.c_double, [C.c_void_p]),
     ("w90g_measure_fp64_peak", C.c_double, []),
+    ("w90g_server_create", C.c_void_p, [C.c_double, C.c_int, C.c_int]),
+    ("w90g_server_submit", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_longlong]),
+    ("w90g_server_poll", C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), _c_int_p, _c_double_p, _c_double_p,
+                                   _c_double_p, C.c_int]),
+    ("w90g_server_pending", C.c_int, [C.c_void_p]),
+    ("w90g_server_drain", None, [C.c_void_p]),
+    ("w90g_server_stats", None, [C.c_void_p, _c_double_p]),
+    ("w90g_server_now", C.c_double, [C.c_void_p]),
+    ("w90g_server_delete", None, [C.c_void_p]),
     ("w90g_ws_vectors", C.c_int, [_c_double_p, _c_int_p, _c_int_p, C.c_double, _c_int_p, _c_int_p, C.c_int]),
     ("w90g_project_overlap_noalloc", C.c_int,
      [C.c_int, C.c_int, C.c_int, _c_int_p, C.c_void_p, C.c_void_p, C.c_void_p]),

@@ -10,6 +10,9 @@
 
 #include <algorithm>
 #include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <mutex>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -50,6 +53,7 @@ struct Handle {
   int search_shells = 36;
   double kmesh_tol = 1.0e-6;
   int gpu_tensor = 0;   // M update on tensor cores (W <= 128)
+  int gpu_tensor_exp = 1;
   KmeshInfo km;
   // preconditioner tables (precond = T), built at cinput_setopt like wann_main's
   // hamiltonian_setup / k_to_r (src/wannierise.F90:269-300)
@@ -210,6 +214,7 @@ int build_spec(Handle* h, ProblemSpec& s) {
   s.wb = h->km.wb;
   s.ctl = h->ctl;
   s.tensor = h->gpu_tensor;
+  s.tensor_exp = h->gpu_tensor_exp;
   s.precond = h->precond;
   s.nrpts = h->nrpts;
   s.pc_kr = h->pc_kr;
@@ -241,6 +246,25 @@ int do_project(Handle* h, double* m, double* u, cudaMemcpyKind in, cudaMemcpyKin
   return 0;
 }
 
+// copy one solve's result into the handle (the library's wannier_data / omega fields);
+// returns the ierr of the solve (non-finite spread, failed unitarity check)
+int apply_result(Handle* h, const w90g::ProblemResult& r, bool print) {
+  h->omega[0] = r.spread.om_i;
+  h->omega[1] = r.spread.om_d;
+  h->omega[2] = r.spread.om_od;
+  h->omega[3] = r.spread.om_tot;
+  h->centres = r.centres;
+  h->spreads = r.spreads;
+  h->log = r.log;
+  h->log_centres = r.log_centres;
+  h->niter = r.niter;
+  h->have_result = true;
+  if (print && h->iprint > 0) print_wout(h, r);
+  if (r.error) return fail(h, 1, "non-finite spread in the engine");
+  if (!(r.unitarity_err <= 1e-5)) return fail(h, 1, "wann_check_unitarity: unitariety of final U violated");
+  return 0;
+}
+
 int do_wannierise(Handle* h, double* m, double* u, cudaMemcpyKind in, cudaMemcpyKind out) {
   if (!h->setup_complete) return fail(h, 1, "cinput_setopt must be called before cwannierise");
   if (!m) return fail(h, 1, "m_matrix_local not set for wannierise");
@@ -255,28 +279,184 @@ int do_wannierise(Handle* h, double* m, double* u, cudaMemcpyKind in, cudaMemcpy
   if (!rc) rc = e->wannierise(err);
   if (!rc) rc = e->store(0, m, u, out, err);
   if (rc) return fail(h, rc, err);
-  const auto& r = e->result(0);
-  if (r.error) {
-    rc = 1;
-    err = "non-finite spread in the engine";
-  } else if (!(r.unitarity_err <= 1e-5)) {
-    rc = 1;
-    err = "wann_check_unitarity: unitariety of final U violated";
-  }
-  h->omega[0] = r.spread.om_i;
-  h->omega[1] = r.spread.om_d;
-  h->omega[2] = r.spread.om_od;
-  h->omega[3] = r.spread.om_tot;
-  h->centres = r.centres;
-  h->spreads = r.spreads;
-  h->log = r.log;
-  h->log_centres = r.log_centres;
-  h->niter = r.niter;
-  h->have_result = true;
-  if (h->iprint > 0) print_wout(h, r);
-  if (rc) return fail(h, rc, err);
-  return 0;
+  return apply_result(h, e->result(0), true);
 }
+
+// ----------------------------------------------------------------------------
+// Serving loop (continuous batching).  Jobs are admitted first-in first-out while the
+// device bytes of the running jobs stay within the HBM budget and a slot is free; each
+// admitted job gets its own engine on its slot's stream, so the kernels of all running
+// jobs overlap on the GPU.  One worker thread keeps two chunks of graph replays in
+// flight per job and polls each chunk's "all done" word through a pinned host flag and
+// an event; a finished job is rotated back into the caller's buffers, its results are
+// written to its handle, and its memory and slot go to the next job in the queue.
+// ----------------------------------------------------------------------------
+struct ServeJob {
+  long long tag = 0;
+  Handle* h = nullptr;
+  double* d_m = nullptr;
+  double* d_u = nullptr;
+  ProblemSpec spec;
+  size_t bytes = 0;
+  double t_submit = 0.0, t_admit = 0.0;
+  int slot = -1;
+  std::unique_ptr<Engine> eng;
+  int inflight = 0;   // chunks in flight (0..2)
+  int head = 0;       // flag/event index (0/1) of the oldest chunk in flight
+};
+
+struct ServeDone {
+  long long tag;
+  int ierr;
+  double t_submit, t_admit, t_done;
+};
+
+struct Server {
+  size_t budget = 0;
+  int max_active = 0, chunk = 8, device = 0;
+  std::mutex mu;
+  std::condition_variable cv;
+  std::deque<std::unique_ptr<ServeJob>> queue;   // guarded by mu
+  std::vector<ServeDone> done;                   // guarded by mu
+  int pending = 0;                               // queued + running, guarded by mu
+  bool stop = false;                             // guarded by mu
+  std::vector<std::unique_ptr<ServeJob>> active; // worker thread only
+  size_t used = 0;                               // worker thread only
+  std::vector<int> free_slots;                   // worker thread only
+  std::vector<cudaStream_t> streams;
+  std::vector<cudaEvent_t> events;               // 2 per slot
+  int* d_flags = nullptr;                        // 2 per slot
+  int* h_flags = nullptr;                        // pinned, 2 per slot
+  std::thread worker;
+  std::chrono::steady_clock::time_point t0;
+  // statistics
+  int peak_active = 0;
+  size_t peak_bytes = 0;
+  long long jobs_done = 0, iters_done = 0;
+
+  double now() const {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  }
+  void finish_job(ServeJob& j, int ierr) {
+    std::lock_guard<std::mutex> lk(mu);
+    done.push_back({j.tag, ierr, j.t_submit, j.t_admit, now()});
+    --pending;
+    ++jobs_done;
+    cv.notify_all();
+  }
+  void start(ServeJob& j) {
+    std::string err;
+    j.eng.reset(new Engine());
+    j.eng->set_stream(streams[j.slot]);
+    j.eng->set_async_alloc(true);
+    int rc = j.eng->setup({j.spec}, err);
+    if (!rc) rc = j.eng->load(0, j.d_m, j.d_u, cudaMemcpyDeviceToDevice, err);
+    if (!rc) rc = j.eng->begin(err);
+    j.t_admit = now();
+    if (rc) j.h->last_error = err;
+    j.inflight = 0;
+    j.head = 0;
+    if (rc) {
+      j.eng.reset();
+      finish_job(j, fail(j.h, rc, err));
+      j.h = nullptr;   // completed
+    }
+  }
+  int launch_chunk(ServeJob& j) {
+    std::string err;
+    const int idx = (j.head + j.inflight) & 1;
+    const int f = j.slot * 2 + idx;
+    int rc = j.eng->advance(chunk, d_flags + f, err);
+    if (!rc && cudaMemcpyAsync(h_flags + f, d_flags + f, sizeof(int), cudaMemcpyDeviceToHost, streams[j.slot]) != cudaSuccess) rc = 1;
+    if (!rc && cudaEventRecord(events[f], streams[j.slot]) != cudaSuccess) rc = 1;
+    if (rc) j.h->last_error = err.empty() ? std::string("serve: chunk launch failed") : err;
+    ++j.inflight;
+    return rc;
+  }
+  void complete(ServeJob& j) {
+    std::string err;
+    int rc = j.eng->finish(err);
+    if (!rc) rc = j.eng->store(0, j.d_m, j.d_u, cudaMemcpyDeviceToDevice, err);
+    int ierr = rc ? fail(j.h, rc, err) : apply_result(j.h, j.eng->result(0), false);
+    iters_done += j.eng->result(0).niter;
+    j.eng.reset();   // arena freed stream-ordered on the slot's stream
+    finish_job(j, ierr);
+  }
+  void run() {
+    cudaSetDevice(device);
+    for (;;) {
+      bool progress = false;
+      std::vector<std::unique_ptr<ServeJob>> admit;
+      {
+        std::unique_lock<std::mutex> lk(mu);
+        while (!queue.empty() && !free_slots.empty() && used + queue.front()->bytes <= budget) {
+          std::unique_ptr<ServeJob> j = std::move(queue.front());
+          queue.pop_front();
+          j->slot = free_slots.back();
+          free_slots.pop_back();
+          used += j->bytes;
+          admit.push_back(std::move(j));
+        }
+        if (stop && queue.empty() && active.empty() && admit.empty()) break;
+      }
+      for (auto& j : admit) {
+        progress = true;
+        start(*j);
+        if (!j->h) {   // failed at start
+          used -= j->bytes;
+          free_slots.push_back(j->slot);
+          continue;
+        }
+        active.push_back(std::move(j));
+      }
+      peak_active = std::max(peak_active, (int)active.size());
+      peak_bytes = std::max(peak_bytes, used);
+      for (size_t i = 0; i < active.size();) {
+        ServeJob& j = *active[i];
+        bool failed = false;
+        while (j.inflight < 2 && j.eng->launched_iters() < j.eng->max_iter() && !failed) failed = launch_chunk(j) != 0;
+        bool finished = failed;
+        if (!failed && j.inflight > 0) {
+          const int f = j.slot * 2 + j.head;
+          const cudaError_t q = cudaEventQuery(events[f]);
+          if (q == cudaSuccess) {
+            progress = true;
+            --j.inflight;
+            j.head ^= 1;
+            if (h_flags[f]) finished = true;
+          } else if (q != cudaErrorNotReady) {
+            j.h->last_error = std::string("serve: ") + cudaGetErrorString(q);
+            failed = finished = true;
+          }
+        } else if (!failed) {
+          finished = true;   // every iteration launched and retired
+        }
+        if (finished) {
+          // drain the other chunk still in flight (a no-op replay) before rotating back
+          cudaStreamSynchronize(streams[j.slot]);
+          if (failed) {
+            j.eng.reset();
+            finish_job(j, fail(j.h, 1, j.h->last_error));
+          } else {
+            complete(j);
+          }
+          used -= j.bytes;
+          free_slots.push_back(j.slot);
+          active.erase(active.begin() + (long)i);
+          progress = true;
+          continue;
+        }
+        ++i;
+      }
+      if (!progress) {
+        std::unique_lock<std::mutex> lk(mu);
+        cv.wait_for(lk, std::chrono::microseconds(20));
+      }
+    }
+  }
+};
+
+Server* SV(void* s) { return static_cast<Server*>(s); }
 
 }  // namespace
 
@@ -390,6 +570,8 @@ void cinput_setopt(void* hv, const char* seedname, int* ierr, int comm) {
   h->kmesh_tol = get_num(h, "kmesh_tol", v) ? v : 1.0e-6;
   // engine key: gpu_tensor = 1 computes M(k,b) = U^H M0 U' on tensor cores (W <= 128)
   h->gpu_tensor = get_num(h, "gpu_tensor", v) ? (int)v : 0;
+  // with gpu_tensor: gpu_tensor_exp = 1 (default) also runs exp(s D) and U dU on tensor cores
+  h->gpu_tensor_exp = get_num(h, "gpu_tensor_exp", v) ? (int)v : 1;
   // options on wann_main's code path that the engine does not implement
   const char* unsupported[] = {"guiding_centres", "slwf_num", "slwf_constrain", "site_symmetry",
                                "gamma_only"};
@@ -658,23 +840,124 @@ void w90g_wannierise_batch_device(void** handles, int nprob, double** d_m, doubl
         ierr[g.idx[j]] = fail(h, g.rc, g.err);
         continue;
       }
-      const auto& r = g.eng->result((int)j);
-      h->omega[0] = r.spread.om_i;
-      h->omega[1] = r.spread.om_d;
-      h->omega[2] = r.spread.om_od;
-      h->omega[3] = r.spread.om_tot;
-      h->centres = r.centres;
-      h->spreads = r.spreads;
-      h->log = r.log;
-      h->log_centres = r.log_centres;
-      h->niter = r.niter;
-      h->have_result = true;
-      if (r.error) ierr[g.idx[j]] = fail(h, 1, "non-finite spread in the engine");
-      else if (!(r.unitarity_err <= 1e-5)) ierr[g.idx[j]] = fail(h, 1, "wann_check_unitarity: unitariety of final U violated");
+      ierr[g.idx[j]] = apply_result(h, g.eng->result((int)j), false);
     }
     g.eng.reset();
     if (g.stream) cudaStreamDestroy(g.stream);
   }
+}
+
+void* w90g_server_create(double hbm_budget_bytes, int max_active, int chunk_iters) {
+  Server* sv = new Server();
+  sv->budget = hbm_budget_bytes > 0 ? (size_t)hbm_budget_bytes : 0;
+  sv->max_active = std::max(1, std::min(max_active, 1024));
+  sv->chunk = std::max(1, chunk_iters);
+  sv->t0 = std::chrono::steady_clock::now();
+  cudaGetDevice(&sv->device);
+  const int n = sv->max_active;
+  bool ok = cudaMalloc(&sv->d_flags, (size_t)2 * n * sizeof(int)) == cudaSuccess &&
+            cudaHostAlloc(&sv->h_flags, (size_t)2 * n * sizeof(int), cudaHostAllocDefault) == cudaSuccess;
+  for (int i = 0; i < n && ok; ++i) {
+    cudaStream_t st;
+    ok = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) == cudaSuccess;
+    if (ok) sv->streams.push_back(st);
+    for (int e = 0; e < 2 && ok; ++e) {
+      cudaEvent_t ev;
+      ok = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) == cudaSuccess;
+      if (ok) sv->events.push_back(ev);
+    }
+    sv->free_slots.push_back(n - 1 - i);
+  }
+  if (!ok) {
+    w90g_server_delete(sv);
+    return nullptr;
+  }
+  sv->worker = std::thread([sv]() { sv->run(); });
+  return sv;
+}
+
+int w90g_server_submit(void* server, void* handle, double* d_m, double* d_u, long long tag) {
+  Server* sv = SV(server);
+  Handle* h = H(handle);
+  if (!sv || !h) return 1;
+  if (!h->setup_complete || !d_m || !d_u) return fail(h, 1, "serve: handle not set up or buffers missing");
+  if (h->num_bands != h->num_wann)
+    return fail(h, 5, "serve: disentanglement (num_bands > num_wann) is not supported by the GPU engine");
+  std::unique_ptr<ServeJob> j(new ServeJob());
+  j->tag = tag;
+  j->h = h;
+  j->d_m = d_m;
+  j->d_u = d_u;
+  build_spec(h, j->spec);
+  j->bytes = Engine::estimate_bytes({j->spec});
+  if (j->bytes > sv->budget) return fail(h, 2, "serve: job needs more device memory than the server's budget");
+  std::lock_guard<std::mutex> lk(sv->mu);
+  j->t_submit = sv->now();
+  sv->queue.push_back(std::move(j));
+  ++sv->pending;
+  sv->cv.notify_all();
+  return 0;
+}
+
+int w90g_server_poll(void* server, long long* tags, int* ierr, double* t_submit, double* t_admit, double* t_done,
+                     int max) {
+  Server* sv = SV(server);
+  std::lock_guard<std::mutex> lk(sv->mu);
+  const int n = std::min(max, (int)sv->done.size());
+  for (int i = 0; i < n; ++i) {
+    const ServeDone& d = sv->done[i];
+    if (tags) tags[i] = d.tag;
+    if (ierr) ierr[i] = d.ierr;
+    if (t_submit) t_submit[i] = d.t_submit;
+    if (t_admit) t_admit[i] = d.t_admit;
+    if (t_done) t_done[i] = d.t_done;
+  }
+  sv->done.erase(sv->done.begin(), sv->done.begin() + n);
+  return n;
+}
+
+int w90g_server_pending(void* server) {
+  Server* sv = SV(server);
+  std::lock_guard<std::mutex> lk(sv->mu);
+  return sv->pending;
+}
+
+void w90g_server_drain(void* server) {
+  Server* sv = SV(server);
+  std::unique_lock<std::mutex> lk(sv->mu);
+  sv->cv.wait(lk, [sv]() { return sv->pending == 0; });
+}
+
+void w90g_server_stats(void* server, double* out4) {
+  Server* sv = SV(server);
+  std::lock_guard<std::mutex> lk(sv->mu);
+  out4[0] = sv->peak_active;
+  out4[1] = (double)sv->peak_bytes;
+  out4[2] = (double)sv->jobs_done;
+  out4[3] = (double)sv->iters_done;
+}
+
+double w90g_server_now(void* server) { return SV(server)->now(); }
+
+void w90g_server_delete(void* server) {
+  Server* sv = SV(server);
+  if (!sv) return;
+  if (sv->worker.joinable()) {
+    {
+      std::lock_guard<std::mutex> lk(sv->mu);
+      sv->stop = true;
+      sv->cv.notify_all();
+    }
+    sv->worker.join();
+  }
+  for (auto st : sv->streams) {
+    cudaStreamSynchronize(st);
+    cudaStreamDestroy(st);
+  }
+  for (auto ev : sv->events) cudaEventDestroy(ev);
+  if (sv->d_flags) cudaFree(sv->d_flags);
+  if (sv->h_flags) cudaFreeHost(sv->h_flags);
+  delete sv;
 }
 
 long long w90g_kernel_launches(void* hv) {

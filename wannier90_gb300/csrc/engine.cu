@@ -1,6 +1,7 @@
 // Host orchestration of the GB300 MLWF engine.
 //
-// Memory: one cudaMalloc arena per batch, sub-allocated at 256-byte alignment; every
+// Memory: one arena per batch (cudaMalloc, or stream-ordered cudaMallocAsync for the
+// serving loop), sub-allocated at 256-byte alignment; every
 // per-problem array of the iteration stays resident in HBM for the whole solve.
 // Launch: the 14-kernel iteration (16 with the tensor-core M update, +2 with the
 // preconditioner; see k_fp64.cu) is captured once into a CUDA graph
@@ -40,6 +41,8 @@ __global__ void k_precond(const Problem* probs, int dir);
 cudaError_t oz_launch(int wp, int step, const Problem* probs, WorkMap wm, int which, int grid,
                       cudaStream_t s);
 cudaError_t oz_set_attributes(int wp);
+cudaError_t oz_exp_launch(int wp, const Problem* probs, WorkMap wm, int which, int grid, cudaStream_t s);
+cudaError_t oz_exp_set_attributes(int wp);
 
 const char* kProfNames[kPNum] = {"k_grad", "k_ctrl_search", "k_exp_u", "k_m_update",
                                  "k_omega", "k_ctrl_step", "k_ctrl_end", "init", "k_precond"};
@@ -66,7 +69,10 @@ Engine::~Engine() { release(); }
 void Engine::release() {
   if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
   graph_exec_ = nullptr;
-  if (arena_) cudaFree(arena_);
+  if (arena_) {
+    if (async_alloc_) cudaFreeAsync(arena_, stream());
+    else cudaFree(arena_);
+  }
   arena_ = nullptr;
   arena_bytes_ = 0;
   if (own_stream_) cudaStreamDestroy(own_stream_);
@@ -96,7 +102,8 @@ int Engine::setup(const std::vector<ProblemSpec>& specs, std::string& err) {
   // layout key: reuse the arena when the problem shapes are unchanged
   std::ostringstream key;
   for (const auto& s : specs)
-    key << s.W << ',' << s.K << ',' << s.B << ',' << s.ctl.num_iter << ',' << s.tensor << ',' << s.precond << ','
+    key << s.W << ',' << s.K << ',' << s.B << ',' << s.ctl.num_iter << ',' << s.tensor << ',' << s.tensor_exp << ','
+        << s.precond << ','
         << s.nrpts << ';';
   specs_ = specs;
   if (arena_ && key.str() == layout_key_) {
@@ -104,18 +111,18 @@ int Engine::setup(const std::vector<ProblemSpec>& specs, std::string& err) {
     for (size_t p = 0; p < specs_.size(); ++p) {
       const auto& s = specs_[p];
       const Problem& P = hprobs_[p];
-      W90G_CHECK(cudaMemcpy((void*)P.nnlist, s.nnlist.data(), s.nnlist.size() * sizeof(int), cudaMemcpyHostToDevice));
-      W90G_CHECK(cudaMemcpy((void*)P.bk, s.bk.data(), s.bk.size() * sizeof(double), cudaMemcpyHostToDevice));
-      W90G_CHECK(cudaMemcpy((void*)P.wb, s.wb.data(), s.wb.size() * sizeof(double), cudaMemcpyHostToDevice));
+      W90G_CHECK(cudaMemcpyAsync((void*)P.nnlist, s.nnlist.data(), s.nnlist.size() * sizeof(int), cudaMemcpyHostToDevice, stream()));
+      W90G_CHECK(cudaMemcpyAsync((void*)P.bk, s.bk.data(), s.bk.size() * sizeof(double), cudaMemcpyHostToDevice, stream()));
+      W90G_CHECK(cudaMemcpyAsync((void*)P.wb, s.wb.data(), s.wb.size() * sizeof(double), cudaMemcpyHostToDevice, stream()));
       if (s.precond) {
-        W90G_CHECK(cudaMemcpy((void*)P.pc_kr, s.pc_kr.data(), s.pc_kr.size() * 8, cudaMemcpyHostToDevice));
-        W90G_CHECK(cudaMemcpy((void*)P.pc_r2, s.pc_r2.data(), s.pc_r2.size() * 8, cudaMemcpyHostToDevice));
-        W90G_CHECK(cudaMemcpy((void*)P.pc_ndeg, s.pc_ndeg.data(), s.pc_ndeg.size() * 8, cudaMemcpyHostToDevice));
+        W90G_CHECK(cudaMemcpyAsync((void*)P.pc_kr, s.pc_kr.data(), s.pc_kr.size() * 8, cudaMemcpyHostToDevice, stream()));
+        W90G_CHECK(cudaMemcpyAsync((void*)P.pc_r2, s.pc_r2.data(), s.pc_r2.size() * 8, cudaMemcpyHostToDevice, stream()));
+        W90G_CHECK(cudaMemcpyAsync((void*)P.pc_ndeg, s.pc_ndeg.data(), s.pc_ndeg.size() * 8, cudaMemcpyHostToDevice, stream()));
       }
       hprobs_[p].ctl = s.ctl;
       hprobs_[p].wbtot = s.wbtot;
     }
-    W90G_CHECK(cudaMemcpy(dprobs_, hprobs_.data(), hprobs_.size() * sizeof(Problem), cudaMemcpyHostToDevice));
+    W90G_CHECK(cudaMemcpyAsync(dprobs_, hprobs_.data(), hprobs_.size() * sizeof(Problem), cudaMemcpyHostToDevice, stream()));
     return 0;
   }
   release();
@@ -123,30 +130,98 @@ int Engine::setup(const std::vector<ProblemSpec>& specs, std::string& err) {
   return alloc(err);
 }
 
+namespace {
+
+// tensor-core M update: every problem asks for it, W <= 128, and every k' has exactly
+// B predecessors (k,b) (true on Monkhorst-Pack meshes); returns the padded width or 0
+int choose_tensor_wp(const std::vector<ProblemSpec>& specs) {
+  bool ok = !specs.empty();
+  int wmax = 0;
+  for (const auto& s : specs) {
+    ok = ok && s.tensor && s.W <= 128;
+    wmax = std::max(wmax, s.W);
+    if (!ok) break;
+    std::vector<int> cnt(s.K, 0);
+    for (int v : s.nnlist) cnt[v]++;
+    for (int c : cnt) ok = ok && (c == s.B);
+  }
+  if (!ok) return 0;
+  return wmax <= 8 ? 8 : (wmax <= 16 ? 16 : (wmax <= 32 ? 32 : (wmax <= 64 ? 64 : 128)));
+}
+
+struct Sizes {
+  size_t M, U, KWW, work, tbuf, diag, offd, gpart, cen, log, logc, nn, bk, wb, st, op1, op2, m0, u0, inv, fr;
+  size_t pkr, pr2, pgr, pgp, ppart;
+  size_t total() const {
+    return 2 * M + 2 * U + 3 * KWW + work + tbuf + 2 * diag + offd + gpart + cen + log + logc + nn + bk + wb + st +
+           op1 + op2 + m0 + u0 + inv + fr + pkr + 2 * pr2 + pgr + pgp + ppart;
+  }
+};
+
+// per-problem device arrays (bytes, 256-aligned) for tensor width wp (0: FP64 path)
+Sizes problem_sizes(const ProblemSpec& s, int wp, int* pc_tiles) {
+  const size_t W = s.W, K = s.K, B = s.B;
+  const size_t WW = W * W;
+  const size_t nt = (s.W + kTileW - 1) / kTileW;
+  Sizes z;
+  z.M = align_up(K * B * WW * 16);
+  z.U = align_up(K * WW * 16);
+  z.KWW = align_up(K * WW * 16);
+  z.work = s.W > 32 ? align_up(K * 6 * WW * 16) : 0;
+  z.tbuf = (s.W > 32 || wp) ? align_up(K * B * WW * 16) : 0;
+  z.m0 = wp ? align_up(K * B * WW * 16) : 0;
+  z.u0 = wp ? align_up(K * WW * 16) : 0;
+  z.inv = wp ? align_up(K * B * 4) : 0;
+  z.fr = wp ? align_up(K * B * 8) : 0;
+  z.diag = align_up(K * B * W * 8);
+  z.offd = align_up(K * B * 8);
+  z.gpart = align_up(K * nt * nt * 2 * 8);
+  z.cen = align_up(3 * 4 * W * 8);
+  z.log = align_up((size_t)(s.ctl.num_iter + 1) * kLogStride * 8);
+  z.logc = align_up((size_t)(s.ctl.num_iter + 1) * 4 * W * 8);
+  z.nn = align_up(K * B * 4);
+  z.bk = align_up(K * B * 3 * 8);
+  z.wb = align_up(B * 8);
+  z.st = align_up(sizeof(CtrlState));
+  const size_t nch = (K * B + 63) / 64;
+  z.op1 = align_up(nch * (4 * W + 2) * 8);
+  z.op2 = align_up(nch * 8);
+  z.pkr = z.pr2 = z.pgr = z.pgp = z.ppart = 0;
+  if (s.precond) {
+    const size_t NR = s.nrpts;
+    const size_t te = (WW + 63) / 64;
+    z.pkr = align_up(K * NR * 16);
+    z.pr2 = align_up(NR * 8);
+    z.pgr = align_up(NR * WW * 16);
+    z.pgp = align_up(K * WW * 16);
+    z.ppart = align_up(te * ((K + 15) / 16) * 8);
+    if (pc_tiles) *pc_tiles = std::max(*pc_tiles, (int)(te * ((std::max(K, NR) + 15) / 16)));
+  }
+  return z;
+}
+
+size_t header_bytes(int np, int n_k) {
+  return align_up(np * sizeof(Problem)) + 4 * align_up((np + 1) * sizeof(int)) + align_up(n_k * sizeof(int)) +
+         align_up(n_k * sizeof(double)) + align_up(sizeof(int));
+}
+
+}  // namespace
+
+size_t Engine::estimate_bytes(const std::vector<ProblemSpec>& specs) {
+  const int wp = choose_tensor_wp(specs);
+  size_t total = 0;
+  int nk = 0;
+  for (const auto& s : specs) {
+    total += problem_sizes(s, wp, nullptr).total();
+    nk += s.K;
+  }
+  return total + header_bytes((int)specs.size(), nk);
+}
+
 int Engine::alloc(std::string& err) {
   const int np = (int)specs_.size();
-  // tensor-core M update: every problem asks for it, W <= 128, and every k' has exactly
-  // B predecessors (k,b) (true on Monkhorst-Pack meshes)
-  tensor_wp_ = 0;
-  {
-    bool ok = np > 0;
-    int wmax = 0;
-    for (const auto& s : specs_) {
-      ok = ok && s.tensor && s.W <= 128;
-      wmax = std::max(wmax, s.W);
-      if (!ok) break;
-      std::vector<int> cnt(s.K, 0);
-      for (int v : s.nnlist) cnt[v]++;
-      for (int c : cnt) ok = ok && (c == s.B);
-    }
-    if (ok) tensor_wp_ = wmax <= 8 ? 8 : (wmax <= 16 ? 16 : (wmax <= 32 ? 32 : (wmax <= 64 ? 64 : 128)));
-  }
+  tensor_wp_ = choose_tensor_wp(specs_);
   if (!own_stream_) W90G_CHECK(cudaStreamCreateWithFlags(&own_stream_, cudaStreamNonBlocking));
-  // sizes
-  struct Sizes {
-    size_t M, U, KWW, work, tbuf, diag, offd, gpart, cen, log, logc, nn, bk, wb, st, op1, op2, m0, u0, inv, fr;
-    size_t pkr, pr2, pgr, pgp, ppart;
-  };
   std::vector<Sizes> sz(np);
   size_t total = 0;
   n_k_ = n_kb_ = n_grad_ = 0;
@@ -156,46 +231,9 @@ int Engine::alloc(std::string& err) {
   std::vector<int> offs_k(np + 1, 0), offs_kb(np + 1, 0), offs_grad(np + 1, 0), offs_chunk(np + 1, 0);
   for (int p = 0; p < np; ++p) {
     const auto& s = specs_[p];
-    const size_t W = s.W, K = s.K, B = s.B;
-    const size_t WW = W * W;
     const int nt = (s.W + kTileW - 1) / kTileW;
-    Sizes& z = sz[p];
-    z.M = align_up(K * B * WW * 16);
-    z.U = align_up(K * WW * 16);
-    z.KWW = align_up(K * WW * 16);
-    z.work = s.W > 32 ? align_up(K * 6 * WW * 16) : 0;
-    z.tbuf = (s.W > 32 || tensor_wp_) ? align_up(K * B * WW * 16) : 0;
-    z.m0 = tensor_wp_ ? align_up(K * B * WW * 16) : 0;
-    z.u0 = tensor_wp_ ? align_up(K * WW * 16) : 0;
-    z.inv = tensor_wp_ ? align_up(K * B * 4) : 0;
-    z.fr = tensor_wp_ ? align_up(K * B * 8) : 0;
-    z.diag = align_up(K * B * W * 8);
-    z.offd = align_up(K * B * 8);
-    z.gpart = align_up(K * nt * nt * 2 * 8);
-    z.cen = align_up(3 * 4 * W * 8);
-    z.log = align_up((size_t)(s.ctl.num_iter + 1) * kLogStride * 8);
-    z.logc = align_up((size_t)(s.ctl.num_iter + 1) * 4 * W * 8);
-    z.nn = align_up(K * B * 4);
-    z.bk = align_up(K * B * 3 * 8);
-    z.wb = align_up(B * 8);
-    z.st = align_up(sizeof(CtrlState));
-    const size_t nch = (K * B + 63) / 64;
-    z.op1 = align_up(nch * (4 * W + 2) * 8);
-    z.op2 = align_up(nch * 8);
-    z.pkr = z.pr2 = z.pgr = z.pgp = z.ppart = 0;
-    if (s.precond) {
-      const size_t NR = s.nrpts;
-      const size_t te = (WW + 63) / 64;
-      z.pkr = align_up(K * NR * 16);
-      z.pr2 = align_up(NR * 8);
-      z.pgr = align_up(NR * WW * 16);
-      z.pgp = align_up(K * WW * 16);
-      z.ppart = align_up(te * ((K + 15) / 16) * 8);
-      pc_tiles_ = std::max(pc_tiles_, (int)(te * ((std::max(K, NR) + 15) / 16)));
-    }
-    total += 2 * z.M + 2 * z.U + 3 * z.KWW + z.work + z.tbuf + 2 * z.diag + z.offd + z.gpart + z.cen +
-             z.log + z.logc + z.nn + z.bk + z.wb + z.st + z.op1 + z.op2 + z.m0 + z.u0 + z.inv + z.fr +
-             z.pkr + 2 * z.pr2 + z.pgr + z.pgp + z.ppart;
+    sz[p] = problem_sizes(s, tensor_wp_, &pc_tiles_);
+    total += sz[p].total();
     offs_k[p + 1] = offs_k[p] + s.K;
     offs_kb[p + 1] = offs_kb[p] + s.K * s.B;
     offs_grad[p + 1] = offs_grad[p] + s.K * nt * nt;
@@ -207,10 +245,9 @@ int Engine::alloc(std::string& err) {
   n_kb_ = offs_kb[np];
   n_grad_ = offs_grad[np];
   n_chunk_ = offs_chunk[np];
-  const size_t hdr = align_up(np * sizeof(Problem)) + 4 * align_up((np + 1) * sizeof(int)) +
-                     align_up(n_k_ * sizeof(int)) + align_up(n_k_ * sizeof(double)) + align_up(sizeof(int));
-  total += hdr;
-  W90G_CHECK(cudaMalloc(&arena_, total));
+  total += header_bytes(np, n_k_);
+  if (async_alloc_) W90G_CHECK(cudaMallocAsync(&arena_, total, stream()));
+  else W90G_CHECK(cudaMalloc(&arena_, total));
   arena_bytes_ = total;
   char* cur = (char*)arena_;
   auto take = [&](size_t n) {
@@ -269,15 +306,15 @@ int Engine::alloc(std::string& err) {
         const int k2 = s.nnlist[kb];
         h_inv[(size_t)k2 * s.B + fill[k2]++] = kb;
       }
-      W90G_CHECK(cudaMemcpy(inv, h_inv.data(), h_inv.size() * sizeof(int), cudaMemcpyHostToDevice));
+      W90G_CHECK(cudaMemcpyAsync(inv, h_inv.data(), h_inv.size() * sizeof(int), cudaMemcpyHostToDevice, stream()));
     }
     P.opart1 = (double*)take(z.op1);
     P.opart2 = (double*)take(z.op2);
     P.nchunk = (s.K * s.B + 63) / 64;
     P.ctl = s.ctl;
-    W90G_CHECK(cudaMemcpy(nn, s.nnlist.data(), s.nnlist.size() * sizeof(int), cudaMemcpyHostToDevice));
-    W90G_CHECK(cudaMemcpy(bk, s.bk.data(), s.bk.size() * sizeof(double), cudaMemcpyHostToDevice));
-    W90G_CHECK(cudaMemcpy(wb, s.wb.data(), s.wb.size() * sizeof(double), cudaMemcpyHostToDevice));
+    W90G_CHECK(cudaMemcpyAsync(nn, s.nnlist.data(), s.nnlist.size() * sizeof(int), cudaMemcpyHostToDevice, stream()));
+    W90G_CHECK(cudaMemcpyAsync(bk, s.bk.data(), s.bk.size() * sizeof(double), cudaMemcpyHostToDevice, stream()));
+    W90G_CHECK(cudaMemcpyAsync(wb, s.wb.data(), s.wb.size() * sizeof(double), cudaMemcpyHostToDevice, stream()));
     P.nnlist = nn;
     P.bk = bk;
     P.wb = wb;
@@ -287,9 +324,9 @@ int Engine::alloc(std::string& err) {
       double* kr = (double*)take(z.pkr);
       double* r2 = (double*)take(z.pr2);
       double* nd = (double*)take(z.pr2);
-      W90G_CHECK(cudaMemcpy(kr, s.pc_kr.data(), s.pc_kr.size() * 8, cudaMemcpyHostToDevice));
-      W90G_CHECK(cudaMemcpy(r2, s.pc_r2.data(), s.pc_r2.size() * 8, cudaMemcpyHostToDevice));
-      W90G_CHECK(cudaMemcpy(nd, s.pc_ndeg.data(), s.pc_ndeg.size() * 8, cudaMemcpyHostToDevice));
+      W90G_CHECK(cudaMemcpyAsync(kr, s.pc_kr.data(), s.pc_kr.size() * 8, cudaMemcpyHostToDevice, stream()));
+      W90G_CHECK(cudaMemcpyAsync(r2, s.pc_r2.data(), s.pc_r2.size() * 8, cudaMemcpyHostToDevice, stream()));
+      W90G_CHECK(cudaMemcpyAsync(nd, s.pc_ndeg.data(), s.pc_ndeg.size() * 8, cudaMemcpyHostToDevice, stream()));
       P.pc_kr = (const double2*)kr;
       P.pc_r2 = r2;
       P.pc_ndeg = nd;
@@ -298,11 +335,11 @@ int Engine::alloc(std::string& err) {
       P.pc_part = (double*)take(z.ppart);
     }
   }
-  W90G_CHECK(cudaMemcpy(dprobs_, hprobs_.data(), np * sizeof(Problem), cudaMemcpyHostToDevice));
-  W90G_CHECK(cudaMemcpy(d_offs_k_, offs_k.data(), (np + 1) * sizeof(int), cudaMemcpyHostToDevice));
-  W90G_CHECK(cudaMemcpy(d_offs_kb_, offs_kb.data(), (np + 1) * sizeof(int), cudaMemcpyHostToDevice));
-  W90G_CHECK(cudaMemcpy(d_offs_grad_, offs_grad.data(), (np + 1) * sizeof(int), cudaMemcpyHostToDevice));
-  W90G_CHECK(cudaMemcpy(d_offs_chunk_, offs_chunk.data(), (np + 1) * sizeof(int), cudaMemcpyHostToDevice));
+  W90G_CHECK(cudaMemcpyAsync(dprobs_, hprobs_.data(), np * sizeof(Problem), cudaMemcpyHostToDevice, stream()));
+  W90G_CHECK(cudaMemcpyAsync(d_offs_k_, offs_k.data(), (np + 1) * sizeof(int), cudaMemcpyHostToDevice, stream()));
+  W90G_CHECK(cudaMemcpyAsync(d_offs_kb_, offs_kb.data(), (np + 1) * sizeof(int), cudaMemcpyHostToDevice, stream()));
+  W90G_CHECK(cudaMemcpyAsync(d_offs_grad_, offs_grad.data(), (np + 1) * sizeof(int), cudaMemcpyHostToDevice, stream()));
+  W90G_CHECK(cudaMemcpyAsync(d_offs_chunk_, offs_chunk.data(), (np + 1) * sizeof(int), cudaMemcpyHostToDevice, stream()));
   // dynamic shared memory limits of the shared-memory kernels: a function attribute is
   // process wide, so every engine sets the same value, the maximum for W <= 32 (engines
   // of different widths may run concurrently in the batched form)
@@ -311,7 +348,10 @@ int Engine::alloc(std::string& err) {
   W90G_CHECK(cudaFuncSetAttribute(k_u_final, cudaFuncAttributeMaxDynamicSharedMemorySize, 3 * wmax * wmax * 16));
   W90G_CHECK(cudaFuncSetAttribute(k_m_update, cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * wmax * wmax * 16));
   W90G_CHECK(cudaFuncSetAttribute(k_lowdin, cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * wmax * wmax * 16));
+  tensor_exp_ = tensor_wp_ != 0;
+  for (const auto& s : specs_) tensor_exp_ = tensor_exp_ && s.tensor_exp;
   if (tensor_wp_) W90G_CHECK(oz_set_attributes(tensor_wp_));
+  if (tensor_exp_) W90G_CHECK(oz_exp_set_attributes(tensor_wp_));
   return 0;
 }
 
@@ -422,37 +462,45 @@ void Engine::launch_mupdate(cudaStream_t s, int which) {
   }
 }
 
+void Engine::launch_exp(cudaStream_t s, int which) {
+  const WorkMap wmk{d_offs_k_, nprob()};
+  if (tensor_exp_) {
+    oz_exp_launch(tensor_wp_, dprobs_, wmk, which, n_k_, s);
+  } else {
+    const int ws = std::max(maxW_small_, 1);
+    k_exp_u<<<n_k_, 256, (size_t)6 * ws * ws * 16, s>>>(dprobs_, wmk, which);
+  }
+}
+
 void Engine::launch_iteration(cudaStream_t s) {
   const int np = nprob();
   const int ws = std::max(maxW_small_, 1);
   const WorkMap wmk{d_offs_k_, np};
   const WorkMap wmkb{d_offs_kb_, np};
   const WorkMap wmg{d_offs_grad_, np};
-  const size_t sm_exp = (size_t)6 * ws * ws * 16;
-  const size_t sm_mu = (size_t)4 * ws * ws * 16;
   k_grad<<<n_grad_, 256, 0, s>>>(dprobs_, wmg);
   if (pc_tiles_) {
     k_precond<<<dim3(pc_tiles_, np), 256, 0, s>>>(dprobs_, 0);
     k_precond<<<dim3(pc_tiles_, np), 256, 0, s>>>(dprobs_, 1);
   }
   k_ctrl_search<<<np, 256, 0, s>>>(dprobs_);
-  k_exp_u<<<n_k_, 256, sm_exp, s>>>(dprobs_, wmk, 0);
+  launch_exp(s, 0);
   launch_mupdate(s, 0);
   launch_omega(s, 0);
   k_ctrl_step<<<(np + 127) / 128, 128, 0, s>>>(dprobs_, np);
-  k_exp_u<<<n_k_, 256, sm_exp, s>>>(dprobs_, wmk, 1);
+  launch_exp(s, 1);
   launch_mupdate(s, 1);
   launch_omega(s, 1);
   k_ctrl_end<<<np, 128, 0, s>>>(dprobs_);
 }
 
-int Engine::wannierise(std::string& err) {
+int Engine::begin(std::string& err) {
   cudaStream_t st = stream();
   launches_ = 0;
+  launched_iters_ = 0;
   const int np = nprob();
   if (init_states(err)) return 1;
   const WorkMap wmkb{d_offs_kb_, np};
-  const WorkMap wmk{d_offs_k_, np};
   if (int rc0 = prepare_tensor(st, err)) return rc0;
   // initial spread (src/wannierise.F90:452-470)
   k_mdiag<<<n_kb_, 128, 0, st>>>(dprobs_, wmkb);
@@ -460,10 +508,8 @@ int Engine::wannierise(std::string& err) {
   k_log_init<<<np, 128, 0, st>>>(dprobs_);
   W90G_CHECK(cudaGetLastError());
   launches_ += 5;
-  // capture one iteration into a graph (re-captured when the stream changes)
+  // capture one iteration into a graph (once per arena layout)
   if (!graph_exec_) {
-    if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
-    graph_exec_ = nullptr;
     cudaStream_t cap;
     W90G_CHECK(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
     cudaGraph_t g;
@@ -475,27 +521,51 @@ int Engine::wannierise(std::string& err) {
     cudaStreamDestroy(cap);
     graph_stream_ = st;
   }
+  return 0;
+}
+
+int Engine::advance(int n, int* d_flag, std::string& err) {
+  cudaStream_t st = stream();
+  n = std::min(n, max_iter_ - launched_iters_);
+  for (int i = 0; i < n; ++i) W90G_CHECK(cudaGraphLaunch(graph_exec_, st));
+  // grad, search, 2 x (exp, M update, 3 spread passes), step, end (+ 2 precond)
+  launches_ += (10LL + 2 * (tensor_wp_ ? 2 : 1) + (pc_tiles_ ? 2 : 0)) * std::max(n, 0);
+  launched_iters_ += std::max(n, 0);
+  if (d_flag) {
+    // every problem done (converged or out of iterations) -> *d_flag = 1
+    k_all_done<<<1, 256, 0, st>>>(dprobs_, nprob(), d_flag);
+    W90G_CHECK(cudaGetLastError());
+    launches_ += 1;
+  }
+  return 0;
+}
+
+int Engine::wannierise(std::string& err) {
+  cudaStream_t st = stream();
+  if (int rc0 = begin(err)) return rc0;
   int* d_alldone = (int*)((char*)d_unit_ + align_up(n_k_ * sizeof(double)));
   int any_window = 0;
   for (const auto& s : specs_) any_window |= (s.ctl.conv_window > 1);
-  int done_iters = 0;
   int chunk = 4;
   int hdone = 0;
-  while (done_iters < max_iter_) {
-    const int n = std::min(chunk, max_iter_ - done_iters);
-    for (int i = 0; i < n; ++i) W90G_CHECK(cudaGraphLaunch(graph_exec_, st));
-    // grad, search, 2 x (exp, M update, 3 spread passes), step, end (+ 2 precond)
-    launches_ += (10LL + 2 * (tensor_wp_ ? 2 : 1) + (pc_tiles_ ? 2 : 0)) * n;
-    done_iters += n;
-    if (any_window && done_iters < max_iter_) {
-      k_all_done<<<1, 256, 0, st>>>(dprobs_, np, d_alldone);
-      launches_ += 1;
+  while (launched_iters_ < max_iter_) {
+    const int n = std::min(chunk, max_iter_ - launched_iters_);
+    const bool poll = any_window && (launched_iters_ + n) < max_iter_;
+    if (int rc0 = advance(n, poll ? d_alldone : nullptr, err)) return rc0;
+    if (poll) {
       W90G_CHECK(cudaMemcpyAsync(&hdone, d_alldone, sizeof(int), cudaMemcpyDeviceToHost, st));
       W90G_CHECK(cudaStreamSynchronize(st));
       if (hdone) break;
       chunk = std::min(chunk * 2, 32);
     }
   }
+  return finish(err);
+}
+
+int Engine::finish(std::string& err) {
+  cudaStream_t st = stream();
+  const int np = nprob();
+  const WorkMap wmk{d_offs_k_, np};
   if (tensor_wp_) {
     const int ws = std::max(maxW_small_, 1);
     k_u_final<<<n_k_, 256, (size_t)3 * ws * ws * 16, st>>>(dprobs_, wmk);
@@ -560,8 +630,6 @@ int Engine::wannierise_profiled(int max_iters, double* ms, int* cnt, std::string
   const WorkMap wmk{d_offs_k_, np};
   const WorkMap wmkb{d_offs_kb_, np};
   const WorkMap wmg{d_offs_grad_, np};
-  const size_t sm_exp = (size_t)6 * ws * ws * 16;
-  const size_t sm_mu = (size_t)4 * ws * ws * 16;
   cudaEvent_t e0, e1;
   W90G_CHECK(cudaEventCreate(&e0));
   W90G_CHECK(cudaEventCreate(&e1));
@@ -593,13 +661,13 @@ int Engine::wannierise_profiled(int max_iters, double* ms, int* cnt, std::string
       rc |= timed(kPPrecond, [&] { k_precond<<<dim3(pc_tiles_, np), 256, 0, st>>>(dprobs_, 1); });
     }
     rc |= timed(kPCtrlSearch, [&] { k_ctrl_search<<<np, 256, 0, st>>>(dprobs_); });
-    rc |= timed(kPExpU, [&] { k_exp_u<<<n_k_, 256, sm_exp, st>>>(dprobs_, wmk, 0); });
+    rc |= timed(kPExpU, [&] { launch_exp(st, 0); });
     rc |= timed(kPMUpdate, [&] { launch_mupdate(st, 0); });
     rc |= timed(kPOmega, [&] { launch_omega(st, 0); });
     rc |= timed(kPCtrlStep, [&] { k_ctrl_step<<<(np + 127) / 128, 128, 0, st>>>(dprobs_, np); });
     W90G_CHECK(cudaMemcpy(&hs, hprobs_[0].st, sizeof(CtrlState), cudaMemcpyDeviceToHost));
     if (hs.do_second) {
-      rc |= timed(kPExpU, [&] { k_exp_u<<<n_k_, 256, sm_exp, st>>>(dprobs_, wmk, 1); });
+      rc |= timed(kPExpU, [&] { launch_exp(st, 1); });
       rc |= timed(kPMUpdate, [&] { launch_mupdate(st, 1); });
       rc |= timed(kPOmega, [&] { launch_omega(st, 1); });
     }

@@ -18,6 +18,7 @@ struct ProblemSpec {
   std::vector<double> wb;    // [b]
   Control ctl{};
   int tensor = 0;            // request the tensor-core M update (W <= 128)
+  int tensor_exp = 1;        // with tensor: exp(s D) and U dU on the tensor cores too
   // preconditioner (precond = T): Wigner-Seitz points R_r of the Born-von Karman
   // supercell, exp(-i 2 pi k.R) table [k][r] (re, im interleaved), |R|^2, degeneracies
   int precond = 0;
@@ -57,8 +58,22 @@ class Engine {
   int store(int p, void* M, void* U, cudaMemcpyKind kind, std::string& err);
   // Loewdin projection on every problem (U holds A on entry).
   int project(std::string& err);
-  // wann_main on every problem; results via result().
+  // wann_main on every problem; results via result().  Equivalent to begin(), advance()
+  // until every problem is done, finish().
   int wannierise(std::string& err);
+  // Stepwise form (used by the serving loop): begin() computes the initial spread and
+  // captures the iteration graph; advance(n, d_flag) enqueues n more iterations and, if
+  // d_flag is given, a kernel that sets *d_flag = 1 once every problem is done;
+  // finish() runs the final rotation/unitarity check and downloads the results.
+  // All work is enqueued on stream(); nothing here synchronises except finish().
+  int begin(std::string& err);
+  int advance(int n, int* d_flag, std::string& err);
+  int finish(std::string& err);
+  int launched_iters() const { return launched_iters_; }
+  int max_iter() const { return max_iter_; }
+  size_t arena_bytes() const { return arena_bytes_; }
+  // device bytes setup() would allocate for these problems (HBM admission)
+  static size_t estimate_bytes(const std::vector<ProblemSpec>& specs);
   // wann_main with each kernel launched individually and timed with CUDA events on the
   // launching stream; ms[i] / cnt[i] accumulate per kernel kind (kProfNames order);
   // only launches that did work are counted (skipped second passes are excluded).
@@ -67,6 +82,9 @@ class Engine {
   int nprob() const { return (int)specs_.size(); }
 
   void set_stream(cudaStream_t s) { user_stream_ = s; }
+  // allocate / free the arena stream-ordered on stream() (the stream must outlive the
+  // engine); avoids the device-wide synchronisation of cudaFree in the serving loop
+  void set_async_alloc(bool on) { async_alloc_ = on; }
   cudaStream_t stream() const { return user_stream_ ? user_stream_ : own_stream_; }
   long long launches() const { return launches_; }
   double last_exp_products() const { return last_exp_products_; }
@@ -77,6 +95,7 @@ class Engine {
   void launch_iteration(cudaStream_t s);
   void launch_omega(cudaStream_t s, int slot);
   void launch_mupdate(cudaStream_t s, int which);
+  void launch_exp(cudaStream_t s, int which);
   int prepare_tensor(cudaStream_t st, std::string& err);
   int init_states(std::string& err);
 
@@ -95,7 +114,8 @@ class Engine {
   int n_k_ = 0, n_kb_ = 0, n_grad_ = 0, n_chunk_ = 0;
   int pc_tiles_ = 0;     // > 0: some problem is preconditioned; CTAs per problem of k_precond
   int maxW_small_ = 0;   // largest W <= 32 in the batch (shared-memory kernels)
-  int tensor_wp_ = 0;    // > 0: tensor M update with padded width 8/16/32 for the whole batch
+  int tensor_wp_ = 0;    // > 0: tensor M update with padded width 8..128 for the whole batch
+  bool tensor_exp_ = false;  // exp(s D) on the tensor cores (k_oz_exp)
   int max_iter_ = 0;
   cudaStream_t own_stream_ = nullptr;
   cudaStream_t user_stream_ = nullptr;
@@ -103,6 +123,8 @@ class Engine {
   cudaStream_t graph_stream_ = nullptr;
   std::string layout_key_;
   long long launches_ = 0;
+  int launched_iters_ = 0;
+  bool async_alloc_ = false;
   double last_exp_products_ = 0.0;
 };
 

@@ -1,0 +1,472 @@
+// Tensor-core rotation step: dU(k) = exp(s D(k)) and U(k) <- U(k) dU(k)
+// (internal_new_u_and_m, src/wannierise.F90:1655-1733) with every W x W complex
+// product on the tcgen05 tensor cores through exact BF16 slicing (see k_tensor.cu).
+//
+// The matrix function is the FP64 path's (k_exp_u in k_fp64.cu): scaling and squaring
+// of a Taylor polynomial evaluated by Paterson-Stockmeyer, degree and squarings chosen
+// per matrix from its 1-norm.  Scalar work (norms, the polynomial's linear combinations,
+// the Hermitian symmetrisation of the even powers) stays in FP64; only the products move
+// to the tensor pipe.  The exp chain (powers, Horner steps, up to ~10 squarings that
+// double any error) needs more than the M update's 7 digits: every operand is split
+// into 8 signed 7-bit digits (56 bits) and the 36 digit pairs with t+u <= 7 are kept,
+// so a product is accurate to ~2^-56 of (row scale x column scale), below FP64 GEMM
+// roundoff; the 8 diagonals are recombined exactly in 128-bit integers.
+//
+// One CTA (256 threads) per (problem, k).  A product C = A B puts the rows of A on the
+// 128 TMEM lanes; only the first WP rows are real.  To keep shared memory small, the 8
+// digit slices of A are stored WP-row blocks apart in one region: the MMA reading slice
+// t sees slices t+1.. in rows >= WP, which only feed accumulator rows nobody reads.
+#include "oz.cuh"
+
+namespace w90g {
+
+namespace {
+
+constexpr int kS8 = 8;   // digits per operand in this kernel
+
+template <int WP>
+struct ExpSmem {
+  using L = TileSmem<WP>;
+  static constexpr int CW = L::CW, KC = L::KC, NC = L::NC, NCH = L::NCH;
+  static constexpr int A_ROWS = (kS8 - 1) * WP + kTileRows;      // overlapped slices
+  static constexpr int A_SLICE = WP * KC * 2;                     // bytes between slices
+  static constexpr int A_BYTES = A_ROWS * KC * 2;
+  static constexpr int B_BYTES = NC * KC * 2;                     // per slice
+  static constexpr int TMEM_COLS = (kS8 * NC <= 128) ? 128 : ((kS8 * NC <= 256) ? 256 : 512);
+  // W <= 32: the accumulators are staged through shared memory (aliasing the digit
+  // slices, free once the MMAs are done) so that all warps recombine, not just the two
+  // warps that can read the TMEM lanes of rows 0..31
+  static constexpr bool STAGED = WP <= 32;
+  static constexpr int STAGE_LD = NC + 1;                         // u32 row stride
+  static constexpr size_t STAGE_BYTES = STAGED ? (size_t)kS8 * WP * STAGE_LD * 4 : 0;
+  static constexpr size_t DIGIT_BYTES = (size_t)A_BYTES + (size_t)kS8 * B_BYTES;
+  static constexpr size_t REGION = DIGIT_BYTES > STAGE_BYTES ? DIGIT_BYTES : STAGE_BYTES;
+  static constexpr bool MATS_IN_SMEM = WP <= 32;
+  static constexpr size_t MAT_BYTES = (size_t)WP * WP * 16;
+  static constexpr size_t BYTES = REGION + (MATS_IN_SMEM ? 6 * MAT_BYTES : 0) + 1024;
+};
+
+__device__ __forceinline__ double cta_max(double v, double* red) {
+  red[threadIdx.x] = v;
+  __syncthreads();
+  for (int s = blockDim.x >> 1; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
+    __syncthreads();
+  }
+  const double r = red[0];
+  __syncthreads();
+  return r;
+}
+
+// per-CTA state of the tensor product
+struct OzCtx {
+  unsigned char* sA;
+  unsigned char* sB;
+  uint32_t tmem;
+  uint32_t mbar;
+  uint32_t phase;
+  int* rowexp;   // [WP]
+  int* colexp;   // [WP]
+  int* bad;
+};
+
+// C = A B for W x W complex column-major matrices (generic pointers; C must not alias
+// A or B).  All threads call; returns false (uniformly) if an MMA wait timed out.
+template <int WP>
+__device__ bool oz_cmm(OzCtx& cx, double2* C, const double2* A, const double2* B, int W) {
+  using E = ExpSmem<WP>;
+  constexpr int CW = E::CW, KC = E::KC, NC = E::NC, NCH = E::NCH;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  // ---- power-of-two scales: rows of A, columns of B (over re and im parts)
+  for (int idx = tid; idx < 2 * WP; idx += blockDim.x) {
+    const int r = idx % WP;
+    unsigned long long mx = 0ull;
+    if (r < W) {
+      if (idx < WP) {
+        for (int l = 0; l < W; ++l) {
+          const double2 a = A[(size_t)l * W + r];
+          mx = max(mx, max(abs_bits(a.x), abs_bits(a.y)));
+        }
+      } else {
+        for (int l = 0; l < W; ++l) {
+          const double2 b = B[(size_t)r * W + l];
+          mx = max(mx, max(abs_bits(b.x), abs_bits(b.y)));
+        }
+      }
+    }
+    (idx < WP ? cx.rowexp : cx.colexp)[r] = exp_above_bits(mx);
+  }
+  __syncthreads();
+  const uint32_t idesc = idesc_bf16(NC);
+  bool ok = true;
+  for (int nc = 0; nc < NCH && ok; ++nc) {
+    for (int kc = 0; kc < NCH && ok; ++kc) {
+      // ---- A chunk: rows r < WP, complex K index l < CW -> real columns l, l + CW
+      for (int e = tid; e < WP * CW; e += blockDim.x) {
+        const int r = e % WP, l = e / WP;
+        const int m = kc * CW + l;
+        double2 a = make_double2(0.0, 0.0);
+        if (r < W && m < W) a = A[(size_t)m * W + r];
+        int xr[kS8], xi[kS8];
+        const int ex = cx.rowexp[r];
+        digits8(scaled_int56(a.x, ex), xr);
+        digits8(scaled_int56(a.y, ex), xi);
+        const uint32_t o_re = kmaj_off(r, l, KC), o_im = kmaj_off(r, l + CW, KC);
+#pragma unroll
+        for (int t = 0; t < kS8; ++t) {
+          *(uint16_t*)(cx.sA + (size_t)t * E::A_SLICE + o_re) = int_to_bf16(xr[t]);
+          *(uint16_t*)(cx.sA + (size_t)t * E::A_SLICE + o_im) = int_to_bf16(xi[t]);
+        }
+      }
+      // ---- B chunk, embedded [[B_r, B_i], [-B_i, B_r]] stored as B^T (K-major):
+      // row = real N index (c | c + CW), column = real K index (l | l + CW)
+      for (int e = tid; e < CW * CW; e += blockDim.x) {
+        const int l = e % CW, c = e / CW;
+        const int mm = kc * CW + l, cc = nc * CW + c;
+        double2 b = make_double2(0.0, 0.0);
+        if (mm < W && cc < W) b = B[(size_t)cc * W + mm];
+        int xr[kS8], xi[kS8];
+        const int ex = cx.colexp[cc < WP ? cc : 0];
+        digits8(scaled_int56(b.x, ex), xr);
+        digits8(scaled_int56(b.y, ex), xi);
+        const uint32_t o00 = kmaj_off(c, l, KC), o01 = kmaj_off(c + CW, l, KC);
+        const uint32_t o10 = kmaj_off(c, l + CW, KC), o11 = kmaj_off(c + CW, l + CW, KC);
+#pragma unroll
+        for (int t = 0; t < kS8; ++t) {
+          unsigned char* sb = cx.sB + (size_t)t * E::B_BYTES;
+          *(uint16_t*)(sb + o00) = int_to_bf16(xr[t]);    // (K re, N re) =  B_r
+          *(uint16_t*)(sb + o01) = int_to_bf16(xi[t]);    // (K re, N im) =  B_i
+          *(uint16_t*)(sb + o10) = int_to_bf16(-xi[t]);   // (K im, N re) = -B_i
+          *(uint16_t*)(sb + o11) = int_to_bf16(xr[t]);    // (K im, N im) =  B_r
+        }
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncthreads();
+      if (tid == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        for (int t = 0; t < kS8; ++t) {
+          for (int u = 0; u + t <= kS8 - 1; ++u) {
+            const uint32_t dtm = cx.tmem + (uint32_t)((t + u) * NC);
+            const uint32_t a0 = smem_u32(cx.sA + (size_t)t * E::A_SLICE);
+            const uint32_t b0 = smem_u32(cx.sB + (size_t)u * E::B_BYTES);
+            const bool first_pair = (kc == 0) && (t == 0);
+#pragma unroll
+            for (int ks = 0; ks < KC / 16; ++ks) {
+              const uint64_t ad = smem_desc(a0 + ks * 256, 128, (KC / 8) * 128);
+              const uint64_t bd = smem_desc(b0 + ks * 256, 128, (KC / 8) * 128);
+              const uint32_t acc = (first_pair && ks == 0) ? 0u : 1u;
+              asm volatile(
+                  "{\n\t.reg .pred p;\n\t"
+                  "setp.ne.b32 p, %4, 0;\n\t"
+                  "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+                  :: "r"(dtm), "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+                  : "memory");
+            }
+          }
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                     :: "r"(cx.mbar) : "memory");
+      }
+      const bool ok_mine = mbar_wait(cx.mbar, cx.phase);
+      cx.phase ^= 1u;
+      if (!ok_mine) *cx.bad = 1;
+      __syncthreads();
+      ok = (*cx.bad == 0);
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    }
+    if (!ok) break;
+    // C(r, c) = (sum_d D_d 2^(7(7-d))) 2^(rowexp + colexp - 63), exact in 128 bits
+    auto recombine = [&](const uint32_t* dr, const uint32_t* di, int stride, int r, int c) {
+      __int128 sr = float_to_int_exact24(__uint_as_float(dr[0]));
+      __int128 si = float_to_int_exact24(__uint_as_float(di[0]));
+#pragma unroll
+      for (int d = 1; d < kS8; ++d) {
+        sr = (sr << 7) + float_to_int_exact24(__uint_as_float(dr[d * stride]));
+        si = (si << 7) + float_to_int_exact24(__uint_as_float(di[d * stride]));
+      }
+      const int sc = cx.rowexp[r] + cx.colexp[c] - 63;
+      C[(size_t)c * W + r] = make_double2(int128_scaled_to_double(sr, sc), int128_scaled_to_double(si, sc));
+    };
+    const int wq = warp & 3, half = warp >> 2;
+    const uint32_t lane_base = (uint32_t)(wq * 32) << 16;
+    const int jbeg = half * (CW / 2), jend = jbeg + CW / 2;
+    if (E::STAGED) {
+      // ---- TMEM -> shared (warps 0 and 4 hold rows 0..31), then all warps recombine
+      uint32_t* stage = (uint32_t*)cx.sA;
+      if (wq == 0) {
+#pragma unroll 1
+        for (int j0 = jbeg; j0 < jend; j0 += 4) {
+#pragma unroll
+          for (int d = 0; d < kS8; ++d) {
+            uint32_t q[4], s4[4];
+            const uint32_t ta = cx.tmem + lane_base + (uint32_t)(d * NC + j0);
+            const uint32_t tb = cx.tmem + lane_base + (uint32_t)(d * NC + CW + j0);
+            asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+                         : "=r"(q[0]), "=r"(q[1]), "=r"(q[2]), "=r"(q[3]) : "r"(ta));
+            asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+                         : "=r"(s4[0]), "=r"(s4[1]), "=r"(s4[2]), "=r"(s4[3]) : "r"(tb));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            if (lane < WP) {
+              uint32_t* row = stage + ((size_t)d * WP + lane) * E::STAGE_LD;
+#pragma unroll
+              for (int j = 0; j < 4; ++j) {
+                row[j0 + j] = q[j];
+                row[CW + j0 + j] = s4[j];
+              }
+            }
+          }
+        }
+      }
+      __syncthreads();
+      for (int e = tid; e < W * CW; e += blockDim.x) {
+        const int r = e % W, j = e / W;
+        const int c = nc * CW + j;
+        if (c >= W) continue;
+        const uint32_t* rowp = stage + (size_t)r * E::STAGE_LD;
+        recombine(rowp + j, rowp + CW + j, WP * E::STAGE_LD, r, c);
+      }
+    } else {
+      // ---- direct: TMEM lane r = row r; warps w and w+4 split the chunk's columns
+      const int r = wq * 32 + lane;
+      if (wq * 32 < W) {   // warp-uniform
+#pragma unroll 1
+        for (int j0 = jbeg; j0 < jend; j0 += 4) {
+          uint32_t q[kS8][4], s4[kS8][4];
+#pragma unroll
+          for (int d = 0; d < kS8; ++d) {
+            const uint32_t ta = cx.tmem + lane_base + (uint32_t)(d * NC + j0);
+            const uint32_t tb = cx.tmem + lane_base + (uint32_t)(d * NC + CW + j0);
+            asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+                         : "=r"(q[d][0]), "=r"(q[d][1]), "=r"(q[d][2]), "=r"(q[d][3])
+                         : "r"(ta));
+            asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+                         : "=r"(s4[d][0]), "=r"(s4[d][1]), "=r"(s4[d][2]), "=r"(s4[d][3])
+                         : "r"(tb));
+          }
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+          if (r < W) {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+              const int c = nc * CW + j0 + j;
+              if (c < W) recombine(&q[0][j], &s4[0][j], 4, r, c);
+            }
+          }
+        }
+      }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+  }
+  __syncthreads();
+  return ok;
+}
+
+// make C exactly Hermitian (sign +1) or anti-Hermitian (sign -1) from its upper triangle,
+// as the FP64 path's structured products produce it
+__device__ void mirror(double2* C, int W, double sign) {
+  for (int e = threadIdx.x; e < W * W; e += blockDim.x) {
+    const int i = e % W, j = e / W;
+    if (i > j) {
+      const double2 u = C[(size_t)i * W + j];
+      C[e] = cmk(sign * u.x, -sign * u.y);
+    } else if (i == j) {
+      const double2 d = C[e];
+      C[e] = (sign > 0) ? cmk(d.x, 0.0) : cmk(0.0, d.y);
+    }
+  }
+  __syncthreads();
+}
+
+__device__ const double kOzInvFact[17] = {
+    1.0, 1.0, 0.5, 1.6666666666666666e-01, 4.1666666666666664e-02, 8.3333333333333332e-03,
+    1.3888888888888889e-03, 1.9841269841269841e-04, 2.4801587301587302e-05,
+    2.7557319223985893e-06, 2.7557319223985888e-07, 2.5052108385441720e-08,
+    2.0876756987868100e-09, 1.6059043836821613e-10, 1.1470745597729725e-11,
+    7.6471637318198164e-13, 4.7794773323873853e-14};
+
+}  // namespace
+
+// which = 0: trial step (also forms D = coefG (G or Gp) + coefD D_prev); 1: optimal step
+template <int WP>
+__global__ void __launch_bounds__(256, 1) k_oz_exp(const Problem* __restrict__ probs, WorkMap wm, int which) {
+  using E = ExpSmem<WP>;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  __shared__ __align__(8) uint64_t mbar;
+  __shared__ uint32_t tmem_slot;
+  __shared__ int s_rowexp[WP], s_colexp[WP];
+  __shared__ int s_bad;
+  __shared__ double red[256];
+
+  int k;
+  const int p = locate(wm, blockIdx.x, k);
+  const Problem& P = probs[p];
+  CtrlState* st = P.st;
+  if (st->done) return;
+  if (which == 1 && !st->do_second) return;
+  const int W = P.W, WW = W * W;
+  const int tid = threadIdx.x, warp = tid >> 5;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                 :: "r"(smem_u32(&tmem_slot)), "r"((uint32_t)E::TMEM_COLS) : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&mbar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    s_bad = 0;
+  }
+  // FP64 matrices: shared memory for WP <= 32, else the per-k workspace (6 W^2)
+  double2* mats = E::MATS_IN_SMEM ? (double2*)(base + E::REGION)
+                                  : (P.work + (size_t)k * 6 * WW);
+  double2 *X = mats, *Y2 = mats + WW, *Y3 = mats + 2 * WW, *Y4 = mats + 3 * WW, *R = mats + 4 * WW,
+          *T = mats + 5 * WW;
+  double2* Dk = P.D + (size_t)k * WW;
+  const double s = (which == 0) ? st->s_trial : st->s_second;
+  if (which == 0) {
+    const double cg = st->coefG, cd = st->coefD;
+    const double2* Gk = (st->use_gp ? P.pc_gp : P.G) + (size_t)k * WW;
+    for (int e = tid; e < WW; e += blockDim.x) {
+      const double2 d = cadd(cscale(Gk[e], cg), cscale(Dk[e], cd));
+      Dk[e] = d;
+      X[e] = cscale(d, s);
+    }
+  } else {
+    for (int e = tid; e < WW; e += blockDim.x) X[e] = cscale(Dk[e], s);
+  }
+  __syncthreads();
+  OzCtx cx{base, base + E::A_BYTES, tmem_slot, smem_u32(&mbar), 0u, s_rowexp, s_colexp, &s_bad};
+
+  // ---- degree / squarings from the 1-norm (the FP64 path's table; costs in products:
+  // powers X^2, X^3 (, X^4) plus the Horner steps)
+  double colmax = 0.0;
+  for (int j = tid; j < W; j += blockDim.x) {
+    double a = 0.0;
+    for (int i = 0; i < W; ++i) a += sqrt(cabs2(X[(size_t)j * W + i]));
+    colmax = fmax(colmax, a);
+  }
+  const double nrm = cta_max(colmax, red);
+  const int cand_m[5] = {4, 6, 8, 12, 16};
+  const int cand_p[5] = {4, 3, 4, 4, 4};
+  const double cand_theta[5] = {1.6e-3, 1.68e-2, 6.6e-2, 0.32, 0.78};
+  const double cand_cost[5] = {3.0, 3.0, 4.0, 5.0, 6.0};
+  int m = 16, pw = 4, js = 0;
+  double best = 1e300;
+  for (int c = 0; c < 5; ++c) {
+    int j = 0;
+    double v = nrm;
+    while (v > cand_theta[c] && j < 60) {
+      v *= 0.5;
+      ++j;
+    }
+    const double cost = cand_cost[c] + j;
+    if (cost < best) {
+      best = cost;
+      m = cand_m[c];
+      pw = cand_p[c];
+      js = j;
+    }
+  }
+  const double sc = ldexp(1.0, -js);
+  for (int e = tid; e < WW; e += blockDim.x) X[e] = cscale(X[e], sc);
+  __syncthreads();
+  bool ok = oz_cmm<WP>(cx, Y2, X, X, W);
+  if (ok) mirror(Y2, W, 1.0);
+  if (ok) ok = oz_cmm<WP>(cx, Y3, Y2, X, W);
+  if (ok) mirror(Y3, W, -1.0);
+  if (ok && pw >= 4) {
+    ok = oz_cmm<WP>(cx, Y4, Y2, Y2, W);
+    if (ok) mirror(Y4, W, 1.0);
+  }
+  const double2* Yp = (pw == 4) ? Y4 : Y3;
+  const int nblk = (m + pw) / pw;
+  auto blk = [&](int q, int e) -> double2 {
+    const int i = e % W, j = e / W;
+    double2 v = cmk(0.0, 0.0);
+    for (int r = 0; r < pw; ++r) {
+      const int deg = pw * q + r;
+      if (deg > m) break;
+      const double c = kOzInvFact[deg];
+      if (r == 0) {
+        if (i == j) v.x += c;
+      } else {
+        const double2 y = (r == 1) ? X[e] : ((r == 2) ? Y2[e] : Y3[e]);
+        v = cadd(v, cscale(y, c));
+      }
+    }
+    return v;
+  };
+  int q = nblk - 1;
+  if (pw * q == m) {
+    const double cm = kOzInvFact[m];
+    for (int e = tid; e < WW; e += blockDim.x) R[e] = cadd(cscale(Yp[e], cm), blk(q - 1, e));
+    q -= 1;
+  } else {
+    for (int e = tid; e < WW; e += blockDim.x) R[e] = blk(q, e);
+  }
+  __syncthreads();
+  for (q = q - 1; q >= 0 && ok; --q) {
+    ok = oz_cmm<WP>(cx, T, Yp, R, W);
+    for (int e = tid; e < WW; e += blockDim.x) R[e] = cadd(T[e], blk(q, e));
+    __syncthreads();
+  }
+  double2* a = R;
+  double2* b = T;
+  for (int sq = 0; sq < js && ok; ++sq) {
+    ok = oz_cmm<WP>(cx, b, a, a, W);
+    double2* tmp = a;
+    a = b;
+    b = tmp;
+  }
+  // dU = exp(s D);  U[cur^1] = U[cur] dU
+  double2* dUk = P.dU + (size_t)k * WW;
+  for (int e = tid; e < WW; e += blockDim.x) dUk[e] = a[e];
+  __syncthreads();
+  const int cur = st->cur;
+  if (ok) ok = oz_cmm<WP>(cx, P.U[cur ^ 1] + (size_t)k * WW, P.U[cur] + (size_t)k * WW, a, W);
+  if (tid == 0) atomicAdd(&st->exp_products, best + 1.0);
+  if (!ok && tid == 0) {
+    st->error = 2;
+    st->done = 1;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;"
+                 :: "r"(cx.tmem), "r"((uint32_t)E::TMEM_COLS) : "memory");
+  }
+}
+
+template <int WP>
+static cudaError_t oz_exp_launch_wp(const Problem* probs, WorkMap wm, int which, int grid, cudaStream_t s) {
+  k_oz_exp<WP><<<grid, 256, ExpSmem<WP>::BYTES, s>>>(probs, wm, which);
+  return cudaGetLastError();
+}
+
+cudaError_t oz_exp_launch(int wp, const Problem* probs, WorkMap wm, int which, int grid, cudaStream_t s) {
+  switch (wp) {
+    case 8: return oz_exp_launch_wp<8>(probs, wm, which, grid, s);
+    case 16: return oz_exp_launch_wp<16>(probs, wm, which, grid, s);
+    case 32: return oz_exp_launch_wp<32>(probs, wm, which, grid, s);
+    case 64: return oz_exp_launch_wp<64>(probs, wm, which, grid, s);
+    default: return oz_exp_launch_wp<128>(probs, wm, which, grid, s);
+  }
+}
+
+template <int WP>
+static cudaError_t oz_exp_attr_wp() {
+  return cudaFuncSetAttribute(k_oz_exp<WP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)ExpSmem<WP>::BYTES);
+}
+
+cudaError_t oz_exp_set_attributes(int wp) {
+  switch (wp) {
+    case 8: return oz_exp_attr_wp<8>();
+    case 16: return oz_exp_attr_wp<16>();
+    case 32: return oz_exp_attr_wp<32>();
+    case 64: return oz_exp_attr_wp<64>();
+    default: return oz_exp_attr_wp<128>();
+  }
+}
+
+}  // namespace w90g

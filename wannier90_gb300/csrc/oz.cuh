@@ -1,0 +1,199 @@
+// Exact BF16 slicing helpers shared by the tensor-core kernels (M update, exp):
+// power-of-two scales, signed 7-bit digits, tcgen05 descriptors, exact int64
+// recombination.  See k_tensor.cu for the scheme.
+#pragma once
+#include <cuda_bf16.h>
+
+#include "w90g.cuh"
+
+namespace w90g {
+namespace {
+
+constexpr int kS = 7;            // digits per operand
+constexpr int kDiag = kS;        // diagonals d = 2 .. S+1
+constexpr int kTileRows = 128;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// shared-memory matrix descriptor: canonical K-major layout, no swizzle
+//   start address, LBO = byte stride between core matrices along K,
+//   SBO = byte stride between 8-row groups, version 1 (bit 46), layout 0
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr >> 4) & 0x3FFF);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+  d |= (uint64_t)1 << 46;
+  return d;
+}
+
+// instruction descriptor, kind::f16: D = F32, A = B = BF16, both K-major, N, M = 128
+__host__ __device__ constexpr uint32_t idesc_bf16(int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(kTileRows >> 4) << 24);
+}
+
+// element (row, k) of a K-major tile with K_real columns, in bytes
+__device__ __forceinline__ uint32_t kmaj_off(int row, int k, int kreal) {
+  return (uint32_t)((row >> 3) * (kreal >> 3) * 128 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
+}
+
+// exact BF16 bits of a small integer (|x| < 2^22): 1.5*2^23 magic, top 16 bits
+__device__ __forceinline__ uint16_t int_to_bf16(int x) {
+  const float f = __int_as_float(0x4B400000 + x) - 12582912.0f;
+  return (uint16_t)(__float_as_uint(f) >> 16);
+}
+
+// exact integer value of an integer-valued float with |f| < 2^22
+__device__ __forceinline__ int float_to_int_exact(float f) {
+  return __float_as_int(f + 12582912.0f) - 0x4B400000;
+}
+
+// |v| as an ordered integer (non-negative doubles compare like their bit patterns)
+__device__ __forceinline__ unsigned long long abs_bits(double v) {
+  return (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
+}
+
+// exponent e with |v| < 2^e from the bits of |v| (0 for v == 0); integer ops only
+__device__ __forceinline__ int exp_above_bits(unsigned long long ab) {
+  return ab ? (int)(ab >> 52) - 1022 : 0;
+}
+
+// N = round(v * 2^(49 - e)) as a signed integer (|N| <= 2^49), integer ops only
+__device__ __forceinline__ long long scaled_int(double v, int e) {
+  const long long bits = __double_as_longlong(v);
+  const int be = (int)((bits >> 52) & 0x7FF);
+  if (be == 0) return 0;   // zero / subnormal
+  const long long mant = (bits & 0x000FFFFFFFFFFFFFLL) | 0x0010000000000000LL;
+  // v = mant * 2^(be - 1075);  v * 2^(49-e) = mant * 2^(be - 1026 - e)
+  const int sh = 1026 + e - be;    // right shift >= 3 since |v| < 2^e
+  long long n;
+  if (sh >= 62) n = 0;
+  else n = (mant + (1LL << (sh - 1))) >> sh;
+  return (bits < 0) ? -n : n;
+}
+
+// signed 7-bit digits of N (|N| <= 2^49), extracted from the bottom:
+// x_7..x_2 in [-64, 63], x_1 the remaining top part (|x_1| <= 128); N = sum_t x_t 2^(7(7-t))
+__device__ __forceinline__ void digits7(long long n, int x[kS]) {
+#pragma unroll
+  for (int t = kS - 1; t > 0; --t) {
+    const int lo = (int)n & 127;
+    const int d = lo - ((lo & 64) << 1);     // centred in [-64, 63]
+    x[t] = d;
+    n = (n - d) >> 7;
+  }
+  x[0] = (int)n;
+}
+
+// 8-digit form (56 bits, used by the exp kernel): N = round(v * 2^(56 - e)), |N| <= 2^56
+__device__ __forceinline__ long long scaled_int56(double v, int e) {
+  const long long bits = __double_as_longlong(v);
+  const int be = (int)((bits >> 52) & 0x7FF);
+  if (be == 0) return 0;
+  const long long mant = (bits & 0x000FFFFFFFFFFFFFLL) | 0x0010000000000000LL;
+  // v * 2^(56-e) = mant * 2^(be - 1019 - e); the right shift is >= -3 since |v| < 2^e
+  const int sh = 1019 + e - be;
+  long long n;
+  if (sh >= 62) n = 0;
+  else if (sh > 0) n = (mant + (1LL << (sh - 1))) >> sh;
+  else n = mant << (-sh);
+  return (bits < 0) ? -n : n;
+}
+
+// 8 signed 7-bit digits of N (|N| <= 2^56): x_8..x_2 in [-64, 63], |x_1| <= 128,
+// N = sum_t x_t 2^(7(8-t))
+__device__ __forceinline__ void digits8(long long n, int x[8]) {
+#pragma unroll
+  for (int t = 7; t > 0; --t) {
+    const int lo = (int)n & 127;
+    const int d = lo - ((lo & 64) << 1);
+    x[t] = d;
+    n = (n - d) >> 7;
+  }
+  x[0] = (int)n;
+}
+
+// exact integer value of an integer-valued float with |f| < 2^24
+__device__ __forceinline__ int float_to_int_exact24(float f) {
+  return (fabsf(f) < 4194304.0f) ? float_to_int_exact(f) : __float2int_rn(f);
+}
+
+// double of S * 2^sc for a 128-bit S, rounded to nearest even, integer ops only
+__device__ __forceinline__ double int128_scaled_to_double(__int128 S, int sc) {
+  if (S == 0) return 0.0;
+  const unsigned long long sign = (S < 0) ? 0x8000000000000000ull : 0ull;
+  unsigned __int128 a = (S < 0) ? (unsigned __int128)(-S) : (unsigned __int128)S;
+  const unsigned long long hi = (unsigned long long)(a >> 64), lo = (unsigned long long)a;
+  const int lz = hi ? __clzll(hi) : 64 + __clzll(lo);
+  a <<= lz;                                          // leading 1 at bit 127
+  const unsigned long long top = (unsigned long long)(a >> 64);
+  const bool sticky = (unsigned long long)a != 0ull;
+  unsigned long long m = top >> 11;                  // 53 bits
+  const unsigned long long rem = top & 0x7FFull;
+  if (rem > 0x400ull || (rem == 0x400ull && (sticky || (m & 1ull)))) m += 1ull;
+  int ex = 127 - lz + sc;
+  if (m >> 53) {
+    m >>= 1;
+    ex += 1;
+  }
+  const unsigned long long bits = sign | ((unsigned long long)(ex + 1023) << 52) | (m & 0x000FFFFFFFFFFFFFull);
+  return __longlong_as_double((long long)bits);
+}
+
+// exact double of S * 2^sc (|S| < 2^63) with integer ops only (round to nearest even)
+__device__ __forceinline__ double int64_scaled_to_double(long long S, int sc) {
+  if (S == 0) return 0.0;
+  const unsigned long long sign = (S < 0) ? 0x8000000000000000ull : 0ull;
+  unsigned long long a = (S < 0) ? (unsigned long long)(-S) : (unsigned long long)S;
+  const int lz = __clzll(a);
+  a <<= lz;                                   // leading 1 at bit 63
+  // keep 53 bits: round to nearest even on the 11 dropped bits
+  unsigned long long m = a >> 11;
+  const unsigned long long rem = a & 0x7FFull;
+  if (rem > 0x400ull || (rem == 0x400ull && (m & 1ull))) m += 1ull;
+  int ex = 63 - lz + sc;                      // value = m * 2^(ex - 52)
+  if (m >> 53) {                              // rounding carried into a new bit
+    m >>= 1;
+    ex += 1;
+  }
+  const unsigned long long bits = sign | ((unsigned long long)(ex + 1023) << 52) | (m & 0x000FFFFFFFFFFFFFull);
+  return __longlong_as_double((long long)bits);
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t parity) {
+  for (int it = 0; it < (1 << 20); ++it) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(addr), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
+// Tile geometry.  Complex dimensions are processed in chunks of CW = min(WP, 32) complex
+// indices; a chunk's real index l < CW is the real part of complex index chunk*CW + l and
+// l >= CW its imaginary part.  KC = NC = 2*CW real entries per chunk, NCH chunks along K
+// and along N (W up to 128).  Shared memory holds the S digit slices of one A chunk
+// (128 x KC) and one B chunk (NC x KC); TMEM holds the S diagonals of one N chunk.
+template <int WP>
+struct TileSmem {
+  static constexpr int CW = WP < 32 ? WP : 32;
+  static constexpr int KC = 2 * CW;
+  static constexpr int NC = 2 * CW;
+  static constexpr int NCH = WP / CW;
+  static constexpr int A_BYTES = kTileRows * KC * 2;
+  static constexpr int B_BYTES = NC * KC * 2;
+  static constexpr int TMEM_COLS = (kDiag * NC <= 128) ? 128 : ((kDiag * NC <= 256) ? 256 : 512);
+  static constexpr size_t BYTES = (size_t)kS * (A_BYTES + B_BYTES) + 1024;
+};
+
+}  // namespace
+
+}  // namespace w90g

@@ -194,6 +194,62 @@ def w90_wannierise_batch_device(commons, m_ptrs, u_ptrs):
     return list(ierr)
 
 
+class Server:
+    """Serving loop (continuous batching) over the C ABI's w90g_server_*: jobs are
+    admitted first-in first-out by an HBM budget and a slot count, run concurrently on
+    the GPU until they converge, and are collected with :meth:`poll`."""
+
+    def __init__(self, hbm_budget_bytes: float, max_active: int = 32, chunk_iters: int = 8):
+        self._L = lib()
+        self._s = self._L.w90g_server_create(float(hbm_budget_bytes), int(max_active), int(chunk_iters))
+        if not self._s:
+            raise W90Error(2, "w90g_server_create failed")
+        self._keep = {}
+
+    def submit(self, common: LibCommon, m_ptr: int, u_ptr: int, tag: int) -> int:
+        """Queue a solve of ``common`` on device buffers (projected M0 / U0, updated in place)."""
+        self._keep[int(tag)] = common
+        return self._L.w90g_server_submit(self._s, common.handle, C.c_void_p(m_ptr), C.c_void_p(u_ptr),
+                                          C.c_longlong(int(tag)))
+
+    def poll(self, max_jobs: int = 1024):
+        """Completed jobs: list of (tag, ierr, t_submit, t_admit, t_done) on the server clock."""
+        tags = (C.c_longlong * max_jobs)()
+        ierr = (C.c_int * max_jobs)()
+        ts, ta, td = ((C.c_double * max_jobs)() for _ in range(3))
+        n = self._L.w90g_server_poll(self._s, tags, ierr, ts, ta, td, max_jobs)
+        out = [(int(tags[i]), int(ierr[i]), ts[i], ta[i], td[i]) for i in range(n)]
+        for t in out:
+            self._keep.pop(t[0], None)
+        return out
+
+    def pending(self) -> int:
+        return int(self._L.w90g_server_pending(self._s))
+
+    def drain(self):
+        self._L.w90g_server_drain(self._s)
+
+    def now(self) -> float:
+        return float(self._L.w90g_server_now(self._s))
+
+    def stats(self) -> dict:
+        out = np.zeros(4, dtype=np.float64)
+        self._L.w90g_server_stats(self._s, out.ctypes.data_as(C.POINTER(C.c_double)))
+        return {"peak_active": int(out[0]), "peak_bytes": float(out[1]), "jobs_done": int(out[2]),
+                "iterations_done": int(out[3])}
+
+    def close(self):
+        if self._s:
+            self._L.w90g_server_delete(self._s)
+            self._s = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def w90_get_centres(common: LibCommon, num_wann: int) -> np.ndarray:
     """Wannier centres as (3, num_wann) (Fortran layout, Angstrom)."""
     out = np.zeros((3, num_wann), dtype=np.float64, order="F")
