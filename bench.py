@@ -46,6 +46,9 @@ WORKLOADS = {
     # 256 independent problems, W ~ U{4,8,...,64}, k-mesh ~ U{3^3,4^3,6^3,8^3}, sc a ~ U[3,7] A,
     # nntot 6, 300 iterations each, solved together
     "batch256": dict(cfg=None, conv_tol=1e-10, conv_window=-1, num_iter=300, nprob=256),
+    # precision stress: sc 8^3 (512 k), nntot 6, num_wann 128, gauge noise 0.5, 200
+    # iterations; tensor-core products against the FP64 engine, per-iteration errors
+    "sc8_w128": dict(cfg="sc8_w128", conv_tol=1e-10, conv_window=-1, num_iter=200, precision_report=True),
     # serving stream: Poisson arrivals (200 req/s), W log-uniform [8,96], k-mesh
     # U{4^3,6^3,8^3,10^3,12^3}, sc/fcc 50/50, gauge noise U[0.1,0.5], each run to
     # convergence (1e-10 A^2 over 5 iterations); admission by a 150 GB HBM budget.
@@ -398,6 +401,90 @@ def run_serve(args, wl):
     return 0
 
 
+def run_precision(args, wl):
+    """Precision report: the same 200 iterations with every product on the FP64 pipe
+    (the plain FP64 engine, reference of this report) and with the tensor-core products,
+    plus the FP64 engine on an input perturbed by 1e-15 (relative), which shows how fast
+    roundoff-level differences grow along this trajectory.  Errors of Omega_I, Omega_D,
+    Omega_OD, Omega and of every centre are reported per iteration."""
+    import numpy as np
+    import torch
+
+    from wannier90_gb300 import library as w90
+    from wannier90_gb300 import synth
+
+    torch.cuda.set_device(0)
+    n_it = args.precision_iters or wl["num_iter"]
+    p = synth.make_problem(**synth.CONFIGS[wl["cfg"]], seed=0)
+    W, K, B = p.num_wann, len(p.kpoints), p.nntot
+    opts = dict(num_iter=n_it, conv_tol=wl["conv_tol"], conv_window=-1, iprint=0)
+    h0 = w90.setup(kpoints=p.kpoints, unit_cell_cart=p.real_lattice, num_wann=W, gpu_tensor=0, **opts)
+    m0 = torch.from_numpy(p.m.reshape(-1, order="F").view(np.float64).copy()).cuda()
+    u0 = torch.from_numpy(p.a.reshape(-1, order="F").view(np.float64).copy()).cuda()
+    w90.check(h0, w90.w90_project_overlap_device(h0, m0.data_ptr(), u0.data_ptr()), "projection")
+    torch.cuda.synchronize()
+    rng = np.random.Generator(np.random.PCG64(12345))
+    noise = torch.from_numpy(1.0 + 1e-15 * rng.standard_normal(m0.numel())).cuda()
+
+    def run(tensor, perturb=False):
+        h = w90.setup(kpoints=p.kpoints, unit_cell_cart=p.real_lattice, num_wann=W, gpu_tensor=tensor, **opts)
+        m, u = m0.clone(), u0.clone()
+        if perturb:
+            m.mul_(noise)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        w90.check(h, w90.w90_wannierise_device(h, m.data_ptr(), u.data_ptr()), "wannierise")
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t
+        log = w90.w90_get_log(h, n_it + 1)
+        cen = w90.w90_get_log_centres(h, n_it + 1, W)
+        return log, cen, dt
+
+    clocks = ClockSampler(0)
+    clocks.start()
+    ref, ref_c, t_ref = run(0)
+    ten, ten_c, t_ten = run(1)
+    clk = clocks.stop()
+    per, per_c, _ = run(0, perturb=True)
+
+    def errors(log, cen):
+        n = min(len(log), len(ref))
+        om = lambda L: np.stack([L[:n, 3] - L[:n, 4] - L[:n, 5], L[:n, 4], L[:n, 5], L[:n, 3]], axis=1)
+        d = np.abs(om(log) - om(ref))
+        rel = d[:, 3] / np.abs(ref[:n, 3])
+        dc = np.abs(cen[:n, :3, :] - ref_c[:n, :3, :]).max(axis=(1, 2))
+        return d, rel, dc
+
+    d_t, rel_t, dc_t = errors(ten, ten_c)
+    d_p, rel_p, dc_p = errors(per, per_c)
+    marks = [i for i in (0, 1, 2, 3, 5, 10, 20, 30, 50, 100, 150, 200) if i < len(rel_t)]
+
+    def first_over(rel, dc):
+        bad = np.nonzero((rel > 1e-8) | (dc > 1e-6))[0]
+        return int(bad[0]) if len(bad) else None
+
+    line = {
+        "metric": "per-iteration error of the tensor-core engine against the FP64 engine",
+        "value": float(rel_t[: first_over(rel_p, dc_p) or len(rel_t)].max()), "unit": "max |dOmega|/Omega in the stable window",
+        "n_gpus": 1, "steps": 1, "warmup": 0, "higher_is_better": False, "dtype": "f64 (FP64 engine) / bf16-sliced (tensor)",
+        "data": "synthetic (seeded tight-binding generator)",
+        "config": {"workload": args.workload, "lattice": "sc a=5", "kmesh": "8^3", "nntot": B, "num_wann": W,
+                   "eps": 0.5, "iterations": n_it},
+        "ms_per_iteration": {"fp64": 1e3 * t_ref / n_it, "tensor": 1e3 * t_ten / n_it,
+                             "speedup": t_ref / t_ten},
+        "first_iteration_over_1e-8_or_1e-6A": {"tensor_vs_fp64": first_over(rel_t, dc_t),
+                                               "fp64_vs_fp64_input_1e-15": first_over(rel_p, dc_p)},
+        "per_iteration": {str(i): {"tensor": {"dOmega_I": d_t[i, 0], "dOmega_D": d_t[i, 1], "dOmega_OD": d_t[i, 2],
+                                              "dOmega_rel": rel_t[i], "dcentre_A": dc_t[i]},
+                                   "fp64_input_1e-15": {"dOmega_rel": rel_p[i], "dcentre_A": dc_p[i]}}
+                          for i in marks},
+        "final_spread": {"fp64": float(ref[-1, 3]), "tensor": float(ten[-1, 3])},
+        "clocks": clk,
+    }
+    print(json.dumps(line, default=float))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -416,6 +503,7 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=0.0, help="arrival rate of the serving stream (200/s)")
     ap.add_argument("--serve-wmax", type=int, default=96, help="largest num_wann of the serving stream")
     ap.add_argument("--serve-nmax", type=int, default=12, help="largest k-mesh edge of the serving stream")
+    ap.add_argument("--precision-iters", type=int, default=0, help="iterations of the precision report (200)")
     ap.add_argument("--profile-case", type=int, default=0,
                     help="run one solve capped at this many iterations and exit (small case for ncu)")
     ap.add_argument("--precision", default="tensor", choices=["tensor", "fp64"],
@@ -432,6 +520,8 @@ def main():
         return run_batch(args, wl)
     if wl.get("serve"):
         return run_serve(args, wl)
+    if wl.get("precision_report"):
+        return run_precision(args, wl)
     rank, local_rank, world = _env_rank()
     import numpy as np
     import torch

@@ -242,8 +242,30 @@ def kmesh_get(real_lattice, kpt_latt, search_shells=36, tol=1.0e-6):
                 if cnt == multi[s]:
                     break
     wbtot = float(wb.sum())
+    # b directions without inversion partners, from the first k-point (:505-528), and
+    # the index of each direction in every k-point's neighbour list (:561-577)
+    compar = lambda a, b: (float(((a - b) ** 2).sum()) < EPS8, float(((a + b) ** 2).sum()) < EPS8)
+    bka = []
+    for nn in range(nntot):
+        if not any(compar(v, bk[0, nn])[1] for v in bka):
+            bka.append(bk[0, nn].copy())
+    nnh = nntot // 2
+    if len(bka) != nnh:
+        raise RuntimeError("Did not find right number of bk directions")
+    bka = np.array(bka)
+    neigh = np.zeros((K, nnh), dtype=np.int64)
+    for nkp in range(K):
+        for na in range(nnh):
+            hit = -1
+            for nn in range(nntot):
+                if compar(bka[na], bk[nkp, nn])[0]:
+                    hit = nn
+            if hit < 0:
+                raise RuntimeError("kmesh_get: failed to find neighbours for this kpoint")
+            neigh[nkp, na] = hit
     return dict(nntot=nntot, nnlist=nnlist, nncell=nncell, wb=wb, bk=bk, wbtot=wbtot,
-                shells=[s + 1 for s in shell_list], dnn=np.array(dnn), multi=np.array(multi))
+                shells=[s + 1 for s in shell_list], dnn=np.array(dnn), multi=np.array(multi),
+                nnh=nnh, bka=bka, neigh=neigh)
 
 
 # ---------------------------------------------------------------------------
@@ -280,15 +302,24 @@ class Spread:
         return Spread(self.om_i, self.om_d, self.om_od, self.om_tot)
 
 
-def wann_omega(M, km, omega_invariant=None):
+def _ln_diag(diag, sheet):
+    """Im ln M_nn on the branch chosen by the guiding centres: aimag(log(csheet*M_nn))
+    - sheet (src/wannierise.F90:2036-2041, :2368-2374); sheet None = no guiding."""
+    if sheet is None:
+        return np.angle(diag)
+    return np.angle(np.exp(1j * sheet) * diag) - sheet
+
+
+def wann_omega(M, km, omega_invariant=None, sheet=None):
     """Returns (Spread, rave[3,W], r2ave[W], rave2[W]).
 
     ``omega_invariant`` None reproduces the ``first_pass`` branch (:2214-2239).
+    ``sheet`` [K,B,W]: branch-cut offsets of the guiding centres (wann_phases).
     """
     K, B, W, _ = M.shape
     wb, bk = km["wb"], km["bk"]
     diag = np.diagonal(M, axis1=2, axis2=3)           # (K,B,W)
-    ln = np.angle(diag)                               # aimag(log(.)) :2034-2043
+    ln = _ln_diag(diag, sheet)                        # aimag(log(.)) :2034-2043
     rave = -np.einsum("b,kbi,kbn->in", wb, bk, ln) / K          # :2045-2061
     rave2 = (rave * rave).sum(axis=0)
     mnn2 = (diag * diag.conj()).real
@@ -307,12 +338,12 @@ def wann_omega(M, km, omega_invariant=None):
     return sp, rave, r2ave, rave2
 
 
-def wann_domega(M, km):
+def wann_domega(M, km, sheet=None):
     """Gradient cdodq(m,n,k) (src/wannierise.F90:2287-2569, non-SLWF branch)."""
     K, B, W, _ = M.shape
     wb, bk = km["wb"], km["bk"]
     diag = np.diagonal(M, axis1=2, axis2=3)
-    lnw = wb[None, :, None] * np.angle(diag)           # :2366-2375
+    lnw = wb[None, :, None] * _ln_diag(diag, sheet)    # :2366-2375
     rave = -np.einsum("kbi,kbn->in", bk, lnw) / K      # :2378-2391
     rnkb = np.einsum("kbi,in->kbn", bk, rave)          # :2409-2417
     crt = M / diag[:, :, None, :]
@@ -326,6 +357,55 @@ def wann_domega(M, km):
     R = crt * rnkb[:, :, None, :]
     G -= (w * (R + H(R)) * (-0.5j)).sum(axis=1)        # :2521-2524
     return G * (4.0 / K)                               # :2531
+
+
+# ---------------------------------------------------------------------------
+# guiding centres: wann_phases (src/wannierise.F90:1756-1976)
+# ---------------------------------------------------------------------------
+def inv3(a):
+    """utility_inv3 (src/utility.F90:233-262): cofactor matrix b and determinant;
+    for the symmetric matrices it is used on, inverse(a) = b / det."""
+    b = np.empty((3, 3))
+    b[0, 0] = a[1, 1] * a[2, 2] - a[2, 1] * a[1, 2]
+    b[0, 1] = a[1, 2] * a[2, 0] - a[2, 2] * a[1, 0]
+    b[0, 2] = a[1, 0] * a[2, 1] - a[2, 0] * a[1, 1]
+    b[1, 0] = a[2, 1] * a[0, 2] - a[0, 1] * a[2, 2]
+    b[1, 1] = a[2, 2] * a[0, 0] - a[0, 2] * a[2, 0]
+    b[1, 2] = a[2, 0] * a[0, 1] - a[0, 0] * a[2, 1]
+    b[2, 0] = a[0, 1] * a[1, 2] - a[1, 1] * a[0, 2]
+    b[2, 1] = a[0, 2] * a[1, 0] - a[1, 2] * a[0, 0]
+    b[2, 2] = a[0, 0] * a[1, 1] - a[1, 0] * a[0, 1]
+    det = float(a[0, 0] * b[0, 0] + a[0, 1] * b[0, 1] + a[0, 2] * b[0, 2])
+    return b, det
+
+
+def wann_phases(M, km, rguide, irguide):
+    """Returns (rguide[3,W], sheet[K,B,W]).  The centres are refitted from the phases of
+    sum_k M_nn(k, b) over the b directions when irguide != 0 (:1830-1925); the sheet is
+    b . rguide_n (:1927-1939)."""
+    K, B, W, _ = M.shape
+    bka, neigh = km["bka"], km["neigh"]
+    rguide = np.array(rguide, dtype=np.float64, copy=True)
+    diag = np.diagonal(M, axis1=2, axis2=3)            # (K,B,W)
+    for n in range(W):
+        csum = np.array([diag[np.arange(K), neigh[:, na], n].sum() for na in range(km["nnh"])])
+        smat = np.zeros((3, 3))
+        svec = np.zeros(3)
+        for nn in range(km["nnh"]):
+            if nn < 3:
+                xx = -math.atan2(csum[nn].imag, csum[nn].real)
+            else:
+                xx0 = float(bka[nn] @ rguide[:, n])
+                z = csum[nn] * complex(math.cos(xx0), math.sin(xx0))
+                xx = xx0 - math.atan2(z.imag, z.real)
+            smat += np.outer(bka[nn], bka[nn])
+            svec += bka[nn] * xx
+            if nn >= 2:
+                sinv, det = inv3(smat)
+                if abs(det) > EPS6 and irguide != 0:
+                    rguide[:, n] = sinv @ svec / det
+    sheet = np.einsum("kbi,in->kbn", km["bk"], rguide)
+    return rguide, sheet
 
 
 # ---------------------------------------------------------------------------
@@ -402,6 +482,9 @@ class WannControl:
     conv_noise_amp: float = -1.0
     conv_noise_num: int = 3
     precond: bool = False
+    guiding_centres: bool = False
+    num_no_guide_iter: int = 0
+    num_guide_cycles: int = 1
 
 
 @dataclass
@@ -443,18 +526,28 @@ def new_u_and_m(cdq, U, M, nnlist):
     return Unew, Mnew
 
 
-def wann_main(M, U, km, ctl: WannControl, record=True, precond=None):
-    """Restatement of wann_main for guiding_centres=F, SLWF=F, no sitesym.
-    ``precond``: the tables of :func:`precond_setup` when ``ctl.precond``."""
+def wann_main(M, U, km, ctl: WannControl, record=True, precond=None, rguide=None):
+    """Restatement of wann_main for SLWF=F, no sitesym.
+    ``precond``: the tables of :func:`precond_setup` when ``ctl.precond``;
+    ``rguide``: guiding centres [3,W] (Cartesian, Angstrom) when ``ctl.guiding_centres``."""
     if ctl.precond and precond is None:
         raise ValueError("precond=T needs the precond_setup tables")
+    if ctl.guiding_centres and rguide is None:
+        raise ValueError("guiding_centres=T needs the projection centres")
     M = M.copy()
     U = U.copy()
     K, B, W, _ = M.shape
     nnlist = km["nnlist"]
     wbtot = km["wbtot"]
 
-    wann_spread, rave, r2ave, rave2 = wann_omega(M, km)          # :452-457
+    sheet = None
+    irguide = 0
+    if ctl.guiding_centres:
+        sheet = np.zeros((K, B, W))
+        if ctl.num_no_guide_iter <= 0:                            # :435-443
+            rguide, sheet = wann_phases(M, km, rguide, irguide)
+            irguide = 1
+    wann_spread, rave, r2ave, rave2 = wann_omega(M, km, sheet=sheet)   # :452-457
     om_invariant = wann_spread.om_i
     res = WannResult(U, M, wann_spread, rave, r2ave - rave2)
     res.initial = IterRecord(0, wann_spread.om_tot, 0.0, wann_spread.copy(), rave.copy(),
@@ -474,7 +567,11 @@ def wann_main(M, U, km, ctl: WannControl, record=True, precond=None):
     alphamin = 0.0
     it = 0
     for it in range(1, ctl.num_iter + 1):
-        cdodq = wann_domega(M, km)                                    # :566-571
+        if (ctl.guiding_centres and it > ctl.num_no_guide_iter
+                and it % max(ctl.num_guide_cycles, 1) == 0):           # :546-555
+            rguide, sheet = wann_phases(M, km, rguide, irguide)
+            irguide = 1
+        cdodq = wann_domega(M, km, sheet=sheet)                       # :566-571
         if ctl.precond:                                               # :577-581
             cdodq_p = precond_search_direction(cdodq, wann_spread.om_tot, precond)
         else:
@@ -522,7 +619,7 @@ def wann_main(M, U, km, ctl: WannControl, record=True, precond=None):
             cdq_t = cdqkeep * (ctl.trial_step / (4.0 * wbtot))        # :605
             U0, M0 = U, M
             U, M = new_u_and_m(cdq_t, U0, M0, nnlist)
-            trial_spread, rave, r2ave, rave2 = wann_omega(M, km, om_invariant)
+            trial_spread, rave, r2ave, rave2 = wann_omega(M, km, om_invariant, sheet=sheet)
             # internal_optimal_step (:1528-1596)
             fac = trial_spread.om_tot - wann_spread.om_tot
             if abs(fac) > TINY_DP:
@@ -549,7 +646,7 @@ def wann_main(M, U, km, ctl: WannControl, record=True, precond=None):
                 U, M = U0, M0
             U, M = new_u_and_m(cdq_a, U, M, nnlist)
             old_spread = wann_spread.copy()
-            wann_spread, rave, r2ave, rave2 = wann_omega(M, km, om_invariant)
+            wann_spread, rave, r2ave, rave2 = wann_omega(M, km, om_invariant, sheet=sheet)
         else:
             old_spread = wann_spread.copy()
             wann_spread = trial_spread.copy()

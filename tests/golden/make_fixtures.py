@@ -17,6 +17,10 @@ testw90_precond_1 / _2) it stores, in one ``.npz``:
   final centres/spreads, the final Omega_I/Omega_D/Omega_OD/Omega_total and the
   b-vector/weight table.
 
+The guiding-centre case (testpostw90_gaas_shc: spinor GaAs, 16 isolated bands,
+guiding_centres = T) has no printed wannierise trajectory; its expected values are the
+final centres and spreads of the checkpoint shipped with that test.
+
 The parser here is deliberately independent of the package's own file readers.
 """
 from __future__ import annotations
@@ -146,6 +150,81 @@ def parse_benchmark(path):
     return conv, initial, final, om, np.array(bvec)
 
 
+def projection_sites(blocks, real_lattice, spinors):
+    """Sites of the projections, in the order of w90_readwrite_get_projections
+    (src/readwrite.F90:3536-3960): per line, per atom of the species, per orbital, per
+    spin.  Only the 'Element:orbital' form with atoms_frac is handled."""
+    norb = {"s": 1, "p": 3, "d": 5, "f": 7, "sp": 2, "sp2": 3, "sp3": 4, "sp3d": 5, "sp3d2": 6}
+    atoms = [(l.split()[0], [float(x) for x in l.split()[1:4]]) for l in blocks["atoms_frac"]]
+    sites = []
+    for line in blocks["projections"]:
+        el, orbs = [x.strip() for x in line.split(":")[:2]]
+        n = sum(norb[o.strip().lower()] for o in orbs.split(";"))
+        for name, frac in atoms:
+            if name.lower() == el.lower():
+                sites += [frac] * (n * (2 if spinors else 1))
+    return np.array(sites)
+
+
+def parse_chk_fmt_tail(lines, num_wann):
+    """Final centres (Angstrom) and spreads: the last 2*num_wann lines of a formatted
+    .chk (src/wannier90_readwrite.F90:2336-2366, written by w90chk2chk -u2f)."""
+    cen = np.array([[float(x) for x in l.split()] for l in lines[-2 * num_wann:-num_wann]])
+    spr = np.array([float(l.split()[0]) for l in lines[-num_wann:]])
+    return cen, spr
+
+
+def build_guiding(ref_root, out_dir):
+    """testpostw90_gaas_shc: GaAs, spinor isolated bands (16), 4x4x4 k, guiding
+    centres, conv_window 40.  Expected values: the final centres and spreads of the
+    checkpoint the test ships (GaAs.chk.fmt.bz2)."""
+    import bz2
+    d = os.path.join(ref_root, "test-suite/tests/testpostw90_gaas_shc")
+    lines = [_strip(l) for l in open(os.path.join(d, "GaAs.win"))]
+    blocks, i = {}, 0
+    lines = [l for l in lines if l]
+    while i < len(lines):
+        if lines[i].lower().startswith("begin"):
+            name = lines[i].lower().split()[1]
+            body = []
+            i += 1
+            while not lines[i].lower().startswith("end"):
+                body.append(lines[i])
+                i += 1
+            blocks[name] = body
+        i += 1
+    kw, real_lattice, kpts = parse_win(os.path.join(d, "GaAs.win"))
+    tmp = os.path.join(out_dir, "_tmp_gaas")
+    os.makedirs(tmp, exist_ok=True)
+    for ext in ("mmn", "amn"):
+        with bz2.open(os.path.join(d, "GaAs.%s.bz2" % ext), "rb") as f, open(os.path.join(tmp, "GaAs." + ext), "wb") as g:
+            g.write(f.read())
+    nb, nk, nntot, heads, blk = parse_mmn(os.path.join(tmp, "GaAs.mmn"))
+    A = parse_amn(os.path.join(tmp, "GaAs.amn"))
+    for ext in ("mmn", "amn"):
+        os.remove(os.path.join(tmp, "GaAs." + ext))
+    os.rmdir(tmp)
+    chk = bz2.open(os.path.join(d, "GaAs.chk.fmt.bz2"), "rt").read().splitlines()
+    W = int(kw["num_wann"])
+    cen, spr = parse_chk_fmt_tail(chk, W)
+    spinors = kw.get("spinors", "f").strip(".").lower().startswith("t")
+    sites = projection_sites(blocks, real_lattice, spinors)
+    knobs = dict(num_wann=W, num_iter=int(kw.get("num_iter", 100)), num_cg_steps=int(kw.get("num_cg_steps", 5)),
+                 conv_tol=float(kw.get("conv_tol", "1e-10").replace("d", "e")),
+                 conv_window=int(kw.get("conv_window", -1)), trial_step=float(kw.get("trial_step", 2.0)),
+                 search_shells=int(kw.get("search_shells", 36)), precond=0, optimisation=3,
+                 guiding_centres=1, num_no_guide_iter=int(kw.get("num_no_guide_iter", 0)),
+                 num_guide_cycles=int(kw.get("num_guide_cycles", 1)))
+    np.savez_compressed(
+        os.path.join(out_dir, "gaas_guide.npz"),
+        real_lattice=real_lattice, kpt_latt=kpts, mp_grid=np.array([int(x) for x in kw["mp_grid"].split()[:3]]),
+        num_bands=nb, num_kpts=nk, nntot=nntot, mmn_heads=heads, mmn_blocks=blk, amn=A,
+        knobs=np.array([knobs[k] for k in sorted(knobs)], dtype=np.float64), knob_names=np.array(sorted(knobs)),
+        proj_site_frac=sites, centres_final=np.concatenate([cen, spr[:, None]], axis=1),
+        omega_final_total=np.array([spr.sum()]))
+    print("gaas_guide", nb, nk, nntot, sites.shape, spr.sum())
+
+
 def build(ref_root, out_dir):
     for name, (sub, seed) in CASES.items():
         d = os.path.join(ref_root, sub)
@@ -179,3 +258,4 @@ def build(ref_root, out_dir):
 if __name__ == "__main__":
     root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     build(root, os.path.dirname(os.path.abspath(__file__)))
+    build_guiding(root, os.path.dirname(os.path.abspath(__file__)))

@@ -46,3 +46,14 @@ def precond_tables(d):
     if not d["knobs"].get("precond", 0):
         return None
     return O.precond_setup(d["real_lattice"], d["kpt_latt"], d["mp_grid"])
+
+
+def guiding(d):
+    """(WannControl, rguide[3,W] Cartesian) of the guiding-centre case."""
+    from oracle import w90_oracle as O
+    kn = d["knobs"]
+    ctl = O.WannControl(num_iter=int(kn["num_iter"]), num_cg_steps=int(kn["num_cg_steps"]),
+                        conv_tol=float(kn["conv_tol"]), conv_window=int(kn["conv_window"]),
+                        trial_step=float(kn["trial_step"]), guiding_centres=True,
+                        num_no_guide_iter=int(kn["num_no_guide_iter"]), num_guide_cycles=int(kn["num_guide_cycles"]))
+    return ctl, (d["proj_site_frac"] @ d["real_lattice"]).T

@@ -27,10 +27,10 @@ from wannier90_gb300 import synth
 pytestmark = pytest.mark.gpu
 
 
-def _oracle(real_lattice, kpoints, M_raw, A, ctl, search_shells=36, precond=None):
+def _oracle(real_lattice, kpoints, M_raw, A, ctl, search_shells=36, precond=None, rguide=None):
     km = O.kmesh_get(real_lattice, kpoints, search_shells)
     U0, M0 = O.overlap_project(M_raw, A, km["nnlist"])
-    r = O.wann_main(M0, U0, km, ctl, precond=precond)
+    r = O.wann_main(M0, U0, km, ctl, precond=precond, rguide=rguide)
     return km, U0, M0, r
 
 
@@ -60,13 +60,13 @@ def _sensitivity(M0, U0, km, ctl, noise, precond=None):
     return {x.iter: abs(x.spread.om_tot - y.spread.om_tot) for x, y in zip([a.initial] + a.iters, [b.initial] + b.iters)}
 
 
-def _stable_window(M0, U0, km, ctl, tol=1e-11, noise=1e-15, precond=None):
+def _stable_window(M0, U0, km, ctl, tol=1e-11, noise=1e-15, precond=None, rguide=None):
     """Last iteration up to which the oracle agrees with itself on an input perturbed by
     `noise` (relative): 1e-15 for the FP64 engine, 1e-13 for the tensor engine, whose
     per-step roundoff (Ozaki slicing, ~2^-49 of the row x column scales) is larger."""
     rng = np.random.default_rng(12345)
-    a = O.wann_main(M0, U0, km, ctl, precond=precond)
-    b = O.wann_main(M0 * (1 + noise * rng.standard_normal(M0.shape)), U0, km, ctl, precond=precond)
+    a = O.wann_main(M0, U0, km, ctl, precond=precond, rguide=rguide)
+    b = O.wann_main(M0 * (1 + noise * rng.standard_normal(M0.shape)), U0, km, ctl, precond=precond, rguide=rguide)
     last = 0
     for x, y in zip(a.iters, b.iters):
         if abs(x.spread.om_tot - y.spread.om_tot) > tol * abs(x.spread.om_tot) + 1e-13:
@@ -240,3 +240,53 @@ def test_tensor_exp_matches_fp64_exp(W, mp):
     def unitarity(U):
         return max(np.abs(U[k] @ U[k].conj().T - np.eye(W)).max() for k in range(len(U)))
     assert unitarity(b["U"]) < max(1e-13, 4 * unitarity(a["U"]))
+
+
+@pytest.mark.parametrize("tensor", [0, 1], ids=["fp64", "tensor"])
+def test_guiding_centres_golden(tensor):
+    """Guiding centres on the reference's spinor GaAs case: the trajectory against the
+    oracle over its stable window, the final state against the shipped checkpoint."""
+    d = G.load("gaas_guide")
+    ctl, rguide = G.guiding(d)
+    ss = int(d["knobs"]["search_shells"])
+    km = O.kmesh_get(d["real_lattice"], d["kpt_latt"], ss)
+    M = G.assemble_m(d, km["nnlist"], km["nncell"])
+    A = np.ascontiguousarray(d["amn"])
+    extra = {"gpu_tensor": tensor, "guiding_centres": 1,
+             "guiding_centres_frac": np.asarray(d["proj_site_frac"], dtype=np.float64),
+             "num_no_guide_iter": int(d["knobs"]["num_no_guide_iter"]),
+             "num_guide_cycles": int(d["knobs"]["num_guide_cycles"])}
+    out = run_engine(d["real_lattice"], d["kpt_latt"], M, A, ctl, int(d["num_bands"]), ss, extra=extra)
+    assert out["ierr"] <= 0, out["err"]
+    U0, M0 = O.overlap_project(M, A, km["nnlist"])
+    short = O.WannControl(**{**ctl.__dict__, "num_iter": 60})
+    r = O.wann_main(M0, U0, km, short, rguide=rguide)
+    window = min(_stable_window(M0, U0, km, short, noise=1e-13 if tensor else 1e-15, rguide=rguide), 60)
+    assert window >= 5
+    _check_trajectory(out, r, upto=window)
+    fin = d["centres_final"]
+    np.testing.assert_allclose(out["centres"].T, fin[:, :3], atol=2e-6)
+    np.testing.assert_allclose(out["spreads"], fin[:, 3], atol=5e-6)
+    assert abs(out["omega"][3] - d["omega_final_total"][0]) < 1e-6
+
+
+@pytest.mark.parametrize("no_guide,cycles", [(0, 1), (3, 2)])
+def test_guiding_centres_synthetic(no_guide, cycles):
+    """num_no_guide_iter / num_guide_cycles schedules on a synthetic problem."""
+    cfg = dict(kind="sc", a=4.0, mp=(3, 3, 3), num_wann=6, rmax=1, eps=0.3)
+    p = synth.make_problem(**cfg, seed=11)
+    M = synth.to_math_m(p.m)
+    A = synth.to_math_u(p.a)
+    ctl = O.WannControl(num_iter=25, guiding_centres=True, num_no_guide_iter=no_guide, num_guide_cycles=cycles)
+    frac = np.ascontiguousarray(p.tau @ np.linalg.inv(p.real_lattice))   # the orbital sites
+    rguide = (frac @ p.real_lattice).T
+    out = run_engine(p.real_lattice, p.kpoints, M, A, ctl, 6,
+                     extra={"guiding_centres": 1, "guiding_centres_frac": frac,
+                            "num_no_guide_iter": no_guide, "num_guide_cycles": cycles})
+    assert out["ierr"] == 0, out["err"]
+    km = O.kmesh_get(p.real_lattice, p.kpoints)
+    U0, M0 = O.overlap_project(M, A, km["nnlist"])
+    r = O.wann_main(M0, U0, km, ctl, rguide=rguide)
+    window = _stable_window(M0, U0, km, ctl, rguide=rguide)
+    assert window >= 3
+    _check_trajectory(out, r, upto=window)

@@ -39,3 +39,18 @@ def test_oracle_reproduces_reference_trajectory(name):
     om = d["omega_final"]
     got = [r.spread.om_i, r.spread.om_d, r.spread.om_od, r.spread.om_tot]
     np.testing.assert_allclose(got, om, atol=1.01e-9)
+
+
+def test_oracle_guiding_centres_reach_reference_checkpoint():
+    """testpostw90_gaas_shc (spinor GaAs, 16 isolated bands, guiding_centres = T,
+    1000 iterations): the final centres and spreads of the shipped checkpoint."""
+    d = G.load("gaas_guide")
+    km = O.kmesh_get(d["real_lattice"], d["kpt_latt"], int(d["knobs"]["search_shells"]))
+    M = G.assemble_m(d, km["nnlist"], km["nncell"])
+    U0, M0 = O.overlap_project(M, d["amn"], km["nnlist"])
+    ctl, rguide = G.guiding(d)
+    r = O.wann_main(M0, U0, km, ctl, rguide=rguide)
+    fin = d["centres_final"]
+    np.testing.assert_allclose(r.centres.T, fin[:, :3], atol=2e-6)
+    np.testing.assert_allclose(r.spreads, fin[:, 3], atol=5e-6)
+    assert abs(r.spread.om_tot - d["omega_final_total"][0]) < 1e-6

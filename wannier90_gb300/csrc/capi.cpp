@@ -59,6 +59,10 @@ struct Handle {
   // hamiltonian_setup / k_to_r (src/wannierise.F90:269-300)
   int precond = 0, nrpts = 0;
   std::vector<double> pc_kr, pc_r2, pc_ndeg;
+  // guiding centres (wann_main :415-420, wann_phases); the centres are the projection
+  // sites, passed as the engine option guiding_centres_frac (num_wann x 3, fractional)
+  int guiding = 0, no_guide_iter = 0, guide_cycles = 1;
+  std::vector<double> rguide0;   // [3][W] Cartesian
   // caller data
   double* m_local = nullptr;
   double* u_matrix = nullptr;
@@ -215,6 +219,15 @@ int build_spec(Handle* h, ProblemSpec& s) {
   s.ctl = h->ctl;
   s.tensor = h->gpu_tensor;
   s.tensor_exp = h->gpu_tensor_exp;
+  s.guiding = h->guiding;
+  s.no_guide_iter = h->no_guide_iter;
+  s.guide_cycles = h->guide_cycles;
+  if (h->guiding) {
+    s.rguide0 = h->rguide0;
+    s.nnh = h->km.nnh;
+    s.bka = h->km.bka;
+    s.neigh = h->km.neigh;
+  }
   s.precond = h->precond;
   s.nrpts = h->nrpts;
   s.pc_kr = h->pc_kr;
@@ -573,7 +586,7 @@ void cinput_setopt(void* hv, const char* seedname, int* ierr, int comm) {
   // with gpu_tensor: gpu_tensor_exp = 1 (default) also runs exp(s D) and U dU on tensor cores
   h->gpu_tensor_exp = get_num(h, "gpu_tensor_exp", v) ? (int)v : 1;
   // options on wann_main's code path that the engine does not implement
-  const char* unsupported[] = {"guiding_centres", "slwf_num", "slwf_constrain", "site_symmetry",
+  const char* unsupported[] = {"slwf_num", "slwf_constrain", "site_symmetry",
                                "gamma_only"};
   for (const char* k : unsupported) {
     if (get_num(h, k, v)) {
@@ -594,6 +607,30 @@ void cinput_setopt(void* hv, const char* seedname, int* ierr, int comm) {
   if (rc) {
     *ierr = fail(h, rc, err);
     return;
+  }
+  h->guiding = get_num(h, "guiding_centres", v) ? (v != 0.0) : 0;
+  h->no_guide_iter = get_num(h, "num_no_guide_iter", v) ? (int)v : 0;
+  h->guide_cycles = get_num(h, "num_guide_cycles", v) ? (int)v : 1;
+  h->rguide0.clear();
+  if (h->guiding) {
+    if (h->no_guide_iter < 0 || h->guide_cycles < 0) {
+      *ierr = fail(h, 5, "Error: num_no_guide_iter and num_guide_cycles must be >= 0");
+      return;
+    }
+    auto git = h->opts.find("guiding_centres_frac");
+    if (git == h->opts.end() || git->second.cols != 3 || git->second.rows < h->num_wann) {
+      *ierr = fail(h, 5, "Error: guiding_centres = T needs the projection centres (guiding_centres_frac, num_wann x 3)");
+      return;
+    }
+    const int W = h->num_wann;
+    h->rguide0.assign((size_t)3 * W, 0.0);
+    for (int n = 0; n < W; ++n)
+      for (int j = 0; j < 3; ++j) {
+        // utility_frac_to_cart: r = sum_i frac_i a_i
+        double x = 0.0;
+        for (int i = 0; i < 3; ++i) x += git->second.v[(size_t)n * 3 + i] * h->real_lattice[i * 3 + j];
+        h->rguide0[(size_t)j * W + n] = x;
+      }
   }
   h->precond = get_num(h, "precond", v) ? (v != 0.0) : 0;
   h->nrpts = 0;

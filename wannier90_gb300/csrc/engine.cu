@@ -38,6 +38,7 @@ __global__ void k_u_final(const Problem* probs, WorkMap wm);
 __global__ void k_u_identity(const Problem* probs, WorkMap wm);
 __global__ void k_frob0(const Problem* probs, WorkMap wm);
 __global__ void k_precond(const Problem* probs, int dir);
+__global__ void k_phases(const Problem* probs, int mode);
 cudaError_t oz_launch(int wp, int step, const Problem* probs, WorkMap wm, int which, int grid,
                       cudaStream_t s);
 cudaError_t oz_set_attributes(int wp);
@@ -93,6 +94,11 @@ int Engine::setup(const std::vector<ProblemSpec>& specs, std::string& err) {
       err = "conv_window larger than the engine maximum (64)";
       return 5;
     }
+    if (s.guiding && (s.nnh < 3 || s.rguide0.size() != (size_t)3 * s.W || s.bka.size() != (size_t)3 * s.nnh ||
+                      s.neigh.size() != (size_t)s.K * s.nnh)) {
+      err = "guiding_centres: centres or b-direction tables missing";
+      return 5;
+    }
     if (s.precond && (s.nrpts < 1 || s.pc_kr.size() != (size_t)2 * s.K * s.nrpts ||
                       s.pc_r2.size() != (size_t)s.nrpts || s.pc_ndeg.size() != (size_t)s.nrpts)) {
       err = "precond: Wigner-Seitz tables missing or inconsistent";
@@ -103,8 +109,7 @@ int Engine::setup(const std::vector<ProblemSpec>& specs, std::string& err) {
   std::ostringstream key;
   for (const auto& s : specs)
     key << s.W << ',' << s.K << ',' << s.B << ',' << s.ctl.num_iter << ',' << s.tensor << ',' << s.tensor_exp << ','
-        << s.precond << ','
-        << s.nrpts << ';';
+        << s.precond << ',' << s.nrpts << ',' << s.guiding << ';';
   specs_ = specs;
   if (arena_ && key.str() == layout_key_) {
     // refresh the read-only tables (they may differ at equal shapes)
@@ -114,6 +119,10 @@ int Engine::setup(const std::vector<ProblemSpec>& specs, std::string& err) {
       W90G_CHECK(cudaMemcpyAsync((void*)P.nnlist, s.nnlist.data(), s.nnlist.size() * sizeof(int), cudaMemcpyHostToDevice, stream()));
       W90G_CHECK(cudaMemcpyAsync((void*)P.bk, s.bk.data(), s.bk.size() * sizeof(double), cudaMemcpyHostToDevice, stream()));
       W90G_CHECK(cudaMemcpyAsync((void*)P.wb, s.wb.data(), s.wb.size() * sizeof(double), cudaMemcpyHostToDevice, stream()));
+      if (s.guiding) {
+        W90G_CHECK(cudaMemcpyAsync((void*)P.bka, s.bka.data(), s.bka.size() * 8, cudaMemcpyHostToDevice, stream()));
+        W90G_CHECK(cudaMemcpyAsync((void*)P.neigh, s.neigh.data(), s.neigh.size() * 4, cudaMemcpyHostToDevice, stream()));
+      }
       if (s.precond) {
         W90G_CHECK(cudaMemcpyAsync((void*)P.pc_kr, s.pc_kr.data(), s.pc_kr.size() * 8, cudaMemcpyHostToDevice, stream()));
         W90G_CHECK(cudaMemcpyAsync((void*)P.pc_r2, s.pc_r2.data(), s.pc_r2.size() * 8, cudaMemcpyHostToDevice, stream()));
@@ -152,9 +161,11 @@ int choose_tensor_wp(const std::vector<ProblemSpec>& specs) {
 struct Sizes {
   size_t M, U, KWW, work, tbuf, diag, offd, gpart, cen, log, logc, nn, bk, wb, st, op1, op2, m0, u0, inv, fr;
   size_t pkr, pr2, pgr, pgp, ppart;
+  size_t gbka, gneigh, grg, gsheet, gcsheet;
   size_t total() const {
     return 2 * M + 2 * U + 3 * KWW + work + tbuf + 2 * diag + offd + gpart + cen + log + logc + nn + bk + wb + st +
-           op1 + op2 + m0 + u0 + inv + fr + pkr + 2 * pr2 + pgr + pgp + ppart;
+           op1 + op2 + m0 + u0 + inv + fr + pkr + 2 * pr2 + pgr + pgp + ppart + gbka + gneigh + grg + gsheet +
+           gcsheet;
   }
 };
 
@@ -197,6 +208,14 @@ Sizes problem_sizes(const ProblemSpec& s, int wp, int* pc_tiles) {
     z.ppart = align_up(te * ((K + 15) / 16) * 8);
     if (pc_tiles) *pc_tiles = std::max(*pc_tiles, (int)(te * ((std::max(K, NR) + 15) / 16)));
   }
+  z.gbka = z.gneigh = z.grg = z.gsheet = z.gcsheet = 0;
+  if (s.guiding) {
+    z.gbka = align_up((size_t)s.nnh * 3 * 8);
+    z.gneigh = align_up(K * s.nnh * 4);
+    z.grg = align_up(3 * W * 8);
+    z.gsheet = align_up(K * B * W * 8);
+    z.gcsheet = align_up(K * B * W * 16);
+  }
   return z;
 }
 
@@ -226,6 +245,7 @@ int Engine::alloc(std::string& err) {
   size_t total = 0;
   n_k_ = n_kb_ = n_grad_ = 0;
   pc_tiles_ = 0;
+  guide_w_ = 0;
   maxW_small_ = 0;
   max_iter_ = 0;
   std::vector<int> offs_k(np + 1, 0), offs_kb(np + 1, 0), offs_grad(np + 1, 0), offs_chunk(np + 1, 0);
@@ -233,6 +253,7 @@ int Engine::alloc(std::string& err) {
     const auto& s = specs_[p];
     const int nt = (s.W + kTileW - 1) / kTileW;
     sz[p] = problem_sizes(s, tensor_wp_, &pc_tiles_);
+    if (s.guiding) guide_w_ = std::max(guide_w_, s.W);
     total += sz[p].total();
     offs_k[p + 1] = offs_k[p] + s.K;
     offs_kb[p + 1] = offs_kb[p] + s.K * s.B;
@@ -318,6 +339,21 @@ int Engine::alloc(std::string& err) {
     P.nnlist = nn;
     P.bk = bk;
     P.wb = wb;
+    P.guiding = s.guiding;
+    P.nnh = s.nnh;
+    P.no_guide_iter = s.no_guide_iter;
+    P.guide_cycles = s.guide_cycles;
+    if (s.guiding) {
+      double* bka = (double*)take(z.gbka);
+      int* neigh = (int*)take(z.gneigh);
+      W90G_CHECK(cudaMemcpyAsync(bka, s.bka.data(), s.bka.size() * 8, cudaMemcpyHostToDevice, stream()));
+      W90G_CHECK(cudaMemcpyAsync(neigh, s.neigh.data(), s.neigh.size() * 4, cudaMemcpyHostToDevice, stream()));
+      P.bka = bka;
+      P.neigh = neigh;
+      P.rguide = (double*)take(z.grg);
+      P.sheet = (double*)take(z.gsheet);
+      P.csheet = (double2*)take(z.gcsheet);
+    }
     P.precond = s.precond;
     P.nrpts = s.precond ? s.nrpts : 0;
     if (s.precond) {
@@ -390,6 +426,16 @@ int Engine::init_states(std::string& err) {
     W90G_CHECK(cudaMemcpyAsync(hprobs_[p].st, &h, sizeof(h), cudaMemcpyHostToDevice, st));
     const auto& s = specs_[p];
     W90G_CHECK(cudaMemsetAsync(hprobs_[p].D, 0, (size_t)s.K * s.W * s.W * 16, st));
+    if (s.guiding) {
+      // centres from the projections; sheet 0 (csheet 1) until the first wann_phases
+      const size_t n = (size_t)s.K * s.B * s.W;
+      guide_init_.assign(2 * n, 0.0);
+      for (size_t i = 0; i < n; ++i) guide_init_[2 * i] = 1.0;
+      W90G_CHECK(cudaMemcpyAsync(hprobs_[p].rguide, s.rguide0.data(), s.rguide0.size() * 8, cudaMemcpyHostToDevice, st));
+      W90G_CHECK(cudaMemsetAsync(hprobs_[p].sheet, 0, n * 8, st));
+      W90G_CHECK(cudaMemcpyAsync(hprobs_[p].csheet, guide_init_.data(), n * 16, cudaMemcpyHostToDevice, st));
+      W90G_CHECK(cudaStreamSynchronize(st));
+    }
   }
   return 0;
 }
@@ -478,6 +524,7 @@ void Engine::launch_iteration(cudaStream_t s) {
   const WorkMap wmk{d_offs_k_, np};
   const WorkMap wmkb{d_offs_kb_, np};
   const WorkMap wmg{d_offs_grad_, np};
+  if (guide_w_) k_phases<<<dim3(guide_w_, np), 256, 0, s>>>(dprobs_, 1);
   k_grad<<<n_grad_, 256, 0, s>>>(dprobs_, wmg);
   if (pc_tiles_) {
     k_precond<<<dim3(pc_tiles_, np), 256, 0, s>>>(dprobs_, 0);
@@ -502,6 +549,11 @@ int Engine::begin(std::string& err) {
   if (init_states(err)) return 1;
   const WorkMap wmkb{d_offs_kb_, np};
   if (int rc0 = prepare_tensor(st, err)) return rc0;
+  // guiding centres before the loop (src/wannierise.F90:435-443)
+  if (guide_w_) {
+    k_phases<<<dim3(guide_w_, np), 256, 0, st>>>(dprobs_, 0);
+    launches_ += 1;
+  }
   // initial spread (src/wannierise.F90:452-470)
   k_mdiag<<<n_kb_, 128, 0, st>>>(dprobs_, wmkb);
   launch_omega(st, 2);
@@ -529,7 +581,7 @@ int Engine::advance(int n, int* d_flag, std::string& err) {
   n = std::min(n, max_iter_ - launched_iters_);
   for (int i = 0; i < n; ++i) W90G_CHECK(cudaGraphLaunch(graph_exec_, st));
   // grad, search, 2 x (exp, M update, 3 spread passes), step, end (+ 2 precond)
-  launches_ += (10LL + 2 * (tensor_wp_ ? 2 : 1) + (pc_tiles_ ? 2 : 0)) * std::max(n, 0);
+  launches_ += (10LL + 2 * (tensor_wp_ ? 2 : 1) + (pc_tiles_ ? 2 : 0) + (guide_w_ ? 1 : 0)) * std::max(n, 0);
   launched_iters_ += std::max(n, 0);
   if (d_flag) {
     // every problem done (converged or out of iterations) -> *d_flag = 1
@@ -648,6 +700,7 @@ int Engine::wannierise_profiled(int max_iters, double* ms, int* cnt, std::string
   };
   int rc = 0;
   rc |= timed(kPInit, [&] {
+    if (guide_w_) k_phases<<<dim3(guide_w_, np), 256, 0, st>>>(dprobs_, 0);
     k_mdiag<<<n_kb_, 128, 0, st>>>(dprobs_, wmkb);
     launch_omega(st, 2);
     k_log_init<<<np, 128, 0, st>>>(dprobs_);
@@ -655,6 +708,7 @@ int Engine::wannierise_profiled(int max_iters, double* ms, int* cnt, std::string
   CtrlState hs;
   const int iters = std::min(max_iters, max_iter_);
   for (int it = 0; it < iters && !rc; ++it) {
+    if (guide_w_) rc |= timed(kPInit, [&] { k_phases<<<dim3(guide_w_, np), 256, 0, st>>>(dprobs_, 1); });
     rc |= timed(kPGrad, [&] { k_grad<<<n_grad_, 256, 0, st>>>(dprobs_, wmg); });
     if (pc_tiles_) {
       rc |= timed(kPPrecond, [&] { k_precond<<<dim3(pc_tiles_, np), 256, 0, st>>>(dprobs_, 0); });

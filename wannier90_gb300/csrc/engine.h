@@ -24,6 +24,11 @@ struct ProblemSpec {
   int precond = 0;
   int nrpts = 0;
   std::vector<double> pc_kr, pc_r2, pc_ndeg;
+  // guiding centres: initial centres [3][W] (Cartesian, Angstrom), b directions and
+  // their neighbour indices (kmesh_info nnh, bka, neigh)
+  int guiding = 0, no_guide_iter = 0, guide_cycles = 1, nnh = 0;
+  std::vector<double> rguide0, bka;
+  std::vector<int> neigh;
 };
 
 struct ProblemResult {
@@ -113,6 +118,7 @@ class Engine {
   double* d_unit_ = nullptr;
   int n_k_ = 0, n_kb_ = 0, n_grad_ = 0, n_chunk_ = 0;
   int pc_tiles_ = 0;     // > 0: some problem is preconditioned; CTAs per problem of k_precond
+  int guide_w_ = 0;      // > 0: some problem uses guiding centres; CTAs per problem of k_phases
   int maxW_small_ = 0;   // largest W <= 32 in the batch (shared-memory kernels)
   int tensor_wp_ = 0;    // > 0: tensor M update with padded width 8..128 for the whole batch
   bool tensor_exp_ = false;  // exp(s D) on the tensor cores (k_oz_exp)
@@ -124,6 +130,7 @@ class Engine {
   std::string layout_key_;
   long long launches_ = 0;
   int launched_iters_ = 0;
+  std::vector<double> guide_init_;   // host staging of csheet = 1
   bool async_alloc_ = false;
   double last_exp_products_ = 0.0;
 };

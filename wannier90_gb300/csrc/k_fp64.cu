@@ -91,7 +91,7 @@ __device__ void cta_gemm(double2* __restrict__ C, int ldc, const double2* __rest
 // Per-block statistics of one M(k,b): Im ln M_nn, |M_nn|^2, sum_{m!=n}|M_mn|^2.
 // (the quantities wann_omega reads, src/wannierise.F90:2034-2043, :2076-2090, :2241-2258)
 __device__ void block_stats(const double2* Mb, int ld, int W, double* ln_out, double* abs2_out,
-                            double* offd_out, double* red) {
+                            double* offd_out, double* red, const Problem* P = nullptr, size_t kb = 0) {
   double off = 0.0;
   for (int e = threadIdx.x; e < W * W; e += blockDim.x) {
     const int m = e % W, n = e / W;
@@ -100,7 +100,7 @@ __device__ void block_stats(const double2* Mb, int ld, int W, double* ln_out, do
   }
   for (int n = threadIdx.x; n < W; n += blockDim.x) {
     const double2 d = Mb[n * ld + n];
-    ln_out[n] = atan2(d.y, d.x);
+    ln_out[n] = P ? guided_ln(*P, kb * W + n, d) : atan2(d.y, d.x);
     abs2_out[n] = d.x * d.x + d.y * d.y;
   }
   const double tot = block_sum(off, red);
@@ -119,7 +119,7 @@ __global__ void k_mdiag(const Problem* __restrict__ probs, WorkMap wm) {
   const int W = P.W;
   const double2* Mb = P.M[P.st->cur] + (size_t)local * W * W;
   block_stats(Mb, W, W, P.diag_ln + (size_t)local * W, P.diag_abs2 + (size_t)local * W,
-              P.offd + local, red);
+              P.offd + local, red, &P, (size_t)local);
 }
 
 // ----------------------------------------------------------------------------
@@ -355,7 +355,7 @@ __global__ void __launch_bounds__(256) k_grad(const Problem* __restrict__ probs,
         const double2 d = Mb[(size_t)m * W + m];
         const double inv = 1.0 / (d.x * d.x + d.y * d.y);
         const double brn = bv[0] * rave[m] + bv[1] * rave[W + m] + bv[2] * rave[2 * W + m];
-        const double q = w * (atan2(d.y, d.x) + brn);
+        const double q = w * (guided_ln(P, ((size_t)k * B + b) * W + m, d) + brn);
         // conj(1/M_mm) = d * inv ;  (i/2) q conj(1/M_mm) = (i/2) q inv (d.x + i d.y)
         s_beta[t] = cmk(-0.5 * w * d.x - 0.5 * q * inv * d.y, -0.5 * w * d.y + 0.5 * q * inv * d.x);
       }
@@ -366,7 +366,7 @@ __global__ void __launch_bounds__(256) k_grad(const Problem* __restrict__ probs,
         const double2 d = Mb[(size_t)n * W + n];
         const double inv = 1.0 / (d.x * d.x + d.y * d.y);
         const double brn = bv[0] * rave[n] + bv[1] * rave[W + n] + bv[2] * rave[2 * W + n];
-        const double q = w * (atan2(d.y, d.x) + brn);
+        const double q = w * (guided_ln(P, ((size_t)k * B + b) * W + n, d) + brn);
         // 1/M_nn = (d.x - i d.y) inv ;  (i/2) q / M_nn = (q inv / 2)(d.y + i d.x)
         s_alpha[u] = cmk(0.5 * w * d.x + 0.5 * q * inv * d.y, -0.5 * w * d.y + 0.5 * q * inv * d.x);
       }
@@ -407,6 +407,127 @@ __global__ void __launch_bounds__(256) k_grad(const Problem* __restrict__ probs,
   if (t == 0) {
     P.gpart[(size_t)local * 2] = g2;
     P.gpart[(size_t)local * 2 + 1] = gd;
+  }
+}
+
+// ----------------------------------------------------------------------------
+// k_phases: wann_phases (src/wannierise.F90:1756-1976) for guiding centres.
+// mode 0: before the loop (num_no_guide_iter <= 0, centres not refitted);
+// mode 1: at the start of an iteration with iter > num_no_guide_iter and
+// mod(iter, num_guide_cycles) = 0.  One CTA per (n, problem):
+//   csum_a = sum_k M_nn(k, neigh(k,a)) over the b directions a; the centre is refitted
+//   (when irguide != 0) by least squares on the unwrapped phases (:1878-1925); then
+//   sheet(n,b,k) = b . rguide_n, csheet = exp(i sheet) and, in mode 1, rave_n on the new
+//   branch (what wann_domega recomputes, :2366-2391) for the gradient.
+// ----------------------------------------------------------------------------
+__global__ void k_phases(const Problem* __restrict__ probs, int mode) {
+  __shared__ double red[256];
+  __shared__ double s_csum[2 * 8];
+  __shared__ double s_rg[3];
+  const Problem& P = probs[blockIdx.y];
+  const CtrlState* st = P.st;
+  const int n = blockIdx.x;
+  if (!P.guiding || n >= P.W || st->done) return;
+  const int iter = st->iter + 1;
+  if (mode == 0 && P.no_guide_iter > 0) return;
+  if (mode == 1 && !(iter > P.no_guide_iter && (P.guide_cycles <= 0 || iter % P.guide_cycles == 0))) return;
+  const int W = P.W, B = P.B, K = P.K, nnh = P.nnh;
+  const double2* M = P.M[st->cur];
+  for (int a = 0; a < nnh; ++a) {
+    double cr = 0.0, ci = 0.0;
+    for (int k = threadIdx.x; k < K; k += blockDim.x) {
+      const int b = P.neigh[(size_t)k * nnh + a];
+      const double2 d = M[((size_t)k * B + b) * W * W + (size_t)n * W + n];
+      cr += d.x;
+      ci += d.y;
+    }
+    cr = block_sum(cr, red);
+    ci = block_sum(ci, red);
+    if (threadIdx.x == 0) {
+      s_csum[2 * a] = cr;
+      s_csum[2 * a + 1] = ci;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double rg[3] = {P.rguide[n], P.rguide[W + n], P.rguide[2 * W + n]};
+    double smat[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, svec[3] = {0, 0, 0};
+    for (int a = 0; a < nnh; ++a) {
+      const double* ba = P.bka + 3 * a;
+      const double2 cs = cmk(s_csum[2 * a], s_csum[2 * a + 1]);
+      double xx;
+      if (a < 3) {
+        xx = -atan2(cs.y, cs.x);
+      } else {
+        const double xx0 = ba[0] * rg[0] + ba[1] * rg[1] + ba[2] * rg[2];
+        double sn, cn;
+        sincos(xx0, &sn, &cn);
+        const double2 z = cmul(cs, cmk(cn, sn));
+        xx = xx0 - atan2(z.y, z.x);
+      }
+      for (int j = 0; j < 3; ++j) {
+        for (int i = 0; i < 3; ++i) smat[j][i] += ba[j] * ba[i];
+        svec[j] += ba[j] * xx;
+      }
+      if (a >= 2) {
+        // cofactor matrix and determinant (utility_inv3, src/utility.F90:233-262)
+        double c[3][3];
+        c[0][0] = smat[1][1] * smat[2][2] - smat[2][1] * smat[1][2];
+        c[0][1] = smat[1][2] * smat[2][0] - smat[2][2] * smat[1][0];
+        c[0][2] = smat[1][0] * smat[2][1] - smat[2][0] * smat[1][1];
+        c[1][0] = smat[2][1] * smat[0][2] - smat[0][1] * smat[2][2];
+        c[1][1] = smat[2][2] * smat[0][0] - smat[0][2] * smat[2][0];
+        c[1][2] = smat[2][0] * smat[0][1] - smat[0][0] * smat[2][1];
+        c[2][0] = smat[0][1] * smat[1][2] - smat[1][1] * smat[0][2];
+        c[2][1] = smat[0][2] * smat[1][0] - smat[1][2] * smat[0][0];
+        c[2][2] = smat[0][0] * smat[1][1] - smat[1][0] * smat[0][1];
+        const double det = smat[0][0] * c[0][0] + smat[0][1] * c[0][1] + smat[0][2] * c[0][2];
+        if (fabs(det) > 1e-6 && st->irguide != 0) {
+          for (int j = 0; j < 3; ++j) {
+            double v = 0.0;
+            for (int i = 0; i < 3; ++i) v += c[j][i] * svec[i] / det;
+            rg[j] = v;
+          }
+        }
+      }
+    }
+    for (int j = 0; j < 3; ++j) {
+      P.rguide[j * W + n] = rg[j];
+      s_rg[j] = rg[j];
+    }
+  }
+  __syncthreads();
+  const double rg0 = s_rg[0], rg1 = s_rg[1], rg2 = s_rg[2];
+  double r0 = 0.0, r1 = 0.0, r2 = 0.0;
+  for (int kb = threadIdx.x; kb < K * B; kb += blockDim.x) {
+    const double* bv = P.bk + (size_t)kb * 3;
+    const double sh = bv[0] * rg0 + bv[1] * rg1 + bv[2] * rg2;
+    double sn, cn;
+    sincos(sh, &sn, &cn);
+    const size_t kbn = (size_t)kb * W + n;
+    P.sheet[kbn] = sh;
+    P.csheet[kbn] = cmk(cn, sn);
+    if (mode == 1) {
+      const double2 d = M[(size_t)kb * W * W + (size_t)n * W + n];
+      const double2 z = cmul(cmk(cn, sn), d);
+      const double ln = atan2(z.y, z.x) - sh;
+      const double wl = P.wb[kb % B] * ln;
+      r0 += wl * bv[0];
+      r1 += wl * bv[1];
+      r2 += wl * bv[2];
+    }
+  }
+  if (mode == 1) {
+    r0 = block_sum(r0, red);
+    r1 = block_sum(r1, red);
+    r2 = block_sum(r2, red);
+    if (threadIdx.x == 0) {
+      // rave of the accepted state on the new branch, read by k_grad
+      double* rave = P.centres + (size_t)2 * 4 * W;
+      rave[n] = -r0 / K;
+      rave[W + n] = -r1 / K;
+      rave[2 * W + n] = -r2 / K;
+    }
   }
 }
 
@@ -585,6 +706,7 @@ __global__ void k_ctrl_search(const Problem* __restrict__ probs) {
   st->coefG = coefG;
   st->coefD = coefD;
   st->use_gp = use_gp;
+  if (P.guiding && iter > P.no_guide_iter && (P.guide_cycles <= 0 || iter % P.guide_cycles == 0)) st->irguide = 1;
   if (c.lfixstep) {
     st->alphamin = c.fixed_step;
     st->s_trial = c.fixed_step / fw;
@@ -843,7 +965,8 @@ __global__ void __launch_bounds__(256) k_m_update(const Problem* __restrict__ pr
     cta_gemm<false>(sM, W, sT, W, sR2, W, W);
     __syncthreads();
     for (int e = threadIdx.x; e < WW; e += blockDim.x) Mout[e] = sM[e];
-    block_stats(sM, W, W, P.diag_ln + (size_t)kb * W, P.diag_abs2 + (size_t)kb * W, P.offd + kb, red);
+    block_stats(sM, W, W, P.diag_ln + (size_t)kb * W, P.diag_abs2 + (size_t)kb * W, P.offd + kb, red, &P,
+                (size_t)kb);
   } else {
     // operands stay in global memory (L1/L2-resident); T = R(k)^H M(k,b) in tbuf
     double2* Tg = P.tbuf + (size_t)kb * WW;
@@ -851,7 +974,8 @@ __global__ void __launch_bounds__(256) k_m_update(const Problem* __restrict__ pr
     __syncthreads();
     cta_gemm<false>(Mout, W, Tg, W, Rk2, W, W);
     __syncthreads();
-    block_stats(Mout, W, W, P.diag_ln + (size_t)kb * W, P.diag_abs2 + (size_t)kb * W, P.offd + kb, red);
+    block_stats(Mout, W, W, P.diag_ln + (size_t)kb * W, P.diag_abs2 + (size_t)kb * W, P.offd + kb, red, &P,
+                (size_t)kb);
   }
 }
 
@@ -975,7 +1099,8 @@ __global__ void k_log_init(const Problem* __restrict__ probs) {
   const double* src = P.centres + (size_t)2 * 4 * W;
   for (int i = threadIdx.x; i < 4 * W; i += blockDim.x) P.log_centres[i] = src[i];
   if (threadIdx.x == 0) {
-    const CtrlState* st = P.st;
+    CtrlState* st = P.st;
+    if (P.guiding && P.no_guide_iter <= 0) st->irguide = 1;   // src/wannierise.F90:435-443
     double* lg = P.log;
     lg[0] = 0;
     lg[1] = st->wann.om_tot;

@@ -255,7 +255,7 @@ __global__ void __launch_bounds__(256, 1) k_oz_mupdate(const Problem* __restrict
         if (STEP == 2 && has_diag) {
           // diagonal statistics (once per row); the off-diagonal sum follows from the
           // invariant |M(k,b)|_F^2 = |M0(k,b)|_F^2 in the spread pass
-          P.diag_ln[(size_t)kb_out * W + rr] = atan2(dim, dre);
+          P.diag_ln[(size_t)kb_out * W + rr] = guided_ln(P, (size_t)kb_out * W + rr, make_double2(dre, dim));
           P.diag_abs2[(size_t)kb_out * W + rr] = dre * dre + dim * dim;
         }
       }

@@ -306,6 +306,46 @@ int kmesh_get(const double real_lattice[9], const double* kpt_latt, int K, int s
       }
   out.wbtot = 0.0;
   for (double w : out.wb) out.wbtot += w;
+  // b directions without inversion partners, from the first k-point (:505-528), and
+  // their index in every k-point's neighbour list (:561-577, last match wins)
+  auto compar = [](const double* a, const double* b, int& pos, int& neg) {
+    double rp = 0.0, rm = 0.0;
+    for (int i = 0; i < 3; ++i) {
+      rp += (a[i] - b[i]) * (a[i] - b[i]);
+      rm += (a[i] + b[i]) * (a[i] + b[i]);
+    }
+    pos = std::fabs(rp) < 1e-8;
+    neg = std::fabs(rm) < 1e-8;
+  };
+  out.nnh = nntot / 2;
+  out.bka.clear();
+  for (int nn = 0; nn < nntot; ++nn) {
+    const double* b = &out.bk[(size_t)nn * 3];
+    bool found = false;
+    for (size_t na = 0; na < out.bka.size() / 3; ++na) {
+      int pos, neg;
+      compar(&out.bka[na * 3], b, pos, neg);
+      if (neg) found = true;
+    }
+    if (!found) out.bka.insert(out.bka.end(), b, b + 3);
+  }
+  if ((int)out.bka.size() != 3 * out.nnh) {
+    err = "Did not find right number of bk directions";
+    return 1;
+  }
+  out.neigh.assign((size_t)K * out.nnh, -1);
+  for (int k = 0; k < K; ++k)
+    for (int na = 0; na < out.nnh; ++na) {
+      for (int nn = 0; nn < nntot; ++nn) {
+        int pos, neg;
+        compar(&out.bka[(size_t)na * 3], &out.bk[((size_t)k * nntot + nn) * 3], pos, neg);
+        if (pos) out.neigh[(size_t)k * out.nnh + na] = nn;
+      }
+      if (out.neigh[(size_t)k * out.nnh + na] < 0) {
+        err = "kmesh_get: failed to find neighbours for this kpoint";
+        return 1;
+      }
+    }
   return 0;
 }
 

@@ -14,6 +14,9 @@ struct KmeshInfo {
   std::vector<double> wb;      // [b]
   std::vector<double> bk;      // [k][b][3], Cartesian 1/Angstrom
   double wbtot = 0.0;
+  int nnh = 0;                 // b directions without inversion partners
+  std::vector<double> bka;     // [nnh][3]
+  std::vector<int> neigh;      // [k][nnh], index into the k-point's nnlist (0-based)
 };
 
 void recip_lattice(const double a[9], double b[9], double* volume);

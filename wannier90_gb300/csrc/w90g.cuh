@@ -79,6 +79,7 @@ struct CtrlState {
   int conv_count, noise_count, lrandom, lfirst, lconverged;
   int first_pass;
   int use_gp;          // precond: the search direction starts from the preconditioned gradient
+  int irguide;         // guiding centres: 0 until the first wann_phases call
   // CG
   double gcnorm0, gcnorm1, gcfac, doda0;
   double coefG, coefD;   // D <- coefG*G + coefD*D_prev
@@ -142,6 +143,13 @@ struct Problem {
   double2* pc_gr;         // [r][W*W] gradient in real space
   double2* pc_gp;         // [k][W*W] preconditioned gradient
   double* pc_part;        // [tile] Re <Gp, G> partials of the back transform
+  // guiding centres (wann_phases, src/wannierise.F90:1756-1976); sheet == null: off
+  int guiding, nnh, no_guide_iter, guide_cycles;
+  const double* bka;      // [nnh][3] b directions
+  const int* neigh;       // [k][nnh] neighbour index of each direction
+  double* rguide;         // [3][W] guiding centres (Cartesian, Angstrom)
+  double* sheet;          // [k][b][n] branch offsets b . rguide_n
+  double2* csheet;        // [k][b][n] exp(i sheet)
 };
 
 // Work map: blockIdx.x -> (problem, local index) over a prefix sum.
@@ -151,6 +159,15 @@ struct WorkMap {
 };
 
 #ifdef __CUDACC__
+// Im ln M_nn(k,b) on the branch of the guiding centres: aimag(log(csheet*M_nn)) - sheet
+// (src/wannierise.F90:2036-2041, :2368-2374); kbn = (k*B + b)*W + n
+__device__ __forceinline__ double guided_ln(const Problem& P, size_t kbn, double2 d) {
+  if (!P.sheet) return atan2(d.y, d.x);
+  const double2 c = P.csheet[kbn];
+  const double2 z = cmul(c, d);
+  return atan2(z.y, z.x) - P.sheet[kbn];
+}
+
 __device__ __forceinline__ int locate(const WorkMap& wm, int item, int& local) {
   int lo = 0, hi = wm.nprob - 1;
   while (lo < hi) {

@@ -93,7 +93,52 @@ def win_system(path):
             opts[k] = int(_flag(kw[k]))
     if "mp_grid" in kw:
         opts["mp_grid"] = np.array([int(x) for x in re.split(r"[\s,]+", kw["mp_grid"])[:3]], dtype=np.int32)
+    for k in ("num_no_guide_iter", "num_guide_cycles", "optimisation"):
+        if k in kw:
+            opts[k] = int(kw[k].split()[0])
+    if opts.get("guiding_centres") and "projections" in blocks:
+        spin = _flag(kw.get("spinors", "f"))
+        opts["guiding_centres_frac"] = projection_sites(blocks, lattice, spin)
     return lattice, kpts, opts
+
+
+_NORB = {"s": 1, "p": 3, "d": 5, "f": 7, "sp": 2, "sp2": 3, "sp3": 4, "sp3d": 5, "sp3d2": 6,
+         "l=0": 1, "l=1": 3, "l=2": 5, "l=3": 7, "l=-1": 2, "l=-2": 3, "l=-3": 4, "l=-4": 5, "l=-5": 6}
+
+
+def projection_sites(blocks, lattice, spinors):
+    """Fractional sites of the projections in the order w90_readwrite_get_projections
+    builds them (src/readwrite.F90:3536-3960): per line, per atom of the species (or the
+    explicit site), per orbital, per spin.  Handles 'Element:orbitals' and
+    'f=x,y,z:orbitals' / 'c=x,y,z:orbitals' with orbitals separated by ';'."""
+    atoms = []
+    if "atoms_frac" in blocks:
+        atoms = [(r.split()[0], np.array([_fnum(x) for x in r.split()[1:4]])) for r in blocks["atoms_frac"]]
+    elif "atoms_cart" in blocks:
+        rows = blocks["atoms_cart"]
+        scale = 1.0
+        if rows[0].lower().startswith(("bohr", "ang")):
+            scale = BOHR_ANGSTROM if rows[0].lower().startswith("bohr") else 1.0
+            rows = rows[1:]
+        inv = np.linalg.inv(np.asarray(lattice))
+        atoms = [(r.split()[0], np.array([_fnum(x) for x in r.split()[1:4]]) * scale @ inv) for r in rows]
+    sites = []
+    for line in blocks["projections"]:
+        parts = [x.strip() for x in line.replace(" ", "").split(":")]
+        if len(parts) < 2:
+            continue
+        where, orbs = parts[0], parts[1]
+        norb = sum(_NORB[o.lower().split(",")[0]] for o in orbs.split(";") if o)
+        nspin = 2 if spinors else 1
+        if where.lower().startswith(("f=", "c=")):
+            v = np.array([_fnum(x) for x in where[2:].split(",")])
+            frac = v if where.lower().startswith("f=") else v @ np.linalg.inv(np.asarray(lattice))
+            sites += [frac] * (norb * nspin)
+        else:
+            for name, frac in atoms:
+                if name.lower() == where.lower():
+                    sites += [frac] * (norb * nspin)
+    return np.array(sites, dtype=np.float64)
 
 
 def write_win(path, lattice, kpts, mp_grid, num_wann, num_bands=None, **keywords):
