@@ -26,5 +26,5 @@ def test_cli_seed_files_to_chk(tmp_path, precision):
     np.testing.assert_allclose(chk["centres"], r.centres, atol=1e-6)
     np.testing.assert_allclose(chk["spreads"], r.spreads, atol=1e-6)
     # near the minimum the gauge is only fixed to ~sqrt(per-step roundoff): 1e-7 for the
-    # FP64 path, a few 1e-7 for the tensor path (Ozaki slicing, 2^-49 of the scales)
-    np.testing.assert_allclose(synth.to_math_u(chk["u"]), r.U, atol=1e-7 if precision == "fp64" else 2e-6)
+    # FP64 path, up to a few 1e-6 for the tensor path (M update sliced to 2^-49 of the scales)
+    np.testing.assert_allclose(synth.to_math_u(chk["u"]), r.U, atol=1e-7 if precision == "fp64" else 5e-6)

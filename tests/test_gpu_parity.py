@@ -264,9 +264,11 @@ def test_guiding_centres_golden(tensor):
     window = min(_stable_window(M0, U0, km, short, noise=1e-13 if tensor else 1e-15, rguide=rguide), 60)
     assert window >= 5
     _check_trajectory(out, r, upto=window)
+    # 1000 iterations end short of convergence (conv_window 40): Omega and the centres
+    # are tight, the split of Omega among the WFs still drifts along the trajectory
     fin = d["centres_final"]
     np.testing.assert_allclose(out["centres"].T, fin[:, :3], atol=2e-6)
-    np.testing.assert_allclose(out["spreads"], fin[:, 3], atol=5e-6)
+    np.testing.assert_allclose(out["spreads"], fin[:, 3], atol=5e-6 if not tensor else 2e-5)
     assert abs(out["omega"][3] - d["omega_final_total"][0]) < 1e-6
 
 

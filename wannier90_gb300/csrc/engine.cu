@@ -178,7 +178,8 @@ Sizes problem_sizes(const ProblemSpec& s, int wp, int* pc_tiles) {
   z.M = align_up(K * B * WW * 16);
   z.U = align_up(K * WW * 16);
   z.KWW = align_up(K * WW * 16);
-  z.work = s.W > 32 ? align_up(K * 6 * WW * 16) : 0;
+  // exp workspace: FP64 kernels for W > 32; tensor exp keeps its matrices here for W > 16
+  z.work = (s.W > 32 || (wp && s.W > 16)) ? align_up(K * 6 * WW * 16) : 0;
   z.tbuf = (s.W > 32 || wp) ? align_up(K * B * WW * 16) : 0;
   z.m0 = wp ? align_up(K * B * WW * 16) : 0;
   z.u0 = wp ? align_up(K * WW * 16) : 0;

@@ -7,15 +7,19 @@
 // per matrix from its 1-norm.  Scalar work (norms, the polynomial's linear combinations,
 // the Hermitian symmetrisation of the even powers) stays in FP64; only the products move
 // to the tensor pipe.  The exp chain (powers, Horner steps, up to ~10 squarings that
-// double any error) needs more than the M update's 7 digits: every operand is split
-// into 8 signed 7-bit digits (56 bits) and the 36 digit pairs with t+u <= 7 are kept,
-// so a product is accurate to ~2^-56 of (row scale x column scale), below FP64 GEMM
-// roundoff; the 8 diagonals are recombined exactly in 128-bit integers.
+// double any error) needs 56-bit operands: a product is accurate to ~2^-56 of
+// (row scale x column scale), below FP64 GEMM roundoff.  Two product forms:
+//   num_wann <= 64: [C_r; C_i] = [[A_r, -A_i], [A_i, A_r]] [B_r; B_i], 7 signed 8-bit
+//     digits, 28 digit pairs (oz_cmm2);
+//   num_wann = 65..128: [C_r C_i] = [A_r A_i] [[B_r, B_i], [-B_i, B_r]], 8 signed
+//     7-bit digits, 36 digit pairs (oz_cmm; K = 256 keeps 8-bit digits from being exact).
 //
-// One CTA (256 threads) per (problem, k).  A product C = A B puts the rows of A on the
-// 128 TMEM lanes; only the first WP rows are real.  To keep shared memory small, the 8
-// digit slices of A are stored WP-row blocks apart in one region: the MMA reading slice
-// t sees slices t+1.. in rows >= WP, which only feed accumulator rows nobody reads.
+// One CTA (256 threads) per (problem, k).  A product puts the rows of its A operand on
+// the 128 TMEM lanes; when fewer rows are real, the digit slices of A are stored
+// row-blocks apart in one region: the MMA reading slice t sees slices t+1.. in the rows
+// beyond, which only feed accumulator rows nobody reads.
+#include <type_traits>
+
 #include "oz.cuh"
 
 namespace w90g {
@@ -261,6 +265,241 @@ __device__ bool oz_cmm(OzCtx& cx, double2* C, const double2* A, const double2* B
   return ok;
 }
 
+// ---------------------------------------------------------------------------
+// Second product form (num_wann <= 64): C = A B through
+//     [C_r; C_i] = [[A_r, -A_i], [A_i, A_r]] [B_r; B_i]
+// i.e. 2W accumulator rows (real parts in rows 0..WP-1, imaginary parts in rows
+// WP..2WP-1), N = W columns, K = 2W; operands split into 7 signed 8-bit digits (56 bits;
+// exact BF16 values) and the 28 digit pairs with t+u <= 6 kept.  Against the first
+// form this halves N and TMEM, drops 36 pairs to 28 at the same 56-bit precision, and
+// (FP64 matrices in L2 instead of shared memory) lets two CTAs share an SM.  Exactness:
+// a diagonal holds at most 7 pairs of products <= 2^14 over K <= 128 terms, < 2^24.
+// ---------------------------------------------------------------------------
+constexpr int kS2 = 7;
+
+template <int WP>
+struct Exp2Smem {
+  static constexpr int CW = WP < 32 ? WP : 32;      // complex inner indices per K chunk
+  static constexpr int KC = 2 * CW;                 // real K per chunk
+  static constexpr int NCHK = WP / CW;              // K chunks
+  static constexpr int ROWS = 2 * WP;               // accumulator rows
+  static constexpr int N = WP < 16 ? 16 : WP;       // accumulator columns (MMA N >= 16)
+  static constexpr int A_SLICE = ROWS * KC * 2;     // bytes between the overlapped slices
+  static constexpr int A_BYTES = (kS2 - 1) * A_SLICE + kTileRows * KC * 2;
+  static constexpr int B_BYTES = N * KC * 2;        // per slice
+  static constexpr int TMEM_COLS = (kS2 * N <= 128) ? 128 : ((kS2 * N <= 256) ? 256 : 512);
+  static constexpr bool STAGED = ROWS <= 64;        // rows in TMEM subpartitions 0-1 only
+  static constexpr int STAGE_LD = N + 1;
+  static constexpr size_t STAGE_BYTES = STAGED ? (size_t)kS2 * ROWS * STAGE_LD * 4 : 0;
+  static constexpr size_t DIGIT_BYTES = (size_t)A_BYTES + (size_t)kS2 * B_BYTES;
+  static constexpr size_t REGION = DIGIT_BYTES > STAGE_BYTES ? DIGIT_BYTES : STAGE_BYTES;
+  static constexpr bool MATS_IN_SMEM = WP <= 16;
+  static constexpr size_t MAT_BYTES = (size_t)WP * WP * 16;
+  static constexpr size_t NEED = REGION + (MATS_IN_SMEM ? 6 * MAT_BYTES : 0) + 1024;
+  // never more CTAs on an SM than its 512 TMEM columns hold: request enough shared
+  // memory that (512 / TMEM_COLS + 1) CTAs cannot fit in the SM's 228 KB
+  static constexpr size_t FLOOR = 233472 / (512 / TMEM_COLS + 1) - 1024 + 16;
+  static constexpr size_t BYTES = NEED > FLOOR ? NEED : FLOOR;
+};
+
+template <int WP>
+__device__ bool oz_cmm2(OzCtx& cx, double2* C, const double2* A, const double2* B, int W) {
+  using E = Exp2Smem<WP>;
+  constexpr int CW = E::CW, KC = E::KC, N = E::N;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  for (int idx = tid; idx < 2 * WP; idx += blockDim.x) {
+    const int r = idx % WP;
+    unsigned long long mx = 0ull;
+    if (r < W) {
+      if (idx < WP) {
+        for (int l = 0; l < W; ++l) {
+          const double2 a = A[(size_t)l * W + r];
+          mx = max(mx, max(abs_bits(a.x), abs_bits(a.y)));
+        }
+      } else {
+        for (int l = 0; l < W; ++l) {
+          const double2 b = B[(size_t)r * W + l];
+          mx = max(mx, max(abs_bits(b.x), abs_bits(b.y)));
+        }
+      }
+    }
+    (idx < WP ? cx.rowexp : cx.colexp)[r] = exp_above_bits(mx);
+  }
+  __syncthreads();
+  const uint32_t idesc = idesc_bf16(N);
+  // a warp slices 4 rows x 8 consecutive K, i.e. whole 16-byte core-matrix rows
+  constexpr int kgroups = CW / 8;
+  bool ok = true;
+  for (int kc = 0; kc < E::NCHK && ok; ++kc) {
+    // ---- A_emb chunk: complex (r, l) -> rows r (re) and WP + r (im), K l (re) / CW + l (im)
+    for (int e = tid; e < WP * CW; e += blockDim.x) {
+      const int ln = e & 31, wi = e >> 5;
+      const int r = (wi / kgroups) * 4 + (ln >> 3), l = (wi % kgroups) * 8 + (ln & 7);
+      const int m = kc * CW + l;
+      double2 a = make_double2(0.0, 0.0);
+      if (r < W && m < W) a = A[(size_t)m * W + r];
+      int xr[kS2], xi[kS2];
+      const int ex = cx.rowexp[r];
+      digits7x8(scaled_int55(a.x, ex), xr);
+      digits7x8(scaled_int55(a.y, ex), xi);
+      const uint32_t o_rr = kmaj_off(r, l, KC), o_ri = kmaj_off(r, l + CW, KC);
+      const uint32_t o_ir = kmaj_off(WP + r, l, KC), o_ii = kmaj_off(WP + r, l + CW, KC);
+#pragma unroll
+      for (int t = 0; t < kS2; ++t) {
+        unsigned char* sa = cx.sA + (size_t)t * E::A_SLICE;
+        *(uint16_t*)(sa + o_rr) = int_to_bf16(xr[t]);    // row re, K re:  A_r
+        *(uint16_t*)(sa + o_ri) = int_to_bf16(-xi[t]);   // row re, K im: -A_i
+        *(uint16_t*)(sa + o_ir) = int_to_bf16(xi[t]);    // row im, K re:  A_i
+        *(uint16_t*)(sa + o_ii) = int_to_bf16(xr[t]);    // row im, K im:  A_r
+      }
+    }
+    // ---- B_emb chunk as B^T (K-major): row = output column c, K l (re) / CW + l (im)
+    for (int e = tid; e < N * CW; e += blockDim.x) {
+      const int ln = e & 31, wi = e >> 5;
+      const int c = (wi / kgroups) * 4 + (ln >> 3), l = (wi % kgroups) * 8 + (ln & 7);
+      const int mm = kc * CW + l;
+      double2 b = make_double2(0.0, 0.0);
+      if (mm < W && c < W) b = B[(size_t)c * W + mm];
+      int xr[kS2], xi[kS2];
+      const int ex = cx.colexp[c < WP ? c : 0];
+      digits7x8(scaled_int55(b.x, ex), xr);
+      digits7x8(scaled_int55(b.y, ex), xi);
+      const uint32_t o_r = kmaj_off(c, l, KC), o_i = kmaj_off(c, l + CW, KC);
+#pragma unroll
+      for (int t = 0; t < kS2; ++t) {
+        unsigned char* sb = cx.sB + (size_t)t * E::B_BYTES;
+        *(uint16_t*)(sb + o_r) = int_to_bf16(xr[t]);
+        *(uint16_t*)(sb + o_i) = int_to_bf16(xi[t]);
+      }
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      for (int t = 0; t < kS2; ++t) {
+        for (int u = 0; u + t <= kS2 - 1; ++u) {
+          const uint32_t dtm = cx.tmem + (uint32_t)((t + u) * N);
+          const uint32_t a0 = smem_u32(cx.sA + (size_t)t * E::A_SLICE);
+          const uint32_t b0 = smem_u32(cx.sB + (size_t)u * E::B_BYTES);
+          const bool first_pair = (kc == 0) && (t == 0);
+#pragma unroll
+          for (int ks = 0; ks < KC / 16; ++ks) {
+            const uint64_t ad = smem_desc(a0 + ks * 256, 128, (KC / 8) * 128);
+            const uint64_t bd = smem_desc(b0 + ks * 256, 128, (KC / 8) * 128);
+            const uint32_t acc = (first_pair && ks == 0) ? 0u : 1u;
+            asm volatile(
+                "{\n\t.reg .pred p;\n\t"
+                "setp.ne.b32 p, %4, 0;\n\t"
+                "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+                :: "r"(dtm), "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+                : "memory");
+          }
+        }
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                   :: "r"(cx.mbar) : "memory");
+    }
+    const bool ok_mine = mbar_wait(cx.mbar, cx.phase);
+    cx.phase ^= 1u;
+    if (!ok_mine) *cx.bad = 1;
+    __syncthreads();
+    ok = (*cx.bad == 0);
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  }
+  if (ok) {
+    // accumulator row `row` (part = row / WP: 0 real, 1 imaginary; rr = row % WP),
+    // column c: sum_d D_d 2^(8(6-d)) 2^(rowexp + colexp - 62)
+    auto recombine = [&](const uint32_t* dd, int stride, int row, int c) {
+      const int rr = row % WP;
+      const double v = recombine7x8(dd, stride, cx.rowexp[rr] + cx.colexp[c] - 62);
+      double* dst = (double*)(C + (size_t)c * W + rr);
+      dst[row / WP] = v;
+    };
+    const int wq = warp & 3, half = warp >> 2;
+    const uint32_t lane_base = (uint32_t)(wq * 32) << 16;
+    constexpr int NH = N / 2;   // columns per warp half
+    if (E::STAGED) {
+      uint32_t* stage = (uint32_t*)cx.sA;
+      if (wq * 32 < E::ROWS) {
+#pragma unroll 1
+        for (int j0 = half * NH; j0 < (half + 1) * NH; j0 += 4) {
+#pragma unroll
+          for (int d = 0; d < kS2; ++d) {
+            uint32_t q[4];
+            asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+                         : "=r"(q[0]), "=r"(q[1]), "=r"(q[2]), "=r"(q[3])
+                         : "r"(cx.tmem + lane_base + (uint32_t)(d * N + j0)));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            const int row = wq * 32 + lane;
+            if (row < E::ROWS) {
+              uint32_t* rp = stage + ((size_t)d * E::ROWS + row) * E::STAGE_LD + j0;
+              rp[0] = q[0];
+              rp[1] = q[1];
+              rp[2] = q[2];
+              rp[3] = q[3];
+            }
+          }
+        }
+      }
+      __syncthreads();
+      for (int e = tid; e < 2 * W * W; e += blockDim.x) {
+        const int rr = e % W, c = (e / W) % W, part = e / (W * W);
+        const int row = part * WP + rr;
+        recombine(stage + (size_t)row * E::STAGE_LD + c, E::ROWS * E::STAGE_LD, row, c);
+      }
+    } else {
+      const int row = wq * 32 + lane;   // all 128 lanes hold rows (ROWS = 128)
+      const int rr = row % WP;
+#pragma unroll 1
+      for (int j0 = half * NH; j0 < (half + 1) * NH; j0 += 4) {
+        uint32_t q[kS2][4];
+#pragma unroll
+        for (int d = 0; d < kS2; ++d)
+          asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+                       : "=r"(q[d][0]), "=r"(q[d][1]), "=r"(q[d][2]), "=r"(q[d][3])
+                       : "r"(cx.tmem + lane_base + (uint32_t)(d * N + j0)));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (rr < W) {
+#pragma unroll
+          for (int j = 0; j < 4; ++j)
+            if (j0 + j < W) recombine(&q[0][j], 4, row, j0 + j);
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  return ok;
+}
+
+// product policies of the exp kernel: first form for WP = 128, second for WP <= 64
+template <int WP>
+struct ProdV1 {
+  using E = ExpSmem<WP>;
+  static constexpr int TMEM_COLS = E::TMEM_COLS;
+  static constexpr bool MATS_IN_SMEM = E::MATS_IN_SMEM;
+  static constexpr size_t REGION = E::REGION, BYTES = E::BYTES;
+  static constexpr size_t SB_OFFSET = E::A_BYTES;
+  __device__ static bool mm(OzCtx& cx, double2* C, const double2* A, const double2* B, int W) {
+    return oz_cmm<WP>(cx, C, A, B, W);
+  }
+};
+
+template <int WP>
+struct ProdV2 {
+  using E = Exp2Smem<WP>;
+  static constexpr int TMEM_COLS = E::TMEM_COLS;
+  static constexpr bool MATS_IN_SMEM = E::MATS_IN_SMEM;
+  static constexpr size_t REGION = E::REGION, BYTES = E::BYTES;
+  static constexpr size_t SB_OFFSET = E::A_BYTES;
+  __device__ static bool mm(OzCtx& cx, double2* C, const double2* A, const double2* B, int W) {
+    return oz_cmm2<WP>(cx, C, A, B, W);
+  }
+};
+
+template <int WP>
+using ExpProd = typename std::conditional<(WP <= 64), ProdV2<WP>, ProdV1<WP>>::type;
+
 // make C exactly Hermitian (sign +1) or anti-Hermitian (sign -1) from its upper triangle,
 // as the FP64 path's structured products produce it
 __device__ void mirror(double2* C, int W, double sign) {
@@ -288,8 +527,8 @@ __device__ const double kOzInvFact[17] = {
 
 // which = 0: trial step (also forms D = coefG (G or Gp) + coefD D_prev); 1: optimal step
 template <int WP>
-__global__ void __launch_bounds__(256, 1) k_oz_exp(const Problem* __restrict__ probs, WorkMap wm, int which) {
-  using E = ExpSmem<WP>;
+__global__ void __launch_bounds__(256, 2) k_oz_exp(const Problem* __restrict__ probs, WorkMap wm, int which) {
+  using E = ExpProd<WP>;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   __shared__ __align__(8) uint64_t mbar;
@@ -336,7 +575,7 @@ __global__ void __launch_bounds__(256, 1) k_oz_exp(const Problem* __restrict__ p
     for (int e = tid; e < WW; e += blockDim.x) X[e] = cscale(Dk[e], s);
   }
   __syncthreads();
-  OzCtx cx{base, base + E::A_BYTES, tmem_slot, smem_u32(&mbar), 0u, s_rowexp, s_colexp, &s_bad};
+  OzCtx cx{base, base + E::SB_OFFSET, tmem_slot, smem_u32(&mbar), 0u, s_rowexp, s_colexp, &s_bad};
 
   // ---- degree / squarings from the 1-norm (the FP64 path's table; costs in products:
   // powers X^2, X^3 (, X^4) plus the Horner steps)
@@ -371,12 +610,12 @@ __global__ void __launch_bounds__(256, 1) k_oz_exp(const Problem* __restrict__ p
   const double sc = ldexp(1.0, -js);
   for (int e = tid; e < WW; e += blockDim.x) X[e] = cscale(X[e], sc);
   __syncthreads();
-  bool ok = oz_cmm<WP>(cx, Y2, X, X, W);
+  bool ok = E::mm(cx, Y2, X, X, W);
   if (ok) mirror(Y2, W, 1.0);
-  if (ok) ok = oz_cmm<WP>(cx, Y3, Y2, X, W);
+  if (ok) ok = E::mm(cx, Y3, Y2, X, W);
   if (ok) mirror(Y3, W, -1.0);
   if (ok && pw >= 4) {
-    ok = oz_cmm<WP>(cx, Y4, Y2, Y2, W);
+    ok = E::mm(cx, Y4, Y2, Y2, W);
     if (ok) mirror(Y4, W, 1.0);
   }
   const double2* Yp = (pw == 4) ? Y4 : Y3;
@@ -407,14 +646,14 @@ __global__ void __launch_bounds__(256, 1) k_oz_exp(const Problem* __restrict__ p
   }
   __syncthreads();
   for (q = q - 1; q >= 0 && ok; --q) {
-    ok = oz_cmm<WP>(cx, T, Yp, R, W);
+    ok = E::mm(cx, T, Yp, R, W);
     for (int e = tid; e < WW; e += blockDim.x) R[e] = cadd(T[e], blk(q, e));
     __syncthreads();
   }
   double2* a = R;
   double2* b = T;
   for (int sq = 0; sq < js && ok; ++sq) {
-    ok = oz_cmm<WP>(cx, b, a, a, W);
+    ok = E::mm(cx, b, a, a, W);
     double2* tmp = a;
     a = b;
     b = tmp;
@@ -424,7 +663,7 @@ __global__ void __launch_bounds__(256, 1) k_oz_exp(const Problem* __restrict__ p
   for (int e = tid; e < WW; e += blockDim.x) dUk[e] = a[e];
   __syncthreads();
   const int cur = st->cur;
-  if (ok) ok = oz_cmm<WP>(cx, P.U[cur ^ 1] + (size_t)k * WW, P.U[cur] + (size_t)k * WW, a, W);
+  if (ok) ok = E::mm(cx, P.U[cur ^ 1] + (size_t)k * WW, P.U[cur] + (size_t)k * WW, a, W);
   if (tid == 0) atomicAdd(&st->exp_products, best + 1.0);
   if (!ok && tid == 0) {
     st->error = 2;
@@ -439,7 +678,7 @@ __global__ void __launch_bounds__(256, 1) k_oz_exp(const Problem* __restrict__ p
 
 template <int WP>
 static cudaError_t oz_exp_launch_wp(const Problem* probs, WorkMap wm, int which, int grid, cudaStream_t s) {
-  k_oz_exp<WP><<<grid, 256, ExpSmem<WP>::BYTES, s>>>(probs, wm, which);
+  k_oz_exp<WP><<<grid, 256, ExpProd<WP>::BYTES, s>>>(probs, wm, which);
   return cudaGetLastError();
 }
 
@@ -456,7 +695,7 @@ cudaError_t oz_exp_launch(int wp, const Problem* probs, WorkMap wm, int which, i
 template <int WP>
 static cudaError_t oz_exp_attr_wp() {
   return cudaFuncSetAttribute(k_oz_exp<WP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)ExpSmem<WP>::BYTES);
+                              (int)ExpProd<WP>::BYTES);
 }
 
 cudaError_t oz_exp_set_attributes(int wp) {

@@ -4,11 +4,11 @@
 // Every complex product is computed through its real embedding
 //     [C_r C_i] = [A_r A_i] [[B_r, B_i], [-B_i, B_r]]      (K = N = 2*WP real)
 // Each operand is scaled per row (A) / per column (B) by a power of two and split into
-// S = 7 signed 7-bit digits (x_1 in [-128,128], x_t in [-64,64] for t > 1), each an exact
-// BF16 value.  For every digit pair (t,u) with t+u <= S+1 the MMA A^(t) B^(u) over the
-// K = 2*WP reduction is exact in the FP32 accumulator (every partial sum is an integer
-// below 2^22), so the pairs of one diagonal d = t+u share one TMEM accumulator.  The
-// epilogue recombines the 7 diagonals exactly in int64 and converts once to FP64.
+// S = 7 signed 7-bit digits (x_1 in [-128,128], x_t in [-64,63] for t > 1), each an exact
+// BF16 value.  For every digit pair (t,u) with t+u <= S-1 (0-based) the MMA A^(t) B^(u)
+// over the K = 2*WP reduction is exact in the FP32 accumulator (every partial sum is an
+// integer below 2^22), so the pairs of one diagonal d = t+u share one TMEM accumulator.
+// The epilogue recombines the 7 diagonals exactly in int64 and rounds once to FP64.
 // Truncation error: ~2^-49 relative to (row scale x column scale) per product term.
 // Widths up to 128 are handled by chunking K and N in 32-complex-column pieces.
 //
@@ -22,6 +22,24 @@
 #include "oz.cuh"
 
 namespace w90g {
+
+// Digit scheme: 7 signed 7-bit digits (49 bits).  (8-bit digits give 56 bits for the
+// same 28 MMAs but their wider exact recombination made the update 20% slower; the
+// update's ~2^-49 error stays far below what the line search resolves.)
+template <int WP>
+__device__ __forceinline__ void split_digits(double v, int e, int x[kS]) {
+  digits7(scaled_int(v, e), x);
+}
+
+// value of the 7 FP32 diagonal accumulators dd[0], dd[stride], ... for row / column
+// exponents summing to escale
+template <int WP>
+__device__ __forceinline__ double recombine_digits(const uint32_t* dd, int stride, int escale) {
+  long long acc = float_to_int_exact(__uint_as_float(dd[0]));
+#pragma unroll
+  for (int d = 1; d < kDiag; ++d) acc = (acc << 7) + float_to_int_exact(__uint_as_float(dd[d * stride]));
+  return int64_scaled_to_double(acc, escale - 56);
+}
 
 // STEP 1: group = k.  STEP 2: group = k'.  which: 0 trial, 1 optimal-step pass.
 template <int WP, int STEP>
@@ -93,7 +111,7 @@ __global__ void __launch_bounds__(256, 1) k_oz_mupdate(const Problem* __restrict
         else val = br;
       }
       int x[kS];
-      digits7(scaled_int(val, s_colexp[cc < WP ? cc : 0]), x);
+      split_digits<WP>(val, s_colexp[cc < WP ? cc : 0], x);
       const uint32_t off = kmaj_off(n, kk, KC);
 #pragma unroll
       for (int t = 0; t < kS; ++t) *(uint16_t*)(sB + (size_t)t * L::B_BYTES + off) = int_to_bf16(x[t]);
@@ -143,8 +161,8 @@ __global__ void __launch_bounds__(256, 1) k_oz_mupdate(const Problem* __restrict
           const double2 a = a_elem(tile * kTileRows + r, kc * CW + l);
           const int ex = s_rowexp[r];
           int xr[kS], xi[kS];
-          digits7(scaled_int(a.x, ex), xr);
-          digits7(scaled_int(a.y, ex), xi);
+          split_digits<WP>(a.x, ex, xr);
+          split_digits<WP>(a.y, ex, xi);
           const uint32_t o_re = kmaj_off(r, l, KC), o_im = kmaj_off(r, l + CW, KC);
 #pragma unroll
           for (int t = 0; t < kS; ++t) {
@@ -226,16 +244,9 @@ __global__ void __launch_bounds__(256, 1) k_oz_mupdate(const Problem* __restrict
           for (int j = 0; j < 4; ++j) {
             const int c = nc * CW + j0 + j;   // complex output column
             // S = sum_d D_d 2^(7(6-d)) by Horner in int64 (exact, |S| < 2^63)
-            long long sr = float_to_int_exact(__uint_as_float(q[0][j]));
-            long long si = float_to_int_exact(__uint_as_float(s4[0][j]));
-#pragma unroll
-            for (int d = 1; d < kDiag; ++d) {
-              sr = (sr << 7) + float_to_int_exact(__uint_as_float(q[d][j]));
-              si = (si << 7) + float_to_int_exact(__uint_as_float(s4[d][j]));
-            }
-            const int sc = erow + s_colexp[c < WP ? c : 0] - 56;   // value = S 2^(erow + ecol - 56)
-            const double re = int64_scaled_to_double(sr, sc);
-            const double im = int64_scaled_to_double(si, sc);
+            const int ecol = s_colexp[c < WP ? c : 0];
+            const double re = recombine_digits<WP>(&q[0][j], 4, erow + ecol);
+            const double im = recombine_digits<WP>(&s4[0][j], 4, erow + ecol);
             if (valid && c < W) {
               if (STEP == 1) {
                 // Z(k,b) row-major: element (j=c, n=rr) at c*W + rr

@@ -115,6 +115,34 @@ __device__ __forceinline__ void digits8(long long n, int x[8]) {
   x[0] = (int)n;
 }
 
+// 8-bit-digit form (56 bits in 7 digits): N = round(v * 2^(55 - e)), |N| <= 2^55
+__device__ __forceinline__ long long scaled_int55(double v, int e) {
+  const long long bits = __double_as_longlong(v);
+  const int be = (int)((bits >> 52) & 0x7FF);
+  if (be == 0) return 0;
+  const long long mant = (bits & 0x000FFFFFFFFFFFFFLL) | 0x0010000000000000LL;
+  // v * 2^(55-e) = mant * 2^(be - 1020 - e); the right shift is >= -2 since |v| < 2^e
+  const int sh = 1020 + e - be;
+  long long n;
+  if (sh >= 62) n = 0;
+  else if (sh > 0) n = (mant + (1LL << (sh - 1))) >> sh;
+  else n = mant << (-sh);
+  return (bits < 0) ? -n : n;
+}
+
+// 7 signed 8-bit digits of N (|N| <= 2^55): x_7..x_2 in [-128, 127], |x_1| <= 128,
+// N = sum_t x_t 2^(8(7-t)); every digit is an exact BF16 value
+__device__ __forceinline__ void digits7x8(long long n, int x[7]) {
+#pragma unroll
+  for (int t = 6; t > 0; --t) {
+    const int lo = (int)n & 255;
+    const int d = lo - ((lo & 128) << 1);
+    x[t] = d;
+    n = (n - d) >> 8;
+  }
+  x[0] = (int)n;
+}
+
 // exact integer value of an integer-valued float with |f| < 2^24
 __device__ __forceinline__ int float_to_int_exact24(float f) {
   return (fabsf(f) < 4194304.0f) ? float_to_int_exact(f) : __float2int_rn(f);
@@ -160,6 +188,19 @@ __device__ __forceinline__ double int64_scaled_to_double(long long S, int sc) {
   }
   const unsigned long long bits = sign | ((unsigned long long)(ex + 1023) << 52) | (m & 0x000FFFFFFFFFFFFFull);
   return __longlong_as_double((long long)bits);
+}
+
+// sum_d D_d 2^(8(6-d)) * 2^sc for the 7 diagonal accumulators of the 8-bit-digit scheme
+// (|D_d| < 2^24): the top four and the bottom three diagonals are combined exactly in
+// int64 (< 2^49 and < 2^41), converted exactly, and added once in FP64 (one rounding)
+__device__ __forceinline__ double recombine7x8(const uint32_t* dd, int stride, int sc) {
+  long long hi = float_to_int_exact24(__uint_as_float(dd[0]));
+#pragma unroll
+  for (int d = 1; d < 4; ++d) hi = (hi << 8) + float_to_int_exact24(__uint_as_float(dd[d * stride]));
+  long long lo = float_to_int_exact24(__uint_as_float(dd[4 * stride]));
+#pragma unroll
+  for (int d = 5; d < 7; ++d) lo = (lo << 8) + float_to_int_exact24(__uint_as_float(dd[d * stride]));
+  return int64_scaled_to_double(hi, sc + 24) + int64_scaled_to_double(lo, sc);
 }
 
 __device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t parity) {
