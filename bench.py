@@ -459,13 +459,22 @@ def run_precision(args, wl):
     d_p, rel_p, dc_p = errors(per, per_c)
     marks = [i for i in (0, 1, 2, 3, 5, 10, 20, 30, 50, 100, 150, 200) if i < len(rel_t)]
 
-    def first_over(rel, dc):
-        bad = np.nonzero((rel > 1e-8) | (dc > 1e-6))[0]
-        return int(bad[0]) if len(bad) else None
+    def first_over(rel, dc, tol_rel=1e-8, tol_c=1e-6):
+        bad = np.nonzero((rel > tol_rel) | (dc > tol_c))[0]
+        return int(bad[0]) if len(bad) else len(rel)
 
+    # stable window: iterations over which roundoff-level input noise (1e-15) moves the
+    # FP64 engine's own trajectory by less than 1e-11 relative (1e-9 A for centres)
+    window = first_over(rel_p, dc_p, 1e-11, 1e-9)
     line = {
         "metric": "per-iteration error of the tensor-core engine against the FP64 engine",
-        "value": float(rel_t[: first_over(rel_p, dc_p) or len(rel_t)].max()), "unit": "max |dOmega|/Omega in the stable window",
+        "value": float(rel_t[:window].max()) if window else 0.0,
+        "unit": "max |dOmega|/Omega over the stable window",
+        "stable_window": window,
+        "max_centre_error_A_in_window": float(dc_t[:window].max()) if window else 0.0,
+        "max_error_in_window": {"dOmega_I": float(d_t[:window, 0].max()) if window else 0.0,
+                                "dOmega_D": float(d_t[:window, 1].max()) if window else 0.0,
+                                "dOmega_OD": float(d_t[:window, 2].max()) if window else 0.0},
         "n_gpus": 1, "steps": 1, "warmup": 0, "higher_is_better": False, "dtype": "f64 (FP64 engine) / bf16-sliced (tensor)",
         "data": "synthetic (seeded tight-binding generator)",
         "config": {"workload": args.workload, "lattice": "sc a=5", "kmesh": "8^3", "nntot": B, "num_wann": W,
@@ -709,8 +718,9 @@ def main():
             "config": {"workload": args.workload, "lattice": synth.CONFIGS[wl["cfg"]]["kind"],
                        "num_kpts": K, "nntot": B, "num_wann": W, "conv_tol": wl["conv_tol"],
                        "conv_window": wl["conv_window"], "iterations_per_solve": niter,
-                       "precision": ("tensor: M(k,b) = U^H M0 U on tcgen05 BF16 MMAs with exact 7-digit "
-                                     "slicing (FP64-accurate); exp, gradient, spread on the FP64 pipe"
+                       "precision": ("tensor: M(k,b) = U^H M0 U (7x7-bit digits) and exp(sD), U dU (56-bit "
+                                     "digits) on tcgen05 BF16 MMAs with exact slicing (FP64-accurate); "
+                                     "gradient, Im ln M_nn, spread and controller on the FP64 pipe"
                                      if args.precision == "tensor" else "fp64"),
                        "l2": "inputs larger than L2 (M = %d MB)" % (bytes_m >> 20),
                        "parallelism": "replicas" if world > 1 else "single"},
