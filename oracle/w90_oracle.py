@@ -288,6 +288,281 @@ def overlap_project(M, A, nnlist):
 
 
 # ---------------------------------------------------------------------------
+# disentanglement: dis_main (src/disentangle.F90:31-284), k-point path, no site symmetry
+# ---------------------------------------------------------------------------
+@dataclass
+class DisControl:
+    """dis_control_type / dis_manifold_type defaults (src/wannier90_types.F90:125-137,
+    src/types.F90:179-199)."""
+    num_iter: int = 200
+    mix_ratio: float = 0.5
+    conv_tol: float = 1.0e-10
+    conv_window: int = 3
+    win_min: float = -1.0e300
+    win_max: float = 1.0e300
+    froz_min: float = -1.0e300
+    froz_max: float = 1.0e300
+    frozen_states: bool = False
+
+
+def _heev(h):
+    """Eigenpairs of a Hermitian matrix, ascending (the reference calls ZHPEVX 'V','A','U')."""
+    w, v, info = lapack.zheev(h, compute_v=1, lower=0)
+    if info != 0:
+        raise RuntimeError("zheev failed")
+    return w, v
+
+
+def dis_windows(eig, num_wann, dc: DisControl):
+    """dis_windows (src/disentangle.F90:851-1171): outer window [nfirstwin, +ndimwin) and
+    the frozen states inside it, per k (0-based band indices)."""
+    K, nb = eig.shape
+    out = dict(ndimwin=np.zeros(K, int), nfirstwin=np.zeros(K, int), ndimfroz=np.zeros(K, int),
+               indxfroz=[], indxnfroz=[], lfrozen=[], eigval_opt=np.zeros((K, nb)))
+    for k in range(K):
+        e = eig[k]
+        if e[0] > dc.win_max or e[-1] < dc.win_min:
+            raise RuntimeError("dis_windows: The outer energy window contains no eigenvalues")
+        imin = -1
+        imax = -1
+        for i in range(nb):
+            if imin < 0:
+                if dc.win_min <= e[i] <= dc.win_max:
+                    imin = i
+                imax = i
+            if e[i] <= dc.win_max:
+                imax = i
+        ndim = imax - imin + 1
+        if ndim < num_wann:
+            raise RuntimeError("dis_windows: Energy window contains fewer states than number of target WFs")
+        fmin, fmax = -1, -2
+        if dc.frozen_states:
+            for i in range(imin, imax + 1):
+                if fmin < 0:
+                    if dc.froz_min <= e[i] <= dc.froz_max:
+                        fmin = fmax = i - imin
+                elif e[i] <= dc.froz_max:
+                    fmax += 1
+        nf = fmax - fmin + 1 if fmin >= 0 else 0
+        if nf > num_wann:
+            raise RuntimeError("dis_windows: More states in the frozen window than target WFs")
+        froz = list(range(fmin, fmin + nf)) if nf else []
+        lfr = np.zeros(ndim, bool)
+        lfr[froz] = True
+        out["ndimwin"][k], out["nfirstwin"][k], out["ndimfroz"][k] = ndim, imin, nf
+        out["indxfroz"].append(np.array(froz, int))
+        out["indxnfroz"].append(np.array([j for j in range(ndim) if not lfr[j]], int))
+        out["lfrozen"].append(lfr)
+        out["eigval_opt"][k, :ndim] = e[imin:imin + ndim]
+    return out
+
+
+def dis_project(A, win, num_wann):
+    """dis_project (src/disentangle.F90:1173-1429): U_opt = Z V^dagger from the SVD of the
+    windowed projections; returns (U_opt [K][nb][W], A_win [K][nb][W]), rows past ndimwin 0."""
+    K, nb, W = A.shape
+    Uo = np.zeros((K, nb, W), dtype=np.complex128)
+    Aw = np.zeros((K, nb, W), dtype=np.complex128)
+    for k in range(K):
+        n, f = win["ndimwin"][k], win["nfirstwin"][k]
+        a = A[k, f:f + n, :]
+        z, sv, vh, info = lapack.zgesvd(a, full_matrices=1, compute_uv=1)[:4]
+        if info != 0:
+            raise RuntimeError("dis_project: problem in ZGESVD 1")
+        Uo[k, :n] = z[:, :W] @ vh
+        Aw[k, :n] = (z[:, :W] * sv[None, :W]) @ vh
+        chk = Uo[k, :n].conj().T @ Uo[k, :n]
+        if np.max(np.abs(chk - np.eye(W))) > EPS5:
+            raise RuntimeError("dis_project: Error in unitarity of initial U in dis_project")
+    return Uo, Aw
+
+
+def dis_proj_froz(Uo, win, num_wann):
+    """dis_proj_froz (src/disentangle.F90:1431-1891): keep the frozen states and complete
+    them with the leading eigenvectors of Q P Q (P the projector on the projected
+    subspace, Q on the non-frozen states), with the reference's zero-eigenvalue fix."""
+    K = Uo.shape[0]
+    W = num_wann
+    Uo = Uo.copy()
+    for k in range(K):
+        n, nf = win["ndimwin"][k], win["ndimfroz"][k]
+        lfr = win["lfrozen"][k]
+        if W > nf:
+            u = Uo[k, :n]
+            P = u @ u.conj().T
+            q = (~lfr).astype(np.float64)
+            QPQ = q[:, None] * P * q[None, :]
+            w, cz = _heev(QPQ)
+            il = n - (W - nf)                      # 0-based first of the leading ones
+            tops = list(range(n - 1, il - 1, -1))
+            nzero = sum(1 for j in tops if w[j] < EPS8)
+            goods = len(tops) - nzero
+            if nzero > 0:
+                vmap = [j for j in range(n - 1, n - 1 - goods, -1)]
+                for _ in range(nzero):
+                    for v in range(n - 1, -1, -1):
+                        if v in vmap:
+                            continue
+                        take = all(abs(np.vdot(Uo[k, :n, m], cz[:, v])) <= EPS8 for m in range(nf))
+                        if take:
+                            vmap.append(v)
+                            break
+                if len(vmap) < W - nf:
+                    raise RuntimeError("dis_proj_froz: Ortho-fix failed to find enough vectors")
+                for c, v in enumerate(vmap[:W - nf]):
+                    Uo[k, :n, nf + c] = cz[:, v]
+            else:
+                for c in range(W - nf):
+                    Uo[k, :n, nf + c] = cz[:, il + c]
+        if nf > 0:
+            for l in range(nf):
+                Uo[k, :, l] = 0.0
+                Uo[k, win["indxfroz"][k][l], l] = 1.0
+    return Uo
+
+
+def slim_m(Mraw, win, nnlist):
+    """internal_slim_m (src/disentangle.F90:453-529): M restricted to the windows,
+    Mw[k,b][:ndimwin(k), :ndimwin(k+b)] (rest zero)."""
+    K, B, nb, _ = Mraw.shape
+    Mw = np.zeros_like(Mraw)
+    for k in range(K):
+        f1, n1 = win["nfirstwin"][k], win["ndimwin"][k]
+        for b in range(B):
+            k2 = nnlist[k, b]
+            f2, n2 = win["nfirstwin"][k2], win["ndimwin"][k2]
+            Mw[k, b, :n1, :n2] = Mraw[k, b, f1:f1 + n1, f2:f2 + n2]
+    return Mw
+
+
+def _zmatrix(Mw, Uo, win, km, k):
+    """internal_zmatrix (src/disentangle.F90:2922-2988) on the non-frozen states of k."""
+    nf_idx = win["indxnfroz"][k]
+    Z = np.zeros((len(nf_idx), len(nf_idx)), dtype=np.complex128)
+    for b in range(km["nntot"]):
+        k2 = km["nnlist"][k, b]
+        cbw = Mw[k, b] @ Uo[k2]                     # (nb, W)
+        c = cbw[nf_idx]
+        Z += km["wb"][b] * (c @ c.conj().T)
+    return Z
+
+
+def _omega_i_k(Mw, Uo, km, k, W, rows=None):
+    """sum_b w_b |U(k)^dag M(k,b) U(k+b)|^2 restricted to the first `rows` rows."""
+    tot = 0.0
+    for b in range(km["nntot"]):
+        k2 = km["nnlist"][k, b]
+        cww = Uo[k].conj().T @ Mw[k, b] @ Uo[k2]
+        if rows is not None:
+            cww = cww[:rows]
+        tot += km["wb"][b] * float((cww.real ** 2 + cww.imag ** 2).sum())
+    return tot
+
+
+@dataclass
+class DisRecord:
+    iter: int
+    omega_i_prev: float   # womegai1 (from the eigenvalues)
+    omega_i: float        # womegai (from the overlaps)
+    delta: float
+
+
+def dis_extract(Mw, Uo, win, km, num_wann, dc: DisControl):
+    """dis_extract (src/disentangle.F90:1893-2864): iterative minimisation of Omega_I
+    with Z-matrix mixing; then the subspace Hamiltonian is diagonalised to fix U_opt's
+    gauge.  Returns (U_opt, Omega_I, records, converged)."""
+    K = Mw.shape[0]
+    W = num_wann
+    Uo = Uo.copy()
+    nf = win["ndimfroz"]
+    zin = [None] * K
+    zout = [None] * K
+    history = np.zeros(dc.conv_window)
+    recs = []
+    converged = False
+    womegai = 0.0
+    for it in range(1, dc.num_iter + 1):
+        if it == 1:
+            for k in range(K):
+                if W > nf[k]:
+                    zin[k] = _zmatrix(Mw, Uo, win, km, k)
+        else:
+            for k in range(K):
+                if W > nf[k]:
+                    zin[k] = dc.mix_ratio * zout[k] + (1.0 - dc.mix_ratio) * zin[k]
+                    zin[k] = np.triu(zin[k]) + np.triu(zin[k], 1).conj().T
+        womegai1 = 0.0
+        Unew = Uo.copy()
+        for k in range(K):
+            wk = W * km["wbtot"]
+            if nf[k] > 0:
+                wk -= _omega_i_k(Mw, Uo, km, k, W, rows=nf[k])
+            if W > nf[k]:
+                w, cz = _heev(zin[k])
+                n = win["ndimwin"][k]
+                m = nf[k]
+                for j in range(n - W, n - nf[k]):
+                    wk -= w[j]
+                    Unew[k, :, m] = 0.0
+                    Unew[k, win["indxnfroz"][k], m] = cz[:, j]
+                    m += 1
+            womegai1 += wk
+        Uo = Unew
+        womegai1 /= K
+        womegai = sum(W * km["wbtot"] - _omega_i_k(Mw, Uo, km, k, W) for k in range(K)) / K
+        delta = womegai1 / womegai - 1.0
+        recs.append(DisRecord(it, womegai1, womegai, delta))
+        for k in range(K):
+            if W > nf[k]:
+                zout[k] = _zmatrix(Mw, Uo, win, km, k)
+        # internal_test_convergence (:2866-2920)
+        if it <= dc.conv_window:
+            history[it - 1] = delta
+        else:
+            history = np.concatenate([history[1:], [delta]])
+        if it >= dc.conv_window and np.all(np.abs(history) < dc.conv_tol):
+            converged = True
+            break
+    # subspace Hamiltonian gauge (:2560-2640)
+    for k in range(K):
+        n = win["ndimwin"][k]
+        ham = Uo[k, :n].conj().T @ (win["eigval_opt"][k, :n, None] * Uo[k, :n])
+        w, cz = _heev(ham)
+        Uo[k, :n] = Uo[k, :n] @ cz
+    return Uo, womegai, recs, converged
+
+
+def dis_main(Mraw, A, eig, km, num_wann, dc: DisControl):
+    """The disentanglement step of the library (w90_disentangle,
+    src/library_interface.F90:362-420): dis_main plus setup_m_loc.  Mraw[k,b,nb,nb],
+    A[k,nb,W], eig[k,nb].  Returns (U0[K,W,W], M0[K,B,W,W], U_opt[K,nb,W], Omega_I, records)
+    with M0 = U0^dag U_opt^dag M U_opt' U0' ready for wann_main."""
+    win = dis_windows(eig, num_wann, dc)
+    Uo, Aw = dis_project(A, win, num_wann)
+    if any(win["ndimfroz"] > 0):
+        Uo = dis_proj_froz(Uo, win, num_wann)
+    Mw = slim_m(Mraw, win, km["nnlist"])
+    Uo, omi, recs, conv = dis_extract(Mw, Uo, win, km, num_wann, dc)
+    K, B = Mraw.shape[:2]
+    W = num_wann
+    Mopt = np.empty((K, B, W, W), dtype=np.complex128)
+    for k in range(K):
+        for b in range(B):
+            Mopt[k, b] = Uo[k].conj().T @ Mw[k, b] @ Uo[km["nnlist"][k, b]]
+    # internal_find_u (:531-698): U = Z V^dagger from the SVD of U_opt^dag A
+    U = np.empty((K, W, W), dtype=np.complex128)
+    for k in range(K):
+        caa = Uo[k].conj().T @ Aw[k]
+        z, sv, vh, info = lapack.zgesvd(caa, full_matrices=1, compute_uv=1)[:4]
+        if info != 0:
+            raise RuntimeError("dis_main: problem in ZGESVD 1")
+        U[k] = z @ vh
+    # setup_m_loc (:286-370)
+    M0 = np.conj(U)[:, None].transpose(0, 1, 3, 2) @ Mopt @ U[km["nnlist"]]
+    return U, M0, Uo, omi, recs
+
+
+# ---------------------------------------------------------------------------
 # wann_omega / wann_domega  (src/wannierise.F90:1979-2284, :2287-2569)
 # ---------------------------------------------------------------------------
 @dataclass

@@ -17,6 +17,10 @@ testw90_precond_1 / _2) it stores, in one ``.npz``:
   final centres/spreads, the final Omega_I/Omega_D/Omega_OD/Omega_total and the
   b-vector/weight table.
 
+The disentanglement cases (testw90_example03 silicon, _example04 copper: num_bands >
+num_wann with outer and frozen energy windows) also store the .eig eigenvalues and every
+printed '<-- DIS' line.
+
 The guiding-centre case (testpostw90_gaas_shc: spinor GaAs, 16 isolated bands,
 guiding_centres = T) has no printed wannierise trajectory; its expected values are the
 final centres and spreads of the checkpoint shipped with that test.
@@ -225,6 +229,76 @@ def build_guiding(ref_root, out_dir):
     print("gaas_guide", nb, nk, nntot, sites.shape, spr.sum())
 
 
+DIS_CASES = {
+    "silicon_dis": ("test-suite/tests/testw90_example03", "silicon"),
+    "copper_dis": ("test-suite/tests/testw90_example04", "copper"),
+}
+
+
+def parse_eig(path, nb, nk):
+    eig = np.zeros((nk, nb))
+    for line in open(path):
+        p = line.split()
+        if len(p) >= 3:
+            eig[int(p[1]) - 1, int(p[0]) - 1] = float(p[2])
+    return eig
+
+
+def parse_dis_lines(path):
+    """Every '<-- DIS' iteration line: iter, Omega_I(i-1), Omega_I(i), delta."""
+    out = []
+    for l in open(path):
+        if l.rstrip().endswith("<-- DIS") and not l.strip().startswith(("+", "|")):
+            p = l.split()
+            out.append([int(p[0]), float(p[1]), float(p[2]), float(p[3])])
+        if "Final Omega_I" in l:
+            final = float(l.split()[2])
+    return np.array(out), final
+
+
+def build_dis(ref_root, out_dir):
+    """Disentanglement cases (num_bands > num_wann, outer and frozen windows): inputs,
+    the printed disentanglement iterations and the wannierise trajectory that follows."""
+    import bz2
+    for name, (sub, seed) in DIS_CASES.items():
+        d = os.path.join(ref_root, sub)
+        kw, real_lattice, kpts = parse_win(os.path.join(d, seed + ".win"))
+        mmn = os.path.join(d, seed + ".mmn")
+        if not os.path.exists(mmn):
+            tmp = os.path.join(out_dir, "_tmp_" + name)
+            os.makedirs(tmp, exist_ok=True)
+            with bz2.open(mmn + ".bz2", "rb") as f, open(os.path.join(tmp, seed + ".mmn"), "wb") as g:
+                g.write(f.read())
+            nb, nk, nntot, heads, blocks = parse_mmn(os.path.join(tmp, seed + ".mmn"))
+            os.remove(os.path.join(tmp, seed + ".mmn"))
+            os.rmdir(tmp)
+        else:
+            nb, nk, nntot, heads, blocks = parse_mmn(mmn)
+        A = parse_amn(os.path.join(d, seed + ".amn"))
+        eig = parse_eig(os.path.join(d, seed + ".eig"), nb, nk)
+        bench = os.path.join(d, "benchmark.out.default.inp=%s.win" % seed)
+        conv, initial, final, om, bvec = parse_benchmark(bench)
+        dis, omi_final = parse_dis_lines(bench)
+        num = lambda k, default: float(kw.get(k, str(default)).replace("d", "e").replace("D", "e"))
+        knobs = dict(num_wann=int(kw["num_wann"]), num_bands=int(kw["num_bands"]),
+                     num_iter=int(kw.get("num_iter", 100)), num_cg_steps=int(kw.get("num_cg_steps", 5)),
+                     conv_tol=num("conv_tol", 1e-10), conv_window=int(kw.get("conv_window", -1)),
+                     trial_step=num("trial_step", 2.0), search_shells=int(kw.get("search_shells", 36)),
+                     dis_num_iter=int(kw.get("dis_num_iter", 200)), dis_mix_ratio=num("dis_mix_ratio", 0.5),
+                     dis_conv_tol=num("dis_conv_tol", 1e-10), dis_conv_window=int(kw.get("dis_conv_window", 3)),
+                     dis_win_min=num("dis_win_min", -1e300), dis_win_max=num("dis_win_max", 1e300),
+                     dis_froz_min=num("dis_froz_min", -1e300), dis_froz_max=num("dis_froz_max", 1e300),
+                     frozen_states=int("dis_froz_max" in kw))
+        np.savez_compressed(
+            os.path.join(out_dir, name + ".npz"),
+            real_lattice=real_lattice, kpt_latt=kpts, mp_grid=np.array([int(x) for x in kw["mp_grid"].split()[:3]]),
+            num_bands=nb, num_kpts=nk, nntot=nntot, mmn_heads=heads, mmn_blocks=blocks, amn=A, eig=eig,
+            knobs=np.array([knobs[k] for k in sorted(knobs)], dtype=np.float64), knob_names=np.array(sorted(knobs)),
+            dis=dis, omega_i_final=np.array([omi_final]), conv=conv, centres_final=final,
+            omega_final=np.array([om["om_i"], om["om_d"], om["om_od"], om["om_tot"]]), bvec_table=bvec)
+        print(name, nb, nk, nntot, dis.shape, omi_final, conv.shape, om)
+
+
 def build(ref_root, out_dir):
     for name, (sub, seed) in CASES.items():
         d = os.path.join(ref_root, sub)
@@ -259,3 +333,4 @@ if __name__ == "__main__":
     root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     build(root, os.path.dirname(os.path.abspath(__file__)))
     build_guiding(root, os.path.dirname(os.path.abspath(__file__)))
+    build_dis(root, os.path.dirname(os.path.abspath(__file__)))

@@ -57,3 +57,17 @@ def guiding(d):
                         trial_step=float(kn["trial_step"]), guiding_centres=True,
                         num_no_guide_iter=int(kn["num_no_guide_iter"]), num_guide_cycles=int(kn["num_guide_cycles"]))
     return ctl, (d["proj_site_frac"] @ d["real_lattice"]).T
+
+
+DIS_CASES = ["silicon_dis", "copper_dis"]
+
+
+def dis_control(d):
+    """DisControl of a disentanglement case."""
+    from oracle import w90_oracle as O
+    kn = d["knobs"]
+    return O.DisControl(num_iter=int(kn["dis_num_iter"]), mix_ratio=float(kn["dis_mix_ratio"]),
+                        conv_tol=float(kn["dis_conv_tol"]), conv_window=int(kn["dis_conv_window"]),
+                        win_min=float(kn["dis_win_min"]), win_max=float(kn["dis_win_max"]),
+                        froz_min=float(kn["dis_froz_min"]), froz_max=float(kn["dis_froz_max"]),
+                        frozen_states=bool(kn["frozen_states"]))

@@ -54,3 +54,27 @@ def test_oracle_guiding_centres_reach_reference_checkpoint():
     np.testing.assert_allclose(r.centres.T, fin[:, :3], atol=2e-6)
     np.testing.assert_allclose(r.spreads, fin[:, 3], atol=5e-6)
     assert abs(r.spread.om_tot - d["omega_final_total"][0]) < 1e-6
+
+
+@pytest.mark.parametrize("name", G.DIS_CASES)
+def test_oracle_disentanglement_reproduces_reference(name):
+    """testw90_example03 (silicon) / _example04 (copper): 12 bands, 8 / 7 WFs, outer and
+    frozen windows.  Every printed '<-- DIS' line (Omega_I before and after the step, 8
+    decimals), the final Omega_I, and the wannierise trajectory that follows."""
+    d = G.load(name)
+    kn = d["knobs"]
+    km = O.kmesh_get(d["real_lattice"], d["kpt_latt"], int(kn["search_shells"]))
+    M = G.assemble_m(d, km["nnlist"], km["nncell"])
+    U0, M0, Uo, omi, recs = O.dis_main(M, d["amn"], d["eig"], km, int(kn["num_wann"]), G.dis_control(d))
+    assert len(recs) == len(d["dis"])
+    for r, (it, prev, cur, delta) in zip(recs, d["dis"]):
+        assert r.iter == int(it)
+        assert abs(r.omega_i_prev - prev) < 1e-8 and abs(r.omega_i - cur) < 1e-8
+    assert abs(omi - d["omega_i_final"][0]) < 1e-8
+    r = O.wann_main(M0, U0, km, G.control(d))
+    rec = {0: r.initial}
+    rec.update({it.iter: it for it in r.iters})
+    for it, delta, rms, spread in d["conv"]:
+        assert abs(rec[int(it)].spread.om_tot - spread) < 2e-10
+    np.testing.assert_allclose(r.centres.T, d["centres_final"][:, :3], atol=1.01e-6)
+    np.testing.assert_allclose([r.spread.om_i, r.spread.om_tot], d["omega_final"][[0, 3]], atol=1.01e-9)
