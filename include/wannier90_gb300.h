@@ -64,6 +64,17 @@ void cset_u_opt(void* handle, double* u_opt);
  * on exit u holds the final U and m is rotated in place to the final gauge. */
 void cwannierise(void* handle, int* ierr);
 
+/* ---- disentanglement: src/c_interface.F90:27-36 (cdisentangle -> w90_disentangle ->
+ *      dis_main + setup_m_loc, src/library_interface.F90:362-420; prototype
+ *      src/wannier90.hh:22) ---------------------------------------------------------------
+ * On entry m holds the raw overlaps (nb x nb blocks), u_opt the projections A (nb x nw)
+ * and eigval the band energies; the dis_* keywords of cinput_setopt set the windows and
+ * the Omega_I iteration.  On exit u_opt holds the optimal subspace (outer-window rows,
+ * from the first), u the internal_find_u rotation (nw x nw), and the top-left nw x nw of
+ * every m block U^dagger U_opt^dagger M U_opt(k+b) U(k+b) -- the input of cwannierise,
+ * which then reads and writes those sub-blocks.  Needs nw <= nb <= 64. */
+void cdisentangle(void* handle, int* ierr);
+
 /* ---- getters: src/c_interface.F90:129-177 ------------------------------------------ */
 void cget_nn(void* handle, int* nntot);
 void cget_nnkp(void* handle, int* nnkp);
@@ -91,6 +102,12 @@ const char* w90g_last_error(void* handle);
  *    device timestamp ns, 0) for iter = 0 (initial state) .. niter.
  * Returns the number of rows written (<= max_rows). */
 int w90g_get_log(void* handle, double* rows, int max_rows);
+/* Disentanglement record of the last cdisentangle: rows of 5 doubles
+ *   (iter, Omega_I(i-1), Omega_I(i), delta (frac.), seconds) -- the "<-- DIS" lines of
+ *   dis_extract (src/disentangle.F90:2480-2490).  Returns the rows written. */
+int w90g_get_dis_log(void* handle, double* rows, int max_rows);
+/* (final Omega_I = omega%invariant, converged 0/1, iterations) of the last cdisentangle */
+void w90g_get_dis_info(void* handle, double* info3);
 /* centres/spreads per iteration: rows of 4*num_wann doubles (x[W], y[W], z[W], spread[W]) */
 int w90g_get_log_centres(void* handle, double* rows, int max_rows);
 /* Same as cwannierise / cproject_overlap but m and u are DEVICE pointers (CUDA memory of
@@ -188,6 +205,7 @@ inline void cset_option(void* blob, std::string key, double x) { cset_option_flo
 inline void cset_option(void* blob, std::string key, double* x, int i1, int i2) {
   cset_option_floatxy(blob, key.c_str(), x, i1, i2);
 }
+inline void cdisentangle(void* blob, int& ierr) { cdisentangle(blob, &ierr); }
 inline void cwannierise(void* blob, int& ierr) { cwannierise(blob, &ierr); }
 inline void cproject_overlap(void* blob, int& ierr) { cproject_overlap(blob, &ierr); }
 inline void cget_nn(void* blob, int& n) { cget_nn(blob, &n); }

@@ -29,6 +29,7 @@ SIGNATURES = [
     ("cset_u_matrix", None, [C.c_void_p, C.c_void_p]),
     ("cset_u_opt", None, [C.c_void_p, C.c_void_p]),
     ("cwannierise", None, [C.c_void_p, _c_int_p]),
+    ("cdisentangle", None, [C.c_void_p, _c_int_p]),
     ("cget_nn", None, [C.c_void_p, _c_int_p]),
     ("cget_nnkp", None, [C.c_void_p, _c_int_p]),
     ("cget_centres", None, [C.c_void_p, _c_double_p]),
@@ -39,6 +40,8 @@ SIGNATURES = [
     ("w90g_last_error", C.c_char_p, [C.c_void_p]),
     ("w90g_get_log", C.c_int, [C.c_void_p, _c_double_p, C.c_int]),
     ("w90g_get_log_centres", C.c_int, [C.c_void_p, _c_double_p, C.c_int]),
+    ("w90g_get_dis_log", C.c_int, [C.c_void_p, _c_double_p, C.c_int]),
+    ("w90g_get_dis_info", None, [C.c_void_p, _c_double_p]),
     ("w90g_wannierise_device", None, [C.c_void_p, C.c_void_p, C.c_void_p, _c_int_p]),
     ("w90g_project_overlap_device", None, [C.c_void_p, C.c_void_p, C.c_void_p, _c_int_p]),
     ("w90g_set_stream", None, [C.c_void_p, C.c_void_p]),

@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "../../include/wannier90_gb300.h"
+#include "dis.h"
 #include "engine.h"
 #include "kmesh.h"
 
@@ -68,6 +69,12 @@ struct Handle {
   double* u_matrix = nullptr;
   double* u_opt = nullptr;
   double* eigval = nullptr;
+  // disentanglement (dis_main + setup_m_loc, src/library_interface.F90:362-420)
+  w90g::DisControl dis_ctl;
+  bool have_disentangled = false;
+  double omega_invariant = 0.0;
+  int dis_converged = 0;
+  std::vector<double> dis_log;
   // results
   bool have_result = false;
   double omega[4] = {0, 0, 0, 0};
@@ -236,6 +243,11 @@ int build_spec(Handle* h, ProblemSpec& s) {
   return 0;
 }
 
+// leading dimension of the caller's M blocks for Engine::load/store: m_matrix_local is
+// (num_bands, num_bands, nntot, num_kpts) and wann_main works on the top-left
+// num_wann x num_wann of each block (src/wannierise.F90:1742-1746); 0 = packed
+int mld(const Handle* h) { return h->num_bands > h->num_wann ? h->num_bands : 0; }
+
 Engine* engine(Handle* h) {
   if (!h->eng) h->eng.reset(new Engine());
   h->eng->set_stream(h->stream);
@@ -246,7 +258,9 @@ int do_project(Handle* h, double* m, double* u, cudaMemcpyKind in, cudaMemcpyKin
   if (!h->setup_complete) return fail(h, 1, "cinput_setopt must be called before cproject_overlap");
   if (!m) return fail(h, 1, "m_matrix_local not set for projovlp call");
   if (!u) return fail(h, 1, "u_matrix not set for projovlp call");
-  if (h->num_bands != h->num_wann) return fail(h, 5, "cproject_overlap: disentanglement (num_bands > num_wann) is not supported by the GPU engine");
+  // w90_project_overlap projects only when no disentanglement ran (src/library_interface.F90:449-459)
+  if (h->have_disentangled) return 0;
+  if (h->num_bands != h->num_wann) return fail(h, 5, "cproject_overlap: num_bands > num_wann needs cdisentangle first");
   ProblemSpec s;
   build_spec(h, s);
   std::string err;
@@ -282,15 +296,15 @@ int do_wannierise(Handle* h, double* m, double* u, cudaMemcpyKind in, cudaMemcpy
   if (!h->setup_complete) return fail(h, 1, "cinput_setopt must be called before cwannierise");
   if (!m) return fail(h, 1, "m_matrix_local not set for wannierise");
   if (!u) return fail(h, 1, "u_matrix not set for wannierise");
-  if (h->num_bands != h->num_wann) return fail(h, 5, "wannierise: disentanglement (num_bands > num_wann) is not supported by the GPU engine");
+  const int ldm = mld(h);
   ProblemSpec s;
   build_spec(h, s);
   std::string err;
   Engine* e = engine(h);
   int rc = e->setup({s}, err);
-  if (!rc) rc = e->load(0, m, u, in, err);
+  if (!rc) rc = e->load(0, m, u, in, err, ldm);
   if (!rc) rc = e->wannierise(err);
-  if (!rc) rc = e->store(0, m, u, out, err);
+  if (!rc) rc = e->store(0, m, u, out, err, ldm);
   if (rc) return fail(h, rc, err);
   return apply_result(h, e->result(0), true);
 }
@@ -363,7 +377,7 @@ struct Server {
     j.eng->set_stream(streams[j.slot]);
     j.eng->set_async_alloc(true);
     int rc = j.eng->setup({j.spec}, err);
-    if (!rc) rc = j.eng->load(0, j.d_m, j.d_u, cudaMemcpyDeviceToDevice, err);
+    if (!rc) rc = j.eng->load(0, j.d_m, j.d_u, cudaMemcpyDeviceToDevice, err, mld(j.h));
     if (!rc) rc = j.eng->begin(err);
     j.t_admit = now();
     if (rc) j.h->last_error = err;
@@ -389,7 +403,7 @@ struct Server {
   void complete(ServeJob& j) {
     std::string err;
     int rc = j.eng->finish(err);
-    if (!rc) rc = j.eng->store(0, j.d_m, j.d_u, cudaMemcpyDeviceToDevice, err);
+    if (!rc) rc = j.eng->store(0, j.d_m, j.d_u, cudaMemcpyDeviceToDevice, err, mld(j.h));
     int ierr = rc ? fail(j.h, rc, err) : apply_result(j.h, j.eng->result(0), false);
     iters_done += j.eng->result(0).niter;
     j.eng.reset();   // arena freed stream-ordered on the slot's stream
@@ -526,6 +540,10 @@ void cinput_setopt(void* hv, const char* seedname, int* ierr, int comm) {
     return;
   }
   h->num_bands = get_num(h, "num_bands", v) ? (int)v : h->num_wann;
+  if (h->num_bands < h->num_wann) {
+    *ierr = fail(h, 5, "Error: num_bands must be greater than or equal to num_wann");
+    return;
+  }
   auto kit = h->opts.find("kpoints");
   if (kit == h->opts.end() || kit->second.cols != 3) {
     *ierr = fail(h, 5, "Error: Did not find the kpoint information in the input file");
@@ -632,6 +650,54 @@ void cinput_setopt(void* hv, const char* seedname, int* ierr, int comm) {
         h->rguide0[(size_t)j * W + n] = x;
       }
   }
+  // disentanglement keywords (src/readwrite.F90:651-682, src/wannier90_readwrite.F90:824-854)
+  {
+    w90g::DisControl d;
+    if (get_num(h, "dis_win_min", v)) d.win_min = v;
+    if (get_num(h, "dis_win_max", v)) d.win_max = v;
+    if (d.win_max < d.win_min) {
+      *ierr = fail(h, 5, "Error: w90_readwrite_read_dis_manifold: check disentanglement windows (win_max < win_min !)");
+      return;
+    }
+    const bool fmax = get_num(h, "dis_froz_max", v);
+    if (fmax) {
+      d.froz_max = v;
+      d.frozen_states = true;
+    }
+    const bool fmin = get_num(h, "dis_froz_min", v);
+    if (fmin) d.froz_min = v;
+    if (fmin && !fmax) {
+      *ierr = fail(h, 5, "Error: w90_readwrite_read_dis_manifold: found dis_froz_min but not dis_froz_max");
+      return;
+    }
+    if (d.froz_max < d.froz_min) {
+      *ierr = fail(h, 5, "Error: w90_readwrite_read_dis_manifold: check disentanglement frozen windows");
+      return;
+    }
+    if (get_num(h, "dis_num_iter", v)) d.num_iter = (int)v;
+    if (d.num_iter < 0) {
+      *ierr = fail(h, 5, "Error: dis_num_iter must be positive");
+      return;
+    }
+    if (get_num(h, "dis_mix_ratio", v)) d.mix_ratio = v;
+    if (d.mix_ratio <= 0.0 || d.mix_ratio > 1.0) {
+      *ierr = fail(h, 5, "Error: dis_mix_ratio must be greater than 0.0 but not greater than 1.0");
+      return;
+    }
+    if (get_num(h, "dis_conv_tol", v)) d.conv_tol = v;
+    if (d.conv_tol < 0.0) {
+      *ierr = fail(h, 5, "Error: dis_conv_tol must be positive");
+      return;
+    }
+    if (get_num(h, "dis_conv_window", v)) d.conv_window = (int)v;
+    if (d.conv_window < 0) {
+      *ierr = fail(h, 5, "Error: dis_conv_window must be positive");
+      return;
+    }
+    h->dis_ctl = d;
+    h->have_disentangled = false;
+    h->dis_log.clear();
+  }
   h->precond = get_num(h, "precond", v) ? (v != 0.0) : 0;
   h->nrpts = 0;
   h->pc_kr.clear();
@@ -690,6 +756,77 @@ void cset_eigval(void* h, double* eigval) { H(h)->eigval = eigval; }
 void cset_m_local(void* h, double* m) { H(h)->m_local = m; }
 void cset_u_matrix(void* h, double* u) { H(h)->u_matrix = u; }
 void cset_u_opt(void* h, double* u) { H(h)->u_opt = u; }
+
+// w90_disentangle (src/library_interface.F90:362-420): dis_main + setup_m_loc.  Inputs:
+// m_local (num_bands, num_bands, nntot, num_kpts), u_opt = the projections
+// (num_bands, num_wann, num_kpts), eigval (num_bands, num_kpts).  Outputs: u_opt = the
+// optimal subspace (rows of the outer window, from the first), u_matrix = internal_find_u,
+// m_local's top-left num_wann x num_wann blocks = U^H U_opt^H M U_opt' U'.
+void cdisentangle(void* hv, int* ierr) {
+  Handle* h = H(hv);
+  *ierr = 0;
+  if (!h->setup_complete) {
+    *ierr = fail(h, 1, "cinput_setopt must be called before cdisentangle");
+    return;
+  }
+  if (!h->m_local) {
+    *ierr = fail(h, 1, "m_matrix_local not associated for disentangle call");
+    return;
+  }
+  if (!h->u_matrix) {
+    *ierr = fail(h, 1, "u_matrix not associated for disentangle call");
+    return;
+  }
+  if (!h->u_opt) {
+    *ierr = fail(h, 1, "u_opt not associated for disentangle call");
+    return;
+  }
+  if (!h->eigval) {
+    *ierr = fail(h, 1, "eigval not associated for disentangle call");
+    return;
+  }
+  const int nb = h->num_bands, W = h->num_wann, K = h->num_kpts, B = h->km.nntot;
+  w90g::DisSpec ds;
+  ds.nb = nb;
+  ds.W = W;
+  ds.K = K;
+  ds.B = B;
+  ds.wbtot = h->km.wbtot;
+  ds.nnlist = h->km.nnlist;
+  ds.wb = h->km.wb;
+  ds.eig = h->eigval;
+  ds.M = h->m_local;
+  ds.A = h->u_opt;
+  ds.ctl = h->dis_ctl;
+  w90g::DisResult r;
+  std::string err;
+  const int rc = w90g::dis_run(ds, r, err);
+  if (rc) {
+    *ierr = fail(h, rc, err);
+    return;
+  }
+  std::copy(r.u_opt.begin(), r.u_opt.end(), h->u_opt);
+  std::copy(r.u.begin(), r.u.end(), h->u_matrix);
+  const size_t WW2 = (size_t)W * W * 2;
+  for (size_t kb = 0; kb < (size_t)K * B; ++kb)
+    for (int j = 0; j < W; ++j)
+      std::copy(r.m.begin() + kb * WW2 + (size_t)j * W * 2, r.m.begin() + kb * WW2 + (size_t)(j + 1) * W * 2,
+                h->m_local + (kb * nb * nb + (size_t)j * nb) * 2);
+  h->omega_invariant = r.omega_invariant;
+  h->dis_converged = r.converged;
+  h->dis_log = r.log;
+  h->have_disentangled = true;
+  if (h->iprint > 0) {
+    const char* bar = "+---------------------------------------------------------------------+<-- DIS";
+    std::printf(" %s\n |  Iter     Omega_I(i-1)      Omega_I(i)      Delta (frac.)    Time   |<-- DIS\n %s\n", bar,
+                bar);
+    for (size_t i = 0; i + w90g::kDisLogStride <= r.log.size(); i += w90g::kDisLogStride)
+      std::printf("  %6d   %14.8f   %14.8f      %10.3E  %8.2f    <-- DIS\n", (int)r.log[i], r.log[i + 1], r.log[i + 2],
+                  r.log[i + 3], r.log[i + 4]);
+    std::printf("\n        Final Omega_I %14.8f (Ang^2)\n\n", r.omega_invariant);
+    std::fflush(stdout);
+  }
+}
 
 void cwannierise(void* hv, int* ierr) {
   Handle* h = H(hv);
@@ -755,6 +892,20 @@ void cget_omega(void* hv, double* omega4) {
 
 const char* w90g_last_error(void* hv) { return H(hv)->last_error.c_str(); }
 
+int w90g_get_dis_log(void* hv, double* rows, int max_rows) {
+  Handle* h = H(hv);
+  const int n = std::min(max_rows, (int)(h->dis_log.size() / w90g::kDisLogStride));
+  std::copy(h->dis_log.begin(), h->dis_log.begin() + (size_t)n * w90g::kDisLogStride, rows);
+  return n;
+}
+
+void w90g_get_dis_info(void* hv, double* info3) {
+  Handle* h = H(hv);
+  info3[0] = h->omega_invariant;
+  info3[1] = (double)h->dis_converged;
+  info3[2] = (double)(h->dis_log.size() / w90g::kDisLogStride);
+}
+
 int w90g_get_log(void* hv, double* rows, int max_rows) {
   Handle* h = H(hv);
   const int n = std::min(max_rows, (int)(h->log.size() / w90g::kLogStride));
@@ -785,7 +936,7 @@ int w90g_profile_device(void* hv, double* d_m, double* d_u, int max_iters, doubl
   std::string err;
   Engine* e = engine(h);
   int rc = e->setup({s}, err);
-  if (!rc) rc = e->load(0, d_m, d_u, cudaMemcpyDeviceToDevice, err);
+  if (!rc) rc = e->load(0, d_m, d_u, cudaMemcpyDeviceToDevice, err, mld(h));
   if (!rc) rc = e->wannierise_profiled(max_iters, ms, counts, err);
   if (rc) return fail(h, rc, err);
   return 0;
@@ -852,7 +1003,7 @@ void w90g_wannierise_batch_device(void** handles, int nprob, double** d_m, doubl
   std::vector<std::thread> threads;
   for (auto& kv : groups) {
     Group* g = &kv.second;
-    threads.emplace_back([g, d_m, d_u]() {
+    threads.emplace_back([g, d_m, d_u, handles]() {
       g->eng.reset(new Engine());
       if (cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking) != cudaSuccess) {
         g->rc = 1;
@@ -862,10 +1013,12 @@ void w90g_wannierise_batch_device(void** handles, int nprob, double** d_m, doubl
       g->eng->set_stream(g->stream);
       g->rc = g->eng->setup(g->specs, g->err);
       for (size_t j = 0; j < g->idx.size() && !g->rc; ++j)
-        g->rc = g->eng->load((int)j, d_m[g->idx[j]], d_u[g->idx[j]], cudaMemcpyDeviceToDevice, g->err);
+        g->rc = g->eng->load((int)j, d_m[g->idx[j]], d_u[g->idx[j]], cudaMemcpyDeviceToDevice, g->err,
+                             mld(H(handles[g->idx[j]])));
       if (!g->rc) g->rc = g->eng->wannierise(g->err);
       for (size_t j = 0; j < g->idx.size() && !g->rc; ++j)
-        g->rc = g->eng->store((int)j, d_m[g->idx[j]], d_u[g->idx[j]], cudaMemcpyDeviceToDevice, g->err);
+        g->rc = g->eng->store((int)j, d_m[g->idx[j]], d_u[g->idx[j]], cudaMemcpyDeviceToDevice, g->err,
+                              mld(H(handles[g->idx[j]])));
     });
   }
   for (auto& t : threads) t.join();
@@ -918,8 +1071,6 @@ int w90g_server_submit(void* server, void* handle, double* d_m, double* d_u, lon
   Handle* h = H(handle);
   if (!sv || !h) return 1;
   if (!h->setup_complete || !d_m || !d_u) return fail(h, 1, "serve: handle not set up or buffers missing");
-  if (h->num_bands != h->num_wann)
-    return fail(h, 5, "serve: disentanglement (num_bands > num_wann) is not supported by the GPU engine");
   std::unique_ptr<ServeJob> j(new ServeJob());
   j->tag = tag;
   j->h = h;

@@ -57,10 +57,11 @@ class Engine {
 
   // (Re)allocate for a batch of problems; reuses the arena when the shapes match.
   int setup(const std::vector<ProblemSpec>& specs, std::string& err);
-  // Copy M (m_matrix layout) and U into buffer 0 of problem p.
-  int load(int p, const void* M, const void* U, cudaMemcpyKind kind, std::string& err);
-  // Copy the accepted M and U of problem p out.
-  int store(int p, void* M, void* U, cudaMemcpyKind kind, std::string& err);
+  // Copy M (m_matrix layout) and U into buffer 0 of problem p.  ldm > W reads the
+  // top-left W x W of ldm x ldm blocks (m_matrix_local after disentanglement).
+  int load(int p, const void* M, const void* U, cudaMemcpyKind kind, std::string& err, int ldm = 0);
+  // Copy the accepted M and U of problem p out (into the top-left W x W for ldm > W).
+  int store(int p, void* M, void* U, cudaMemcpyKind kind, std::string& err, int ldm = 0);
   // Loewdin projection on every problem (U holds A on entry).
   int project(std::string& err);
   // wann_main on every problem; results via result().  Equivalent to begin(), advance()

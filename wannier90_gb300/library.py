@@ -3,8 +3,9 @@
 The reference exposes ``w90_library`` (src/library_interface.F90) to Python through
 f90wrap (wrap/Makefile.serial:52-71): a ``lib_common_type`` object plus module
 functions ``w90_set_option``, ``w90_input_setopt``, ``w90_get_nn``, ``w90_get_nnkp``,
-``w90_set_m_local``, ``w90_set_u_matrix``, ``w90_set_u_opt``, ``w90_project_overlap``,
-``w90_wannierise``, ``w90_get_centres``, ``w90_get_spreads``.  This module provides the
+``w90_set_m_local``, ``w90_set_u_matrix``, ``w90_set_u_opt``, ``w90_set_eigval``,
+``w90_disentangle``, ``w90_project_overlap``, ``w90_wannierise``, ``w90_get_centres``,
+``w90_get_spreads``.  This module provides the
 same names and argument meaning on top of the engine's C ABI
 (include/wannier90_gb300.h).  Arrays are NumPy arrays in Fortran order, exactly the
 reference's shapes:
@@ -159,6 +160,31 @@ def w90_project_overlap(common: LibCommon) -> int:
     ierr = C.c_int(0)
     common._L.cproject_overlap(common._h, C.byref(ierr))
     return ierr.value
+
+
+def w90_disentangle(common: LibCommon) -> int:
+    """dis_main + setup_m_loc (src/library_interface.F90:362-420) on the GPU.  Reads
+    m_local (raw overlaps), u_opt (projections) and eigval; writes u_opt (optimal
+    subspace), u_matrix (internal_find_u) and the top-left num_wann x num_wann of every
+    m_local block."""
+    ierr = C.c_int(0)
+    common._L.cdisentangle(common._h, C.byref(ierr))
+    return ierr.value
+
+
+def w90_get_dis_log(common: LibCommon, max_rows: int) -> np.ndarray:
+    """Omega_I iteration record of the last w90_disentangle: columns iter,
+    Omega_I(i-1), Omega_I(i), delta (frac.), seconds."""
+    out = np.zeros((max_rows, 5), dtype=np.float64)
+    n = common._L.w90g_get_dis_log(common._h, out.ctypes.data_as(C.POINTER(C.c_double)), max_rows)
+    return out[:n]
+
+
+def w90_get_dis_info(common: LibCommon) -> dict:
+    """Final Omega_I (omega%invariant), convergence flag and iteration count."""
+    out = np.zeros(3, dtype=np.float64)
+    common._L.w90g_get_dis_info(common._h, out.ctypes.data_as(C.POINTER(C.c_double)))
+    return {"omega_invariant": float(out[0]), "converged": bool(out[1]), "iterations": int(out[2])}
 
 
 def w90_wannierise(common: LibCommon) -> int:

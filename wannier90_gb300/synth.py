@@ -78,49 +78,105 @@ def kmesh_tables(real_lattice, kpoints, search_shells=36):
     return B, nnlist, nncell, bk
 
 
-def make_problem(kind="sc", a=5.0, mp=(4, 4, 4), num_wann=8, rmax=2, eps=0.3, seed=0,
-                 search_shells=36) -> TBProblem:
-    rng = np.random.Generator(np.random.PCG64(seed))
-    W = int(num_wann)
+def _tb_bands(rng, kind, a, mp, norb, rmax):
+    """Random tight-binding model with `norb` orbitals: lattice, k-points, orbital
+    positions, band energies E[k, m] (ascending) and eigenvectors C[k, :, m]."""
     A = lattice(kind, a)
     kp = mp_kpoints(*mp)
     K = len(kp)
-    tau_frac = rng.random((W, 3))
+    tau_frac = rng.random((norb, 3))
     tau = tau_frac @ A
     # hoppings
     rng_R = np.arange(-rmax, rmax + 1)
     Rs = np.array([[i, j, k] for i in rng_R for j in rng_R for k in rng_R], dtype=np.float64)
     nR = len(Rs)
     half = [r for r in range(nR) if tuple(Rs[r]) > (0.0, 0.0, 0.0)]
-    HR = np.zeros((nR, W, W), dtype=np.complex128)
+    HR = np.zeros((nR, norb, norb), dtype=np.complex128)
     idx = {tuple(r): i for i, r in enumerate(Rs)}
     for r in half:
-        x = (rng.standard_normal((W, W)) + 1j * rng.standard_normal((W, W))) / math.sqrt(2.0)
+        x = (rng.standard_normal((norb, norb)) + 1j * rng.standard_normal((norb, norb))) / math.sqrt(2.0)
         Rc = Rs[r] @ A
         x *= math.exp(-np.linalg.norm(Rc) / (0.7 * a))
         HR[r] = x
         HR[idx[tuple(-Rs[r])]] = x.conj().T
-    x0 = (rng.standard_normal((W, W)) + 1j * rng.standard_normal((W, W))) / math.sqrt(2.0)
+    x0 = (rng.standard_normal((norb, norb)) + 1j * rng.standard_normal((norb, norb))) / math.sqrt(2.0)
     HR[idx[(0.0, 0.0, 0.0)]] = 0.5 * (x0 + x0.conj().T)
     # Bloch Hamiltonians and eigenvectors
     ph = np.exp(2j * math.pi * (kp @ Rs.T))                      # (K, nR)
-    Hk = (ph @ HR.reshape(nR, W * W)).reshape(K, W, W)
+    Hk = (ph @ HR.reshape(nR, norb * norb)).reshape(K, norb, norb)
     Hk = 0.5 * (Hk + np.conj(np.swapaxes(Hk, 1, 2)))
-    _, Ck = np.linalg.eigh(Hk)                                     # columns = bands
-    # overlaps
+    Ek, Ck = np.linalg.eigh(Hk)                                    # columns = bands
+    return A, kp, tau, Ek, Ck
+
+
+def _tb_overlaps(A, kp, tau, Ck, search_shells):
+    """M_mn(k,b) = sum_a conj(C_am(k)) C_an(k+b) e^{-i b.tau_a} on the engine's k-mesh."""
     B, nnlist, nncell, bk = kmesh_tables(A, kp, search_shells)
-    phase = np.exp(-1j * np.einsum("kbi,ai->kba", bk, tau))        # (K,B,W)
-    Ckp = Ck[nnlist]                                               # (K,B,W,W)
+    phase = np.exp(-1j * np.einsum("kbi,ai->kba", bk, tau))        # (K,B,norb)
+    Ckp = Ck[nnlist]                                               # (K,B,norb,norb)
     M = np.conj(Ck)[:, None].transpose(0, 1, 3, 2) @ (phase[..., None] * Ckp)   # [k,b,m,n]
-    # projections
+    return B, nnlist, nncell, bk, M
+
+
+def _random_unitaries(rng, K, W, eps):
+    """exp(eps X_k), X_k seeded anti-Hermitian with N(0,1) entries."""
     Xk = rng.standard_normal((K, W, W)) + 1j * rng.standard_normal((K, W, W))
     Xk = 0.5 * (Xk - np.conj(np.swapaxes(Xk, 1, 2)))
     ev, V = np.linalg.eigh(1j * eps * Xk)                          # exp(eps X) = V e^{-i ev} V^H
-    Ek = (V * np.exp(-1j * ev)[:, None, :]) @ np.conj(np.swapaxes(V, 1, 2))
+    return (V * np.exp(-1j * ev)[:, None, :]) @ np.conj(np.swapaxes(V, 1, 2))
+
+
+def make_problem(kind="sc", a=5.0, mp=(4, 4, 4), num_wann=8, rmax=2, eps=0.3, seed=0,
+                 search_shells=36) -> TBProblem:
+    rng = np.random.Generator(np.random.PCG64(seed))
+    W = int(num_wann)
+    A, kp, tau, _, Ck = _tb_bands(rng, kind, a, mp, W, rmax)
+    K = len(kp)
+    B, nnlist, nncell, bk, M = _tb_overlaps(A, kp, tau, Ck, search_shells)
+    # projections
+    Ek = _random_unitaries(rng, K, W, eps)
     Amat = np.conj(np.swapaxes(Ck, 1, 2)) @ Ek                     # [k,m,n]
     m = np.asfortranarray(M.transpose(2, 3, 1, 0))
     af = np.asfortranarray(Amat.transpose(1, 2, 0))
     return TBProblem(A, kp, tuple(mp), W, B, nnlist, nncell, bk, m, af, tau, seed)
+
+
+@dataclass
+class EntangledProblem:
+    """Input of the disentanglement step: num_bands > num_wann bands per k-point."""
+    real_lattice: np.ndarray
+    kpoints: np.ndarray
+    mp_grid: tuple
+    num_bands: int
+    num_wann: int
+    nntot: int
+    nnlist: np.ndarray
+    nncell: np.ndarray
+    bk: np.ndarray
+    m: np.ndarray              # (nb,nb,B,K) F-order complex128, raw overlaps
+    a: np.ndarray              # (nb,W,K)    F-order complex128, projections
+    eig: np.ndarray            # (nb,K)      F-order float64, band energies (ascending)
+    tau: np.ndarray
+    seed: int
+
+
+def make_entangled_problem(kind="sc", a=5.0, mp=(4, 4, 4), num_bands=12, num_wann=8, rmax=2, eps=0.3,
+                           seed=0, search_shells=36) -> EntangledProblem:
+    """Tight-binding model with num_bands orbitals, all bands kept; the trial orbitals are
+    the first num_wann orbitals rotated by a seeded random unitary per k, so
+    A_mn(k) = sum_{a < num_wann} conj(C_am(k)) (exp(eps X_k))_an."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    nb, W = int(num_bands), int(num_wann)
+    A, kp, tau, Ek, Ck = _tb_bands(rng, kind, a, mp, nb, rmax)
+    K = len(kp)
+    B, nnlist, nncell, bk, M = _tb_overlaps(A, kp, tau, Ck, search_shells)
+    G = np.zeros((K, nb, W), dtype=np.complex128)
+    G[:, :W, :] = _random_unitaries(rng, K, W, eps)
+    Amat = np.conj(np.swapaxes(Ck, 1, 2)) @ G                      # [k,m,n]
+    return EntangledProblem(A, kp, tuple(mp), nb, W, B, nnlist, nncell, bk,
+                            np.asfortranarray(M.transpose(2, 3, 1, 0)),
+                            np.asfortranarray(Amat.transpose(1, 2, 0)),
+                            np.asfortranarray(Ek.T), tau, seed)
 
 
 # the workloads of the benchmark configurations (sizes as named in the suite)
