@@ -1,0 +1,152 @@
+"""Parity of the GPU disentanglement (cdisentangle: dis_main + setup_m_loc) with the
+oracle and with the reference's own outputs, through the C ABI.
+
+Quantities compared are the ones that do not depend on the gauge freedom of the
+eigen-solvers: the Omega_I record of every iteration, the final Omega_I, the rotated
+overlaps M0 = U^H U_opt^H M U_opt' U' (U = polar(U_opt^H A) absorbs any unitary mixing
+of U_opt's columns, so M0 and U_opt U depend only on the optimal subspace), and U_opt U.
+Tolerances: Omega_I 1e-10 relative against the oracle and 1e-8 absolute against the
+reference's printed 8 decimals; M0 and U_opt U 1e-9 absolute (the eigenvalue gaps at the
+selection cut are 1e-2 or larger, so eigenvector roundoff stays at 1e-13).
+"""
+import numpy as np
+import pytest
+
+from oracle import w90_oracle as O
+from tests import golden_cases as G
+from tests.engine_dis import entangled_windows, run_dis
+from wannier90_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _check_dis(out, recs, omi, U0, M0, Uo, rel=1e-10):
+    assert out["ierr"] == 0, out["err"]
+    log = out["dis_log"]
+    assert len(log) == len(recs), (len(log), len(recs))
+    for row, r in zip(log, recs):
+        assert int(row[0]) == r.iter
+        assert abs(row[1] - r.omega_i_prev) <= rel * abs(r.omega_i_prev), (r.iter, row[1], r.omega_i_prev)
+        assert abs(row[2] - r.omega_i) <= rel * abs(r.omega_i), (r.iter, row[2], r.omega_i)
+    assert abs(out["dis_info"]["omega_invariant"] - omi) <= rel * abs(omi)
+    np.testing.assert_allclose(out["M0"], M0, atol=1e-9)
+    np.testing.assert_allclose(out["Uopt"] @ out["U0"], Uo @ U0, atol=1e-9)
+    # U is unitary and U_opt has orthonormal columns
+    W = U0.shape[1]
+    for k in range(len(U0)):
+        np.testing.assert_allclose(out["U0"][k].conj().T @ out["U0"][k], np.eye(W), atol=1e-12)
+        np.testing.assert_allclose(out["Uopt"][k].conj().T @ out["Uopt"][k], np.eye(W), atol=1e-12)
+
+
+@pytest.mark.parametrize("tensor", [0, 1], ids=["fp64", "tensor"])
+@pytest.mark.parametrize("name", G.DIS_CASES)
+def test_disentangle_golden(name, tensor):
+    """testw90_example03 (silicon, 12 bands -> 8 WFs) and _example04 (copper, 12 -> 7):
+    outer and frozen windows; every '<-- DIS' line, the final Omega_I, then wann_main on
+    the disentangled overlaps against the printed '<-- CONV' lines and final centres."""
+    d = G.load(name)
+    kn = d["knobs"]
+    ss = int(kn["search_shells"])
+    W = int(kn["num_wann"])
+    km = O.kmesh_get(d["real_lattice"], d["kpt_latt"], ss)
+    M = G.assemble_m(d, km["nnlist"], km["nncell"])
+    dc = G.dis_control(d)
+    ctl = G.control(d)
+    out = run_dis(d["real_lattice"], d["kpt_latt"], M, d["amn"], d["eig"], W, dc, ss, wann_ctl=ctl,
+                  extra={"gpu_tensor": tensor})
+    U0, M0, Uo, omi, recs = O.dis_main(M, d["amn"], d["eig"], km, W, dc)
+    _check_dis(out, recs, omi, U0, M0, Uo)
+    # the reference's printed DIS lines (8 decimals) and final Omega_I
+    for row, (it, prev, cur, delta) in zip(out["dis_log"], d["dis"]):
+        assert int(row[0]) == int(it)
+        assert abs(row[1] - prev) < 1e-8 and abs(row[2] - cur) < 1e-8
+    assert abs(out["dis_info"]["omega_invariant"] - d["omega_i_final"][0]) < 1e-8
+    # wann_main on the top-left num_wann x num_wann blocks of m_local
+    assert out["wann_ierr"] == 0, out["wann_err"]
+    by_iter = {int(row[0]): row for row in out["log"]}
+    tol = 2e-10 if not tensor else 2e-9
+    for it, delta, rms, spread in d["conv"]:
+        assert abs(by_iter[int(it)][3] - spread) < tol + 1e-10 * spread, (int(it), by_iter[int(it)][3], spread)
+    np.testing.assert_allclose(out["centres"].T, d["centres_final"][:, :3], atol=1.01e-6)
+    np.testing.assert_allclose(out["omega"][[0, 3]], d["omega_final"][[0, 3]], atol=1.01e-9)
+    # wann_main wrote only the top-left blocks: the rest of m_local is the raw overlaps
+    nb = M.shape[2]
+    mask = np.ones((nb, nb), dtype=bool)
+    mask[:W, :W] = False
+    np.testing.assert_array_equal(out["m_after_wann"][:, :, mask], M[:, :, mask])
+    r = O.wann_main(M0, U0, km, ctl)
+    np.testing.assert_allclose(out["centres"], r.centres, atol=1e-6)
+
+
+@pytest.mark.parametrize("case", [
+    dict(kind="sc", mp=(4, 4, 4), num_bands=12, num_wann=8, frozen=True, seed=1),
+    dict(kind="fcc", mp=(4, 4, 4), num_bands=20, num_wann=16, frozen=False, seed=2),
+    dict(kind="bcc", mp=(3, 3, 3), num_bands=40, num_wann=24, frozen=True, seed=3),
+    dict(kind="sc", mp=(2, 2, 3), num_bands=64, num_wann=40, frozen=True, seed=4),
+], ids=["sc4_12to8_frozen", "fcc4_20to16_outer", "bcc3_40to24_frozen", "sc_64to40_frozen"])
+def test_disentangle_synthetic(case):
+    """Seeded entangled tight-binding problems: windows that cut bands off at the bottom
+    at some k-points (nfirstwin > 0), a varying number of window and frozen states per k,
+    and the largest band count the engine takes (64)."""
+    c = dict(case)
+    frozen = c.pop("frozen")
+    p = synth.make_entangled_problem(a=5.0, rmax=2, eps=0.3, **c)
+    eig = np.ascontiguousarray(p.eig.T)
+    W = p.num_wann
+    w = entangled_windows(eig, W)
+    dc = O.DisControl(num_iter=200, mix_ratio=0.5, conv_tol=1e-10, conv_window=3,
+                      win_min=w["win_min"], win_max=w["win_max"])
+    if frozen:
+        dc.froz_max = w["froz_max"]
+        dc.frozen_states = True
+    M = synth.to_math_m(p.m)
+    A = synth.to_math_u(p.a)
+    km = O.kmesh_get(p.real_lattice, p.kpoints, 36)
+    out = run_dis(p.real_lattice, p.kpoints, M, A, eig, W, dc)
+    U0, M0, Uo, omi, recs = O.dis_main(M, A, eig, km, W, dc)
+    _check_dis(out, recs, omi, U0, M0, Uo)
+    win = O.dis_windows(eig, W, dc)
+    assert (win["nfirstwin"] > 0).any() and (win["nfirstwin"] == 0).any()
+    if frozen:
+        assert (win["ndimfroz"] > 0).any()
+
+
+def test_disentangle_mix_and_window_options():
+    """dis_mix_ratio < 1 with a short dis_conv_window (converges at a clean crossing of
+    the tolerance: delta falls by 2% per iteration there), and dis_num_iter reached before
+    convergence (the record stops at dis_num_iter, converged = False).  Windows are set:
+    with every band kept the orbital subspace of the model gives Omega_I = 0 and delta is
+    roundoff over roundoff."""
+    p = synth.make_entangled_problem(kind="sc", mp=(3, 3, 3), num_bands=14, num_wann=9, seed=7)
+    eig = np.ascontiguousarray(p.eig.T)
+    M = synth.to_math_m(p.m)
+    A = synth.to_math_u(p.a)
+    km = O.kmesh_get(p.real_lattice, p.kpoints, 36)
+    w = entangled_windows(eig, p.num_wann)
+    win = dict(win_min=w["win_min"], win_max=w["win_max"])
+    for dc in (O.DisControl(num_iter=400, mix_ratio=0.3, conv_tol=1e-5, conv_window=2, **win),
+               O.DisControl(num_iter=4, mix_ratio=0.7, conv_tol=1e-14, conv_window=3, **win)):
+        out = run_dis(p.real_lattice, p.kpoints, M, A, eig, p.num_wann, dc)
+        U0, M0, Uo, omi, recs = O.dis_main(M, A, eig, km, p.num_wann, dc)
+        _check_dis(out, recs, omi, U0, M0, Uo)
+        assert out["dis_info"]["iterations"] == len(recs)
+        tail = recs[-dc.conv_window:]
+        conv = len(recs) >= dc.conv_window and all(abs(r.delta) < dc.conv_tol for r in tail)
+        assert out["dis_info"]["converged"] == conv
+
+
+def test_project_overlap_after_disentangle_is_noop():
+    """w90_project_overlap does nothing once disentanglement ran
+    (src/library_interface.F90:449-459)."""
+    from wannier90_gb300 import library as w90
+    p = synth.make_entangled_problem(kind="sc", mp=(2, 2, 2), num_bands=10, num_wann=6, seed=9)
+    eig = np.ascontiguousarray(p.eig.T)
+    out = run_dis(p.real_lattice, p.kpoints, synth.to_math_m(p.m), synth.to_math_u(p.a), eig, p.num_wann,
+                  O.DisControl())
+    assert out["ierr"] == 0, out["err"]
+    c = out["handle"]
+    u_before = np.array(c._keep["u"], copy=True)
+    m_before = np.array(c._keep["m"], copy=True)
+    assert w90.w90_project_overlap(c) == 0
+    np.testing.assert_array_equal(c._keep["u"], u_before)
+    np.testing.assert_array_equal(c._keep["m"], m_before)
