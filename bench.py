@@ -55,6 +55,16 @@ WORKLOADS = {
     # One step = the first `njobs` arrivals of the seeded stream, end to end.
     "serve": dict(cfg=None, conv_tol=1e-10, conv_window=5, num_iter=20000, serve=True, rate=200.0, njobs=24,
                   budget=150e9, slots=64),
+    # entangled bands: fcc a = 6 A, 8x8x8 k-mesh (512 k), nntot 8, 48 orbitals -> 32 WFs,
+    # the 16 other orbitals raised by 8 (energy units of the model) so their bands overlap
+    # the top of the target manifold; outer window ~40 of 48 bands (lowest band cut at
+    # some k), frozen window up to 17 states; dis_main (dis_num_iter 200, dis_conv_tol
+    # 1e-10, window 3, mixing 0.5) + setup_m_loc, then wann_main to convergence (1e-10 A^2
+    # over 5 iterations).  One step = the whole library run (cdisentangle + cwannierise).
+    "dis_fcc8_b48w32": dict(cfg=None, dis=True, problem=dict(kind="fcc", a=6.0, mp=(8, 8, 8), num_bands=48,
+                                                               num_wann=32, rmax=2, eps=0.3, offset=8.0),
+                            dis_num_iter=200, dis_conv_tol=1e-10, dis_conv_window=3, dis_mix_ratio=0.5,
+                            conv_tol=1e-10, conv_window=5, num_iter=20000),
 }
 
 
@@ -120,6 +130,41 @@ def _cpu_worker(args):
     r = O.wann_main(M0, U0, km, ctl, record=False)
     dt = time.perf_counter() - t
     return dt / max(r.niter, 1)
+
+
+def _cpu_dis_worker(args):
+    """Seconds per dis_extract iteration and per wann_main iteration of the oracle on one
+    core (entangled workload)."""
+    wl, iters = args
+    os.environ["OPENBLAS_NUM_THREADS"] = "1"
+    os.environ["OMP_NUM_THREADS"] = "1"
+    import numpy as np
+
+    from oracle import w90_oracle as O
+    from wannier90_gb300 import synth
+
+    p = synth.make_entangled_problem(**wl["problem"], seed=0)
+    eig = np.ascontiguousarray(p.eig.T)
+    w = synth.entangled_windows(eig, p.num_wann)
+    km = O.kmesh_get(p.real_lattice, p.kpoints)
+    M = synth.to_math_m(p.m)
+    A = synth.to_math_u(p.a)
+    dc = O.DisControl(num_iter=iters, mix_ratio=wl["dis_mix_ratio"], conv_tol=0.0, conv_window=wl["dis_conv_window"],
+                      win_min=w["win_min"], win_max=w["win_max"], froz_max=w["froz_max"], frozen_states=True)
+    t = time.perf_counter()
+    U0, M0, _, _, recs = O.dis_main(M, A, eig, km, p.num_wann, dc)
+    t_dis = (time.perf_counter() - t) / max(len(recs), 1)
+    t = time.perf_counter()
+    r = O.wann_main(M0, U0, km, O.WannControl(num_iter=iters, conv_window=-1), record=False)
+    t_wann = (time.perf_counter() - t) / max(r.niter, 1)
+    return t_dis, t_wann
+
+
+def cpu_dis_seconds(wl, iters, procs):
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(procs) as pool:
+        per = pool.map(_cpu_dis_worker, [(wl, iters)] * procs)
+    return statistics.mean(x[0] for x in per), statistics.mean(x[1] for x in per)
 
 
 def cpu_seconds_per_iteration(wl, iters, procs):
@@ -196,6 +241,8 @@ def run_reference_arm(args, wl):
     rank, _, world = _env_rank()
     if rank != 0:
         return 0
+    if wl.get("dis"):
+        return run_reference_arm_dis(args, wl)
     procs = os.cpu_count() or 1
     iters = args.cpu_iters
     spi = cpu_seconds_per_iteration(wl, iters, procs)
@@ -223,6 +270,218 @@ def run_reference_arm(args, wl):
     }
     print(json.dumps(line))
     return 0
+
+
+def run_reference_arm_dis(args, wl):
+    """CPU restatement of the entangled workload: dis_extract and wann_main iterations timed
+    on every core, solves/s extrapolated with the GPU arm's iteration counts."""
+    procs = os.cpu_count() or 1
+    n_dis, n_wann = KNOWN_ITERS[args.workload]
+    t_steps, vals = [], []
+    for _ in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        t_dis, t_wann = cpu_dis_seconds(wl, args.cpu_iters, procs)
+        t_steps.append(time.perf_counter() - t0)
+        vals.append(procs / (t_dis * n_dis + t_wann * n_wann))
+    value = statistics.mean(vals[args.warmup:])
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(t_steps[args.warmup:]),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded entangled tight-binding generator)",
+        "config": {"workload": args.workload, "note": "CPU restatement of dis_main + wann_main (NumPy/LAPACK), "
+                   "not wannier90.x: no Fortran compiler in the image"},
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": procs, "kind": "port",
+                         "sample": "%d dis_extract + %d wann_main iterations per core (1 process per core, 1 BLAS "
+                                   "thread); solves/s = cores / (s_per_dis_iter * %d + s_per_wann_iter * %d)"
+                                   % (args.cpu_iters, args.cpu_iters, n_dis, n_wann)},
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def _dis_flops(p, w):
+    """Algorithmic FP64 FLOPs of one k_dis_z launch: per (k,b) C_b = M_w(k,b) U_opt(k+b)
+    (n x W x n') and the upper triangle of C_b C_b^H over the window (n(n+1)/2 x W), per k
+    tr(U^H Z U) (n x n x W); 8 real FLOPs per complex multiply-add."""
+    import numpy as np
+    eig = np.ascontiguousarray(p.eig.T)                      # ascending per k
+    inwin = (eig >= w["win_min"]) & (eig <= w["win_max"])
+    n = inwin.sum(axis=1)                                    # window states per k
+    W = p.num_wann
+    z = 0.0
+    for k in range(len(n)):
+        for b in range(p.nntot):
+            k2 = p.nnlist[k, b]
+            z += 8.0 * (n[k] * W * n[k2] + n[k] * (n[k] + 1) / 2 * W)
+        z += 8.0 * n[k] * n[k] * W
+    return z
+
+
+def run_dis(args, wl):
+    """Entangled workload: cdisentangle + cwannierise on one problem.  value = solves/s with
+    the inputs resident in HBM (device entry points); e2e through cdisentangle /
+    cwannierise with host buffers."""
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    from wannier90_gb300 import library as w90
+    from wannier90_gb300 import synth
+
+    torch.cuda.set_device(0)
+    p = synth.make_entangled_problem(**wl["problem"], seed=0)
+    nb, W, K, B = p.num_bands, p.num_wann, len(p.kpoints), p.nntot
+    eig = np.ascontiguousarray(p.eig.T)
+    w = synth.entangled_windows(eig, W)
+    opts = dict(num_iter=wl["num_iter"], conv_tol=wl["conv_tol"], conv_window=wl["conv_window"], iprint=0,
+                gpu_tensor=1 if args.precision == "tensor" else 0, dis_num_iter=wl["dis_num_iter"],
+                dis_conv_tol=wl["dis_conv_tol"], dis_conv_window=wl["dis_conv_window"],
+                dis_mix_ratio=wl["dis_mix_ratio"], dis_win_min=w["win_min"], dis_win_max=w["win_max"],
+                dis_froz_max=w["froz_max"])
+    h = w90.setup(kpoints=p.kpoints, unit_cell_cart=p.real_lattice, num_wann=W, num_bands=nb, **opts)
+    stream = torch.cuda.Stream()
+    w90.w90_set_stream(h, stream.cuda_stream)
+    m0 = torch.from_numpy(p.m.reshape(-1, order="F").view(np.float64).copy()).cuda()
+    a0 = torch.from_numpy(p.a.reshape(-1, order="F").view(np.float64).copy()).cuda()
+    e0 = torch.from_numpy(np.ascontiguousarray(p.eig.reshape(-1, order="F"))).cuda()
+    m_w, a_w = torch.empty_like(m0), torch.empty_like(a0)
+    u_w = torch.zeros(2 * W * W * K, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    if args.profile_case > 0:
+        # one disentanglement capped at profile_case iterations, no wannierisation (ncu)
+        hp = w90.setup(kpoints=p.kpoints, unit_cell_cart=p.real_lattice, num_wann=W, num_bands=nb,
+                       **dict(opts, dis_num_iter=args.profile_case))
+        m_w.copy_(m0)
+        a_w.copy_(a0)
+        w90.check(hp, w90.w90_disentangle_device(hp, m_w.data_ptr(), a_w.data_ptr(), u_w.data_ptr(), e0.data_ptr()),
+                  "profile case")
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": args.profile_case, "workload": args.workload,
+                          "omega_invariant": w90.w90_get_dis_info(hp)["omega_invariant"]}))
+        return 0
+
+    def device_step():
+        with torch.cuda.stream(stream):
+            m_w.copy_(m0)
+            a_w.copy_(a0)
+        w90.check(h, w90.w90_disentangle_device(h, m_w.data_ptr(), a_w.data_ptr(), u_w.data_ptr(), e0.data_ptr()),
+                  "disentangle")
+        w90.check(h, w90.w90_wannierise_device(h, m_w.data_ptr(), u_w.data_ptr()), "wannierise")
+
+    for _ in range(args.warmup):
+        device_step()
+    torch.cuda.synchronize()
+    n_dis = len(w90.w90_get_dis_log(h, wl["dis_num_iter"] + 1))
+    n_wann = int(w90.w90_get_log(h, wl["num_iter"] + 1)[-1][0])
+    l0 = w90.w90_kernel_launches(h)
+    clocks = ClockSampler(0)
+    torch.cuda.synchronize()
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        device_step()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    launches = w90.w90_kernel_launches(h) - l0
+    ms_per_step = ev0.elapsed_time(ev1) / args.steps
+    value = 1e3 / ms_per_step
+    info = w90.w90_get_dis_info(h)
+    omega = w90.w90_get_omega(h)
+
+    # e2e: the library calls with host buffers (pageable NumPy arrays, as a Fortran or
+    # C++ caller passes them), copies inside the calls
+    m_h = np.empty_like(p.m)
+    a_h = np.empty_like(p.a)
+    u_h = np.zeros((W, W, K), dtype=np.complex128, order="F")
+    e_h = np.asfortranarray(p.eig)
+    w90.w90_set_m_local(h, m_h)
+    w90.w90_set_u_opt(h, a_h)
+    w90.w90_set_u_matrix(h, u_h)
+    w90.w90_set_eigval(h, e_h)
+    e2e_t = []
+    for _ in range(max(1, args.e2e_steps)):
+        m_h[...] = p.m
+        a_h[...] = p.a
+        t0 = time.perf_counter()
+        w90.check(h, w90.w90_disentangle(h), "disentangle")
+        w90.check(h, w90.w90_wannierise(h), "wannierise")
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_value = 1.0 / statistics.mean(e2e_t)
+    h2d = p.m.nbytes + p.a.nbytes + p.eig.nbytes + 2 * W * W * B * K * 16 + W * W * K * 16
+    d2h = p.a.nbytes + W * W * K * 16 + 2 * W * W * B * K * 16 + W * W * K * 16
+
+    # per-kernel device times of the disentanglement (CUDA events around every launch)
+    with torch.cuda.stream(stream):
+        m_w.copy_(m0)
+        a_w.copy_(a0)
+    torch.cuda.synchronize()
+    ierr, prof = w90.w90_profile_dis_device(h, m_w.data_ptr(), a_w.data_ptr(), u_w.data_ptr(), e0.data_ptr())
+    w90.check(h, ierr, "profile")
+    tot = sum(v[0] for v in prof.values())
+    per_kernel = {k: {"ms_total": v[0], "launches": v[1], "ms_avg": v[0] / v[1] if v[1] else None,
+                      "share": v[0] / tot if tot else None} for k, v in prof.items()}
+    # wall split of one step between the two library calls (device entry points)
+    with torch.cuda.stream(stream):
+        m_w.copy_(m0)
+        a_w.copy_(a0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    w90.check(h, w90.w90_disentangle_device(h, m_w.data_ptr(), a_w.data_ptr(), u_w.data_ptr(), e0.data_ptr()),
+              "disentangle")
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    w90.check(h, w90.w90_wannierise_device(h, m_w.data_ptr(), u_w.data_ptr()), "wannierise")
+    torch.cuda.synchronize()
+    phase_s = {"disentangle": t1 - t0, "wannierise": time.perf_counter() - t1}
+    fp64_peak = lib_fp64_peak()
+    zf = _dis_flops(p, w)
+    dom = max(per_kernel, key=lambda k: per_kernel[k]["ms_total"])
+    zavg = per_kernel["k_dis_z"]["ms_avg"]
+    achieved = zf / (zavg * 1e-3) / 1e12
+    roof = {"bound": "fp64", "kernel": "k_dis_z", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+            "frac": achieved / fp64_peak if fp64_peak > 0 else None, "traffic": None,
+            "peak_source": "FP64 FMA probe measured in this run (MEASURED_PEAKS.json has no FP64 figure)",
+            "algorithmic_flops_per_launch": zf, "dominant_dis_kernel": dom,
+            "dis_ms_total": tot, "per_kernel": per_kernel, "phase_seconds": phase_s,
+            "note": "k_dis_z is the dominant kernel of the disentanglement; the wannierisation phase "
+                    "runs the kernels of the isolated-band workloads (see fcc10_w32)"}
+    cpu = None
+    if not args.no_cpu_baseline:
+        procs = os.cpu_count() or 1
+        t_dis, t_wann = cpu_dis_seconds(wl, args.cpu_iters, procs)
+        cpu = {"value": procs / (t_dis * n_dis + t_wann * n_wann), "unit": "solves/s", "cores": procs,
+               "kind": "port",
+               "sample": "%d dis_extract + %d wann_main iterations per core on %d cores (1 process per core, "
+                         "1 BLAS thread); %.3f s/dis iter, %.3f s/wann iter; solves/s = cores / (s/dis iter * %d "
+                         "+ s/wann iter * %d)" % (args.cpu_iters, args.cpu_iters, procs, t_dis, t_wann, n_dis,
+                                                  n_wann)}
+    line = {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded entangled tight-binding generator)",
+        "config": {"workload": args.workload, "lattice": "fcc", "num_kpts": K, "nntot": B, "num_bands": nb,
+                   "num_wann": W, "dis_iterations": n_dis, "dis_converged": info["converged"],
+                   "dis_max_jacobi_sweeps": info["max_sweeps"], "offset": wl["problem"]["offset"],
+                   "omega_invariant": info["omega_invariant"], "wannierise_iterations": n_wann,
+                   "omega_total": float(omega[3]), "windows": w,
+                   "precision": "disentanglement fp64; wannierise " + args.precision,
+                   "l2": "inputs larger than L2 (M = %d MB)" % (p.m.nbytes >> 20)},
+        "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(launches) // args.steps * args.steps,
+        "roofline": roof, "cpu_baseline": cpu, "clocks": clk,
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def lib_fp64_peak():
+    from wannier90_gb300._native import lib
+    return lib().w90g_measure_fp64_peak()
 
 
 def run_batch(args, wl):
@@ -525,6 +784,8 @@ def main():
             args.assume_iters = KNOWN_ITERS.get(args.workload, 1000)
         return run_reference_arm(args, wl)
 
+    if wl.get("dis"):
+        return run_dis(args, wl)
     if wl.get("nprob"):
         return run_batch(args, wl)
     if wl.get("serve"):
@@ -738,7 +999,7 @@ def main():
 
 
 # iterations per solve of each workload as measured by the GPU arm (FP64 engine)
-KNOWN_ITERS = {"fcc10_w32": 1834, "sc4_w8": 200}
+KNOWN_ITERS = {"fcc10_w32": 1834, "sc4_w8": 200, "dis_fcc8_b48w32": (200, 3053)}
 
 if __name__ == "__main__":
     sys.exit(main())

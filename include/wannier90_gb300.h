@@ -106,8 +106,19 @@ int w90g_get_log(void* handle, double* rows, int max_rows);
  *   (iter, Omega_I(i-1), Omega_I(i), delta (frac.), seconds) -- the "<-- DIS" lines of
  *   dis_extract (src/disentangle.F90:2480-2490).  Returns the rows written. */
 int w90g_get_dis_log(void* handle, double* rows, int max_rows);
-/* (final Omega_I = omega%invariant, converged 0/1, iterations) of the last cdisentangle */
-void w90g_get_dis_info(void* handle, double* info3);
+/* (final Omega_I = omega%invariant, converged 0/1, iterations, most Jacobi sweeps of a
+ *  Z eigenproblem) of the last cdisentangle */
+void w90g_get_dis_info(void* handle, double* info4);
+/* cdisentangle on DEVICE buffers (same layouts; d_eig (nb, nk) is read back to the host
+ * for the windows).  Outputs are written back on the device; w90g_wannierise_device on
+ * the same d_m / d_u then works on the top-left nw x nw blocks. */
+void w90g_disentangle_device(void* handle, double* d_m_matrix, double* d_u_opt, double* d_u_matrix,
+                             const double* d_eigval, int* ierr);
+/* Same, timing every kernel launch with CUDA events: ms[i] / counts[i] per kernel i
+ * (names from w90g_dis_kernel_name, "" past the last kernel).  Returns ierr. */
+int w90g_profile_dis_device(void* handle, double* d_m_matrix, double* d_u_opt, double* d_u_matrix,
+                            const double* d_eigval, double* ms, int* counts);
+const char* w90g_dis_kernel_name(int i);
 /* centres/spreads per iteration: rows of 4*num_wann doubles (x[W], y[W], z[W], spread[W]) */
 int w90g_get_log_centres(void* handle, double* rows, int max_rows);
 /* Same as cwannierise / cproject_overlap but m and u are DEVICE pointers (CUDA memory of

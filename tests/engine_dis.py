@@ -4,6 +4,7 @@ import numpy as np
 
 from wannier90_gb300 import library as w90
 from wannier90_gb300 import synth
+from wannier90_gb300.synth import entangled_windows  # noqa: F401  (re-exported for the tests)
 
 
 def dis_options(dc):
@@ -63,14 +64,3 @@ def run_dis(real_lattice, kpoints, M_raw, A, eig, num_wann, dc, search_shells=36
         out["spreads"] = w90.w90_get_spreads(c, num_wann)
         out["omega"] = w90.w90_get_omega(c)
     return out
-
-
-def entangled_windows(eig, W):
-    """Outer and frozen windows for a synthetic entangled problem (eig[k, nb]): the outer
-    window drops the lowest band at some k-points (nfirstwin > 0), keeps >= W + 1 states
-    everywhere and about half of the bands above W on average; the frozen window holds at
-    most W // 2 + 1 states."""
-    nb = eig.shape[1]
-    return dict(win_min=float(eig[:, 1].min()),
-                win_max=float(max(eig[:, W].max(), np.median(eig[:, (W + nb) // 2]))),
-                froz_max=float(eig[:, W // 2].min()))

@@ -150,3 +150,44 @@ def test_project_overlap_after_disentangle_is_noop():
     assert w90.w90_project_overlap(c) == 0
     np.testing.assert_array_equal(c._keep["u"], u_before)
     np.testing.assert_array_equal(c._keep["m"], m_before)
+
+
+def test_device_entry_equals_host_entry():
+    """w90g_disentangle_device + w90g_wannierise_device on device buffers give the host
+    path's results bit for bit (same kernels, same order), and the profiled form too."""
+    import torch
+
+    from wannier90_gb300 import library as w90
+    p = synth.make_entangled_problem(kind="fcc", mp=(3, 3, 3), num_bands=16, num_wann=10, seed=11)
+    eig = np.ascontiguousarray(p.eig.T)
+    w = entangled_windows(eig, p.num_wann)
+    dc = O.DisControl(num_iter=80, win_min=w["win_min"], win_max=w["win_max"], froz_max=w["froz_max"],
+                      frozen_states=True)
+    ctl = O.WannControl(num_iter=40, conv_window=-1)
+    M = synth.to_math_m(p.m)
+    A = synth.to_math_u(p.a)
+    host = run_dis(p.real_lattice, p.kpoints, M, A, eig, p.num_wann, dc, wann_ctl=ctl)
+    assert host["ierr"] == 0 and host["wann_ierr"] == 0
+    from tests.engine_dis import dis_options
+    for profiled in (False, True):
+        c = w90.setup(kpoints=p.kpoints, unit_cell_cart=p.real_lattice, num_wann=p.num_wann, num_bands=p.num_bands,
+                      iprint=0, num_iter=40, conv_window=-1, **dis_options(dc))
+        dm = torch.from_numpy(p.m.reshape(-1, order="F").view(np.float64).copy()).cuda()
+        da = torch.from_numpy(p.a.reshape(-1, order="F").view(np.float64).copy()).cuda()
+        du = torch.zeros(2 * p.num_wann ** 2 * len(p.kpoints), dtype=torch.float64, device="cuda")
+        de = torch.from_numpy(np.ascontiguousarray(p.eig.reshape(-1, order="F"))).cuda()
+        if profiled:
+            ierr, prof = w90.w90_profile_dis_device(c, dm.data_ptr(), da.data_ptr(), du.data_ptr(), de.data_ptr())
+            assert prof["k_dis_step"][1] == len(host["dis_log"]) and prof["k_dis_rotate"][1] == 1
+            assert all(ms >= 0.0 for ms, _ in prof.values())
+        else:
+            ierr = w90.w90_disentangle_device(c, dm.data_ptr(), da.data_ptr(), du.data_ptr(), de.data_ptr())
+        assert ierr == 0, c.last_error()
+        np.testing.assert_array_equal(w90.w90_get_dis_log(c, 100)[:, :4], host["dis_log"][:, :4])
+        u = du.cpu().numpy().view(np.complex128).reshape((p.num_wann, p.num_wann, -1), order="F")
+        np.testing.assert_array_equal(synth.to_math_u(u), host["U0"])
+        assert w90.w90_wannierise_device(c, dm.data_ptr(), du.data_ptr()) == 0, c.last_error()
+        m = dm.cpu().numpy().view(np.complex128).reshape(p.m.shape, order="F")
+        np.testing.assert_array_equal(synth.to_math_m(m), host["m_after_wann"])
+        np.testing.assert_array_equal(w90.w90_get_centres(c, p.num_wann), host["centres"])
+        assert w90.w90_kernel_launches(c) > 0

@@ -75,6 +75,8 @@ struct Handle {
   double omega_invariant = 0.0;
   int dis_converged = 0;
   std::vector<double> dis_log;
+  long long dis_launches = 0;
+  int dis_max_sweeps = 0;
   // results
   bool have_result = false;
   double omega[4] = {0, 0, 0, 0};
@@ -307,6 +309,61 @@ int do_wannierise(Handle* h, double* m, double* u, cudaMemcpyKind in, cudaMemcpy
   if (!rc) rc = e->store(0, m, u, out, err, ldm);
   if (rc) return fail(h, rc, err);
   return apply_result(h, e->result(0), true);
+}
+
+// w90_disentangle (src/library_interface.F90:362-420): dis_main + setup_m_loc.  Inputs:
+// m (num_bands, num_bands, nntot, num_kpts), uopt = the projections
+// (num_bands, num_wann, num_kpts), eig (num_bands, num_kpts).  Outputs: uopt = the
+// optimal subspace (rows of the outer window, from the first), u = internal_find_u,
+// m's top-left num_wann x num_wann blocks = U^H U_opt^H M U_opt' U'.
+int do_disentangle(Handle* h, double* m, double* uopt, double* u, const double* eig, bool device, double* prof_ms,
+                   int* prof_counts) {
+  if (!h->setup_complete) return fail(h, 1, "cinput_setopt must be called before cdisentangle");
+  if (!m) return fail(h, 1, "m_matrix_local not associated for disentangle call");
+  if (!u) return fail(h, 1, "u_matrix not associated for disentangle call");
+  if (!uopt) return fail(h, 1, "u_opt not associated for disentangle call");
+  if (!eig) return fail(h, 1, "eigval not associated for disentangle call");
+  const int W = h->num_wann;
+  w90g::DisSpec ds;
+  ds.nb = h->num_bands;
+  ds.W = W;
+  ds.K = h->num_kpts;
+  ds.B = h->km.nntot;
+  ds.wbtot = h->km.wbtot;
+  ds.nnlist = h->km.nnlist;
+  ds.wb = h->km.wb;
+  ds.eig = eig;
+  ds.M = m;
+  ds.A = uopt;
+  ds.uopt_out = uopt;
+  ds.u_out = u;
+  ds.m_out = m;
+  ds.device = device;
+  ds.stream = h->stream;
+  ds.ctl = h->dis_ctl;
+  ds.prof_ms = prof_ms;
+  ds.prof_counts = prof_counts;
+  w90g::DisResult r;
+  std::string err;
+  const int rc = w90g::dis_run(ds, r, err);
+  h->dis_launches += r.launches;
+  if (rc) return fail(h, rc, err);
+  h->omega_invariant = r.omega_invariant;
+  h->dis_converged = r.converged;
+  h->dis_log = r.log;
+  h->dis_max_sweeps = r.max_sweeps;
+  h->have_disentangled = true;
+  if (h->iprint > 0) {
+    const char* bar = "+---------------------------------------------------------------------+<-- DIS";
+    std::printf(" %s\n |  Iter     Omega_I(i-1)      Omega_I(i)      Delta (frac.)    Time   |<-- DIS\n %s\n", bar,
+                bar);
+    for (size_t i = 0; i + w90g::kDisLogStride <= r.log.size(); i += w90g::kDisLogStride)
+      std::printf("  %6d   %14.8f   %14.8f      %10.3E  %8.2f    <-- DIS\n", (int)r.log[i], r.log[i + 1], r.log[i + 2],
+                  r.log[i + 3], r.log[i + 4]);
+    std::printf("\n        Final Omega_I %14.8f (Ang^2)\n\n", r.omega_invariant);
+    std::fflush(stdout);
+  }
+  return 0;
 }
 
 // ----------------------------------------------------------------------------
@@ -757,76 +814,25 @@ void cset_m_local(void* h, double* m) { H(h)->m_local = m; }
 void cset_u_matrix(void* h, double* u) { H(h)->u_matrix = u; }
 void cset_u_opt(void* h, double* u) { H(h)->u_opt = u; }
 
-// w90_disentangle (src/library_interface.F90:362-420): dis_main + setup_m_loc.  Inputs:
-// m_local (num_bands, num_bands, nntot, num_kpts), u_opt = the projections
-// (num_bands, num_wann, num_kpts), eigval (num_bands, num_kpts).  Outputs: u_opt = the
-// optimal subspace (rows of the outer window, from the first), u_matrix = internal_find_u,
-// m_local's top-left num_wann x num_wann blocks = U^H U_opt^H M U_opt' U'.
 void cdisentangle(void* hv, int* ierr) {
   Handle* h = H(hv);
-  *ierr = 0;
-  if (!h->setup_complete) {
-    *ierr = fail(h, 1, "cinput_setopt must be called before cdisentangle");
-    return;
-  }
-  if (!h->m_local) {
-    *ierr = fail(h, 1, "m_matrix_local not associated for disentangle call");
-    return;
-  }
-  if (!h->u_matrix) {
-    *ierr = fail(h, 1, "u_matrix not associated for disentangle call");
-    return;
-  }
-  if (!h->u_opt) {
-    *ierr = fail(h, 1, "u_opt not associated for disentangle call");
-    return;
-  }
-  if (!h->eigval) {
-    *ierr = fail(h, 1, "eigval not associated for disentangle call");
-    return;
-  }
-  const int nb = h->num_bands, W = h->num_wann, K = h->num_kpts, B = h->km.nntot;
-  w90g::DisSpec ds;
-  ds.nb = nb;
-  ds.W = W;
-  ds.K = K;
-  ds.B = B;
-  ds.wbtot = h->km.wbtot;
-  ds.nnlist = h->km.nnlist;
-  ds.wb = h->km.wb;
-  ds.eig = h->eigval;
-  ds.M = h->m_local;
-  ds.A = h->u_opt;
-  ds.ctl = h->dis_ctl;
-  w90g::DisResult r;
-  std::string err;
-  const int rc = w90g::dis_run(ds, r, err);
-  if (rc) {
-    *ierr = fail(h, rc, err);
-    return;
-  }
-  std::copy(r.u_opt.begin(), r.u_opt.end(), h->u_opt);
-  std::copy(r.u.begin(), r.u.end(), h->u_matrix);
-  const size_t WW2 = (size_t)W * W * 2;
-  for (size_t kb = 0; kb < (size_t)K * B; ++kb)
-    for (int j = 0; j < W; ++j)
-      std::copy(r.m.begin() + kb * WW2 + (size_t)j * W * 2, r.m.begin() + kb * WW2 + (size_t)(j + 1) * W * 2,
-                h->m_local + (kb * nb * nb + (size_t)j * nb) * 2);
-  h->omega_invariant = r.omega_invariant;
-  h->dis_converged = r.converged;
-  h->dis_log = r.log;
-  h->have_disentangled = true;
-  if (h->iprint > 0) {
-    const char* bar = "+---------------------------------------------------------------------+<-- DIS";
-    std::printf(" %s\n |  Iter     Omega_I(i-1)      Omega_I(i)      Delta (frac.)    Time   |<-- DIS\n %s\n", bar,
-                bar);
-    for (size_t i = 0; i + w90g::kDisLogStride <= r.log.size(); i += w90g::kDisLogStride)
-      std::printf("  %6d   %14.8f   %14.8f      %10.3E  %8.2f    <-- DIS\n", (int)r.log[i], r.log[i + 1], r.log[i + 2],
-                  r.log[i + 3], r.log[i + 4]);
-    std::printf("\n        Final Omega_I %14.8f (Ang^2)\n\n", r.omega_invariant);
-    std::fflush(stdout);
-  }
+  *ierr = do_disentangle(h, h->m_local, h->u_opt, h->u_matrix, h->eigval, false, nullptr, nullptr);
 }
+
+void w90g_disentangle_device(void* hv, double* d_m, double* d_uopt, double* d_u, const double* d_eig, int* ierr) {
+  *ierr = do_disentangle(H(hv), d_m, d_uopt, d_u, d_eig, true, nullptr, nullptr);
+}
+
+int w90g_profile_dis_device(void* hv, double* d_m, double* d_uopt, double* d_u, const double* d_eig, double* ms,
+                            int* counts) {
+  for (int i = 0; i < w90g::kDisKernels; ++i) {
+    ms[i] = 0.0;
+    counts[i] = 0;
+  }
+  return do_disentangle(H(hv), d_m, d_uopt, d_u, d_eig, true, ms, counts);
+}
+
+const char* w90g_dis_kernel_name(int i) { return w90g::dis_kernel_name(i); }
 
 void cwannierise(void* hv, int* ierr) {
   Handle* h = H(hv);
@@ -899,11 +905,12 @@ int w90g_get_dis_log(void* hv, double* rows, int max_rows) {
   return n;
 }
 
-void w90g_get_dis_info(void* hv, double* info3) {
+void w90g_get_dis_info(void* hv, double* info4) {
   Handle* h = H(hv);
-  info3[0] = h->omega_invariant;
-  info3[1] = (double)h->dis_converged;
-  info3[2] = (double)(h->dis_log.size() / w90g::kDisLogStride);
+  info4[0] = h->omega_invariant;
+  info4[1] = (double)h->dis_converged;
+  info4[2] = (double)(h->dis_log.size() / w90g::kDisLogStride);
+  info4[3] = (double)h->dis_max_sweeps;
 }
 
 int w90g_get_log(void* hv, double* rows, int max_rows) {
@@ -1150,7 +1157,7 @@ void w90g_server_delete(void* server) {
 
 long long w90g_kernel_launches(void* hv) {
   Handle* h = H(hv);
-  return h->eng ? h->eng->launches() : 0;
+  return (h->eng ? h->eng->launches() : 0) + h->dis_launches;
 }
 
 }  // extern "C"

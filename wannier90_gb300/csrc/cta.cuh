@@ -37,10 +37,14 @@ __device__ __forceinline__ double block_max(double v, double* red) {
 // pointer, overwritten by its near-diagonal form); V receives the eigenvectors
 // (columns).  Rotation for pair (p,q):  J = [[c, s e^{i phi}], [-s e^{-i phi}, c]],
 // phi = arg(H_pq), (c, s) the real Jacobi rotation of [[H_pp, |H_pq|], [|H_pq|, H_qq]].
+// Convergence: sum_{p != q} |H_pq|^2 <= 1e-30 ||H||_F^2.  With skip_rel > 0, pairs with
+// |H_pq|^2 <= skip_rel ||H||_F^2 are left alone and a sweep that rotates no pair also ends
+// the solve (the threshold-Jacobi rule: reachable at any size, where the plain criterion
+// can sit at the roundoff floor of large matrices).
 // Returns the number of sweeps used (or -1 when not converged within max_sweeps).
 // ----------------------------------------------------------------------------
 __device__ __noinline__ static int cta_jacobi(double2* H, double2* V, int W, int max_sweeps, double* red,
-                          double* rc, double2* rse, int* rp, int* rq) {
+                          double* rc, double2* rse, int* rp, int* rq, double skip_rel = 0.0) {
   const int WW = W * W;
   for (int e = threadIdx.x; e < WW; e += blockDim.x) {
     V[e] = cmk((e % W) == (e / W) ? 1.0 : 0.0, 0.0);
@@ -59,6 +63,8 @@ __device__ __noinline__ static int cta_jacobi(double2* H, double2* V, int W, int
     fro = block_sum(fro, red);
     if (off <= 1.0e-30 * fro || off == 0.0) return sweep;
     if (sweep == max_sweeps) break;
+    const double thr = skip_rel * fro;
+    int rotated = 0;
     for (int r = 0; r < n - 1; ++r) {
       for (int t = threadIdx.x; t < npair; t += blockDim.x) {
         int p, q;
@@ -79,7 +85,8 @@ __device__ __noinline__ static int cta_jacobi(double2* H, double2* V, int W, int
         if (q < W) {
           const double2 b = H[q * W + p];
           const double ab = sqrt(cabs2(b));
-          if (ab > 1.0e-300) {
+          if (ab > 1.0e-300 && (skip_rel == 0.0 || ab * ab > thr)) {
+            ++rotated;
             const double a = H[p * W + p].x, d = H[q * W + q].x;
             const double th = (d - a) / (2.0 * ab);
             const double tt = (th >= 0.0 ? 1.0 : -1.0) / (fabs(th) + sqrt(1.0 + th * th));
@@ -124,6 +131,7 @@ __device__ __noinline__ static int cta_jacobi(double2* H, double2* V, int W, int
       }
       __syncthreads();
     }
+    if (skip_rel > 0.0 && block_sum((double)rotated, red) == 0.0) return sweep + 1;
   }
   return -1;
 }

@@ -56,6 +56,8 @@ struct DisDev {
   double* wk1;           // [k] Omega_I(i-1) parts (from the eigenvalues)
   double* wk;            // [k] Omega_I(i) parts (from the overlaps)
   int* status;           // [k]
+  double2* Vz;           // [k] m x m eigenvectors of the last Z (warm start of the next)
+  int* max_sweeps;       // Jacobi sweeps, max over k and iterations
 };
 
 __device__ __forceinline__ double2 op_el(const double2* X, int ld, bool c, int i, int j) {
@@ -247,19 +249,21 @@ __global__ void __launch_bounds__(256) k_dis_froz(DisDev D) {
   }
 }
 
-// ---- internal_zmatrix (:2922-2988): Z(k) = sum_b w_b C_b C_b^H on the non-frozen
-// states, C_b = M_w(k,b) U_opt(k+b).  Upper triangle summed, lower mirrored.
-__global__ void __launch_bounds__(256) k_dis_z(DisDev D, int cur, int to_in) {
+// ---- internal_zmatrix (:2922-2988), kept on every window state: Zf(k) = sum_b w_b C_b C_b^H
+// with C_b = M_w(k,b) U_opt(k+b) (n x W).  The reference's Z is the block of Zf on the
+// non-frozen states; the rest gives the Omega_I parts without a second pass over the
+// overlaps:  sum_b w_b |U(k)^H M_w U(k+b)|_F^2 = tr(U^H Zf U), and for a frozen column
+// e_f of U the row sum is Zf_ff.  Upper triangle summed, lower mirrored.  With
+// want_omega, also wk[k] = W wbtot - Re tr(U^H Zf U) (Omega_I(i) part, :2480-2500).
+__global__ void __launch_bounds__(256) k_dis_z(DisDev D, int cur, int to_in, int want_omega) {
+  __shared__ double red[256];
   const int k = blockIdx.x;
-  const int nb = D.nb, W = D.W, n = D.ndim[k], nf = D.nfroz[k], B = D.B;
-  if (W <= nf) return;
-  const int m = n - nf;
+  const int nb = D.nb, W = D.W, n = D.ndim[k], B = D.B;
   const size_t NN = (size_t)nb * nb;
   double2* ws = D.ws + (size_t)k * kWs * NN;
   double2* Zacc = ws + NN;
   double2* Z = (to_in ? D.Zin : D.Zout) + (size_t)k * NN;
-  const int* nfi = D.nfidx + (size_t)k * nb;
-  for (int e = threadIdx.x; e < m * m; e += blockDim.x) Zacc[e] = cmk(0, 0);
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) Zacc[e] = cmk(0, 0);
   for (int b = 0; b < B; ++b) {
     const int k2 = D.nnlist[k * B + b];
     const int n2 = D.ndim[k2];
@@ -269,61 +273,54 @@ __global__ void __launch_bounds__(256) k_dis_z(DisDev D, int cur, int to_in) {
     cta_zgemm(ws, nb, Mw, nb, false, U2, nb, false, n, W, n2);   // C_b (n x W)
     __syncthreads();
     const double w = D.wb[b];
-    for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
-      const int p = e % m, q = e / m;
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+      const int p = e % n, q = e / n;
       if (p > q) continue;
-      const int pp = nfi[p], qq = nfi[q];
       double2 acc = cmk(0, 0);
-      for (int l = 0; l < W; ++l) cfma(acc, ws[(size_t)l * nb + pp], cconj(ws[(size_t)l * nb + qq]));
+      for (int l = 0; l < W; ++l) cfma(acc, ws[(size_t)l * nb + p], cconj(ws[(size_t)l * nb + q]));
       Zacc[e] = cadd(Zacc[e], cscale(acc, w));
     }
   }
   __syncthreads();
-  for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
-    const int p = e % m, q = e / m;
-    Z[(size_t)q * nb + p] = (p <= q) ? Zacc[e] : cconj(Zacc[(size_t)p * m + q]);
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    const int p = e % n, q = e / n;
+    Z[(size_t)q * nb + p] = (p <= q) ? Zacc[e] : cconj(Zacc[(size_t)p * n + q]);
   }
-}
-
-// sum_b w_b sum_{r < rows} |(U(k)^H M_w(k,b) U(k+b))_{r,:}|^2 with U = U[cur]
-__device__ double omega_rows(const DisDev& D, int k, int cur, int rows, double2* ws, double* red) {
-  const int nb = D.nb, W = D.W, n = D.ndim[k], B = D.B;
-  const size_t NN = (size_t)nb * nb;
+  if (!want_omega) return;
+  __syncthreads();
+  // tr(U^H Zf U) = sum_{j} sum_p conj(U_pj) (Zf U)_pj
   const double2* Uk = D.U[cur] + (size_t)k * nb * W;
-  double tot = 0.0;
-  for (int b = 0; b < B; ++b) {
-    const int k2 = D.nnlist[k * B + b];
-    const int n2 = D.ndim[k2];
-    const double2* Mw = D.Mw + ((size_t)k * B + b) * NN;
-    const double2* U2 = D.U[cur] + (size_t)k2 * nb * W;
-    __syncthreads();
-    cta_zgemm(ws, nb, Uk, nb, true, Mw, nb, false, rows, n2, n);          // rows x n2
-    __syncthreads();
-    cta_zgemm(ws + NN, nb, ws, nb, false, U2, nb, false, rows, W, n2);    // rows x W
-    __syncthreads();
-    double s = 0.0;
-    for (int e = threadIdx.x; e < rows * W; e += blockDim.x) {
-      const int i = e % rows, j = e / rows;
-      s += cabs2(ws[NN + (size_t)j * nb + i]);
-    }
-    tot += D.wb[b] * block_sum(s, red);
+  double t = 0.0;
+  for (int e = threadIdx.x; e < n * W; e += blockDim.x) {
+    const int p = e % n, j = e / n;
+    double2 acc = cmk(0, 0);
+    for (int q = 0; q < n; ++q) cfma(acc, Z[(size_t)q * nb + p], Uk[(size_t)j * nb + q]);
+    const double2 u = Uk[(size_t)j * nb + p];
+    t += u.x * acc.x + u.y * acc.y;
   }
-  return tot;
+  t = block_sum(t, red);
+  if (threadIdx.x == 0) D.wk[k] = (double)W * D.wbtot - t;
 }
 
-// ---- one step of dis_extract (:2160-2470): mix Z, diagonalise, new U_opt (into
-// U[cur^1]), and the Omega_I(i-1) part of this k (frozen rows with the old U_opt).
+// ---- one step of dis_extract (:2160-2470): mix Z on the non-frozen states, diagonalise,
+// new U_opt into U[cur^1], and the Omega_I(i-1) part of this k:
+//   W wbtot - sum_{frozen f} Zf_ff (old U) - sum of the selected eigenvalues.
+// Dynamic shared memory: the m x m eigenproblem (H, V) of the largest m over k.
 __global__ void __launch_bounds__(256) k_dis_step(DisDev D, int cur, int it) {
   __shared__ DisShared sh;
+  extern __shared__ double2 dsm[];
   const int k = blockIdx.x;
-  const int nb = D.nb, W = D.W, n = D.ndim[k], nf = D.nfroz[k];
+  const int nb = D.nb, W = D.W, n = D.ndim[k], nf = D.nfroz[k], ff = D.ffirst[k];
   const size_t NN = (size_t)nb * nb;
-  double2* ws = D.ws + (size_t)k * kWs * NN;
   const double2* Uo = D.U[cur] + (size_t)k * nb * W;
   double2* Un = D.U[cur ^ 1] + (size_t)k * nb * W;
+  double2* Zi = D.Zin + (size_t)k * NN;
+  const double2* Zo = D.Zout + (size_t)k * NN;
+  // Zf of the old U_opt: Zin before the first mixing, Zout afterwards
+  const double2* Zold = (it > 1) ? Zo : Zi;
   double wk1 = (double)W * D.wbtot;
-  if (nf > 0) wk1 -= omega_rows(D, k, cur, nf, ws, sh.red);
-  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int l = 0; l < nf; ++l) wk1 -= Zold[(size_t)(ff + l) * nb + ff + l].x;
   // frozen columns carry over; the others are rebuilt below
   for (int e = threadIdx.x; e < nb * W; e += blockDim.x) {
     const int c = e / nb;
@@ -331,54 +328,67 @@ __global__ void __launch_bounds__(256) k_dis_step(DisDev D, int cur, int it) {
   }
   if (W > nf) {
     const int m = n - nf;
-    double2* Zi = D.Zin + (size_t)k * NN;
-    const double2* Zo = D.Zout + (size_t)k * NN;
+    const int* nfi = D.nfidx + (size_t)k * nb;
     if (it > 1) {
       for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
         const int p = e % m, q = e / m;
         if (p <= q) {
-          const size_t o = (size_t)q * nb + p;
+          const size_t o = (size_t)nfi[q] * nb + nfi[p];
           Zi[o] = cadd(cscale(Zo[o], D.mix), cscale(Zi[o], 1.0 - D.mix));
         }
       }
       __syncthreads();
+    }
+    const size_t mm = (size_t)m * m;
+    double2 *H = dsm, *V = dsm + mm, *T = dsm + 2 * mm;
+    double2* Vz = D.Vz + (size_t)k * NN;
+    for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
+      const int p = e % m, q = e / m;
+      H[e] = (p <= q) ? Zi[(size_t)nfi[q] * nb + nfi[p]] : cconj(Zi[(size_t)nfi[p] * nb + nfi[q]]);
+    }
+    __syncthreads();
+    // Z moves little from one iteration to the next: rotate it into the previous
+    // eigenbasis, H = Vz^H Z Vz (Hermitised), so Jacobi starts near-diagonal
+    const bool warm = it > 1;
+    if (warm) {
+      cta_zgemm(T, m, H, m, false, Vz, m, false, m, m, m);
+      __syncthreads();
+      cta_zgemm(H, m, Vz, m, true, T, m, false, m, m, m);
+      __syncthreads();
       for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
         const int p = e % m, q = e / m;
-        if (p > q) Zi[(size_t)q * nb + p] = cconj(Zi[(size_t)p * nb + q]);
+        if (p < q) {
+          const double2 a = H[(size_t)q * m + p], b = cconj(H[(size_t)p * m + q]);
+          const double2 h = cscale(cadd(a, b), 0.5);
+          H[(size_t)q * m + p] = h;
+          H[(size_t)p * m + q] = cconj(h);
+        } else if (p == q) {
+          H[e].y = 0.0;
+        }
       }
       __syncthreads();
     }
-    double2 *H = ws, *V = ws + NN;
-    for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
-      const int p = e % m, q = e / m;
-      H[e] = Zi[(size_t)q * nb + p];
-    }
-    __syncthreads();
-    const int sw = cta_jacobi(H, V, m, 60, sh.red, sh.rc, sh.rse, sh.rp, sh.rq);
+    const int sw = cta_jacobi(H, V, m, 60, sh.red, sh.rc, sh.rse, sh.rp, sh.rq, 1.0e-30);
     sort_eigs(H, m, sh.ord, sh.ev);
+    if (warm) {
+      cta_zgemm(T, m, Vz, m, false, V, m, false, m, m, m);   // eigenvectors of Z
+      __syncthreads();
+    } else {
+      T = V;
+    }
+    for (int e = threadIdx.x; e < m * m; e += blockDim.x) Vz[e] = T[e];
     const int j0 = n - W, j1 = n - nf;   // selected ascending positions [j0, j1)
     if (threadIdx.x == 0) {
       for (int j = j0; j < j1; ++j) wk1 -= sh.ev[sh.ord[j]];
       if (sw < 0) D.status[k] = 2;
+      atomicMax(D.max_sweeps, sw);
     }
-    const int* nfi = D.nfidx + (size_t)k * nb;
-    __syncthreads();
     for (int e = threadIdx.x; e < m * (j1 - j0); e += blockDim.x) {
       const int i = e % m, c = e / m;
-      Un[(size_t)(nf + c) * nb + nfi[i]] = V[(size_t)sh.ord[j0 + c] * m + i];
+      Un[(size_t)(nf + c) * nb + nfi[i]] = T[(size_t)sh.ord[j0 + c] * m + i];
     }
   }
   if (threadIdx.x == 0) D.wk1[k] = wk1;
-}
-
-// ---- Omega_I(i) part of this k with the new U_opt (:2480-2500)
-__global__ void __launch_bounds__(256) k_dis_omega(DisDev D, int cur) {
-  __shared__ double red[256];
-  const int k = blockIdx.x;
-  const size_t NN = (size_t)D.nb * D.nb;
-  double2* ws = D.ws + (size_t)k * kWs * NN;
-  const double t = omega_rows(D, k, cur, D.W, ws, red);
-  if (threadIdx.x == 0) D.wk[k] = (double)D.W * D.wbtot - t;
 }
 
 // ---- subspace Hamiltonian gauge (:2560-2640): U_opt <- U_opt V with V the eigenvectors
@@ -454,6 +464,12 @@ __global__ void __launch_bounds__(256) k_dis_rotate(DisDev D, int cur) {
 
 }  // namespace
 
+const char* dis_kernel_name(int i) {
+  static const char* names[kDisKernels] = {"k_dis_project", "k_dis_froz", "k_dis_z", "k_dis_step",
+                                           "k_dis_gauge", "k_dis_findu", "k_dis_rotate"};
+  return (i >= 0 && i < kDisKernels) ? names[i] : "";
+}
+
 #define DIS_CHECK(call)                                                     \
   do {                                                                      \
     cudaError_t e_ = (call);                                                \
@@ -464,22 +480,20 @@ __global__ void __launch_bounds__(256) k_dis_rotate(DisDev D, int cur) {
     }                                                                       \
   } while (0)
 
-int dis_run(const DisSpec& s, DisResult& r, std::string& err) {
-  const int nb = s.nb, W = s.W, K = s.K, B = s.B;
-  if (nb < W || nb > 64 || W < 1 || K < 1 || B < 1) {
-    err = "disentangle: the GPU engine needs num_wann <= num_bands <= 64";
-    return 5;
-  }
-  const DisControl& c = s.ctl;
-  if (c.conv_window < 0 || c.num_iter < 0) {
-    err = "disentangle: dis_num_iter and dis_conv_window must be positive";
-    return 5;
-  }
-  // ---- dis_windows (:851-1171) on the host
-  std::vector<int> ndim(K), nfirst(K), nfroz(K), ffirst(K), nfidx((size_t)K * nb, 0);
-  std::vector<double> eigw((size_t)K * nb, 0.0);
+// dis_windows (src/disentangle.F90:851-1171) on the host: outer window [nfirst, +ndim),
+// frozen states [ffirst, +nfroz) inside it, the non-frozen window states, and the
+// window eigenvalues.  Returns 0 or 1 (fatal) with err set.
+static int dis_windows(const DisControl& c, const double* eig, int nb, int W, int K, std::vector<int>& ndim,
+                       std::vector<int>& nfirst, std::vector<int>& nfroz, std::vector<int>& ffirst,
+                       std::vector<int>& nfidx, std::vector<double>& eigw, std::string& err) {
+  ndim.assign(K, 0);
+  nfirst.assign(K, 0);
+  nfroz.assign(K, 0);
+  ffirst.assign(K, 0);
+  nfidx.assign((size_t)K * nb, 0);
+  eigw.assign((size_t)K * nb, 0.0);
   for (int k = 0; k < K; ++k) {
-    const double* e = s.eig + (size_t)k * nb;
+    const double* e = eig + (size_t)k * nb;
     if (e[0] > c.win_max || e[nb - 1] < c.win_min) {
       err = "dis_windows: The outer energy window contains no eigenvalues";
       return 1;
@@ -523,6 +537,39 @@ int dis_run(const DisSpec& s, DisResult& r, std::string& err) {
       if (!(nfroz[k] > 0 && j >= ffirst[k] && j < ffirst[k] + nfroz[k])) nfidx[(size_t)k * nb + cnt++] = j;
     for (int i = 0; i < ndim[k]; ++i) eigw[(size_t)k * nb + i] = e[imin + i];
   }
+  return 0;
+}
+
+int dis_run(const DisSpec& s, DisResult& r, std::string& err) {
+  const int nb = s.nb, W = s.W, K = s.K, B = s.B;
+  if (nb < W || nb > 64 || W < 1 || K < 1 || B < 1) {
+    err = "disentangle: the GPU engine needs num_wann <= num_bands <= 64";
+    return 5;
+  }
+  const DisControl& c = s.ctl;
+  if (c.conv_window < 0 || c.num_iter < 0) {
+    err = "disentangle: dis_num_iter and dis_conv_window must be positive";
+    return 5;
+  }
+  const cudaMemcpyKind in_kind = s.device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  const cudaMemcpyKind out_kind = s.device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  std::vector<int> ndim, nfirst, nfroz, ffirst, nfidx;
+  std::vector<double> eigw, eig_host;
+  const double* eig = s.eig;
+  if (s.device) {
+    // the windows are set up on the host: bring the band energies over first
+    eig_host.resize((size_t)K * nb);
+    cudaError_t e = cudaMemcpy(eig_host.data(), s.eig, eig_host.size() * 8, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) {
+      err = std::string("disentangle: eigval copy: ") + cudaGetErrorString(e);
+      return 1;
+    }
+    eig = eig_host.data();
+  }
+  {
+    const int wrc = dis_windows(c, eig, nb, W, K, ndim, nfirst, nfroz, ffirst, nfidx, eigw, err);
+    if (wrc) return wrc;
+  }
   bool any_froz = false;
   for (int v : nfroz) any_froz = any_froz || v > 0;
 
@@ -547,13 +594,42 @@ int dis_run(const DisSpec& s, DisResult& r, std::string& err) {
                o_zin = take((size_t)K * NN * 16), o_zout = take((size_t)K * NN * 16),
                o_uw = take((size_t)K * W * W * 16), o_m0 = take((size_t)K * B * W * W * 16),
                o_ws = take((size_t)K * kWs * NN * 16), o_wk1 = take(K * 8), o_wk = take(K * 8),
-               o_st = take(K * 4);
+               o_st = take(K * 4), o_vz = take((size_t)K * NN * 16), o_sw = take(4);
   const size_t rot_smem = ((size_t)W * nb + 2 * (size_t)W * W) * 16;
+  int mmax = 0;
+  for (int k = 0; k < K; ++k) mmax = std::max(mmax, ndim[k] - nfroz[k]);
+  const size_t step_smem = 3 * (size_t)mmax * mmax * 16;
   int cur = 0, it = 0;
   double womegai = 0.0;
-  cudaStream_t st = nullptr;
-  DIS_CHECK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-  DIS_CHECK(cudaMalloc(&arena, off));
+  cudaStream_t st = s.stream;
+  bool own_stream = false;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  // launch with optional per-kernel event timing
+  auto launch = [&](int id, auto&& fn) -> cudaError_t {
+    if (s.prof_ms) cudaEventRecord(ev[0], st);
+    fn();
+    ++r.launches;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || !s.prof_ms) return e;
+    cudaEventRecord(ev[1], st);
+    e = cudaEventSynchronize(ev[1]);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, ev[0], ev[1]);
+    s.prof_ms[id] += ms;
+    if (s.prof_counts) ++s.prof_counts[id];
+    return e;
+  };
+  r.launches = 0;
+  if (!st) {
+    DIS_CHECK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    own_stream = true;
+  }
+  if (s.prof_ms) {
+    DIS_CHECK(cudaEventCreate(&ev[0]));
+    DIS_CHECK(cudaEventCreate(&ev[1]));
+  }
+  DIS_CHECK(cudaFuncSetAttribute(k_dis_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)step_smem));
+  DIS_CHECK(cudaMallocAsync(&arena, off, st));
   {
     char* a = (char*)arena;
     D.nb = nb;
@@ -583,6 +659,8 @@ int dis_run(const DisSpec& s, DisResult& r, std::string& err) {
     D.wk1 = (double*)(a + o_wk1);
     D.wk = (double*)(a + o_wk);
     D.status = (int*)(a + o_st);
+    D.Vz = (double2*)(a + o_vz);
+    D.max_sweeps = (int*)(a + o_sw);
   }
   DIS_CHECK(cudaMemcpyAsync((void*)D.nnlist, s.nnlist.data(), (size_t)K * B * 4, cudaMemcpyHostToDevice, st));
   DIS_CHECK(cudaMemcpyAsync((void*)D.wb, s.wb.data(), B * 8, cudaMemcpyHostToDevice, st));
@@ -592,15 +670,12 @@ int dis_run(const DisSpec& s, DisResult& r, std::string& err) {
   DIS_CHECK(cudaMemcpyAsync((void*)D.ffirst, ffirst.data(), K * 4, cudaMemcpyHostToDevice, st));
   DIS_CHECK(cudaMemcpyAsync((void*)D.nfidx, nfidx.data(), (size_t)K * nb * 4, cudaMemcpyHostToDevice, st));
   DIS_CHECK(cudaMemcpyAsync((void*)D.eig, eigw.data(), (size_t)K * nb * 8, cudaMemcpyHostToDevice, st));
-  DIS_CHECK(cudaMemcpyAsync((void*)D.Mraw, s.M, (size_t)K * B * NN * 16, cudaMemcpyHostToDevice, st));
-  DIS_CHECK(cudaMemcpyAsync(D.U[0], s.A, (size_t)K * nb * W * 16, cudaMemcpyHostToDevice, st));
+  DIS_CHECK(cudaMemcpyAsync((void*)D.Mraw, s.M, (size_t)K * B * NN * 16, in_kind, st));
+  DIS_CHECK(cudaMemcpyAsync(D.U[0], s.A, (size_t)K * nb * W * 16, in_kind, st));
   DIS_CHECK(cudaMemsetAsync(D.status, 0, K * 4, st));
-  k_dis_project<<<K, 256, 0, st>>>(D);
-  DIS_CHECK(cudaGetLastError());
-  if (any_froz) {
-    k_dis_froz<<<K, 256, 0, st>>>(D);
-    DIS_CHECK(cudaGetLastError());
-  }
+  DIS_CHECK(cudaMemsetAsync(D.max_sweeps, 0, 4, st));
+  DIS_CHECK(launch(kDisProject, [&] { k_dis_project<<<K, 256, 0, st>>>(D); }));
+  if (any_froz) DIS_CHECK(launch(kDisFroz, [&] { k_dis_froz<<<K, 256, 0, st>>>(D); }));
   DIS_CHECK(cudaMemcpyAsync(status.data(), D.status, K * 4, cudaMemcpyDeviceToHost, st));
   DIS_CHECK(cudaStreamSynchronize(st));
   for (int k = 0; k < K; ++k) {
@@ -613,15 +688,12 @@ int dis_run(const DisSpec& s, DisResult& r, std::string& err) {
     }
   }
   // ---- dis_extract iterations
-  k_dis_z<<<K, 256, 0, st>>>(D, cur, 1);
-  DIS_CHECK(cudaGetLastError());
+  DIS_CHECK(launch(kDisZ, [&] { k_dis_z<<<K, 256, 0, st>>>(D, cur, 1, 0); }));
   r.log.clear();
   r.converged = 0;
   for (it = 1; it <= c.num_iter; ++it) {
-    k_dis_step<<<K, 256, 0, st>>>(D, cur, it);
-    k_dis_omega<<<K, 256, 0, st>>>(D, cur ^ 1);
-    k_dis_z<<<K, 256, 0, st>>>(D, cur ^ 1, 0);
-    DIS_CHECK(cudaGetLastError());
+    DIS_CHECK(launch(kDisStep, [&] { k_dis_step<<<K, 256, step_smem, st>>>(D, cur, it); }));
+    DIS_CHECK(launch(kDisZ, [&] { k_dis_z<<<K, 256, 0, st>>>(D, cur ^ 1, 0, 1); }));
     DIS_CHECK(cudaMemcpyAsync(wk1.data(), D.wk1, K * 8, cudaMemcpyDeviceToHost, st));
     DIS_CHECK(cudaMemcpyAsync(wk.data(), D.wk, K * 8, cudaMemcpyDeviceToHost, st));
     DIS_CHECK(cudaStreamSynchronize(st));
@@ -654,19 +726,12 @@ int dis_run(const DisSpec& s, DisResult& r, std::string& err) {
       }
     }
   }
-  k_dis_gauge<<<K, 256, 0, st>>>(D, cur);
-  k_dis_findu<<<K, 256, 0, st>>>(D, cur);
-  DIS_CHECK(cudaGetLastError());
+  DIS_CHECK(launch(kDisGauge, [&] { k_dis_gauge<<<K, 256, 0, st>>>(D, cur); }));
+  DIS_CHECK(launch(kDisFindU, [&] { k_dis_findu<<<K, 256, 0, st>>>(D, cur); }));
   DIS_CHECK(cudaFuncSetAttribute(k_dis_rotate, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rot_smem));
-  k_dis_rotate<<<K * B, 256, rot_smem, st>>>(D, cur);
-  DIS_CHECK(cudaGetLastError());
-  r.u_opt.assign((size_t)K * nb * W * 2, 0.0);
-  r.u.assign((size_t)K * W * W * 2, 0.0);
-  r.m.assign((size_t)K * B * W * W * 2, 0.0);
-  DIS_CHECK(cudaMemcpyAsync(r.u_opt.data(), D.U[cur], r.u_opt.size() * 8, cudaMemcpyDeviceToHost, st));
-  DIS_CHECK(cudaMemcpyAsync(r.u.data(), D.U0, r.u.size() * 8, cudaMemcpyDeviceToHost, st));
-  DIS_CHECK(cudaMemcpyAsync(r.m.data(), D.M0, r.m.size() * 8, cudaMemcpyDeviceToHost, st));
+  DIS_CHECK(launch(kDisRotate, [&] { k_dis_rotate<<<K * B, 256, rot_smem, st>>>(D, cur); }));
   DIS_CHECK(cudaMemcpyAsync(status.data(), D.status, K * 4, cudaMemcpyDeviceToHost, st));
+  DIS_CHECK(cudaMemcpyAsync(&r.max_sweeps, D.max_sweeps, 4, cudaMemcpyDeviceToHost, st));
   DIS_CHECK(cudaStreamSynchronize(st));
   for (int k = 0; k < K; ++k) {
     if (status[k]) {
@@ -675,12 +740,21 @@ int dis_run(const DisSpec& s, DisResult& r, std::string& err) {
       goto done;
     }
   }
+  if (s.uopt_out) DIS_CHECK(cudaMemcpyAsync(s.uopt_out, D.U[cur], (size_t)K * nb * W * 16, out_kind, st));
+  if (s.u_out) DIS_CHECK(cudaMemcpyAsync(s.u_out, D.U0, (size_t)K * W * W * 16, out_kind, st));
+  if (s.m_out) DIS_CHECK(copy_wblocks(s.m_out, nb, D.M0, W, W, K * B, out_kind, st));
+  DIS_CHECK(cudaStreamSynchronize(st));
   r.omega_invariant = womegai;
   r.ndimwin = ndim;
   r.nfirstwin = nfirst;
 done:
-  if (arena) cudaFree(arena);
-  if (st) cudaStreamDestroy(st);
+  if (arena) {
+    cudaFreeAsync(arena, st);
+    cudaStreamSynchronize(st);
+  }
+  if (ev[0]) cudaEventDestroy(ev[0]);
+  if (ev[1]) cudaEventDestroy(ev[1]);
+  if (own_stream) cudaStreamDestroy(st);
   return rc;
 }
 

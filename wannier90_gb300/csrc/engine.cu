@@ -392,22 +392,11 @@ int Engine::alloc(std::string& err) {
   return 0;
 }
 
-// one strided copy of the top-left W x W of each ldm x ldm block (K*B blocks)
-static cudaError_t copy_blocks(void* dst, int ldd, const void* src, int lds, int W, int nblk, cudaMemcpyKind kind,
-                               cudaStream_t st) {
-  cudaMemcpy3DParms q = {};
-  q.srcPtr = make_cudaPitchedPtr(const_cast<void*>(src), (size_t)lds * 16, (size_t)W * 16, (size_t)lds);
-  q.dstPtr = make_cudaPitchedPtr(dst, (size_t)ldd * 16, (size_t)W * 16, (size_t)ldd);
-  q.extent = make_cudaExtent((size_t)W * 16, (size_t)W, (size_t)nblk);
-  q.kind = kind;
-  return cudaMemcpy3DAsync(&q, st);
-}
-
 int Engine::load(int p, const void* M, const void* U, cudaMemcpyKind kind, std::string& err, int ldm) {
   const auto& s = specs_[p];
   const size_t WW = (size_t)s.W * s.W;
   cudaStream_t st = stream();
-  if (M && ldm > s.W) W90G_CHECK(copy_blocks(hprobs_[p].M[0], s.W, M, ldm, s.W, s.K * s.B, kind, st));
+  if (M && ldm > s.W) W90G_CHECK(copy_wblocks(hprobs_[p].M[0], s.W, M, ldm, s.W, s.K * s.B, kind, st));
   else if (M) W90G_CHECK(cudaMemcpyAsync(hprobs_[p].M[0], M, (size_t)s.K * s.B * WW * 16, kind, st));
   if (U) W90G_CHECK(cudaMemcpyAsync(hprobs_[p].U[0], U, (size_t)s.K * WW * 16, kind, st));
   return 0;
@@ -421,7 +410,7 @@ int Engine::store(int p, void* M, void* U, cudaMemcpyKind kind, std::string& err
   W90G_CHECK(cudaMemcpyAsync(&hs, hprobs_[p].st, sizeof(CtrlState), cudaMemcpyDeviceToHost, st));
   W90G_CHECK(cudaStreamSynchronize(st));
   const int cur = hs.cur;
-  if (M && ldm > s.W) W90G_CHECK(copy_blocks(M, ldm, hprobs_[p].M[cur], s.W, s.W, s.K * s.B, kind, st));
+  if (M && ldm > s.W) W90G_CHECK(copy_wblocks(M, ldm, hprobs_[p].M[cur], s.W, s.W, s.K * s.B, kind, st));
   else if (M) W90G_CHECK(cudaMemcpyAsync(M, hprobs_[p].M[cur], (size_t)s.K * s.B * WW * 16, kind, st));
   if (U) W90G_CHECK(cudaMemcpyAsync(U, hprobs_[p].U[cur], (size_t)s.K * WW * 16, kind, st));
   W90G_CHECK(cudaStreamSynchronize(st));

@@ -179,4 +179,17 @@ __device__ __forceinline__ int locate(const WorkMap& wm, int item, int& local) {
 }
 #endif
 
+// Host: one strided copy of the top-left W x W of each of nblk complex128 blocks
+// (leading dimensions ldd / lds), e.g. the num_wann x num_wann part of the
+// (num_bands, num_bands) blocks of m_matrix_local.
+inline cudaError_t copy_wblocks(void* dst, int ldd, const void* src, int lds, int W, int nblk, cudaMemcpyKind kind,
+                                cudaStream_t st) {
+  cudaMemcpy3DParms q = {};
+  q.srcPtr = make_cudaPitchedPtr(const_cast<void*>(src), (size_t)lds * 16, (size_t)W * 16, (size_t)lds);
+  q.dstPtr = make_cudaPitchedPtr(dst, (size_t)ldd * 16, (size_t)W * 16, (size_t)ldd);
+  q.extent = make_cudaExtent((size_t)W * 16, (size_t)W, (size_t)nblk);
+  q.kind = kind;
+  return cudaMemcpy3DAsync(&q, st);
+}
+
 }  // namespace w90g

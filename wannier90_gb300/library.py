@@ -172,6 +172,29 @@ def w90_disentangle(common: LibCommon) -> int:
     return ierr.value
 
 
+def w90_disentangle_device(common: LibCommon, m_ptr: int, u_opt_ptr: int, u_ptr: int, eig_ptr: int) -> int:
+    """w90_disentangle with m_local, u_opt, u_matrix and eigval resident in device memory."""
+    ierr = C.c_int(0)
+    common._L.w90g_disentangle_device(common._h, C.c_void_p(m_ptr), C.c_void_p(u_opt_ptr), C.c_void_p(u_ptr),
+                                      C.c_void_p(eig_ptr), C.byref(ierr))
+    return ierr.value
+
+
+def w90_profile_dis_device(common: LibCommon, m_ptr: int, u_opt_ptr: int, u_ptr: int, eig_ptr: int):
+    """Disentanglement on device buffers with per-kernel CUDA-event timing:
+    (ierr, {kernel: (ms_total, launches)})."""
+    L = common._L
+    names = []
+    while L.w90g_dis_kernel_name(len(names)):
+        names.append(L.w90g_dis_kernel_name(len(names)).decode())
+    ms = np.zeros(len(names), dtype=np.float64)
+    counts = np.zeros(len(names), dtype=np.int32)
+    ierr = L.w90g_profile_dis_device(common._h, C.c_void_p(m_ptr), C.c_void_p(u_opt_ptr), C.c_void_p(u_ptr),
+                                     C.c_void_p(eig_ptr), ms.ctypes.data_as(C.POINTER(C.c_double)),
+                                     counts.ctypes.data_as(C.POINTER(C.c_int)))
+    return ierr, {nm: (float(ms[i]), int(counts[i])) for i, nm in enumerate(names)}
+
+
 def w90_get_dis_log(common: LibCommon, max_rows: int) -> np.ndarray:
     """Omega_I iteration record of the last w90_disentangle: columns iter,
     Omega_I(i-1), Omega_I(i), delta (frac.), seconds."""
@@ -181,10 +204,12 @@ def w90_get_dis_log(common: LibCommon, max_rows: int) -> np.ndarray:
 
 
 def w90_get_dis_info(common: LibCommon) -> dict:
-    """Final Omega_I (omega%invariant), convergence flag and iteration count."""
-    out = np.zeros(3, dtype=np.float64)
+    """Final Omega_I (omega%invariant), convergence flag, iteration count and the most
+    Jacobi sweeps one Z eigenproblem took."""
+    out = np.zeros(4, dtype=np.float64)
     common._L.w90g_get_dis_info(common._h, out.ctypes.data_as(C.POINTER(C.c_double)))
-    return {"omega_invariant": float(out[0]), "converged": bool(out[1]), "iterations": int(out[2])}
+    return {"omega_invariant": float(out[0]), "converged": bool(out[1]), "iterations": int(out[2]),
+            "max_sweeps": int(out[3])}
 
 
 def w90_wannierise(common: LibCommon) -> int:

@@ -78,9 +78,10 @@ def kmesh_tables(real_lattice, kpoints, search_shells=36):
     return B, nnlist, nncell, bk
 
 
-def _tb_bands(rng, kind, a, mp, norb, rmax):
+def _tb_bands(rng, kind, a, mp, norb, rmax, onsite=None):
     """Random tight-binding model with `norb` orbitals: lattice, k-points, orbital
-    positions, band energies E[k, m] (ascending) and eigenvectors C[k, :, m]."""
+    positions, band energies E[k, m] (ascending) and eigenvectors C[k, :, m].  `onsite`
+    (length norb) is added to the diagonal of H(R = 0)."""
     A = lattice(kind, a)
     kp = mp_kpoints(*mp)
     K = len(kp)
@@ -101,6 +102,8 @@ def _tb_bands(rng, kind, a, mp, norb, rmax):
         HR[idx[tuple(-Rs[r])]] = x.conj().T
     x0 = (rng.standard_normal((norb, norb)) + 1j * rng.standard_normal((norb, norb))) / math.sqrt(2.0)
     HR[idx[(0.0, 0.0, 0.0)]] = 0.5 * (x0 + x0.conj().T)
+    if onsite is not None:
+        HR[idx[(0.0, 0.0, 0.0)]] += np.diag(np.asarray(onsite, dtype=np.float64))
     # Bloch Hamiltonians and eigenvectors
     ph = np.exp(2j * math.pi * (kp @ Rs.T))                      # (K, nR)
     Hk = (ph @ HR.reshape(nR, norb * norb)).reshape(K, norb, norb)
@@ -161,13 +164,16 @@ class EntangledProblem:
 
 
 def make_entangled_problem(kind="sc", a=5.0, mp=(4, 4, 4), num_bands=12, num_wann=8, rmax=2, eps=0.3,
-                           seed=0, search_shells=36) -> EntangledProblem:
+                           seed=0, search_shells=36, offset=0.0) -> EntangledProblem:
     """Tight-binding model with num_bands orbitals, all bands kept; the trial orbitals are
     the first num_wann orbitals rotated by a seeded random unitary per k, so
-    A_mn(k) = sum_{a < num_wann} conj(C_am(k)) (exp(eps X_k))_an."""
+    A_mn(k) = sum_{a < num_wann} conj(C_am(k)) (exp(eps X_k))_an.  `offset` raises the
+    on-site energy of the other num_bands - num_wann orbitals, which then form bands
+    above the target manifold that overlap it only partly (offset 0: fully mixed)."""
     rng = np.random.Generator(np.random.PCG64(seed))
     nb, W = int(num_bands), int(num_wann)
-    A, kp, tau, Ek, Ck = _tb_bands(rng, kind, a, mp, nb, rmax)
+    onsite = np.concatenate([np.zeros(W), np.full(nb - W, float(offset))]) if offset else None
+    A, kp, tau, Ek, Ck = _tb_bands(rng, kind, a, mp, nb, rmax, onsite)
     K = len(kp)
     B, nnlist, nncell, bk, M = _tb_overlaps(A, kp, tau, Ck, search_shells)
     G = np.zeros((K, nb, W), dtype=np.complex128)
@@ -177,6 +183,17 @@ def make_entangled_problem(kind="sc", a=5.0, mp=(4, 4, 4), num_bands=12, num_wan
                             np.asfortranarray(M.transpose(2, 3, 1, 0)),
                             np.asfortranarray(Amat.transpose(1, 2, 0)),
                             np.asfortranarray(Ek.T), tau, seed)
+
+
+def entangled_windows(eig, W):
+    """Outer and frozen windows for an entangled problem (eig[k, nb]): the outer window
+    drops the lowest band at some k-points (nfirstwin > 0), keeps >= W + 1 states
+    everywhere and about half of the bands above W on average; the frozen window holds
+    at most W // 2 + 1 states."""
+    nb = eig.shape[1]
+    return dict(win_min=float(eig[:, 1].min()),
+                win_max=float(max(eig[:, W].max(), np.median(eig[:, (W + nb) // 2]))),
+                froz_max=float(eig[:, W // 2].min()))
 
 
 # the workloads of the benchmark configurations (sizes as named in the suite)
