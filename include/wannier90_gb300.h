@@ -135,7 +135,7 @@ void w90g_project_overlap_device(void* handle, double* d_m_matrix, double* d_u_m
 void w90g_wannierise_batch_device(void** handles, int nprob, double** d_m, double** d_u, int* ierr);
 /* Run the engine's work on a caller-provided cudaStream_t (NULL = the engine's own). */
 void w90g_set_stream(void* handle, void* cuda_stream);
-/* Number of engine kernels launched by the last call on this handle. */
+/* Kernels launched by the last wannierisation plus the last disentanglement on this handle. */
 long long w90g_kernel_launches(void* handle);
 /* Profiling run of wannierise on device buffers: every kernel launched alone and timed
  * with CUDA events on the launching stream (at most max_iters iterations).  ms[i] and

@@ -346,7 +346,7 @@ int do_disentangle(Handle* h, double* m, double* uopt, double* u, const double* 
   w90g::DisResult r;
   std::string err;
   const int rc = w90g::dis_run(ds, r, err);
-  h->dis_launches += r.launches;
+  h->dis_launches = r.launches;   // kernels of the last disentanglement
   if (rc) return fail(h, rc, err);
   h->omega_invariant = r.omega_invariant;
   h->dis_converged = r.converged;
@@ -662,7 +662,7 @@ void cinput_setopt(void* hv, const char* seedname, int* ierr, int comm) {
   h->gpu_tensor_exp = get_num(h, "gpu_tensor_exp", v) ? (int)v : 1;
   // options on wann_main's code path that the engine does not implement
   const char* unsupported[] = {"slwf_num", "slwf_constrain", "site_symmetry",
-                               "gamma_only"};
+                               "gamma_only", "dis_spheres_num"};
   for (const char* k : unsupported) {
     if (get_num(h, k, v)) {
       const bool active = (std::string(k) == "slwf_num") ? ((int)v != h->num_wann) : (v != 0.0);

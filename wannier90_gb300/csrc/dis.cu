@@ -440,7 +440,7 @@ __global__ void __launch_bounds__(256) k_dis_findu(DisDev D, int cur) {
   if (threadIdx.x == 0 && sh.flag) D.status[k] = 10 + sh.flag;
 }
 
-// ---- dis_main's M_opt = U_opt^H M U_opt' and setup_m_loc's U0^H M_opt U0', per (k,b)
+// ---- dis_main's M_opt = U_opt^H M U_opt' (:220-235) and setup_m_loc's U0^H M_opt U0', per (k,b)
 __global__ void __launch_bounds__(256) k_dis_rotate(DisDev D, int cur) {
   const int kb = blockIdx.x;
   const int k = kb / D.B;
