@@ -106,6 +106,10 @@ int w90g_get_log(void* handle, double* rows, int max_rows);
  *   (iter, Omega_I(i-1), Omega_I(i), delta (frac.), seconds) -- the "<-- DIS" lines of
  *   dis_extract (src/disentangle.F90:2480-2490).  Returns the rows written. */
 int w90g_get_dis_log(void* handle, double* rows, int max_rows);
+/* Outer window of the last cdisentangle per k: ndimwin[nk] states from band nfirstwin[nk]
+ * (0-based) -- dis_manifold%ndimwin / nfirstwin, and lwindow(i,k) = nfirstwin <= i <
+ * nfirstwin + ndimwin, as the checkpoint stores them. */
+void w90g_get_dis_windows(void* handle, int* ndimwin, int* nfirstwin);
 /* (final Omega_I = omega%invariant, converged 0/1, iterations, most Jacobi sweeps of a
  *  Z eigenproblem) of the last cdisentangle */
 void w90g_get_dis_info(void* handle, double* info4);

@@ -28,3 +28,40 @@ def test_cli_seed_files_to_chk(tmp_path, precision):
     # near the minimum the gauge is only fixed to ~sqrt(per-step roundoff): 1e-7 for the
     # FP64 path, up to a few 1e-6 for the tensor path (M update sliced to 2^-49 of the scales)
     np.testing.assert_allclose(synth.to_math_u(chk["u"]), r.U, atol=1e-7 if precision == "fp64" else 5e-6)
+
+
+@pytest.mark.parametrize("name", ["silicon_dis"])
+def test_cli_entangled_seed_files(tmp_path, name):
+    """Entangled bands through the file flow: .win (dis_* keywords) / .mmn / .amn / .eig ->
+    cdisentangle + cwannierise -> a disentangled .chk; against the reference's printed
+    final Omega_I and centres."""
+    from tests import golden_cases as G
+    d = G.load(name)
+    kn = d["knobs"]
+    ss = int(kn["search_shells"])
+    km = O.kmesh_get(d["real_lattice"], d["kpt_latt"], ss)
+    M = G.assemble_m(d, km["nnlist"], km["nncell"])
+    dc = G.dis_control(d)
+    ctl = G.control(d)
+    nb, nw, K = int(d["num_bands"]), int(kn["num_wann"]), len(d["kpt_latt"])
+    seed = str(tmp_path / name)
+    kw = dict(num_iter=ctl.num_iter, conv_tol=ctl.conv_tol, trial_step=ctl.trial_step, search_shells=ss,
+              iprint=0, dis_num_iter=dc.num_iter, dis_mix_ratio=dc.mix_ratio, dis_conv_tol=dc.conv_tol,
+              dis_conv_window=dc.conv_window, dis_win_max=dc.win_max, dis_froz_max=dc.froz_max)
+    w90io.write_win(seed + ".win", d["real_lattice"], d["kpt_latt"], d["mp_grid"], nw, num_bands=nb, **kw)
+    w90io.write_mmn(seed + ".mmn", synth.from_math_m(M), km["nnlist"], km["nncell"])
+    w90io.write_amn(seed + ".amn", synth.from_math_u(d["amn"]))
+    w90io.write_eig(seed + ".eig", np.asfortranarray(d["eig"].T))
+    assert cli.run(seed, "fp64") == 0
+    chk = w90io.read_chk(seed + ".chk")
+    assert chk["have_disentangled"] and chk["num_bands"] == nb and chk["num_wann"] == nw
+    assert abs(chk["omega_invariant"] - d["omega_i_final"][0]) < 1e-8
+    win = O.dis_windows(d["eig"], nw, dc)
+    np.testing.assert_array_equal(chk["ndimwin"], win["ndimwin"])
+    for k in range(K):
+        f, n = win["nfirstwin"][k], win["ndimwin"][k]
+        assert chk["lwindow"][f:f + n, k].all() and chk["lwindow"][:, k].sum() == n
+    np.testing.assert_allclose(chk["centres"].T, d["centres_final"][:, :3], atol=1.01e-6)
+    uo = synth.to_math_u(chk["u_opt"])
+    for k in range(K):
+        np.testing.assert_allclose(uo[k].conj().T @ uo[k], np.eye(nw), atol=1e-12)

@@ -76,3 +76,40 @@ def test_chk_layout(tmp_path):
     # first record: 4-byte marker 33, 33-byte header, marker 33 (Fortran sequential)
     raw = open(f, "rb").read(41)
     assert struct.unpack("<i", raw[:4])[0] == 33 and struct.unpack("<i", raw[37:41])[0] == 33
+
+
+def test_chk_disentangled_records(tmp_path):
+    """have_disentangled = T adds omega_invariant, lwindow(nb,nk), ndimwin(nk) and
+    u_matrix_opt(nb,nw,nk) before U (src/wannier90_readwrite.F90:2356-2363)."""
+    p = _small()
+    nb, nw, nk = 8, 5, 27
+    rng = np.random.default_rng(3)
+    u = np.asfortranarray(np.broadcast_to(np.eye(nw, dtype=complex)[:, :, None], (nw, nw, nk)).copy())
+    uopt = np.asfortranarray(rng.standard_normal((nb, nw, nk)) + 1j * rng.standard_normal((nb, nw, nk)))
+    ndim = rng.integers(nw, nb + 1, nk).astype(np.int32)
+    lwin = np.zeros((nb, nk), dtype=bool, order="F")
+    for k in range(nk):
+        lwin[:ndim[k], k] = True
+    cen = np.asfortranarray(np.arange(3 * nw, dtype=float).reshape(3, nw))
+    f = str(tmp_path / "d.chk")
+    w90io.write_chk(f, num_bands=nb, lattice=p.real_lattice, kpts=p.kpoints, mp_grid=(3, 3, 3), nntot=p.nntot,
+                    num_wann=nw, u=u, m=p.m, centres=cen, spreads=np.ones(nw),
+                    dis=dict(omega_invariant=12.5, lwindow=lwin, ndimwin=ndim, u_opt=uopt))
+    r = w90io.read_chk(f)
+    assert r["have_disentangled"] and r["omega_invariant"] == 12.5
+    np.testing.assert_array_equal(r["lwindow"], lwin)
+    np.testing.assert_array_equal(r["ndimwin"], ndim)
+    np.testing.assert_array_equal(r["u_opt"], uopt)
+    np.testing.assert_array_equal(r["u"], u)
+    np.testing.assert_array_equal(r["m"], p.m)
+
+
+def test_win_dis_keywords(tmp_path):
+    p = _small()
+    f = str(tmp_path / "w.win")
+    w90io.write_win(f, p.real_lattice, p.kpoints, (3, 3, 3), 4, num_bands=9, dis_win_max=17.0,
+                    dis_froz_max=6.4, dis_num_iter=120, dis_mix_ratio=1.0, dis_conv_tol=1e-10, dis_conv_window=3)
+    _, _, o = w90io.win_system(f)
+    assert o["num_bands"] == 9 and o["dis_num_iter"] == 120 and o["dis_conv_window"] == 3
+    assert o["dis_win_max"] == 17.0 and o["dis_froz_max"] == 6.4 and o["dis_mix_ratio"] == 1.0
+    assert o["dis_conv_tol"] == 1e-10 and "dis_win_min" not in o

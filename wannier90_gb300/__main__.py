@@ -1,9 +1,13 @@
-"""``python -m wannier90_gb300 seedname``: the wannier90.x flow for isolated bands.
+"""``python -m wannier90_gb300 seedname``: the wannier90.x flow (src/wannier_prog.F90).
 
-Reads ``seedname.win``, builds the k-mesh, reads ``seedname.mmn`` / ``seedname.amn``
-(the projections are read into u_matrix, src/wannier_prog.F90:523-529), runs the
-Loewdin projection and wann_main on the GPU, prints the wannierise section of the
-.wout when iprint > 0, and writes ``seedname.chk`` (src/wannier_prog.F90:256-275).
+Reads ``seedname.win``, builds the k-mesh, reads ``seedname.mmn`` / ``seedname.amn``.
+Isolated bands (num_bands = num_wann): the projections are read into u_matrix
+(src/wannier_prog.F90:523-529) and the Loewdin projection runs.  Entangled bands
+(num_bands > num_wann): ``seedname.eig`` is read too, the projections go into u_opt
+and the disentanglement (dis_main + setup_m_loc) runs with the ``dis_*`` keywords of
+the .win.  Then wann_main runs on the GPU, the wannierise section of the .wout is printed
+when iprint > 0, and ``seedname.chk`` is written (src/wannier_prog.F90:256-275), with
+Omega_I, lwindow, ndimwin and U_opt after a disentanglement.
 Options: ``--precision tensor|fp64`` (default tensor).
 """
 from __future__ import annotations
@@ -21,8 +25,6 @@ def run(seedname, precision="tensor"):
     lattice, kpts, opts = w90io.win_system(seedname + ".win")
     nw = int(opts.pop("num_wann"))
     nb = int(opts.pop("num_bands", nw))
-    if nb != nw:
-        raise SystemExit("disentanglement (num_bands > num_wann) is not supported by the GPU engine")
     mp = opts.pop("mp_grid", None)
     opts.setdefault("iprint", 1)
     opts["gpu_tensor"] = 1 if precision == "tensor" else 0
@@ -32,19 +34,37 @@ def run(seedname, precision="tensor"):
     gkpb = np.transpose(w90.w90_get_gkpb(c, K), (1, 2, 0))
     m = w90io.read_mmn(seedname + ".mmn", nnkp, gkpb)
     a = w90io.read_amn(seedname + ".amn")
-    u = np.asfortranarray(a[:, :nw, :].copy())
-    uopt = np.asfortranarray(np.broadcast_to(np.eye(nb, nw, dtype=np.complex128)[:, :, None], (nb, nw, K)).copy())
-    w90.w90_set_m_local(c, m)
-    w90.w90_set_u_matrix(c, u)
-    w90.w90_set_u_opt(c, uopt)
-    w90.check(c, w90.w90_project_overlap(c), "w90_project_overlap")
+    dis = None
+    if nb > nw:
+        eig = w90io.read_eig(seedname + ".eig", nb, K)
+        u = np.zeros((nw, nw, K), dtype=np.complex128, order="F")
+        uopt = np.asfortranarray(a[:, :nw, :].copy())
+        w90.w90_set_eigval(c, eig)
+        w90.w90_set_m_local(c, m)
+        w90.w90_set_u_matrix(c, u)
+        w90.w90_set_u_opt(c, uopt)
+        w90.check(c, w90.w90_disentangle(c), "w90_disentangle")
+        ndim, nfirst = w90.w90_get_dis_windows(c, K)
+        lwindow = np.zeros((nb, K), dtype=bool, order="F")
+        for k in range(K):
+            lwindow[nfirst[k]:nfirst[k] + ndim[k], k] = True
+        dis = dict(omega_invariant=w90.w90_get_dis_info(c)["omega_invariant"], lwindow=lwindow, ndimwin=ndim,
+                   u_opt=uopt)
+    else:
+        u = np.asfortranarray(a[:, :nw, :].copy())
+        uopt = np.asfortranarray(np.broadcast_to(np.eye(nb, nw, dtype=np.complex128)[:, :, None],
+                                                 (nb, nw, K)).copy())
+        w90.w90_set_m_local(c, m)
+        w90.w90_set_u_matrix(c, u)
+        w90.w90_set_u_opt(c, uopt)
+        w90.check(c, w90.w90_project_overlap(c), "w90_project_overlap")
     ierr = w90.w90_wannierise(c)
     w90.check(c, ierr, "w90_wannierise")
     centres = w90.w90_get_centres(c, nw)
     spreads = w90.w90_get_spreads(c, nw)
     w90io.write_chk(seedname + ".chk", num_bands=nb, lattice=lattice, kpts=kpts,
                     mp_grid=mp if mp is not None else (0, 0, 0), nntot=w90.w90_get_nn(c), num_wann=nw,
-                    u=u, m=m, centres=centres, spreads=spreads)
+                    u=u, m=np.asfortranarray(m[:nw, :nw]), centres=centres, spreads=spreads, dis=dis)
     return ierr
 
 

@@ -42,6 +42,7 @@ SIGNATURES = [
     ("w90g_get_log_centres", C.c_int, [C.c_void_p, _c_double_p, C.c_int]),
     ("w90g_get_dis_log", C.c_int, [C.c_void_p, _c_double_p, C.c_int]),
     ("w90g_get_dis_info", None, [C.c_void_p, _c_double_p]),
+    ("w90g_get_dis_windows", None, [C.c_void_p, _c_int_p, _c_int_p]),
     ("w90g_disentangle_device", None, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, _c_int_p]),
     ("w90g_profile_dis_device", C.c_int,
      [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, _c_double_p, _c_int_p]),

@@ -77,6 +77,7 @@ struct Handle {
   std::vector<double> dis_log;
   long long dis_launches = 0;
   int dis_max_sweeps = 0;
+  std::vector<int> dis_ndimwin, dis_nfirstwin;
   // results
   bool have_result = false;
   double omega[4] = {0, 0, 0, 0};
@@ -352,6 +353,8 @@ int do_disentangle(Handle* h, double* m, double* uopt, double* u, const double* 
   h->dis_converged = r.converged;
   h->dis_log = r.log;
   h->dis_max_sweeps = r.max_sweeps;
+  h->dis_ndimwin = r.ndimwin;
+  h->dis_nfirstwin = r.nfirstwin;
   h->have_disentangled = true;
   if (h->iprint > 0) {
     const char* bar = "+---------------------------------------------------------------------+<-- DIS";
@@ -903,6 +906,12 @@ int w90g_get_dis_log(void* hv, double* rows, int max_rows) {
   const int n = std::min(max_rows, (int)(h->dis_log.size() / w90g::kDisLogStride));
   std::copy(h->dis_log.begin(), h->dis_log.begin() + (size_t)n * w90g::kDisLogStride, rows);
   return n;
+}
+
+void w90g_get_dis_windows(void* hv, int* ndimwin, int* nfirstwin) {
+  Handle* h = H(hv);
+  std::copy(h->dis_ndimwin.begin(), h->dis_ndimwin.end(), ndimwin);
+  std::copy(h->dis_nfirstwin.begin(), h->dis_nfirstwin.end(), nfirstwin);
 }
 
 void w90g_get_dis_info(void* hv, double* info4) {

@@ -203,6 +203,15 @@ def w90_get_dis_log(common: LibCommon, max_rows: int) -> np.ndarray:
     return out[:n]
 
 
+def w90_get_dis_windows(common: LibCommon, num_kpts: int):
+    """(ndimwin[nk], nfirstwin[nk] 0-based) of the last w90_disentangle's outer window."""
+    nd = np.zeros(num_kpts, dtype=np.int32)
+    nf = np.zeros(num_kpts, dtype=np.int32)
+    common._L.w90g_get_dis_windows(common._h, nd.ctypes.data_as(C.POINTER(C.c_int)),
+                                   nf.ctypes.data_as(C.POINTER(C.c_int)))
+    return nd, nf
+
+
 def w90_get_dis_info(common: LibCommon) -> dict:
     """Final Omega_I (omega%invariant), convergence flag, iteration count and the most
     Jacobi sweeps one Z eigenproblem took."""

@@ -79,8 +79,10 @@ def win_system(path):
     kpts = np.array([[_fnum(x) for x in r.split()[:3]] for r in blocks["kpoints"]])
     opts = {}
     ints = ("num_wann", "num_bands", "num_iter", "num_cg_steps", "conv_window", "search_shells",
-            "iprint", "num_print_cycles", "conv_noise_num")
-    reals = ("conv_tol", "trial_step", "fixed_step", "conv_noise_amp", "kmesh_tol")
+            "iprint", "num_print_cycles", "conv_noise_num", "dis_num_iter", "dis_conv_window",
+            "dis_spheres_num")
+    reals = ("conv_tol", "trial_step", "fixed_step", "conv_noise_amp", "kmesh_tol", "dis_win_min",
+             "dis_win_max", "dis_froz_min", "dis_froz_max", "dis_mix_ratio", "dis_conv_tol")
     bools = ("precond", "guiding_centres", "gamma_only")
     for k in ints:
         if k in kw:
@@ -255,8 +257,10 @@ def recip_lattice(lattice):
 
 
 def write_chk(path, *, num_bands, lattice, kpts, mp_grid, nntot, num_wann, u, m, centres, spreads,
-              exclude_bands=(), checkpoint="postwann", header=None):
-    """centres (3, num_wann) Angstrom; u (nw,nw,nk); m (nw,nw,nntot,nk)."""
+              exclude_bands=(), checkpoint="postwann", header=None, dis=None):
+    """centres (3, num_wann) Angstrom; u (nw,nw,nk); m (nw,nw,nntot,nk).  dis: None, or
+    for a disentangled run dict(omega_invariant, lwindow (nb,nk) bool, ndimwin (nk),
+    u_opt (nb,nw,nk))."""
     if header is None:
         now = datetime.datetime.now()
         header = "written on " + now.strftime("%d%b%Y") + " at " + now.strftime("%H:%M:%S")
@@ -275,7 +279,12 @@ def write_chk(path, *, num_bands, lattice, kpts, mp_grid, nntot, num_wann, u, m,
         _rec(f, struct.pack("<i", nntot))
         _rec(f, struct.pack("<i", num_wann))
         _rec(f, checkpoint.ljust(20)[:20].encode())
-        _rec(f, struct.pack("<i", 0))                                               # have_disentangled = F
+        _rec(f, struct.pack("<i", 1 if dis is not None else 0))                     # have_disentangled
+        if dis is not None:
+            _rec(f, struct.pack("<d", float(dis["omega_invariant"])))
+            _rec(f, np.asarray(dis["lwindow"], dtype="<i4").reshape(-1, order="F").tobytes())
+            _rec(f, np.asarray(dis["ndimwin"], dtype="<i4").tobytes())
+            _rec(f, np.asarray(dis["u_opt"], dtype="<c16").reshape(-1, order="F").tobytes())
         _rec(f, np.asarray(u, dtype="<c16").reshape(-1, order="F").tobytes())
         _rec(f, np.asarray(m, dtype="<c16").reshape(-1, order="F").tobytes())
         _rec(f, np.asarray(centres, dtype="<f8").reshape(-1, order="F").tobytes())
@@ -283,7 +292,7 @@ def write_chk(path, *, num_bands, lattice, kpts, mp_grid, nntot, num_wann, u, m,
 
 
 def read_chk(path):
-    """Parse a .chk written by write_chk (or by wannier90.x for isolated bands)."""
+    """Parse a .chk written by write_chk or by wannier90.x."""
     recs = []
     with open(path, "rb") as f:
         while True:
@@ -308,8 +317,13 @@ def read_chk(path):
     nw = struct.unpack("<i", recs[i])[0]; i += 1
     out["checkpoint"] = recs[i].decode().strip(); i += 1
     have_dis = struct.unpack("<i", recs[i])[0]; i += 1
+    out["have_disentangled"] = bool(have_dis)
     if have_dis:
-        raise ValueError("disentangled checkpoints are not supported")
+        nb = out["num_bands"]
+        out["omega_invariant"] = struct.unpack("<d", recs[i])[0]; i += 1
+        out["lwindow"] = np.frombuffer(recs[i], "<i4").reshape(nb, nk, order="F").astype(bool); i += 1
+        out["ndimwin"] = np.frombuffer(recs[i], "<i4").copy(); i += 1
+        out["u_opt"] = np.frombuffer(recs[i], "<c16").reshape(nb, nw, nk, order="F").copy(); i += 1
     out["u"] = np.frombuffer(recs[i], "<c16").reshape(nw, nw, nk, order="F").copy(); i += 1
     out["m"] = np.frombuffer(recs[i], "<c16").reshape(nw, nw, nntot, nk, order="F").copy(); i += 1
     out["centres"] = np.frombuffer(recs[i], "<f8").reshape(3, nw, order="F").copy(); i += 1
