@@ -139,6 +139,17 @@ void w90g_project_overlap_device(void* handle, double* d_m_matrix, double* d_u_m
 void w90g_wannierise_batch_device(void** handles, int nprob, double** d_m, double** d_u, int* ierr);
 /* Run the engine's work on a caller-provided cudaStream_t (NULL = the engine's own). */
 void w90g_set_stream(void* handle, void* cuda_stream);
+/* ---- seed files: overlap_read (src/overlap.F90:234-366) and the .eig reader
+ *      (src/readwrite.F90:583-635), parsed in parallel on the host ------------------------
+ * m: complex (nb, nb, nntot, nk); each block (k, k2, G) of the file is placed at the slot nn
+ * with nnlist[k][nn] = k2 (0-based) and nncell[k][nn][0..2] = G, as cget_nnkp / cget_gkpb
+ * give them.  a: complex (nb, nproj, nk).  eig: (nb, nk).  nthreads 0 = all cores.
+ * Return 0, or 6 (file error) with the reference's message in err (errlen bytes). */
+int w90g_read_mmn(const char* path, int nb, int nk, int nntot, const int* nnlist, const int* nncell,
+                  double* m_matrix, int nthreads, char* err, int errlen);
+int w90g_read_amn(const char* path, int nb, int nproj, int nk, double* a_matrix, int nthreads, char* err,
+                  int errlen);
+int w90g_read_eig(const char* path, int nb, int nk, double* eigval, char* err, int errlen);
 /* Kernels launched by the last wannierisation plus the last disentanglement on this handle. */
 long long w90g_kernel_launches(void* handle);
 /* Profiling run of wannierise on device buffers: every kernel launched alone and timed

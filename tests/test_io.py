@@ -113,3 +113,78 @@ def test_win_dis_keywords(tmp_path):
     assert o["num_bands"] == 9 and o["dis_num_iter"] == 120 and o["dis_conv_window"] == 3
     assert o["dis_win_max"] == 17.0 and o["dis_froz_max"] == 6.4 and o["dis_mix_ratio"] == 1.0
     assert o["dis_conv_tol"] == 1e-10 and "dis_win_min" not in o
+
+
+def _fortranish(path):
+    """Rewrite a seed file the way other writers format it: 'D' exponents, commas, a blank
+    record every few records, trailing items after the values."""
+    lines = open(path).read().split("\n")
+    out = lines[:2]
+    for i, l in enumerate(lines[2:]):
+        p = l.split()
+        if len(p) == 2:
+            out.append(("  %.14E, %.14E   trailing" % (float(p[0]), float(p[1]))).replace("E", "D"))
+        else:
+            out.append(l)
+        if i % 7 == 3:
+            out.append("   ")
+    open(path, "w").write("\n".join(out))
+
+
+@pytest.mark.parametrize("threads", [1, 3, 0])
+def test_native_readers_match_record_reader(tmp_path, threads):
+    """The parallel native .mmn/.amn/.eig readers against the record-by-record checker,
+    bit for bit, on plain files and on files with D exponents, commas, blank records and
+    trailing items; any thread count gives the same arrays."""
+    from tests import seed_reference as R
+    p = _small()
+    f = str(tmp_path / "s")
+    w90io.write_mmn(f + ".mmn", p.m, p.nnlist, p.nncell)
+    w90io.write_amn(f + ".amn", p.a)
+    eig = np.asfortranarray(np.sort(np.random.default_rng(2).standard_normal((5, 27)), axis=0))
+    w90io.write_eig(f + ".eig", eig)
+    for variant in (False, True):
+        if variant:
+            _fortranish(f + ".mmn")
+        m = w90io.read_mmn(f + ".mmn", p.nnlist, p.nncell, nthreads=threads)
+        np.testing.assert_array_equal(m, R.read_mmn(f + ".mmn", p.nnlist, p.nncell))
+    np.testing.assert_array_equal(w90io.read_amn(f + ".amn", nthreads=threads), R.read_amn(f + ".amn"))
+    np.testing.assert_array_equal(w90io.read_eig(f + ".eig", 5, 27), R.read_eig(f + ".eig", 5, 27))
+
+
+def test_native_reader_errors_and_duplicates(tmp_path):
+    """overlap_read's checks: neighbour count, a block whose (k2, G) is no neighbour, a
+    truncated file; when two blocks name the same neighbour slot the later one wins, as in
+    a sequential read; the .eig band/k order check."""
+    from tests import seed_reference as R
+    p = _small()
+    f = str(tmp_path / "e")
+    w90io.write_mmn(f + ".mmn", p.m, p.nnlist, p.nncell)
+    with pytest.raises(ValueError, match="number of k-points|nearest neighbours"):
+        w90io.read_mmn(f + ".mmn", p.nnlist[:, :-1], p.nncell[:, :-1])
+    bad = np.array(p.nncell)
+    bad[0, :, 0] += 7
+    with pytest.raises(ValueError, match="Neighbour not found"):
+        w90io.read_mmn(f + ".mmn", p.nnlist, bad)
+    txt = open(f + ".mmn").read().split("\n")
+    open(f + "_t.mmn", "w").write("\n".join(txt[: len(txt) // 2]))
+    with pytest.raises(ValueError, match="Problem reading"):
+        w90io.read_mmn(f + "_t.mmn", p.nnlist, p.nncell)
+    # block 1 relabelled as block 0's (k, k2, G): slot of block 0 takes block 1's values
+    nb = p.m.shape[0]
+    per = 1 + nb * nb
+    dup = list(txt)
+    dup[2 + per] = txt[2]
+    open(f + "_d.mmn", "w").write("\n".join(dup))
+    m = w90io.read_mmn(f + "_d.mmn", p.nnlist, p.nncell, nthreads=4)
+    np.testing.assert_array_equal(m, R.read_mmn(f + "_d.mmn", p.nnlist, p.nncell))
+    k0, k1 = 0, 0
+    b0, b1 = 0, 1
+    np.testing.assert_allclose(m[:, :, b0, k0], p.m[:, :, b1, k1], atol=1e-12)
+    assert not m[:, :, b1, k1].any()
+    w90io.write_eig(f + ".eig", np.zeros((5, 27)))
+    t = open(f + ".eig").read().split("\n")
+    t[3], t[4] = t[4], t[3]
+    open(f + ".eig", "w").write("\n".join(t))
+    with pytest.raises(ValueError, match="mismatch"):
+        w90io.read_eig(f + ".eig", 5, 27)

@@ -26,6 +26,7 @@
 #include "dis.h"
 #include "engine.h"
 #include "kmesh.h"
+#include "seedio.h"
 
 namespace {
 
@@ -1162,6 +1163,36 @@ void w90g_server_delete(void* server) {
   if (sv->d_flags) cudaFree(sv->d_flags);
   if (sv->h_flags) cudaFreeHost(sv->h_flags);
   delete sv;
+}
+
+// ---- seed-file readers (no handle: plain arrays; err receives the message) ----------
+static void put_err(const std::string& e, char* err, int errlen) {
+  if (err && errlen > 0) {
+    std::strncpy(err, e.c_str(), (size_t)errlen - 1);
+    err[errlen - 1] = '\0';
+  }
+}
+
+int w90g_read_mmn(const char* path, int nb, int nk, int nntot, const int* nnlist, const int* nncell, double* m,
+                  int nthreads, char* err, int errlen) {
+  std::string e;
+  const int rc = w90g::read_mmn(path, nb, nk, nntot, nnlist, nncell, m, nthreads, e);
+  put_err(e, err, errlen);
+  return rc;
+}
+
+int w90g_read_amn(const char* path, int nb, int nproj, int nk, double* a, int nthreads, char* err, int errlen) {
+  std::string e;
+  const int rc = w90g::read_amn(path, nb, nproj, nk, a, nthreads, e);
+  put_err(e, err, errlen);
+  return rc;
+}
+
+int w90g_read_eig(const char* path, int nb, int nk, double* eig, char* err, int errlen) {
+  std::string e;
+  const int rc = w90g::read_eig(path, nb, nk, eig, e);
+  put_err(e, err, errlen);
+  return rc;
 }
 
 long long w90g_kernel_launches(void* hv) {

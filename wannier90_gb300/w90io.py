@@ -162,28 +162,33 @@ def write_win(path, lattice, kpts, mp_grid, num_wann, num_bands=None, **keywords
 # --------------------------------------------------------------------------------
 # .mmn / .amn / .eig   (src/overlap.F90:234-366)
 # --------------------------------------------------------------------------------
-def read_mmn(path, nnlist, nncell):
-    """Overlaps placed at (k, nn) by matching each block's (k2, G) with the k-mesh tables,
-    as overlap_read does.  nnlist (K,B) 0-based, nncell (K,B,3)."""
-    nnlist = np.asarray(nnlist)
-    nncell = np.asarray(nncell)
+def _header(path):
     with open(path) as f:
         f.readline()
-        nb, nk, nntot = (int(x) for x in f.readline().split())
-        if nnlist.shape != (nk, nntot):
-            raise ValueError(".mmn has not the right number of k-points / nearest neighbours")
-        m = np.zeros((nb, nb, nntot, nk), dtype=np.complex128, order="F")
-        data = np.loadtxt(f, ndmin=2) if False else None
-        for _ in range(nk * nntot):
-            head = f.readline().split()
-            k, k2 = int(head[0]) - 1, int(head[1]) - 1
-            g = tuple(int(x) for x in head[2:5])
-            vals = np.array([[float(x) for x in f.readline().split()[:2]] for _ in range(nb * nb)])
-            blk = (vals[:, 0] + 1j * vals[:, 1]).reshape(nb, nb, order="F")   # (m, n), m fastest
-            hit = [b for b in range(nntot) if nnlist[k, b] == k2 and tuple(nncell[k, b]) == g]
-            if len(hit) != 1:
-                raise ValueError("Error reading %s: neighbour not found / not unique" % path)
-            m[:, :, hit[0], k] = blk
+        return [int(x) for x in f.readline().split()[:3]]
+
+
+def _check(rc, err):
+    if rc:
+        raise ValueError(err.value.decode())
+
+
+def read_mmn(path, nnlist, nncell, nthreads=0):
+    """Overlaps placed at (k, nn) by matching each block's (k2, G) with the k-mesh tables,
+    as overlap_read does.  nnlist (K,B) 0-based, nncell (K,B,3).  Parsed in parallel by the
+    native reader (w90g_read_mmn)."""
+    import ctypes as C
+
+    from ._native import lib
+    nnlist = np.ascontiguousarray(nnlist, dtype=np.int32)
+    nncell = np.ascontiguousarray(nncell, dtype=np.int32)
+    nb, nk, nntot = _header(path)
+    if nnlist.shape != (nk, nntot):
+        raise ValueError(".mmn has not the right number of k-points / nearest neighbours")
+    m = np.zeros((nb, nb, nntot, nk), dtype=np.complex128, order="F")
+    err = C.create_string_buffer(512)
+    _check(lib().w90g_read_mmn(path.encode(), nb, nk, nntot, nnlist.ctypes.data_as(C.POINTER(C.c_int)),
+                               nncell.ctypes.data_as(C.POINTER(C.c_int)), m.ctypes.data, nthreads, err, 512), err)
     return m
 
 
@@ -201,14 +206,15 @@ def write_mmn(path, m, nnlist, nncell, comment="written by wannier90_gb300"):
                     f.write("%18.12f%18.12f\n" % (z.real, z.imag))
 
 
-def read_amn(path):
-    with open(path) as f:
-        f.readline()
-        nb, nk, npj = (int(x) for x in f.readline().split())
-        a = np.zeros((nb, npj, nk), dtype=np.complex128, order="F")
-        for _ in range(nb * npj * nk):
-            p = f.readline().split()
-            a[int(p[0]) - 1, int(p[1]) - 1, int(p[2]) - 1] = float(p[3]) + 1j * float(p[4])
+def read_amn(path, nthreads=0):
+    """Projections A(m, n, k), parsed in parallel by the native reader (w90g_read_amn)."""
+    import ctypes as C
+
+    from ._native import lib
+    nb, nk, npj = _header(path)
+    a = np.zeros((nb, npj, nk), dtype=np.complex128, order="F")
+    err = C.create_string_buffer(512)
+    _check(lib().w90g_read_amn(path.encode(), nb, npj, nk, a.ctypes.data, nthreads, err, 512), err)
     return a
 
 
@@ -225,11 +231,13 @@ def write_amn(path, a, comment="written by wannier90_gb300"):
 
 
 def read_eig(path, num_bands, num_kpts):
+    """Band energies eig(n, k) with the reference's band/k-point order check."""
+    import ctypes as C
+
+    from ._native import lib
     e = np.zeros((num_bands, num_kpts), order="F")
-    for line in open(path):
-        p = line.split()
-        if len(p) >= 3:
-            e[int(p[0]) - 1, int(p[1]) - 1] = float(p[2])
+    err = C.create_string_buffer(512)
+    _check(lib().w90g_read_eig(path.encode(), num_bands, num_kpts, e.ctypes.data, err, 512), err)
     return e
 
 
