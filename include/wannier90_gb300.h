@@ -150,6 +150,17 @@ int w90g_read_mmn(const char* path, int nb, int nk, int nntot, const int* nnlist
 int w90g_read_amn(const char* path, int nb, int nproj, int nk, double* a_matrix, int nthreads, char* err,
                   int errlen);
 int w90g_read_eig(const char* path, int nb, int nk, double* eigval, char* err, int errlen);
+/* .mmn straight into DEVICE memory d_m_matrix (same layout), parsed on the GPU on the
+ * caller's stream (NULL = default stream): records indexed and numbers converted by
+ * kernels (Clinger's exact fast path); a file outside that path (more than 19 digits or
+ * 2^53 in a mantissa, exponents beyond 10^+-22, blank records, two blocks for one slot)
+ * is read by w90g_read_mmn and copied, with the same result.  *used_gpu: 1 if the
+ * kernels parsed it; *launches: kernels launched; timing3 (NULL or 3 doubles): ms of the
+ * value-conversion kernel, of all parse kernels, of the text copy.  Return as
+ * w90g_read_mmn. */
+int w90g_read_mmn_device(const char* path, int nb, int nk, int nntot, const int* nnlist, const int* nncell,
+                         double* d_m_matrix, void* cuda_stream, int* used_gpu, long long* launches,
+                         double* timing3, char* err, int errlen);
 /* Kernels launched by the last wannierisation plus the last disentanglement on this handle. */
 long long w90g_kernel_launches(void* handle);
 /* Profiling run of wannierise on device buffers: every kernel launched alone and timed

@@ -47,6 +47,9 @@ SIGNATURES = [
                                 C.c_char_p, C.c_int]),
     ("w90g_read_amn", C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_char_p, C.c_int]),
     ("w90g_read_eig", C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_void_p, C.c_char_p, C.c_int]),
+    ("w90g_read_mmn_device", C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_int, _c_int_p, _c_int_p, C.c_void_p,
+                                       C.c_void_p, _c_int_p, C.POINTER(C.c_longlong), _c_double_p, C.c_char_p,
+                                       C.c_int]),
     ("w90g_disentangle_device", None, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, _c_int_p]),
     ("w90g_profile_dis_device", C.c_int,
      [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, _c_double_p, _c_int_p]),

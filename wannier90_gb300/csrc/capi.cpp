@@ -1188,6 +1188,20 @@ int w90g_read_amn(const char* path, int nb, int nproj, int nk, double* a, int nt
   return rc;
 }
 
+int w90g_read_mmn_device(const char* path, int nb, int nk, int nntot, const int* nnlist, const int* nncell,
+                         double* d_m, void* stream, int* used_gpu, long long* launches, double* timing3, char* err,
+                         int errlen) {
+  std::string e;
+  int ug = 0;
+  long long nl = 0;
+  const int rc =
+      w90g::read_mmn_device(path, nb, nk, nntot, nnlist, nncell, d_m, (cudaStream_t)stream, &ug, &nl, timing3, e);
+  if (used_gpu) *used_gpu = ug;
+  if (launches) *launches = nl;
+  put_err(e, err, errlen);
+  return rc;
+}
+
 int w90g_read_eig(const char* path, int nb, int nk, double* eig, char* err, int errlen) {
   std::string e;
   const int rc = w90g::read_eig(path, nb, nk, eig, e);

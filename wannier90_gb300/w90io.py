@@ -206,6 +206,30 @@ def write_mmn(path, m, nnlist, nncell, comment="written by wannier90_gb300"):
                     f.write("%18.12f%18.12f\n" % (z.real, z.imag))
 
 
+def read_mmn_device(path, nnlist, nncell, d_m, stream=0, timing=None):
+    """.mmn parsed on the GPU into the device buffer at address d_m (complex128,
+    (nb, nb, nntot, nk) column-major; e.g. a torch tensor's data_ptr()).  Returns
+    (used_gpu, kernels launched); `timing` (a float64 array of 3) receives the ms of the
+    value-conversion kernel, of all parse kernels and of the text copy."""
+    import ctypes as C
+
+    from ._native import lib
+    nnlist = np.ascontiguousarray(nnlist, dtype=np.int32)
+    nncell = np.ascontiguousarray(nncell, dtype=np.int32)
+    nb, nk, nntot = _header(path)
+    if nnlist.shape != (nk, nntot):
+        raise ValueError(".mmn has not the right number of k-points / nearest neighbours")
+    err = C.create_string_buffer(512)
+    used = C.c_int(0)
+    nl = C.c_longlong(0)
+    _check(lib().w90g_read_mmn_device(path.encode(), nb, nk, nntot, nnlist.ctypes.data_as(C.POINTER(C.c_int)),
+                                      nncell.ctypes.data_as(C.POINTER(C.c_int)), C.c_void_p(d_m),
+                                      C.c_void_p(stream), C.byref(used), C.byref(nl),
+                                      None if timing is None else timing.ctypes.data_as(C.POINTER(C.c_double)),
+                                      err, 512), err)
+    return bool(used.value), int(nl.value)
+
+
 def read_amn(path, nthreads=0):
     """Projections A(m, n, k), parsed in parallel by the native reader (w90g_read_amn)."""
     import ctypes as C
