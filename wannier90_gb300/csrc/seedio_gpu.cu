@@ -143,17 +143,45 @@ __global__ void k_seed_scan(int* counts, int nc, int* total) {
   if (t == 1023) *total = s[1023];
 }
 
-// starts[0] = 0, starts[r+1] = position after the r-th newline (0-based r)
+// starts[0] = 0, starts[r+1] = position after the r-th newline (0-based r).  One warp per
+// 4 KB chunk: lane l scans bytes [l*128, (l+1)*128) of it (eight 16-byte loads), an
+// exclusive shuffle scan of the lanes' newline counts gives each lane its first record.
 __global__ void k_seed_starts(const char* __restrict__ txt, size_t n, const int* __restrict__ offs,
                               long long* __restrict__ starts) {
+  constexpr int kLane = kChunk / 32;
   const size_t c = blockIdx.x;
-  const size_t lo = c * kChunk, hi = min(n, lo + kChunk);
-  if (threadIdx.x == 0) {
-    int r = offs[c];
-    for (size_t i = lo; i < hi; ++i)
-      if (txt[i] == '\n') starts[++r] = (long long)i + 1;
+  const int lane = threadIdx.x;
+  const size_t lo = c * kChunk + (size_t)lane * kLane;
+  const size_t hi = min(n, lo + kLane);
+  // the text buffer is 16-byte aligned (cudaMallocAsync) and chunk / lane spans are
+  // multiples of 16, so whole 16-byte vectors can be loaded up to the last full one
+  int cnt = 0;
+  if (lo < hi) {
+    if (hi - lo == (size_t)kLane) {
+      const uint4* v = reinterpret_cast<const uint4*>(txt + lo);
+#pragma unroll
+      for (int q = 0; q < kLane / 16; ++q) {
+        const uint4 w = v[q];
+        const unsigned int u[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+        for (int h = 0; h < 4; ++h)
+#pragma unroll
+          for (int bt = 0; bt < 4; ++bt) cnt += (((u[h] >> (8 * bt)) & 0xffu) == (unsigned)'\n');
+      }
+    } else {
+      for (size_t i = lo; i < hi; ++i) cnt += (txt[i] == '\n');
+    }
   }
-  if (c == 0 && threadIdx.x == 0) starts[0] = 0;
+  int inc = cnt;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, inc, d);
+    if (lane >= d) inc += y;
+  }
+  int r = offs[c] + inc - cnt;
+  for (size_t i = lo; i < hi; ++i)
+    if (txt[i] == '\n') starts[++r] = (long long)i + 1;
+  if (c == 0 && lane == 0) starts[0] = 0;
 }
 
 // blank-record check over records [first, nrec)
