@@ -42,6 +42,8 @@ __global__ void k_phases(const Problem* probs, int mode);
 cudaError_t oz_launch(int wp, int step, const Problem* probs, WorkMap wm, int which, int grid,
                       cudaStream_t s);
 cudaError_t oz_set_attributes(int wp);
+void oz_preslice_bytes(int wp, int K, int B, size_t* data, size_t* exps);
+cudaError_t oz_preslice_launch(int wp, const Problem* probs, WorkMap wm, int grid, cudaStream_t s);
 cudaError_t oz_exp_launch(int wp, const Problem* probs, WorkMap wm, int which, int grid, cudaStream_t s);
 cudaError_t oz_exp_set_attributes(int wp);
 
@@ -160,11 +162,12 @@ int choose_tensor_wp(const std::vector<ProblemSpec>& specs) {
 
 struct Sizes {
   size_t M, U, KWW, work, tbuf, diag, offd, gpart, cen, log, logc, nn, bk, wb, st, op1, op2, m0, u0, inv, fr;
+  size_t m0s, m0e;
   size_t pkr, pr2, pgr, pgp, ppart;
   size_t gbka, gneigh, grg, gsheet, gcsheet;
   size_t total() const {
     return 2 * M + 2 * U + 3 * KWW + work + tbuf + 2 * diag + offd + gpart + cen + log + logc + nn + bk + wb + st +
-           op1 + op2 + m0 + u0 + inv + fr + pkr + 2 * pr2 + pgr + pgp + ppart + gbka + gneigh + grg + gsheet +
+           op1 + op2 + m0 + u0 + inv + fr + m0s + m0e + pkr + 2 * pr2 + pgr + pgp + ppart + gbka + gneigh + grg + gsheet +
            gcsheet;
   }
 };
@@ -185,6 +188,13 @@ Sizes problem_sizes(const ProblemSpec& s, int wp, int* pc_tiles) {
   z.u0 = wp ? align_up(K * WW * 16) : 0;
   z.inv = wp ? align_up(K * B * 4) : 0;
   z.fr = wp ? align_up(K * B * 8) : 0;
+  z.m0s = z.m0e = 0;
+  if (wp) {
+    size_t d = 0, e = 0;
+    oz_preslice_bytes(wp, (int)K, (int)B, &d, &e);
+    z.m0s = align_up(d);
+    z.m0e = align_up(e);
+  }
   z.diag = align_up(K * B * W * 8);
   z.offd = align_up(K * B * 8);
   z.gpart = align_up(K * nt * nt * 2 * 8);
@@ -322,6 +332,8 @@ int Engine::alloc(std::string& err) {
     P.inv_nnlist = inv;
     P.tensor = tensor_wp_ ? 1 : 0;
     P.frob0 = z.fr ? (double*)take(z.fr) : nullptr;
+    P.m0s = z.m0s ? (unsigned char*)take(z.m0s) : nullptr;
+    P.m0s_exp = z.m0e ? (int*)take(z.m0e) : nullptr;
     if (inv) {
       std::vector<int> h_inv((size_t)s.K * s.B), fill(s.K, 0);
       for (int kb = 0; kb < s.K * s.B; ++kb) {
@@ -494,7 +506,9 @@ int Engine::prepare_tensor(cudaStream_t st, std::string& err) {
   k_u_identity<<<n_k_, 256, 0, st>>>(dprobs_, wmk);
   k_frob0<<<n_kb_, 128, 0, st>>>(dprobs_, wmkb);
   W90G_CHECK(cudaGetLastError());
-  launches_ += 2;
+  // step 1's A operand (the entry overlaps) in digit planes, once per solve
+  W90G_CHECK(oz_preslice_launch(tensor_wp_, dprobs_, wmk, n_k_, st));
+  launches_ += 3;
   return 0;
 }
 

@@ -41,6 +41,48 @@ __device__ __forceinline__ double recombine_digits(const uint32_t* dd, int strid
   return int64_scaled_to_double(acc, escale - 56);
 }
 
+// Row exponents of A tile `tile` (2 threads per row, all 256 threads of the CTA).
+template <int WP, class AElem>
+__device__ __forceinline__ void a_row_exponents(int tile, int W, int* rowexp, AElem&& a_elem) {
+  const int tid = threadIdx.x;
+  const int r = tid >> 1, half = tid & 1;
+  const int row = tile * kTileRows + r;
+  unsigned long long mx = 0ull;
+  for (int m = half; m < W; m += 2) {
+    const double2 a = a_elem(row, m);
+    mx = max(mx, max(abs_bits(a.x), abs_bits(a.y)));
+  }
+  mx = max(mx, (unsigned long long)__shfl_xor_sync(0xffffffffu, (long long)mx, 1));
+  if (half == 0) rowexp[r] = exp_above_bits(mx);
+}
+
+// The kS digit planes of A chunk (tile, kc) in the canonical K-major layout, written to
+// dst (shared memory, or the global image the shared-memory copy is taken from): a warp
+// writes 4 consecutive 16-byte core rows.
+template <int WP, class AElem>
+__device__ __forceinline__ void a_slice_chunk(unsigned char* dst, int tile, int kc, const int* rowexp,
+                                              AElem&& a_elem) {
+  using L = TileSmem<WP>;
+  constexpr int CW = L::CW, KC = L::KC;
+  for (int e = threadIdx.x; e < kTileRows * CW; e += blockDim.x) {
+    const int ln = e & 31, wi = e >> 5;
+    constexpr int mgroups = CW / 8;
+    const int r = (wi / mgroups) * 4 + (ln >> 3);
+    const int l = (wi % mgroups) * 8 + (ln & 7);
+    const double2 a = a_elem(tile * kTileRows + r, kc * CW + l);
+    const int ex = rowexp[r];
+    int xr[kS], xi[kS];
+    split_digits<WP>(a.x, ex, xr);
+    split_digits<WP>(a.y, ex, xi);
+    const uint32_t o_re = kmaj_off(r, l, KC), o_im = kmaj_off(r, l + CW, KC);
+#pragma unroll
+    for (int t = 0; t < kS; ++t) {
+      *(uint16_t*)(dst + (size_t)t * L::A_BYTES + o_re) = int_to_bf16(xr[t]);
+      *(uint16_t*)(dst + (size_t)t * L::A_BYTES + o_im) = int_to_bf16(xi[t]);
+    }
+  }
+}
+
 // STEP 1: group = k.  STEP 2: group = k'.  which: 0 trial, 1 optimal-step pass.
 template <int WP, int STEP>
 __global__ void __launch_bounds__(256, 1) k_oz_mupdate(const Problem* __restrict__ probs, WorkMap wm, int which) {
@@ -51,6 +93,7 @@ __global__ void __launch_bounds__(256, 1) k_oz_mupdate(const Problem* __restrict
   unsigned char* sA = base;                                   // kS slices of an A chunk
   unsigned char* sB = base + (size_t)kS * L::A_BYTES;          // kS slices of a B chunk
   __shared__ __align__(8) uint64_t mbar;
+  __shared__ __align__(8) uint64_t mbar_ld;   // completion of the bulk copies of presliced A
   __shared__ uint32_t tmem_base_slot;
   __shared__ int s_rowexp[kTileRows];
   __shared__ int s_colexp[WP];
@@ -75,6 +118,7 @@ __global__ void __launch_bounds__(256, 1) k_oz_mupdate(const Problem* __restrict
   }
   if (tid == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&mbar)) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&mbar_ld)) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     s_bad = 0;
   }
@@ -124,7 +168,7 @@ __global__ void __launch_bounds__(256, 1) k_oz_mupdate(const Problem* __restrict
   if (NCH == 1) slice_b(0, 0);
   const uint32_t tmem = tmem_base_slot;
   const uint32_t idesc = idesc_bf16(NC);
-  uint32_t phase = 0;
+  uint32_t phase = 0, phase_ld = 0;
 
   // A element (row, complex K index m) of this tile
   auto a_elem = [&](int row, int m) -> double2 {
@@ -135,45 +179,57 @@ __global__ void __launch_bounds__(256, 1) k_oz_mupdate(const Problem* __restrict
     return P.tbuf[(size_t)kb * WW + (size_t)rr * W + m];                          // Z(k,b)(m=rr, j=m), row-major
   };
 
+  // step 1 takes its A operand (the entry overlaps, fixed for the whole solve) from the
+  // digit planes sliced once by k_oz_preslice: the same bytes, copied instead of computed
+  const bool presliced = (STEP == 1) && (P.m0s != nullptr);
   for (int tile = 0; tile < ntiles; ++tile) {
     // ---- row scales over the full row (2 threads per row)
-    {
-      const int r = tid >> 1, half = tid & 1;
-      const int row = tile * kTileRows + r;
-      unsigned long long mx = 0ull;
-      for (int m = half; m < W; m += 2) {
-        const double2 a = a_elem(row, m);
-        mx = max(mx, max(abs_bits(a.x), abs_bits(a.y)));
-      }
-      mx = max(mx, (unsigned long long)__shfl_xor_sync(0xffffffffu, (long long)mx, 1));
-      if (half == 0) s_rowexp[r] = exp_above_bits(mx);
+    if (presliced) {
+      if (tid < kTileRows) s_rowexp[tid] = P.m0s_exp[((size_t)g * ntiles + tile) * kTileRows + tid];
+    } else {
+      a_row_exponents<WP>(tile, W, s_rowexp, a_elem);
     }
     __syncthreads();
     for (int nc = 0; nc < NCH; ++nc) {
       bool ok = true;
       for (int kc = 0; kc < NCH; ++kc) {
-        // ---- slice the kc chunk of A: a warp writes 4 consecutive 16-byte core rows
-        for (int e = tid; e < kTileRows * CW; e += blockDim.x) {
-          const int ln = e & 31, wi = e >> 5;
-          constexpr int mgroups = CW / 8;
-          const int r = (wi / mgroups) * 4 + (ln >> 3);
-          const int l = (wi % mgroups) * 8 + (ln & 7);
-          const double2 a = a_elem(tile * kTileRows + r, kc * CW + l);
-          const int ex = s_rowexp[r];
-          int xr[kS], xi[kS];
-          split_digits<WP>(a.x, ex, xr);
-          split_digits<WP>(a.y, ex, xi);
-          const uint32_t o_re = kmaj_off(r, l, KC), o_im = kmaj_off(r, l + CW, KC);
+        // ---- the kc chunk of A: kS digit planes, either copied by the bulk-copy engine
+        // from the presliced image (one cp.async.bulk per plane, completion counted in bytes
+        // on mbar_ld; sA is free: the previous MMAs completed before their epilogue) or
+        // sliced here
+        if (presliced) {
+          if (tid == 0) {
+            const unsigned char* src = P.m0s + (((size_t)g * ntiles + tile) * NCH + kc) * (size_t)kS * L::A_BYTES;
+            asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}"
+                         :: "r"(smem_u32(&mbar_ld)), "r"((uint32_t)(kS * L::A_BYTES)) : "memory");
 #pragma unroll
-          for (int t = 0; t < kS; ++t) {
-            *(uint16_t*)(sA + (size_t)t * L::A_BYTES + o_re) = int_to_bf16(xr[t]);
-            *(uint16_t*)(sA + (size_t)t * L::A_BYTES + o_im) = int_to_bf16(xi[t]);
+            for (int t = 0; t < kS; ++t)
+              asm volatile(
+                  "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                  :: "r"(smem_u32(sA + (size_t)t * L::A_BYTES)), "l"(src + (size_t)t * L::A_BYTES),
+                     "r"((uint32_t)L::A_BYTES), "r"(smem_u32(&mbar_ld))
+                  : "memory");
           }
+        } else {
+          a_slice_chunk<WP>(sA, tile, kc, s_rowexp, a_elem);
         }
         if (NCH > 1) slice_b(nc, kc);
+        if (presliced) {
+          // bounded wait; on a timeout, a second bounded wait lets the copies in flight land
+          // before the CTA gives up its shared memory
+          if (!mbar_wait(smem_u32(&mbar_ld), phase_ld)) {
+            s_bad = 1;
+            mbar_wait(smem_u32(&mbar_ld), phase_ld);
+          }
+          phase_ld ^= 1u;
+        }
         // generic-proxy smem writes -> visible to the tensor core (async proxy)
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
+        if (s_bad) {
+          ok = false;
+          break;
+        }
         // ---- MMAs: digit pairs (t,u), t+u <= S-1 (0-based) -> accumulator of diagonal t+u
         if (tid == 0) {
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -285,6 +341,57 @@ __global__ void __launch_bounds__(256, 1) k_oz_mupdate(const Problem* __restrict
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;"
                  :: "r"(tmem), "r"((uint32_t)L::TMEM_COLS) : "memory");
   }
+}
+
+// Slices step 1's A operand once per solve: for every k, tile and K chunk, the kS digit
+// planes exactly as k_oz_mupdate<WP, 1> would write them to shared memory, plus the tile's
+// row exponents.  One CTA (256 threads) per k.
+template <int WP>
+__global__ void __launch_bounds__(256) k_oz_preslice(const Problem* __restrict__ probs, WorkMap wm) {
+  using L = TileSmem<WP>;
+  constexpr int NCH = L::NCH;
+  __shared__ int s_rowexp[kTileRows];
+  int g;
+  const int p = locate(wm, blockIdx.x, g);
+  const Problem& P = probs[p];
+  if (!P.m0s) return;
+  const int W = P.W, B = P.B, WW = W * W;
+  const int ntiles = (B * WP + kTileRows - 1) / kTileRows;
+  auto a_elem = [&](int row, int m) -> double2 {
+    const int bi = row / WP, rr = row % WP;
+    if (bi >= B || rr >= W || m >= W) return make_double2(0.0, 0.0);
+    return P.M0[((size_t)g * B + bi) * WW + (size_t)rr * W + m];
+  };
+  for (int tile = 0; tile < ntiles; ++tile) {
+    a_row_exponents<WP>(tile, W, s_rowexp, a_elem);
+    __syncthreads();
+    if (threadIdx.x < kTileRows) P.m0s_exp[((size_t)g * ntiles + tile) * kTileRows + threadIdx.x] = s_rowexp[threadIdx.x];
+    for (int kc = 0; kc < NCH; ++kc)
+      a_slice_chunk<WP>(P.m0s + (((size_t)g * ntiles + tile) * NCH + kc) * (size_t)kS * L::A_BYTES, tile, kc,
+                        s_rowexp, a_elem);
+    __syncthreads();
+  }
+}
+
+// bytes of the pre-sliced A operand and of its row exponents for K k-points, B neighbours
+void oz_preslice_bytes(int wp, int K, int B, size_t* data, size_t* exps) {
+  const int cw = wp < 32 ? wp : 32;
+  const size_t a_bytes = (size_t)kTileRows * 2 * cw * 2;
+  const size_t ntiles = ((size_t)B * wp + kTileRows - 1) / kTileRows;
+  *data = (size_t)K * ntiles * (wp / cw) * kS * a_bytes;
+  *exps = (size_t)K * ntiles * kTileRows * 4;
+}
+
+cudaError_t oz_preslice_launch(int wp, const Problem* probs, WorkMap wm, int grid, cudaStream_t s) {
+  switch (wp) {
+    case 8: k_oz_preslice<8><<<grid, 256, 0, s>>>(probs, wm); break;
+    case 16: k_oz_preslice<16><<<grid, 256, 0, s>>>(probs, wm); break;
+    case 32: k_oz_preslice<32><<<grid, 256, 0, s>>>(probs, wm); break;
+    case 64: k_oz_preslice<64><<<grid, 256, 0, s>>>(probs, wm); break;
+    case 128: k_oz_preslice<128><<<grid, 256, 0, s>>>(probs, wm); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
 }
 
 // host-side launchers (the template kernels stay private to this translation unit)
