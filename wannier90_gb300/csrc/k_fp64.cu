@@ -281,6 +281,13 @@ __global__ void __launch_bounds__(256) k_omega_p3(const Problem* __restrict__ pr
 // ----------------------------------------------------------------------------
 constexpr int kTile = 32;
 
+// Im ln M_nn(k,b) of the accepted M for the gradient: the block statistics already hold it
+// (written from the same M_nn by the pass that formed M, with the same function), except
+// with guiding centres, whose sheets may have moved since (k_phases runs first)
+__device__ __forceinline__ double diag_ln_of(const Problem& P, size_t kbn, double2 d) {
+  return P.guiding ? guided_ln(P, kbn, d) : P.diag_ln[kbn];
+}
+
 __global__ void __launch_bounds__(256) k_grad(const Problem* __restrict__ probs, WorkMap wm) {
   __shared__ double2 sA[kTile * (kTile + 1)];   // A[j*(33)+i] = M(r0+i, c0+j)
   __shared__ double2 sT[kTile * (kTile + 1)];   // T[i*(33)+j] = M(c0+j, r0+i)
@@ -328,7 +335,7 @@ __global__ void __launch_bounds__(256) k_grad(const Problem* __restrict__ probs,
         const double2 d = Mb[(size_t)m * W + m];
         const double inv = 1.0 / (d.x * d.x + d.y * d.y);
         const double brn = bv[0] * rave[m] + bv[1] * rave[W + m] + bv[2] * rave[2 * W + m];
-        const double q = w * (guided_ln(P, ((size_t)k * B + b) * W + m, d) + brn);
+        const double q = w * (diag_ln_of(P, ((size_t)k * B + b) * W + m, d) + brn);
         // conj(1/M_mm) = d * inv ;  (i/2) q conj(1/M_mm) = (i/2) q inv (d.x + i d.y)
         s_beta[t] = cmk(-0.5 * w * d.x - 0.5 * q * inv * d.y, -0.5 * w * d.y + 0.5 * q * inv * d.x);
       }
@@ -339,7 +346,7 @@ __global__ void __launch_bounds__(256) k_grad(const Problem* __restrict__ probs,
         const double2 d = Mb[(size_t)n * W + n];
         const double inv = 1.0 / (d.x * d.x + d.y * d.y);
         const double brn = bv[0] * rave[n] + bv[1] * rave[W + n] + bv[2] * rave[2 * W + n];
-        const double q = w * (guided_ln(P, ((size_t)k * B + b) * W + n, d) + brn);
+        const double q = w * (diag_ln_of(P, ((size_t)k * B + b) * W + n, d) + brn);
         // 1/M_nn = (d.x - i d.y) inv ;  (i/2) q / M_nn = (q inv / 2)(d.y + i d.x)
         s_alpha[u] = cmk(0.5 * w * d.x + 0.5 * q * inv * d.y, -0.5 * w * d.y + 0.5 * q * inv * d.x);
       }
