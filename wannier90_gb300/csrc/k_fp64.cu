@@ -245,13 +245,21 @@ __global__ void __launch_bounds__(256) k_omega_p3(const Problem* __restrict__ pr
     cen[2 * W + i] = x2;
     cen[3 * W + i] = q / (double)K - (x0 * x0 + x1 * x1 + x2 * x2);
   }
-  double od = 0.0, oi = 0.0, dd = 0.0;
+  // the three chunk sums run on the last three threads, alongside the r^2 sums above
+  // (each in chunk order)
+  __shared__ double s_sum[3];
+  const int u = t - ((int)blockDim.x - 3);
+  if (u >= 0) {
+    double acc = 0.0;
+    if (u == 2)
+      for (int c = 0; c < P.nchunk; ++c) acc += P.opart2[c];
+    else
+      for (int c = 0; c < P.nchunk; ++c) acc += P.opart1[(size_t)c * stride + 4 * W + u];
+    s_sum[u] = acc;
+  }
+  __syncthreads();
   if (t == 0) {
-    for (int c = 0; c < P.nchunk; ++c) {
-      od += P.opart1[(size_t)c * stride + 4 * W];
-      oi += P.opart1[(size_t)c * stride + 4 * W + 1];
-      dd += P.opart2[c];
-    }
+    const double od = s_sum[0], oi = s_sum[1], dd = s_sum[2];
     const bool first = (slot == 2) && st->first_pass;
     if (first) {
       st->om_invariant = oi / (double)K;
