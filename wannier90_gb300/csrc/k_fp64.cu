@@ -231,31 +231,57 @@ __global__ void __launch_bounds__(256) k_omega_p3(const Problem* __restrict__ pr
   const Problem& P = probs[blockIdx.x];
   CtrlState* st = P.st;
   if (omega_skip(st, slot)) return;
-  omega_rave(P, s_rave);
   const int W = P.W, K = P.K;
   const int stride = 4 * W + 2;
   const int t = threadIdx.x;
   double* cen = P.centres + (size_t)slot * 4 * W;
-  for (int i = t; i < W; i += blockDim.x) {
-    double q = 0.0;
-    for (int c = 0; c < P.nchunk; ++c) q += P.opart1[(size_t)c * stride + 3 * W + i];
-    const double x0 = s_rave[i], x1 = s_rave[W + i], x2 = s_rave[2 * W + i];
-    cen[i] = x0;
-    cen[W + i] = x1;
-    cen[2 * W + i] = x2;
-    cen[3 * W + i] = q / (double)K - (x0 * x0 + x1 * x1 + x2 * x2);
-  }
-  // the three chunk sums run on the last three threads, alongside the r^2 sums above
-  // (each in chunk order)
+  // Omega_OD, Omega_I and Omega_D totals over the chunks, on the last three threads
   __shared__ double s_sum[3];
   const int u = t - ((int)blockDim.x - 3);
-  if (u >= 0) {
+  auto totals = [&]() {
+    if (u < 0) return;
     double acc = 0.0;
     if (u == 2)
       for (int c = 0; c < P.nchunk; ++c) acc += P.opart2[c];
     else
       for (int c = 0; c < P.nchunk; ++c) acc += P.opart1[(size_t)c * stride + 4 * W + u];
     s_sum[u] = acc;
+  };
+  if (4 * W + 3 <= (int)blockDim.x) {
+    // every chunk sum on its own thread, all at once: rave (3W), r^2 (W), and the three
+    // totals on the last three threads below (each in chunk order)
+    __shared__ double s_q[256];
+    if (t < 3 * W) {
+      double sacc = 0.0;
+      for (int c = 0; c < P.nchunk; ++c) sacc += P.opart1[(size_t)c * stride + t];
+      s_rave[t] = -sacc / (double)P.K;
+    } else if (t < 4 * W) {
+      double q = 0.0;
+      for (int c = 0; c < P.nchunk; ++c) q += P.opart1[(size_t)c * stride + t];
+      s_q[t - 3 * W] = q;
+    } else {
+      totals();
+    }
+    __syncthreads();
+    if (t < W) {
+      const double x0 = s_rave[t], x1 = s_rave[W + t], x2 = s_rave[2 * W + t];
+      cen[t] = x0;
+      cen[W + t] = x1;
+      cen[2 * W + t] = x2;
+      cen[3 * W + t] = s_q[t] / (double)K - (x0 * x0 + x1 * x1 + x2 * x2);
+    }
+  } else {
+    omega_rave(P, s_rave);
+    for (int i = t; i < W; i += blockDim.x) {
+      double q = 0.0;
+      for (int c = 0; c < P.nchunk; ++c) q += P.opart1[(size_t)c * stride + 3 * W + i];
+      const double x0 = s_rave[i], x1 = s_rave[W + i], x2 = s_rave[2 * W + i];
+      cen[i] = x0;
+      cen[W + i] = x1;
+      cen[2 * W + i] = x2;
+      cen[3 * W + i] = q / (double)K - (x0 * x0 + x1 * x1 + x2 * x2);
+    }
+    totals();
   }
   __syncthreads();
   if (t == 0) {
