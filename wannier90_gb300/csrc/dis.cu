@@ -32,6 +32,9 @@ namespace w90g {
 namespace {
 
 constexpr int kWs = 8;   // workspace per k, in units of nb*nb complex entries
+// dynamic shared memory of k_dis_step (3 m x m) and k_dis_rotate (W x nb + 2 W x W) at
+// the largest band count (64)
+constexpr size_t kDisMaxSmem = 3 * 64 * 64 * 16;
 
 struct DisDev {
   int nb, W, K, B;
@@ -628,7 +631,10 @@ int dis_run(const DisSpec& s, DisResult& r, std::string& err) {
     DIS_CHECK(cudaEventCreate(&ev[0]));
     DIS_CHECK(cudaEventCreate(&ev[1]));
   }
-  DIS_CHECK(cudaFuncSetAttribute(k_dis_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)step_smem));
+  // the attributes are process-wide: always the largest any call needs (nb <= 64), so
+  // concurrent calls of different sizes never lower them under one another
+  DIS_CHECK(cudaFuncSetAttribute(k_dis_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDisMaxSmem));
+  DIS_CHECK(cudaFuncSetAttribute(k_dis_rotate, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDisMaxSmem));
   DIS_CHECK(cudaMallocAsync(&arena, off, st));
   {
     char* a = (char*)arena;
@@ -728,7 +734,6 @@ int dis_run(const DisSpec& s, DisResult& r, std::string& err) {
   }
   DIS_CHECK(launch(kDisGauge, [&] { k_dis_gauge<<<K, 256, 0, st>>>(D, cur); }));
   DIS_CHECK(launch(kDisFindU, [&] { k_dis_findu<<<K, 256, 0, st>>>(D, cur); }));
-  DIS_CHECK(cudaFuncSetAttribute(k_dis_rotate, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rot_smem));
   DIS_CHECK(launch(kDisRotate, [&] { k_dis_rotate<<<K * B, 256, rot_smem, st>>>(D, cur); }));
   DIS_CHECK(cudaMemcpyAsync(status.data(), D.status, K * 4, cudaMemcpyDeviceToHost, st));
   DIS_CHECK(cudaMemcpyAsync(&r.max_sweeps, D.max_sweeps, 4, cudaMemcpyDeviceToHost, st));
