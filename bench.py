@@ -106,6 +106,20 @@ def _gen_batch_problem(i):
     return i, p
 
 
+def replica_rate(ms_local, steps, world, dist=None, device="cuda"):
+    """Replicas: every rank times its own `steps` solves; the job's time is the slowest
+    rank's (max over ranks) and the whole-job rate counts every rank's solves.
+    Returns (ms per step, solves/s of the job)."""
+    ms = ms_local
+    if dist is not None:
+        import torch
+        t = torch.tensor([ms], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / steps
+    return ms_per_step, world * 1e3 / ms_per_step
+
+
 def _env_rank():
     return (int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0")),
             int(os.environ.get("WORLD_SIZE", "1")))
@@ -992,13 +1006,7 @@ def main():
     clk = clocks.stop()
     if dist:
         dist.barrier()
-    ms = ev0.elapsed_time(ev1)
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    ms_per_step = ms / args.steps
-    value = world * 1e3 / ms_per_step
+    ms_per_step, value = replica_rate(ev0.elapsed_time(ev1), args.steps, world, dist, "cuda")
 
     # e2e through the reference-named C ABI with host buffers (pinned)
     m_host0 = torch.from_numpy(m0.cpu().numpy()).pin_memory()
