@@ -74,6 +74,39 @@ struct OzCtx {
   int* bad;
 };
 
+// Power-of-two scales of a product: the exponent above the largest |re| or |im| of every
+// row of A and every column of B.  The 2 WP rows / columns share the CTA's 256 threads
+// (TPI consecutive lanes each, then a max across those lanes), so each thread reads
+// W / TPI entries instead of W; the maximum does not depend on the order.
+template <int WP>
+__device__ __forceinline__ void ab_exponents(OzCtx& cx, const double2* A, const double2* B, int W) {
+  constexpr int ITEMS = 2 * WP;
+  constexpr int TPI = ITEMS >= 256 ? 1 : (256 / ITEMS > 32 ? 32 : 256 / ITEMS);
+  for (int base = 0; base < ITEMS * TPI; base += blockDim.x) {
+    const int gi = base + (int)threadIdx.x;
+    const int idx = gi / TPI, sub = gi % TPI;
+    const int r = idx % WP;
+    unsigned long long mx = 0ull;
+    if (idx < ITEMS && r < W) {
+      if (idx < WP) {
+        for (int l = sub; l < W; l += TPI) {
+          const double2 a = A[(size_t)l * W + r];
+          mx = max(mx, max(abs_bits(a.x), abs_bits(a.y)));
+        }
+      } else {
+        for (int l = sub; l < W; l += TPI) {
+          const double2 b = B[(size_t)r * W + l];
+          mx = max(mx, max(abs_bits(b.x), abs_bits(b.y)));
+        }
+      }
+    }
+#pragma unroll
+    for (int o = 1; o < TPI; o <<= 1)
+      mx = max(mx, (unsigned long long)__shfl_xor_sync(0xffffffffu, (long long)mx, o));
+    if (idx < ITEMS && sub == 0) (idx < WP ? cx.rowexp : cx.colexp)[r] = exp_above_bits(mx);
+  }
+}
+
 // C = A B for W x W complex column-major matrices (generic pointers; C must not alias
 // A or B).  All threads call; returns false (uniformly) if an MMA wait timed out.
 template <int WP>
@@ -82,24 +115,7 @@ __device__ bool oz_cmm(OzCtx& cx, double2* C, const double2* A, const double2* B
   constexpr int CW = E::CW, KC = E::KC, NC = E::NC, NCH = E::NCH;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   // ---- power-of-two scales: rows of A, columns of B (over re and im parts)
-  for (int idx = tid; idx < 2 * WP; idx += blockDim.x) {
-    const int r = idx % WP;
-    unsigned long long mx = 0ull;
-    if (r < W) {
-      if (idx < WP) {
-        for (int l = 0; l < W; ++l) {
-          const double2 a = A[(size_t)l * W + r];
-          mx = max(mx, max(abs_bits(a.x), abs_bits(a.y)));
-        }
-      } else {
-        for (int l = 0; l < W; ++l) {
-          const double2 b = B[(size_t)r * W + l];
-          mx = max(mx, max(abs_bits(b.x), abs_bits(b.y)));
-        }
-      }
-    }
-    (idx < WP ? cx.rowexp : cx.colexp)[r] = exp_above_bits(mx);
-  }
+  ab_exponents<WP>(cx, A, B, W);
   __syncthreads();
   const uint32_t idesc = idesc_bf16(NC);
   bool ok = true;
@@ -307,24 +323,7 @@ __device__ bool oz_cmm2(OzCtx& cx, double2* C, const double2* A, const double2* 
   using E = Exp2Smem<WP>;
   constexpr int CW = E::CW, KC = E::KC, N = E::N;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  for (int idx = tid; idx < 2 * WP; idx += blockDim.x) {
-    const int r = idx % WP;
-    unsigned long long mx = 0ull;
-    if (r < W) {
-      if (idx < WP) {
-        for (int l = 0; l < W; ++l) {
-          const double2 a = A[(size_t)l * W + r];
-          mx = max(mx, max(abs_bits(a.x), abs_bits(a.y)));
-        }
-      } else {
-        for (int l = 0; l < W; ++l) {
-          const double2 b = B[(size_t)r * W + l];
-          mx = max(mx, max(abs_bits(b.x), abs_bits(b.y)));
-        }
-      }
-    }
-    (idx < WP ? cx.rowexp : cx.colexp)[r] = exp_above_bits(mx);
-  }
+  ab_exponents<WP>(cx, A, B, W);
   __syncthreads();
   const uint32_t idesc = idesc_bf16(N);
   // a warp slices 4 rows x 8 consecutive K, i.e. whole 16-byte core-matrix rows
