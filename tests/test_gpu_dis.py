@@ -191,3 +191,64 @@ def test_device_entry_equals_host_entry():
         np.testing.assert_array_equal(synth.to_math_m(m), host["m_after_wann"])
         np.testing.assert_array_equal(w90.w90_get_centres(c, p.num_wann), host["centres"])
         assert w90.w90_kernel_launches(c) > 0
+
+
+def test_entangled_problems_in_batched_and_served_forms():
+    """After w90g_disentangle_device, the (nb x nb)-block overlaps go through the batched
+    and the served forms like isolated ones (top-left num_wann blocks): each member's
+    result is bitwise the stand-alone w90g_wannierise_device result."""
+    import torch
+
+    from tests.engine_dis import dis_options
+    from wannier90_gb300 import library as w90
+    cases = [dict(kind="sc", mp=(3, 3, 3), num_bands=12, num_wann=8, seed=21, tensor=1),
+             dict(kind="fcc", mp=(3, 3, 3), num_bands=16, num_wann=10, seed=22, tensor=0),
+             dict(kind="sc", mp=(2, 2, 3), num_bands=20, num_wann=13, seed=23, tensor=1)]
+    handles, ms, us, alone = [], [], [], []
+    for c in cases:
+        c = dict(c)
+        tensor = c.pop("tensor")
+        p = synth.make_entangled_problem(eps=0.3, **c)
+        eig = np.ascontiguousarray(p.eig.T)
+        w = entangled_windows(eig, p.num_wann)
+        dc = O.DisControl(num_iter=40, win_min=w["win_min"], win_max=w["win_max"], froz_max=w["froz_max"],
+                          frozen_states=True)
+        h = w90.setup(kpoints=p.kpoints, unit_cell_cart=p.real_lattice, num_wann=p.num_wann,
+                      num_bands=p.num_bands, iprint=0, num_iter=12, conv_window=-1, gpu_tensor=tensor,
+                      **dis_options(dc))
+        dm = torch.from_numpy(p.m.reshape(-1, order="F").view(np.float64).copy()).cuda()
+        da = torch.from_numpy(p.a.reshape(-1, order="F").view(np.float64).copy()).cuda()
+        du = torch.zeros(2 * p.num_wann ** 2 * len(p.kpoints), dtype=torch.float64, device="cuda")
+        de = torch.from_numpy(np.ascontiguousarray(p.eig.reshape(-1, order="F"))).cuda()
+        assert w90.w90_disentangle_device(h, dm.data_ptr(), da.data_ptr(), du.data_ptr(), de.data_ptr()) == 0
+        m1, u1 = dm.clone(), du.clone()
+        assert w90.w90_wannierise_device(h, m1.data_ptr(), u1.data_ptr()) == 0, h.last_error()
+        torch.cuda.synchronize()
+        alone.append((m1.cpu().numpy(), u1.cpu().numpy(), w90.w90_get_log(h, 13).copy()))
+        handles.append(h)
+        ms.append(dm)
+        us.append(du)
+    # batched
+    mb = [m.clone() for m in ms]
+    ub = [u.clone() for u in us]
+    ierr = w90.w90_wannierise_batch_device(handles, [m.data_ptr() for m in mb], [u.data_ptr() for u in ub])
+    torch.cuda.synchronize()
+    assert ierr == [0] * len(cases), [h.last_error() for h in handles]
+    for i, h in enumerate(handles):
+        np.testing.assert_array_equal(w90.w90_get_log(h, 13)[:, :8], alone[i][2][:, :8])
+        np.testing.assert_array_equal(mb[i].cpu().numpy(), alone[i][0])
+        np.testing.assert_array_equal(ub[i].cpu().numpy(), alone[i][1])
+    # served
+    srv = w90.Server(8e9, max_active=2)
+    ms2 = [m.clone() for m in ms]
+    us2 = [u.clone() for u in us]
+    for i, h in enumerate(handles):
+        assert srv.submit(h, ms2[i].data_ptr(), us2[i].data_ptr(), tag=i) == 0, h.last_error()
+    srv.drain()
+    done = srv.poll()
+    assert sorted(d[0] for d in done) == list(range(len(cases))) and all(d[1] == 0 for d in done)
+    torch.cuda.synchronize()
+    for i in range(len(cases)):
+        np.testing.assert_array_equal(ms2[i].cpu().numpy(), alone[i][0])
+        np.testing.assert_array_equal(us2[i].cpu().numpy(), alone[i][1])
+    srv.close()
