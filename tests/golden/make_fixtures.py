@@ -232,6 +232,10 @@ def build_guiding(ref_root, out_dir):
 DIS_CASES = {
     "silicon_dis": ("test-suite/tests/testw90_example03", "silicon"),
     "copper_dis": ("test-suite/tests/testw90_example04", "copper"),
+    # 8 bands -> 4 WFs, outer window with a lower bound, frozen window with both bounds
+    "basic2_dis": ("test-suite/tests/testw90_basic2", "wannier"),
+    # 12 -> 8 (bands 1-5 excluded upstream), mixing ratio 1, conv_window 3
+    "gaas192_dis": ("test-suite/tests/testw90_gaas_disentanglement_issue192", "gaas"),
 }
 
 

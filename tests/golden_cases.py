@@ -59,7 +59,7 @@ def guiding(d):
     return ctl, (d["proj_site_frac"] @ d["real_lattice"]).T
 
 
-DIS_CASES = ["silicon_dis", "copper_dis"]
+DIS_CASES = ["silicon_dis", "copper_dis", "basic2_dis", "gaas192_dis"]
 
 
 def dis_control(d):
@@ -71,3 +71,29 @@ def dis_control(d):
                         win_min=float(kn["dis_win_min"]), win_max=float(kn["dis_win_max"]),
                         froz_min=float(kn["dis_froz_min"]), froz_max=float(kn["dis_froz_max"]),
                         frozen_states=bool(kn["frozen_states"]))
+
+
+def conv_sensitivity(M0, U0, km, ctl, noise=1e-14, runs=2):
+    """Per iteration, the largest change of the oracle's own wann_main spread when M0 is
+    perturbed by `noise` (relative, seeded): the part of a printed trajectory that no FP64
+    implementation can reproduce more closely."""
+    import numpy as np
+
+    from oracle import w90_oracle as O
+    base = O.wann_main(M0, U0, km, ctl)
+    ref = {x.iter: x.spread.om_tot for x in [base.initial] + base.iters}
+    sens = {i: 0.0 for i in ref}
+    rng = np.random.default_rng(2024)
+    for _ in range(runs):
+        r = O.wann_main(M0 * (1 + noise * rng.standard_normal(M0.shape)), U0, km, ctl)
+        for x in [r.initial] + r.iters:
+            if x.iter in sens:
+                sens[x.iter] = max(sens[x.iter], abs(x.spread.om_tot - ref[x.iter]))
+    return sens
+
+
+def conv_tolerance(sens, it, spread, floor=2e-10, factor=10.0):
+    """2e-10 A^2 where the trajectory is insensitive at that level, else `factor` times the
+    measured sensitivity (at least the metric's 1e-8 relative)."""
+    s = sens.get(int(it), 0.0)
+    return floor if s < 0.1 * floor else max(factor * s, 1e-8 * abs(spread))

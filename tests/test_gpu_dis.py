@@ -41,8 +41,9 @@ def _check_dis(out, recs, omi, U0, M0, Uo, rel=1e-10):
 @pytest.mark.parametrize("tensor", [0, 1], ids=["fp64", "tensor"])
 @pytest.mark.parametrize("name", G.DIS_CASES)
 def test_disentangle_golden(name, tensor):
-    """testw90_example03 (silicon, 12 bands -> 8 WFs) and _example04 (copper, 12 -> 7):
-    outer and frozen windows; every '<-- DIS' line, the final Omega_I, then wann_main on
+    """testw90_example03 (silicon, 12 bands -> 8 WFs), _example04 (copper, 12 -> 7),
+    testw90_basic2 (8 -> 4, lower window bounds), testw90_gaas_disentanglement_issue192
+    (12 -> 8, mixing ratio 1): every '<-- DIS' line, the final Omega_I, then wann_main on
     the disentangled overlaps against the printed '<-- CONV' lines and final centres."""
     d = G.load(name)
     kn = d["knobs"]
@@ -61,12 +62,18 @@ def test_disentangle_golden(name, tensor):
         assert int(row[0]) == int(it)
         assert abs(row[1] - prev) < 1e-8 and abs(row[2] - cur) < 1e-8
     assert abs(out["dis_info"]["omega_invariant"] - d["omega_i_final"][0]) < 1e-8
-    # wann_main on the top-left num_wann x num_wann blocks of m_local
+    # wann_main on the top-left num_wann x num_wann blocks of m_local: each printed spread
+    # within 2e-10 A^2 where the trajectory is stable at that level, else within ten times
+    # the oracle's own sensitivity to a 1e-14 perturbation of M0 (the GaAs case's middle
+    # iterations move by 1e-5 A^2 under it).  The tensor path rounds every product at
+    # ~2^-49 of its scales on every iteration, a perturbation renewed at each step: 2e-9,
+    # and twenty times the largest change over four 1e-13 perturbations
     assert out["wann_ierr"] == 0, out["wann_err"]
     by_iter = {int(row[0]): row for row in out["log"]}
-    tol = 2e-10 if not tensor else 2e-9
+    sens = G.conv_sensitivity(M0, U0, km, ctl, noise=1e-13 if tensor else 1e-14, runs=4 if tensor else 2)
     for it, delta, rms, spread in d["conv"]:
-        assert abs(by_iter[int(it)][3] - spread) < tol + 1e-10 * spread, (int(it), by_iter[int(it)][3], spread)
+        tol = G.conv_tolerance(sens, it, spread, floor=2e-9 if tensor else 2e-10, factor=20.0 if tensor else 10.0)
+        assert abs(by_iter[int(it)][3] - spread) < tol, (int(it), by_iter[int(it)][3], spread, tol)
     np.testing.assert_allclose(out["centres"].T, d["centres_final"][:, :3], atol=1.01e-6)
     np.testing.assert_allclose(out["omega"][[0, 3]], d["omega_final"][[0, 3]], atol=1.01e-9)
     # wann_main wrote only the top-left blocks: the rest of m_local is the raw overlaps

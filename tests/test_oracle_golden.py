@@ -58,9 +58,13 @@ def test_oracle_guiding_centres_reach_reference_checkpoint():
 
 @pytest.mark.parametrize("name", G.DIS_CASES)
 def test_oracle_disentanglement_reproduces_reference(name):
-    """testw90_example03 (silicon) / _example04 (copper): 12 bands, 8 / 7 WFs, outer and
-    frozen windows.  Every printed '<-- DIS' line (Omega_I before and after the step, 8
-    decimals), the final Omega_I, and the wannierise trajectory that follows."""
+    """testw90_example03 (silicon) / _example04 (copper): 12 bands, 8 / 7 WFs;
+    testw90_basic2: 8 -> 4 with lower window bounds; testw90_gaas_disentanglement_issue192:
+    12 -> 8, mixing ratio 1.  Every printed '<-- DIS' line (Omega_I before and after the
+    step, 8 decimals), the final Omega_I, and the wannierise trajectory that follows: each
+    printed spread within 2e-10 A^2 where the trajectory is stable at that level, else within
+    ten times the spread that a 1e-14 perturbation of M0 causes in the oracle itself (the
+    GaAs case's middle iterations move by 1e-5 A^2 under it), and the final state."""
     d = G.load(name)
     kn = d["knobs"]
     km = O.kmesh_get(d["real_lattice"], d["kpt_latt"], int(kn["search_shells"]))
@@ -74,7 +78,9 @@ def test_oracle_disentanglement_reproduces_reference(name):
     r = O.wann_main(M0, U0, km, G.control(d))
     rec = {0: r.initial}
     rec.update({it.iter: it for it in r.iters})
+    sens = G.conv_sensitivity(M0, U0, km, G.control(d))
     for it, delta, rms, spread in d["conv"]:
-        assert abs(rec[int(it)].spread.om_tot - spread) < 2e-10
+        tol = G.conv_tolerance(sens, it, spread)
+        assert abs(rec[int(it)].spread.om_tot - spread) < tol, (int(it), rec[int(it)].spread.om_tot, spread, tol)
     np.testing.assert_allclose(r.centres.T, d["centres_final"][:, :3], atol=1.01e-6)
     np.testing.assert_allclose([r.spread.om_i, r.spread.om_tot], d["omega_final"][[0, 3]], atol=1.01e-9)
