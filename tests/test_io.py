@@ -188,3 +188,16 @@ def test_native_reader_errors_and_duplicates(tmp_path):
     open(f + ".eig", "w").write("\n".join(t))
     with pytest.raises(ValueError, match="mismatch"):
         w90io.read_eig(f + ".eig", 5, 27)
+
+
+def test_exclude_bands_range_vector(tmp_path):
+    """exclude_bands ranges as the .win writes them; the CLI keeps them for the checkpoint."""
+    assert w90io.parse_range_vector("1-5") == [1, 2, 3, 4, 5]
+    assert w90io.parse_range_vector("1-3, 7 9-10") == [1, 2, 3, 7, 9, 10]
+    with pytest.raises(ValueError):
+        w90io.parse_range_vector("5-1")
+    p = _small()
+    f = str(tmp_path / "x.win")
+    w90io.write_win(f, p.real_lattice, p.kpoints, (3, 3, 3), 4, exclude_bands="1-5")
+    _, _, o = w90io.win_system(f)
+    assert o["exclude_bands"] == [1, 2, 3, 4, 5]

@@ -26,6 +26,8 @@ def run(seedname, precision="tensor"):
     nw = int(opts.pop("num_wann"))
     nb = int(opts.pop("num_bands", nw))
     mp = opts.pop("mp_grid", None)
+    # the seed files hold the bands left after exclusion; the list goes to the checkpoint
+    exclude = opts.pop("exclude_bands", [])
     opts.setdefault("iprint", 1)
     opts["gpu_tensor"] = 1 if precision == "tensor" else 0
     c = w90.setup(kpoints=kpts, unit_cell_cart=lattice, num_wann=nw, num_bands=nb, mp_grid=mp, **opts)
@@ -64,7 +66,8 @@ def run(seedname, precision="tensor"):
     spreads = w90.w90_get_spreads(c, nw)
     w90io.write_chk(seedname + ".chk", num_bands=nb, lattice=lattice, kpts=kpts,
                     mp_grid=mp if mp is not None else (0, 0, 0), nntot=w90.w90_get_nn(c), num_wann=nw,
-                    u=u, m=np.asfortranarray(m[:nw, :nw]), centres=centres, spreads=spreads, dis=dis)
+                    u=u, m=np.asfortranarray(m[:nw, :nw]), centres=centres, spreads=spreads, dis=dis,
+                    exclude_bands=exclude)
     return ierr
 
 

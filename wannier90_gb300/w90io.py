@@ -66,6 +66,24 @@ def _flag(s):
     return s.strip().lower().lstrip(".").startswith("t")
 
 
+def parse_range_vector(text):
+    """A .win range list ("1-5, 7 9-10") as the sorted 1-based integers it names
+    (w90_readwrite_get_range_vector, src/readwrite.F90)."""
+    out = []
+    for tok in re.split(r"[\s,]+", text.strip()):
+        if not tok:
+            continue
+        if "-" in tok[1:]:
+            a, b = tok.split("-", 1)
+            lo, hi = int(a), int(b)
+            if hi < lo:
+                raise ValueError("range %s is decreasing" % tok)
+            out.extend(range(lo, hi + 1))
+        else:
+            out.append(int(tok))
+    return sorted(set(out))
+
+
 def win_system(path):
     """Lattice (rows a_i, Angstrom), k-points (fractional), mp_grid and the wannierise
     keywords of a .win file, as library options."""
@@ -98,6 +116,8 @@ def win_system(path):
     for k in ("num_no_guide_iter", "num_guide_cycles", "optimisation"):
         if k in kw:
             opts[k] = int(kw[k].split()[0])
+    if "exclude_bands" in kw:
+        opts["exclude_bands"] = parse_range_vector(kw["exclude_bands"])
     if opts.get("guiding_centres") and "projections" in blocks:
         spin = _flag(kw.get("spinors", "f"))
         opts["guiding_centres_frac"] = projection_sites(blocks, lattice, spin)
