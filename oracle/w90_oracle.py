@@ -567,14 +567,37 @@ def dis_main(Mraw, A, eig, km, num_wann, dc: DisControl):
 # ---------------------------------------------------------------------------
 @dataclass
 class Spread:
-    """localisation_vars_type (src/wannierise.F90:35-43)."""
+    """localisation_vars_type (src/wannierise.F90:35-43).  With selective localisation
+    om_i and om_od are not computed (left 0) and om_iod / om_nu hold the SLWF terms."""
     om_i: float = 0.0
     om_d: float = 0.0
     om_od: float = 0.0
     om_tot: float = 0.0
+    om_iod: float = 0.0
+    om_nu: float = 0.0
 
     def copy(self):
-        return Spread(self.om_i, self.om_d, self.om_od, self.om_tot)
+        return Spread(self.om_i, self.om_d, self.om_od, self.om_tot, self.om_iod, self.om_nu)
+
+
+@dataclass
+class Slwf:
+    """wann_slwf_type as wann_main uses it (src/wannier90_types.F90:147-161): the first
+    ``num`` Wannier functions are the objective ones; ``lam`` is lambda_loc (the
+    constraint's Lagrange multiplier, 0 when slwf_constrain = F, src/wannierise.F90:445-450);
+    ``centres`` [3, W] are the constrained centres (Cartesian, Angstrom; None when
+    unconstrained)."""
+    num: int
+    lam: float = 0.0
+    centres: np.ndarray | None = None
+
+    def __post_init__(self):
+        if self.centres is None:
+            self.lam = 0.0
+
+    @property
+    def constrain(self):
+        return self.centres is not None
 
 
 def _ln_diag(diag, sheet):
@@ -585,11 +608,12 @@ def _ln_diag(diag, sheet):
     return np.angle(np.exp(1j * sheet) * diag) - sheet
 
 
-def wann_omega(M, km, omega_invariant=None, sheet=None):
+def wann_omega(M, km, omega_invariant=None, sheet=None, slwf=None):
     """Returns (Spread, rave[3,W], r2ave[W], rave2[W]).
 
     ``omega_invariant`` None reproduces the ``first_pass`` branch (:2214-2239).
     ``sheet`` [K,B,W]: branch-cut offsets of the guiding centres (wann_phases).
+    ``slwf`` (:class:`Slwf`): the selective-localisation branch (:2144-2211).
     """
     K, B, W, _ = M.shape
     wb, bk = km["wb"], km["bk"]
@@ -599,6 +623,8 @@ def wann_omega(M, km, omega_invariant=None, sheet=None):
     rave2 = (rave * rave).sum(axis=0)
     mnn2 = (diag * diag.conj()).real
     r2ave = np.einsum("b,kbn->n", wb, 1.0 - mnn2 + ln ** 2) / K  # :2076-2090
+    if slwf is not None:
+        return _omega_slwf(ln, mnn2, rave, wb, bk, K, slwf), rave, r2ave, rave2
     absm2 = (M * M.conj()).real
     if omega_invariant is None:
         summ = absm2.sum(axis=(2, 3))                  # (K,B)
@@ -613,14 +639,75 @@ def wann_omega(M, km, omega_invariant=None, sheet=None):
     return sp, rave, r2ave, rave2
 
 
-def wann_domega(M, km, sheet=None):
-    """Gradient cdodq(m,n,k) (src/wannierise.F90:2287-2569, non-SLWF branch)."""
+def _omega_slwf(ln, mnn2, rave, wb, bk, K, slwf):
+    """wann_omega's selective-localisation branch (src/wannierise.F90:2144-2211):
+    Omega_IOD over the objective WFs (minus lambda ln^2 when constrained), Omega_D
+    weighted by (1 - lambda), and the constraint term Omega_nu."""
+    s, lam = slwf.num, slwf.lam
+    ln_s, a_s = ln[:, :, :s], mnn2[:, :, :s]
+    summ = a_s.sum(axis=2)
+    if slwf.constrain:
+        summ = summ - lam * (ln_s ** 2).sum(axis=2)                  # :2153-2157
+    om_iod = float(np.einsum("b,kb->", wb, s - summ) / K)             # :2158-2167
+    brn = np.einsum("kbi,in->kbn", bk, rave)[:, :, :s]
+    om_d = float(np.einsum("b,kbn->", (1.0 - lam) * wb, (ln_s + brn) ** 2) / K)   # :2169-2183
+    om_nu = 0.0
+    if slwf.constrain:                                                # :2186-2208
+        bc = np.einsum("kbi,in->kbn", bk, slwf.centres)[:, :, :s]
+        om_nu = float(np.einsum("b,kbn->", 2.0 * wb, ln_s * lam * bc) / K)
+        om_nu += lam * float((slwf.centres[:, :s] ** 2).sum())
+    return Spread(0.0, om_d, 0.0, om_iod + om_d + om_nu, om_iod, om_nu)
+
+
+def _domega_slwf(M, diag, lnw, rnkb, wb, bk, K, slwf):
+    """wann_domega's selective-localisation branch (src/wannierise.F90:2431-2509), term
+    by term: objective rows/columns only, the constraint terms when constrained."""
+    W = M.shape[-1]
+    s, lam = slwf.num, slwf.lam
+    c = -0.5j
+    H = lambda X: np.conj(np.swapaxes(X, -1, -2))
+    crt = M / diag[:, :, None, :]                      # crt(m,n) = M_mn / M_nn
+    cr = M * np.conj(diag)[:, :, None, :]              # cr(m,n)  = M_mn conj(M_nn)
+    crt_h, cr_h = H(crt), H(cr)                        # conj(crt(n,m)), conj(cr(n,m)) at (m,n)
+    w = wb[None, :, None, None]
+    qn, qm = lnw[:, :, None, :], lnw[:, :, :, None]
+    rn, rm = rnkb[:, :, None, :], rnkb[:, :, :, None]
+    obj = np.arange(W) < s
+    # m <= slwf_num, n <= slwf_num (:2434-2468)
+    gb = w * 0.5 * (cr - cr_h)
+    gb = gb - (crt * qn + crt_h * qm) * c
+    gb = gb - (crt * rn + crt_h * rm) * c
+    # m <= slwf_num < n (:2469-2486)
+    gm = -w * 0.5 * cr_h - crt_h * (qm + w * rm) * c
+    # n <= slwf_num < m (:2487-2504)
+    gn = w * cr * 0.5 - crt * (qn + w * rn) * c
+    if slwf.constrain:
+        r0 = np.einsum("kbi,in->kbn", bk, slwf.centres)      # r0kb (:2396-2406)
+        r0n, r0m = r0[:, :, None, :], r0[:, :, :, None]
+        gb = gb + lam * (crt * qn + crt_h * qm) * c
+        gb = gb + w * lam * (crt * rn + crt_h * rm) * c
+        gb = gb - lam * (crt * qn + crt_h * qm) * c
+        gb = gb - w * lam * (r0n * crt + r0m * crt_h) * c
+        gm = gm + lam * crt_h * (qm + w * rm) * c - lam * crt_h * qm * c
+        gm = gm - w * lam * r0m * crt_h * c
+        gn = gn + lam * crt * (qn + w * rn) * c - lam * crt * qn * c
+        gn = gn - w * lam * r0n * crt * c
+    mo, no = obj[:, None], obj[None, :]
+    g = np.where(mo & no, gb, np.where(mo & ~no, gm, np.where(~mo & no, gn, 0.0)))
+    return g.sum(axis=1) * (4.0 / K)                   # :2531
+
+
+def wann_domega(M, km, sheet=None, slwf=None):
+    """Gradient cdodq(m,n,k) (src/wannierise.F90:2287-2569); ``slwf``: the
+    selective-localisation branch."""
     K, B, W, _ = M.shape
     wb, bk = km["wb"], km["bk"]
     diag = np.diagonal(M, axis1=2, axis2=3)
     lnw = wb[None, :, None] * _ln_diag(diag, sheet)    # :2366-2375
     rave = -np.einsum("kbi,kbn->in", bk, lnw) / K      # :2378-2391
     rnkb = np.einsum("kbi,in->kbn", bk, rave)          # :2409-2417
+    if slwf is not None:
+        return _domega_slwf(M, diag, lnw, rnkb, wb, bk, K, slwf)
     crt = M / diag[:, :, None, :]
     cr = M * np.conj(diag)[:, :, None, :]
     G = np.zeros((K, W, W), dtype=np.complex128)
@@ -801,10 +888,11 @@ def new_u_and_m(cdq, U, M, nnlist):
     return Unew, Mnew
 
 
-def wann_main(M, U, km, ctl: WannControl, record=True, precond=None, rguide=None):
-    """Restatement of wann_main for SLWF=F, no sitesym.
+def wann_main(M, U, km, ctl: WannControl, record=True, precond=None, rguide=None, slwf=None):
+    """Restatement of wann_main (no site symmetry).
     ``precond``: the tables of :func:`precond_setup` when ``ctl.precond``;
-    ``rguide``: guiding centres [3,W] (Cartesian, Angstrom) when ``ctl.guiding_centres``."""
+    ``rguide``: guiding centres [3,W] (Cartesian, Angstrom) when ``ctl.guiding_centres``;
+    ``slwf``: :class:`Slwf` for selective localisation (slwf_num < num_wann)."""
     if ctl.precond and precond is None:
         raise ValueError("precond=T needs the precond_setup tables")
     if ctl.guiding_centres and rguide is None:
@@ -822,7 +910,7 @@ def wann_main(M, U, km, ctl: WannControl, record=True, precond=None, rguide=None
         if ctl.num_no_guide_iter <= 0:                            # :435-443
             rguide, sheet = wann_phases(M, km, rguide, irguide)
             irguide = 1
-    wann_spread, rave, r2ave, rave2 = wann_omega(M, km, sheet=sheet)   # :452-457
+    wann_spread, rave, r2ave, rave2 = wann_omega(M, km, sheet=sheet, slwf=slwf)   # :452-457
     om_invariant = wann_spread.om_i
     res = WannResult(U, M, wann_spread, rave, r2ave - rave2)
     res.initial = IterRecord(0, wann_spread.om_tot, 0.0, wann_spread.copy(), rave.copy(),
@@ -846,7 +934,7 @@ def wann_main(M, U, km, ctl: WannControl, record=True, precond=None, rguide=None
                 and it % max(ctl.num_guide_cycles, 1) == 0):           # :546-555
             rguide, sheet = wann_phases(M, km, rguide, irguide)
             irguide = 1
-        cdodq = wann_domega(M, km, sheet=sheet)                       # :566-571
+        cdodq = wann_domega(M, km, sheet=sheet, slwf=slwf)            # :566-571
         if ctl.precond:                                               # :577-581
             cdodq_p = precond_search_direction(cdodq, wann_spread.om_tot, precond)
         else:
@@ -894,7 +982,7 @@ def wann_main(M, U, km, ctl: WannControl, record=True, precond=None, rguide=None
             cdq_t = cdqkeep * (ctl.trial_step / (4.0 * wbtot))        # :605
             U0, M0 = U, M
             U, M = new_u_and_m(cdq_t, U0, M0, nnlist)
-            trial_spread, rave, r2ave, rave2 = wann_omega(M, km, om_invariant, sheet=sheet)
+            trial_spread, rave, r2ave, rave2 = wann_omega(M, km, om_invariant, sheet=sheet, slwf=slwf)
             # internal_optimal_step (:1528-1596)
             fac = trial_spread.om_tot - wann_spread.om_tot
             if abs(fac) > TINY_DP:
@@ -921,7 +1009,7 @@ def wann_main(M, U, km, ctl: WannControl, record=True, precond=None, rguide=None
                 U, M = U0, M0
             U, M = new_u_and_m(cdq_a, U, M, nnlist)
             old_spread = wann_spread.copy()
-            wann_spread, rave, r2ave, rave2 = wann_omega(M, km, om_invariant, sheet=sheet)
+            wann_spread, rave, r2ave, rave2 = wann_omega(M, km, om_invariant, sheet=sheet, slwf=slwf)
         else:
             old_spread = wann_spread.copy()
             wann_spread = trial_spread.copy()

@@ -21,6 +21,9 @@ The disentanglement cases (testw90_example03 silicon, _example04 copper: num_ban
 num_wann with outer and frozen energy windows) also store the .eig eigenvalues and every
 printed '<-- DIS' line.
 
+The selective-localisation case (testw90_example26: GaAs, slwf_num = 1 with a constrained
+centre) also stores the constrained centres and every '<-- SPRD' line (Omega_IOD, Omega_D).
+
 The guiding-centre case (testpostw90_gaas_shc: spinor GaAs, 16 isolated bands,
 guiding_centres = T) has no printed wannierise trajectory; its expected values are the
 final centres and spreads of the checkpoint shipped with that test.
@@ -303,6 +306,71 @@ def build_dis(ref_root, out_dir):
         print(name, nb, nk, nntot, dis.shape, omi_final, conv.shape, om)
 
 
+def parse_sprd(path):
+    """Every '<-- SPRD' line as {key: value} (O_D, O_OD / O_IOD, O_TOT)."""
+    out = []
+    for l in open(path):
+        if l.rstrip().endswith("<-- SPRD"):
+            out.append({k: float(v) for k, v in re.findall(r"(O_[A-Z]+)=\s*([-\d.Ee+]+)", l)})
+    return out
+
+
+def build_slwf(ref_root, out_dir):
+    """testw90_example26: GaAs, 4 isolated bands, 4x4x4 k, selective localisation of
+    one WF (slwf_num = 1) with its centre constrained (slwf_constrain = T, slwf_lambda = 1)
+    to the <slwf_centres> site; the other constrained centres default to the projection
+    sites (src/readwrite.F90:3266-3357)."""
+    d = os.path.join(ref_root, "test-suite/tests/testw90_example26")
+    win = os.path.join(d, "gaas.win")
+    kw, real_lattice, kpts = parse_win(win)
+    lines = [l for l in (_strip(x) for x in open(win)) if l]
+    blocks, i = {}, 0
+    while i < len(lines):
+        if lines[i].lower().startswith("begin"):
+            name = lines[i].lower().split()[1]
+            body = []
+            i += 1
+            while not lines[i].lower().startswith("end"):
+                body.append(lines[i])
+                i += 1
+            blocks[name] = body
+        i += 1
+    W = int(kw["num_wann"])
+    sites = []
+    for line in blocks["projections"]:                 # 'f= x, y, z: orbital' lines
+        xyz = line.split(":")[0].split("=")[1]
+        sites.append([float(x) for x in xyz.replace(",", " ").split()])
+    cfrac = np.array(sites, dtype=np.float64)
+    for line in blocks["slwf_centres"]:
+        p = line.split()
+        cfrac[int(p[0]) - 1] = [float(x) for x in p[1:4]]
+    nb, nk, nntot, heads, blocks_m = parse_mmn(os.path.join(d, "gaas.mmn"))
+    A = parse_amn(os.path.join(d, "gaas.amn"))
+    bench = os.path.join(d, "benchmark.out.default.inp=gaas.win")
+    conv, initial, final, om, bvec = parse_benchmark(bench)
+    sprd = parse_sprd(bench)
+    txt = open(bench).read()
+    fin = {key: float(re.search(tag + r"\s*=\s*([-\d.]+)", txt).group(1))
+           for key, tag in (("iod_c", "Omega IOD_C"), ("d", r"Omega D  "), ("rest", "Omega Rest"),
+                            ("penalty", "Penalty func"), ("total_c", "Omega Total_C"))}
+    tf = lambda v: float(str(v).strip(".").lower().startswith("t"))
+    knobs = dict(num_wann=W, num_iter=int(kw.get("num_iter", 100)), num_cg_steps=int(kw.get("num_cg_steps", 5)),
+                 conv_tol=float(kw.get("conv_tol", "1e-10").replace("d", "e")),
+                 conv_window=int(kw.get("conv_window", -1)), trial_step=float(kw.get("trial_step", 2.0)),
+                 search_shells=int(kw.get("search_shells", 36)), slwf_num=int(kw["slwf_num"]),
+                 slwf_constrain=tf(kw.get("slwf_constrain", "f")), slwf_lambda=float(kw.get("slwf_lambda", 1.0)))
+    np.savez_compressed(
+        os.path.join(out_dir, "slwf26.npz"),
+        real_lattice=real_lattice, kpt_latt=kpts, mp_grid=np.array([int(x) for x in kw["mp_grid"].split()[:3]]),
+        num_bands=nb, num_kpts=nk, nntot=nntot, mmn_heads=heads, mmn_blocks=blocks_m, amn=A,
+        knobs=np.array([knobs[k] for k in sorted(knobs)], dtype=np.float64), knob_names=np.array(sorted(knobs)),
+        slwf_centres_frac=cfrac, conv=conv, centres_initial=initial, centres_final=final,
+        sprd=np.array([[x.get("O_IOD", np.nan), x.get("O_D", np.nan), x.get("O_TOT", np.nan)] for x in sprd]),
+        omega_final_slwf=np.array([fin["iod_c"], fin["d"], fin["rest"], fin["penalty"], fin["total_c"]]),
+        bvec_table=bvec)
+    print("slwf26", nb, nk, nntot, conv.shape, len(sprd), fin)
+
+
 def build(ref_root, out_dir):
     for name, (sub, seed) in CASES.items():
         d = os.path.join(ref_root, sub)
@@ -338,3 +406,4 @@ if __name__ == "__main__":
     build(root, os.path.dirname(os.path.abspath(__file__)))
     build_guiding(root, os.path.dirname(os.path.abspath(__file__)))
     build_dis(root, os.path.dirname(os.path.abspath(__file__)))
+    build_slwf(root, os.path.dirname(os.path.abspath(__file__)))

@@ -59,6 +59,18 @@ def guiding(d):
     return ctl, (d["proj_site_frac"] @ d["real_lattice"]).T
 
 
+def slwf(d):
+    """(WannControl, Slwf) of the selective-localisation case: constrained centres in
+    Cartesian Angstrom (utility_frac_to_cart of the fractional sites)."""
+    from oracle import w90_oracle as O
+    kn = d["knobs"]
+    ctl = O.WannControl(num_iter=int(kn["num_iter"]), num_cg_steps=int(kn["num_cg_steps"]),
+                        conv_tol=float(kn["conv_tol"]), conv_window=int(kn["conv_window"]),
+                        trial_step=float(kn["trial_step"]))
+    cen = (d["slwf_centres_frac"] @ d["real_lattice"]).T if kn["slwf_constrain"] else None
+    return ctl, O.Slwf(int(kn["slwf_num"]), float(kn["slwf_lambda"]), cen)
+
+
 DIS_CASES = ["silicon_dis", "copper_dis", "basic2_dis", "gaas192_dis"]
 
 
@@ -73,23 +85,27 @@ def dis_control(d):
                         frozen_states=bool(kn["frozen_states"]))
 
 
-def conv_sensitivity(M0, U0, km, ctl, noise=1e-14, runs=2):
+def conv_sensitivity(M0, U0, km, ctl, noise=1e-14, runs=2, slwf=None, grad=False):
     """Per iteration, the largest change of the oracle's own wann_main spread when M0 is
     perturbed by `noise` (relative, seeded): the part of a printed trajectory that no FP64
-    implementation can reproduce more closely."""
+    implementation can reproduce more closely.  grad=True also returns the same for the
+    RMS gradient column."""
     import numpy as np
 
     from oracle import w90_oracle as O
-    base = O.wann_main(M0, U0, km, ctl)
+    base = O.wann_main(M0, U0, km, ctl, slwf=slwf)
     ref = {x.iter: x.spread.om_tot for x in [base.initial] + base.iters}
+    gref = {x.iter: x.rms_grad for x in [base.initial] + base.iters}
     sens = {i: 0.0 for i in ref}
+    gsens = {i: 0.0 for i in ref}
     rng = np.random.default_rng(2024)
     for _ in range(runs):
-        r = O.wann_main(M0 * (1 + noise * rng.standard_normal(M0.shape)), U0, km, ctl)
+        r = O.wann_main(M0 * (1 + noise * rng.standard_normal(M0.shape)), U0, km, ctl, slwf=slwf)
         for x in [r.initial] + r.iters:
             if x.iter in sens:
                 sens[x.iter] = max(sens[x.iter], abs(x.spread.om_tot - ref[x.iter]))
-    return sens
+                gsens[x.iter] = max(gsens[x.iter], abs(x.rms_grad - gref[x.iter]))
+    return (sens, gsens) if grad else sens
 
 
 def conv_tolerance(sens, it, spread, floor=2e-10, factor=10.0):
@@ -97,3 +113,10 @@ def conv_tolerance(sens, it, spread, floor=2e-10, factor=10.0):
     measured sensitivity (at least the metric's 1e-8 relative)."""
     s = sens.get(int(it), 0.0)
     return floor if s < 0.1 * floor else max(factor * s, 1e-8 * abs(spread))
+
+
+def grad_tolerance(gsens, it, rms, factor=10.0):
+    """The printed RMS gradient: 1e-6 + 1e-3 relative (its roundoff floor near a minimum),
+    or `factor` times its measured sensitivity where that is larger (a converged SLWF run,
+    whose non-objective gauge is free, moves it by up to 1e-4 under a 1e-14 perturbation)."""
+    return max(1e-6 + 1e-3 * rms, factor * gsens.get(int(it), 0.0))

@@ -1,7 +1,9 @@
 """The oracle against the reference's own regression outputs (parity pin of the oracle).
 
 Inputs and expected values are the reference test suite's (test-suite/tests/testw90_example02,
-_example01, _example05, _basic1, and the preconditioned _precond_1 / _precond_2), packed by tests/golden/make_fixtures.py.  Every printed
+_example01, _example05, _basic1, the preconditioned _precond_1 / _precond_2, the
+selective-localisation _example26, the disentanglement cases and the guiding-centre
+checkpoint), packed by tests/golden/make_fixtures.py.  Every printed
 <-- CONV spread (10 decimals) must match to 2e-10 A^2 (RMS gradient to 1e-3 relative above a 1e-6 roundoff floor), final centres to 1e-6 A (printed to
 6 decimals), spreads to 1e-7 A^2 and the b-vector / weight table to 1e-6.
 """
@@ -84,3 +86,52 @@ def test_oracle_disentanglement_reproduces_reference(name):
         assert abs(rec[int(it)].spread.om_tot - spread) < tol, (int(it), rec[int(it)].spread.om_tot, spread, tol)
     np.testing.assert_allclose(r.centres.T, d["centres_final"][:, :3], atol=1.01e-6)
     np.testing.assert_allclose([r.spread.om_i, r.spread.om_tot], d["omega_final"][[0, 3]], atol=1.01e-9)
+
+
+def test_oracle_selective_localisation_reproduces_reference():
+    """testw90_example26 (GaAs, 4 WFs, 4x4x4 k, 100 iterations): selective localisation
+    of WF 1 (slwf_num = 1) with its centre constrained (slwf_constrain = T,
+    slwf_lambda = 1).  Every printed spread within 2e-10 A^2 where the trajectory is
+    stable at that level, else within ten times the spread that a 1e-14 perturbation of
+    M0 causes in the oracle itself; the RMS gradient likewise; the printed Omega_IOD
+    (Omega_IOD + Omega_nu) and Omega_D of every '<-- SPRD' line; the final centres, spreads
+    and the Omega IOD_C / D / Rest / Penalty / Total_C block (the non-objective WFs' parts
+    to their roundoff sensitivity)."""
+    d = G.load("slwf26")
+    kn = d["knobs"]
+    km = O.kmesh_get(d["real_lattice"], d["kpt_latt"], int(kn["search_shells"]))
+    tab = d["bvec_table"]
+    np.testing.assert_allclose(km["bk"][0], tab[:, :3], atol=1e-6)
+    np.testing.assert_allclose(km["wb"], tab[:, 3], atol=1e-6)
+    M = G.assemble_m(d, km["nnlist"], km["nncell"])
+    U0, M0 = O.overlap_project(M, d["amn"], km["nnlist"])
+    ctl, sl = G.slwf(d)
+    r = O.wann_main(M0, U0, km, ctl, slwf=sl)
+    sens, gsens = G.conv_sensitivity(M0, U0, km, ctl, runs=3, slwf=sl, grad=True)
+    recs = [r.initial] + r.iters
+    assert len(recs) == len(d["conv"]) == len(d["sprd"])
+    for got, (it, delta, rms, spread), (iod, od, tot) in zip(recs, d["conv"], d["sprd"]):
+        assert got.iter == int(it)
+        tol = G.conv_tolerance(sens, it, spread)
+        assert abs(got.spread.om_tot - spread) < tol, (it, got.spread.om_tot, spread, tol)
+        assert abs(got.rms_grad - rms) < G.grad_tolerance(gsens, it, rms), (it, got.rms_grad, rms)
+        # SPRD lines carry 7 decimals
+        assert abs(got.spread.om_iod + got.spread.om_nu - iod) < 6e-8 + tol
+        assert abs(got.spread.om_d - od) < 6e-8 + tol
+    fin = d["centres_final"]
+    s = sl.num
+    # the objective WF is pinned; the others are outside the functional (their gauge is
+    # free), so where the run stops them depends on roundoff: a 1e-14 perturbation of M0
+    # moves their spreads and centres by up to 2e-6 in the oracle itself
+    np.testing.assert_allclose(r.centres.T[:s], fin[:s, :3], rtol=0, atol=1.01e-6)
+    np.testing.assert_allclose(r.spreads[:s], fin[:s, 3], rtol=0, atol=1.01e-8)
+    np.testing.assert_allclose(r.centres.T[s:], fin[s:, :3], rtol=0, atol=2e-5)
+    np.testing.assert_allclose(r.spreads[s:], fin[s:, 3], rtol=0, atol=2e-5)
+    iod_c, om_d, rest, penalty, total_c = d["omega_final_slwf"]
+    sp = r.spread
+    assert abs(sp.om_iod + sp.om_nu - iod_c) < 1.01e-9
+    assert abs(sp.om_d - om_d) < 1.01e-9
+    assert abs(r.spreads.sum() + sp.om_tot - rest) < 6e-5
+    rnr0n2 = ((r.centres[:, :sl.num] - sl.centres[:, :sl.num]) ** 2).sum()     # :829-836
+    assert abs(rnr0n2 - penalty) < 1.01e-9
+    assert abs(sp.om_tot - total_c) < 1.01e-9
