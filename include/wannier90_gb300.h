@@ -49,7 +49,15 @@ void cset_option_float33(void* handle, const char* keyword, const double* value3
 /* value: double[x][y] row-major (e.g. kpoints: x = num_kpts, y = 3) */
 void cset_option_floatxy(void* handle, const char* keyword, const double* values, int x, int y);
 
-/* ---- process options, build the k-mesh: src/c_interface.F90:49-68 ---------------- */
+/* ---- process options, build the k-mesh: src/c_interface.F90:49-68 ----------------
+ * Keywords read by the engine besides the system ones: num_iter, num_cg_steps, conv_tol,
+ * conv_window, trial_step / fixed_step, precond (+ mp_grid), guiding_centres,
+ * num_no_guide_iter, num_guide_cycles, slwf_num, slwf_constrain, slwf_lambda, dis_*,
+ * search_shells, kmesh_tol, iprint.  Block data the C binding cannot pass as text comes
+ * as floatxy tables: guiding_centres_frac (num_wann x 3, the projection sites) and
+ * slwf_centres_frac (num_wann x 3, the constrained centres: the <slwf_centres> rows
+ * over the projection sites; without it slwf_constrain uses guiding_centres_frac).
+ * site_symmetry, gamma_only, conv_noise_amp > 0 and dis_spheres_num > 0 give ierr 5. */
 void cinput_setopt(void* handle, const char* seedname, int* ierr, int comm);
 
 /* ---- data pointers (caller keeps ownership): src/c_interface.F90:82-127 ----------- */
@@ -87,7 +95,10 @@ void cget_spreads(void* handle, double* spreads);
  *   exports to Fortran only.  On entry u holds A(k) (num_wann x num_wann), m the raw
  *   overlaps; on exit u = Z V^dagger and m = U^dagger M U(k+b).
  * cget_omega: (Omega_I, Omega_D, Omega_OD, Omega_total) of the last wannierisation
- *   (common_data%omega / wann_spread, src/wannierise.F90:457-470). */
+ *   (common_data%omega / wann_spread, src/wannierise.F90:457-470).  With selective
+ *   localisation (slwf_num < num_wann) Omega_I is left as it was (the disentanglement's,
+ *   else 0), Omega_D is (1 - lambda) times the objective WFs' part and the third entry is
+ *   Omega_IOD + Omega_nu, what the reference prints as O_IOD. */
 void cproject_overlap(void* handle, int* ierr);
 void cget_omega(void* handle, double* omega4);
 /* cget_gkpb: nncell of kmesh_info ([nntot][nk][3] int32), the G offsets of k+b
@@ -99,7 +110,9 @@ void cget_gkpb(void* handle, int* gkpb);
 const char* w90g_last_error(void* handle);
 /* Per-iteration record of the last wannierisation: rows of 10 doubles
  *   (iter, delta Omega, RMS gradient, Omega_total, Omega_D, Omega_OD, lquad, alphamin,
- *    device timestamp ns, 0) for iter = 0 (initial state) .. niter.
+ *    device timestamp ns, Omega_nu) for iter = 0 (initial state) .. niter; with
+ *   selective localisation Omega_OD holds Omega_IOD + Omega_nu and Omega_nu the centre
+ *   constraint's term (0 otherwise).
  * Returns the number of rows written (<= max_rows). */
 int w90g_get_log(void* handle, double* rows, int max_rows);
 /* Disentanglement record of the last cdisentangle: rows of 5 doubles

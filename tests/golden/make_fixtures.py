@@ -364,7 +364,7 @@ def build_slwf(ref_root, out_dir):
         real_lattice=real_lattice, kpt_latt=kpts, mp_grid=np.array([int(x) for x in kw["mp_grid"].split()[:3]]),
         num_bands=nb, num_kpts=nk, nntot=nntot, mmn_heads=heads, mmn_blocks=blocks_m, amn=A,
         knobs=np.array([knobs[k] for k in sorted(knobs)], dtype=np.float64), knob_names=np.array(sorted(knobs)),
-        slwf_centres_frac=cfrac, conv=conv, centres_initial=initial, centres_final=final,
+        slwf_centres_frac=cfrac, proj_site_frac=np.array(sites, dtype=np.float64), conv=conv, centres_initial=initial, centres_final=final,
         sprd=np.array([[x.get("O_IOD", np.nan), x.get("O_D", np.nan), x.get("O_TOT", np.nan)] for x in sprd]),
         omega_final_slwf=np.array([fin["iod_c"], fin["d"], fin["rest"], fin["penalty"], fin["total_c"]]),
         bvec_table=bvec)

@@ -65,6 +65,13 @@ struct Handle {
   // sites, passed as the engine option guiding_centres_frac (num_wann x 3, fractional)
   int guiding = 0, no_guide_iter = 0, guide_cycles = 1;
   std::vector<double> rguide0;   // [3][W] Cartesian
+  // selective localisation (wann_slwf_type): slwf_num objective WFs (0 = off), lambda_loc
+  // and the constrained centres [3][W] (Cartesian; empty = unconstrained), from slwf_num /
+  // slwf_constrain / slwf_lambda and the engine option slwf_centres_frac (num_wann x 3,
+  // fractional; the <slwf_centres> block merged over the projection sites)
+  int slwf_num = 0;
+  double slwf_lambda = 0.0;
+  std::vector<double> slwf_c;
   // caller data
   double* m_local = nullptr;
   double* u_matrix = nullptr;
@@ -185,11 +192,22 @@ void print_wout(const Handle* h, const w90g::ProblemResult& r) {
     const double tsec = (lg[8] - t0) * 1e-9;
     std::printf(" %6d  %s  %15.10f  %18.10f   %8.2f  <-- CONV\n", it, fort_e(lg[1], 12, 3).c_str(), lg[2], lg[3],
                 tsec);
-    std::printf("        O_D=%15.7f O_OD=%15.7f O_TOT=%15.7f <-- SPRD\n", lg[4], lg[5], lg[3]);
-    if (it > 0) {
-      const double* pv = &r.log[(size_t)(i - 1) * w90g::kLogStride];
-      std::printf(" Delta: O_D=%s O_OD=%s O_TOT=%s <-- DLTA\n", fort_e(lg[4] - pv[4], 15, 7).c_str(),
-                  fort_e(lg[5] - pv[5], 15, 7).c_str(), fort_e(lg[3] - pv[3], 15, 7).c_str());
+    const double* pv = it > 0 ? &r.log[(size_t)(i - 1) * w90g::kLogStride] : nullptr;
+    if (h->slwf_num > 0) {
+      // O_IOD = Omega_IOD + Omega_nu; its Delta holds Omega_nu fixed (src/wannierise.F90:712-740)
+      if (it == 0) {
+        std::printf("       O_D=%15.7f O_IOD=%15.7f O_TOT=%15.7f <-- SPRD\n", lg[4], lg[5], lg[3]);
+      } else {
+        std::printf("       O_IOD=%15.7f O_D=%15.7f O_TOT=%15.7f <-- SPRD\n", lg[5], lg[4], lg[3]);
+        std::printf("Delta: O_IOD=%s O_D=%s O_TOT=%s <-- DLTA\n",
+                    fort_e((lg[5] - lg[9]) - (pv[5] - pv[9]), 15, 7).c_str(), fort_e(lg[4] - pv[4], 15, 7).c_str(),
+                    fort_e(lg[3] - pv[3], 15, 7).c_str());
+      }
+    } else {
+      std::printf("        O_D=%15.7f O_OD=%15.7f O_TOT=%15.7f <-- SPRD\n", lg[4], lg[5], lg[3]);
+      if (it > 0)
+        std::printf(" Delta: O_D=%s O_OD=%s O_TOT=%s <-- DLTA\n", fort_e(lg[4] - pv[4], 15, 7).c_str(),
+                    fort_e(lg[5] - pv[5], 15, 7).c_str(), fort_e(lg[3] - pv[3], 15, 7).c_str());
     }
     std::printf(" %s\n", std::string(78, '-').c_str());
   }
@@ -205,10 +223,35 @@ void print_wout(const Handle* h, const w90g::ProblemResult& r) {
     cen4[3 * W + n] = r.spreads[n];
   }
   print_centres(h, cen4.data());
-  std::printf("        Spreads (Ang^2)       Omega I      = %15.9f\n", r.spread.om_i);
-  std::printf("        ================       Omega D      = %15.9f\n", r.spread.om_d);
-  std::printf("                               Omega OD     = %15.9f\n", r.spread.om_od);
-  std::printf("    Final Spread (Ang^2)       Omega Total  = %15.9f\n", r.spread.om_tot);
+  if (h->slwf_num > 0) {
+    // src/wannierise.F90:827-865
+    double ssum = 0.0, pen = 0.0;
+    for (int n = 0; n < W; ++n) ssum += r.spreads[n];
+    const bool constrained = !h->slwf_c.empty();
+    if (constrained)
+      for (int n = 0; n < h->slwf_num; ++n)
+        for (int i = 0; i < 3; ++i) {
+          const double dx = r.centres[n * 3 + i] - h->slwf_c[(size_t)i * W + n];
+          pen += dx * dx;
+        }
+    if (constrained) {
+      std::printf("         Spreads (Ang^2)       Omega IOD_C   = %15.9f\n", r.spread.om_od);
+      std::printf("        ================       Omega D       = %15.9f\n", r.spread.om_d);
+      std::printf("                               Omega Rest    = %15.9f\n", ssum + r.spread.om_tot);
+      std::printf("                               Penalty func  = %15.9f\n", pen);
+      std::printf("    Final Spread (Ang^2)       Omega Total_C = %15.9f\n", r.spread.om_tot);
+    } else {
+      std::printf("         Spreads (Ang^2)       Omega IOD    = %15.9f\n", r.spread.om_od);
+      std::printf("        ================       Omega D      = %15.9f\n", r.spread.om_d);
+      std::printf("                               Omega Rest   = %15.9f\n", ssum + r.spread.om_tot);
+      std::printf("    Final Spread (Ang^2)       Omega Total  = %15.9f\n", r.spread.om_tot);
+    }
+  } else {
+    std::printf("         Spreads (Ang^2)       Omega I      = %15.9f\n", r.spread.om_i);
+    std::printf("        ================       Omega D      = %15.9f\n", r.spread.om_d);
+    std::printf("                               Omega OD     = %15.9f\n", r.spread.om_od);
+    std::printf("    Final Spread (Ang^2)       Omega Total  = %15.9f\n", r.spread.om_tot);
+  }
   std::printf(" %s\n", std::string(78, '-').c_str());
   std::fflush(stdout);
 }
@@ -239,6 +282,9 @@ int build_spec(Handle* h, ProblemSpec& s) {
     s.bka = h->km.bka;
     s.neigh = h->km.neigh;
   }
+  s.slwf_num = h->slwf_num;
+  s.slwf_lambda = h->slwf_lambda;
+  s.slwf_c = h->slwf_c;
   s.precond = h->precond;
   s.nrpts = h->nrpts;
   s.pc_kr = h->pc_kr;
@@ -280,7 +326,9 @@ int do_project(Handle* h, double* m, double* u, cudaMemcpyKind in, cudaMemcpyKin
 // copy one solve's result into the handle (the library's wannier_data / omega fields);
 // returns the ierr of the solve (non-finite spread, failed unitarity check)
 int apply_result(Handle* h, const w90g::ProblemResult& r, bool print) {
-  h->omega[0] = r.spread.om_i;
+  // with selective localisation wann_main leaves omega%invariant as it was
+  // (src/wannierise.F90:460-470): the disentanglement's Omega_I, else 0
+  h->omega[0] = h->slwf_num > 0 ? (h->have_disentangled ? h->omega_invariant : 0.0) : r.spread.om_i;
   h->omega[1] = r.spread.om_d;
   h->omega[2] = r.spread.om_od;
   h->omega[3] = r.spread.om_tot;
@@ -665,11 +713,10 @@ void cinput_setopt(void* hv, const char* seedname, int* ierr, int comm) {
   // with gpu_tensor: gpu_tensor_exp = 1 (default) also runs exp(s D) and U dU on tensor cores
   h->gpu_tensor_exp = get_num(h, "gpu_tensor_exp", v) ? (int)v : 1;
   // options on wann_main's code path that the engine does not implement
-  const char* unsupported[] = {"slwf_num", "slwf_constrain", "site_symmetry",
-                               "gamma_only", "dis_spheres_num"};
+  const char* unsupported[] = {"site_symmetry", "gamma_only", "dis_spheres_num"};
   for (const char* k : unsupported) {
     if (get_num(h, k, v)) {
-      const bool active = (std::string(k) == "slwf_num") ? ((int)v != h->num_wann) : (v != 0.0);
+      const bool active = v != 0.0;
       if (active) {
         *ierr = fail(h, 5, std::string("Option '") + k + "' is not supported by the GPU engine");
         return;
@@ -710,6 +757,60 @@ void cinput_setopt(void* hv, const char* seedname, int* ierr, int comm) {
         for (int i = 0; i < 3; ++i) x += git->second.v[(size_t)n * 3 + i] * h->real_lattice[i * 3 + j];
         h->rguide0[(size_t)j * W + n] = x;
       }
+  }
+  // selective localisation and constrained centres
+  // (src/wannier90_readwrite.F90:757-802, :1660-1708; src/readwrite.F90:3266-3357)
+  {
+    h->slwf_num = 0;
+    h->slwf_lambda = 0.0;
+    h->slwf_c.clear();
+    const int W = h->num_wann;
+    int snum = W;
+    if (get_num(h, "slwf_num", v)) {
+      snum = (int)v;
+      if (snum > W || snum < 1) {
+        *ierr = fail(h, 5, "Error: slwf_num must be an integer between 1 and num_wann");
+        return;
+      }
+    }
+    const bool selective = snum < W;
+    bool constrain = get_num(h, "slwf_constrain", v) && v != 0.0;
+    if (constrain && !selective) {
+      if (h->iprint > 0) std::printf(" No selective localisation requested. Ignoring constraints on centres\n");
+      constrain = false;
+    }
+    double lambda = 1.0;
+    if (get_num(h, "slwf_lambda", v)) {
+      lambda = v;
+      if (lambda < 0.0) {
+        *ierr = fail(h, 5, "Error: slwf_lambda  must be positive.");
+        return;
+      }
+    }
+    if (selective) {
+      h->slwf_num = snum;
+      if (constrain) {
+        auto cit = h->opts.find("slwf_centres_frac");
+        if (cit == h->opts.end()) cit = h->opts.find("guiding_centres_frac");
+        if (cit == h->opts.end()) {
+          *ierr = fail(h, 5, "Error: slwf_constrain = true, but neither <slwf_centre> block  nor "
+                             "<projection_block> are specified.");
+          return;
+        }
+        if (cit->second.cols != 3 || cit->second.rows < W) {
+          *ierr = fail(h, 5, "Error: slwf_centres_frac must be num_wann x 3");
+          return;
+        }
+        h->slwf_lambda = lambda;
+        h->slwf_c.assign((size_t)3 * W, 0.0);
+        for (int n = 0; n < W; ++n)
+          for (int j = 0; j < 3; ++j) {
+            double x = 0.0;   // utility_frac_to_cart
+            for (int i = 0; i < 3; ++i) x += cit->second.v[(size_t)n * 3 + i] * h->real_lattice[i * 3 + j];
+            h->slwf_c[(size_t)j * W + n] = x;
+          }
+      }
+    }
   }
   // disentanglement keywords (src/readwrite.F90:651-682, src/wannier90_readwrite.F90:824-854)
   {

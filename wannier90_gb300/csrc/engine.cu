@@ -101,6 +101,11 @@ int Engine::setup(const std::vector<ProblemSpec>& specs, std::string& err) {
       err = "guiding_centres: centres or b-direction tables missing";
       return 5;
     }
+    if (s.slwf_num < 0 || s.slwf_num >= s.W ||
+        (s.slwf_num > 0 && !s.slwf_c.empty() && s.slwf_c.size() != (size_t)3 * s.W)) {
+      err = "slwf: slwf_num outside 1..num_wann-1 or constrained centres not num_wann x 3";
+      return 5;
+    }
     if (s.precond && (s.nrpts < 1 || s.pc_kr.size() != (size_t)2 * s.K * s.nrpts ||
                       s.pc_r2.size() != (size_t)s.nrpts || s.pc_ndeg.size() != (size_t)s.nrpts)) {
       err = "precond: Wigner-Seitz tables missing or inconsistent";
@@ -111,7 +116,7 @@ int Engine::setup(const std::vector<ProblemSpec>& specs, std::string& err) {
   std::ostringstream key;
   for (const auto& s : specs)
     key << s.W << ',' << s.K << ',' << s.B << ',' << s.ctl.num_iter << ',' << s.tensor << ',' << s.tensor_exp << ','
-        << s.precond << ',' << s.nrpts << ',' << s.guiding << ';';
+        << s.precond << ',' << s.nrpts << ',' << s.guiding << ',' << (s.slwf_num > 0) << ';';
   specs_ = specs;
   if (arena_ && key.str() == layout_key_) {
     // refresh the read-only tables (they may differ at equal shapes)
@@ -132,6 +137,7 @@ int Engine::setup(const std::vector<ProblemSpec>& specs, std::string& err) {
       }
       hprobs_[p].ctl = s.ctl;
       hprobs_[p].wbtot = s.wbtot;
+      if (int rc = set_slwf(p, err)) return rc;
     }
     W90G_CHECK(cudaMemcpyAsync(dprobs_, hprobs_.data(), hprobs_.size() * sizeof(Problem), cudaMemcpyHostToDevice, stream()));
     return 0;
@@ -165,10 +171,11 @@ struct Sizes {
   size_t m0s, m0e;
   size_t pkr, pr2, pgr, pgp, ppart;
   size_t gbka, gneigh, grg, gsheet, gcsheet;
+  size_t slwf;
   size_t total() const {
     return 2 * M + 2 * U + 3 * KWW + work + tbuf + 2 * diag + offd + gpart + cen + log + logc + nn + bk + wb + st +
            op1 + op2 + m0 + u0 + inv + fr + m0s + m0e + pkr + 2 * pr2 + pgr + pgp + ppart + gbka + gneigh + grg + gsheet +
-           gcsheet;
+           gcsheet + slwf;
   }
 };
 
@@ -219,6 +226,7 @@ Sizes problem_sizes(const ProblemSpec& s, int wp, int* pc_tiles) {
     z.ppart = align_up(te * ((K + 15) / 16) * 8);
     if (pc_tiles) *pc_tiles = std::max(*pc_tiles, (int)(te * ((std::max(K, NR) + 15) / 16)));
   }
+  z.slwf = s.slwf_num > 0 ? align_up(3 * W * 8) : 0;
   z.gbka = z.gneigh = z.grg = z.gsheet = z.gcsheet = 0;
   if (s.guiding) {
     z.gbka = align_up((size_t)s.nnh * 3 * 8);
@@ -367,6 +375,8 @@ int Engine::alloc(std::string& err) {
       P.sheet = (double*)take(z.gsheet);
       P.csheet = (double2*)take(z.gcsheet);
     }
+    P.slwf_c = z.slwf ? (const double*)take(z.slwf) : nullptr;
+    if (int rc = set_slwf(p, err)) return rc;
     P.precond = s.precond;
     P.nrpts = s.precond ? s.nrpts : 0;
     if (s.precond) {
@@ -401,6 +411,31 @@ int Engine::alloc(std::string& err) {
   for (const auto& s : specs_) tensor_exp_ = tensor_exp_ && s.tensor_exp;
   if (tensor_wp_) W90G_CHECK(oz_set_attributes(tensor_wp_));
   if (tensor_exp_) W90G_CHECK(oz_exp_set_attributes(tensor_wp_));
+  return 0;
+}
+
+// selective-localisation fields of problem p from its spec (the centre array is part of
+// the layout when slwf_num > 0; zero when unconstrained)
+int Engine::set_slwf(int p, std::string& err) {
+  const auto& s = specs_[p];
+  Problem& P = hprobs_[p];
+  P.slwf_num = s.slwf_num;
+  P.slwf_lambda = 0.0;
+  P.slwf_nu0 = 0.0;
+  if (s.slwf_num <= 0) return 0;
+  std::vector<double> c((size_t)3 * s.W, 0.0);
+  if (!s.slwf_c.empty()) {
+    // lambda_loc = lambda only with constrained centres (src/wannierise.F90:445-450)
+    c = s.slwf_c;
+    P.slwf_lambda = s.slwf_lambda;
+    double c2 = 0.0;
+    for (int n = 0; n < s.slwf_num; ++n)
+      for (int i = 0; i < 3; ++i) c2 += c[(size_t)i * s.W + n] * c[(size_t)i * s.W + n];
+    P.slwf_nu0 = s.slwf_lambda * c2;
+  }
+  slwf_host_.resize(hprobs_.size());
+  slwf_host_[p] = c;   // the copy below reads it asynchronously
+  W90G_CHECK(cudaMemcpyAsync((void*)P.slwf_c, slwf_host_[p].data(), c.size() * 8, cudaMemcpyHostToDevice, stream()));
   return 0;
 }
 

@@ -29,6 +29,11 @@ struct ProblemSpec {
   int guiding = 0, no_guide_iter = 0, guide_cycles = 1, nnh = 0;
   std::vector<double> rguide0, bka;
   std::vector<int> neigh;
+  // selective localisation: slwf_num objective WFs (0 = off, i.e. slwf_num = num_wann),
+  // lambda_loc, constrained centres [3][W] (Cartesian, Angstrom; empty = unconstrained)
+  int slwf_num = 0;
+  double slwf_lambda = 0.0;
+  std::vector<double> slwf_c;
 };
 
 struct ProblemResult {
@@ -104,6 +109,7 @@ class Engine {
   void launch_exp(cudaStream_t s, int which);
   int prepare_tensor(cudaStream_t st, std::string& err);
   int init_states(std::string& err);
+  int set_slwf(int p, std::string& err);
 
   std::vector<ProblemSpec> specs_;
   std::vector<Problem> hprobs_;
@@ -132,6 +138,7 @@ class Engine {
   long long launches_ = 0;
   int launched_iters_ = 0;
   std::vector<double> guide_init_;   // host staging of csheet = 1
+  std::vector<std::vector<double>> slwf_host_;   // host staging of the constrained centres
   bool async_alloc_ = false;
   double last_exp_products_ = 0.0;
 };

@@ -96,13 +96,17 @@ __global__ void k_mdiag(const Problem* __restrict__ probs, WorkMap wm) {
 }
 
 // ----------------------------------------------------------------------------
-// wann_omega (src/wannierise.F90:1979-2284), non-SLWF branch, as a deterministic
-// three-pass reduction over chunks of kOmegaChunk (k,b) blocks:
+// wann_omega (src/wannierise.F90:1979-2284) as a deterministic three-pass reduction
+// over chunks of kOmegaChunk (k,b) blocks:
 //   p1: per chunk  P_n = sum wb b ln_n (3W), q_n = sum wb (1 - |M_nn|^2 + ln_n^2) (W),
 //       sum wb offd, and (first pass only) sum wb (W - sum|M|^2)
 //   p2: rave = -(1/K) sum_chunks P (same fixed order in every CTA), then the chunk's
 //       part of sum wb (ln_n + b.rave_n)^2
 //   p3: one CTA per problem: totals, centres, spreads, Omega terms.
+// Selective localisation (slwf_num = s > 0, :2144-2211): p1's off-diagonal slot holds
+// sum over n < s of wb (1 - |M_nn|^2 + lambda ln_n^2) (Omega_IOD) and its Omega_I slot
+// sum over n < s of 2 wb lambda ln_n (b.c_n) (the k-sum of Omega_nu); p2 sums over n < s
+// only; p3 forms Omega_D = (1 - lambda) dd / K, Omega_nu = that sum / K + lambda sum |c_n|^2.
 // slot: 0 trial, 1 optimal step, 2 initial (accepted).  Fixed thread ownership and
 // fixed-order reductions make the result independent of scheduling.
 // ----------------------------------------------------------------------------
@@ -131,6 +135,15 @@ __global__ void __launch_bounds__(256) k_omega_p1(const Problem* __restrict__ pr
   const int n = t % W, sub = t / W;
   const bool act = sub < nsub;
   double r0 = 0, r1 = 0, r2 = 0, q = 0;
+  // selective localisation: this thread's WF is an objective one
+  const bool obj = P.slwf_num > 0 && n < P.slwf_num;
+  const double lam = P.slwf_lambda;
+  double iod = 0.0, nu = 0.0, c0 = 0.0, c1 = 0.0, c2 = 0.0;
+  if (obj) {
+    c0 = P.slwf_c[n];
+    c1 = P.slwf_c[W + n];
+    c2 = P.slwf_c[2 * W + n];
+  }
   if (act) {
     for (int kb = kb0 + sub; kb < kb1; kb += nsub) {
       const double w = P.wb[kb % B];
@@ -142,6 +155,11 @@ __global__ void __launch_bounds__(256) k_omega_p1(const Problem* __restrict__ pr
       r1 = fma(wl, bv[1], r1);
       r2 = fma(wl, bv[2], r2);
       q += w * (1.0 - a + l * l);
+      if (obj) {
+        const double bc = bv[0] * c0 + bv[1] * c1 + bv[2] * c2;
+        iod += w * (1.0 - a + lam * l * l);
+        nu += 2.0 * wl * lam * bc;
+      }
     }
   }
   double* out = P.opart1 + (size_t)ch * (4 * W + 2);
@@ -155,6 +173,16 @@ __global__ void __launch_bounds__(256) k_omega_p1(const Problem* __restrict__ pr
       out[c * W + t] = sacc;
     }
     __syncthreads();
+  }
+  if (P.slwf_num > 0) {
+    // Omega_IOD in the off-diagonal slot, the k-sum of Omega_nu in the Omega_I slot
+    iod = block_sum(act ? iod : 0.0, red);
+    nu = block_sum(act ? nu : 0.0, red);
+    if (t == 0) {
+      out[4 * W] = iod;
+      out[4 * W + 1] = nu;
+    }
+    return;
   }
   const bool first = (slot == 2) && st->first_pass;
   double od = 0.0, oi = 0.0;
@@ -212,7 +240,8 @@ __global__ void __launch_bounds__(256) k_omega_p2(const Problem* __restrict__ pr
   const int nsub = blockDim.x / W;
   const int n = t % W, sub = t / W;
   double dd = 0.0;
-  if (sub < nsub) {
+  // selective localisation: Omega_D over the objective WFs only
+  if (sub < nsub && (P.slwf_num == 0 || n < P.slwf_num)) {
     const double x0 = s_rave[n], x1 = s_rave[W + n], x2 = s_rave[2 * W + n];
     for (int kb = kb0 + sub; kb < kb1; kb += nsub) {
       const double w = P.wb[kb % B];
@@ -286,16 +315,27 @@ __global__ void __launch_bounds__(256) k_omega_p3(const Problem* __restrict__ pr
   __syncthreads();
   if (t == 0) {
     const double od = s_sum[0], oi = s_sum[1], dd = s_sum[2];
-    const bool first = (slot == 2) && st->first_pass;
-    if (first) {
-      st->om_invariant = oi / (double)K;
-      st->first_pass = 0;
-    }
     Spread sp;
-    sp.om_i = st->om_invariant;
-    sp.om_d = dd / (double)K;
-    sp.om_od = od / (double)K;
-    sp.om_tot = sp.om_i + sp.om_d + sp.om_od;
+    if (P.slwf_num > 0) {
+      // Omega_tot = Omega_IOD + Omega_D + Omega_nu (Omega_I is never formed); om_od
+      // carries Omega_IOD + Omega_nu, what the reference prints as O_IOD
+      const double iod = od / (double)K;
+      sp.om_nu = oi / (double)K + P.slwf_nu0;
+      sp.om_i = 0.0;
+      sp.om_d = (1.0 - P.slwf_lambda) * dd / (double)K;
+      sp.om_od = iod + sp.om_nu;
+      sp.om_tot = iod + sp.om_d + sp.om_nu;
+    } else {
+      if ((slot == 2) && st->first_pass) {
+        st->om_invariant = oi / (double)K;
+        st->first_pass = 0;
+      }
+      sp.om_i = st->om_invariant;
+      sp.om_d = dd / (double)K;
+      sp.om_od = od / (double)K;
+      sp.om_tot = sp.om_i + sp.om_d + sp.om_od;
+      sp.om_nu = 0.0;
+    }
     if (slot == 2) st->wann = sp;
     else st->slot[slot] = sp;
     if (!isfinite(sp.om_tot)) {
@@ -307,7 +347,7 @@ __global__ void __launch_bounds__(256) k_omega_p3(const Problem* __restrict__ pr
 }
 
 // ----------------------------------------------------------------------------
-// k_grad: wann_domega (src/wannierise.F90:2287-2569), non-SLWF branch, fused with the
+// k_grad: wann_domega (src/wannierise.F90:2287-2569), both branches, fused with the
 // per-k partial dot products of internal_search_direction (:1424-1431).
 // grid: one CTA per (problem, k, tile_i, tile_j) of 32x32 tiles; 256 threads.
 // rave is the one computed by the preceding spread pass on the same M (the reference
@@ -322,11 +362,33 @@ __device__ __forceinline__ double diag_ln_of(const Problem& P, size_t kbn, doubl
   return P.guiding ? guided_ln(P, kbn, d) : P.diag_ln[kbn];
 }
 
+// q of the factored gradient for index j (row or column) of block (k,b): the plain form
+// wb (ln_j + b.r_j) for both variants; with selective localisation (src/wannierise.F90:
+// 2431-2509, factored) qx for a partner inside the objective block and qy for one outside
+//   qx = wb ln_j + (b.r_j)(1 - wb lambda) + wb lambda (b.c_j)
+//   qy = wb ln_j + wb (b.r_j)(1 - lambda) + wb lambda (b.c_j)
+// and false for a non-objective j, whose coefficients are zero.
+__device__ __forceinline__ bool grad_q(const Problem& P, double w, double l, double brn, const double* bv, int j,
+                                       double& qx, double& qy) {
+  if (P.slwf_num == 0) {
+    qx = qy = w * (l + brn);
+    return true;
+  }
+  if (j >= P.slwf_num) return false;
+  const double lam = P.slwf_lambda;
+  const int W = P.W;
+  const double r0 = bv[0] * P.slwf_c[j] + bv[1] * P.slwf_c[W + j] + bv[2] * P.slwf_c[2 * W + j];
+  qx = w * l + brn * (1.0 - w * lam) + w * lam * r0;
+  qy = w * l + w * brn * (1.0 - lam) + w * lam * r0;
+  return true;
+}
+
 __global__ void __launch_bounds__(256) k_grad(const Problem* __restrict__ probs, WorkMap wm) {
   __shared__ double2 sA[kTile * (kTile + 1)];   // A[j*(33)+i] = M(r0+i, c0+j)
   __shared__ double2 sT[kTile * (kTile + 1)];   // T[i*(33)+j] = M(c0+j, r0+i)
-  // per-column / per-row coefficients of the factored gradient (see below)
-  __shared__ double2 s_alpha[kTile], s_beta[kTile];
+  // per-column / per-row coefficients of the factored gradient (see below); variant 0 for
+  // a partner index inside the objective block, 1 outside (equal without SLWF)
+  __shared__ double2 s_alpha[2][kTile], s_beta[2][kTile];
   __shared__ double red[256];
   int local;
   const int p = locate(wm, blockIdx.x, local);
@@ -342,6 +404,7 @@ __global__ void __launch_bounds__(256) k_grad(const Problem* __restrict__ probs,
   const double* rave = P.centres + (size_t)2 * 4 * W;  // accepted slot
   const double2* Mk = P.M[st->cur] + (size_t)k * B * W * W;
   const int t = threadIdx.x;
+  const int S = P.slwf_num > 0 ? P.slwf_num : W;   // objective WFs 0..S-1
 
   double2 acc[4];
 #pragma unroll
@@ -362,16 +425,22 @@ __global__ void __launch_bounds__(256) k_grad(const Problem* __restrict__ probs,
     // G_mn += wb/2 (M_mn conj(M_nn) - conj(M_nm) M_mm) + (i/2)(M_mn q_n / M_nn + conj(M_nm) q_m / conj(M_mm))
     //       = M_mn alpha_n + conj(M_nm) beta_m,
     // alpha_n =  wb/2 conj(M_nn) + (i/2) q_n / M_nn,   beta_m = -wb/2 M_mm + (i/2) q_m / conj(M_mm)
-    // with q = wb (Im ln M_nn + b.rave_n)  (src/wannierise.F90:2366-2375, :2409-2417, :2499-2527)
+    // with q = wb (Im ln M_nn + b.rave_n)  (src/wannierise.F90:2366-2375, :2409-2417, :2499-2527);
+    // selective localisation: q from grad_q, zero coefficients for non-objective indices
     if (t < kTile) {
       if (t < nr) {
         const int m = r0 + t;
         const double2 d = Mb[(size_t)m * W + m];
         const double inv = 1.0 / (d.x * d.x + d.y * d.y);
         const double brn = bv[0] * rave[m] + bv[1] * rave[W + m] + bv[2] * rave[2 * W + m];
-        const double q = w * (diag_ln_of(P, ((size_t)k * B + b) * W + m, d) + brn);
-        // conj(1/M_mm) = d * inv ;  (i/2) q conj(1/M_mm) = (i/2) q inv (d.x + i d.y)
-        s_beta[t] = cmk(-0.5 * w * d.x - 0.5 * q * inv * d.y, -0.5 * w * d.y + 0.5 * q * inv * d.x);
+        double qv[2];
+        if (grad_q(P, w, diag_ln_of(P, ((size_t)k * B + b) * W + m, d), brn, bv, m, qv[0], qv[1])) {
+          // conj(1/M_mm) = d * inv ;  (i/2) q conj(1/M_mm) = (i/2) q inv (d.x + i d.y)
+          for (int v = 0; v < 2; ++v)
+            s_beta[v][t] = cmk(-0.5 * w * d.x - 0.5 * qv[v] * inv * d.y, -0.5 * w * d.y + 0.5 * qv[v] * inv * d.x);
+        } else {
+          s_beta[0][t] = s_beta[1][t] = cmk(0.0, 0.0);
+        }
       }
     } else if (t < 2 * kTile) {
       const int u = t - kTile;
@@ -380,9 +449,14 @@ __global__ void __launch_bounds__(256) k_grad(const Problem* __restrict__ probs,
         const double2 d = Mb[(size_t)n * W + n];
         const double inv = 1.0 / (d.x * d.x + d.y * d.y);
         const double brn = bv[0] * rave[n] + bv[1] * rave[W + n] + bv[2] * rave[2 * W + n];
-        const double q = w * (diag_ln_of(P, ((size_t)k * B + b) * W + n, d) + brn);
-        // 1/M_nn = (d.x - i d.y) inv ;  (i/2) q / M_nn = (q inv / 2)(d.y + i d.x)
-        s_alpha[u] = cmk(0.5 * w * d.x + 0.5 * q * inv * d.y, -0.5 * w * d.y + 0.5 * q * inv * d.x);
+        double qv[2];
+        if (grad_q(P, w, diag_ln_of(P, ((size_t)k * B + b) * W + n, d), brn, bv, n, qv[0], qv[1])) {
+          // 1/M_nn = (d.x - i d.y) inv ;  (i/2) q / M_nn = (q inv / 2)(d.y + i d.x)
+          for (int v = 0; v < 2; ++v)
+            s_alpha[v][u] = cmk(0.5 * w * d.x + 0.5 * qv[v] * inv * d.y, -0.5 * w * d.y + 0.5 * qv[v] * inv * d.x);
+        } else {
+          s_alpha[0][u] = s_alpha[1][u] = cmk(0.0, 0.0);
+        }
       }
     }
     __syncthreads();
@@ -393,8 +467,9 @@ __global__ void __launch_bounds__(256) k_grad(const Problem* __restrict__ probs,
       if (i < nr && j < nc) {
         const double2 mmn = sA[j * (kTile + 1) + i];    // M_mn
         const double2 mnm = sT[i * (kTile + 1) + j];    // M_nm
-        cfma(acc[qq], mmn, s_alpha[j]);
-        cfmac(acc[qq], mnm, s_beta[i]);
+        // variant by the partner index: row m for alpha_n, column n for beta_m
+        cfma(acc[qq], mmn, s_alpha[r0 + i < S ? 0 : 1][j]);
+        cfmac(acc[qq], mnm, s_beta[c0 + j < S ? 0 : 1][i]);
       }
     }
   }
@@ -1080,6 +1155,7 @@ __global__ void k_ctrl_end(const Problem* __restrict__ probs) {
   unsigned long long tns;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(tns));
   lg[8] = (double)tns;
+  lg[9] = st->wann.om_nu;
   if (c.conv_window > 1) {
     const double delta = st->wann.om_tot - st->old.om_tot;
     const int cw = c.conv_window;
@@ -1127,6 +1203,7 @@ __global__ void k_log_init(const Problem* __restrict__ probs) {
     unsigned long long tns;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(tns));
     lg[8] = (double)tns;
+    lg[9] = st->wann.om_nu;
   }
 }
 

@@ -63,8 +63,11 @@ __device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
 // ----------------------------------------------------------------------------
 constexpr int kMaxConvWindow = 64;
 
+// With selective localisation om_i is not computed (0), om_od holds
+// Omega_IOD + Omega_nu (the sum the reference prints as O_IOD) and om_nu the centre
+// constraint's Omega_nu (0 otherwise).
 struct Spread {
-  double om_i, om_d, om_od, om_tot;
+  double om_i, om_d, om_od, om_tot, om_nu;
 };
 
 struct CtrlState {
@@ -101,7 +104,7 @@ struct Control {
 };
 
 // per-iteration record (the <-- CONV / <-- SPRD lines, src/wannierise.F90:704-756)
-constexpr int kLogStride = 10;  // iter, delta, rms_grad, om_tot, om_d, om_od, lquad, alphamin, t_ns, pad
+constexpr int kLogStride = 10;  // iter, delta, rms_grad, om_tot, om_d, om_od, lquad, alphamin, t_ns, om_nu
 
 struct Problem {
   int W, K, B, nthr_pad;
@@ -153,6 +156,13 @@ struct Problem {
   double* rguide;         // [3][W] guiding centres (Cartesian, Angstrom)
   double* sheet;          // [k][b][n] branch offsets b . rguide_n
   double2* csheet;        // [k][b][n] exp(i sheet)
+  // selective localisation (src/wannierise.F90:2144-2211, :2431-2509): slwf_num > 0 makes
+  // WFs 0..slwf_num-1 the objective ones; slwf_lambda is lambda_loc (0 unless the centres
+  // are constrained); slwf_c [3][W] the constrained centres (Cartesian, Angstrom), zero
+  // when unconstrained; slwf_nu0 = lambda * sum_{n < slwf_num} |c_n|^2
+  int slwf_num, pad4;
+  double slwf_lambda, slwf_nu0;
+  const double* slwf_c;
 };
 
 // Work map: blockIdx.x -> (problem, local index) over a prefix sum.

@@ -332,7 +332,9 @@ def w90_get_omega(common: LibCommon) -> np.ndarray:
 
 def w90_get_log(common: LibCommon, max_rows: int) -> np.ndarray:
     """Per-iteration record: columns iter, dOmega, rms_grad, Omega, Omega_D, Omega_OD,
-    lquad, alphamin, device time (ns), 0."""
+    lquad, alphamin, device time (ns), Omega_nu.  With selective localisation Omega_OD
+    holds Omega_IOD + Omega_nu (the reference's printed O_IOD) and Omega_nu the centre
+    constraint's term; Omega_nu is 0 otherwise."""
     out = np.zeros((max_rows, 10), dtype=np.float64)
     n = common._L.w90g_get_log(common._h, out.ctypes.data_as(C.POINTER(C.c_double)), max_rows)
     return out[:n]

@@ -98,10 +98,10 @@ def win_system(path):
     opts = {}
     ints = ("num_wann", "num_bands", "num_iter", "num_cg_steps", "conv_window", "search_shells",
             "iprint", "num_print_cycles", "conv_noise_num", "dis_num_iter", "dis_conv_window",
-            "dis_spheres_num")
+            "dis_spheres_num", "slwf_num")
     reals = ("conv_tol", "trial_step", "fixed_step", "conv_noise_amp", "kmesh_tol", "dis_win_min",
-             "dis_win_max", "dis_froz_min", "dis_froz_max", "dis_mix_ratio", "dis_conv_tol")
-    bools = ("precond", "guiding_centres", "gamma_only")
+             "dis_win_max", "dis_froz_min", "dis_froz_max", "dis_mix_ratio", "dis_conv_tol", "slwf_lambda")
+    bools = ("precond", "guiding_centres", "gamma_only", "slwf_constrain")
     for k in ints:
         if k in kw:
             opts[k] = int(kw[k].split()[0])
@@ -121,7 +121,28 @@ def win_system(path):
     if opts.get("guiding_centres") and "projections" in blocks:
         spin = _flag(kw.get("spinors", "f"))
         opts["guiding_centres_frac"] = projection_sites(blocks, lattice, spin)
+    if opts.get("slwf_constrain") and ("projections" in blocks or "slwf_centres" in blocks):
+        opts["slwf_centres_frac"] = slwf_centres(blocks, lattice, int(opts.get("num_wann", 0)),
+                                                 _flag(kw.get("spinors", "f")))
     return lattice, kpts, opts
+
+
+def slwf_centres(blocks, lattice, num_wann, spinors=False):
+    """Constrained centres (num_wann x 3, fractional) as w90_readwrite_get_centre_constraints
+    forms them (src/readwrite.F90:3266-3357): the projection sites, then each
+    <slwf_centres> row 'index x y z [lambda]' replacing its WF's centre (a per-centre
+    lambda is read and ignored, as there)."""
+    cen = np.zeros((num_wann, 3))
+    if "projections" in blocks:
+        sites = projection_sites(blocks, lattice, spinors)
+        n = min(num_wann, len(sites))
+        cen[:n] = sites[:n]
+    for row in blocks.get("slwf_centres", []):
+        p = row.split()
+        if len(p) > 5:
+            raise ValueError("Didn't expect anything else after Lagrange multiplier")
+        cen[int(p[0]) - 1] = [_fnum(x) for x in p[1:4]]
+    return cen
 
 
 _NORB = {"s": 1, "p": 3, "d": 5, "f": 7, "sp": 2, "sp2": 3, "sp3": 4, "sp3d": 5, "sp3d2": 6,
