@@ -108,10 +108,13 @@ def conv_sensitivity(M0, U0, km, ctl, noise=1e-14, runs=2, slwf=None, grad=False
     return (sens, gsens) if grad else sens
 
 
-def conv_tolerance(sens, it, spread, floor=2e-10, factor=10.0):
+def conv_tolerance(sens, it, spread, floor=2e-10, factor=10.0, span=0):
     """2e-10 A^2 where the trajectory is insensitive at that level, else `factor` times the
-    measured sensitivity (at least the metric's 1e-8 relative)."""
-    s = sens.get(int(it), 0.0)
+    measured sensitivity (at least the metric's 1e-8 relative).  span > 0 takes the
+    sensitivity as the largest over iterations it-span..it+span: a few perturbed runs
+    sample it, and a sample can dip at one iteration of a segment that is sensitive."""
+    it = int(it)
+    s = max(sens.get(j, 0.0) for j in range(it - span, it + span + 1))
     return floor if s < 0.1 * floor else max(factor * s, 1e-8 * abs(spread))
 
 
