@@ -13,8 +13,10 @@ are called through ``scipy.linalg.lapack`` (same LAPACK routines the reference
 links; bundled OpenBLAS build).
 
 Parity pin: ``tests/test_oracle_golden.py`` runs this oracle on the reference's
-own regression inputs (Pb, GaAs, diamond, basic1; fixtures under
-``tests/golden/``) and compares every printed ``<-- CONV`` spread (10 decimals),
+own regression inputs (Pb, GaAs, diamond, basic1, the preconditioned GaAs runs,
+selective localisation (example26), site symmetry (example21), four
+disentanglement cases and a guiding-centre checkpoint; fixtures under
+``tests/golden/``) and compares every printed ``<-- CONV`` / ``<-- DIS`` line,
 the final centres/spreads and the b-vector tables with the reference's
 benchmark outputs.
 
@@ -271,8 +273,9 @@ def kmesh_get(real_lattice, kpt_latt, search_shells=36, tol=1.0e-6):
 # ---------------------------------------------------------------------------
 # overlap_project (Loewdin)  (src/overlap.F90:758-952)
 # ---------------------------------------------------------------------------
-def overlap_project(M, A, nnlist):
-    """U(k) = Z V^dagger from zgesvd of A(k); M(k,b) <- U(k)^dag M(k,b) U(k+b)."""
+def overlap_project(M, A, nnlist, sitesym=None):
+    """U(k) = Z V^dagger from zgesvd of A(k); M(k,b) <- U(k)^dag M(k,b) U(k+b).
+    ``sitesym``: U is made symmetry-adapted first (src/overlap.F90:901-905)."""
     K, B, W, _ = M.shape
     U = np.empty((K, W, W), dtype=np.complex128)
     for k in range(K):
@@ -283,8 +286,160 @@ def overlap_project(M, A, nnlist):
         chk = U[k].conj().T @ U[k]
         if np.max(np.abs(chk - np.eye(W))) > EPS5:
             raise RuntimeError("unitarity of initial U")
+    if sitesym is not None:
+        U = sitesym_symmetrize_u_matrix(U, sitesym)
     Mout = np.conj(U)[:, None].transpose(0, 1, 3, 2) @ M @ U[nnlist]
     return U, Mout
+
+
+# ---------------------------------------------------------------------------
+# symmetry-adapted mode (site_symmetry = T): src/sitesym.F90
+# ---------------------------------------------------------------------------
+@dataclass
+class Sitesym:
+    """sitesym_type (src/wannier90_types.F90:260-268) with 0-based indices:
+    ik2ir[k] (irreducible index of k), ir2ik[ir], kptsym[isym, ir] (index of R_isym k_ir),
+    d_wann[ir, isym] = D(R, k_ir) (W x W), d_band[ir, isym] = d(R, k_ir) (nb x nb),
+    eps = symmetrize_eps (default 1e-3)."""
+    ik2ir: np.ndarray
+    ir2ik: np.ndarray
+    kptsym: np.ndarray
+    d_wann: np.ndarray
+    d_band: np.ndarray
+    eps: float = 1.0e-3
+
+    @property
+    def nsym(self):
+        return self.kptsym.shape[0]
+
+    @property
+    def nkirr(self):
+        return len(self.ir2ik)
+
+    def irreducible(self, k):
+        return self.ir2ik[self.ik2ir[k]] == k
+
+
+def _orthogonalize_u(u, n):
+    """orthogonalize_u (src/sitesym.F90:500-548): the polar factor of u[:n] through
+    zgesvd('A','A'): u = L[:, :m] R."""
+    m = u.shape[1]
+    L, sv, R, info = lapack.zgesvd(np.ascontiguousarray(u[:n, :]), full_matrices=1, compute_uv=1)[:4]
+    if info != 0:
+        raise RuntimeError("ERROR: IN ZGESVD IN orthogonalize_u")
+    out = np.zeros_like(u)
+    out[:n, :] = L[:, :m] @ R
+    return out
+
+
+def _symmetrize_ukirr(u, ir, sym, n=None):
+    """symmetrize_ukirr (src/sitesym.F90:392-497): average d^+(R,k) u D(R,k) over the
+    little group {R: Rk = k} and orthonormalise, until sum |ngk I - sum u^+ d^+ u D| <
+    symmetrize_eps (100 passes at most)."""
+    W = u.shape[1]
+    ntmp = u.shape[0] if n is None else n
+    ik = sym.ir2ik[ir]
+    little = [isym for isym in range(sym.nsym) if sym.kptsym[isym, ir] == ik]
+    ngk = len(little)
+    if ngk == 1:
+        return _orthogonalize_u(u, ntmp)
+    for it in range(1, 101):
+        usum = np.zeros_like(u)
+        cmat2 = ngk * np.eye(W, dtype=np.complex128)
+        for isym in little:
+            sub = u[:ntmp] @ sym.d_wann[ir, isym]
+            cmat = np.zeros_like(u)
+            cmat[:ntmp] = sym.d_band[ir, isym][:ntmp, :ntmp].conj().T @ sub
+            usum += cmat
+            cmat2 -= u[:ntmp].conj().T @ cmat[:ntmp]
+        diff = float(np.abs(cmat2).sum())
+        if diff < sym.eps:
+            break
+        if it == 100:
+            raise RuntimeError("symmetrize_ukirr: not converged (diff %.10e, eps %.10e)" % (diff, sym.eps))
+        u = _orthogonalize_u(usum / ngk, ntmp)
+    return u
+
+
+def sitesym_symmetrize_u_matrix(U, sym):
+    """sitesym_symmetrize_u_matrix (src/sitesym.F90:104-192), the wannierisation form
+    (ndim = num_wann): U(k_ir) symmetrised, then U(R k_ir) = d(R,k) U(k) D^+(R,k) for
+    each star member not yet set."""
+    U = U.copy()
+    done = np.zeros(len(U), dtype=bool)
+    for ir in range(sym.nkirr):
+        ik = sym.ir2ik[ir]
+        done[ik] = True
+        U[ik] = _symmetrize_ukirr(U[ik], ir, sym)
+        for isym in range(1, sym.nsym):
+            irk = sym.kptsym[isym, ir]
+            if done[irk]:
+                continue
+            done[irk] = True
+            U[irk] = sym.d_band[ir, isym] @ U[ik] @ sym.d_wann[ir, isym].conj().T
+    if not done.all():
+        raise RuntimeError("error in sitesym_symmetrize_u_matrix")
+    return U
+
+
+def sitesym_symmetrize_gradient(G, sym, mode):
+    """sitesym_symmetrize_gradient (src/sitesym.F90:195-278).  mode 1: the star's
+    gradients gathered onto k_ir, G(k_ir) += D^+(R,k) G(Rk) D(R,k) for each star member,
+    and zero at the reducible k; mode 2: G(k_ir) averaged over its little group."""
+    G = G.copy()
+    if mode == 1:
+        found = np.zeros(len(G), dtype=bool)
+        for ir in range(sym.nkirr):
+            ik = sym.ir2ik[ir]
+            tot = G[ik].copy()
+            found[ik] = True
+            for isym in range(1, sym.nsym):
+                irk = sym.kptsym[isym, ir]
+                if found[irk]:
+                    continue
+                found[irk] = True
+                D = sym.d_wann[ir, isym]
+                tot = tot + (D.conj().T @ G[irk]) @ D
+            G[ik] = tot
+        for k in range(len(G)):
+            if not sym.irreducible(k):
+                G[k] = 0.0
+    elif mode == 2:
+        for ir in range(sym.nkirr):
+            ik = sym.ir2ik[ir]
+            ngk = int(np.count_nonzero(sym.kptsym[:, ir] == ik))
+            if ngk == 1:
+                continue
+            tot = G[ik].copy()
+            for isym in range(1, sym.nsym):
+                if sym.kptsym[isym, ir] != ik:
+                    continue
+                D = sym.d_wann[ir, isym]
+                tot = tot + D.conj().T @ (G[ik] @ D)
+            G[ik] = tot / ngk
+    else:
+        raise ValueError("unknown mode argument in sitesym_symmetrize_gradient")
+    return G
+
+
+def sitesym_symmetrize_rotation(dU, sym):
+    """sitesym_symmetrize_rotation (src/sitesym.F90:281-328): dU(R k_ir) =
+    D(R,k) dU(k_ir) D^+(R,k) for each star member not yet set."""
+    dU = dU.copy()
+    done = np.zeros(len(dU), dtype=bool)
+    for ir in range(sym.nkirr):
+        ik = sym.ir2ik[ir]
+        done[ik] = True
+        for isym in range(1, sym.nsym):
+            irk = sym.kptsym[isym, ir]
+            if irk == ik or done[irk]:
+                continue
+            done[irk] = True
+            D = sym.d_wann[ir, isym]
+            dU[irk] = D @ (dU[ik] @ D.conj().T)
+    if not done.all():
+        raise RuntimeError("error in sitesym_symmetrize_rotation")
+    return dU
 
 
 # ---------------------------------------------------------------------------
@@ -874,25 +1029,35 @@ class WannResult:
     niter: int = 0
 
 
-def new_u_and_m(cdq, U, M, nnlist):
-    """internal_new_u_and_m (src/wannierise.F90:1599-1751): zheev of i*cdq, dU=V e^{-i l} V^dag."""
+def new_u_and_m(cdq, U, M, nnlist, sitesym=None):
+    """internal_new_u_and_m (src/wannierise.F90:1599-1751): zheev of i*cdq, dU=V e^{-i l} V^dag.
+    ``sitesym``: dU at the irreducible k only, the rest by sitesym_symmetrize_rotation
+    (:1656-1659, :1719-1726)."""
     K, W, _ = cdq.shape
-    dU = np.empty_like(cdq)
+    dU = cdq.copy()
     for k in range(K):
+        if sitesym is not None and not sitesym.irreducible(k):
+            continue
         w, v, info = lapack.zheev(1j * cdq[k], compute_v=1, lower=0)
         if info != 0:
             raise RuntimeError("zheev failed in internal_new_u_and_m")
         dU[k] = (v * np.exp(-1j * w)[None, :]) @ v.conj().T
+    if sitesym is not None:
+        dU = sitesym_symmetrize_rotation(dU, sitesym)
     Unew = U @ dU                                                     # :1728-1733
     Mnew = np.conj(np.swapaxes(dU, 1, 2))[:, None] @ M @ dU[nnlist]  # :1736-1748
     return Unew, Mnew
 
 
-def wann_main(M, U, km, ctl: WannControl, record=True, precond=None, rguide=None, slwf=None):
-    """Restatement of wann_main (no site symmetry).
+def wann_main(M, U, km, ctl: WannControl, record=True, precond=None, rguide=None, slwf=None, sitesym=None):
+    """Restatement of wann_main.
     ``precond``: the tables of :func:`precond_setup` when ``ctl.precond``;
     ``rguide``: guiding centres [3,W] (Cartesian, Angstrom) when ``ctl.guiding_centres``;
-    ``slwf``: :class:`Slwf` for selective localisation (slwf_num < num_wann)."""
+    ``slwf``: :class:`Slwf` for selective localisation (slwf_num < num_wann);
+    ``sitesym``: :class:`Sitesym` for the symmetry-adapted mode (site_symmetry = T).
+    The mode-2 symmetrisation the reference applies to its global cdq array after the
+    search direction (:589-591) acts on the previous step's rotation, which
+    internal_new_u_and_m overwrites before reading it: it does not enter the run."""
     if ctl.precond and precond is None:
         raise ValueError("precond=T needs the precond_setup tables")
     if ctl.guiding_centres and rguide is None:
@@ -935,6 +1100,9 @@ def wann_main(M, U, km, ctl: WannControl, record=True, precond=None, rguide=None
             rguide, sheet = wann_phases(M, km, rguide, irguide)
             irguide = 1
         cdodq = wann_domega(M, km, sheet=sheet, slwf=slwf)            # :566-571
+        if sitesym is not None:                                       # :2543-2551
+            cdodq = sitesym_symmetrize_gradient(cdodq, sitesym, 1)
+            cdodq = sitesym_symmetrize_gradient(cdodq, sitesym, 2)
         if ctl.precond:                                               # :577-581
             cdodq_p = precond_search_direction(cdodq, wann_spread.om_tot, precond)
         else:
@@ -981,7 +1149,7 @@ def wann_main(M, U, km, ctl: WannControl, record=True, precond=None, rguide=None
         else:
             cdq_t = cdqkeep * (ctl.trial_step / (4.0 * wbtot))        # :605
             U0, M0 = U, M
-            U, M = new_u_and_m(cdq_t, U0, M0, nnlist)
+            U, M = new_u_and_m(cdq_t, U0, M0, nnlist, sitesym)
             trial_spread, rave, r2ave, rave2 = wann_omega(M, km, om_invariant, sheet=sheet, slwf=slwf)
             # internal_optimal_step (:1528-1596)
             fac = trial_spread.om_tot - wann_spread.om_tot
@@ -1007,7 +1175,7 @@ def wann_main(M, U, km, ctl: WannControl, record=True, precond=None, rguide=None
             cdq_a = cdqkeep * (alphamin / (4.0 * wbtot))              # :665
             if not ctl.lfixstep:
                 U, M = U0, M0
-            U, M = new_u_and_m(cdq_a, U, M, nnlist)
+            U, M = new_u_and_m(cdq_a, U, M, nnlist, sitesym)
             old_spread = wann_spread.copy()
             wann_spread, rave, r2ave, rave2 = wann_omega(M, km, om_invariant, sheet=sheet, slwf=slwf)
         else:

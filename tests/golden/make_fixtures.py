@@ -24,6 +24,9 @@ printed '<-- DIS' line.
 The selective-localisation case (testw90_example26: GaAs, slwf_num = 1 with a constrained
 centre) also stores the constrained centres and every '<-- SPRD' line (Omega_IOD, Omega_D).
 
+The site-symmetry case (testw90_example21_As_sp: GaAs sp3, site_symmetry = T) also stores
+the symmetry data of its .dmn file (k-point stars and the D matrices).
+
 The guiding-centre case (testpostw90_gaas_shc: spinor GaAs, 16 isolated bands,
 guiding_centres = T) has no printed wannierise trajectory; its expected values are the
 final centres and spreads of the checkpoint shipped with that test.
@@ -371,6 +374,59 @@ def build_slwf(ref_root, out_dir):
     print("slwf26", nb, nk, nntot, conv.shape, len(sprd), fin)
 
 
+def parse_dmn(path, nw):
+    """A .dmn file as sitesym_read reads it (src/sitesym.F90:698-765): list-directed
+    integers ik2ir(nk), ir2ik(nkirr), kptsym(nsym, nkirr), then the complex
+    d_matrix_wann(nw, nw, nsym, nkirr) and d_matrix_band(nb, nb, nsym, nkirr), all
+    Fortran order.  Returned 1-based as in the file; the matrices as [ir, isym, i, j]."""
+    lines = open(path).read().splitlines()
+    nb, nsym, nkirr, nk = (int(x) for x in lines[1].split())
+    ints, cplx = [], []
+    for l in lines[2:]:
+        l = l.strip()
+        if not l:
+            continue
+        if l.startswith("("):
+            re_, im_ = l.strip("()").split(",")
+            cplx.append(float(re_) + 1j * float(im_))
+        else:
+            ints += [int(x) for x in l.split()]
+    ik2ir = np.array(ints[:nk])
+    ir2ik = np.array(ints[nk:nk + nkirr])
+    kptsym = np.array(ints[nk + nkirr:nk + nkirr + nsym * nkirr]).reshape(nkirr, nsym).T
+    cw = np.array(cplx[:nw * nw * nsym * nkirr]).reshape(nkirr, nsym, nw, nw).transpose(0, 1, 3, 2)
+    cb = np.array(cplx[nw * nw * nsym * nkirr:]).reshape(nkirr, nsym, nb, nb).transpose(0, 1, 3, 2)
+    return nb, nsym, nkirr, nk, ik2ir, ir2ik, kptsym, cw, cb
+
+
+def build_sitesym(ref_root, out_dir):
+    """testw90_example21_As_sp: GaAs, 4 isolated bands (sp3 on As), 4x4x4 k, symmetry-
+    adapted mode (site_symmetry = T, symmetrize_eps = 1e-9) with the test's .dmn."""
+    d = os.path.join(ref_root, "test-suite/tests/testw90_example21_As_sp")
+    kw, real_lattice, kpts = parse_win(os.path.join(d, "GaAs.win"))
+    W = int(kw["num_wann"])
+    nb, nk, nntot, heads, blocks = parse_mmn(os.path.join(d, "GaAs.mmn"))
+    A = parse_amn(os.path.join(d, "GaAs.amn"))
+    dnb, nsym, nkirr, dnk, ik2ir, ir2ik, kptsym, dw, db = parse_dmn(os.path.join(d, "GaAs.dmn"), W)
+    assert dnb == nb and dnk == nk
+    bench = os.path.join(d, "benchmark.out.default.inp=GaAs.win")
+    conv, initial, final, om, bvec = parse_benchmark(bench)
+    num = lambda k, default: float(kw.get(k, str(default)).replace("d", "e").replace("D", "e"))
+    knobs = dict(num_wann=W, num_iter=int(kw.get("num_iter", 100)), num_cg_steps=int(kw.get("num_cg_steps", 5)),
+                 conv_tol=num("conv_tol", 1e-10), conv_window=int(kw.get("conv_window", -1)),
+                 trial_step=num("trial_step", 2.0), search_shells=int(kw.get("search_shells", 36)),
+                 symmetrize_eps=num("symmetrize_eps", 1e-3))
+    np.savez_compressed(
+        os.path.join(out_dir, "sitesym21.npz"),
+        real_lattice=real_lattice, kpt_latt=kpts, mp_grid=np.array([int(x) for x in kw["mp_grid"].split()[:3]]),
+        num_bands=nb, num_kpts=nk, nntot=nntot, mmn_heads=heads, mmn_blocks=blocks, amn=A,
+        knobs=np.array([knobs[k] for k in sorted(knobs)], dtype=np.float64), knob_names=np.array(sorted(knobs)),
+        ik2ir=ik2ir, ir2ik=ir2ik, kptsym=kptsym, d_matrix_wann=dw, d_matrix_band=db,
+        conv=conv, centres_initial=initial, centres_final=final,
+        omega_final=np.array([om["om_i"], om["om_d"], om["om_od"], om["om_tot"]]), bvec_table=bvec)
+    print("sitesym21", nb, nk, nntot, nsym, nkirr, conv.shape, om)
+
+
 def build(ref_root, out_dir):
     for name, (sub, seed) in CASES.items():
         d = os.path.join(ref_root, sub)
@@ -407,3 +463,4 @@ if __name__ == "__main__":
     build_guiding(root, os.path.dirname(os.path.abspath(__file__)))
     build_dis(root, os.path.dirname(os.path.abspath(__file__)))
     build_slwf(root, os.path.dirname(os.path.abspath(__file__)))
+    build_sitesym(root, os.path.dirname(os.path.abspath(__file__)))

@@ -71,6 +71,13 @@ def slwf(d):
     return ctl, O.Slwf(int(kn["slwf_num"]), float(kn["slwf_lambda"]), cen)
 
 
+def sitesym(d):
+    """Sitesym (0-based) of the site-symmetry case, from its .dmn data."""
+    from oracle import w90_oracle as O
+    return O.Sitesym(d["ik2ir"] - 1, d["ir2ik"] - 1, d["kptsym"] - 1, d["d_matrix_wann"], d["d_matrix_band"],
+                     float(d["knobs"]["symmetrize_eps"]))
+
+
 DIS_CASES = ["silicon_dis", "copper_dis", "basic2_dis", "gaas192_dis"]
 
 

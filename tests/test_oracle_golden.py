@@ -135,3 +135,36 @@ def test_oracle_selective_localisation_reproduces_reference():
     rnr0n2 = ((r.centres[:, :sl.num] - sl.centres[:, :sl.num]) ** 2).sum()     # :829-836
     assert abs(rnr0n2 - penalty) < 1.01e-9
     assert abs(sp.om_tot - total_c) < 1.01e-9
+
+
+def test_oracle_site_symmetry_reproduces_reference():
+    """testw90_example21_As_sp (GaAs sp3, 4 WFs, 64 k of which 10 irreducible, 24
+    symmetries, site_symmetry = T, symmetrize_eps = 1e-9): the symmetry-adapted initial
+    U, the symmetrised gradient (sitesym_symmetrize_gradient modes 1 and 2) and the
+    rotations of the reducible k from the irreducible ones.  Every printed spread within
+    2e-10 A^2, the final centres/spreads and Omega terms to the printed decimals; the
+    run differs from the plain one from its initial state on."""
+    d = G.load("sitesym21")
+    kn = d["knobs"]
+    km = O.kmesh_get(d["real_lattice"], d["kpt_latt"], int(kn["search_shells"]))
+    tab = d["bvec_table"]
+    np.testing.assert_allclose(km["bk"][0], tab[:, :3], atol=1e-6)
+    M = G.assemble_m(d, km["nnlist"], km["nncell"])
+    sym = G.sitesym(d)
+    U0, M0 = O.overlap_project(M, d["amn"], km["nnlist"], sitesym=sym)
+    r = O.wann_main(M0, U0, km, G.control(d), sitesym=sym)
+    recs = [r.initial] + r.iters
+    assert len(recs) == len(d["conv"])
+    for got, (it, delta, rms, spread) in zip(recs, d["conv"]):
+        assert got.iter == int(it)
+        assert abs(got.spread.om_tot - spread) < 2e-10, (it, got.spread.om_tot, spread)
+        assert abs(got.rms_grad - rms) < 1e-6 + 1e-3 * rms
+    fin = d["centres_final"]
+    np.testing.assert_allclose(r.centres.T, fin[:, :3], rtol=0, atol=1.01e-6)
+    np.testing.assert_allclose(r.spreads, fin[:, 3], rtol=0, atol=1.01e-8)
+    sp = r.spread
+    np.testing.assert_allclose([sp.om_i, sp.om_d, sp.om_od, sp.om_tot], d["omega_final"], rtol=0, atol=1.01e-9)
+    # the symmetry-adapted mode is what reproduces the printed run
+    U0p, M0p = O.overlap_project(M, d["amn"], km["nnlist"])
+    plain = O.wann_main(M0p, U0p, km, O.WannControl(**{**G.control(d).__dict__, "num_iter": 3}))
+    assert abs(plain.iters[2].spread.om_tot - d["conv"][3][3]) > 1e-6
