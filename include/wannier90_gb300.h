@@ -52,12 +52,14 @@ void cset_option_floatxy(void* handle, const char* keyword, const double* values
 /* ---- process options, build the k-mesh: src/c_interface.F90:49-68 ----------------
  * Keywords read by the engine besides the system ones: num_iter, num_cg_steps, conv_tol,
  * conv_window, trial_step / fixed_step, precond (+ mp_grid), guiding_centres,
- * num_no_guide_iter, num_guide_cycles, slwf_num, slwf_constrain, slwf_lambda, dis_*,
+ * num_no_guide_iter, num_guide_cycles, slwf_num, slwf_constrain, slwf_lambda,
+ * site_symmetry, symmetrize_eps, dis_*,
  * search_shells, kmesh_tol, iprint.  Block data the C binding cannot pass as text comes
  * as floatxy tables: guiding_centres_frac (num_wann x 3, the projection sites) and
  * slwf_centres_frac (num_wann x 3, the constrained centres: the <slwf_centres> rows
  * over the projection sites; without it slwf_constrain uses guiding_centres_frac).
- * site_symmetry, gamma_only, conv_noise_amp > 0 and dis_spheres_num > 0 give ierr 5. */
+ * site_symmetry (+ symmetrize_eps) needs num_bands = num_wann and w90g_set_sitesym;
+ * gamma_only, conv_noise_amp > 0 and dis_spheres_num > 0 give ierr 5. */
 void cinput_setopt(void* handle, const char* seedname, int* ierr, int comm);
 
 /* ---- data pointers (caller keeps ownership): src/c_interface.F90:82-127 ----------- */
@@ -123,6 +125,17 @@ int w90g_get_dis_log(void* handle, double* rows, int max_rows);
  * (0-based) -- dis_manifold%ndimwin / nfirstwin, and lwindow(i,k) = nfirstwin <= i <
  * nfirstwin + ndimwin, as the checkpoint stores them. */
 void w90g_get_dis_windows(void* handle, int* ndimwin, int* nfirstwin);
+/* Symmetry data of the symmetry-adapted mode (site_symmetry = T; what sitesym_read reads
+ * from the .dmn file, src/sitesym.F90:698-765; the reference's C binding has no way to
+ * pass it): the file's counts nb, nsym, nkirr, nk; 1-based ik2ir[nk], ir2ik[nkirr],
+ * kptsym(nsym, nkirr); d_matrix_wann(nw, nw, nsym, nkirr) and d_matrix_band(nb, nb, nsym,
+ * nkirr), Fortran order, complex as (re, im) pairs.  After cinput_setopt.  Returns the
+ * ierr: 6 when the counts or indices disagree with the handle (the reference's
+ * "Number of bands / k-points is not correct" messages), 1 when the stars do not cover
+ * the mesh.  With site_symmetry = T, cproject_overlap makes the initial U symmetry-
+ * adapted and cwannierise symmetrises the gradient and rotations (isolated bands). */
+int w90g_set_sitesym(void* handle, int nb, int nsym, int nkirr, int nk, const int* ik2ir, const int* ir2ik,
+                     const int* kptsym, const double* d_wann, const double* d_band);
 /* (final Omega_I = omega%invariant, converged 0/1, iterations, most Jacobi sweeps of a
  *  Z eigenproblem) of the last cdisentangle */
 void w90g_get_dis_info(void* handle, double* info4);

@@ -130,3 +130,36 @@ def grad_tolerance(gsens, it, rms, factor=10.0):
     or `factor` times its measured sensitivity where that is larger (a converged SLWF run,
     whose non-objective gauge is free, moves it by up to 1e-4 under a 1e-14 perturbation)."""
     return max(1e-6 + 1e-3 * rms, factor * gsens.get(int(it), 0.0))
+
+
+def write_dmn(path, d):
+    """The fixture's symmetry data in the .dmn layout (10 integers a line, one complex
+    '(re, im)' a line, blank lines between the records)."""
+    ik2ir, ir2ik, kptsym = d["ik2ir"], d["ir2ik"], d["kptsym"]
+    dw = d["d_matrix_wann"].transpose(2, 3, 1, 0)      # [ir, isym, i, j] -> (i, j, isym, ir)
+    db = d["d_matrix_band"].transpose(2, 3, 1, 0)
+    nsym, nkirr = kptsym.shape
+    nb = db.shape[0]
+
+    def ints(v):
+        v = list(v)
+        return "\n".join("".join("%9d" % x for x in v[i:i + 10]) for i in range(0, len(v), 10)) + "\n \n"
+
+    with open(path, "w") as f:
+        f.write(" Created by the test\n")
+        f.write("%9d%9d%9d%9d\n \n" % (nb, nsym, nkirr, len(ik2ir)))
+        f.write(ints(ik2ir))
+        f.write(ints(ir2ik))
+        for ir in range(nkirr):
+            f.write(ints(kptsym[:, ir]))
+        for arr in (dw, db):
+            for z in arr.reshape(-1, order="F"):
+                f.write(" (%17.10E,%17.10E)\n" % (z.real, z.imag))
+
+
+def dmn_dict(d):
+    """The site-symmetry fixture as w90io.read_dmn returns a .dmn file (Fortran shapes)."""
+    return dict(num_bands=4, nsymmetry=24, nkptirr=10, num_kpts=64, ik2ir=d["ik2ir"].copy(),
+                ir2ik=d["ir2ik"].copy(), kptsym=d["kptsym"].copy(),
+                d_matrix_wann=d["d_matrix_wann"].transpose(2, 3, 1, 0).copy(),
+                d_matrix_band=d["d_matrix_band"].transpose(2, 3, 1, 0).copy())

@@ -5,7 +5,8 @@ Isolated bands (num_bands = num_wann): the projections are read into u_matrix
 (src/wannier_prog.F90:523-529) and the Loewdin projection runs.  Entangled bands
 (num_bands > num_wann): ``seedname.eig`` is read too, the projections go into u_opt
 and the disentanglement (dis_main + setup_m_loc) runs with the ``dis_*`` keywords of
-the .win.  Then wann_main runs on the GPU, the wannierise section of the .wout is printed
+the .win.  With site_symmetry = T, ``seedname.dmn`` supplies the symmetry data.  Then
+wann_main runs on the GPU, the wannierise section of the .wout is printed
 when iprint > 0, and ``seedname.chk`` is written (src/wannier_prog.F90:256-275), with
 Omega_I, lwindow, ndimwin and U_opt after a disentanglement.
 Options: ``--precision tensor|fp64`` (default tensor).
@@ -32,6 +33,9 @@ def run(seedname, precision="tensor"):
     opts["gpu_tensor"] = 1 if precision == "tensor" else 0
     c = w90.setup(kpoints=kpts, unit_cell_cart=lattice, num_wann=nw, num_bands=nb, mp_grid=mp, **opts)
     K = len(kpts)
+    if opts.get("site_symmetry"):
+        # sitesym_read after the input (src/wannier_prog.F90:174-177)
+        w90.check(c, w90.w90_set_sitesym(c, w90io.read_dmn(seedname + ".dmn", nw)), "sitesym_read")
     nnkp = w90.w90_get_nnkp(c, K) - 1
     gkpb = np.transpose(w90.w90_get_gkpb(c, K), (1, 2, 0))
     m = w90io.read_mmn(seedname + ".mmn", nnkp, gkpb)

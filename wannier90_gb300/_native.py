@@ -43,6 +43,8 @@ SIGNATURES = [
     ("w90g_get_dis_log", C.c_int, [C.c_void_p, _c_double_p, C.c_int]),
     ("w90g_get_dis_info", None, [C.c_void_p, _c_double_p]),
     ("w90g_get_dis_windows", None, [C.c_void_p, _c_int_p, _c_int_p]),
+    ("w90g_set_sitesym", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, _c_int_p, _c_int_p, _c_int_p,
+                                   _c_double_p, _c_double_p]),
     ("w90g_read_mmn", C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_int, _c_int_p, _c_int_p, C.c_void_p, C.c_int,
                                 C.c_char_p, C.c_int]),
     ("w90g_read_amn", C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_char_p, C.c_int]),

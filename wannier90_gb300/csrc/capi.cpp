@@ -72,6 +72,14 @@ struct Handle {
   int slwf_num = 0;
   double slwf_lambda = 0.0;
   std::vector<double> slwf_c;
+  // symmetry-adapted mode (site_symmetry = T): the .dmn data as sitesym_read holds it,
+  // set by w90g_set_sitesym, turned into the engine's tables (ProblemSpec::sym_*)
+  int site_symmetry = 0;
+  double symmetrize_eps = 1.0e-3;
+  bool have_sym = false;
+  int sym_nir = 0, sym_nk = 0, sym_nb = 0;
+  std::vector<int> sym_ik, sym_moff, sym_mem, sym_goff, sym_grp;
+  std::vector<double> sym_d, sym_db;
   // caller data
   double* m_local = nullptr;
   double* u_matrix = nullptr;
@@ -285,6 +293,17 @@ int build_spec(Handle* h, ProblemSpec& s) {
   s.slwf_num = h->slwf_num;
   s.slwf_lambda = h->slwf_lambda;
   s.slwf_c = h->slwf_c;
+  if (h->site_symmetry && h->have_sym && h->sym_nk == h->num_kpts && h->sym_nb == h->num_wann) {
+    s.sym_nir = h->sym_nir;
+    s.sym_eps = h->symmetrize_eps;
+    s.sym_ik = h->sym_ik;
+    s.sym_moff = h->sym_moff;
+    s.sym_mem = h->sym_mem;
+    s.sym_goff = h->sym_goff;
+    s.sym_grp = h->sym_grp;
+    s.sym_d = h->sym_d;
+    s.sym_db = h->sym_db;
+  }
   s.precond = h->precond;
   s.nrpts = h->nrpts;
   s.pc_kr = h->pc_kr;
@@ -304,8 +323,15 @@ Engine* engine(Handle* h) {
   return h->eng.get();
 }
 
+// site_symmetry = T without its data: the reference stops reading the .dmn file
+bool sym_missing(Handle* h) {
+  return h->site_symmetry && !(h->have_sym && h->sym_nk == h->num_kpts && h->sym_nb == h->num_wann);
+}
+const char* kSymMissing = "site_symmetry = T needs the symmetry data of the .dmn file (w90g_set_sitesym)";
+
 int do_project(Handle* h, double* m, double* u, cudaMemcpyKind in, cudaMemcpyKind out) {
   if (!h->setup_complete) return fail(h, 1, "cinput_setopt must be called before cproject_overlap");
+  if (sym_missing(h)) return fail(h, 6, kSymMissing);
   if (!m) return fail(h, 1, "m_matrix_local not set for projovlp call");
   if (!u) return fail(h, 1, "u_matrix not set for projovlp call");
   // w90_project_overlap projects only when no disentanglement ran (src/library_interface.F90:449-459)
@@ -346,6 +372,7 @@ int apply_result(Handle* h, const w90g::ProblemResult& r, bool print) {
 
 int do_wannierise(Handle* h, double* m, double* u, cudaMemcpyKind in, cudaMemcpyKind out) {
   if (!h->setup_complete) return fail(h, 1, "cinput_setopt must be called before cwannierise");
+  if (sym_missing(h)) return fail(h, 6, kSymMissing);
   if (!m) return fail(h, 1, "m_matrix_local not set for wannierise");
   if (!u) return fail(h, 1, "u_matrix not set for wannierise");
   const int ldm = mld(h);
@@ -713,7 +740,7 @@ void cinput_setopt(void* hv, const char* seedname, int* ierr, int comm) {
   // with gpu_tensor: gpu_tensor_exp = 1 (default) also runs exp(s D) and U dU on tensor cores
   h->gpu_tensor_exp = get_num(h, "gpu_tensor_exp", v) ? (int)v : 1;
   // options on wann_main's code path that the engine does not implement
-  const char* unsupported[] = {"site_symmetry", "gamma_only", "dis_spheres_num"};
+  const char* unsupported[] = {"gamma_only", "dis_spheres_num"};
   for (const char* k : unsupported) {
     if (get_num(h, k, v)) {
       const bool active = v != 0.0;
@@ -757,6 +784,14 @@ void cinput_setopt(void* hv, const char* seedname, int* ierr, int comm) {
         for (int i = 0; i < 3; ++i) x += git->second.v[(size_t)n * 3 + i] * h->real_lattice[i * 3 + j];
         h->rguide0[(size_t)j * W + n] = x;
       }
+  }
+  // symmetry-adapted mode (src/wannier90_readwrite.F90:387-412); the engine runs it for
+  // isolated bands (the disentanglement's symmetrised Z matrices are not built)
+  h->site_symmetry = get_num(h, "site_symmetry", v) ? (v != 0.0) : 0;
+  h->symmetrize_eps = get_num(h, "symmetrize_eps", v) ? v : 1.0e-3;
+  if (h->site_symmetry && h->num_bands != h->num_wann) {
+    *ierr = fail(h, 5, "Option 'site_symmetry' with num_bands > num_wann is not supported by the GPU engine");
+    return;
   }
   // selective localisation and constrained centres
   // (src/wannier90_readwrite.F90:757-802, :1660-1708; src/readwrite.F90:3266-3357)
@@ -1010,6 +1045,90 @@ int w90g_get_dis_log(void* hv, double* rows, int max_rows) {
   return n;
 }
 
+// sitesym_read's data (src/sitesym.F90:698-765): the .dmn counts, 1-based ik2ir(nk),
+// ir2ik(nkirr), kptsym(nsym, nkirr), d_matrix_wann(nw, nw, nsym, nkirr) and
+// d_matrix_band(nb, nb, nsym, nkirr), Fortran order, complex as (re, im) pairs.  The
+// star / little-group tables are built here, in the reference's loop order.
+int w90g_set_sitesym(void* hv, int nb, int nsym, int nkirr, int nk, const int* ik2ir, const int* ir2ik,
+                     const int* kptsym, const double* d_wann, const double* d_band) {
+  Handle* h = H(hv);
+  if (!h->setup_complete) return fail(h, 1, "cinput_setopt must be called before w90g_set_sitesym");
+  if (nb != h->num_bands) return fail(h, 6, "Error: Number of bands is not correct (sitesym_read)");
+  if (nk != h->num_kpts) return fail(h, 6, "Error: Number of k-points is not correct (sitesym_read)");
+  if (nsym < 1 || nkirr < 1 || nkirr > nk || !ik2ir || !ir2ik || !kptsym || !d_wann || !d_band)
+    return fail(h, 6, "Error: symmetry data missing or inconsistent (sitesym_read)");
+  for (int k = 0; k < nk; ++k)
+    if (ik2ir[k] < 1 || ik2ir[k] > nkirr) return fail(h, 6, "Error: ik2ir out of range (sitesym_read)");
+  for (int ir = 0; ir < nkirr; ++ir) {
+    if (ir2ik[ir] < 1 || ir2ik[ir] > nk) return fail(h, 6, "Error: ir2ik out of range (sitesym_read)");
+    if (ik2ir[ir2ik[ir] - 1] != ir + 1) return fail(h, 6, "Error: ik2ir and ir2ik disagree (sitesym_read)");
+  }
+  for (int i = 0; i < nsym * nkirr; ++i)
+    if (kptsym[i] < 1 || kptsym[i] > nk) return fail(h, 6, "Error: kptsym out of range (sitesym_read)");
+  const int W = h->num_wann;
+  const size_t WW = (size_t)W * W, BB = (size_t)nb * nb;
+  std::vector<int> slot((size_t)nsym * nkirr, -1);
+  std::vector<double> dw, db;
+  auto slot_of = [&](int ir, int isym) {
+    int& sl = slot[(size_t)ir * nsym + isym];
+    if (sl < 0) {
+      sl = (int)(dw.size() / (2 * WW));
+      const double* a = d_wann + 2 * WW * ((size_t)ir * nsym + isym);
+      const double* b = d_band + 2 * BB * ((size_t)ir * nsym + isym);
+      dw.insert(dw.end(), a, a + 2 * WW);
+      db.insert(db.end(), b, b + 2 * BB);   // nb = nw: isolated bands
+    }
+    return sl;
+  };
+  std::vector<int> ik(nkirr), moff, mem, goff, grp;
+  std::vector<char> done(nk, 0);
+  // star members in first-occurrence order (sitesym_symmetrize_rotation / _gradient
+  // mode 1 / _u_matrix, :119-190, :222-240, :305-322)
+  for (int ir = 0; ir < nkirr; ++ir) {
+    ik[ir] = ir2ik[ir] - 1;
+    done[ik[ir]] = 1;
+    moff.push_back((int)mem.size() / 2);
+    for (int isym = 1; isym < nsym; ++isym) {
+      const int irk = kptsym[(size_t)ir * nsym + isym] - 1;
+      if (done[irk]) continue;
+      done[irk] = 1;
+      mem.push_back(irk);
+      mem.push_back(slot_of(ir, isym));
+    }
+  }
+  moff.push_back((int)mem.size() / 2);
+  for (int k = 0; k < nk; ++k) {
+    if (!done[k]) return fail(h, 1, "error in sitesym_symmetrize_rotation");
+    // the members are exactly the k whose irreducible point is another k (mode 1 zeroes those)
+    const bool irr = ir2ik[ik2ir[k] - 1] - 1 == k;
+    bool member = false;
+    for (size_t m = 0; m < mem.size(); m += 2) member = member || mem[m] == k;
+    if (irr == member) return fail(h, 6, "Error: k-point stars and ik2ir disagree (sitesym_read)");
+  }
+  // little groups {R : R k = k} in isym order, the first symmetry included (symmetrize_ukirr, :451-470)
+  for (int ir = 0; ir < nkirr; ++ir) {
+    goff.push_back((int)grp.size() / 2);
+    for (int isym = 0; isym < nsym; ++isym)
+      if (kptsym[(size_t)ir * nsym + isym] - 1 == ik[ir]) {
+        grp.push_back(isym);
+        grp.push_back(slot_of(ir, isym));
+      }
+  }
+  goff.push_back((int)grp.size() / 2);
+  h->sym_nir = nkirr;
+  h->sym_nk = nk;
+  h->sym_nb = nb;
+  h->sym_ik = ik;
+  h->sym_moff = moff;
+  h->sym_mem = mem;
+  h->sym_goff = goff;
+  h->sym_grp = grp;
+  h->sym_d = dw;
+  h->sym_db = db;
+  h->have_sym = true;
+  return 0;
+}
+
 void w90g_get_dis_windows(void* hv, int* ndimwin, int* nfirstwin) {
   Handle* h = H(hv);
   std::copy(h->dis_ndimwin.begin(), h->dis_ndimwin.end(), ndimwin);
@@ -1049,6 +1168,7 @@ void w90g_set_stream(void* hv, void* cuda_stream) {
 int w90g_profile_device(void* hv, double* d_m, double* d_u, int max_iters, double* ms, int* counts) {
   Handle* h = H(hv);
   if (!h->setup_complete) return fail(h, 1, "cinput_setopt must be called before w90g_profile_device");
+  if (sym_missing(h)) return fail(h, 6, kSymMissing);
   ProblemSpec s;
   build_spec(h, s);
   std::string err;
@@ -1109,6 +1229,10 @@ void w90g_wannierise_batch_device(void** handles, int nprob, double** d_m, doubl
     ierr[i] = 0;
     if (!h->setup_complete || !d_m[i] || !d_u[i]) {
       ierr[i] = fail(h, 1, "batch: handle not set up or buffers missing");
+      continue;
+    }
+    if (sym_missing(h)) {
+      ierr[i] = fail(h, 6, kSymMissing);
       continue;
     }
     ProblemSpec s;
@@ -1189,6 +1313,7 @@ int w90g_server_submit(void* server, void* handle, double* d_m, double* d_u, lon
   Handle* h = H(handle);
   if (!sv || !h) return 1;
   if (!h->setup_complete || !d_m || !d_u) return fail(h, 1, "serve: handle not set up or buffers missing");
+  if (sym_missing(h)) return fail(h, 6, kSymMissing);
   std::unique_ptr<ServeJob> j(new ServeJob());
   j->tag = tag;
   j->h = h;

@@ -39,6 +39,10 @@ __global__ void k_u_identity(const Problem* probs, WorkMap wm);
 __global__ void k_frob0(const Problem* probs, WorkMap wm);
 __global__ void k_precond(const Problem* probs, int dir);
 __global__ void k_phases(const Problem* probs, int mode);
+// kernels (k_sitesym.cu)
+__global__ void k_sym_grad(const Problem* probs, WorkMap wm);
+__global__ void k_sym_dir(const Problem* probs, WorkMap wm);
+__global__ void k_sym_u(const Problem* probs, WorkMap wm);
 cudaError_t oz_launch(int wp, int step, const Problem* probs, WorkMap wm, int which, int grid,
                       cudaStream_t s);
 cudaError_t oz_set_attributes(int wp);
@@ -106,6 +110,15 @@ int Engine::setup(const std::vector<ProblemSpec>& specs, std::string& err) {
       err = "slwf: slwf_num outside 1..num_wann-1 or constrained centres not num_wann x 3";
       return 5;
     }
+    if (s.sym_nir > 0) {
+      const size_t nir = s.sym_nir, WW2 = (size_t)2 * s.W * s.W;
+      if (s.sym_ik.size() != nir || s.sym_moff.size() != nir + 1 || s.sym_goff.size() != nir + 1 ||
+          s.sym_mem.size() != (size_t)2 * s.sym_moff[nir] || s.sym_grp.size() != (size_t)2 * s.sym_goff[nir] ||
+          s.sym_d.empty() || s.sym_d.size() % WW2 != 0 || s.sym_db.size() != s.sym_d.size()) {
+        err = "site symmetry: tables missing or inconsistent";
+        return 5;
+      }
+    }
     if (s.precond && (s.nrpts < 1 || s.pc_kr.size() != (size_t)2 * s.K * s.nrpts ||
                       s.pc_r2.size() != (size_t)s.nrpts || s.pc_ndeg.size() != (size_t)s.nrpts)) {
       err = "precond: Wigner-Seitz tables missing or inconsistent";
@@ -116,7 +129,8 @@ int Engine::setup(const std::vector<ProblemSpec>& specs, std::string& err) {
   std::ostringstream key;
   for (const auto& s : specs)
     key << s.W << ',' << s.K << ',' << s.B << ',' << s.ctl.num_iter << ',' << s.tensor << ',' << s.tensor_exp << ','
-        << s.precond << ',' << s.nrpts << ',' << s.guiding << ',' << (s.slwf_num > 0) << ';';
+        << s.precond << ',' << s.nrpts << ',' << s.guiding << ',' << (s.slwf_num > 0) << ',' << s.sym_nir << ','
+        << s.sym_mem.size() << ',' << s.sym_grp.size() << ',' << s.sym_d.size() << ';';
   specs_ = specs;
   if (arena_ && key.str() == layout_key_) {
     // refresh the read-only tables (they may differ at equal shapes)
@@ -138,6 +152,7 @@ int Engine::setup(const std::vector<ProblemSpec>& specs, std::string& err) {
       hprobs_[p].ctl = s.ctl;
       hprobs_[p].wbtot = s.wbtot;
       if (int rc = set_slwf(p, err)) return rc;
+      if (int rc = set_sym(p, err)) return rc;
     }
     W90G_CHECK(cudaMemcpyAsync(dprobs_, hprobs_.data(), hprobs_.size() * sizeof(Problem), cudaMemcpyHostToDevice, stream()));
     return 0;
@@ -172,10 +187,11 @@ struct Sizes {
   size_t pkr, pr2, pgr, pgp, ppart;
   size_t gbka, gneigh, grg, gsheet, gcsheet;
   size_t slwf;
+  size_t symi, symd, symw;
   size_t total() const {
     return 2 * M + 2 * U + 3 * KWW + work + tbuf + 2 * diag + offd + gpart + cen + log + logc + nn + bk + wb + st +
            op1 + op2 + m0 + u0 + inv + fr + m0s + m0e + pkr + 2 * pr2 + pgr + pgp + ppart + gbka + gneigh + grg + gsheet +
-           gcsheet + slwf;
+           gcsheet + slwf + symi + 2 * symd + symw;
   }
 };
 
@@ -227,6 +243,14 @@ Sizes problem_sizes(const ProblemSpec& s, int wp, int* pc_tiles) {
     if (pc_tiles) *pc_tiles = std::max(*pc_tiles, (int)(te * ((std::max(K, NR) + 15) / 16)));
   }
   z.slwf = s.slwf_num > 0 ? align_up(3 * W * 8) : 0;
+  z.symi = z.symd = z.symw = 0;
+  if (s.sym_nir > 0) {
+    const size_t nint = s.sym_ik.size() + s.sym_moff.size() + s.sym_mem.size() + s.sym_goff.size() +
+                        s.sym_grp.size() + (size_t)s.sym_nir;
+    z.symi = align_up(nint * 4);
+    z.symd = align_up(s.sym_d.size() * 8);
+    z.symw = align_up((size_t)s.sym_nir * kSymWork * WW * 16);
+  }
   z.gbka = z.gneigh = z.grg = z.gsheet = z.gcsheet = 0;
   if (s.guiding) {
     z.gbka = align_up((size_t)s.nnh * 3 * 8);
@@ -239,7 +263,7 @@ Sizes problem_sizes(const ProblemSpec& s, int wp, int* pc_tiles) {
 }
 
 size_t header_bytes(int np, int n_k) {
-  return align_up(np * sizeof(Problem)) + 4 * align_up((np + 1) * sizeof(int)) + align_up(n_k * sizeof(int)) +
+  return align_up(np * sizeof(Problem)) + 5 * align_up((np + 1) * sizeof(int)) + align_up(n_k * sizeof(int)) +
          align_up(n_k * sizeof(double)) + align_up(sizeof(int));
 }
 
@@ -267,7 +291,8 @@ int Engine::alloc(std::string& err) {
   guide_w_ = 0;
   maxW_small_ = 0;
   max_iter_ = 0;
-  std::vector<int> offs_k(np + 1, 0), offs_kb(np + 1, 0), offs_grad(np + 1, 0), offs_chunk(np + 1, 0);
+  std::vector<int> offs_k(np + 1, 0), offs_kb(np + 1, 0), offs_grad(np + 1, 0), offs_chunk(np + 1, 0),
+      offs_ir(np + 1, 0);
   for (int p = 0; p < np; ++p) {
     const auto& s = specs_[p];
     const int nt = (s.W + kTileW - 1) / kTileW;
@@ -278,6 +303,7 @@ int Engine::alloc(std::string& err) {
     offs_kb[p + 1] = offs_kb[p] + s.K * s.B;
     offs_grad[p + 1] = offs_grad[p] + s.K * nt * nt;
     offs_chunk[p + 1] = offs_chunk[p] + (s.K * s.B + 63) / 64;
+    offs_ir[p + 1] = offs_ir[p] + s.sym_nir;
     if (s.W <= 32) maxW_small_ = std::max(maxW_small_, s.W);
     max_iter_ = std::max(max_iter_, s.ctl.num_iter);
   }
@@ -285,6 +311,7 @@ int Engine::alloc(std::string& err) {
   n_kb_ = offs_kb[np];
   n_grad_ = offs_grad[np];
   n_chunk_ = offs_chunk[np];
+  n_ir_ = offs_ir[np];
   total += header_bytes(np, n_k_);
   if (async_alloc_) W90G_CHECK(cudaMallocAsync(&arena_, total, stream()));
   else W90G_CHECK(cudaMalloc(&arena_, total));
@@ -300,6 +327,7 @@ int Engine::alloc(std::string& err) {
   d_offs_kb_ = (int*)take(align_up((np + 1) * sizeof(int)));
   d_offs_grad_ = (int*)take(align_up((np + 1) * sizeof(int)));
   d_offs_chunk_ = (int*)take(align_up((np + 1) * sizeof(int)));
+  d_offs_ir_ = (int*)take(align_up((np + 1) * sizeof(int)));
   d_status_ = (int*)take(align_up(n_k_ * sizeof(int)));
   d_unit_ = (double*)take(align_up(n_k_ * sizeof(double)));
   int* d_alldone = (int*)take(align_up(sizeof(int)));
@@ -377,6 +405,13 @@ int Engine::alloc(std::string& err) {
     }
     P.slwf_c = z.slwf ? (const double*)take(z.slwf) : nullptr;
     if (int rc = set_slwf(p, err)) return rc;
+    if (z.symi) {
+      P.sym_ik = (const int*)take(z.symi);
+      P.sym_d = (const double2*)take(z.symd);
+      P.sym_db = (const double2*)take(z.symd);
+      P.sym_work = (double2*)take(z.symw);
+    }
+    if (int rc = set_sym(p, err)) return rc;
     P.precond = s.precond;
     P.nrpts = s.precond ? s.nrpts : 0;
     if (s.precond) {
@@ -399,6 +434,8 @@ int Engine::alloc(std::string& err) {
   W90G_CHECK(cudaMemcpyAsync(d_offs_kb_, offs_kb.data(), (np + 1) * sizeof(int), cudaMemcpyHostToDevice, stream()));
   W90G_CHECK(cudaMemcpyAsync(d_offs_grad_, offs_grad.data(), (np + 1) * sizeof(int), cudaMemcpyHostToDevice, stream()));
   W90G_CHECK(cudaMemcpyAsync(d_offs_chunk_, offs_chunk.data(), (np + 1) * sizeof(int), cudaMemcpyHostToDevice, stream()));
+  W90G_CHECK(cudaMemcpyAsync(d_offs_ir_, offs_ir.data(), (np + 1) * sizeof(int), cudaMemcpyHostToDevice, stream()));
+  W90G_CHECK(cudaStreamSynchronize(stream()));   // the host offset vectors go out of scope
   // dynamic shared memory limits of the shared-memory kernels: a function attribute is
   // process wide, so every engine sets the same value, the maximum for W <= 32 (engines
   // of different widths may run concurrently in the batched form)
@@ -436,6 +473,36 @@ int Engine::set_slwf(int p, std::string& err) {
   slwf_host_.resize(hprobs_.size());
   slwf_host_[p] = c;   // the copy below reads it asynchronously
   W90G_CHECK(cudaMemcpyAsync((void*)P.slwf_c, slwf_host_[p].data(), c.size() * 8, cudaMemcpyHostToDevice, stream()));
+  return 0;
+}
+
+// symmetry tables of problem p into its arena block: one int block (sym_ik, sym_moff,
+// sym_mem, sym_goff, sym_grp, sym_status) and the slot matrices
+int Engine::set_sym(int p, std::string& err) {
+  const auto& s = specs_[p];
+  Problem& P = hprobs_[p];
+  P.sym_nir = s.sym_nir;
+  P.sym_eps = s.sym_eps;
+  if (s.sym_nir <= 0) return 0;
+  std::vector<int> ints;
+  ints.insert(ints.end(), s.sym_ik.begin(), s.sym_ik.end());
+  ints.insert(ints.end(), s.sym_moff.begin(), s.sym_moff.end());
+  ints.insert(ints.end(), s.sym_mem.begin(), s.sym_mem.end());
+  ints.insert(ints.end(), s.sym_goff.begin(), s.sym_goff.end());
+  ints.insert(ints.end(), s.sym_grp.begin(), s.sym_grp.end());
+  ints.insert(ints.end(), (size_t)s.sym_nir, 0);
+  int* base = const_cast<int*>(P.sym_ik);
+  size_t o = 0;
+  P.sym_moff = base + (o += s.sym_ik.size());
+  P.sym_mem = base + (o += s.sym_moff.size());
+  P.sym_goff = base + (o += s.sym_mem.size());
+  P.sym_grp = base + (o += s.sym_goff.size());
+  P.sym_status = base + (o += s.sym_grp.size());
+  sym_host_.resize(hprobs_.size());
+  sym_host_[p] = std::move(ints);
+  W90G_CHECK(cudaMemcpyAsync(base, sym_host_[p].data(), sym_host_[p].size() * 4, cudaMemcpyHostToDevice, stream()));
+  W90G_CHECK(cudaMemcpyAsync((void*)P.sym_d, s.sym_d.data(), s.sym_d.size() * 8, cudaMemcpyHostToDevice, stream()));
+  W90G_CHECK(cudaMemcpyAsync((void*)P.sym_db, s.sym_db.data(), s.sym_db.size() * 8, cudaMemcpyHostToDevice, stream()));
   return 0;
 }
 
@@ -499,9 +566,13 @@ int Engine::project(std::string& err) {
   const WorkMap wmkb{d_offs_kb_, nprob()};
   k_lowdin<<<n_k_, 256, 4 * ws * ws * 16, st>>>(dprobs_, wmk, d_status_);
   W90G_CHECK(cudaGetLastError());
-  k_m_update<<<n_kb_, 256, 4 * ws * ws * 16, st>>>(dprobs_, wmkb, 1, 0);
-  W90G_CHECK(cudaGetLastError());
-  launches_ += 2;
+  launches_ += 1;
+  // symmetry-adapted initial U (src/overlap.F90:901-905)
+  if (n_ir_) {
+    k_sym_u<<<n_ir_, 256, 0, st>>>(dprobs_, WorkMap{d_offs_ir_, nprob()});
+    W90G_CHECK(cudaGetLastError());
+    launches_ += 1;
+  }
   std::vector<int> status(n_k_);
   W90G_CHECK(cudaMemcpyAsync(status.data(), d_status_, n_k_ * sizeof(int), cudaMemcpyDeviceToHost, st));
   W90G_CHECK(cudaStreamSynchronize(st));
@@ -515,6 +586,26 @@ int Engine::project(std::string& err) {
       return 1;
     }
   }
+  for (size_t p = 0; p < hprobs_.size(); ++p) {
+    const int nir = hprobs_[p].sym_nir;
+    if (nir <= 0) continue;
+    std::vector<int> ss(nir);
+    W90G_CHECK(cudaMemcpy(ss.data(), hprobs_[p].sym_status, nir * sizeof(int), cudaMemcpyDeviceToHost));
+    for (int ir = 0; ir < nir; ++ir) {
+      if (ss[ir] == 1) {
+        // set_error_unconv (src/sitesym.F90:478-486)
+        err = "symmetrize_ukirr: not converged";
+        return -1;
+      }
+      if (ss[ir] == 2) {
+        err = " ERROR: IN ZGESVD IN orthogonalize_u";
+        return 1;
+      }
+    }
+  }
+  k_m_update<<<n_kb_, 256, 4 * ws * ws * 16, st>>>(dprobs_, wmkb, 1, 0);
+  W90G_CHECK(cudaGetLastError());
+  launches_ += 1;
   return 0;
 }
 
@@ -578,11 +669,13 @@ void Engine::launch_iteration(cudaStream_t s) {
   const WorkMap wmg{d_offs_grad_, np};
   if (guide_w_) k_phases<<<dim3(guide_w_, np), 256, 0, s>>>(dprobs_, 1);
   k_grad<<<n_grad_, 256, 0, s>>>(dprobs_, wmg);
+  if (n_ir_) k_sym_grad<<<n_ir_, 256, 0, s>>>(dprobs_, WorkMap{d_offs_ir_, np});
   if (pc_tiles_) {
     k_precond<<<dim3(pc_tiles_, np), 256, 0, s>>>(dprobs_, 0);
     k_precond<<<dim3(pc_tiles_, np), 256, 0, s>>>(dprobs_, 1);
   }
   k_ctrl_search<<<np, 256, 0, s>>>(dprobs_);
+  if (n_ir_) k_sym_dir<<<n_ir_, 256, 0, s>>>(dprobs_, WorkMap{d_offs_ir_, np});
   launch_exp(s, 0);
   launch_mupdate(s, 0);
   launch_omega(s, 0);
@@ -633,7 +726,8 @@ int Engine::advance(int n, int* d_flag, std::string& err) {
   n = std::min(n, max_iter_ - launched_iters_);
   for (int i = 0; i < n; ++i) W90G_CHECK(cudaGraphLaunch(graph_exec_, st));
   // grad, search, 2 x (exp, M update, 3 spread passes), step, end (+ 2 precond)
-  launches_ += (10LL + 2 * (tensor_wp_ ? 2 : 1) + (pc_tiles_ ? 2 : 0) + (guide_w_ ? 1 : 0)) * std::max(n, 0);
+  launches_ += (10LL + 2 * (tensor_wp_ ? 2 : 1) + (pc_tiles_ ? 2 : 0) + (guide_w_ ? 1 : 0) + (n_ir_ ? 2 : 0)) *
+                std::max(n, 0);
   launched_iters_ += std::max(n, 0);
   if (d_flag) {
     // every problem done (converged or out of iterations) -> *d_flag = 1

@@ -34,6 +34,12 @@ struct ProblemSpec {
   int slwf_num = 0;
   double slwf_lambda = 0.0;
   std::vector<double> slwf_c;
+  // symmetry-adapted mode (isolated bands): the tables of Problem::sym_* (sym_nir = 0:
+  // off); sym_d / sym_db hold the slot matrices, W x W column-major, re/im interleaved
+  int sym_nir = 0;
+  double sym_eps = 1.0e-3;
+  std::vector<int> sym_ik, sym_moff, sym_mem, sym_goff, sym_grp;
+  std::vector<double> sym_d, sym_db;
 };
 
 struct ProblemResult {
@@ -110,6 +116,7 @@ class Engine {
   int prepare_tensor(cudaStream_t st, std::string& err);
   int init_states(std::string& err);
   int set_slwf(int p, std::string& err);
+  int set_sym(int p, std::string& err);
 
   std::vector<ProblemSpec> specs_;
   std::vector<Problem> hprobs_;
@@ -124,6 +131,8 @@ class Engine {
   int* d_status_ = nullptr;
   double* d_unit_ = nullptr;
   int n_k_ = 0, n_kb_ = 0, n_grad_ = 0, n_chunk_ = 0;
+  int n_ir_ = 0;         // irreducible k-points of the symmetry-adapted problems (CTAs of k_sym_*)
+  int* d_offs_ir_ = nullptr;
   int pc_tiles_ = 0;     // > 0: some problem is preconditioned; CTAs per problem of k_precond
   int guide_w_ = 0;      // > 0: some problem uses guiding centres; CTAs per problem of k_phases
   int maxW_small_ = 0;   // largest W <= 32 in the batch (shared-memory kernels)
@@ -139,6 +148,7 @@ class Engine {
   int launched_iters_ = 0;
   std::vector<double> guide_init_;   // host staging of csheet = 1
   std::vector<std::vector<double>> slwf_host_;   // host staging of the constrained centres
+  std::vector<std::vector<int>> sym_host_;       // host staging of the symmetry tables
   bool async_alloc_ = false;
   double last_exp_products_ = 0.0;
 };

@@ -984,7 +984,8 @@ __global__ void __launch_bounds__(256) k_exp_u(const Problem* __restrict__ probs
           *T = buf + 5 * WW;
   double2* Dk = P.D + (size_t)k * WW;
   const double s = (which == 0) ? st->s_trial : st->s_second;
-  if (which == 0) {
+  if (which == 0 && P.sym_nir == 0) {
+    // (in the symmetry-adapted mode k_sym_dir has formed D already)
     const double cg = st->coefG, cd = st->coefD;
     const double2* Gk = (st->use_gp ? P.pc_gp : P.G) + (size_t)k * WW;
     for (int e = threadIdx.x; e < WW; e += blockDim.x) {

@@ -562,7 +562,8 @@ __global__ void __launch_bounds__(256, 2) k_oz_exp(const Problem* __restrict__ p
           *T = mats + 5 * WW;
   double2* Dk = P.D + (size_t)k * WW;
   const double s = (which == 0) ? st->s_trial : st->s_second;
-  if (which == 0) {
+  if (which == 0 && P.sym_nir == 0) {
+    // (in the symmetry-adapted mode k_sym_dir has formed D already)
     const double cg = st->coefG, cd = st->coefD;
     const double2* Gk = (st->use_gp ? P.pc_gp : P.G) + (size_t)k * WW;
     for (int e = tid; e < WW; e += blockDim.x) {

@@ -163,7 +163,28 @@ struct Problem {
   int slwf_num, pad4;
   double slwf_lambda, slwf_nu0;
   const double* slwf_c;
+  // symmetry-adapted mode (site_symmetry = T, src/sitesym.F90): sym_nir > 0 irreducible
+  // k-points; per irreducible ir its k (sym_ik), its star's reducible members
+  // sym_mem[sym_moff[ir] .. sym_moff[ir+1]) as (k, slot) pairs in the reference's
+  // first-occurrence order, its little group {R : R k = k} sym_grp[sym_goff[ir] ..
+  // sym_goff[ir+1]) as (isym, slot) pairs in isym order (isym 0-based, the identity
+  // first); slot s indexes D(R, k_ir) = sym_d[s] and d(R, k_ir) = sym_db[s] (W x W,
+  // column-major); sym_work kSymWork W x W matrices per irreducible k; sym_status the
+  // initial symmetrisation's result per irreducible k
+  int sym_nir, pad5;
+  double sym_eps;
+  const int* sym_ik;
+  const int* sym_moff;
+  const int* sym_mem;
+  const int* sym_goff;
+  const int* sym_grp;
+  const double2* sym_d;
+  const double2* sym_db;
+  double2* sym_work;
+  int* sym_status;
 };
+
+constexpr int kSymWork = 5;
 
 // Work map: blockIdx.x -> (problem, local index) over a prefix sum.
 struct WorkMap {

@@ -203,6 +203,19 @@ def w90_get_dis_log(common: LibCommon, max_rows: int) -> np.ndarray:
     return out[:n]
 
 
+def w90_set_sitesym(common: LibCommon, dmn: dict) -> int:
+    """The symmetry data of the symmetry-adapted mode (sitesym_read's content; see
+    w90io.read_dmn for the keys).  Returns the ierr."""
+    i32 = lambda a: np.ascontiguousarray(np.asarray(a, dtype=np.int32).reshape(-1, order="F"))
+    c128 = lambda a: np.ascontiguousarray(np.asarray(a, dtype=np.complex128).reshape(-1, order="F"))
+    ik2ir, ir2ik, kptsym = i32(dmn["ik2ir"]), i32(dmn["ir2ik"]), i32(dmn["kptsym"])
+    dw, db = c128(dmn["d_matrix_wann"]), c128(dmn["d_matrix_band"])
+    ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int))
+    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    return common._L.w90g_set_sitesym(common._h, int(dmn["num_bands"]), int(dmn["nsymmetry"]), int(dmn["nkptirr"]),
+                                      int(dmn["num_kpts"]), ip(ik2ir), ip(ir2ik), ip(kptsym), dp(dw), dp(db))
+
+
 def w90_get_dis_windows(common: LibCommon, num_kpts: int):
     """(ndimwin[nk], nfirstwin[nk] 0-based) of the last w90_disentangle's outer window."""
     nd = np.zeros(num_kpts, dtype=np.int32)

@@ -100,8 +100,9 @@ def win_system(path):
             "iprint", "num_print_cycles", "conv_noise_num", "dis_num_iter", "dis_conv_window",
             "dis_spheres_num", "slwf_num")
     reals = ("conv_tol", "trial_step", "fixed_step", "conv_noise_amp", "kmesh_tol", "dis_win_min",
-             "dis_win_max", "dis_froz_min", "dis_froz_max", "dis_mix_ratio", "dis_conv_tol", "slwf_lambda")
-    bools = ("precond", "guiding_centres", "gamma_only", "slwf_constrain")
+             "dis_win_max", "dis_froz_min", "dis_froz_max", "dis_mix_ratio", "dis_conv_tol", "slwf_lambda",
+             "symmetrize_eps")
+    bools = ("precond", "guiding_centres", "gamma_only", "slwf_constrain", "site_symmetry")
     for k in ints:
         if k in kw:
             opts[k] = int(kw[k].split()[0])
@@ -293,6 +294,35 @@ def write_amn(path, a, comment="written by wannier90_gb300"):
                 for mm in range(nb):
                     z = a[mm, n, k]
                     f.write("%5d%5d%5d%18.12f%18.12f\n" % (mm + 1, n + 1, k + 1, z.real, z.imag))
+
+
+def read_dmn(path, num_wann):
+    """A .dmn file as sitesym_read reads it (src/sitesym.F90:698-765): the counts
+    (num_bands, nsymmetry, nkptirr, num_kpts), then list-directed ik2ir(num_kpts),
+    ir2ik(nkptirr), kptsym(nsymmetry, nkptirr) (1-based), d_matrix_wann(num_wann,
+    num_wann, nsymmetry, nkptirr) and d_matrix_band(num_bands, num_bands, nsymmetry,
+    nkptirr) with complex values written '(re, im)'.  Arrays are returned with those
+    Fortran shapes and index order."""
+    with open(path) as f:
+        f.readline()
+        nb, nsym, nkirr, nk = (int(x) for x in f.readline().split()[:4])
+        rest = f.read()
+    first = rest.find("(")
+    ints = np.array(rest[:first if first >= 0 else len(rest)].replace(",", " ").split(), dtype=np.int64)
+    want = nk + nkirr + nsym * nkirr
+    if len(ints) < want:
+        raise ValueError("%s: expected %d integers before the matrices, found %d" % (path, want, len(ints)))
+    vals = re.findall(r"\(\s*([^,\s]+)\s*,\s*([^)\s]+)\s*\)", rest[first:] if first >= 0 else "")
+    z = np.array([_fnum(a) + 1j * _fnum(b) for a, b in vals], dtype=np.complex128)
+    nw2 = num_wann * num_wann * nsym * nkirr
+    nb2 = nb * nb * nsym * nkirr
+    if len(z) < nw2 + nb2:
+        raise ValueError("%s: expected %d complex values, found %d" % (path, nw2 + nb2, len(z)))
+    return dict(num_bands=nb, nsymmetry=nsym, nkptirr=nkirr, num_kpts=nk,
+                ik2ir=ints[:nk], ir2ik=ints[nk:nk + nkirr],
+                kptsym=ints[nk + nkirr:want].reshape((nsym, nkirr), order="F"),
+                d_matrix_wann=z[:nw2].reshape((num_wann, num_wann, nsym, nkirr), order="F"),
+                d_matrix_band=z[nw2:nw2 + nb2].reshape((nb, nb, nsym, nkirr), order="F"))
 
 
 def read_eig(path, num_bands, num_kpts):
