@@ -27,6 +27,7 @@
 #include "engine.h"
 #include "kmesh.h"
 #include "seedio.h"
+#include "sym_tables.h"
 
 namespace {
 
@@ -1055,76 +1056,20 @@ int w90g_set_sitesym(void* hv, int nb, int nsym, int nkirr, int nk, const int* i
   if (!h->setup_complete) return fail(h, 1, "cinput_setopt must be called before w90g_set_sitesym");
   if (nb != h->num_bands) return fail(h, 6, "Error: Number of bands is not correct (sitesym_read)");
   if (nk != h->num_kpts) return fail(h, 6, "Error: Number of k-points is not correct (sitesym_read)");
-  if (nsym < 1 || nkirr < 1 || nkirr > nk || !ik2ir || !ir2ik || !kptsym || !d_wann || !d_band)
-    return fail(h, 6, "Error: symmetry data missing or inconsistent (sitesym_read)");
-  for (int k = 0; k < nk; ++k)
-    if (ik2ir[k] < 1 || ik2ir[k] > nkirr) return fail(h, 6, "Error: ik2ir out of range (sitesym_read)");
-  for (int ir = 0; ir < nkirr; ++ir) {
-    if (ir2ik[ir] < 1 || ir2ik[ir] > nk) return fail(h, 6, "Error: ir2ik out of range (sitesym_read)");
-    if (ik2ir[ir2ik[ir] - 1] != ir + 1) return fail(h, 6, "Error: ik2ir and ir2ik disagree (sitesym_read)");
-  }
-  for (int i = 0; i < nsym * nkirr; ++i)
-    if (kptsym[i] < 1 || kptsym[i] > nk) return fail(h, 6, "Error: kptsym out of range (sitesym_read)");
-  const int W = h->num_wann;
-  const size_t WW = (size_t)W * W, BB = (size_t)nb * nb;
-  std::vector<int> slot((size_t)nsym * nkirr, -1);
-  std::vector<double> dw, db;
-  auto slot_of = [&](int ir, int isym) {
-    int& sl = slot[(size_t)ir * nsym + isym];
-    if (sl < 0) {
-      sl = (int)(dw.size() / (2 * WW));
-      const double* a = d_wann + 2 * WW * ((size_t)ir * nsym + isym);
-      const double* b = d_band + 2 * BB * ((size_t)ir * nsym + isym);
-      dw.insert(dw.end(), a, a + 2 * WW);
-      db.insert(db.end(), b, b + 2 * BB);   // nb = nw: isolated bands
-    }
-    return sl;
-  };
-  std::vector<int> ik(nkirr), moff, mem, goff, grp;
-  std::vector<char> done(nk, 0);
-  // star members in first-occurrence order (sitesym_symmetrize_rotation / _gradient
-  // mode 1 / _u_matrix, :119-190, :222-240, :305-322)
-  for (int ir = 0; ir < nkirr; ++ir) {
-    ik[ir] = ir2ik[ir] - 1;
-    done[ik[ir]] = 1;
-    moff.push_back((int)mem.size() / 2);
-    for (int isym = 1; isym < nsym; ++isym) {
-      const int irk = kptsym[(size_t)ir * nsym + isym] - 1;
-      if (done[irk]) continue;
-      done[irk] = 1;
-      mem.push_back(irk);
-      mem.push_back(slot_of(ir, isym));
-    }
-  }
-  moff.push_back((int)mem.size() / 2);
-  for (int k = 0; k < nk; ++k) {
-    if (!done[k]) return fail(h, 1, "error in sitesym_symmetrize_rotation");
-    // the members are exactly the k whose irreducible point is another k (mode 1 zeroes those)
-    const bool irr = ir2ik[ik2ir[k] - 1] - 1 == k;
-    bool member = false;
-    for (size_t m = 0; m < mem.size(); m += 2) member = member || mem[m] == k;
-    if (irr == member) return fail(h, 6, "Error: k-point stars and ik2ir disagree (sitesym_read)");
-  }
-  // little groups {R : R k = k} in isym order, the first symmetry included (symmetrize_ukirr, :451-470)
-  for (int ir = 0; ir < nkirr; ++ir) {
-    goff.push_back((int)grp.size() / 2);
-    for (int isym = 0; isym < nsym; ++isym)
-      if (kptsym[(size_t)ir * nsym + isym] - 1 == ik[ir]) {
-        grp.push_back(isym);
-        grp.push_back(slot_of(ir, isym));
-      }
-  }
-  goff.push_back((int)grp.size() / 2);
-  h->sym_nir = nkirr;
+  w90g::SymTables t;
+  std::string msg;
+  if (int rc = w90g::build_sym_tables(h->num_wann, nb, nsym, nkirr, nk, ik2ir, ir2ik, kptsym, d_wann, d_band, t, msg))
+    return fail(h, rc, msg);
+  h->sym_nir = t.nir;
   h->sym_nk = nk;
   h->sym_nb = nb;
-  h->sym_ik = ik;
-  h->sym_moff = moff;
-  h->sym_mem = mem;
-  h->sym_goff = goff;
-  h->sym_grp = grp;
-  h->sym_d = dw;
-  h->sym_db = db;
+  h->sym_ik = t.ik;
+  h->sym_moff = t.moff;
+  h->sym_mem = t.mem;
+  h->sym_goff = t.goff;
+  h->sym_grp = t.grp;
+  h->sym_d = t.d;
+  h->sym_db = t.db;
   h->have_sym = true;
   return 0;
 }
