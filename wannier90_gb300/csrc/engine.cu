@@ -435,7 +435,6 @@ int Engine::alloc(std::string& err) {
   W90G_CHECK(cudaMemcpyAsync(d_offs_grad_, offs_grad.data(), (np + 1) * sizeof(int), cudaMemcpyHostToDevice, stream()));
   W90G_CHECK(cudaMemcpyAsync(d_offs_chunk_, offs_chunk.data(), (np + 1) * sizeof(int), cudaMemcpyHostToDevice, stream()));
   W90G_CHECK(cudaMemcpyAsync(d_offs_ir_, offs_ir.data(), (np + 1) * sizeof(int), cudaMemcpyHostToDevice, stream()));
-  W90G_CHECK(cudaStreamSynchronize(stream()));   // the host offset vectors go out of scope
   // dynamic shared memory limits of the shared-memory kernels: a function attribute is
   // process wide, so every engine sets the same value, the maximum for W <= 32 (engines
   // of different widths may run concurrently in the batched form)
