@@ -332,12 +332,13 @@ def _orthogonalize_u(u, n):
     return out
 
 
-def _symmetrize_ukirr(u, ir, sym, n=None):
+def _symmetrize_ukirr(u, ir, sym, n=None, d_band=None):
     """symmetrize_ukirr (src/sitesym.F90:392-497): average d^+(R,k) u D(R,k) over the
     little group {R: Rk = k} and orthonormalise, until sum |ngk I - sum u^+ d^+ u D| <
     symmetrize_eps (100 passes at most)."""
     W = u.shape[1]
     ntmp = u.shape[0] if n is None else n
+    db = sym.d_band if d_band is None else d_band
     ik = sym.ir2ik[ir]
     little = [isym for isym in range(sym.nsym) if sym.kptsym[isym, ir] == ik]
     ngk = len(little)
@@ -349,7 +350,7 @@ def _symmetrize_ukirr(u, ir, sym, n=None):
         for isym in little:
             sub = u[:ntmp] @ sym.d_wann[ir, isym]
             cmat = np.zeros_like(u)
-            cmat[:ntmp] = sym.d_band[ir, isym][:ntmp, :ntmp].conj().T @ sub
+            cmat[:ntmp] = db[ir, isym][:ntmp, :ntmp].conj().T @ sub
             usum += cmat
             cmat2 -= u[:ntmp].conj().T @ cmat[:ntmp]
         diff = float(np.abs(cmat2).sum())
@@ -361,22 +362,26 @@ def _symmetrize_ukirr(u, ir, sym, n=None):
     return u
 
 
-def sitesym_symmetrize_u_matrix(U, sym):
-    """sitesym_symmetrize_u_matrix (src/sitesym.F90:104-192), the wannierisation form
-    (ndim = num_wann): U(k_ir) symmetrised, then U(R k_ir) = d(R,k) U(k) D^+(R,k) for
-    each star member not yet set."""
+def sitesym_symmetrize_u_matrix(U, sym, ndimwin=None, d_band=None):
+    """sitesym_symmetrize_u_matrix (src/sitesym.F90:104-192): U(k_ir) symmetrised, then
+    U(R k_ir) = d(R,k) U(k) D^+(R,k) for each star member not yet set.  ndimwin None: the
+    wannierisation form (ndim = num_wann); else the disentanglement form, U_opt with
+    n = ndimwin(k_ir) window rows.  d_band overrides sym.d_band (after
+    sitesym_replace_d_matrix_band it is D itself)."""
     U = U.copy()
+    db = sym.d_band if d_band is None else d_band
     done = np.zeros(len(U), dtype=bool)
     for ir in range(sym.nkirr):
         ik = sym.ir2ik[ir]
         done[ik] = True
-        U[ik] = _symmetrize_ukirr(U[ik], ir, sym)
+        n = U.shape[1] if ndimwin is None else int(ndimwin[ik])
+        U[ik] = _symmetrize_ukirr(U[ik], ir, sym, None if ndimwin is None else n, d_band=db)
         for isym in range(1, sym.nsym):
             irk = sym.kptsym[isym, ir]
             if done[irk]:
                 continue
             done[irk] = True
-            U[irk] = sym.d_band[ir, isym] @ U[ik] @ sym.d_wann[ir, isym].conj().T
+            U[irk][:n] = db[ir, isym][:n, :n] @ U[ik][:n] @ sym.d_wann[ir, isym].conj().T
     if not done.all():
         raise RuntimeError("error in sitesym_symmetrize_u_matrix")
     return U
@@ -440,6 +445,88 @@ def sitesym_symmetrize_rotation(dU, sym):
     if not done.all():
         raise RuntimeError("error in sitesym_symmetrize_rotation")
     return dU
+
+
+def sitesym_symmetrize_zmatrix(Z, sym, ndimwin):
+    """sitesym_symmetrize_zmatrix (src/sitesym.F90:331-391): at each irreducible k,
+    Z(k) += d^+ Z(Rk) d over the star's first occurrences, then the little-group terms
+    d^+ Z d of that sum, divided by the little group's order.  Z: list of nd x nd (the
+    window part); the reducible k are left as they are."""
+    Z = [None if z is None else z.copy() for z in Z]
+    found = np.zeros(len(Z), dtype=bool)
+    for ir in range(sym.nkirr):
+        ik = sym.ir2ik[ir]
+        nd = int(ndimwin[ik])
+        found[ik] = True
+        for isym in range(1, sym.nsym):
+            irk = sym.kptsym[isym, ir]
+            if found[irk]:
+                continue
+            found[irk] = True
+            d = sym.d_band[ir, isym][:nd, :nd]
+            Z[ik] = Z[ik] + d.conj().T @ (Z[irk][:nd, :nd] @ d)
+        tmp = Z[ik].copy()
+        for isym in range(1, sym.nsym):
+            if sym.kptsym[isym, ir] != ik:
+                continue
+            d = sym.d_band[ir, isym][:nd, :nd]
+            Z[ik] = Z[ik] + d.conj().T @ (tmp @ d)
+        Z[ik] = Z[ik] / int(np.count_nonzero(sym.kptsym[:, ir] == ik))
+    return Z
+
+
+def _gen_eig_larger(h11, h12, h22, s11, s12, s22):
+    """The eigenvector of the larger eigenvalue of H v = w S v (2 x 2 Hermitian, S
+    positive definite), normalised to v^+ S v = 1, in the phase ZHPGVX gives it: what
+    sitesym_dis_extract_symmetry takes (src/sitesym.F90:649-668).  ZHPGVX reduces with the
+    upper Cholesky factor of S and zhptrd, whose reflector leaves the last coordinate
+    alone, so the second component comes out real; on these problems it comes out
+    positive.  The phase is not free: the symmetrisation that follows averages d^+ U D
+    column by column, and the testw90_disentanglement_sawfs lines move by 1e-7 A^2 under
+    another choice (5e-9 with this one)."""
+    H = np.array([[h11, h12], [np.conj(h12), h22]], dtype=np.complex128)
+    S = np.array([[s11, s12], [np.conj(s12), s22]], dtype=np.complex128)
+    L = np.linalg.cholesky(S)
+    Li = np.linalg.inv(L)
+    w, y = np.linalg.eigh(Li @ H @ Li.conj().T)
+    v = Li.conj().T @ y[:, 1]
+    if v[1] != 0:
+        v = v * (abs(v[1]) / v[1])
+    return v
+
+
+def sitesym_dis_extract_symmetry(sym, U, Z, ik, n, num_wann):
+    """sitesym_dis_extract_symmetry (src/sitesym.F90:550-695): steepest descent of
+    Omega_I at an irreducible k within the symmetric subspaces.  Per pass: ZU = Z U,
+    lambda = U^+ Z U, dU = ZU - U lambda (done when sum |dU| < 1e-10); each column moves
+    to the larger solution of the 2 x 2 problem in span(u_i, dU_i); then symmetrize_ukirr.
+    Up to 50 passes.  Returns (U, lambda of the last pass)."""
+    U = U.copy()
+    ir = sym.ik2ir[ik]
+    Zn = Z[:n, :n]
+    lam = None
+    for _ in range(50):
+        ZU = Zn @ U[:n]
+        lam = U[:n].conj().T @ ZU
+        dU = ZU - U[:n] @ lam
+        if np.abs(dU).sum() < 1e-10:
+            return U, lam
+        Unew = np.zeros_like(U)
+        for i in range(num_wann):
+            u, zu, du = U[:n, i], ZU[:, i], dU[:, i]
+            h11 = np.vdot(u, zu).real
+            h12 = np.vdot(zu, du)
+            h22 = np.vdot(du, Zn @ du).real
+            s11 = np.vdot(u, u).real
+            s12 = np.vdot(u, du)
+            s22 = np.vdot(du, du).real
+            if abs(s22) < 1e-10:
+                Unew[:, i] = U[:, i]
+                continue
+            v = _gen_eig_larger(h11, h12, h22, s11, s12, s22)
+            Unew[:n, i] = v[0] * u + v[1] * du
+        U = _symmetrize_ukirr(Unew, ir, sym, n)
+    return U, lam
 
 
 # ---------------------------------------------------------------------------
@@ -622,10 +709,14 @@ class DisRecord:
     delta: float
 
 
-def dis_extract(Mw, Uo, win, km, num_wann, dc: DisControl):
+def dis_extract(Mw, Uo, win, km, num_wann, dc: DisControl, sitesym=None):
     """dis_extract (src/disentangle.F90:1893-2864): iterative minimisation of Omega_I
     with Z-matrix mixing; then the subspace Hamiltonian is diagonalised to fix U_opt's
-    gauge.  Returns (U_opt, Omega_I, records, converged)."""
+    gauge.  Returns (U_opt, Omega_I, records, converged).
+    ``sitesym``: the symmetry-adapted form (:2193-2207, :2214-2216, :2242-2247,
+    :2289-2298, :2404-2411, :2504-2513, :2675): symmetrised Z matrices, updates at the
+    irreducible k only (each weighted by its star in Omega_I(i-1)), symmetrised U_opt,
+    and no final gauge change."""
     K = Mw.shape[0]
     W = num_wann
     Uo = Uo.copy()
@@ -636,13 +727,20 @@ def dis_extract(Mw, Uo, win, km, num_wann, dc: DisControl):
     recs = []
     converged = False
     womegai = 0.0
+    sym = sitesym
+    if sym is not None and any(nf > 0):
+        raise RuntimeError("not implemented in symmetry-adapted mode")
     for it in range(1, dc.num_iter + 1):
         if it == 1:
             for k in range(K):
                 if W > nf[k]:
                     zin[k] = _zmatrix(Mw, Uo, win, km, k)
+            if sym is not None:
+                zin = sitesym_symmetrize_zmatrix(zin, sym, win["ndimwin"])
         else:
             for k in range(K):
+                if sym is not None and not sym.irreducible(k):
+                    continue
                 if W > nf[k]:
                     zin[k] = dc.mix_ratio * zout[k] + (1.0 - dc.mix_ratio) * zin[k]
                     zin[k] = np.triu(zin[k]) + np.triu(zin[k], 1).conj().T
@@ -650,6 +748,15 @@ def dis_extract(Mw, Uo, win, km, num_wann, dc: DisControl):
         Unew = Uo.copy()
         for k in range(K):
             wk = W * km["wbtot"]
+            if sym is not None:
+                if not sym.irreducible(k):
+                    continue
+                ir = sym.ik2ir[k]
+                wk = wk * sym.nsym / int(np.count_nonzero(sym.kptsym[:, ir] == k))
+                Unew[k], lam = sitesym_dis_extract_symmetry(sym, Uo[k], zin[k], k, win["ndimwin"][k], W)
+                wk -= float(np.trace(lam).real)
+                womegai1 += wk
+                continue
             if nf[k] > 0:
                 wk -= _omega_i_k(Mw, Uo, km, k, W, rows=nf[k])
             if W > nf[k]:
@@ -663,6 +770,8 @@ def dis_extract(Mw, Uo, win, km, num_wann, dc: DisControl):
                     m += 1
             womegai1 += wk
         Uo = Unew
+        if sym is not None:
+            Uo = sitesym_symmetrize_u_matrix(Uo, sym, ndimwin=win["ndimwin"])
         womegai1 /= K
         womegai = sum(W * km["wbtot"] - _omega_i_k(Mw, Uo, km, k, W) for k in range(K)) / K
         delta = womegai1 / womegai - 1.0
@@ -670,6 +779,8 @@ def dis_extract(Mw, Uo, win, km, num_wann, dc: DisControl):
         for k in range(K):
             if W > nf[k]:
                 zout[k] = _zmatrix(Mw, Uo, win, km, k)
+        if sym is not None:
+            zout = sitesym_symmetrize_zmatrix(zout, sym, win["ndimwin"])
         # internal_test_convergence (:2866-2920)
         if it <= dc.conv_window:
             history[it - 1] = delta
@@ -678,8 +789,8 @@ def dis_extract(Mw, Uo, win, km, num_wann, dc: DisControl):
         if it >= dc.conv_window and np.all(np.abs(history) < dc.conv_tol):
             converged = True
             break
-    # subspace Hamiltonian gauge (:2560-2640)
-    for k in range(K):
+    # subspace Hamiltonian gauge (:2560-2640); kept out in the symmetry-adapted mode (:2675)
+    for k in range(K if sym is None else 0):
         n = win["ndimwin"][k]
         ham = Uo[k, :n].conj().T @ (win["eigval_opt"][k, :n, None] * Uo[k, :n])
         w, cz = _heev(ham)
@@ -687,17 +798,23 @@ def dis_extract(Mw, Uo, win, km, num_wann, dc: DisControl):
     return Uo, womegai, recs, converged
 
 
-def dis_main(Mraw, A, eig, km, num_wann, dc: DisControl):
+def dis_main(Mraw, A, eig, km, num_wann, dc: DisControl, sitesym=None):
     """The disentanglement step of the library (w90_disentangle,
     src/library_interface.F90:362-420): dis_main plus setup_m_loc.  Mraw[k,b,nb,nb],
     A[k,nb,W], eig[k,nb].  Returns (U0[K,W,W], M0[K,B,W,W], U_opt[K,nb,W], Omega_I, records)
-    with M0 = U0^dag U_opt^dag M U_opt' U0' ready for wann_main."""
+    with M0 = U0^dag U_opt^dag M U_opt' U0' ready for wann_main.
+    ``sitesym``: the symmetry-adapted mode (src/disentangle.F90:151-157, :186-190, :237,
+    :627-629, :688-692)."""
     win = dis_windows(eig, num_wann, dc)
     Uo, Aw = dis_project(A, win, num_wann)
     if any(win["ndimfroz"] > 0):
+        if sitesym is not None:
+            raise RuntimeError("in symmetry-adapted mode, frozen window not implemented yet")
         Uo = dis_proj_froz(Uo, win, num_wann)
     Mw = slim_m(Mraw, win, km["nnlist"])
-    Uo, omi, recs, conv = dis_extract(Mw, Uo, win, km, num_wann, dc)
+    if sitesym is not None:
+        Uo = sitesym_symmetrize_u_matrix(Uo, sitesym, ndimwin=win["ndimwin"])
+    Uo, omi, recs, conv = dis_extract(Mw, Uo, win, km, num_wann, dc, sitesym=sitesym)
     K, B = Mraw.shape[:2]
     W = num_wann
     Mopt = np.empty((K, B, W, W), dtype=np.complex128)
@@ -705,13 +822,18 @@ def dis_main(Mraw, A, eig, km, num_wann, dc: DisControl):
         for b in range(B):
             Mopt[k, b] = Uo[k].conj().T @ Mw[k, b] @ Uo[km["nnlist"][k, b]]
     # internal_find_u (:531-698): U = Z V^dagger from the SVD of U_opt^dag A
-    U = np.empty((K, W, W), dtype=np.complex128)
+    U = np.zeros((K, W, W), dtype=np.complex128)
     for k in range(K):
+        if sitesym is not None and not sitesym.irreducible(k):
+            continue
         caa = Uo[k].conj().T @ Aw[k]
         z, sv, vh, info = lapack.zgesvd(caa, full_matrices=1, compute_uv=1)[:4]
         if info != 0:
             raise RuntimeError("dis_main: problem in ZGESVD 1")
         U[k] = z @ vh
+    if sitesym is not None:
+        # sitesym_replace_d_matrix_band: d_band <- D from here on
+        U = sitesym_symmetrize_u_matrix(U, sitesym, d_band=sitesym.d_wann)
     # setup_m_loc (:286-370)
     M0 = np.conj(U)[:, None].transpose(0, 1, 3, 2) @ Mopt @ U[km["nnlist"]]
     return U, M0, Uo, omi, recs

@@ -24,8 +24,9 @@ printed '<-- DIS' line.
 The selective-localisation case (testw90_example26: GaAs, slwf_num = 1 with a constrained
 centre) also stores the constrained centres and every '<-- SPRD' line (Omega_IOD, Omega_D).
 
-The site-symmetry case (testw90_example21_As_sp: GaAs sp3, site_symmetry = T) also stores
-the symmetry data of its .dmn file (k-point stars and the D matrices).
+The site-symmetry cases (testw90_example21_As_sp: GaAs sp3; testw90_disentanglement_sawfs:
+H3S, entangled) also store the symmetry data of their .dmn files (k-point stars and the D
+matrices).
 
 The guiding-centre case (testpostw90_gaas_shc: spinor GaAs, 16 isolated bands,
 guiding_centres = T) has no printed wannierise trajectory; its expected values are the
@@ -427,6 +428,42 @@ def build_sitesym(ref_root, out_dir):
     print("sitesym21", nb, nk, nntot, nsym, nkirr, conv.shape, om)
 
 
+def build_sitesym_dis(ref_root, out_dir):
+    """testw90_disentanglement_sawfs: H3S, 20 bands -> 12 WFs, 2x2x2 k (3 irreducible, 48
+    symmetries), outer window only, site_symmetry = T (symmetrize_eps = 1e-8), ten
+    disentanglement and ten wannierisation iterations."""
+    d = os.path.join(ref_root, "test-suite/tests/testw90_disentanglement_sawfs")
+    kw, real_lattice, kpts = parse_win(os.path.join(d, "H3S.win"))
+    W = int(kw["num_wann"])
+    nb, nk, nntot, heads, blocks = parse_mmn(os.path.join(d, "H3S.mmn"))
+    A = parse_amn(os.path.join(d, "H3S.amn"))
+    eig = parse_eig(os.path.join(d, "H3S.eig"), nb, nk)
+    dnb, nsym, nkirr, dnk, ik2ir, ir2ik, kptsym, dw, db = parse_dmn(os.path.join(d, "H3S.dmn"), W)
+    assert dnb == nb and dnk == nk
+    bench = os.path.join(d, "benchmark.out.default.inp=H3S.win")
+    conv, initial, final, om, bvec = parse_benchmark(bench)
+    dis, omi_final = parse_dis_lines(bench)
+    num = lambda k, default: float(kw.get(k, str(default)).replace("d", "e").replace("D", "e"))
+    knobs = dict(num_wann=W, num_bands=nb, num_iter=int(kw.get("num_iter", 100)),
+                 num_cg_steps=int(kw.get("num_cg_steps", 5)), conv_tol=num("conv_tol", 1e-10),
+                 conv_window=int(kw.get("conv_window", -1)), trial_step=num("trial_step", 2.0),
+                 search_shells=int(kw.get("search_shells", 36)), dis_num_iter=int(kw.get("dis_num_iter", 200)),
+                 dis_mix_ratio=num("dis_mix_ratio", 0.5), dis_conv_tol=num("dis_conv_tol", 1e-10),
+                 dis_conv_window=int(kw.get("dis_conv_window", 3)), dis_win_min=num("dis_win_min", -1e300),
+                 dis_win_max=num("dis_win_max", 1e300), dis_froz_min=num("dis_froz_min", -1e300),
+                 dis_froz_max=num("dis_froz_max", 1e300), frozen_states=int("dis_froz_max" in kw),
+                 symmetrize_eps=num("symmetrize_eps", 1e-3))
+    np.savez_compressed(
+        os.path.join(out_dir, "sitesym_dis.npz"),
+        real_lattice=real_lattice, kpt_latt=kpts, mp_grid=np.array([int(x) for x in kw["mp_grid"].split()[:3]]),
+        num_bands=nb, num_kpts=nk, nntot=nntot, mmn_heads=heads, mmn_blocks=blocks, amn=A, eig=eig,
+        knobs=np.array([knobs[k] for k in sorted(knobs)], dtype=np.float64), knob_names=np.array(sorted(knobs)),
+        ik2ir=ik2ir, ir2ik=ir2ik, kptsym=kptsym, d_matrix_wann=dw, d_matrix_band=db,
+        dis=dis, omega_i_final=np.array([omi_final]), conv=conv, centres_final=final,
+        omega_final=np.array([om["om_i"], om["om_d"], om["om_od"], om["om_tot"]]), bvec_table=bvec)
+    print("sitesym_dis", nb, nk, nntot, nsym, nkirr, dis.shape, omi_final, conv.shape, om)
+
+
 def build(ref_root, out_dir):
     for name, (sub, seed) in CASES.items():
         d = os.path.join(ref_root, sub)
@@ -464,3 +501,4 @@ if __name__ == "__main__":
     build_dis(root, os.path.dirname(os.path.abspath(__file__)))
     build_slwf(root, os.path.dirname(os.path.abspath(__file__)))
     build_sitesym(root, os.path.dirname(os.path.abspath(__file__)))
+    build_sitesym_dis(root, os.path.dirname(os.path.abspath(__file__)))

@@ -168,3 +168,33 @@ def test_oracle_site_symmetry_reproduces_reference():
     U0p, M0p = O.overlap_project(M, d["amn"], km["nnlist"])
     plain = O.wann_main(M0p, U0p, km, O.WannControl(**{**G.control(d).__dict__, "num_iter": 3}))
     assert abs(plain.iters[2].spread.om_tot - d["conv"][3][3]) > 1e-6
+
+
+def test_oracle_symmetry_adapted_disentanglement_reproduces_reference():
+    """testw90_disentanglement_sawfs (H3S, 20 bands -> 12 WFs, 8 k of which 3
+    irreducible, 48 symmetries, outer window only, site_symmetry = T): the symmetry-adapted
+    U_opt, the symmetrised Z matrices, the constrained extraction at the irreducible k
+    (sitesym_dis_extract_symmetry), the symmetric initial U, then the symmetric
+    wannierisation.  Every '<-- DIS' line (8 decimals) within 1e-8, the printed
+    '<-- CONV' spreads within 2e-10 A^2, the final Omega terms and centres."""
+    d = G.load("sitesym_dis")
+    kn = d["knobs"]
+    km = O.kmesh_get(d["real_lattice"], d["kpt_latt"], int(kn["search_shells"]))
+    np.testing.assert_allclose(km["wb"], d["bvec_table"][:, 3], atol=1e-6)
+    M = G.assemble_m(d, km["nnlist"], km["nncell"])
+    sym = G.sitesym(d)
+    U0, M0, Uo, omi, recs = O.dis_main(M, d["amn"], d["eig"], km, int(kn["num_wann"]), G.dis_control(d),
+                                       sitesym=sym)
+    assert len(recs) == len(d["dis"])
+    for r, (it, prev, cur, delta) in zip(recs, d["dis"]):
+        assert r.iter == int(it)
+        assert abs(r.omega_i_prev - prev) < 1e-8 and abs(r.omega_i - cur) < 1e-8, (r.iter, r, prev, cur)
+    assert abs(omi - d["omega_i_final"][0]) < 1e-8
+    r = O.wann_main(M0, U0, km, G.control(d), sitesym=sym)
+    rec = {0: r.initial}
+    rec.update({x.iter: x for x in r.iters})
+    for it, delta, rms, spread in d["conv"]:
+        assert abs(rec[int(it)].spread.om_tot - spread) < 2e-10, (int(it), rec[int(it)].spread.om_tot, spread)
+    sp = r.spread
+    np.testing.assert_allclose([sp.om_i, sp.om_d, sp.om_od, sp.om_tot], d["omega_final"], rtol=0, atol=1.01e-9)
+    np.testing.assert_allclose(r.centres.T, d["centres_final"][:, :3], rtol=0, atol=1.01e-6)
