@@ -854,12 +854,18 @@ int Engine::wannierise_profiled(int max_iters, double* ms, int* cnt, std::string
   const int iters = std::min(max_iters, max_iter_);
   for (int it = 0; it < iters && !rc; ++it) {
     if (guide_w_) rc |= timed(kPInit, [&] { k_phases<<<dim3(guide_w_, np), 256, 0, st>>>(dprobs_, 1); });
-    rc |= timed(kPGrad, [&] { k_grad<<<n_grad_, 256, 0, st>>>(dprobs_, wmg); });
+    rc |= timed(kPGrad, [&] {
+      k_grad<<<n_grad_, 256, 0, st>>>(dprobs_, wmg);
+      if (n_ir_) k_sym_grad<<<n_ir_, 256, 0, st>>>(dprobs_, WorkMap{d_offs_ir_, np});
+    });
     if (pc_tiles_) {
       rc |= timed(kPPrecond, [&] { k_precond<<<dim3(pc_tiles_, np), 256, 0, st>>>(dprobs_, 0); });
       rc |= timed(kPPrecond, [&] { k_precond<<<dim3(pc_tiles_, np), 256, 0, st>>>(dprobs_, 1); });
     }
-    rc |= timed(kPCtrlSearch, [&] { k_ctrl_search<<<np, 256, 0, st>>>(dprobs_); });
+    rc |= timed(kPCtrlSearch, [&] {
+      k_ctrl_search<<<np, 256, 0, st>>>(dprobs_);
+      if (n_ir_) k_sym_dir<<<n_ir_, 256, 0, st>>>(dprobs_, WorkMap{d_offs_ir_, np});
+    });
     rc |= timed(kPExpU, [&] { launch_exp(st, 0); });
     rc |= timed(kPMUpdate, [&] { launch_mupdate(st, 0); });
     rc |= timed(kPOmega, [&] { launch_omega(st, 0); });
