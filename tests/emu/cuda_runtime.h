@@ -20,12 +20,23 @@ struct uint3 { unsigned x, y, z; };
 struct dim3 { unsigned x, y, z; };
 inline double2 make_double2(double x, double y) { return double2{x, y}; }
 
+#ifdef EMU_FIBERS
+extern uint3 threadIdx;      // the threads of a CTA are fibers of one host thread
+#else
 extern thread_local uint3 threadIdx;
+#endif
 extern uint3 blockIdx;
 extern dim3 blockDim, gridDim;
 void emu_syncthreads();
 #define __syncthreads() emu_syncthreads()
 template <class T> inline T __ldg(const T* p) { return *p; }
+// CUDA's integer min / max overloads
+inline int min(int a, int b) { return a < b ? a : b; }
+inline int max(int a, int b) { return a > b ? a : b; }
+inline long long min(long long a, long long b) { return a < b ? a : b; }
+inline long long max(long long a, long long b) { return a > b ? a : b; }
+inline size_t min(size_t a, size_t b) { return a < b ? a : b; }
+inline size_t max(size_t a, size_t b) { return a > b ? a : b; }
 using std::fma;
 using std::sqrt;
 using std::fabs;

@@ -1,11 +1,14 @@
-"""The symmetry-adapted kernels (wannier90_gb300/csrc/k_sitesym.cu) executed on the CPU.
+"""The symmetry-adapted kernels (wannier90_gb300/csrc/k_sitesym.cu) and the FP64
+iteration (k_fp64.cu) executed on the CPU.
 
-tests/emu/ compiles the kernel source unchanged with g++ against a host stand-in for
-<cuda_runtime.h>: each CTA runs as 256 host threads with a barrier for __syncthreads
-(these kernels use block-level synchronisation only).  The results are compared with
-the oracle's restatement of src/sitesym.F90 on the reference's example21 symmetry data
-(GaAs, 64 k, 10 irreducible, 24 symmetries), together with the host tables the C ABI
-builds (sym_tables.cpp, compiled into the same harness).
+tests/emu/ compiles the kernel sources with g++ against a host stand-in for
+<cuda_runtime.h>: each CTA runs as 256 host threads (or fibers) with a barrier for
+__syncthreads -- these kernels use block-level synchronisation only.  k_sitesym.cu is
+compiled unchanged; k_fp64.cu gets two mechanical edits (dynamic shared memory, the
+%globaltimer read).  The results are compared with the oracle's restatement of
+src/sitesym.F90 and src/wannierise.F90 on the reference's example21 data (GaAs, 64 k, 10
+irreducible, 24 symmetries), together with the host tables the C ABI builds
+(sym_tables.cpp, compiled into the same harness).  The tensor-core kernels stay GPU-only.
 """
 import ctypes as C
 import os
@@ -157,3 +160,73 @@ def test_k_sym_u_reports_no_convergence(emu):
     status = np.full(nkirr, -7, dtype=np.int32)
     assert _call(emu, "emu_sym_u", d, 4, 64, 0.0, _ptr(ub.view(np.float64)), _ptr(status, C.c_int), 32, 0) == 0
     assert status[0] == 1
+
+
+# ---------------------------------------------------------------------------
+# the whole FP64 iteration with site symmetry (tests/emu/emu_iter.cpp)
+# ---------------------------------------------------------------------------
+@pytest.fixture(scope="module")
+def emu_iter(tmp_path_factory):
+    """k_fp64.cu + k_sitesym.cu under the fiber emulation.  The copy of k_fp64.cu gets the
+    two mechanical edits the host build needs: dynamic shared memory from emu_dyn_smem()
+    and the %globaltimer read as 0."""
+    import re
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("g++ not available")
+    tmp = tmp_path_factory.mktemp("emu_iter")
+    src = open(os.path.join(CSRC, "k_fp64.cu")).read()
+    src, n_smem = re.subn(r"extern __shared__ double2 smem\[\];", "double2* smem = emu_dyn_smem<double2>();", src)
+    src, n_timer = re.subn(r'asm volatile\("mov\.u64 %0, %%globaltimer;" : "=l"\((\w+)\)\);', r"\1 = 0;", src)
+    assert n_smem >= 1 and n_timer == 2
+    (tmp / "k_fp64_emu.cu").write_text(src)
+    out = str(tmp / "emu_iter.so")
+    subprocess.run([gxx, "-std=c++20", "-O1", "-shared", "-fPIC", "-D__CUDACC__", "-DEMU_FIBERS", "-I" + str(tmp),
+                    "-I" + os.path.join(HERE, "emu"), "-I" + CSRC, os.path.join(HERE, "emu", "emu_iter.cpp"),
+                    os.path.join(CSRC, "sym_tables.cpp"), "-o", out], check=True)
+    lib = C.CDLL(out)
+    ip, dp = C.POINTER(C.c_int), C.POINTER(C.c_double)
+    lib.emu_wann_main.argtypes = [C.c_int, C.c_int, C.c_int, ip, dp, dp, C.c_double, dp, dp, C.c_int, C.c_int,
+                                  C.c_int, C.c_double, C.c_double, C.c_int, C.c_int, ip, ip, ip, dp, dp, C.c_double,
+                                  dp, dp, ip]
+    lib.emu_wann_main.restype = C.c_int
+    return lib
+
+
+def test_emulated_iteration_with_site_symmetry(emu_iter):
+    """example21 through the engine's launch order on the emulated kernels: the Loewdin
+    projection with the symmetry-adapted U (k_lowdin, k_sym_u, k_m_update), the initial
+    spread, then four iterations (k_grad, k_sym_grad, k_ctrl_search, k_sym_dir, k_exp_u
+    reading the rotated directions, k_m_update, the spread passes, the controller).  Every
+    spread and RMS gradient against the oracle's symmetry-adapted run (1e-12) and the
+    reference's printed lines (2e-10 A^2)."""
+    d = G.load("sitesym21")
+    km = O.kmesh_get(d["real_lattice"], d["kpt_latt"], int(d["knobs"]["search_shells"]))
+    M = G.assemble_m(d, km["nnlist"], km["nncell"])
+    K, B, W, niter = len(d["kpt_latt"]), km["nntot"], 4, 4
+    nsym, nkirr, ik2ir, ir2ik, kpt, dw, db = _sym_args(d)
+    Mb = np.ascontiguousarray(M.transpose(0, 1, 3, 2)).astype(np.complex128)
+    Ab = np.ascontiguousarray(d["amn"].transpose(0, 2, 1)).astype(np.complex128)
+    nn = np.ascontiguousarray(km["nnlist"], dtype=np.int32)
+    bk = np.ascontiguousarray(km["bk"], dtype=np.float64)
+    wb = np.ascontiguousarray(km["wb"], dtype=np.float64)
+    log = np.zeros((niter + 1) * 10)
+    U = np.zeros(K * W * W, dtype=np.complex128)
+    status = np.zeros(2, dtype=np.int32)
+    rows = emu_iter.emu_wann_main(W, K, B, _ptr(nn, C.c_int), _ptr(bk), _ptr(wb), km["wbtot"],
+                                  _ptr(Mb.view(np.float64)), _ptr(Ab.view(np.float64)), niter, 5, -1, 1e-10, 2.0, nsym,
+                                  nkirr, _ptr(ik2ir, C.c_int), _ptr(ir2ik, C.c_int), _ptr(kpt, C.c_int),
+                                  _ptr(dw.view(np.float64)), _ptr(db.view(np.float64)),
+                                  float(d["knobs"]["symmetrize_eps"]), _ptr(log), _ptr(U.view(np.float64)),
+                                  _ptr(status, C.c_int))
+    assert rows == niter + 1 and status[0] == 0 and status[1] == 0
+    log = log.reshape(-1, 10)[:rows]
+    sym = G.sitesym(d)
+    U0, M0 = O.overlap_project(M, d["amn"], km["nnlist"], sitesym=sym)
+    r = O.wann_main(M0, U0, km, O.WannControl(num_iter=niter), sitesym=sym)
+    for row, x, printed in zip(log, [r.initial] + r.iters, d["conv"]):
+        assert int(row[0]) == x.iter == int(printed[0])
+        assert abs(row[3] - x.spread.om_tot) < 1e-12, (x.iter, row[3], x.spread.om_tot)
+        assert abs(row[2] - x.rms_grad) <= 1e-10 * max(1.0, x.rms_grad)
+        assert abs(row[3] - printed[3]) < 2e-10
+    np.testing.assert_allclose(_unblocks(U.reshape(K, W, W)), r.U, atol=1e-12)
