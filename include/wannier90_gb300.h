@@ -58,7 +58,7 @@ void cset_option_floatxy(void* handle, const char* keyword, const double* values
  * as floatxy tables: guiding_centres_frac (num_wann x 3, the projection sites) and
  * slwf_centres_frac (num_wann x 3, the constrained centres: the <slwf_centres> rows
  * over the projection sites; without it slwf_constrain uses guiding_centres_frac).
- * site_symmetry (+ symmetrize_eps) needs num_bands = num_wann and w90g_set_sitesym;
+ * site_symmetry (+ symmetrize_eps) needs w90g_set_sitesym;
  * gamma_only, conv_noise_amp > 0 and dis_spheres_num > 0 give ierr 5. */
 void cinput_setopt(void* handle, const char* seedname, int* ierr, int comm);
 
@@ -133,7 +133,8 @@ void w90g_get_dis_windows(void* handle, int* ndimwin, int* nfirstwin);
  * ierr: 6 when the counts or indices disagree with the handle (the reference's
  * "Number of bands / k-points is not correct" messages), 1 when the stars do not cover
  * the mesh.  With site_symmetry = T, cproject_overlap makes the initial U symmetry-
- * adapted and cwannierise symmetrises the gradient and rotations (isolated bands). */
+ * adapted, cdisentangle runs the symmetry-adapted disentanglement (outer window only, as
+ * in the reference) and cwannierise symmetrises the gradient and rotations. */
 int w90g_set_sitesym(void* handle, int nb, int nsym, int nkirr, int nk, const int* ik2ir, const int* ir2ik,
                      const int* kptsym, const double* d_wann, const double* d_band);
 /* (final Omega_I = omega%invariant, converged 0/1, iterations, most Jacobi sweeps of a

@@ -23,8 +23,11 @@ def dis_options(dc):
     return o
 
 
-def run_dis(real_lattice, kpoints, M_raw, A, eig, num_wann, dc, search_shells=36, wann_ctl=None, extra=None):
-    """M_raw[k,b,nb,nb], A[k,nb,W], eig[k,nb] (math layout) -> dict of results (math layout)."""
+def run_dis(real_lattice, kpoints, M_raw, A, eig, num_wann, dc, search_shells=36, wann_ctl=None, extra=None,
+            before=None):
+    """M_raw[k,b,nb,nb], A[k,nb,W], eig[k,nb] (math layout) -> dict of results (math layout).
+    before(handle): called after cinput_setopt (e.g. to pass the symmetry data); returns
+    an ierr that must be 0."""
     K, nb, W = A.shape
     opts = dict(iprint=0, search_shells=int(search_shells))
     opts.update(dis_options(dc))
@@ -37,6 +40,8 @@ def run_dis(real_lattice, kpoints, M_raw, A, eig, num_wann, dc, search_shells=36
             opts["trial_step"] = float(wann_ctl.trial_step)
     opts.update(extra or {})
     c = w90.setup(kpoints=kpoints, unit_cell_cart=real_lattice, num_wann=num_wann, num_bands=nb, **opts)
+    if before is not None:
+        assert before(c) == 0, c.last_error()
     m = np.array(synth.from_math_m(M_raw), order="F", copy=True)
     uopt = np.array(synth.from_math_u(A), order="F", copy=True)
     u = np.zeros((W, W, K), dtype=np.complex128, order="F")

@@ -159,7 +159,9 @@ def write_dmn(path, d):
 
 def dmn_dict(d):
     """The site-symmetry fixture as w90io.read_dmn returns a .dmn file (Fortran shapes)."""
-    return dict(num_bands=4, nsymmetry=24, nkptirr=10, num_kpts=64, ik2ir=d["ik2ir"].copy(),
+    nsym, nkirr = d["kptsym"].shape
+    return dict(num_bands=d["d_matrix_band"].shape[-1], nsymmetry=nsym, nkptirr=nkirr, num_kpts=len(d["ik2ir"]),
+                ik2ir=d["ik2ir"].copy(),
                 ir2ik=d["ir2ik"].copy(), kptsym=d["kptsym"].copy(),
                 d_matrix_wann=d["d_matrix_wann"].transpose(2, 3, 1, 0).copy(),
                 d_matrix_band=d["d_matrix_band"].transpose(2, 3, 1, 0).copy())

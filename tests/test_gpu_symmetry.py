@@ -121,3 +121,28 @@ def test_symmetry_adapted_cli(tmp_path, capfd):
         assert abs(conv[int(it)] - spread) < 2.6e-10, int(it)
     chk = w90io.read_chk(seed + ".chk")
     np.testing.assert_allclose(chk["centres"].T, d["centres_final"][:, :3], atol=1.01e-6)
+
+
+def test_symmetry_adapted_disentanglement_golden():
+    """testw90_disentanglement_sawfs through the C ABI: site_symmetry = T with the .dmn
+    data, cdisentangle (symmetry-adapted), then cwannierise.  Every '<-- DIS' line (8
+    decimals) within 1e-8, the final Omega_I, the printed '<-- CONV' spreads within
+    2e-10 A^2 and the final Omega terms."""
+    from tests.engine_dis import run_dis
+    d = G.load("sitesym_dis")
+    kn = d["knobs"]
+    km = O.kmesh_get(d["real_lattice"], d["kpt_latt"], int(kn["search_shells"]))
+    M = G.assemble_m(d, km["nnlist"], km["nncell"])
+    out = run_dis(d["real_lattice"], d["kpt_latt"], M, np.ascontiguousarray(d["amn"]), d["eig"], int(kn["num_wann"]),
+                  G.dis_control(d), int(kn["search_shells"]), wann_ctl=G.control(d),
+                  extra={"site_symmetry": True, "symmetrize_eps": float(kn["symmetrize_eps"])},
+                  before=lambda c: w90.w90_set_sitesym(c, G.dmn_dict(d)))
+    assert out["ierr"] == 0 and out["wann_ierr"] == 0, (out["err"], out.get("wann_err"))
+    for row, (it, prev, cur, delta) in zip(out["dis_log"], d["dis"]):
+        assert int(row[0]) == int(it)
+        assert abs(row[1] - prev) < 1e-8 and abs(row[2] - cur) < 1e-8, (int(it), row, prev, cur)
+    assert abs(out["dis_info"]["omega_invariant"] - d["omega_i_final"][0]) < 1e-8
+    by_iter = {int(r[0]): r for r in out["log"]}
+    for it, delta, rms, spread in d["conv"]:
+        assert abs(by_iter[int(it)][3] - spread) < 2e-10, (int(it), by_iter[int(it)][3], spread)
+    np.testing.assert_allclose(out["omega"], d["omega_final"], rtol=0, atol=2e-9)

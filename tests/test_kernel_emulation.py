@@ -230,3 +230,79 @@ def test_emulated_iteration_with_site_symmetry(emu_iter):
         assert abs(row[2] - x.rms_grad) <= 1e-10 * max(1.0, x.rms_grad)
         assert abs(row[3] - printed[3]) < 2e-10
     np.testing.assert_allclose(_unblocks(U.reshape(K, W, W)), r.U, atol=1e-12)
+
+
+# ---------------------------------------------------------------------------
+# the symmetry-adapted disentanglement (tests/emu/emu_dis.cpp)
+# ---------------------------------------------------------------------------
+@pytest.fixture(scope="module")
+def emu_dis(tmp_path_factory):
+    """The kernel part of dis.cu (everything before dis_run) under the fiber emulation; the
+    copy reads its dynamic shared memory from emu_dyn_smem()."""
+    import re
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("g++ not available")
+    tmp = tmp_path_factory.mktemp("emu_dis")
+    src = open(os.path.join(CSRC, "dis.cu")).read()
+    src = src[:src.index("int dis_run(")] + "}  // namespace w90g\n"
+    src, n_smem = re.subn(r"extern __shared__ double2 (\w+)\[\];", r"double2* \1 = emu_dyn_smem<double2>();", src)
+    assert n_smem == 2
+    (tmp / "dis_emu.cu").write_text(src)
+    out = str(tmp / "emu_dis.so")
+    subprocess.run([gxx, "-std=c++20", "-O1", "-shared", "-fPIC", "-D__CUDACC__", "-DEMU_FIBERS", "-I" + str(tmp),
+                    "-I" + os.path.join(HERE, "emu"), "-I" + CSRC, os.path.join(HERE, "emu", "emu_dis.cpp"),
+                    os.path.join(CSRC, "sym_tables.cpp"), "-o", out], check=True)
+    lib = C.CDLL(out)
+    ip, dp = C.POINTER(C.c_int), C.POINTER(C.c_double)
+    lib.emu_dis_sym.argtypes = ([C.c_int] * 4 + [ip, dp, C.c_double, dp, dp, dp, C.c_int, C.c_double, C.c_double,
+                                C.c_int, C.c_double, C.c_double, C.c_int, C.c_int, ip, ip, ip, dp, dp, C.c_double,
+                                C.c_int, dp, dp, dp, dp, ip])
+    lib.emu_dis_sym.restype = C.c_int
+    return lib
+
+
+def test_emulated_symmetry_adapted_disentanglement(emu_dis):
+    """testw90_disentanglement_sawfs (H3S, 20 -> 12, 3 irreducible of 8 k, 48 symmetries)
+    through dis_run's symmetry-adapted launch order on the emulated kernels (k_dis_project,
+    k_dis_sym_u, k_dis_z, k_dis_sym_z, k_dis_sym_step, k_dis_findu, k_dis_rotate): the
+    first two iterations' Omega_I(i-1), Omega_I(i) against the oracle (1e-10) and the
+    printed lines (1e-8), U_opt U0 and M0 against the oracle (1e-9; U_opt and U0 alone
+    are fixed only up to a rotation that cancels there).  32 emulated threads per CTA:
+    the kernels take any power-of-two block size, and the nested fixed points of the
+    constrained extraction take minutes at 256."""
+    d = G.load("sitesym_dis")
+    kn = d["knobs"]
+    km = O.kmesh_get(d["real_lattice"], d["kpt_latt"], int(kn["search_shells"]))
+    M = G.assemble_m(d, km["nnlist"], km["nncell"])
+    nb, W, K, B = int(d["num_bands"]), int(kn["num_wann"]), len(d["kpt_latt"]), km["nntot"]
+    dc = G.dis_control(d)
+    dc.num_iter = 2
+    nsym, nkirr, ik2ir, ir2ik, kpt, dw, db = _sym_args(d)
+    Mf = np.ascontiguousarray(M.transpose(0, 1, 3, 2)).astype(np.complex128)
+    Af = np.ascontiguousarray(d["amn"].transpose(0, 2, 1)).astype(np.complex128)
+    eig = np.ascontiguousarray(d["eig"])
+    nn = np.ascontiguousarray(km["nnlist"], dtype=np.int32)
+    wb = np.ascontiguousarray(km["wb"])
+    log = np.zeros(3 * dc.num_iter)
+    U0 = np.zeros(K * W * W, dtype=np.complex128)
+    M0 = np.zeros(K * B * W * W, dtype=np.complex128)
+    Uo = np.zeros(K * nb * W, dtype=np.complex128)
+    status = np.zeros(1, dtype=np.int32)
+    rows = emu_dis.emu_dis_sym(nb, W, K, B, _ptr(nn, C.c_int), _ptr(wb), km["wbtot"], _ptr(eig),
+                               _ptr(Mf.view(np.float64)), _ptr(Af.view(np.float64)), dc.num_iter, dc.mix_ratio,
+                               dc.conv_tol, dc.conv_window, dc.win_min, dc.win_max, nsym, nkirr, _ptr(ik2ir, C.c_int),
+                               _ptr(ir2ik, C.c_int), _ptr(kpt, C.c_int), _ptr(dw.view(np.float64)),
+                               _ptr(db.view(np.float64)), float(kn["symmetrize_eps"]), 32, _ptr(log),
+                               _ptr(U0.view(np.float64)), _ptr(M0.view(np.float64)), _ptr(Uo.view(np.float64)),
+                               _ptr(status, C.c_int))
+    assert rows == 2 and status[0] == 0
+    U0o, M0o, Uoo, omi, recs = O.dis_main(M, d["amn"], d["eig"], km, W, dc, sitesym=G.sitesym(d))
+    for row, r, printed in zip(log.reshape(-1, 3), recs, d["dis"]):
+        assert abs(row[1] - r.omega_i_prev) < 1e-10 and abs(row[2] - r.omega_i) < 1e-10
+        assert abs(row[1] - printed[1]) < 1e-8 and abs(row[2] - printed[2]) < 1e-8
+    U0e = U0.reshape(K, W, W).transpose(0, 2, 1)
+    Uoe = Uo.reshape(K, W, nb).transpose(0, 2, 1)
+    for k in range(K):
+        np.testing.assert_allclose(Uoe[k] @ U0e[k], Uoo[k] @ U0o[k], atol=1e-9)
+    np.testing.assert_allclose(M0.reshape(K, B, W, W).transpose(0, 1, 3, 2), M0o, atol=1e-9)

@@ -75,10 +75,13 @@ def test_set_sitesym_errors(mutate, code, msg):
     assert msg in c.last_error()
 
 
-def test_site_symmetry_needs_isolated_bands_and_its_data():
+def test_site_symmetry_needs_its_data():
     d = G.load("sitesym21")
+    # entangled bands are accepted; the data must then carry num_bands bands
     c, ierr = _handle(d, site_symmetry=True, num_bands=6)
-    assert ierr == 5 and "site_symmetry" in c.last_error()
+    assert ierr == 0, c.last_error()
+    assert w90.w90_set_sitesym(c, G.dmn_dict(d)) == 6
+    assert "Number of bands is not correct" in c.last_error()
     # site_symmetry = T without w90g_set_sitesym: the projection stops before the device
     c, ierr = _handle(d, site_symmetry=True)
     assert ierr == 0

@@ -78,7 +78,7 @@ struct Handle {
   int site_symmetry = 0;
   double symmetrize_eps = 1.0e-3;
   bool have_sym = false;
-  int sym_nir = 0, sym_nk = 0, sym_nb = 0;
+  int sym_nir = 0, sym_nk = 0, sym_nb = 0, sym_nsym = 0;
   std::vector<int> sym_ik, sym_moff, sym_mem, sym_goff, sym_grp;
   std::vector<double> sym_d, sym_db;
   // caller data
@@ -294,7 +294,7 @@ int build_spec(Handle* h, ProblemSpec& s) {
   s.slwf_num = h->slwf_num;
   s.slwf_lambda = h->slwf_lambda;
   s.slwf_c = h->slwf_c;
-  if (h->site_symmetry && h->have_sym && h->sym_nk == h->num_kpts && h->sym_nb == h->num_wann) {
+  if (h->site_symmetry && h->have_sym && h->sym_nk == h->num_kpts && h->sym_nb == h->num_bands) {
     s.sym_nir = h->sym_nir;
     s.sym_eps = h->symmetrize_eps;
     s.sym_ik = h->sym_ik;
@@ -303,7 +303,9 @@ int build_spec(Handle* h, ProblemSpec& s) {
     s.sym_goff = h->sym_goff;
     s.sym_grp = h->sym_grp;
     s.sym_d = h->sym_d;
-    s.sym_db = h->sym_db;
+    // after a disentanglement d(R,k) is replaced by D(R,k) (sitesym_replace_d_matrix_band,
+    // src/disentangle.F90:237); with isolated bands the two have the same size
+    s.sym_db = h->num_bands == h->num_wann ? h->sym_db : h->sym_d;
   }
   s.precond = h->precond;
   s.nrpts = h->nrpts;
@@ -326,7 +328,7 @@ Engine* engine(Handle* h) {
 
 // site_symmetry = T without its data: the reference stops reading the .dmn file
 bool sym_missing(Handle* h) {
-  return h->site_symmetry && !(h->have_sym && h->sym_nk == h->num_kpts && h->sym_nb == h->num_wann);
+  return h->site_symmetry && !(h->have_sym && h->sym_nk == h->num_kpts && h->sym_nb == h->num_bands);
 }
 const char* kSymMissing = "site_symmetry = T needs the symmetry data of the .dmn file (w90g_set_sitesym)";
 
@@ -401,6 +403,7 @@ int do_disentangle(Handle* h, double* m, double* uopt, double* u, const double* 
   if (!u) return fail(h, 1, "u_matrix not associated for disentangle call");
   if (!uopt) return fail(h, 1, "u_opt not associated for disentangle call");
   if (!eig) return fail(h, 1, "eigval not associated for disentangle call");
+  if (sym_missing(h)) return fail(h, 6, kSymMissing);
   const int W = h->num_wann;
   w90g::DisSpec ds;
   ds.nb = h->num_bands;
@@ -421,6 +424,18 @@ int do_disentangle(Handle* h, double* m, double* uopt, double* u, const double* 
   ds.ctl = h->dis_ctl;
   ds.prof_ms = prof_ms;
   ds.prof_counts = prof_counts;
+  if (h->site_symmetry) {
+    ds.sym_nir = h->sym_nir;
+    ds.sym_nsym = h->sym_nsym;
+    ds.sym_eps = h->symmetrize_eps;
+    ds.sym_ik = h->sym_ik;
+    ds.sym_moff = h->sym_moff;
+    ds.sym_mem = h->sym_mem;
+    ds.sym_goff = h->sym_goff;
+    ds.sym_grp = h->sym_grp;
+    ds.sym_d = h->sym_d;
+    ds.sym_db = h->sym_db;
+  }
   w90g::DisResult r;
   std::string err;
   const int rc = w90g::dis_run(ds, r, err);
@@ -790,10 +805,6 @@ void cinput_setopt(void* hv, const char* seedname, int* ierr, int comm) {
   // isolated bands (the disentanglement's symmetrised Z matrices are not built)
   h->site_symmetry = get_num(h, "site_symmetry", v) ? (v != 0.0) : 0;
   h->symmetrize_eps = get_num(h, "symmetrize_eps", v) ? v : 1.0e-3;
-  if (h->site_symmetry && h->num_bands != h->num_wann) {
-    *ierr = fail(h, 5, "Option 'site_symmetry' with num_bands > num_wann is not supported by the GPU engine");
-    return;
-  }
   // selective localisation and constrained centres
   // (src/wannier90_readwrite.F90:757-802, :1660-1708; src/readwrite.F90:3266-3357)
   {
@@ -1061,6 +1072,7 @@ int w90g_set_sitesym(void* hv, int nb, int nsym, int nkirr, int nk, const int* i
   if (int rc = w90g::build_sym_tables(h->num_wann, nb, nsym, nkirr, nk, ik2ir, ir2ik, kptsym, d_wann, d_band, t, msg))
     return fail(h, rc, msg);
   h->sym_nir = t.nir;
+  h->sym_nsym = t.nsym;
   h->sym_nk = nk;
   h->sym_nb = nb;
   h->sym_ik = t.ik;

@@ -61,7 +61,24 @@ struct DisDev {
   int* status;           // [k]
   double2* Vz;           // [k] m x m eigenvectors of the last Z (warm start of the next)
   int* max_sweeps;       // Jacobi sweeps, max over k and iterations
+  // symmetry-adapted mode (sym_nir > 0 irreducible k): the star / little-group tables of
+  // the wannierisation (Problem::sym_*), the band representation d(R,k) as nb x nb slots
+  // (sym_db) and the Wannier one D(R,k) as W x W slots (sym_d); sym_ws kDisSymWs nb x nb
+  // matrices per irreducible k; sym_status per irreducible k
+  int sym_nir, sym_nsym;
+  double sym_eps;
+  const int* sym_ik;
+  const int* sym_moff;
+  const int* sym_mem;
+  const int* sym_goff;
+  const int* sym_grp;
+  const double2* sym_d;
+  const double2* sym_db;
+  double2* sym_ws;
+  int* sym_status;
 };
+
+constexpr int kDisSymWs = 16;
 
 __device__ __forceinline__ double2 op_el(const double2* X, int ld, bool c, int i, int j) {
   // element (i, j) of X (c = false) or of X^H (c = true)
@@ -465,11 +482,328 @@ __global__ void __launch_bounds__(256) k_dis_rotate(DisDev D, int cur) {
   cta_zgemm(D.M0 + (size_t)kb * W * W, W, T3, W, false, D.U0 + (size_t)k2 * W * W, W, false, W, W, W);
 }
 
+// ---- symmetry-adapted mode (src/sitesym.F90, src/disentangle.F90:151-157, :186-190,
+// :2193-2298, :2404-2411, :2504-2513, :627-629, :688-692).  One CTA per irreducible k.
+
+// symmetrize_ukirr (src/sitesym.F90:392-497) on U (n rows used, leading dimension ld, W
+// columns) at irreducible ir: the little group's average of d^+ U D, made unitary by
+// orthogonalize_u's polar factor, until sum |ngk I - sum U^+ d^+ U D| < sym_eps (100
+// passes).  d: band-representation slots with leading dimension ldd (their top-left
+// n x n is used).  ws: 8 scratch matrices of ld x W (ld >= W).  Returns 0, 1 (not
+// converged) or 2 (polar factor failed).
+__device__ int dis_sym_ukirr(const DisDev& D, int ir, double2* U, int ld, int n, const double2* dslots, int ldd,
+                             double2* ws, DisShared& sh) {
+  const int W = D.W;
+  const size_t L = (size_t)ld * W, WW = (size_t)W * W, DD = (size_t)ldd * ldd;
+  double2 *Us = ws, *A = ws + L, *Bm = ws + 2 * L, *C2 = ws + 3 * L, *S = ws + 4 * L, *V = ws + 5 * L,
+          *T = ws + 6 * L, *Y = ws + 7 * L;
+  const int g0 = D.sym_goff[ir], g1 = D.sym_goff[ir + 1];
+  const int ngk = g1 - g0;
+  __syncthreads();
+  if (ngk == 1) {
+    cta_polar(U, ld, U, ld, n, W, S, V, T, Y, sh.js(), &sh.flag);
+    return sh.flag ? 2 : 0;
+  }
+  for (int it = 1; it <= 100; ++it) {
+    for (int e = threadIdx.x; e < (int)L; e += blockDim.x) Us[e] = cmk(0, 0);
+    for (int e = threadIdx.x; e < (int)WW; e += blockDim.x) C2[e] = cmk((e % W) == (e / W) ? (double)ngk : 0.0, 0.0);
+    for (int g = g0; g < g1; ++g) {
+      const int slot = D.sym_grp[2 * g + 1];
+      const double2* Dm = D.sym_d + (size_t)slot * WW;
+      const double2* dm = dslots + (size_t)slot * DD;
+      __syncthreads();
+      cta_zgemm(A, ld, U, ld, false, Dm, W, false, n, W, W);        // cmat_sub = U D
+      __syncthreads();
+      cta_zgemm(Bm, ld, dm, ldd, true, A, ld, false, n, W, n);      // cmat = d^+ cmat_sub
+      __syncthreads();
+      for (int e = threadIdx.x; e < n * W; e += blockDim.x) {
+        const int i = e % n, j = e / n;
+        Us[(size_t)j * ld + i] = cadd(Us[(size_t)j * ld + i], Bm[(size_t)j * ld + i]);
+      }
+      for (int e = threadIdx.x; e < (int)WW; e += blockDim.x) {
+        const int i = e % W, j = e / W;
+        double2 acc = cmk(0, 0);
+        for (int l = 0; l < n; ++l) cfmac(acc, U[(size_t)i * ld + l], Bm[(size_t)j * ld + l]);   // (U^+ cmat)_ij
+        C2[e] = csub(C2[e], acc);
+      }
+    }
+    __syncthreads();
+    double diff = 0.0;
+    for (int e = threadIdx.x; e < (int)WW; e += blockDim.x) diff += sqrt(cabs2(C2[e]));
+    diff = block_sum(diff, sh.red);
+    if (diff < D.sym_eps) return 0;
+    if (it == 100) return 1;
+    const double inv = 1.0 / (double)ngk;
+    for (int e = threadIdx.x; e < n * W; e += blockDim.x) {
+      const int i = e % n, j = e / n;
+      Us[(size_t)j * ld + i] = cscale(Us[(size_t)j * ld + i], inv);
+    }
+    __syncthreads();
+    cta_polar(U, ld, Us, ld, n, W, S, V, T, Y, sh.js(), &sh.flag);
+    if (sh.flag) return 2;
+  }
+  return 1;
+}
+
+// sitesym_symmetrize_u_matrix (src/sitesym.F90:104-192).  mode 0: U_opt in U[buf]
+// (window rows n = ndim(k_ir), d = the band slots); mode 1: the initial U (W x W, d = D
+// after sitesym_replace_d_matrix_band).  Then U(R k) = d U(k_ir) D^+ over the star.
+__global__ void __launch_bounds__(256) k_dis_sym_u(DisDev D, int buf, int mode) {
+  __shared__ DisShared sh;
+  const int ir = blockIdx.x;
+  const int nb = D.nb, W = D.W;
+  const int ik = D.sym_ik[ir];
+  const size_t NN = (size_t)nb * nb, WW = (size_t)W * W;
+  double2* ws = D.sym_ws + (size_t)ir * kDisSymWs * NN;
+  const int ld = mode ? W : nb;
+  const int n = mode ? W : D.ndim[ik];
+  const double2* dslots = mode ? D.sym_d : D.sym_db;
+  const int ldd = mode ? W : nb;
+  double2* base = mode ? D.U0 : D.U[buf];
+  const size_t blk = mode ? WW : (size_t)nb * W;
+  double2* U = base + (size_t)ik * blk;
+  const int status = dis_sym_ukirr(D, ir, U, ld, n, dslots, ldd, ws, sh);
+  __syncthreads();
+  double2* A = ws + 8 * NN;
+  for (int m = D.sym_moff[ir]; m < D.sym_moff[ir + 1]; ++m) {
+    const int slot = D.sym_mem[2 * m + 1];
+    const double2* Dm = D.sym_d + (size_t)slot * WW;
+    const double2* dm = dslots + (size_t)slot * ldd * ldd;
+    double2* Um = base + (size_t)D.sym_mem[2 * m] * blk;
+    cta_zgemm(A, ld, dm, ldd, false, U, ld, false, n, W, n);        // d U
+    __syncthreads();
+    cta_zgemm(Um, ld, A, ld, false, Dm, W, true, n, W, W);          // ... D^+
+    __syncthreads();
+  }
+  if (threadIdx.x == 0 && status) D.sym_status[ir] = status + 10 * mode;
+}
+
+// sitesym_symmetrize_zmatrix (src/sitesym.F90:331-391) on Zin (which = 0) or Zout: at each
+// irreducible k, Z += d^+ Z(Rk) d over the star's first occurrences, then the little
+// group's d^+ Z d of that sum, divided by the group's order (window block nd x nd).
+__global__ void __launch_bounds__(256) k_dis_sym_z(DisDev D, int which) {
+  const int ir = blockIdx.x;
+  const int nb = D.nb;
+  const int ik = D.sym_ik[ir];
+  const int nd = D.ndim[ik];
+  const size_t NN = (size_t)nb * nb;
+  double2* Zb = which ? D.Zout : D.Zin;
+  double2* Z = Zb + (size_t)ik * NN;
+  double2* ws = D.sym_ws + (size_t)ir * kDisSymWs * NN;
+  double2 *C1 = ws, *C2 = ws + NN, *Tmp = ws + 2 * NN;
+  for (int m = D.sym_moff[ir]; m < D.sym_moff[ir + 1]; ++m) {
+    const double2* dm = D.sym_db + (size_t)D.sym_mem[2 * m + 1] * NN;
+    const double2* Zm = Zb + (size_t)D.sym_mem[2 * m] * NN;
+    __syncthreads();
+    cta_zgemm(C1, nb, Zm, nb, false, dm, nb, false, nd, nd, nd);    // cmat1 = Z(Rk) d
+    __syncthreads();
+    cta_zgemm(C2, nb, dm, nb, true, C1, nb, false, nd, nd, nd);     // cmat2 = d^+ cmat1
+    __syncthreads();
+    for (int e = threadIdx.x; e < nd * nd; e += blockDim.x) {
+      const size_t o = (size_t)(e / nd) * nb + e % nd;
+      Z[o] = cadd(Z[o], C2[o]);
+    }
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < nd * nd; e += blockDim.x) {
+    const size_t o = (size_t)(e / nd) * nb + e % nd;
+    Tmp[o] = Z[o];
+  }
+  const int g0 = D.sym_goff[ir], g1 = D.sym_goff[ir + 1];
+  for (int g = g0; g < g1; ++g) {
+    if (D.sym_grp[2 * g] == 0) continue;    // isym = 1 is not part of this sum
+    const double2* dm = D.sym_db + (size_t)D.sym_grp[2 * g + 1] * NN;
+    __syncthreads();
+    cta_zgemm(C1, nb, Tmp, nb, false, dm, nb, false, nd, nd, nd);
+    __syncthreads();
+    cta_zgemm(C2, nb, dm, nb, true, C1, nb, false, nd, nd, nd);
+    __syncthreads();
+    for (int e = threadIdx.x; e < nd * nd; e += blockDim.x) {
+      const size_t o = (size_t)(e / nd) * nb + e % nd;
+      Z[o] = cadd(Z[o], C2[o]);
+    }
+  }
+  __syncthreads();
+  const double inv = 1.0 / (double)(g1 - g0);
+  for (int e = threadIdx.x; e < nd * nd; e += blockDim.x) {
+    const size_t o = (size_t)(e / nd) * nb + e % nd;
+    Z[o] = cscale(Z[o], inv);
+  }
+}
+
+// The eigenvector of the larger eigenvalue of H v = w S v (2 x 2 Hermitian, S positive
+// definite, both packed as (11, 12, 22)), S-normalised, with a real non-negative second
+// component -- the phase ZHPGVX returns (zhptrd's reflector leaves the last coordinate
+// alone).  Through the Cholesky factor S = L L^+.
+__device__ void gen_eig2_larger(double h11, double2 h12, double h22, double s11, double2 s12, double s22,
+                                double2* v) {
+  // S = L L^+, L = [l11 0; l21 l22];  L^{-1} = [1/l11 0; i10 1/l22]
+  const double l11 = sqrt(s11);
+  const double2 l21 = cscale(cconj(s12), 1.0 / l11);
+  const double l22 = sqrt(fmax(s22 - cabs2(l21), 1e-300));
+  const double2 i10 = cscale(l21, -1.0 / (l11 * l22));
+  // C = L^{-1} H L^{-+}: first M1 = L^{-1} H, then C = M1 L^{-+}, L^{-+} = [1/l11 conj(i10); 0 1/l22]
+  const double2 m10 = cadd(cscale(i10, h11), cscale(cconj(h12), 1.0 / l22));
+  const double2 m11 = cadd(cmul(i10, h12), cmk(h22 / l22, 0.0));
+  const double c00 = h11 / s11;
+  const double2 c10 = cscale(m10, 1.0 / l11);
+  const double c11 = cadd(cmul(m10, cconj(i10)), cscale(m11, 1.0 / l22)).x;
+  // the larger eigenvalue of [c00 conj(c10); c10 c11] and its eigenvector
+  const double hm = 0.5 * (c00 - c11);
+  const double lam = 0.5 * (c00 + c11) + sqrt(hm * hm + cabs2(c10));
+  double2 y0, y1;
+  if (cabs2(c10) > 0.0) {
+    y0 = cconj(c10);                 // (C - lam) y = 0 from the first row
+    y1 = cmk(lam - c00, 0.0);
+  } else {
+    y0 = cmk(c00 >= c11 ? 1.0 : 0.0, 0.0);
+    y1 = cmk(c00 >= c11 ? 0.0 : 1.0, 0.0);
+  }
+  const double ny = sqrt(cabs2(y0) + cabs2(y1));
+  y0 = cscale(y0, 1.0 / ny);
+  y1 = cscale(y1, 1.0 / ny);
+  // v = L^{-+} y
+  const double2 v0 = cadd(cscale(y0, 1.0 / l11), cmul(cconj(i10), y1));
+  const double2 v1 = cscale(y1, 1.0 / l22);
+  // phase: second component real, >= 0
+  const double a = sqrt(cabs2(v1));
+  if (a > 0.0) {
+    const double2 ph = cscale(cconj(v1), 1.0 / a);
+    v[0] = cmul(v0, ph);
+    v[1] = cmk(a, 0.0);
+  } else {
+    v[0] = v0;
+    v[1] = v1;
+  }
+}
+
+// dis_extract's refinement at an irreducible k (:2289-2298, sitesym_dis_extract_symmetry
+// src/sitesym.F90:550-695): Z mixing (:2209-2228), then up to 50 passes of ZU = Z U,
+// lambda = U^+ Z U, dU = ZU - U lambda (done when sum |dU| < 1e-10), each column moved to
+// the larger solution of the 2 x 2 problem in span(u_i, dU_i), symmetrize_ukirr.
+// Omega_I(i-1) part: W wbtot nsym / ngk - Re tr lambda.  The star's reducible k keep
+// their U_opt (symmetrised afterwards) and add nothing.
+__global__ void __launch_bounds__(256) k_dis_sym_step(DisDev D, int cur, int it) {
+  __shared__ DisShared sh;
+  __shared__ double s_h[8];
+  __shared__ double2 s_v[2];
+  __shared__ double s_red8[8][256];
+  const int ir = blockIdx.x;
+  const int nb = D.nb, W = D.W;
+  const int k = D.sym_ik[ir];
+  const int n = D.ndim[k];
+  const size_t NN = (size_t)nb * nb, L = (size_t)nb * W;
+  double2* Zi = D.Zin + (size_t)k * NN;
+  const double2* Zo = D.Zout + (size_t)k * NN;
+  double2* ws = D.sym_ws + (size_t)ir * kDisSymWs * NN;
+  double2 *U = ws, *ZU = ws + NN, *dU = ws + 2 * NN, *lam = ws + 3 * NN, *Un = ws + 4 * NN, *Zh = ws + 5 * NN,
+          *Zd = ws + 6 * NN;
+  double2* uws = ws + 7 * NN;   // 8 blocks for dis_sym_ukirr
+  // the star's reducible k: U_opt carried over, no Omega_I(i-1) part
+  for (int m = D.sym_moff[ir]; m < D.sym_moff[ir + 1]; ++m) {
+    const int km = D.sym_mem[2 * m];
+    const double2* src = D.U[cur] + (size_t)km * L;
+    double2* dst = D.U[cur ^ 1] + (size_t)km * L;
+    for (int e = threadIdx.x; e < (int)L; e += blockDim.x) dst[e] = src[e];
+    if (threadIdx.x == 0) D.wk1[km] = 0.0;
+  }
+  if (it > 1) {
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+      const int p = e % n, q = e / n;
+      if (p <= q) {
+        const size_t o = (size_t)q * nb + p;
+        Zi[o] = cadd(cscale(Zo[o], D.mix), cscale(Zi[o], 1.0 - D.mix));
+      }
+    }
+    __syncthreads();
+  }
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    const int p = e % n, q = e / n;
+    Zh[(size_t)q * nb + p] = (p <= q) ? Zi[(size_t)q * nb + p] : cconj(Zi[(size_t)p * nb + q]);
+  }
+  const double2* Uo = D.U[cur] + (size_t)k * L;
+  for (int e = threadIdx.x; e < (int)L; e += blockDim.x) U[e] = Uo[e];
+  int status = 0;
+  for (int pass = 0; pass < 50; ++pass) {
+    __syncthreads();
+    cta_zgemm(ZU, nb, Zh, nb, false, U, nb, false, n, W, n);        // Z U
+    __syncthreads();
+    cta_zgemm(lam, W, U, nb, true, ZU, nb, false, W, W, n);         // lambda = U^+ Z U
+    __syncthreads();
+    cta_zgemm(dU, nb, U, nb, false, lam, W, false, n, W, W);        // U lambda
+    __syncthreads();
+    double sa = 0.0;
+    for (int e = threadIdx.x; e < n * W; e += blockDim.x) {
+      const size_t o = (size_t)(e / n) * nb + e % n;
+      dU[o] = csub(ZU[o], dU[o]);
+      sa += sqrt(cabs2(dU[o]));
+    }
+    sa = block_sum(sa, sh.red);
+    if (sa < 1e-10) break;
+    for (int i = 0; i < W; ++i) {
+      const double2 *u = U + (size_t)i * nb, *zu = ZU + (size_t)i * nb, *du = dU + (size_t)i * nb;
+      for (int p = threadIdx.x; p < n; p += blockDim.x) {
+        double2 acc = cmk(0, 0);
+        for (int q = 0; q < n; ++q) cfma(acc, Zh[(size_t)q * nb + p], du[q]);
+        Zd[p] = acc;
+      }
+      __syncthreads();
+      // h11 = Re u^+ zu, h12 = zu^+ du, h22 = Re du^+ Z du, s11 = u^+ u, s12 = u^+ du, s22 = du^+ du
+      double t[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+      for (int p = threadIdx.x; p < n; p += blockDim.x) {
+        t[0] += u[p].x * zu[p].x + u[p].y * zu[p].y;
+        t[1] += zu[p].x * du[p].x + zu[p].y * du[p].y;
+        t[2] += zu[p].x * du[p].y - zu[p].y * du[p].x;
+        t[3] += du[p].x * Zd[p].x + du[p].y * Zd[p].y;
+        t[4] += cabs2(u[p]);
+        t[5] += u[p].x * du[p].x + u[p].y * du[p].y;
+        t[6] += u[p].x * du[p].y - u[p].y * du[p].x;
+        t[7] += cabs2(du[p]);
+      }
+      // the eight sums in one tree (blockDim is a power of two <= 256)
+      for (int c = 0; c < 8; ++c) s_red8[c][threadIdx.x] = t[c];
+      __syncthreads();
+      for (int h = blockDim.x >> 1; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h)
+          for (int c = 0; c < 8; ++c) s_red8[c][threadIdx.x] += s_red8[c][threadIdx.x + h];
+        __syncthreads();
+      }
+      if (threadIdx.x < 8) s_h[threadIdx.x] = s_red8[threadIdx.x][0];
+      __syncthreads();
+      const bool keep = fabs(s_h[7]) < 1e-10;
+      if (threadIdx.x == 0 && !keep)
+        gen_eig2_larger(s_h[0], cmk(s_h[1], s_h[2]), s_h[3], s_h[4], cmk(s_h[5], s_h[6]), s_h[7], s_v);
+      __syncthreads();
+      double2* un = Un + (size_t)i * nb;
+      for (int p = threadIdx.x; p < nb; p += blockDim.x) {
+        if (keep) un[p] = u[p];
+        else un[p] = (p < n) ? cadd(cmul(s_v[0], u[p]), cmul(s_v[1], du[p])) : cmk(0, 0);
+      }
+      __syncthreads();
+    }
+    status = dis_sym_ukirr(D, ir, Un, nb, n, D.sym_db, nb, uws, sh);
+    __syncthreads();
+    for (int e = threadIdx.x; e < (int)L; e += blockDim.x) U[e] = Un[e];
+    if (status) break;
+  }
+  __syncthreads();
+  double2* Un_out = D.U[cur ^ 1] + (size_t)k * L;
+  for (int e = threadIdx.x; e < (int)L; e += blockDim.x) Un_out[e] = U[e];
+  double tr = 0.0;
+  for (int j = threadIdx.x; j < W; j += blockDim.x) tr += lam[(size_t)j * W + j].x;
+  tr = block_sum(tr, sh.red);
+  if (threadIdx.x == 0) {
+    const int ngk = D.sym_goff[ir + 1] - D.sym_goff[ir];
+    D.wk1[k] = (double)W * D.wbtot * D.sym_nsym / ngk - tr;
+    if (status) D.sym_status[ir] = status;
+  }
+}
+
 }  // namespace
 
 const char* dis_kernel_name(int i) {
   static const char* names[kDisKernels] = {"k_dis_project", "k_dis_froz", "k_dis_z", "k_dis_step",
-                                           "k_dis_gauge", "k_dis_findu", "k_dis_rotate"};
+                                           "k_dis_gauge", "k_dis_findu", "k_dis_rotate", "k_dis_sym"};
   return (i >= 0 && i < kDisKernels) ? names[i] : "";
 }
 
@@ -575,6 +909,22 @@ int dis_run(const DisSpec& s, DisResult& r, std::string& err) {
   }
   bool any_froz = false;
   for (int v : nfroz) any_froz = any_froz || v > 0;
+  const int nir = s.sym_nir;
+  if (nir > 0) {
+    if (any_froz) {
+      // dis_main (src/disentangle.F90:154-157)
+      err = "in symmetry-adapted mode, frozen window not implemented yet";
+      return 1;
+    }
+    const size_t nslot = s.sym_d.size() / (2 * (size_t)W * W);
+    if (s.sym_ik.size() != (size_t)nir || s.sym_moff.size() != (size_t)nir + 1 ||
+        s.sym_goff.size() != (size_t)nir + 1 || s.sym_mem.size() != 2 * (size_t)s.sym_moff[nir] ||
+        s.sym_grp.size() != 2 * (size_t)s.sym_goff[nir] || nslot == 0 ||
+        s.sym_db.size() != nslot * 2 * (size_t)nb * nb || s.sym_nsym < 1) {
+      err = "disentangle: site symmetry tables missing or inconsistent";
+      return 5;
+    }
+  }
 
   const auto t0 = std::chrono::steady_clock::now();
   int rc = 0;
@@ -598,6 +948,15 @@ int dis_run(const DisSpec& s, DisResult& r, std::string& err) {
                o_uw = take((size_t)K * W * W * 16), o_m0 = take((size_t)K * B * W * W * 16),
                o_ws = take((size_t)K * kWs * NN * 16), o_wk1 = take(K * 8), o_wk = take(K * 8),
                o_st = take(K * 4), o_vz = take((size_t)K * NN * 16), o_sw = take(4);
+  // symmetry tables: ik, moff, mem, goff, grp, status; slot matrices; workspace
+  std::vector<int> sym_ints;
+  if (nir > 0) {
+    for (auto* v : {&s.sym_ik, &s.sym_moff, &s.sym_mem, &s.sym_goff, &s.sym_grp})
+      sym_ints.insert(sym_ints.end(), v->begin(), v->end());
+    sym_ints.insert(sym_ints.end(), (size_t)nir, 0);
+  }
+  const size_t o_syi = take(sym_ints.size() * 4), o_syd = take(s.sym_d.size() * 8),
+               o_sydb = take(s.sym_db.size() * 8), o_syws = take((size_t)nir * kDisSymWs * NN * 16);
   const size_t rot_smem = ((size_t)W * nb + 2 * (size_t)W * W) * 16;
   int mmax = 0;
   for (int k = 0; k < K; ++k) mmax = std::max(mmax, ndim[k] - nfroz[k]);
@@ -667,6 +1026,27 @@ int dis_run(const DisSpec& s, DisResult& r, std::string& err) {
     D.status = (int*)(a + o_st);
     D.Vz = (double2*)(a + o_vz);
     D.max_sweeps = (int*)(a + o_sw);
+    D.sym_nir = nir;
+    D.sym_nsym = s.sym_nsym;
+    D.sym_eps = s.sym_eps;
+    if (nir > 0) {
+      int* si = (int*)(a + o_syi);
+      size_t o = 0;
+      D.sym_ik = si;
+      D.sym_moff = si + (o += s.sym_ik.size());
+      D.sym_mem = si + (o += s.sym_moff.size());
+      D.sym_goff = si + (o += s.sym_mem.size());
+      D.sym_grp = si + (o += s.sym_goff.size());
+      D.sym_status = si + (o += s.sym_grp.size());
+      D.sym_d = (const double2*)(a + o_syd);
+      D.sym_db = (const double2*)(a + o_sydb);
+      D.sym_ws = (double2*)(a + o_syws);
+    }
+  }
+  if (nir > 0) {
+    DIS_CHECK(cudaMemcpyAsync((void*)D.sym_ik, sym_ints.data(), sym_ints.size() * 4, cudaMemcpyHostToDevice, st));
+    DIS_CHECK(cudaMemcpyAsync((void*)D.sym_d, s.sym_d.data(), s.sym_d.size() * 8, cudaMemcpyHostToDevice, st));
+    DIS_CHECK(cudaMemcpyAsync((void*)D.sym_db, s.sym_db.data(), s.sym_db.size() * 8, cudaMemcpyHostToDevice, st));
   }
   DIS_CHECK(cudaMemcpyAsync((void*)D.nnlist, s.nnlist.data(), (size_t)K * B * 4, cudaMemcpyHostToDevice, st));
   DIS_CHECK(cudaMemcpyAsync((void*)D.wb, s.wb.data(), B * 8, cudaMemcpyHostToDevice, st));
@@ -693,13 +1073,22 @@ int dis_run(const DisSpec& s, DisResult& r, std::string& err) {
       goto done;
     }
   }
+  // symmetry-adapted U_opt (src/disentangle.F90:186-190)
+  if (nir > 0) DIS_CHECK(launch(kDisSym, [&] { k_dis_sym_u<<<nir, 256, 0, st>>>(D, cur, 0); }));
   // ---- dis_extract iterations
   DIS_CHECK(launch(kDisZ, [&] { k_dis_z<<<K, 256, 0, st>>>(D, cur, 1, 0); }));
+  if (nir > 0) DIS_CHECK(launch(kDisSym, [&] { k_dis_sym_z<<<nir, 256, 0, st>>>(D, 0); }));
   r.log.clear();
   r.converged = 0;
   for (it = 1; it <= c.num_iter; ++it) {
-    DIS_CHECK(launch(kDisStep, [&] { k_dis_step<<<K, 256, step_smem, st>>>(D, cur, it); }));
+    if (nir > 0) {
+      DIS_CHECK(launch(kDisSym, [&] { k_dis_sym_step<<<nir, 256, 0, st>>>(D, cur, it); }));
+      DIS_CHECK(launch(kDisSym, [&] { k_dis_sym_u<<<nir, 256, 0, st>>>(D, cur ^ 1, 0); }));
+    } else {
+      DIS_CHECK(launch(kDisStep, [&] { k_dis_step<<<K, 256, step_smem, st>>>(D, cur, it); }));
+    }
     DIS_CHECK(launch(kDisZ, [&] { k_dis_z<<<K, 256, 0, st>>>(D, cur ^ 1, 0, 1); }));
+    if (nir > 0) DIS_CHECK(launch(kDisSym, [&] { k_dis_sym_z<<<nir, 256, 0, st>>>(D, 1); }));
     DIS_CHECK(cudaMemcpyAsync(wk1.data(), D.wk1, K * 8, cudaMemcpyDeviceToHost, st));
     DIS_CHECK(cudaMemcpyAsync(wk.data(), D.wk, K * 8, cudaMemcpyDeviceToHost, st));
     DIS_CHECK(cudaStreamSynchronize(st));
@@ -732,8 +1121,11 @@ int dis_run(const DisSpec& s, DisResult& r, std::string& err) {
       }
     }
   }
-  DIS_CHECK(launch(kDisGauge, [&] { k_dis_gauge<<<K, 256, 0, st>>>(D, cur); }));
+  // the subspace-Hamiltonian gauge is kept out in the symmetry-adapted mode (:2675)
+  if (nir == 0) DIS_CHECK(launch(kDisGauge, [&] { k_dis_gauge<<<K, 256, 0, st>>>(D, cur); }));
   DIS_CHECK(launch(kDisFindU, [&] { k_dis_findu<<<K, 256, 0, st>>>(D, cur); }));
+  // symmetric initial U with d = D (sitesym_replace_d_matrix_band, :237, :688-692)
+  if (nir > 0) DIS_CHECK(launch(kDisSym, [&] { k_dis_sym_u<<<nir, 256, 0, st>>>(D, cur, 1); }));
   DIS_CHECK(launch(kDisRotate, [&] { k_dis_rotate<<<K * B, 256, rot_smem, st>>>(D, cur); }));
   DIS_CHECK(cudaMemcpyAsync(status.data(), D.status, K * 4, cudaMemcpyDeviceToHost, st));
   DIS_CHECK(cudaMemcpyAsync(&r.max_sweeps, D.max_sweeps, 4, cudaMemcpyDeviceToHost, st));
@@ -743,6 +1135,23 @@ int dis_run(const DisSpec& s, DisResult& r, std::string& err) {
       err = "disentangle: eigensolver failure or rank-deficient U_opt^H A at k-point " + std::to_string(k + 1);
       rc = 1;
       goto done;
+    }
+  }
+  if (nir > 0) {
+    std::vector<int> ss(nir);
+    DIS_CHECK(cudaMemcpy(ss.data(), D.sym_status, nir * sizeof(int), cudaMemcpyDeviceToHost));
+    for (int v : ss) {
+      if (v % 10 == 1) {
+        // set_error_unconv (src/sitesym.F90:478-486)
+        err = "symmetrize_ukirr: not converged";
+        rc = -1;
+        goto done;
+      }
+      if (v) {
+        err = " ERROR: IN ZGESVD IN orthogonalize_u";
+        rc = 1;
+        goto done;
+      }
     }
   }
   if (s.uopt_out) DIS_CHECK(cudaMemcpyAsync(s.uopt_out, D.U[cur], (size_t)K * nb * W * 16, out_kind, st));

@@ -20,7 +20,7 @@ struct DisControl {
 };
 
 // kernels of the disentanglement, in the order of DisSpec::prof_ms
-enum DisKernel { kDisProject = 0, kDisFroz, kDisZ, kDisStep, kDisGauge, kDisFindU, kDisRotate, kDisKernels };
+enum DisKernel { kDisProject = 0, kDisFroz, kDisZ, kDisStep, kDisGauge, kDisFindU, kDisRotate, kDisSym, kDisKernels };
 const char* dis_kernel_name(int i);
 
 struct DisSpec {
@@ -44,6 +44,12 @@ struct DisSpec {
   // indexed by DisKernel; null = no timing
   double* prof_ms = nullptr;
   int* prof_counts = nullptr;
+  // symmetry-adapted mode (site_symmetry = T): the tables of w90g_set_sitesym with the
+  // band slots nb x nb (sym_db) and the Wannier slots W x W (sym_d); sym_nir = 0: off
+  int sym_nir = 0, sym_nsym = 0;
+  double sym_eps = 1.0e-3;
+  std::vector<int> sym_ik, sym_moff, sym_mem, sym_goff, sym_grp;
+  std::vector<double> sym_d, sym_db;
 };
 
 struct DisResult {

@@ -43,6 +43,7 @@ int build_sym_tables(int nw, int nb, int nsym, int nkirr, int nk, const int* ik2
     return sl;
   };
   r.nir = nkirr;
+  r.nsym = nsym;
   r.ik.resize(nkirr);
   std::vector<char> done(nk, 0);
   // star members in first-occurrence order (sitesym_symmetrize_rotation / _gradient

@@ -8,7 +8,7 @@
 namespace w90g {
 
 struct SymTables {
-  int nir = 0;
+  int nir = 0, nsym = 0;
   std::vector<int> ik;              // [nir] irreducible k (0-based)
   std::vector<int> moff, mem;       // star members: mem[2m] = k, mem[2m+1] = slot
   std::vector<int> goff, grp;       // little groups: grp[2g] = isym (0-based), grp[2g+1] = slot
