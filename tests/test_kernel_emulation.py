@@ -306,3 +306,50 @@ def test_emulated_symmetry_adapted_disentanglement(emu_dis):
     for k in range(K):
         np.testing.assert_allclose(Uoe[k] @ U0e[k], Uoo[k] @ U0o[k], atol=1e-9)
     np.testing.assert_allclose(M0.reshape(K, B, W, W).transpose(0, 1, 3, 2), M0o, atol=1e-9)
+
+
+@pytest.mark.parametrize("name", G.DIS_CASES)
+def test_emulated_disentanglement_with_frozen_states(emu_dis, name):
+    """The reference's disentanglement cases (silicon, copper, basic2, GaAs issue 192: 64 k,
+    outer and frozen windows) through dis_run's plain launch order on the emulated kernels
+    (k_dis_project, k_dis_froz, k_dis_z, k_dis_step, k_dis_gauge, k_dis_findu,
+    k_dis_rotate): every Omega_I line against the oracle (1e-10) and the printed lines
+    (1e-8), U_opt U and M0 against the oracle (1e-9).  32 emulated threads per CTA."""
+    d = G.load(name)
+    kn = d["knobs"]
+    km = O.kmesh_get(d["real_lattice"], d["kpt_latt"], int(kn["search_shells"]))
+    M = G.assemble_m(d, km["nnlist"], km["nncell"])
+    nb, W, K, B = int(d["num_bands"]), int(kn["num_wann"]), len(d["kpt_latt"]), km["nntot"]
+    dc = G.dis_control(d)
+    lib = emu_dis
+    ip, dp = C.POINTER(C.c_int), C.POINTER(C.c_double)
+    lib.emu_dis_plain.argtypes = ([C.c_int] * 4 + [ip, dp, C.c_double, dp, dp, dp, C.c_int, C.c_double, C.c_double,
+                                  C.c_int, C.c_double, C.c_double, C.c_int, C.c_double, C.c_double, C.c_int, dp, dp, dp,
+                                  dp, ip])
+    lib.emu_dis_plain.restype = C.c_int
+    Mf = np.ascontiguousarray(M.transpose(0, 1, 3, 2)).astype(np.complex128)
+    Af = np.ascontiguousarray(d["amn"].transpose(0, 2, 1)).astype(np.complex128)
+    eig = np.ascontiguousarray(d["eig"])
+    nn = np.ascontiguousarray(km["nnlist"], dtype=np.int32)
+    wb = np.ascontiguousarray(km["wb"])
+    log = np.zeros(3 * dc.num_iter)
+    U0 = np.zeros(K * W * W, dtype=np.complex128)
+    M0 = np.zeros(K * B * W * W, dtype=np.complex128)
+    Uo = np.zeros(K * nb * W, dtype=np.complex128)
+    status = np.zeros(1, dtype=np.int32)
+    rows = lib.emu_dis_plain(nb, W, K, B, _ptr(nn, C.c_int), _ptr(wb), km["wbtot"], _ptr(eig),
+                             _ptr(Mf.view(np.float64)), _ptr(Af.view(np.float64)), dc.num_iter, dc.mix_ratio,
+                             dc.conv_tol, dc.conv_window, dc.win_min, dc.win_max, int(dc.frozen_states), dc.froz_min,
+                             dc.froz_max, 32, _ptr(log), _ptr(U0.view(np.float64)), _ptr(M0.view(np.float64)),
+                             _ptr(Uo.view(np.float64)), _ptr(status, C.c_int))
+    assert status[0] == 0
+    U0o, M0o, Uoo, omi, recs = O.dis_main(M, d["amn"], d["eig"], km, W, dc)
+    assert rows == len(recs) == len(d["dis"])
+    for row, r, printed in zip(log.reshape(-1, 3), recs, d["dis"]):
+        assert abs(row[1] - r.omega_i_prev) < 1e-10 and abs(row[2] - r.omega_i) < 1e-10
+        assert abs(row[1] - printed[1]) < 1e-8 and abs(row[2] - printed[2]) < 1e-8
+    U0e = U0.reshape(K, W, W).transpose(0, 2, 1)
+    Uoe = Uo.reshape(K, W, nb).transpose(0, 2, 1)
+    for k in range(K):
+        np.testing.assert_allclose(Uoe[k] @ U0e[k], Uoo[k] @ U0o[k], atol=1e-9)
+    np.testing.assert_allclose(M0.reshape(K, B, W, W).transpose(0, 1, 3, 2), M0o, atol=1e-9)
