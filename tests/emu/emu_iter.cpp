@@ -16,14 +16,15 @@
 extern "C" {
 
 // M (K*B blocks W x W) and A (K blocks) column-major complex; tables as for
-// w90g_set_sitesym (nsym = 0: no symmetry).  Writes log ((num_iter+1) x kLogStride),
+// w90g_set_sitesym (nsym = 0: no symmetry); slwf_num > 0: selective localisation with
+// lambda and the constrained centres [3][W] (null: unconstrained).  Writes log ((num_iter+1) x kLogStride),
 // the final U (K blocks), status[2] = (projection status, unitarity/other).
 // Returns the number of log rows.
 int emu_wann_main(int W, int K, int B, const int* nnlist, const double* bk, const double* wb, double wbtot,
                   const double* Mraw, const double* A, int num_iter, int num_cg_steps, int conv_window,
                   double conv_tol, double trial_step, int nsym, int nkirr, const int* ik2ir, const int* ir2ik,
-                  const int* kptsym, const double* dw, const double* db, double eps, double* log_out, double* U_out,
-                  int* status) {
+                  const int* kptsym, const double* dw, const double* db, double eps, int slwf_num, double slwf_lambda,
+                  const double* slwf_c, double* log_out, double* U_out, int* status) {
   using namespace w90g;
   const size_t WW = (size_t)W * W, KB = (size_t)K * B;
   const int nt = (W + 31) / 32, ntt = nt * nt;
@@ -94,6 +95,21 @@ int emu_wann_main(int W, int K, int B, const int* nnlist, const double* bk, cons
     P.sym_db = reinterpret_cast<const double2*>(t.db.data());
     work.assign((size_t)t.nir * kSymWork * WW * 2, 0.0);
     P.sym_work = reinterpret_cast<double2*>(work.data());
+  }
+  // selective localisation (Engine::set_slwf): centres [3][W], lambda_loc, nu0
+  std::vector<double> slwfc;
+  if (slwf_num > 0) {
+    P.slwf_num = slwf_num;
+    slwfc.assign(3 * (size_t)W, 0.0);
+    if (slwf_c) {
+      slwfc.assign(slwf_c, slwf_c + 3 * (size_t)W);
+      P.slwf_lambda = slwf_lambda;
+      double c2 = 0.0;
+      for (int n = 0; n < slwf_num; ++n)
+        for (int i = 0; i < 3; ++i) c2 += slwfc[(size_t)i * W + n] * slwfc[(size_t)i * W + n];
+      P.slwf_nu0 = slwf_lambda * c2;
+    }
+    P.slwf_c = slwfc.data();
   }
   int offs_k[2] = {0, K}, offs_kb[2] = {0, (int)KB}, offs_grad[2] = {0, K * ntt}, offs_chunk[2] = {0, nchunk},
       offs_ir[2] = {0, P.sym_nir};

@@ -188,7 +188,7 @@ def emu_iter(tmp_path_factory):
     ip, dp = C.POINTER(C.c_int), C.POINTER(C.c_double)
     lib.emu_wann_main.argtypes = [C.c_int, C.c_int, C.c_int, ip, dp, dp, C.c_double, dp, dp, C.c_int, C.c_int,
                                   C.c_int, C.c_double, C.c_double, C.c_int, C.c_int, ip, ip, ip, dp, dp, C.c_double,
-                                  dp, dp, ip]
+                                  C.c_int, C.c_double, dp, dp, dp, ip]
     lib.emu_wann_main.restype = C.c_int
     return lib
 
@@ -217,8 +217,8 @@ def test_emulated_iteration_with_site_symmetry(emu_iter):
                                   _ptr(Mb.view(np.float64)), _ptr(Ab.view(np.float64)), niter, 5, -1, 1e-10, 2.0, nsym,
                                   nkirr, _ptr(ik2ir, C.c_int), _ptr(ir2ik, C.c_int), _ptr(kpt, C.c_int),
                                   _ptr(dw.view(np.float64)), _ptr(db.view(np.float64)),
-                                  float(d["knobs"]["symmetrize_eps"]), _ptr(log), _ptr(U.view(np.float64)),
-                                  _ptr(status, C.c_int))
+                                  float(d["knobs"]["symmetrize_eps"]), 0, 0.0, None, _ptr(log),
+                                  _ptr(U.view(np.float64)), _ptr(status, C.c_int))
     assert rows == niter + 1 and status[0] == 0 and status[1] == 0
     log = log.reshape(-1, 10)[:rows]
     sym = G.sitesym(d)
@@ -353,3 +353,42 @@ def test_emulated_disentanglement_with_frozen_states(emu_dis, name):
     for k in range(K):
         np.testing.assert_allclose(Uoe[k] @ U0e[k], Uoo[k] @ U0o[k], atol=1e-9)
     np.testing.assert_allclose(M0.reshape(K, B, W, W).transpose(0, 1, 3, 2), M0o, atol=1e-9)
+
+
+def test_emulated_iteration_with_selective_localisation(emu_iter):
+    """testw90_example26 (GaAs, slwf_num = 1 with its centre constrained, lambda = 1) through
+    the engine's launch order on the emulated FP64 kernels: the SLWF spread passes and the
+    factored SLWF gradient.  Every spread, O_IOD and Omega_nu against the oracle (1e-11)
+    and the printed lines of the first iterations (2e-10 A^2, 1.2e-9 from the third on,
+    where the printed run itself is sensitive at 1e-10)."""
+    d = G.load("slwf26")
+    kn = d["knobs"]
+    km = O.kmesh_get(d["real_lattice"], d["kpt_latt"], int(kn["search_shells"]))
+    M = G.assemble_m(d, km["nnlist"], km["nncell"])
+    K, B, W, niter = len(d["kpt_latt"]), km["nntot"], 4, 3
+    ctl, sl = G.slwf(d)
+    Mb = np.ascontiguousarray(M.transpose(0, 1, 3, 2)).astype(np.complex128)
+    Ab = np.ascontiguousarray(d["amn"].transpose(0, 2, 1)).astype(np.complex128)
+    nn = np.ascontiguousarray(km["nnlist"], dtype=np.int32)
+    bk = np.ascontiguousarray(km["bk"], dtype=np.float64)
+    wb = np.ascontiguousarray(km["wb"], dtype=np.float64)
+    cen = np.ascontiguousarray(sl.centres, dtype=np.float64)       # [3][W] Cartesian
+    log = np.zeros((niter + 1) * 10)
+    U = np.zeros(K * W * W, dtype=np.complex128)
+    status = np.zeros(2, dtype=np.int32)
+    z = np.zeros(1, dtype=np.int32)
+    rows = emu_iter.emu_wann_main(W, K, B, _ptr(nn, C.c_int), _ptr(bk), _ptr(wb), km["wbtot"],
+                                  _ptr(Mb.view(np.float64)), _ptr(Ab.view(np.float64)), niter, ctl.num_cg_steps,
+                                  ctl.conv_window, ctl.conv_tol, ctl.trial_step, 0, 0, _ptr(z, C.c_int),
+                                  _ptr(z, C.c_int), _ptr(z, C.c_int), None, None, 0.0, sl.num, sl.lam, _ptr(cen),
+                                  _ptr(log), _ptr(U.view(np.float64)), _ptr(status, C.c_int))
+    assert rows == niter + 1 and status[1] == 0
+    log = log.reshape(-1, 10)[:rows]
+    U0, M0 = O.overlap_project(M, d["amn"], km["nnlist"])
+    r = O.wann_main(M0, U0, km, O.WannControl(num_iter=niter), slwf=sl)
+    for row, x, printed in zip(log, [r.initial] + r.iters, d["conv"]):
+        sp = x.spread
+        # the cancelling Omega_IOD and Omega_nu terms are summed in another order: 1e-11
+        assert abs(row[3] - sp.om_tot) < 1e-11 and abs(row[5] - (sp.om_iod + sp.om_nu)) < 1e-11
+        assert abs(row[9] - sp.om_nu) < 1e-11 and abs(row[4] - sp.om_d) < 1e-11
+        assert abs(row[3] - printed[3]) < 2e-10 + 1e-9 * (x.iter >= 3)
