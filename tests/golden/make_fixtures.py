@@ -28,6 +28,9 @@ The site-symmetry cases (testw90_example21_As_sp: GaAs sp3; testw90_disentanglem
 H3S, entangled) also store the symmetry data of their .dmn files (k-point stars and the D
 matrices).
 
+The restart case (testw90_example02_restart: restart = wannierise) stores the U and M of
+the checkpoint the test ships and the run's printed lines.
+
 The guiding-centre case (testpostw90_gaas_shc: spinor GaAs, 16 isolated bands,
 guiding_centres = T) has no printed wannierise trajectory; its expected values are the
 final centres and spreads of the checkpoint shipped with that test.
@@ -464,6 +467,51 @@ def build_sitesym_dis(ref_root, out_dir):
     print("sitesym_dis", nb, nk, nntot, nsym, nkirr, dis.shape, omi_final, conv.shape, om)
 
 
+def parse_chk_fmt(lines):
+    """A formatted checkpoint (w90chk2chk -u2f of the .chk, src/wannier90_readwrite.F90:
+    2336-2366) without disentanglement: (num_wann, nntot, num_kpts, u[k,m,n], m[k,b,m,n])."""
+    i = 1
+    nb = int(lines[i]); i += 1
+    nex = int(lines[i]); i += 1 + (1 if nex > 0 else 0)
+    i += 2                                        # real and reciprocal lattice
+    nk = int(lines[i]); i += 1
+    i += 1 + nk                                   # mp_grid, k-points
+    nntot = int(lines[i]); i += 1
+    W = int(lines[i]); i += 1
+    i += 1                                        # checkpoint
+    assert int(lines[i]) == 0, "disentangled checkpoints are not handled here"
+    i += 1
+    vals = np.array([[float(x) for x in l.split()] for l in lines[i:i + W * W * nk + W * W * nntot * nk]])
+    z = vals[:, 0] + 1j * vals[:, 1]
+    u = z[:W * W * nk].reshape(nk, W, W).transpose(0, 2, 1)                  # (m,n,k) Fortran
+    m = z[W * W * nk:].reshape(nk, nntot, W, W).transpose(0, 1, 3, 2)        # (m,n,b,k) Fortran
+    return W, nntot, nk, np.ascontiguousarray(u), np.ascontiguousarray(m)
+
+
+def build_restart(ref_root, out_dir):
+    """testw90_example02_restart: lead, restart = wannierise from the converged checkpoint
+    the test ships (lead.chk.fmt.bz2), 20 more iterations."""
+    import bz2
+    d = os.path.join(ref_root, "test-suite/tests/testw90_example02_restart")
+    kw, real_lattice, kpts = parse_win(os.path.join(d, "lead.win"))
+    lines = bz2.open(os.path.join(d, "lead.chk.fmt.bz2"), "rt").read().splitlines()
+    W, nntot, nk, u, m = parse_chk_fmt(lines)
+    bench = os.path.join(d, "benchmark.out.default.inp=lead.win")
+    conv, initial, final, om, bvec = parse_benchmark(bench)
+    knobs = dict(num_wann=W, num_iter=int(kw.get("num_iter", 100)), num_cg_steps=int(kw.get("num_cg_steps", 5)),
+                 conv_tol=float(kw.get("conv_tol", "1e-10").replace("d", "e")),
+                 conv_window=int(kw.get("conv_window", -1)), trial_step=float(kw.get("trial_step", 2.0)),
+                 search_shells=int(kw.get("search_shells", 36)))
+    np.savez_compressed(
+        os.path.join(out_dir, "restart02.npz"),
+        real_lattice=real_lattice, kpt_latt=kpts, mp_grid=np.array([int(x) for x in kw["mp_grid"].split()[:3]]),
+        num_kpts=nk, nntot=nntot, u=u, m=m,
+        knobs=np.array([knobs[k] for k in sorted(knobs)], dtype=np.float64), knob_names=np.array(sorted(knobs)),
+        conv=conv, centres_final=final, omega_final=np.array([om["om_i"], om["om_d"], om["om_od"], om["om_tot"]]),
+        bvec_table=bvec)
+    print("restart02", W, nntot, nk, conv.shape, om)
+
+
 def build(ref_root, out_dir):
     for name, (sub, seed) in CASES.items():
         d = os.path.join(ref_root, sub)
@@ -502,3 +550,4 @@ if __name__ == "__main__":
     build_slwf(root, os.path.dirname(os.path.abspath(__file__)))
     build_sitesym(root, os.path.dirname(os.path.abspath(__file__)))
     build_sitesym_dis(root, os.path.dirname(os.path.abspath(__file__)))
+    build_restart(root, os.path.dirname(os.path.abspath(__file__)))

@@ -65,3 +65,29 @@ def test_cli_entangled_seed_files(tmp_path, name):
     uo = synth.to_math_u(chk["u_opt"])
     for k in range(K):
         np.testing.assert_allclose(uo[k].conj().T @ uo[k], np.eye(nw), atol=1e-12)
+
+
+def test_cli_restart_wannierise(tmp_path, capfd):
+    """testw90_example02_restart: restart = wannierise continues wann_main from the
+    checkpoint (here the shipped one's U and M written as a .chk) -- no .mmn / .amn are
+    read; every printed spread within 2e-10 A^2 of the reference's."""
+    from tests import golden_cases as G
+    d = G.load("restart02")
+    kn = d["knobs"]
+    seed = str(tmp_path / "lead")
+    w90io.write_win(seed + ".win", d["real_lattice"], d["kpt_latt"], d["mp_grid"], int(kn["num_wann"]),
+                    num_iter=int(kn["num_iter"]), search_shells=int(kn["search_shells"]), iprint=1,
+                    restart="wannierise")
+    W, K = int(kn["num_wann"]), len(d["kpt_latt"])
+    w90io.write_chk(seed + ".chk", num_bands=W, lattice=d["real_lattice"], kpts=d["kpt_latt"], mp_grid=d["mp_grid"],
+                    nntot=int(d["nntot"]), num_wann=W, u=np.asfortranarray(d["u"].transpose(1, 2, 0)),
+                    m=np.asfortranarray(d["m"].transpose(2, 3, 1, 0)), centres=np.zeros((3, W)), spreads=np.zeros(W))
+    capfd.readouterr()
+    assert cli.run(seed, "fp64") == 0
+    text = capfd.readouterr().out.splitlines()
+    conv = {int(l.split()[0]): float(l.split()[3]) for l in text
+            if l.rstrip().endswith("<-- CONV") and not l.strip().startswith(("+", "|"))}
+    for it, delta, rms, spread in d["conv"]:
+        assert abs(conv[int(it)] - spread) < 2e-10, int(it)
+    chk = w90io.read_chk(seed + ".chk")
+    np.testing.assert_allclose(chk["centres"].T, d["centres_final"][:, :3], atol=1.01e-6)

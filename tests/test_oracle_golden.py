@@ -198,3 +198,20 @@ def test_oracle_symmetry_adapted_disentanglement_reproduces_reference():
     sp = r.spread
     np.testing.assert_allclose([sp.om_i, sp.om_d, sp.om_od, sp.om_tot], d["omega_final"], rtol=0, atol=1.01e-9)
     np.testing.assert_allclose(r.centres.T, d["centres_final"][:, :3], rtol=0, atol=1.01e-6)
+
+
+def test_oracle_restart_from_checkpoint_reproduces_reference():
+    """testw90_example02_restart (lead, restart = wannierise): wann_main continued from the
+    U and M of the checkpoint the test ships; every printed spread within 2e-10 A^2, the
+    final Omega terms and centres."""
+    d = G.load("restart02")
+    km = O.kmesh_get(d["real_lattice"], d["kpt_latt"], int(d["knobs"]["search_shells"]))
+    np.testing.assert_allclose(km["wb"], d["bvec_table"][:, 3], atol=1e-6)
+    r = O.wann_main(d["m"], d["u"], km, G.control(d))
+    recs = [r.initial] + r.iters
+    assert len(recs) == len(d["conv"])
+    for got, (it, delta, rms, spread) in zip(recs, d["conv"]):
+        assert got.iter == int(it) and abs(got.spread.om_tot - spread) < 2e-10
+    sp = r.spread
+    np.testing.assert_allclose([sp.om_i, sp.om_d, sp.om_od, sp.om_tot], d["omega_final"], rtol=0, atol=1.01e-9)
+    np.testing.assert_allclose(r.centres.T, d["centres_final"][:, :3], rtol=0, atol=1.01e-6)

@@ -5,7 +5,8 @@ Isolated bands (num_bands = num_wann): the projections are read into u_matrix
 (src/wannier_prog.F90:523-529) and the Loewdin projection runs.  Entangled bands
 (num_bands > num_wann): ``seedname.eig`` is read too, the projections go into u_opt
 and the disentanglement (dis_main + setup_m_loc) runs with the ``dis_*`` keywords of
-the .win.  With site_symmetry = T, ``seedname.dmn`` supplies the symmetry data.  Then
+the .win.  With site_symmetry = T, ``seedname.dmn`` supplies the symmetry data; with
+restart = wannierise the run continues from ``seedname.chk`` instead.  Then
 wann_main runs on the GPU, the wannierise section of the .wout is printed
 when iprint > 0, and ``seedname.chk`` is written (src/wannier_prog.F90:256-275), with
 Omega_I, lwindow, ndimwin and U_opt after a disentanglement.
@@ -29,10 +30,15 @@ def run(seedname, precision="tensor"):
     mp = opts.pop("mp_grid", None)
     # the seed files hold the bands left after exclusion; the list goes to the checkpoint
     exclude = opts.pop("exclude_bands", [])
+    restart = opts.pop("restart", None)
+    if restart is not None and restart != "wannierise":
+        raise SystemExit("restart = %s: only restart = wannierise is supported" % restart)
     opts.setdefault("iprint", 1)
     opts["gpu_tensor"] = 1 if precision == "tensor" else 0
     c = w90.setup(kpoints=kpts, unit_cell_cart=lattice, num_wann=nw, num_bands=nb, mp_grid=mp, **opts)
     K = len(kpts)
+    if restart == "wannierise":
+        return _restart_wannierise(c, seedname, nb, nw, lattice, kpts, mp, exclude)
     if opts.get("site_symmetry"):
         # sitesym_read after the input (src/wannier_prog.F90:174-177)
         w90.check(c, w90.w90_set_sitesym(c, w90io.read_dmn(seedname + ".dmn", nw)), "sitesym_read")
@@ -72,6 +78,29 @@ def run(seedname, precision="tensor"):
                     mp_grid=mp if mp is not None else (0, 0, 0), nntot=w90.w90_get_nn(c), num_wann=nw,
                     u=u, m=np.asfortranarray(m[:nw, :nw]), centres=centres, spreads=spreads, dis=dis,
                     exclude_bands=exclude)
+    return ierr
+
+
+def _restart_wannierise(c, seedname, nb, nw, lattice, kpts, mp, exclude):
+    """restart = wannierise: wann_main continues from the U and M of seedname.chk (the
+    reference reads the checkpoint instead of the overlaps and the projections,
+    src/wannier_prog.F90)."""
+    chk = w90io.read_chk(seedname + ".chk")
+    if chk["num_wann"] != nw or chk["num_kpts"] != len(kpts):
+        raise SystemExit("restart: %s.chk does not match the .win (num_wann / k-points)" % seedname)
+    if chk.get("have_disentangled"):
+        raise SystemExit("restart: a disentangled checkpoint needs the disentanglement data, not supported")
+    u = np.asfortranarray(chk["u"].astype(np.complex128))
+    m = np.asfortranarray(chk["m"].astype(np.complex128))
+    uopt = np.asfortranarray(np.broadcast_to(np.eye(nb, nw, dtype=np.complex128)[:, :, None], (nb, nw, len(kpts))).copy())
+    w90.w90_set_m_local(c, m)
+    w90.w90_set_u_matrix(c, u)
+    w90.w90_set_u_opt(c, uopt)
+    ierr = w90.w90_wannierise(c)
+    w90.check(c, ierr, "w90_wannierise")
+    w90io.write_chk(seedname + ".chk", num_bands=nb, lattice=lattice, kpts=kpts,
+                    mp_grid=mp if mp is not None else (0, 0, 0), nntot=w90.w90_get_nn(c), num_wann=nw, u=u, m=m,
+                    centres=w90.w90_get_centres(c, nw), spreads=w90.w90_get_spreads(c, nw), exclude_bands=exclude)
     return ierr
 
 

@@ -119,6 +119,8 @@ def win_system(path):
             opts[k] = int(kw[k].split()[0])
     if "exclude_bands" in kw:
         opts["exclude_bands"] = parse_range_vector(kw["exclude_bands"])
+    if "restart" in kw:
+        opts["restart"] = kw["restart"].split()[0].lower()
     if opts.get("guiding_centres") and "projections" in blocks:
         spin = _flag(kw.get("spinors", "f"))
         opts["guiding_centres_frac"] = projection_sites(blocks, lattice, spin)
