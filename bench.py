@@ -128,6 +128,40 @@ def _env_rank():
 # ----------------------------------------------------------------------------------
 # CPU restatement timing (oracle) -- used by the cpu_baseline leg and --impl reference
 # ----------------------------------------------------------------------------------
+def _oracle_kmesh(real_lattice, kpoints, search_shells):
+    """The k-mesh tables of the oracle's kmesh_get in the generator's layout."""
+    from oracle import w90_oracle as O
+    km = O.kmesh_get(real_lattice, kpoints, search_shells)
+    return km["nntot"], km["nnlist"], km["nncell"], km["bk"]
+
+
+def oracle_iterations(workload):
+    """Iterations per converged solve of the oracle's own wann_main on this workload: the
+    committed fixture of the oracle run to convergence (tests/golden/make_converged.py);
+    fixed-length workloads run their num_iter."""
+    wl = WORKLOADS[workload]
+    if wl.get("conv_window", -1) <= 1:
+        return wl["num_iter"]
+    import numpy as np
+    z = np.load(os.path.join(ROOT, "tests", "golden", workload + "_conv.npz"))
+    return int(z["niter"])
+
+
+def bench_config(workload, wl, K=None, B=None, W=None, world=1):
+    """The config object of both arms' lines (identical keys and values for one workload)."""
+    from wannier90_gb300 import synth
+    c = synth.CONFIGS[wl["cfg"]]
+    K = K or c["mp"][0] * c["mp"][1] * c["mp"][2]
+    B = B or {"sc": 6, "fcc": 8, "bcc": 12}[c["kind"]]
+    W = W or c["num_wann"]
+    return {"workload": workload, "lattice": c["kind"], "a_angstrom": c["a"],
+            "kmesh": "%dx%dx%d" % tuple(c["mp"]), "num_kpts": K, "nntot": B, "num_wann": W,
+            "conv_tol": wl["conv_tol"], "conv_window": wl["conv_window"], "num_iter_cap": wl["num_iter"],
+            "seed": 0, "l2": ("inputs larger than L2 (M = %d MiB)" if W * W * K * B * 16 > 129e6 else
+                              "inputs smaller than L2 (M = %d MiB), not flushed") % (W * W * K * B * 16 >> 20),
+            "parallelism": "replicas" if world > 1 else "single"}
+
+
 def _cpu_worker(args):
     wl, seed, iters = args
     os.environ["OPENBLAS_NUM_THREADS"] = "1"
@@ -137,7 +171,8 @@ def _cpu_worker(args):
     from oracle import w90_oracle as O
     from wannier90_gb300 import synth
 
-    p = synth.make_problem(**synth.CONFIGS[wl["cfg"]], seed=seed)
+    # the problem is built on the oracle's k-mesh: nothing of the engine's library is loaded
+    p = synth.make_problem(**synth.CONFIGS[wl["cfg"]], seed=seed, kmesh=_oracle_kmesh)
     M = synth.to_math_m(p.m)
     A = synth.to_math_u(p.a)
     km = O.kmesh_get(p.real_lattice, p.kpoints)
@@ -265,7 +300,7 @@ def run_reference_arm(args, wl):
     procs = os.cpu_count() or 1
     iters = args.cpu_iters
     spi = cpu_seconds_per_iteration(wl, iters, procs)
-    niter = args.assume_iters
+    niter = args.assume_iters or oracle_iterations(args.workload)
     # each step: a bounded sample (iters iterations on every core); solves/s extrapolated
     t_steps = []
     for _ in range(args.warmup + args.steps):
@@ -279,12 +314,13 @@ def run_reference_arm(args, wl):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(t_steps[args.warmup:]),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded tight-binding generator)",
-        "config": {"workload": args.workload, "note": "CPU restatement of wann_main (NumPy/LAPACK), "
-                   "not wannier90.x: no Fortran compiler in the image"},
+        "config": bench_config(args.workload, wl, world=world),
+        "note": "CPU restatement of wann_main (NumPy/LAPACK), not wannier90.x: no Fortran compiler in the image",
+        "iterations_per_solve": niter,
         "cpu_baseline": {"value": value, "unit": "solves/s", "cores": procs, "kind": "port",
                          "sample": "%d iterations per core of the %s solve (1 process per core, 1 BLAS thread), "
-                                   "solves/s = cores / (s_per_iter * %d iterations per solve)"
-                                   % (iters, args.workload, niter)},
+                                   "solves/s = cores / (s_per_iter * %d iterations per solve; the oracle's own "
+                                   "converged count)" % (iters, args.workload, niter)},
         "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -904,10 +940,12 @@ def main():
     ap.add_argument("--workload", default="fcc10_w32", choices=sorted(WORKLOADS))
     ap.add_argument("--cpu-iters", type=int, default=4)
     ap.add_argument("--assume-iters", type=int, default=0,
-                    help="iterations per solve for the reference arm (0: measured by the GPU arm's table)")
+                    help="iterations per solve for the reference arm (0: the oracle's converged count)")
+    ap.add_argument("--fp64-steps", type=int, default=2,
+                    help="timed solves of the plain FP64 GPU path reported beside the tensor path")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-iters", type=int, default=6)
-    ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--e2e-steps", type=int, default=0, help="solves of the e2e leg (0: --steps)")
     ap.add_argument("--batch-size", type=int, default=0, help="problems in the batched workload (default 256)")
     ap.add_argument("--serve-jobs", type=int, default=0, help="requests of the serving stream (default 24)")
     ap.add_argument("--serve-rate", type=float, default=0.0, help="arrival rate of the serving stream (200/s)")
@@ -922,8 +960,6 @@ def main():
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":
-        if args.assume_iters <= 0:
-            args.assume_iters = KNOWN_ITERS.get(args.workload, 1000)
         return run_reference_arm(args, wl)
 
     if wl.get("dis"):
@@ -997,16 +1033,46 @@ def main():
         dist.barrier()
     torch.cuda.synchronize()
     clocks.start()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ev0.record(stream)
-    for _ in range(args.steps):
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    evs[0].record(stream)
+    for i in range(args.steps):
         device_step()
-    ev1.record(stream)
+        evs[i + 1].record(stream)
     torch.cuda.synchronize()
     clk = clocks.stop()
     if dist:
         dist.barrier()
-    ms_per_step, value = replica_rate(ev0.elapsed_time(ev1), args.steps, world, dist, "cuda")
+    ms_per_step, value = replica_rate(evs[0].elapsed_time(evs[-1]), args.steps, world, dist, "cuda")
+    lat_ms = [evs[i].elapsed_time(evs[i + 1]) for i in range(args.steps)]
+
+    # the plain FP64 GPU path on the same problem (the metric compares the two)
+    fp64 = None
+    if args.precision == "tensor" and args.fp64_steps > 0:
+        h64 = w90.setup(kpoints=p.kpoints, unit_cell_cart=p.real_lattice, num_wann=W, **dict(opts, gpu_tensor=0))
+        w90.w90_set_stream(h64, stream.cuda_stream)
+
+        def fp64_step():
+            with torch.cuda.stream(stream):
+                m_work.copy_(m0)
+                u_work.copy_(u0)
+            ierr = w90.w90_wannierise_device(h64, m_work.data_ptr(), u_work.data_ptr())
+            if ierr > 0:
+                raise RuntimeError(h64.last_error())
+
+        fp64_step()
+        torch.cuda.synchronize()
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(args.fp64_steps + 1)]
+        e[0].record(stream)
+        for i in range(args.fp64_steps):
+            fp64_step()
+            e[i + 1].record(stream)
+        torch.cuda.synchronize()
+        ms64, v64 = replica_rate(e[0].elapsed_time(e[-1]), args.fp64_steps, world, dist, "cuda")
+        n64 = int(w90.w90_get_log(h64, wl["num_iter"] + 1)[-1][0])
+        fp64 = {"value": v64, "unit": "solves/s", "ms_per_step": ms64, "steps": args.fp64_steps,
+                "iterations_per_solve": n64, "ms_per_iteration": ms64 / n64,
+                "mixed_over_fp64": value / v64,
+                "mixed_over_fp64_per_iteration": (ms64 / n64) / (ms_per_step / niter)}
 
     # e2e through the reference-named C ABI with host buffers (pinned)
     m_host0 = torch.from_numpy(m0.cpu().numpy()).pin_memory()
@@ -1031,7 +1097,7 @@ def main():
             raise RuntimeError(h.last_error())
         return dt
 
-    e2e_t = [e2e_step() for _ in range(max(1, args.e2e_steps))]
+    e2e_t = [e2e_step() for _ in range(max(1, args.e2e_steps or args.steps))]
     e2e_value = world / statistics.mean(e2e_t)
     bytes_m = W * W * B * K * 16
     bytes_u = W * W * K * 16
@@ -1064,25 +1130,36 @@ def main():
     peak = float(MEASURED.get("bf16_tflops", 1900.0))
     peak_src = ("bf16_tflops of MEASURED_PEAKS.json (burst), of measured" if "bf16_tflops" in MEASURED
                 else "1.9 PFLOP/s bf16 burst, of fallback")
+    hbm_peak = float(MEASURED.get("hbm_gbs", 6800.0))
     if args.precision == "tensor" and dom in ("k_m_update", "k_exp_u"):
         if dom == "k_m_update":
-            flops = tile_flops * 2 * K * -(-(B * wp) // 128)
-            fp64_eq = useful_mupdate
+            issued = tile_flops * 2 * K * -(-(B * wp) // 128)
+            algo = useful_mupdate
+            algo_bytes = 16.0 * K * W * W * (2 * B + 3)
             kname = "k_oz_mupdate (tcgen05, steps 1+2)"
         else:
             cnt_exp = max(per_kernel["k_exp_u"]["launches"], 1)
             prods = exp_products / cnt_exp / K           # products per matrix per launch
-            flops = tile_flops * prods * K
-            fp64_eq = prods * K * 8.0 * W ** 3
+            issued = tile_flops * prods * K
+            algo = prods * K * 8.0 * W ** 3
+            algo_bytes = 16.0 * K * W * W * 3
             kname = "k_oz_exp (tcgen05)"
-        achieved = flops / (avg * 1e-3) / 1e12
+        sec = avg * 1e-3
+        achieved = algo / sec / 1e12
+        traffic = NCU_TRAFFIC.get((args.workload, dom))
         roof = {"bound": "tensor", "kernel": kname, "achieved": achieved, "peak": peak,
-                "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
                 "peak_source": peak_src,
-                "algorithmic_flops_per_launch": flops,
-                "fp64_equivalent": {"flops_per_launch": fp64_eq,
-                                    "tflops": fp64_eq / (avg * 1e-3) / 1e12,
-                                    "fp64_pipe_peak_tflops": fp64_peak}}
+                "algorithmic_flops_per_launch": algo,
+                "algorithmic_flops_note": "complex FP64-equivalent products (8 W^3 real FLOP each): "
+                                          "2 per (k,b) for the M update, the exp chain's products for exp",
+                "issued_mma": {"flops_per_launch": issued, "tflops": issued / sec / 1e12,
+                               "frac": issued / sec / 1e12 / peak,
+                               "note": "BF16 MMA FLOP actually issued: 28 digit pairs x 128 x 2WP x 2WP per tile"},
+                "hbm": {"algorithmic_bytes_per_launch": algo_bytes, "gbs": algo_bytes / sec / 1e9,
+                        "peak_gbs": hbm_peak, "frac": algo_bytes / sec / 1e9 / hbm_peak},
+                "fp64_pipe": {"tflops": achieved, "fp64_pipe_peak_tflops": fp64_peak,
+                              "ratio": achieved / fp64_peak if fp64_peak > 0 else None}}
     else:
         if dom == "k_exp_u":
             cnt_exp = max(per_kernel["k_exp_u"]["launches"], 1)
@@ -1093,7 +1170,8 @@ def main():
             flops = useful_mupdate
         achieved = flops / (avg * 1e-3) / 1e12
         roof = {"bound": "fp64", "kernel": dom, "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
-                "frac": achieved / fp64_peak if fp64_peak > 0 else None, "traffic": None,
+                "frac": achieved / fp64_peak if fp64_peak > 0 else None,
+                "traffic": NCU_TRAFFIC.get((args.workload + ":fp64", dom)),
                 "peak_source": "FP64 FMA probe measured in this run (MEASURED_PEAKS.json has no FP64 figure)",
                 "algorithmic_flops_per_launch": flops}
     roof["per_kernel"] = per_kernel
@@ -1114,17 +1192,17 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded tight-binding generator)",
-            "config": {"workload": args.workload, "lattice": synth.CONFIGS[wl["cfg"]]["kind"],
-                       "num_kpts": K, "nntot": B, "num_wann": W, "conv_tol": wl["conv_tol"],
-                       "conv_window": wl["conv_window"], "iterations_per_solve": niter,
-                       "precision": ("tensor: M(k,b) = U^H M0 U (7x7-bit digits) and exp(sD), U dU (56-bit "
-                                     "digits) on tcgen05 BF16 MMAs with exact slicing (FP64-accurate); "
-                                     "gradient, Im ln M_nn, spread and controller on the FP64 pipe"
-                                     if args.precision == "tensor" else "fp64"),
-                       "l2": "inputs larger than L2 (M = %d MB)" % (bytes_m >> 20),
-                       "parallelism": "replicas" if world > 1 else "single"},
+            "config": bench_config(args.workload, wl, K, B, W, world),
+            "iterations_per_solve": niter,
+            "precision": ("tensor: M(k,b) = U^H M0 U (7x7-bit digits) and exp(sD), U dU (56-bit "
+                          "digits) on tcgen05 BF16 MMAs with exact slicing (FP64-accurate); "
+                          "gradient, Im ln M_nn, spread and controller on the FP64 pipe"
+                          if args.precision == "tensor" else "fp64"),
+            "latency_ms": {"p50": float(np.percentile(lat_ms, 50)), "p99": float(np.percentile(lat_ms, 99)),
+                           "max": float(max(lat_ms)), "note": "per converged solve, device-resident inputs"},
+            "fp64_gpu": fp64,
             "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": bytes_m + bytes_u,
-                    "d2h_bytes_per_step": bytes_m + bytes_u},
+                    "d2h_bytes_per_step": bytes_m + bytes_u, "steps": len(e2e_t)},
             "gpu_launches": int(launches) * args.steps,
             "roofline": roof,
             "cpu_baseline": cpu,
@@ -1136,8 +1214,16 @@ def main():
     return 0
 
 
-# iterations per solve of each workload as measured by the GPU arm (FP64 engine)
-KNOWN_ITERS = {"fcc10_w32": 1834, "sc4_w8": 200, "dis_fcc8_b48w32": (200, 3053)}
+# iterations per solve of the entangled workload as measured by the GPU arm (FP64 engine):
+# (dis_main iterations, wann_main iterations)
+KNOWN_ITERS = {"dis_fcc8_b48w32": (200, 3053)}
+
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of the dominant
+# kernel, from the committed ncu captures under profiles/ (name of the summary beside each)
+NCU_TRAFFIC = {
+    # profiles/k_oz_mupdate_fcc10_w32.md: steps 1 + 2 of one M update
+    ("fcc10_w32", "k_m_update"): 584.4e6,
+}
 
 if __name__ == "__main__":
     sys.exit(main())

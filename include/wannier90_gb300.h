@@ -241,12 +241,15 @@ int w90g_ws_vectors(const double* real_lattice33, const int* mp_grid3, const int
  * A(k) on entry), updated in place; nnkp is the host array cget_nnkp returns
  * ([nntot][num_kpts], 1-based).  Scratch lives in a file-scope device array of about
  * 4.3 MB that every GPU loading the library keeps until exit; limits num_wann <= 32,
- * num_kpts <= 4096, num_kpts*nntot <= 8192 (larger sizes return 5 without GPU work).
- * The first call on a device resolves that array's address (cudaGetSymbolAddress) and
- * sets kernel attributes, so make it before any stream capture.  Calls share the array:
- * calls whose GPU work overlaps (other streams or threads) race.  cuda_stream may be
- * NULL (legacy default stream).  Returns 0 ok, 1 CUDA error / rank-deficient A(k),
- * 5 sizes out of range.  Synchronises the stream before returning. */
+ * num_kpts <= 4096, num_kpts*nntot <= 8192, and every nnkp entry in 1..num_kpts
+ * (anything else returns 5 without GPU work).  Every call resolves that array's address
+ * (cudaGetSymbolAddress); the first call on a device, and the first after a device
+ * reset, also sets kernel attributes, so make it before any stream capture.  Calls share
+ * the array: calls whose GPU work overlaps (other streams or threads) race.  An error
+ * already pending on the calling thread (cudaPeekAtLastError) makes the call return 1
+ * and is left pending.  cuda_stream may be NULL (legacy default stream).  Returns 0 ok,
+ * 1 CUDA error / rank-deficient A(k), 5 sizes or nnkp out of range.  Synchronises the
+ * stream before returning. */
 int w90g_project_overlap_noalloc(int num_wann, int num_kpts, int nntot, const int* nnkp,
                                  double* d_m_matrix, double* d_u_matrix, void* cuda_stream);
 

@@ -543,7 +543,9 @@ def build(ref_root, out_dir):
 
 
 if __name__ == "__main__":
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("W90_REFERENCE")
+    if not root or not os.path.isdir(root):
+        raise SystemExit("usage: make_fixtures.py <Wannier90 source tree> (or set W90_REFERENCE)")
     build(root, os.path.dirname(os.path.abspath(__file__)))
     build_guiding(root, os.path.dirname(os.path.abspath(__file__)))
     build_dis(root, os.path.dirname(os.path.abspath(__file__)))

@@ -91,3 +91,52 @@ def test_cli_restart_wannierise(tmp_path, capfd):
         assert abs(conv[int(it)] - spread) < 2e-10, int(it)
     chk = w90io.read_chk(seed + ".chk")
     np.testing.assert_allclose(chk["centres"].T, d["centres_final"][:, :3], atol=1.01e-6)
+
+
+def test_cli_restart_after_disentanglement(tmp_path):
+    """An entangled run checkpoints the disentangled subspace; restart = wannierise from
+    that checkpoint continues wann_main on its num_wann x num_wann overlaps and keeps
+    U_opt, the windows and Omega_I.  Run 0 wannierisation iterations after the
+    disentanglement, then restart for the full count: the same trajectory as the one-shot
+    run (the controller starts from the same state), so the same final centres."""
+    from tests import golden_cases as G
+    d = G.load("silicon_dis")
+    kn = d["knobs"]
+    ss = int(kn["search_shells"])
+    km = O.kmesh_get(d["real_lattice"], d["kpt_latt"], ss)
+    M = G.assemble_m(d, km["nnlist"], km["nncell"])
+    dc = G.dis_control(d)
+    ctl = G.control(d)
+    nb, nw = int(d["num_bands"]), int(kn["num_wann"])
+
+    def files(seed, num_iter, **extra):
+        kw = dict(num_iter=num_iter, conv_tol=ctl.conv_tol, trial_step=ctl.trial_step, search_shells=ss,
+                  iprint=0, dis_num_iter=dc.num_iter, dis_mix_ratio=dc.mix_ratio, dis_conv_tol=dc.conv_tol,
+                  dis_conv_window=dc.conv_window, dis_win_max=dc.win_max, dis_froz_max=dc.froz_max, **extra)
+        w90io.write_win(seed + ".win", d["real_lattice"], d["kpt_latt"], d["mp_grid"], nw, num_bands=nb, **kw)
+
+    one = str(tmp_path / "one")
+    files(one, ctl.num_iter)
+    w90io.write_mmn(one + ".mmn", synth.from_math_m(M), km["nnlist"], km["nncell"])
+    w90io.write_amn(one + ".amn", synth.from_math_u(d["amn"]))
+    w90io.write_eig(one + ".eig", np.asfortranarray(d["eig"].T))
+    assert cli.run(one, "fp64") == 0
+    ref = w90io.read_chk(one + ".chk")
+    two = str(tmp_path / "two")
+    files(two, 0)
+    for ext in (".mmn", ".amn", ".eig"):
+        with open(one + ext) as a, open(two + ext, "w") as b:
+            b.write(a.read())
+    assert cli.run(two, "fp64") == 0
+    mid = w90io.read_chk(two + ".chk")
+    assert mid["have_disentangled"]
+    files(two, ctl.num_iter, restart="wannierise")
+    assert cli.run(two, "fp64") == 0
+    end = w90io.read_chk(two + ".chk")
+    assert end["have_disentangled"] and end["num_bands"] == nb
+    assert end["omega_invariant"] == ref["omega_invariant"]
+    np.testing.assert_array_equal(end["ndimwin"], ref["ndimwin"])
+    np.testing.assert_array_equal(end["lwindow"], ref["lwindow"])
+    np.testing.assert_array_equal(end["u_opt"], ref["u_opt"])
+    np.testing.assert_allclose(end["centres"], ref["centres"], atol=1e-8)
+    np.testing.assert_allclose(end["spreads"], ref["spreads"], atol=1e-8)

@@ -61,7 +61,16 @@ def test_served_jobs_equal_standalone_runs():
     assert sorted(d[0] for d in done) == list(range(len(JOBS)))
     assert all(d[1] == 0 for d in done), [(d[0], jobs[d[0]][0].last_error()) for d in done if d[1]]
     assert all(d[2] <= d[3] <= d[4] for d in done)
-    assert 1 <= stats["peak_active"] <= 4 and stats["peak_bytes"] <= budget
+    assert 2 <= stats["peak_active"] <= 4 and stats["peak_bytes"] <= budget
+    # continuous batching, not a queue: jobs ran at the same time, and a job that arrived
+    # while others held the slots / memory waited and was admitted while another still ran
+    spans = {d[0]: (d[3], d[4]) for d in done}
+    overlapping = [(i, j) for i in spans for j in spans
+                   if i < j and spans[i][0] < spans[j][1] and spans[j][0] < spans[i][1]]
+    assert overlapping, spans
+    queued = [d for d in done if d[3] > d[2]
+              and any(o[0] != d[0] and o[3] < d[3] < o[4] for o in done)]
+    assert queued, [(d[0], d[2], d[3], d[4]) for d in done]
     for i, (h, m, u) in enumerate(jobs):
         m_a, u_a, log_a, cen_a = alone[i]
         log_b = w90.w90_get_log(h, NUM_ITER + 1)

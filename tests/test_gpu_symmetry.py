@@ -146,3 +146,40 @@ def test_symmetry_adapted_disentanglement_golden():
     for it, delta, rms, spread in d["conv"]:
         assert abs(by_iter[int(it)][3] - spread) < 2e-10, (int(it), by_iter[int(it)][3], spread)
     np.testing.assert_allclose(out["omega"], d["omega_final"], rtol=0, atol=2e-9)
+
+
+def test_symmetry_adapted_restart_cli(tmp_path, capfd):
+    """restart = wannierise with site_symmetry = T: the .dmn is read before the restart
+    branch (sitesym_read precedes it in the reference's program), and wann_main continues
+    from the checkpoint in the symmetry-adapted mode: every spread of the restarted run
+    against the oracle's symmetry-adapted wann_main from the same U and M."""
+    from wannier90_gb300 import __main__ as cli
+    from wannier90_gb300 import w90io
+    d = G.load("sitesym21")
+    kn = d["knobs"]
+    ss = int(kn["search_shells"])
+    km = O.kmesh_get(d["real_lattice"], d["kpt_latt"], ss)
+    M = G.assemble_m(d, km["nnlist"], km["nncell"])
+    seed = str(tmp_path / "GaAs")
+    first = 12
+    w90io.write_win(seed + ".win", d["real_lattice"], d["kpt_latt"], d["mp_grid"], 4, search_shells=ss, iprint=0,
+                    site_symmetry=".true.", symmetrize_eps="1d-9", num_iter=first)
+    w90io.write_mmn(seed + ".mmn", synth.from_math_m(M), km["nnlist"], km["nncell"])
+    w90io.write_amn(seed + ".amn", synth.from_math_u(d["amn"]))
+    G.write_dmn(seed + ".dmn", d)
+    assert cli.run(seed, "fp64") == 0
+    chk = w90io.read_chk(seed + ".chk")
+    more = 20
+    w90io.write_win(seed + ".win", d["real_lattice"], d["kpt_latt"], d["mp_grid"], 4, search_shells=ss, iprint=1,
+                    site_symmetry=".true.", symmetrize_eps="1d-9", num_iter=more, restart="wannierise")
+    capfd.readouterr()
+    assert cli.run(seed, "fp64") == 0
+    text = capfd.readouterr().out.splitlines()
+    conv = {int(l.split()[0]): float(l.split()[3]) for l in text
+            if l.rstrip().endswith("<-- CONV") and not l.strip().startswith(("+", "|"))}
+    r = O.wann_main(synth.to_math_m(chk["m"]), synth.to_math_u(chk["u"]), km, O.WannControl(num_iter=more),
+                    sitesym=G.sitesym(d))
+    for rec in r.iters:
+        assert abs(conv[rec.iter] - rec.spread.om_tot) < 1e-9, rec.iter
+    end = w90io.read_chk(seed + ".chk")
+    np.testing.assert_allclose(end["centres"], r.centres, atol=1e-6)

@@ -10,7 +10,11 @@ from tests import golden_cases as G
 from wannier90_gb300 import library as w90
 from wannier90_gb300 import synth, w90io
 
-REF = "/root/reference/test-suite/tests/testw90_example02"
+from tests.conftest import reference_root
+
+# the reference's own example02 (lead) inputs, read from the Wannier90 source tree named
+# by W90_REFERENCE; skipped without it
+REF = os.path.join(reference_root() or "", "test-suite", "tests", "testw90_example02")
 
 
 def _small():
@@ -42,7 +46,7 @@ def test_win_roundtrip(tmp_path):
     assert opts["precond"] == 0 and list(opts["mp_grid"]) == [3, 3, 3]
 
 
-@pytest.mark.skipif(not os.path.isdir(REF), reason="Wannier90 source tree not present")
+@pytest.mark.skipif(reference_root() is None, reason="W90_REFERENCE (Wannier90 source tree) not set")
 def test_reads_reference_inputs():
     d = G.load("pb")
     lat, kp, opts = w90io.win_system(os.path.join(REF, "lead.win"))

@@ -58,3 +58,9 @@ def test_noalloc_rejects_sizes_beyond_its_scratch():
     assert L.w90g_project_overlap_noalloc(33, 1, 8, ip, dummy, dummy, None) == 5
     assert L.w90g_project_overlap_noalloc(8, 4097, 1, ip, dummy, dummy, None) == 5
     assert L.w90g_project_overlap_noalloc(8, 1000, 9, ip, dummy, dummy, None) == 5
+    # an nnkp entry that names no k-point would be a gather index outside U on the GPU
+    for bad in (0, 3, -1):
+        table = np.ones(8, dtype=np.int32)
+        table[5] = bad
+        tp = table.ctypes.data_as(C.POINTER(C.c_int))
+        assert L.w90g_project_overlap_noalloc(8, 2, 4, tp, dummy, dummy, None) == 5

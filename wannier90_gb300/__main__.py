@@ -35,10 +35,10 @@ def run(seedname, precision="tensor"):
         raise SystemExit("restart = %s: only restart = wannierise is supported" % restart)
     opts.setdefault("iprint", 1)
     opts["gpu_tensor"] = 1 if precision == "tensor" else 0
-    c = w90.setup(kpoints=kpts, unit_cell_cart=lattice, num_wann=nw, num_bands=nb, mp_grid=mp, **opts)
     K = len(kpts)
     if restart == "wannierise":
-        return _restart_wannierise(c, seedname, nb, nw, lattice, kpts, mp, exclude)
+        return _restart_wannierise(seedname, nb, nw, lattice, kpts, mp, exclude, opts)
+    c = w90.setup(kpoints=kpts, unit_cell_cart=lattice, num_wann=nw, num_bands=nb, mp_grid=mp, **opts)
     if opts.get("site_symmetry"):
         # sitesym_read after the input (src/wannier_prog.F90:174-177)
         w90.check(c, w90.w90_set_sitesym(c, w90io.read_dmn(seedname + ".dmn", nw)), "sitesym_read")
@@ -62,6 +62,12 @@ def run(seedname, precision="tensor"):
             lwindow[nfirst[k]:nfirst[k] + ndim[k], k] = True
         dis = dict(omega_invariant=w90.w90_get_dis_info(c)["omega_invariant"], lwindow=lwindow, ndimwin=ndim,
                    u_opt=uopt)
+        # the 'postdis' checkpoint (src/wannier_prog.F90:264-266): U_opt, windows and the
+        # rotated num_wann x num_wann overlaps, from which restart = wannierise continues
+        w90io.write_chk(seedname + ".chk", num_bands=nb, lattice=lattice, kpts=kpts,
+                        mp_grid=mp if mp is not None else (0, 0, 0), nntot=w90.w90_get_nn(c), num_wann=nw,
+                        u=u, m=np.asfortranarray(m[:nw, :nw]), centres=np.zeros((3, nw)),
+                        spreads=np.zeros(nw), dis=dis, exclude_bands=exclude, checkpoint="postdis")
     else:
         u = np.asfortranarray(a[:, :nw, :].copy())
         uopt = np.asfortranarray(np.broadcast_to(np.eye(nb, nw, dtype=np.complex128)[:, :, None],
@@ -81,18 +87,31 @@ def run(seedname, precision="tensor"):
     return ierr
 
 
-def _restart_wannierise(c, seedname, nb, nw, lattice, kpts, mp, exclude):
+def _restart_wannierise(seedname, nb, nw, lattice, kpts, mp, exclude, opts):
     """restart = wannierise: wann_main continues from the U and M of seedname.chk (the
     reference reads the checkpoint instead of the overlaps and the projections,
-    src/wannier_prog.F90)."""
+    src/wannier_prog.F90:204-235).  The symmetry data are read first, as sitesym_read
+    comes before the restart branch (src/wannier_prog.F90:174-177).  A checkpoint
+    written after a disentanglement ('postdis', or a finished entangled run) holds the
+    num_wann x num_wann overlaps of the optimal subspace: wann_main runs on them, and its
+    U_opt, windows and Omega_I go into the new checkpoint unchanged."""
     chk = w90io.read_chk(seedname + ".chk")
-    if chk["num_wann"] != nw or chk["num_kpts"] != len(kpts):
+    K = len(kpts)
+    if chk["num_wann"] != nw or chk["num_kpts"] != K:
         raise SystemExit("restart: %s.chk does not match the .win (num_wann / k-points)" % seedname)
+    dis = None
     if chk.get("have_disentangled"):
-        raise SystemExit("restart: a disentangled checkpoint needs the disentanglement data, not supported")
+        if chk["num_bands"] != nb:
+            raise SystemExit("restart: %s.chk does not match the .win (num_bands)" % seedname)
+        dis = dict(omega_invariant=chk["omega_invariant"], lwindow=chk["lwindow"], ndimwin=chk["ndimwin"],
+                   u_opt=chk["u_opt"])
+    # the overlaps of the checkpoint are num_wann x num_wann blocks
+    c = w90.setup(kpoints=kpts, unit_cell_cart=lattice, num_wann=nw, num_bands=nw, mp_grid=mp, **opts)
+    if opts.get("site_symmetry"):
+        w90.check(c, w90.w90_set_sitesym(c, w90io.read_dmn(seedname + ".dmn", nw)), "sitesym_read")
     u = np.asfortranarray(chk["u"].astype(np.complex128))
     m = np.asfortranarray(chk["m"].astype(np.complex128))
-    uopt = np.asfortranarray(np.broadcast_to(np.eye(nb, nw, dtype=np.complex128)[:, :, None], (nb, nw, len(kpts))).copy())
+    uopt = np.asfortranarray(np.broadcast_to(np.eye(nw, dtype=np.complex128)[:, :, None], (nw, nw, K)).copy())
     w90.w90_set_m_local(c, m)
     w90.w90_set_u_matrix(c, u)
     w90.w90_set_u_opt(c, uopt)
@@ -100,7 +119,8 @@ def _restart_wannierise(c, seedname, nb, nw, lattice, kpts, mp, exclude):
     w90.check(c, ierr, "w90_wannierise")
     w90io.write_chk(seedname + ".chk", num_bands=nb, lattice=lattice, kpts=kpts,
                     mp_grid=mp if mp is not None else (0, 0, 0), nntot=w90.w90_get_nn(c), num_wann=nw, u=u, m=m,
-                    centres=w90.w90_get_centres(c, nw), spreads=w90.w90_get_spreads(c, nw), exclude_bands=exclude)
+                    centres=w90.w90_get_centres(c, nw), spreads=w90.w90_get_spreads(c, nw), dis=dis,
+                    exclude_bands=exclude)
     return ierr
 
 

@@ -188,8 +188,12 @@ __device__ bool oz_cmm(OzCtx& cx, double2* C, const double2* A, const double2* B
                      :: "r"(cx.mbar) : "memory");
       }
       const bool ok_mine = mbar_wait(cx.mbar, cx.phase);
+      if (!ok_mine) {
+        // record the error; drain the MMAs before tensor memory or the operands are reused
+        *cx.bad = 1;
+        mbar_drain(cx.mbar, cx.phase);
+      }
       cx.phase ^= 1u;
-      if (!ok_mine) *cx.bad = 1;
       __syncthreads();
       ok = (*cx.bad == 0);
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -399,8 +403,11 @@ __device__ bool oz_cmm2(OzCtx& cx, double2* C, const double2* A, const double2* 
                    :: "r"(cx.mbar) : "memory");
     }
     const bool ok_mine = mbar_wait(cx.mbar, cx.phase);
+    if (!ok_mine) {
+      *cx.bad = 1;
+      mbar_drain(cx.mbar, cx.phase);
+    }
     cx.phase ^= 1u;
-    if (!ok_mine) *cx.bad = 1;
     __syncthreads();
     ok = (*cx.bad == 0);
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");

@@ -215,11 +215,11 @@ __global__ void __launch_bounds__(256, 1) k_oz_mupdate(const Problem* __restrict
         }
         if (NCH > 1) slice_b(nc, kc);
         if (presliced) {
-          // bounded wait; on a timeout, a second bounded wait lets the copies in flight land
-          // before the CTA gives up its shared memory
+          // bounded wait; on a timeout the error is recorded and the drain wait lets the
+          // copies in flight land before the CTA gives up its shared memory
           if (!mbar_wait(smem_u32(&mbar_ld), phase_ld)) {
             s_bad = 1;
-            mbar_wait(smem_u32(&mbar_ld), phase_ld);
+            mbar_drain(smem_u32(&mbar_ld), phase_ld);
           }
           phase_ld ^= 1u;
         }
@@ -259,8 +259,13 @@ __global__ void __launch_bounds__(256, 1) k_oz_mupdate(const Problem* __restrict
                        :: "r"(smem_u32(&mbar)) : "memory");
         }
         const bool ok_mine = mbar_wait(smem_u32(&mbar), phase);
+        if (!ok_mine) {
+          // the MMAs may still run: record the error, then wait (drain limit) for their
+          // commit before the CTA reads or frees tensor memory or reuses the operands
+          s_bad = 1;
+          mbar_drain(smem_u32(&mbar), phase);
+        }
         phase ^= 1u;
-        if (!ok_mine) s_bad = 1;
         __syncthreads();
         ok = (s_bad == 0);   // uniform across the CTA
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");

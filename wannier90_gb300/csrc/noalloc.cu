@@ -7,7 +7,8 @@
 // few bytes of descriptor and the per-block statistics the kernels write live in one
 // file-scope device array instead of a cudaMalloc'd arena.
 //
-// Limits: num_wann <= 32, num_kpts <= 4096, num_kpts * nntot <= 8192.  The array holds
+// Limits: num_wann <= 32, num_kpts <= 4096, num_kpts * nntot <= 8192, every nnkp entry in
+// 1..num_kpts (anything else returns 5 before the GPU is touched).  The array holds
 // about 4.2 MB and stays allocated on every GPU that loads the library until the process
 // exits.  All calls share it: two calls whose work overlaps on the GPU (different
 // streams, or different host threads) race on it.
@@ -60,14 +61,16 @@ __global__ void k_noalloc_nnlist(int K, int B) {
   }
 }
 
-// Once per device, with that device current: resolve the scratch address and raise the
-// dynamic shared-memory limit of the two kernels (no allocation involved).
+// On every call, with the device current: resolve the scratch address (no allocation
+// involved) and, when it differs from the one this device had before -- the first call,
+// or a new primary context after cudaDeviceReset -- raise the dynamic shared-memory limit
+// of the two kernels again.
 int setup_device(int dev, NoAllocScratch** out) {
   std::lock_guard<std::mutex> lk(g_setup_mu);
   if (dev < 0 || dev >= kNaMaxDev) return 1;
-  if (!g_scratch_addr[dev]) {
-    void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return 1;
+  void* p = nullptr;
+  if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return 1;
+  if (g_scratch_addr[dev] != p) {
     const int smem = 4 * kNaMaxW * kNaMaxW * 16;
     if (cudaFuncSetAttribute(k_lowdin, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
       return 1;
@@ -88,7 +91,12 @@ extern "C" int w90g_project_overlap_noalloc(int num_wann, int num_kpts, int nnto
   if (num_wann < 1 || num_wann > kNaMaxW || num_kpts < 1 || num_kpts > kNaMaxK || nntot < 1 ||
       nntot > 12 || (long long)num_kpts * nntot > kNaMaxKB || !nnkp || !d_m_matrix || !d_u_matrix)
     return 5;   // sizes beyond the scratch array, or missing buffers
-  cudaGetLastError();   // clear a stale error so the checks below see only this call's
+  // the table is a gather index on the GPU: every entry must name a k-point (1-based)
+  for (long long i = 0; i < (long long)num_kpts * nntot; ++i)
+    if (nnkp[i] < 1 || nnkp[i] > num_kpts) return 5;
+  // an error left pending by earlier work of the caller is not cleared here: it is
+  // reported as a failure of this call and stays pending for the caller to read
+  if (cudaPeekAtLastError() != cudaSuccess) return 1;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return 1;
   NoAllocScratch* s = nullptr;

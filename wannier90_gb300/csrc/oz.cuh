@@ -203,18 +203,41 @@ __device__ __forceinline__ double recombine7x8(const uint32_t* dd, int stride, i
   return int64_scaled_to_double(hi, sc + 24) + int64_scaled_to_double(lo, sc);
 }
 
+// Spin limits of the mbarrier waits.  A wait that runs out of W90G_SPIN_LIMIT tries makes
+// the kernel record an error; before it leaves, the kernel waits again (up to
+// W90G_DRAIN_LIMIT tries) for the asynchronous work it has issued -- MMAs tracked by a
+// commit, bulk copies tracked by a transaction count -- so that no MMA or copy still
+// writes shared or tensor memory that the CTA gives back.  A test build sets a tiny
+// W90G_SPIN_LIMIT to drive that path.
+#ifndef W90G_SPIN_LIMIT
+#define W90G_SPIN_LIMIT (1 << 20)
+#endif
+#ifndef W90G_DRAIN_LIMIT
+#define W90G_DRAIN_LIMIT (1 << 22)
+#endif
+
+__device__ __forceinline__ bool mbar_try(uint32_t addr, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(addr), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// the drain after a timed-out wait: the same phase, the long limit
+__device__ __forceinline__ bool mbar_drain(uint32_t addr, uint32_t parity) {
+  for (int it = 0; it < W90G_DRAIN_LIMIT; ++it)
+    if (mbar_try(addr, parity)) return true;
+  return false;
+}
+
 __device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t parity) {
-  for (int it = 0; it < (1 << 20); ++it) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(addr), "r"(parity)
-        : "memory");
-    if (ok) return true;
-  }
+  for (int it = 0; it < W90G_SPIN_LIMIT; ++it)
+    if (mbar_try(addr, parity)) return true;
   return false;
 }
 

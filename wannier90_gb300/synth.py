@@ -112,9 +112,11 @@ def _tb_bands(rng, kind, a, mp, norb, rmax, onsite=None):
     return A, kp, tau, Ek, Ck
 
 
-def _tb_overlaps(A, kp, tau, Ck, search_shells):
-    """M_mn(k,b) = sum_a conj(C_am(k)) C_an(k+b) e^{-i b.tau_a} on the engine's k-mesh."""
-    B, nnlist, nncell, bk = kmesh_tables(A, kp, search_shells)
+def _tb_overlaps(A, kp, tau, Ck, search_shells, kmesh=None):
+    """M_mn(k,b) = sum_a conj(C_am(k)) C_an(k+b) e^{-i b.tau_a} on the engine's k-mesh
+    (or on the tables ``kmesh(real_lattice, kpoints, search_shells)`` returns, a
+    (B, nnlist, nncell, bk) tuple in kmesh_tables' layout)."""
+    B, nnlist, nncell, bk = (kmesh or kmesh_tables)(A, kp, search_shells)
     phase = np.exp(-1j * np.einsum("kbi,ai->kba", bk, tau))        # (K,B,norb)
     Ckp = Ck[nnlist]                                               # (K,B,norb,norb)
     M = np.conj(Ck)[:, None].transpose(0, 1, 3, 2) @ (phase[..., None] * Ckp)   # [k,b,m,n]
@@ -130,12 +132,14 @@ def _random_unitaries(rng, K, W, eps):
 
 
 def make_problem(kind="sc", a=5.0, mp=(4, 4, 4), num_wann=8, rmax=2, eps=0.3, seed=0,
-                 search_shells=36) -> TBProblem:
+                 search_shells=36, kmesh=None) -> TBProblem:
+    """``kmesh``: optional k-mesh builder with kmesh_tables' signature and result; by
+    default the engine's own (which loads the C library)."""
     rng = np.random.Generator(np.random.PCG64(seed))
     W = int(num_wann)
     A, kp, tau, _, Ck = _tb_bands(rng, kind, a, mp, W, rmax)
     K = len(kp)
-    B, nnlist, nncell, bk, M = _tb_overlaps(A, kp, tau, Ck, search_shells)
+    B, nnlist, nncell, bk, M = _tb_overlaps(A, kp, tau, Ck, search_shells, kmesh)
     # projections
     Ek = _random_unitaries(rng, K, W, eps)
     Amat = np.conj(np.swapaxes(Ck, 1, 2)) @ Ek                     # [k,m,n]
