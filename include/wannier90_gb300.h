@@ -62,11 +62,57 @@ void cset_option_floatxy(void* handle, const char* keyword, const double* values
  * gamma_only, conv_noise_amp > 0 and dis_spheres_num > 0 give ierr 5. */
 void cinput_setopt(void* handle, const char* seedname, int* ierr, int comm);
 
+/* ---- .win input: cinput_reader, src/c_interface.F90:70-80 (w90_input_reader,
+ *      src/library_interface.F90:294-360) --------------------------------------------
+ * After cinput_setopt: reads seedname.win (the seedname given to cinput_setopt) with the
+ * reference's tokenizer rules (lower case, '!' and '#' comments, `key = value`,
+ * `key : value` or `key value`, begin/end blocks); a keyword outside the set wannier90.x
+ * and postw90.x accept (src/readwrite.F90:903-1176, plus the engine's gpu_* keys), or one
+ * given twice, gives ierr 5 with the reference's message.  Keywords of the .win take
+ * precedence over earlier options; the system (num_wann, num_bands, mp_grid,
+ * unit_cell_cart, kpoints) must agree with cinput_setopt's (else 5); the setup is then
+ * redone with the merged options.  Called before cinput_setopt or with options set
+ * since: ierr 1.  File missing: 6. */
+void cinput_reader(void* handle, int* ierr);
+/* cinput_reader_special (src/wannier90.hh:11, declared there without a definition in
+ * src/c_interface.F90): the whole input, system included, from seedname.win -- the file
+ * form of cset_option_* + cinput_setopt.  unit_cell_cart may give `bohr` or `ang` units;
+ * projection-derived tables (guiding_centres_frac, slwf_centres_frac) still come through
+ * cset_option_floatxy.  ierr as cinput_setopt / cinput_reader. */
+void cinput_reader_special(void* handle, const char* seedname, int* ierr);
+
 /* ---- data pointers (caller keeps ownership): src/c_interface.F90:82-127 ----------- */
 void cset_eigval(void* handle, double* eigval);
 void cset_m_local(void* handle, double* m_matrix);
 void cset_u_matrix(void* handle, double* u_matrix);
 void cset_u_opt(void* handle, double* u_opt);
+
+/* cset_a_matrix (src/wannier90.hh:31): the caller's projections A_mn(k), complex
+ * [nk][nw][nb].  coverlaps reads seedname.amn into it; cproject_overlap (nb = nw) and
+ * cdisentangle copy it into u_matrix / u_opt before they start. */
+void cset_a_matrix(void* handle, double* a_matrix);
+/* cset_kpoint_distribution (src/wannier90.hh:28; set_kpoint_distribution,
+ * src/wannier_prog.F90:798-820): dist[nk] = the rank owning each k-point.  The engine is
+ * one process on one GPU: the all-zero distribution is accepted, any other makes the next
+ * work call (coverlaps, cproject_overlap, cdisentangle, cwannierise) return 5. */
+void cset_kpoint_distribution(void* handle, const int* dist);
+/* cset_parallel_comms (src/wannier90.hh:29): the MPI communicator (Fortran handle);
+ * stored, not used (no collective runs: every k-point is on this GPU). */
+void cset_parallel_comms(void* handle, int comm);
+/* coverlaps (src/wannier90.hh:21; overlaps, src/wannier_prog.F90:478-537): reads
+ * seedname.mmn into m_local and seedname.amn into the projections -- the cset_a_matrix
+ * buffer if set, else u_matrix (nb = nw) or u_opt (nb > nw) -- with overlap_read's checks
+ * and messages (src/overlap.F90:234-366).  ierr: 1 when called before cinput_setopt or a
+ * buffer is missing, 6 for a file error. */
+void coverlaps(void* handle, int* ierr);
+/* cchkpt (src/wannier90.hh:9; write_chkpt, src/wannier_prog.F90:575-700): writes
+ * seedname.chk, checkpoint label `label` ("postdis", "postwann"), in the unformatted
+ * layout of w90_wannier90_readwrite_write_chkpt (src/wannier90_readwrite.F90:2278-2373):
+ * exclude_bands, lattice, k-points, u_matrix, u_opt, the leading nw x nw block of every
+ * m_local block, centres and spreads of the last wannierisation, and after a
+ * disentanglement Omega_I, lwindow and ndimwin.  No ierr (as the prototype): failures
+ * (missing buffers, file errors) are reported by w90g_last_error. */
+void cchkpt(void* handle, const char* label);
 
 /* ---- work: src/c_interface.F90:38-47 (cwannierise -> w90_wannierise ->
  *      wann_main, src/library_interface.F90:464-530) ----------------------------------
@@ -272,6 +318,13 @@ inline void cset_option(void* blob, std::string key, double x) { cset_option_flo
 inline void cset_option(void* blob, std::string key, double* x, int i1, int i2) {
   cset_option_floatxy(blob, key.c_str(), x, i1, i2);
 }
+inline void cinput_reader(void* blob, int& ierr) { cinput_reader(blob, &ierr); }
+inline void cinput_reader_special(void* blob, std::string seed, int& ierr) {
+  cinput_reader_special(blob, seed.c_str(), &ierr);
+}
+inline void cchkpt(void* blob, std::string label) { cchkpt(blob, label.c_str()); }
+inline void coverlaps(void* blob, int& ierr) { coverlaps(blob, &ierr); }
+inline void cset_a_matrix(void* blob, std::complex<double>* a) { cset_a_matrix(blob, reinterpret_cast<double*>(a)); }
 inline void cdisentangle(void* blob, int& ierr) { cdisentangle(blob, &ierr); }
 inline void cwannierise(void* blob, int& ierr) { cwannierise(blob, &ierr); }
 inline void cproject_overlap(void* blob, int& ierr) { cproject_overlap(blob, &ierr); }

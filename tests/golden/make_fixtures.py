@@ -488,6 +488,31 @@ def parse_chk_fmt(lines):
     return W, nntot, nk, np.ascontiguousarray(u), np.ascontiguousarray(m)
 
 
+def parse_chk_fmt_records(lines, W, nntot, nk):
+    """The records of a formatted checkpoint other than u and m, in file order: header,
+    num_bands, exclude_bands, the real and reciprocal lattice as the nine numbers of their
+    records, mp_grid, the checkpoint label, have_disentangled, centres and spreads
+    (src/wannier90_readwrite.F90:2336-2366)."""
+    i = 0
+    header = lines[i]; i += 1
+    nb = int(lines[i]); i += 1
+    nex = int(lines[i]); i += 1
+    exclude = np.array([int(x) for x in lines[i].split()], dtype=np.int64) if nex > 0 else np.zeros(0, np.int64)
+    i += 1 if nex > 0 else 0
+    lat9 = np.array([float(x) for x in lines[i].split()]); i += 1
+    rec9 = np.array([float(x) for x in lines[i].split()]); i += 1
+    i += 1                                        # num_kpts
+    mp = np.array([int(x) for x in lines[i].split()]); i += 1
+    i += nk + 2                                   # k-points, nntot, num_wann
+    label = lines[i].strip(); i += 1
+    have_dis = int(lines[i]); i += 1
+    i += W * W * nk + W * W * nntot * nk
+    cen = np.array([[float(x) for x in l.split()] for l in lines[i:i + W]]); i += W
+    spr = np.array([float(l.split()[0]) for l in lines[i:i + W]])
+    return dict(chk_header=header, chk_num_bands=nb, chk_exclude=exclude, chk_lattice9=lat9, chk_recip9=rec9,
+                chk_mp_grid=mp, chk_label=label, chk_have_dis=have_dis, chk_centres=cen, chk_spreads=spr)
+
+
 def build_restart(ref_root, out_dir):
     """testw90_example02_restart: lead, restart = wannierise from the converged checkpoint
     the test ships (lead.chk.fmt.bz2), 20 more iterations."""
@@ -508,7 +533,7 @@ def build_restart(ref_root, out_dir):
         num_kpts=nk, nntot=nntot, u=u, m=m,
         knobs=np.array([knobs[k] for k in sorted(knobs)], dtype=np.float64), knob_names=np.array(sorted(knobs)),
         conv=conv, centres_final=final, omega_final=np.array([om["om_i"], om["om_d"], om["om_od"], om["om_tot"]]),
-        bvec_table=bvec)
+        bvec_table=bvec, **parse_chk_fmt_records(lines, W, nntot, nk))
     print("restart02", W, nntot, nk, conv.shape, om)
 
 

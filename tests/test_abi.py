@@ -30,3 +30,18 @@ def test_library_exports_every_declared_symbol():
         assert hasattr(L, n), n
     bound = {s[0] for s in _native.SIGNATURES}
     assert names == bound, (names ^ bound)
+
+
+def test_fortran_shim_binds_every_declared_symbol():
+    """include/wannier90_gb300.F90 (the iso_c_binding module for Fortran hosts) has an
+    interface block for every entry point of the C header, under its C name, and the
+    w90_library module keeps the reference's procedure names for the wannierisation path
+    (src/library_interface.F90:101-136)."""
+    txt = open(os.path.join(ROOT, "include", "wannier90_gb300.F90")).read()
+    bound = set(re.findall(r'bind\(c, name="([a-z_0-9]+)"\)', txt))
+    assert _declared() <= bound, _declared() - bound
+    for name in ("w90_set_option", "w90_input_setopt", "w90_input_reader", "w90_get_nn", "w90_get_nnkp",
+                 "w90_get_gkpb", "w90_set_m_local", "w90_set_u_matrix", "w90_set_u_opt", "w90_set_eigval",
+                 "w90_disentangle", "w90_project_overlap", "w90_wannierise", "w90_get_centres", "w90_get_spreads",
+                 "w90_create_kmesh"):
+        assert re.search(r"subroutine %s\b" % name, txt) or re.search(r"interface %s\b" % name, txt), name

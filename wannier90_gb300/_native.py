@@ -24,6 +24,13 @@ SIGNATURES = [
     ("cset_option_float33", None, [C.c_void_p, C.c_char_p, _c_double_p]),
     ("cset_option_floatxy", None, [C.c_void_p, C.c_char_p, _c_double_p, C.c_int, C.c_int]),
     ("cinput_setopt", None, [C.c_void_p, C.c_char_p, _c_int_p, C.c_int]),
+    ("cinput_reader", None, [C.c_void_p, _c_int_p]),
+    ("cinput_reader_special", None, [C.c_void_p, C.c_char_p, _c_int_p]),
+    ("cset_a_matrix", None, [C.c_void_p, C.c_void_p]),
+    ("cset_kpoint_distribution", None, [C.c_void_p, _c_int_p]),
+    ("cset_parallel_comms", None, [C.c_void_p, C.c_int]),
+    ("coverlaps", None, [C.c_void_p, _c_int_p]),
+    ("cchkpt", None, [C.c_void_p, C.c_char_p]),
     ("cset_eigval", None, [C.c_void_p, C.c_void_p]),
     ("cset_m_local", None, [C.c_void_p, C.c_void_p]),
     ("cset_u_matrix", None, [C.c_void_p, C.c_void_p]),

@@ -28,6 +28,7 @@
 #include "kmesh.h"
 #include "seedio.h"
 #include "sym_tables.h"
+#include "winfile.h"
 
 namespace {
 
@@ -100,6 +101,16 @@ struct Handle {
   double omega[4] = {0, 0, 0, 0};
   std::vector<double> centres, spreads, log, log_centres;
   int niter = 0;
+  // library-mode bookkeeping: the seedname of cinput_setopt (files of cinput_reader,
+  // coverlaps, cchkpt), the options it consumed (cinput_reader adds the .win keywords
+  // to them), the optional projections buffer of cset_a_matrix, exclude_bands for the
+  // checkpoint, and a rejected k-point distribution (reported by the next work call)
+  std::string seedname;
+  std::map<std::string, Opt> applied_opts;
+  double* a_matrix = nullptr;
+  std::vector<int> exclude_bands;
+  std::string dist_error;
+  int comm = 0;
   // engine
   std::unique_ptr<Engine> eng;
   cudaStream_t stream = nullptr;
@@ -271,6 +282,130 @@ int fail(Handle* h, int code, const std::string& msg) {
   return code;
 }
 
+// ---- .win keywords -> options (cinput_reader / cinput_reader_special) ----------------
+// How the engine reads each keyword it uses; keywords it does not use are accepted
+// (read_win checks them against the reference's set) and left alone.
+const char* const kWinInts[] = {"num_wann", "num_bands", "num_iter", "num_cg_steps", "conv_window",
+                                "search_shells", "iprint", "num_print_cycles", "conv_noise_num", "dis_num_iter",
+                                "dis_conv_window", "dis_spheres_num", "slwf_num", "num_no_guide_iter",
+                                "num_guide_cycles", "optimisation", "timing_level", "num_dump_cycles"};
+const char* const kWinReals[] = {"conv_tol", "trial_step", "fixed_step", "conv_noise_amp", "kmesh_tol",
+                                 "dis_win_min", "dis_win_max", "dis_froz_min", "dis_froz_max", "dis_mix_ratio",
+                                 "dis_conv_tol", "slwf_lambda", "symmetrize_eps", "ws_distance_tol"};
+const char* const kWinLogicals[] = {"precond", "guiding_centres", "gamma_only", "slwf_constrain",
+                                    "site_symmetry"};
+
+bool in_list(const std::string& k, const char* const* list, size_t n) {
+  for (size_t i = 0; i < n; ++i)
+    if (k == list[i]) return true;
+  return false;
+}
+
+Opt make_opt(const std::vector<double>& v, int rows, int cols, bool is_int) {
+  Opt o;
+  o.v = v;
+  o.rows = rows;
+  o.cols = cols;
+  o.is_int = is_int;
+  return o;
+}
+
+// Options of a tokenized .win, as cset_option_* would set them.  Returns 0 or 5 (err).
+int win_options(const w90g::WinFile& w, std::map<std::string, Opt>& out, std::string& err) {
+  out.clear();
+  for (const auto& kv : w.keys) {
+    const std::string& k = kv.first;
+    const std::string& t = kv.second;
+    const bool engine_int = k.compare(0, 4, "gpu_") == 0;
+    if (engine_int || in_list(k, kWinInts, sizeof kWinInts / sizeof *kWinInts)) {
+      int x;
+      if (!w90g::parse_int(t, x)) {
+        err = "Error: Problem reading keyword " + k;
+        return 5;
+      }
+      out[k] = make_opt({(double)x}, 1, 1, true);
+    } else if (in_list(k, kWinReals, sizeof kWinReals / sizeof *kWinReals)) {
+      double x;
+      if (!w90g::parse_real(t, x)) {
+        err = "Error: Problem reading keyword " + k;
+        return 5;
+      }
+      out[k] = make_opt({x}, 1, 1, false);
+    } else if (in_list(k, kWinLogicals, sizeof kWinLogicals / sizeof *kWinLogicals)) {
+      bool b;
+      if (!w90g::parse_logical(t, b)) {
+        err = "Error: Problem reading logical keyword " + k;
+        return 5;
+      }
+      out[k] = make_opt({b ? 1.0 : 0.0}, 1, 1, true);
+    } else if (k == "mp_grid" || k == "ws_search_size") {
+      std::vector<double> x;
+      if (!w90g::parse_reals(t, x) || (k == "mp_grid" && x.size() != 3)) {
+        err = "Error: Problem reading keyword " + k;
+        return 5;
+      }
+      out[k] = make_opt(x, 1, (int)x.size(), true);
+    } else if (k == "exclude_bands") {
+      std::vector<int> r;
+      if (!w90g::parse_range_vector(t, r)) {
+        err = "Error: Problem reading keyword exclude_bands";
+        return 5;
+      }
+      out[k] = make_opt(std::vector<double>(r.begin(), r.end()), 1, (int)r.size(), true);
+    }
+  }
+  auto cell = w.blocks.find("unit_cell_cart");
+  if (cell != w.blocks.end()) {
+    std::vector<std::string> rows = cell->second;
+    double scale = 1.0;
+    if (!rows.empty() && (rows[0].compare(0, 4, "bohr") == 0 || rows[0].compare(0, 3, "ang") == 0)) {
+      if (rows[0].compare(0, 4, "bohr") == 0) scale = w90g::kBohrAngstrom;
+      rows.erase(rows.begin());
+    }
+    std::vector<double> a;
+    for (const auto& r : rows) {
+      std::vector<double> x;
+      if (!w90g::parse_reals(r, x) || x.size() < 3) {
+        err = "Error: Problem reading block keyword unit_cell_cart";
+        return 5;
+      }
+      for (int i = 0; i < 3; ++i) a.push_back(x[i] * scale);
+    }
+    if (a.size() != 9) {
+      err = "Error: Wrong number of lines in block unit_cell_cart";
+      return 5;
+    }
+    out["unit_cell_cart"] = make_opt(a, 3, 3, false);
+  }
+  auto kp = w.blocks.find("kpoints");
+  if (kp != w.blocks.end()) {
+    std::vector<double> a;
+    for (const auto& r : kp->second) {
+      std::vector<double> x;
+      if (!w90g::parse_reals(r, x) || x.size() < 3) {
+        err = "Error: Problem reading block keyword kpoints";
+        return 5;
+      }
+      for (int i = 0; i < 3; ++i) a.push_back(x[i]);
+    }
+    out["kpoints"] = make_opt(a, (int)a.size() / 3, 3, false);
+  }
+  return 0;
+}
+
+bool same_values(const Opt& a, const Opt& b) {
+  if (a.v.size() != b.v.size()) return false;
+  for (size_t i = 0; i < a.v.size(); ++i)
+    if (std::fabs(a.v[i] - b.v[i]) > 1e-10 * std::max(1.0, std::fabs(a.v[i]))) return false;
+  return true;
+}
+
+// the k-point distribution a single-GPU engine can honour: every k on rank 0
+int check_distribution(Handle* h) {
+  if (!h->dist_error.empty()) return fail(h, 5, h->dist_error);
+  return 0;
+}
+
 int build_spec(Handle* h, ProblemSpec& s) {
   s.W = h->num_wann;
   s.K = h->num_kpts;
@@ -334,6 +469,7 @@ const char* kSymMissing = "site_symmetry = T needs the symmetry data of the .dmn
 
 int do_project(Handle* h, double* m, double* u, cudaMemcpyKind in, cudaMemcpyKind out) {
   if (!h->setup_complete) return fail(h, 1, "cinput_setopt must be called before cproject_overlap");
+  if (check_distribution(h)) return 5;
   if (sym_missing(h)) return fail(h, 6, kSymMissing);
   if (!m) return fail(h, 1, "m_matrix_local not set for projovlp call");
   if (!u) return fail(h, 1, "u_matrix not set for projovlp call");
@@ -375,6 +511,7 @@ int apply_result(Handle* h, const w90g::ProblemResult& r, bool print) {
 
 int do_wannierise(Handle* h, double* m, double* u, cudaMemcpyKind in, cudaMemcpyKind out) {
   if (!h->setup_complete) return fail(h, 1, "cinput_setopt must be called before cwannierise");
+  if (check_distribution(h)) return 5;
   if (sym_missing(h)) return fail(h, 6, kSymMissing);
   if (!m) return fail(h, 1, "m_matrix_local not set for wannierise");
   if (!u) return fail(h, 1, "u_matrix not set for wannierise");
@@ -399,6 +536,7 @@ int do_wannierise(Handle* h, double* m, double* u, cudaMemcpyKind in, cudaMemcpy
 int do_disentangle(Handle* h, double* m, double* uopt, double* u, const double* eig, bool device, double* prof_ms,
                    int* prof_counts) {
   if (!h->setup_complete) return fail(h, 1, "cinput_setopt must be called before cdisentangle");
+  if (check_distribution(h)) return 5;
   if (!m) return fail(h, 1, "m_matrix_local not associated for disentangle call");
   if (!u) return fail(h, 1, "u_matrix not associated for disentangle call");
   if (!uopt) return fail(h, 1, "u_opt not associated for disentangle call");
@@ -673,8 +811,6 @@ void cset_option_floatxy(void* h, const char* key, const double* values, int x, 
 // w90_input_setopt (src/library_interface.F90:161-292) restricted to what wann_main uses;
 // keyword defaults of src/wannier90_types.F90:170-192 and src/wannier90_readwrite.F90:647-754.
 void cinput_setopt(void* hv, const char* seedname, int* ierr, int comm) {
-  (void)seedname;
-  (void)comm;
   Handle* h = H(hv);
   *ierr = 0;
   if (!h) {
@@ -684,6 +820,15 @@ void cinput_setopt(void* hv, const char* seedname, int* ierr, int comm) {
   if (h->opts.empty()) {
     *ierr = fail(h, 1, " input_setopt called with no input");
     return;
+  }
+  h->seedname = seedname ? seedname : "";
+  h->comm = comm;
+  h->applied_opts = h->opts;
+  h->exclude_bands.clear();
+  {
+    auto eit = h->opts.find("exclude_bands");
+    if (eit != h->opts.end())
+      for (double x : eit->second.v) h->exclude_bands.push_back((int)x);
   }
   double v;
   h->num_wann = get_num(h, "num_wann", v) ? (int)v : 0;
@@ -968,6 +1113,9 @@ void cset_u_opt(void* h, double* u) { H(h)->u_opt = u; }
 
 void cdisentangle(void* hv, int* ierr) {
   Handle* h = H(hv);
+  // projections given through cset_a_matrix are the initial u_opt (nb x nw x nk)
+  if (h->a_matrix && h->u_opt && h->setup_complete && h->a_matrix != h->u_opt)
+    std::memcpy(h->u_opt, h->a_matrix, sizeof(double) * 2 * h->num_bands * h->num_wann * h->num_kpts);
   *ierr = do_disentangle(h, h->m_local, h->u_opt, h->u_matrix, h->eigval, false, nullptr, nullptr);
 }
 
@@ -998,6 +1146,10 @@ void cwannierise(void* hv, int* ierr) {
 
 void cproject_overlap(void* hv, int* ierr) {
   Handle* h = H(hv);
+  // projections given through cset_a_matrix are A(k) (num_bands = num_wann here)
+  if (h->a_matrix && h->u_matrix && h->setup_complete && h->num_bands == h->num_wann &&
+      h->a_matrix != h->u_matrix)
+    std::memcpy(h->u_matrix, h->a_matrix, sizeof(double) * 2 * h->num_wann * h->num_wann * h->num_kpts);
   *ierr = do_project(h, h->m_local, h->u_matrix, cudaMemcpyHostToDevice, cudaMemcpyDeviceToHost);
 }
 
@@ -1395,6 +1547,210 @@ int w90g_read_eig(const char* path, int nb, int nk, double* eig, char* err, int 
 long long w90g_kernel_launches(void* hv) {
   Handle* h = H(hv);
   return (h->eng ? h->eng->launches() : 0) + h->dis_launches;
+}
+
+
+// ---- the remaining names of the reference's C++ prototypes (src/wannier90.hh:9-31) ----
+
+// cinput_reader -> w90_input_reader (src/c_interface.F90:70-80,
+// src/library_interface.F90:294-360): after cinput_setopt, the other keywords of
+// seedname.win; keywords the .win sets take precedence over earlier options, the system
+// (num_wann, num_bands, mp_grid, unit_cell_cart, kpoints) must agree with what
+// cinput_setopt received, and the setup (k-mesh, preconditioner tables, windows) is
+// redone with the merged options.
+void cinput_reader(void* hv, int* ierr) {
+  Handle* h = H(hv);
+  *ierr = 0;
+  if (!h) {
+    *ierr = 1;
+    return;
+  }
+  if (!h->opts.empty() || !h->setup_complete) {
+    *ierr = fail(h, 1, "Error: input reader called when unspent options present (setopt must be called first)");
+    return;
+  }
+  w90g::WinFile w;
+  std::string err;
+  int rc = w90g::read_win(h->seedname + ".win", w, err);
+  std::map<std::string, Opt> win;
+  if (!rc) rc = win_options(w, win, err);
+  if (rc) {
+    *ierr = fail(h, rc, err);
+    return;
+  }
+  std::map<std::string, Opt> merged = h->applied_opts;
+  for (const auto& kv : win) {
+    const std::string& k = kv.first;
+    const bool system = k == "num_wann" || k == "num_bands" || k == "mp_grid" || k == "unit_cell_cart" ||
+                        k == "kpoints";
+    if (system) {
+      auto it = merged.find(k);
+      if (it != merged.end() && !same_values(it->second, kv.second)) {
+        *ierr = fail(h, 5, "Error: " + k + " of " + h->seedname +
+                               ".win differs from the value set through the library");
+        return;
+      }
+    }
+    merged[k] = kv.second;
+  }
+  h->opts = merged;
+  h->setup_complete = false;
+  const std::string seed = h->seedname;
+  cinput_setopt(hv, seed.c_str(), ierr, h->comm);
+}
+
+// cinput_reader_special (src/wannier90.hh:11): the whole input, system included, from
+// seedname.win -- the file form of cset_option_* + cinput_setopt (wannier90.x reads it
+// with w90_wannier90_readwrite_read_special, src/library_interface.F90:203-218).
+void cinput_reader_special(void* hv, const char* seedname, int* ierr) {
+  Handle* h = H(hv);
+  *ierr = 0;
+  if (!h || !seedname) {
+    *ierr = 1;
+    return;
+  }
+  if (!h->opts.empty()) {
+    *ierr = fail(h, 1, "Error: (library use) options interface and .win parsing clash.  See library "
+                       "documentation \"setting options.\" (readwrite.F90)");
+    return;
+  }
+  w90g::WinFile w;
+  std::string err;
+  int rc = w90g::read_win(std::string(seedname) + ".win", w, err);
+  std::map<std::string, Opt> win;
+  if (!rc) rc = win_options(w, win, err);
+  if (rc) {
+    *ierr = fail(h, rc, err);
+    return;
+  }
+  h->opts = win;
+  cinput_setopt(hv, seedname, ierr, h->comm);
+}
+
+// cset_a_matrix (src/wannier90.hh:31): the caller's projections A_mn(k), complex
+// (num_bands, num_wann, num_kpts).  coverlaps reads seedname.amn into it; cproject_overlap
+// (isolated bands) and cdisentangle take their starting u_matrix / u_opt from it.
+void cset_a_matrix(void* hv, double* a) { H(hv)->a_matrix = a; }
+
+// cset_kpoint_distribution (src/wannier90.hh:28; set_kpoint_distribution,
+// src/wannier_prog.F90:798-820): the rank owning each k-point.  One process drives one
+// GPU and holds every k, so only the all-zero distribution is accepted; any other makes
+// the next cproject_overlap / cdisentangle / cwannierise return 5.
+void cset_kpoint_distribution(void* hv, const int* dist) {
+  Handle* h = H(hv);
+  h->dist_error.clear();
+  if (!dist) return;
+  if (!h->setup_complete) {
+    h->dist_error = "Error in k-point distribution: set after cinput_setopt (num_kpts unknown)";
+    return;
+  }
+  for (int k = 0; k < h->num_kpts; ++k)
+    if (dist[k] != 0) {
+      h->dist_error = "k-point distribution over several ranks is not supported by the single-GPU engine "
+                      "(every k-point must be on rank 0)";
+      return;
+    }
+}
+
+// cset_parallel_comms (src/wannier90.hh:29): the MPI communicator, kept and not used.
+void cset_parallel_comms(void* hv, int comm) { H(hv)->comm = comm; }
+
+// coverlaps (src/wannier90.hh:21; overlaps, src/wannier_prog.F90:478-537): read
+// seedname.mmn into m_matrix_local and seedname.amn into the projections -- the
+// cset_a_matrix buffer if one is set, else u_matrix (isolated) / u_opt (entangled) --
+// with overlap_read's checks and messages (src/overlap.F90:234-366).
+void coverlaps(void* hv, int* ierr) {
+  Handle* h = H(hv);
+  *ierr = 0;
+  if (!h->setup_complete) {
+    *ierr = fail(h, 1, "kmesh is not setup before calling overlaps read routine");
+    return;
+  }
+  if (check_distribution(h)) {
+    *ierr = 5;
+    return;
+  }
+  const bool entangled = h->num_bands > h->num_wann;
+  double* a = h->a_matrix ? h->a_matrix : (entangled ? h->u_opt : h->u_matrix);
+  if (!a) {
+    *ierr = fail(h, 1, entangled ? "u_opt not associated at overlaps read routine"
+                                 : "u_matrix not associated at overlaps read routine");
+    return;
+  }
+  if (!h->m_local) {
+    *ierr = fail(h, 1, "m_matrix_local not associated at overlaps read routine");
+    return;
+  }
+  char err[512] = {0};
+  int rc = w90g_read_mmn((h->seedname + ".mmn").c_str(), h->num_bands, h->num_kpts, h->km.nntot,
+                         h->km.nnlist.data(), h->km.nncell.data(), h->m_local, 0, err, (int)sizeof err);
+  if (!rc) rc = w90g_read_amn((h->seedname + ".amn").c_str(), h->num_bands, h->num_wann, h->num_kpts, a, 0, err,
+                              (int)sizeof err);
+  if (rc) *ierr = fail(h, rc, err);
+}
+
+// cchkpt (src/wannier90.hh:9; write_chkpt, src/wannier_prog.F90:575-700): write
+// seedname.chk with the checkpoint label (e.g. "postdis", "postwann") in the layout of
+// w90_wannier90_readwrite_write_chkpt (src/wannier90_readwrite.F90:2278-2373): the
+// caller's u_matrix, u_opt and the leading num_wann x num_wann block of every m_matrix
+// block, the centres and spreads of the last wannierisation, the windows and Omega_I of
+// the last disentanglement.  Errors go to w90g_last_error (the prototype returns none).
+void cchkpt(void* hv, const char* label) {
+  Handle* h = H(hv);
+  h->last_error.clear();
+  if (!h->setup_complete) {
+    fail(h, 1, "cinput_setopt must be called before write_chkpt");
+    return;
+  }
+  if (!h->u_opt) {
+    fail(h, 1, "u_opt not set for write_chkpt call");
+    return;
+  }
+  if (!h->u_matrix) {
+    fail(h, 1, "u_matrix not set for write_chkpt call");
+    return;
+  }
+  if (!h->m_local) {
+    fail(h, 1, "m_matrix_local not set for write_chkpt call");
+    return;
+  }
+  w90g::ChkData d;
+  char date[64];
+  const std::time_t now = std::time(nullptr);
+  std::tm tmv;
+  localtime_r(&now, &tmv);
+  // io_date's fields: day right-justified in 2, month abbreviation, year; hh:mm:ss
+  static const char* const months[] = {"Jan", "Feb", "Mar", "Apr", "May", "Jun",
+                                       "Jul", "Aug", "Sep", "Oct", "Nov", "Dec"};
+  std::snprintf(date, sizeof date, "written on %2d%s%04d at %02d:%02d:%02d ", tmv.tm_mday, months[tmv.tm_mon],
+                tmv.tm_year + 1900, tmv.tm_hour, tmv.tm_min, tmv.tm_sec);
+  d.header = date;
+  d.num_bands = h->num_bands;
+  d.num_kpts = h->num_kpts;
+  d.nntot = h->km.nntot;
+  d.num_wann = h->num_wann;
+  d.exclude_bands = h->exclude_bands;
+  std::memcpy(d.real_lattice, h->real_lattice, sizeof d.real_lattice);
+  for (int i = 0; i < 3; ++i) d.mp_grid[i] = h->mp_grid[i];
+  d.kpt_latt = h->kpt_latt.data();
+  d.checkpoint = label ? label : "postwann";
+  d.have_disentangled = h->have_disentangled;
+  if (h->have_disentangled) {
+    d.omega_invariant = h->omega_invariant;
+    d.ndimwin = h->dis_ndimwin;
+    d.lwindow.assign((size_t)h->num_bands * h->num_kpts, 0);
+    for (int k = 0; k < h->num_kpts; ++k)
+      for (int i = 0; i < h->dis_ndimwin[k]; ++i)
+        d.lwindow[(size_t)k * h->num_bands + h->dis_nfirstwin[k] + i] = 1;
+  }
+  d.u_opt = h->u_opt;
+  d.u = h->u_matrix;
+  d.m = h->m_local;
+  d.ldm = h->num_bands;
+  d.centres = h->centres.data();
+  d.spreads = h->spreads.data();
+  std::string err;
+  if (w90g::write_chk(h->seedname + ".chk", d, err)) fail(h, 6, err);
 }
 
 }  // extern "C"

@@ -110,6 +110,63 @@ def w90_input_setopt(common: LibCommon, seedname: str = "wannier", comm: int = 0
     return ierr.value
 
 
+def w90_input_reader(common: LibCommon) -> int:
+    """w90_input_reader (src/library_interface.F90:294-360): the remaining keywords of
+    seedname.win after w90_input_setopt (seedname as given there)."""
+    ierr = C.c_int(0)
+    common._L.cinput_reader(common._h, C.byref(ierr))
+    if ierr.value == 0:
+        nn = C.c_int(0)
+        common._L.cget_nn(common._h, C.byref(nn))
+        common.nntot = nn.value
+    return ierr.value
+
+
+def w90_input_reader_special(common: LibCommon, seedname: str) -> int:
+    """The whole input, system included, from seedname.win (cinput_reader_special)."""
+    ierr = C.c_int(0)
+    common._L.cinput_reader_special(common._h, seedname.encode(), C.byref(ierr))
+    if ierr.value == 0:
+        nn = C.c_int(0)
+        common._L.cget_nn(common._h, C.byref(nn))
+        common.nntot = nn.value
+    return ierr.value
+
+
+def w90_set_kpoint_distribution(common: LibCommon, dist):
+    """set_kpoint_distribution (src/wannier_prog.F90:798-820): only all-zero (one rank)
+    is accepted; anything else makes the next work call return 5."""
+    d = np.ascontiguousarray(dist, dtype=np.int32)
+    common._keep["dist"] = d
+    common._L.cset_kpoint_distribution(common._h, d.ctypes.data_as(C.POINTER(C.c_int)))
+
+
+def w90_set_parallel_comms(common: LibCommon, comm: int):
+    common._L.cset_parallel_comms(common._h, int(comm))
+
+
+def w90_set_a_matrix(common: LibCommon, a):
+    """The projections A (num_bands, num_wann, num_kpts): filled by w90_overlaps, the start
+    of w90_project_overlap (isolated) / w90_disentangle (entangled)."""
+    common._keep["a"] = _cplx(a)
+    common._L.cset_a_matrix(common._h, common._keep["a"].ctypes.data)
+
+
+def w90_overlaps(common: LibCommon) -> int:
+    """overlaps (src/wannier_prog.F90:478-537): seedname.mmn into m, seedname.amn into
+    the projections."""
+    ierr = C.c_int(0)
+    common._L.coverlaps(common._h, C.byref(ierr))
+    return ierr.value
+
+
+def w90_write_chkpt(common: LibCommon, label: str = "postwann") -> int:
+    """write_chkpt (src/wannier_prog.F90:575-700): seedname.chk; returns 0, or 1 with
+    the message in last_error()."""
+    common._L.cchkpt(common._h, label.encode())
+    return 1 if common.last_error() else 0
+
+
 def w90_get_nn(common: LibCommon) -> int:
     nn = C.c_int(0)
     common._L.cget_nn(common._h, C.byref(nn))
@@ -391,7 +448,8 @@ def check(common: LibCommon, ierr: int, what: str):
     return ierr
 
 
-def setup(*, kpoints, unit_cell_cart, num_wann, num_bands=None, mp_grid=None, **options) -> LibCommon:
+def setup(*, kpoints, unit_cell_cart, num_wann, num_bands=None, mp_grid=None, seedname="wannier",
+          **options) -> LibCommon:
     """wannier_setup-style helper (test-suite/libv2-demo/*/wannier.cc:5-34)."""
     c = w90_create()
     kp = np.asarray(kpoints, dtype=np.float64)
@@ -404,7 +462,7 @@ def setup(*, kpoints, unit_cell_cart, num_wann, num_bands=None, mp_grid=None, **
         w90_set_option(c, "mp_grid", np.asarray(mp_grid, dtype=np.int32))
     for k, v in options.items():
         w90_set_option(c, k, v)
-    check(c, w90_input_setopt(c), "w90_input_setopt")
+    check(c, w90_input_setopt(c, seedname), "w90_input_setopt")
     c.num_wann = int(num_wann)
     c.num_bands = int(num_bands or num_wann)
     c.num_kpts = int(kp.shape[0])
