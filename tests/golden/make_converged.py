@@ -28,7 +28,11 @@ import os
 import sys
 import time
 
-import numpy as np
+# one BLAS thread per process (set before numpy loads OpenBLAS; the workers inherit it)
+os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+os.environ.setdefault("OMP_NUM_THREADS", "1")
+
+import numpy as np  # noqa: E402
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
@@ -66,7 +70,6 @@ def problem(name):
 
 def run(job):
     name, rel, num_iter, conv_window = job
-    os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
     from oracle import w90_oracle as O
     t0 = time.time()
     km, U0, M0 = problem(name)

@@ -89,7 +89,10 @@ SIGNATURES = [
 
 
 def lib_path():
-    return os.path.join(os.path.dirname(os.path.abspath(__file__)), "lib", "libw90gb300.so")
+    """The in-tree library; W90G_LIBRARY names another build of it (the test of the
+    kernels' bounded-wait path loads one compiled with a tiny spin limit)."""
+    return os.environ.get("W90G_LIBRARY") or os.path.join(os.path.dirname(os.path.abspath(__file__)), "lib",
+                                                           "libw90gb300.so")
 
 
 def lib():

@@ -43,9 +43,12 @@ def _stale(out, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(verbose=False, force=False, extra_nvcc=()):
+def build(verbose=False, force=False, extra_nvcc=(), libdir=None):
+    """Compile and link; returns the library path.  libdir / extra_nvcc give a separate
+    build (e.g. the bounded-wait test's, with -DW90G_SPIN_LIMIT=...) beside the main one."""
     nvcc = _nvcc()
-    os.makedirs(os.path.join(LIBDIR, "obj"), exist_ok=True)
+    libdir = libdir or LIBDIR
+    os.makedirs(os.path.join(libdir, "obj"), exist_ok=True)
     cu, cpp = sources()
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     headers.append(os.path.join(os.path.dirname(HERE), "include", "wannier90_gb300.h"))
@@ -53,7 +56,7 @@ def build(verbose=False, force=False, extra_nvcc=()):
     objs = []
     for f in cu + cpp:
         src = os.path.join(CSRC, f)
-        obj = os.path.join(LIBDIR, "obj", f + ".o")
+        obj = os.path.join(libdir, "obj", f + ".o")
         objs.append(obj)
         if not force and not _stale(obj, [src] + headers):
             continue
@@ -76,7 +79,7 @@ def build(verbose=False, force=False, extra_nvcc=()):
             sys.stderr.write(r.stdout + r.stderr)
         if r.returncode != 0:
             raise RuntimeError("build failed:\n%s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
-    out = lib_path()
+    out = os.path.join(libdir, LIBNAME)
     if force or _stale(out, objs):
         cmd = [nvcc, *ARCH, "-shared", "-o", out, *objs, "-lcudart_static" if False else "-cudart=static"]
         r = subprocess.run(cmd, capture_output=True, text=True)

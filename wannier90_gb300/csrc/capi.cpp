@@ -58,6 +58,7 @@ struct Handle {
   double kmesh_tol = 1.0e-6;
   int gpu_tensor = 0;   // M update on tensor cores (W <= 128)
   int gpu_tensor_exp = 1;
+  int gpu_mupdate_pipe = 1;   // tensor path, W <= 32: pipelined M-update kernel
   KmeshInfo km;
   // preconditioner tables (precond = T), built at cinput_setopt like wann_main's
   // hamiltonian_setup / k_to_r (src/wannierise.F90:269-300)
@@ -417,6 +418,7 @@ int build_spec(Handle* h, ProblemSpec& s) {
   s.ctl = h->ctl;
   s.tensor = h->gpu_tensor;
   s.tensor_exp = h->gpu_tensor_exp;
+  s.mupdate_pipe = h->gpu_mupdate_pipe;
   s.guiding = h->guiding;
   s.no_guide_iter = h->no_guide_iter;
   s.guide_cycles = h->guide_cycles;
@@ -504,6 +506,9 @@ int apply_result(Handle* h, const w90g::ProblemResult& r, bool print) {
   h->niter = r.niter;
   h->have_result = true;
   if (print && h->iprint > 0) print_wout(h, r);
+  if (r.error == 2)
+    return fail(h, 1, "tensor-core kernel: a bounded wait ran out (device status 2); the kernel drained the work "
+                      "it had issued and stopped the solve");
   if (r.error) return fail(h, 1, "non-finite spread in the engine");
   if (!(r.unitarity_err <= 1e-5)) return fail(h, 1, "wann_check_unitarity: unitariety of final U violated");
   return 0;
@@ -900,6 +905,10 @@ void cinput_setopt(void* hv, const char* seedname, int* ierr, int comm) {
   h->gpu_tensor = get_num(h, "gpu_tensor", v) ? (int)v : 0;
   // with gpu_tensor: gpu_tensor_exp = 1 (default) also runs exp(s D) and U dU on tensor cores
   h->gpu_tensor_exp = get_num(h, "gpu_tensor_exp", v) ? (int)v : 1;
+  // with gpu_tensor and num_wann <= 32: gpu_mupdate_pipe = 1 (default) runs the M update
+  // as the pipelined warp-specialised kernel, 0 as the one-CTA-per-group kernel (same digits,
+  // bitwise the same result)
+  h->gpu_mupdate_pipe = get_num(h, "gpu_mupdate_pipe", v) ? (int)v : 1;
   // options on wann_main's code path that the engine does not implement
   const char* unsupported[] = {"gamma_only", "dis_spheres_num"};
   for (const char* k : unsupported) {
@@ -1348,6 +1357,8 @@ void w90g_wannierise_batch_device(void** handles, int nprob, double** d_m, doubl
     build_spec(h, s);
     int key = 0;
     if (s.tensor && s.W <= 128) key = s.W <= 8 ? 8 : (s.W <= 16 ? 16 : (s.W <= 32 ? 32 : (s.W <= 64 ? 64 : 128)));
+    if (key && key <= 32 && !s.mupdate_pipe) key += 1000;   // the one-CTA-per-group kernel
+    if (key && !s.tensor_exp) key += 2000;                   // exp(s D) on the FP64 pipe
     groups[key].idx.push_back(i);
     groups[key].specs.push_back(s);
   }

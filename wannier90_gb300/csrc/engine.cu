@@ -43,6 +43,10 @@ __global__ void k_phases(const Problem* probs, int mode);
 __global__ void k_sym_grad(const Problem* probs, WorkMap wm);
 __global__ void k_sym_dir(const Problem* probs, WorkMap wm);
 __global__ void k_sym_u(const Problem* probs, WorkMap wm);
+cudaError_t oz2_launch(int wp, int step, const Problem* probs, WorkMap wm, int which, int ngroups,
+                       cudaStream_t s);
+cudaError_t oz2_set_attributes(int wp);
+cudaError_t oz2_preslice_launch(int wp, const Problem* probs, WorkMap wm, int grid, cudaStream_t s);
 cudaError_t oz_launch(int wp, int step, const Problem* probs, WorkMap wm, int which, int grid,
                       cudaStream_t s);
 cudaError_t oz_set_attributes(int wp);
@@ -183,14 +187,14 @@ int choose_tensor_wp(const std::vector<ProblemSpec>& specs) {
 
 struct Sizes {
   size_t M, U, KWW, work, tbuf, diag, offd, gpart, cen, log, logc, nn, bk, wb, st, op1, op2, m0, u0, inv, fr;
-  size_t m0s, m0e;
+  size_t m0s, m0e, zexp;
   size_t pkr, pr2, pgr, pgp, ppart;
   size_t gbka, gneigh, grg, gsheet, gcsheet;
   size_t slwf;
   size_t symi, symd, symw;
   size_t total() const {
     return 2 * M + 2 * U + 3 * KWW + work + tbuf + 2 * diag + offd + gpart + cen + log + logc + nn + bk + wb + st +
-           op1 + op2 + m0 + u0 + inv + fr + m0s + m0e + pkr + 2 * pr2 + pgr + pgp + ppart + gbka + gneigh + grg + gsheet +
+           op1 + op2 + m0 + u0 + inv + fr + m0s + m0e + zexp + pkr + 2 * pr2 + pgr + pgp + ppart + gbka + gneigh + grg + gsheet +
            gcsheet + slwf + symi + 2 * symd + symw;
   }
 };
@@ -212,6 +216,7 @@ Sizes problem_sizes(const ProblemSpec& s, int wp, int* pc_tiles) {
   z.inv = wp ? align_up(K * B * 4) : 0;
   z.fr = wp ? align_up(K * B * 8) : 0;
   z.m0s = z.m0e = 0;
+  z.zexp = (wp && wp <= 32) ? align_up(K * B * W * 4) : 0;
   if (wp) {
     size_t d = 0, e = 0;
     oz_preslice_bytes(wp, (int)K, (int)B, &d, &e);
@@ -370,6 +375,7 @@ int Engine::alloc(std::string& err) {
     P.frob0 = z.fr ? (double*)take(z.fr) : nullptr;
     P.m0s = z.m0s ? (unsigned char*)take(z.m0s) : nullptr;
     P.m0s_exp = z.m0e ? (int*)take(z.m0e) : nullptr;
+    P.zexp = z.zexp ? (int*)take(z.zexp) : nullptr;
     if (inv) {
       std::vector<int> h_inv((size_t)s.K * s.B), fill(s.K, 0);
       for (int kb = 0; kb < s.K * s.B; ++kb) {
@@ -445,7 +451,9 @@ int Engine::alloc(std::string& err) {
   W90G_CHECK(cudaFuncSetAttribute(k_lowdin, cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * wmax * wmax * 16));
   tensor_exp_ = tensor_wp_ != 0;
   for (const auto& s : specs_) tensor_exp_ = tensor_exp_ && s.tensor_exp;
-  if (tensor_wp_) W90G_CHECK(oz_set_attributes(tensor_wp_));
+  pipe_ = tensor_wp_ != 0 && tensor_wp_ <= 32;
+  for (const auto& s : specs_) pipe_ = pipe_ && s.mupdate_pipe;
+  if (tensor_wp_) W90G_CHECK(pipe_ ? oz2_set_attributes(tensor_wp_) : oz_set_attributes(tensor_wp_));
   if (tensor_exp_) W90G_CHECK(oz_exp_set_attributes(tensor_wp_));
   return 0;
 }
@@ -632,7 +640,8 @@ int Engine::prepare_tensor(cudaStream_t st, std::string& err) {
   k_frob0<<<n_kb_, 128, 0, st>>>(dprobs_, wmkb);
   W90G_CHECK(cudaGetLastError());
   // step 1's A operand (the entry overlaps) in digit planes, once per solve
-  W90G_CHECK(oz_preslice_launch(tensor_wp_, dprobs_, wmk, n_k_, st));
+  W90G_CHECK(pipe_ ? oz2_preslice_launch(tensor_wp_, dprobs_, wmk, n_k_, st)
+                  : oz_preslice_launch(tensor_wp_, dprobs_, wmk, n_k_, st));
   launches_ += 3;
   return 0;
 }
@@ -641,7 +650,10 @@ void Engine::launch_mupdate(cudaStream_t s, int which) {
   const int np = nprob();
   const WorkMap wmk{d_offs_k_, np};
   const WorkMap wmkb{d_offs_kb_, np};
-  if (tensor_wp_) {
+  if (pipe_) {
+    oz2_launch(tensor_wp_, 1, dprobs_, wmk, which, n_k_, s);
+    oz2_launch(tensor_wp_, 2, dprobs_, wmk, which, n_k_, s);
+  } else if (tensor_wp_) {
     oz_launch(tensor_wp_, 1, dprobs_, wmk, which, n_k_, s);
     oz_launch(tensor_wp_, 2, dprobs_, wmk, which, n_k_, s);
   } else {

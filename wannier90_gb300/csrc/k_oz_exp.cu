@@ -88,16 +88,17 @@ __device__ __forceinline__ void ab_exponents(OzCtx& cx, const double2* A, const 
     const int r = idx % WP;
     unsigned long long mx = 0ull;
     if (idx < ITEMS && r < W) {
-      if (idx < WP) {
-        for (int l = sub; l < W; l += TPI) {
-          const double2 a = A[(size_t)l * W + r];
-          mx = max(mx, max(abs_bits(a.x), abs_bits(a.y)));
+      // eight independent loads per round (the matrices may sit in L2), then the max
+      const bool row_of_a = idx < WP;
+      for (int l0 = sub; l0 < W; l0 += 8 * TPI) {
+        double2 v[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          const int l = l0 + i * TPI;
+          v[i] = (l < W) ? (row_of_a ? A[(size_t)l * W + r] : B[(size_t)r * W + l]) : make_double2(0.0, 0.0);
         }
-      } else {
-        for (int l = sub; l < W; l += TPI) {
-          const double2 b = B[(size_t)r * W + l];
-          mx = max(mx, max(abs_bits(b.x), abs_bits(b.y)));
-        }
+#pragma unroll
+        for (int i = 0; i < 8; ++i) mx = max(mx, max(abs_bits(v[i].x), abs_bits(v[i].y)));
       }
     }
 #pragma unroll
@@ -334,13 +335,25 @@ __device__ bool oz_cmm2(OzCtx& cx, double2* C, const double2* A, const double2* 
   constexpr int kgroups = CW / 8;
   bool ok = true;
   for (int kc = 0; kc < E::NCHK && ok; ++kc) {
-    // ---- A_emb chunk: complex (r, l) -> rows r (re) and WP + r (im), K l (re) / CW + l (im)
-    for (int e = tid; e < WP * CW; e += blockDim.x) {
+    // ---- A_emb chunk: complex (r, l) -> rows r (re) and WP + r (im), K l (re) / CW + l (im);
+    // each thread's elements are loaded together first (they may come from L2)
+    constexpr int NA = (WP * CW + 255) / 256;
+    double2 av[NA];
+#pragma unroll
+    for (int i = 0; i < NA; ++i) {
+      const int e = tid + i * 256;
       const int ln = e & 31, wi = e >> 5;
       const int r = (wi / kgroups) * 4 + (ln >> 3), l = (wi % kgroups) * 8 + (ln & 7);
       const int m = kc * CW + l;
-      double2 a = make_double2(0.0, 0.0);
-      if (r < W && m < W) a = A[(size_t)m * W + r];
+      av[i] = (e < WP * CW && r < W && m < W) ? A[(size_t)m * W + r] : make_double2(0.0, 0.0);
+    }
+#pragma unroll
+    for (int i = 0; i < NA; ++i) {
+      const int e = tid + i * 256;
+      if (e >= WP * CW) break;
+      const int ln = e & 31, wi = e >> 5;
+      const int r = (wi / kgroups) * 4 + (ln >> 3), l = (wi % kgroups) * 8 + (ln & 7);
+      const double2 a = av[i];
       int xr[kS2], xi[kS2];
       const int ex = cx.rowexp[r];
       digits7x8(scaled_int55(a.x, ex), xr);
@@ -357,12 +370,23 @@ __device__ bool oz_cmm2(OzCtx& cx, double2* C, const double2* A, const double2* 
       }
     }
     // ---- B_emb chunk as B^T (K-major): row = output column c, K l (re) / CW + l (im)
-    for (int e = tid; e < N * CW; e += blockDim.x) {
+    constexpr int NB = (N * CW + 255) / 256;
+    double2 bv[NB];
+#pragma unroll
+    for (int i = 0; i < NB; ++i) {
+      const int e = tid + i * 256;
       const int ln = e & 31, wi = e >> 5;
       const int c = (wi / kgroups) * 4 + (ln >> 3), l = (wi % kgroups) * 8 + (ln & 7);
       const int mm = kc * CW + l;
-      double2 b = make_double2(0.0, 0.0);
-      if (mm < W && c < W) b = B[(size_t)c * W + mm];
+      bv[i] = (e < N * CW && mm < W && c < W) ? B[(size_t)c * W + mm] : make_double2(0.0, 0.0);
+    }
+#pragma unroll
+    for (int i = 0; i < NB; ++i) {
+      const int e = tid + i * 256;
+      if (e >= N * CW) break;
+      const int ln = e & 31, wi = e >> 5;
+      const int c = (wi / kgroups) * 4 + (ln >> 3), l = (wi % kgroups) * 8 + (ln & 7);
+      const double2 b = bv[i];
       int xr[kS2], xi[kS2];
       const int ex = cx.colexp[c < WP ? c : 0];
       digits7x8(scaled_int55(b.x, ex), xr);
@@ -429,20 +453,22 @@ __device__ bool oz_cmm2(OzCtx& cx, double2* C, const double2* A, const double2* 
       if (wq * 32 < E::ROWS) {
 #pragma unroll 1
         for (int j0 = half * NH; j0 < (half + 1) * NH; j0 += 4) {
+          uint32_t q[kS2][4];
 #pragma unroll
-          for (int d = 0; d < kS2; ++d) {
-            uint32_t q[4];
+          for (int d = 0; d < kS2; ++d)
             asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
-                         : "=r"(q[0]), "=r"(q[1]), "=r"(q[2]), "=r"(q[3])
+                         : "=r"(q[d][0]), "=r"(q[d][1]), "=r"(q[d][2]), "=r"(q[d][3])
                          : "r"(cx.tmem + lane_base + (uint32_t)(d * N + j0)));
-            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-            const int row = wq * 32 + lane;
-            if (row < E::ROWS) {
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+          const int row = wq * 32 + lane;
+          if (row < E::ROWS) {
+#pragma unroll
+            for (int d = 0; d < kS2; ++d) {
               uint32_t* rp = stage + ((size_t)d * E::ROWS + row) * E::STAGE_LD + j0;
-              rp[0] = q[0];
-              rp[1] = q[1];
-              rp[2] = q[2];
-              rp[3] = q[3];
+              rp[0] = q[d][0];
+              rp[1] = q[d][1];
+              rp[2] = q[d][2];
+              rp[3] = q[d][3];
             }
           }
         }
@@ -509,6 +535,7 @@ using ExpProd = typename std::conditional<(WP <= 64), ProdV2<WP>, ProdV1<WP>>::t
 // make C exactly Hermitian (sign +1) or anti-Hermitian (sign -1) from its upper triangle,
 // as the FP64 path's structured products produce it
 __device__ void mirror(double2* C, int W, double sign) {
+#pragma unroll 4
   for (int e = threadIdx.x; e < W * W; e += blockDim.x) {
     const int i = e % W, j = e / W;
     if (i > j) {
@@ -573,12 +600,14 @@ __global__ void __launch_bounds__(256, 2) k_oz_exp(const Problem* __restrict__ p
     // (in the symmetry-adapted mode k_sym_dir has formed D already)
     const double cg = st->coefG, cd = st->coefD;
     const double2* Gk = (st->use_gp ? P.pc_gp : P.G) + (size_t)k * WW;
+    #pragma unroll 4
     for (int e = tid; e < WW; e += blockDim.x) {
       const double2 d = cadd(cscale(Gk[e], cg), cscale(Dk[e], cd));
       Dk[e] = d;
       X[e] = cscale(d, s);
     }
   } else {
+    #pragma unroll 4
     for (int e = tid; e < WW; e += blockDim.x) X[e] = cscale(Dk[e], s);
   }
   __syncthreads();
@@ -586,12 +615,19 @@ __global__ void __launch_bounds__(256, 2) k_oz_exp(const Problem* __restrict__ p
 
   // ---- degree / squarings from the 1-norm (the FP64 path's table; costs in products:
   // powers X^2, X^3 (, X^4) plus the Horner steps)
+  // 1-norm: the moduli |X_ij| by all threads into shared scratch (the digit region is
+  // free before the first product), then each column summed in row order as before
+  double* absx = (double*)base;
+#pragma unroll 4
+  for (int e = tid; e < WW; e += blockDim.x) absx[e] = sqrt(cabs2(X[e]));
+  __syncthreads();
   double colmax = 0.0;
   for (int j = tid; j < W; j += blockDim.x) {
     double a = 0.0;
-    for (int i = 0; i < W; ++i) a += sqrt(cabs2(X[(size_t)j * W + i]));
+    for (int i = 0; i < W; ++i) a += absx[(size_t)j * W + i];
     colmax = fmax(colmax, a);
   }
+  __syncthreads();
   const double nrm = cta_max(colmax, red);
   const int cand_m[5] = {4, 6, 8, 12, 16};
   const int cand_p[5] = {4, 3, 4, 4, 4};
@@ -615,6 +651,7 @@ __global__ void __launch_bounds__(256, 2) k_oz_exp(const Problem* __restrict__ p
     }
   }
   const double sc = ldexp(1.0, -js);
+  #pragma unroll 4
   for (int e = tid; e < WW; e += blockDim.x) X[e] = cscale(X[e], sc);
   __syncthreads();
   bool ok = E::mm(cx, Y2, X, X, W);
@@ -646,14 +683,17 @@ __global__ void __launch_bounds__(256, 2) k_oz_exp(const Problem* __restrict__ p
   int q = nblk - 1;
   if (pw * q == m) {
     const double cm = kOzInvFact[m];
+    #pragma unroll 4
     for (int e = tid; e < WW; e += blockDim.x) R[e] = cadd(cscale(Yp[e], cm), blk(q - 1, e));
     q -= 1;
   } else {
+    #pragma unroll 4
     for (int e = tid; e < WW; e += blockDim.x) R[e] = blk(q, e);
   }
   __syncthreads();
   for (q = q - 1; q >= 0 && ok; --q) {
     ok = E::mm(cx, T, Yp, R, W);
+    #pragma unroll 4
     for (int e = tid; e < WW; e += blockDim.x) R[e] = cadd(T[e], blk(q, e));
     __syncthreads();
   }
@@ -667,6 +707,7 @@ __global__ void __launch_bounds__(256, 2) k_oz_exp(const Problem* __restrict__ p
   }
   // dU = exp(s D);  U[cur^1] = U[cur] dU
   double2* dUk = P.dU + (size_t)k * WW;
+  #pragma unroll 4
   for (int e = tid; e < WW; e += blockDim.x) dUk[e] = a[e];
   __syncthreads();
   const int cur = st->cur;

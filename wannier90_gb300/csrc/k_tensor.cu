@@ -48,9 +48,13 @@ __device__ __forceinline__ void a_row_exponents(int tile, int W, int* rowexp, AE
   const int r = tid >> 1, half = tid & 1;
   const int row = tile * kTileRows + r;
   unsigned long long mx = 0ull;
-  for (int m = half; m < W; m += 2) {
-    const double2 a = a_elem(row, m);
-    mx = max(mx, max(abs_bits(a.x), abs_bits(a.y)));
+  // eight independent loads in flight per round (the max does not depend on the order)
+  for (int m0 = half; m0 < W; m0 += 16) {
+    double2 v[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = (m0 + 2 * i < W) ? a_elem(row, m0 + 2 * i) : make_double2(0.0, 0.0);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) mx = max(mx, max(abs_bits(v[i].x), abs_bits(v[i].y)));
   }
   mx = max(mx, (unsigned long long)__shfl_xor_sync(0xffffffffu, (long long)mx, 1));
   if (half == 0) rowexp[r] = exp_above_bits(mx);
@@ -125,14 +129,27 @@ __global__ void __launch_bounds__(256, 1) k_oz_mupdate(const Problem* __restrict
 
   // ---- B operand of the group: step 1 conj(U(k)), step 2 U(k'); B(K=m, N=c) = (conj) U(m, c)
   const double2* Ug = Unew + (size_t)g * WW;
-  for (int c = tid; c < WP; c += blockDim.x) {
+  {
+    // column scales: 256 / WP threads per column, four independent loads per round, a max
+    // across those lanes
+    constexpr int TPC = 256 / WP;
+    const int c = tid / TPC, sub = tid % TPC;
     unsigned long long mx = 0ull;
     if (c < W)
-      for (int m = 0; m < W; ++m) {
-        const double2 u = Ug[(size_t)c * W + m];
-        mx = max(mx, max(abs_bits(u.x), abs_bits(u.y)));
+      for (int m0 = sub; m0 < W; m0 += 4 * TPC) {
+        double2 v[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const int m = m0 + i * TPC;
+          v[i] = (m < W) ? Ug[(size_t)c * W + m] : make_double2(0.0, 0.0);
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i) mx = max(mx, max(abs_bits(v[i].x), abs_bits(v[i].y)));
       }
-    s_colexp[c] = exp_above_bits(mx);
+#pragma unroll
+    for (int o = 1; o < TPC; o <<= 1)
+      mx = max(mx, (unsigned long long)__shfl_xor_sync(0xffffffffu, (long long)mx, o));
+    if (sub == 0 && c < WP) s_colexp[c] = exp_above_bits(mx);
   }
 
   // slice the (nc, kc) chunk of B^T (K-major: rows = real N index within the chunk)

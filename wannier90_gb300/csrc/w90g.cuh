@@ -130,6 +130,8 @@ struct Problem {
   unsigned char* m0s;   // tensor path: step 1's A operand (M0 rows) in BF16 digit planes,
                         // the shared-memory image of every (k, tile, K chunk)
   int* m0s_exp;         // tensor path: the row exponents of those tiles [k][tile][128]
+  int* zexp;            // pipelined tensor path: step 2's row exponents [k][b][row of Z(k,b)],
+                        // written by step 1's epilogue
   double2* U0;          // tensor path: U at entry; U[] then holds R = U0^H U
   const int* inv_nnlist;  // tensor path: [k'][i] = k*B+b with nnlist(k,b) = k'
   double* frob0;        // tensor path: |M0(k,b)|_F^2
