@@ -1,13 +1,14 @@
 """The tensor-core kernels' bounded waits, driven to run out on purpose.
 
-A copy of the library is compiled with W90G_SPIN_LIMIT=1 (one try per mbarrier wait; the
-drain limit that follows a timeout is unchanged), so the kernels' waits on their MMA
-commits and bulk copies give up almost at once.  Each kernel must then record device
-status 2, wait for the MMAs and copies it already issued, free its tensor memory and
-return: the call reports the error, and the GPU stays usable -- a normal solve in the same
-test afterwards gives the expected result.  Three routes: the pipelined M update
-(num_wann <= 32, FP64 exp so that the M update runs first), the tensor exp, and the
-one-CTA-per-group M update (num_wann > 32)."""
+A copy of the library is compiled with W90G_SPIN_LIMIT=0 (no tries: every mbarrier wait
+that is not skipped gives up at once; the drain limit that follows a timeout is
+unchanged).  Each kernel must then record device status 2, wait for the MMAs and bulk
+copies it already issued, free its tensor memory and return: the call reports the error,
+and the GPU stays usable -- a normal solve in the same test afterwards gives the expected
+result.  Three routes: the pipelined M update (num_wann <= 32, FP64 exp so that the M
+update runs first; its producer has issued one bulk copy per stage slot, which the drain
+must let land), the tensor exp (its first product's MMAs are in flight), and the
+one-CTA-per-group M update (num_wann > 32, its first bulk copy in flight)."""
 import json
 import os
 import subprocess
@@ -48,7 +49,7 @@ CASES = [(8, 0), (24, 1), (40, 0)]
 
 
 def test_timed_out_waits_report_error_and_leave_the_gpu_usable(tmp_path):
-    lib = B.build(extra_nvcc=["-DW90G_SPIN_LIMIT=1"], libdir=str(tmp_path / "spin1"))
+    lib = B.build(extra_nvcc=["-DW90G_SPIN_LIMIT=0"], libdir=str(tmp_path / "spin0"))
     env = dict(os.environ, W90G_LIBRARY=lib)
     r = subprocess.run([sys.executable, "-c", CHILD % dict(root=ROOT, cases=CASES)], capture_output=True,
                        text=True, env=env, timeout=600)

@@ -56,3 +56,19 @@ def test_pipelined_batch_uneven_widths_equals_standalone():
         np.testing.assert_array_equal(w90.w90_get_log(h, 31)[:, :8], alone[i][2][:, :8])
         np.testing.assert_array_equal(ms[i].cpu().numpy(), alone[i][0])
         np.testing.assert_array_equal(us[i].cpu().numpy(), alone[i][1])
+
+
+@pytest.mark.parametrize("W", [20, 32])
+def test_exp_matrices_in_shared_memory_bitwise(W):
+    """The tensor exp with its FP64 matrices in shared memory (gpu_exp_smem = 1) is the same
+    arithmetic as with them in L2: bitwise the same trajectory."""
+    p = synth.make_problem(kind="fcc", a=5.0, mp=(3, 3, 3), num_wann=W, rmax=1, eps=0.3, seed=13)
+    M = synth.to_math_m(p.m)
+    A = synth.to_math_u(p.a)
+    ctl = O.WannControl(num_iter=20)
+    a = run_engine(p.real_lattice, p.kpoints, M, A, ctl, W, extra={"gpu_tensor": 1, "gpu_exp_smem": 0})
+    b = run_engine(p.real_lattice, p.kpoints, M, A, ctl, W, extra={"gpu_tensor": 1, "gpu_exp_smem": 1})
+    assert a["ierr"] == 0 and b["ierr"] == 0, (a["err"], b["err"])
+    np.testing.assert_array_equal(b["log"][:, :8], a["log"][:, :8])
+    np.testing.assert_array_equal(b["U"], a["U"])
+    np.testing.assert_array_equal(b["M"], a["M"])

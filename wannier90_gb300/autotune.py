@@ -10,7 +10,10 @@ Candidates (engine options of the handle):
                  K extent of a tile staged at once (gpu_mupdate_pipe = 0);
 * ``tensor_fp64exp`` -- the tcgen05 M update with exp(sD) and U dU on the FP64 pipe
                  (gpu_tensor_exp = 0), which wins for the smallest widths where a W x W
-                 product fills little of a 128-row MMA tile.
+                 product fills little of a 128-row MMA tile;
+* ``tensor_smemexp`` -- 16 < num_wann <= 32: the tensor exp with its six FP64 matrices in
+                 shared memory, one CTA per SM (gpu_exp_smem = 1), instead of in L2 with two
+                 CTAs per SM.
 
 The padded tile width (8 / 16 / 32 / 64 / 128) follows from num_wann.  For each width the
 tuner times a few iterations of a seeded tight-binding probe (sc lattice, 4x4x4 k-mesh,
@@ -37,6 +40,7 @@ CANDIDATES = {
     "tensor": dict(gpu_tensor=1, gpu_tensor_exp=1, gpu_mupdate_pipe=1),
     "tensor_cta": dict(gpu_tensor=1, gpu_tensor_exp=1, gpu_mupdate_pipe=0),
     "tensor_fp64exp": dict(gpu_tensor=1, gpu_tensor_exp=0, gpu_mupdate_pipe=1),
+    "tensor_smemexp": dict(gpu_tensor=1, gpu_tensor_exp=1, gpu_mupdate_pipe=1, gpu_exp_smem=1),
 }
 
 
@@ -46,6 +50,8 @@ def candidates_for(num_wann: int):
     names = ["fp64", "tensor", "tensor_fp64exp"]
     if num_wann <= 32:
         names.append("tensor_cta")
+    if 16 < num_wann <= 32:
+        names.append("tensor_smemexp")
     return names
 
 

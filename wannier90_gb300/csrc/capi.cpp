@@ -59,6 +59,7 @@ struct Handle {
   int gpu_tensor = 0;   // M update on tensor cores (W <= 128)
   int gpu_tensor_exp = 1;
   int gpu_mupdate_pipe = 1;   // tensor path, W <= 32: pipelined M-update kernel
+  int gpu_exp_smem = 0;       // tensor exp, 16 < W <= 32: matrices in shared memory
   KmeshInfo km;
   // preconditioner tables (precond = T), built at cinput_setopt like wann_main's
   // hamiltonian_setup / k_to_r (src/wannierise.F90:269-300)
@@ -419,6 +420,7 @@ int build_spec(Handle* h, ProblemSpec& s) {
   s.tensor = h->gpu_tensor;
   s.tensor_exp = h->gpu_tensor_exp;
   s.mupdate_pipe = h->gpu_mupdate_pipe;
+  s.exp_smem = h->gpu_exp_smem;
   s.guiding = h->guiding;
   s.no_guide_iter = h->no_guide_iter;
   s.guide_cycles = h->guide_cycles;
@@ -909,6 +911,9 @@ void cinput_setopt(void* hv, const char* seedname, int* ierr, int comm) {
   // as the pipelined warp-specialised kernel, 0 as the one-CTA-per-group kernel (same digits,
   // bitwise the same result)
   h->gpu_mupdate_pipe = get_num(h, "gpu_mupdate_pipe", v) ? (int)v : 1;
+  // with the tensor exp and 16 < num_wann <= 32: gpu_exp_smem = 1 keeps the exp chain's six
+  // FP64 matrices in shared memory (one CTA per SM) instead of L2 (two CTAs per SM)
+  h->gpu_exp_smem = get_num(h, "gpu_exp_smem", v) ? (int)v : 0;
   // options on wann_main's code path that the engine does not implement
   const char* unsupported[] = {"gamma_only", "dis_spheres_num"};
   for (const char* k : unsupported) {
@@ -1359,6 +1364,7 @@ void w90g_wannierise_batch_device(void** handles, int nprob, double** d_m, doubl
     if (s.tensor && s.W <= 128) key = s.W <= 8 ? 8 : (s.W <= 16 ? 16 : (s.W <= 32 ? 32 : (s.W <= 64 ? 64 : 128)));
     if (key && key <= 32 && !s.mupdate_pipe) key += 1000;   // the one-CTA-per-group kernel
     if (key && !s.tensor_exp) key += 2000;                   // exp(s D) on the FP64 pipe
+    if (key == 32 && s.tensor_exp && s.exp_smem) key += 4000;  // exp matrices in shared memory
     groups[key].idx.push_back(i);
     groups[key].specs.push_back(s);
   }

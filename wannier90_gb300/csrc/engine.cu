@@ -52,8 +52,9 @@ cudaError_t oz_launch(int wp, int step, const Problem* probs, WorkMap wm, int wh
 cudaError_t oz_set_attributes(int wp);
 void oz_preslice_bytes(int wp, int K, int B, size_t* data, size_t* exps);
 cudaError_t oz_preslice_launch(int wp, const Problem* probs, WorkMap wm, int grid, cudaStream_t s);
-cudaError_t oz_exp_launch(int wp, const Problem* probs, WorkMap wm, int which, int grid, cudaStream_t s);
-cudaError_t oz_exp_set_attributes(int wp);
+cudaError_t oz_exp_launch(int wp, int smem_mats, const Problem* probs, WorkMap wm, int which, int grid,
+                          cudaStream_t s);
+cudaError_t oz_exp_set_attributes(int wp, int smem_mats);
 
 const char* kProfNames[kPNum] = {"k_grad", "k_ctrl_search", "k_exp_u", "k_m_update",
                                  "k_omega", "k_ctrl_step", "k_ctrl_end", "init", "k_precond"};
@@ -454,7 +455,9 @@ int Engine::alloc(std::string& err) {
   pipe_ = tensor_wp_ != 0 && tensor_wp_ <= 32;
   for (const auto& s : specs_) pipe_ = pipe_ && s.mupdate_pipe;
   if (tensor_wp_) W90G_CHECK(pipe_ ? oz2_set_attributes(tensor_wp_) : oz_set_attributes(tensor_wp_));
-  if (tensor_exp_) W90G_CHECK(oz_exp_set_attributes(tensor_wp_));
+  exp_smem_ = tensor_exp_ && tensor_wp_ == 32;
+  for (const auto& s : specs_) exp_smem_ = exp_smem_ && s.exp_smem;
+  if (tensor_exp_) W90G_CHECK(oz_exp_set_attributes(tensor_wp_, exp_smem_ ? 1 : 0));
   return 0;
 }
 
@@ -665,7 +668,7 @@ void Engine::launch_mupdate(cudaStream_t s, int which) {
 void Engine::launch_exp(cudaStream_t s, int which) {
   const WorkMap wmk{d_offs_k_, nprob()};
   if (tensor_exp_) {
-    oz_exp_launch(tensor_wp_, dprobs_, wmk, which, n_k_, s);
+    oz_exp_launch(tensor_wp_, exp_smem_ ? 1 : 0, dprobs_, wmk, which, n_k_, s);
   } else {
     const int ws = std::max(maxW_small_, 1);
     k_exp_u<<<n_k_, 256, (size_t)6 * ws * ws * 16, s>>>(dprobs_, wmk, which);

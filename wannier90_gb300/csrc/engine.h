@@ -20,6 +20,7 @@ struct ProblemSpec {
   int tensor = 0;            // request the tensor-core M update (W <= 128)
   int tensor_exp = 1;        // with tensor: exp(s D) and U dU on the tensor cores too
   int mupdate_pipe = 1;      // with tensor and W <= 32: the pipelined M-update kernel (k_mupdate2.cu)
+  int exp_smem = 0;          // with tensor exp and 16 < W <= 32: the exp chain's matrices in shared memory
   // preconditioner (precond = T): Wigner-Seitz points R_r of the Born-von Karman
   // supercell, exp(-i 2 pi k.R) table [k][r] (re, im interleaved), |R|^2, degeneracies
   int precond = 0;
@@ -140,6 +141,7 @@ class Engine {
   int tensor_wp_ = 0;    // > 0: tensor M update with padded width 8..128 for the whole batch
   bool tensor_exp_ = false;  // exp(s D) on the tensor cores (k_oz_exp)
   bool pipe_ = false;        // tensor M update by the pipelined kernel (tensor_wp_ <= 32)
+  bool exp_smem_ = false;    // tensor exp with its FP64 matrices in shared memory (tensor_wp_ == 32)
   int max_iter_ = 0;
   cudaStream_t own_stream_ = nullptr;
   cudaStream_t user_stream_ = nullptr;

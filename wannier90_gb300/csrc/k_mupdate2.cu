@@ -7,14 +7,15 @@
 // (group g, 128-row tile) of its share of the groups, with warp-specialised roles
 // connected by mbarriers:
 //
-//   warps 16-19 producer: per group, the column scales of the shared operand and its
-//               7 digit planes (double-buffered B); per tile, the A operand one K-step
-//               (16 real K, all 7 planes, 28 KB) at a time into a ring of stages --
-//               step 1 as one bulk copy per stage from the digit image of the entry
-//               overlaps (k_oz_preslice2), step 2 by slicing Z in registers;
-//   warp 20     MMA issue (one thread): per stage the 28 digit-pair MMAs, a commit that
+//   producer warps (4 in step 1, 8 in step 2): per group, the column scales of the
+//               shared operand and its 7 digit planes (double-buffered B); per tile, the
+//               A operand one K-step (16 real K, all 7 planes, 28 KB) at a time into a ring
+//               of stages -- step 1 as one bulk copy per stage from the digit image of the
+//               entry overlaps (k_oz_preslice2), step 2 by slicing Z in registers;
+//   one warp    MMA issue (one thread): per stage the 28 digit-pair MMAs, a commit that
 //               frees the stage, a commit per tile that hands the accumulators over;
-//   warps 0-15  epilogue (4 per TMEM lane quarter): TMEM -> registers, exact recombination, FP64 stores (and in
+//   epilogue warps (16 in step 1, 8 in step 2; 4 or 2 column groups per TMEM lane
+//               quarter): TMEM -> registers, exact recombination, FP64 stores (and in
 //               step 1 the row scales step 2 will use, by a segmented warp max; in step
 //               2 the diagonal statistics of the spread).
 //
@@ -33,13 +34,22 @@ namespace w90g {
 
 namespace {
 
-constexpr int kEpiWarps = 16;                             // 4 per TMEM lane quarter
-constexpr int kProdWarps = 4;
-constexpr int kMmaWarp = kEpiWarps + kProdWarps;          // 20
-constexpr int kThreads2 = (kMmaWarp + 1) * 32;            // 672
-constexpr int kProdThreads = kProdWarps * 32;
-constexpr int kEpiThreads = kEpiWarps * 32;
 constexpr int kDynBudget = 232448 - 5120;                 // opt-in smem minus static use and slack
+
+// Warp roles per step.  Step 1's A operand arrives by bulk copy, so its producer is light
+// and 16 epilogue warps (4 per TMEM lane quarter) share the recombination; step 2 slices Z
+// in its producer, which gets 8 warps, and 8 epilogue warps remain.
+template <int STEP>
+struct Roles {
+  static constexpr int EPI = STEP == 1 ? 16 : 8;           // epilogue warps 0 .. EPI-1
+  static constexpr int PROD = STEP == 1 ? 4 : 8;           // producer warps EPI .. EPI+PROD-1
+  static constexpr int MMA = EPI + PROD;                   // the MMA-issue warp
+  static constexpr int THREADS = (MMA + 1) * 32;
+  static constexpr int ET = EPI * 32, PT = PROD * 32;
+  static constexpr int GROUPS = EPI / 4;                   // column groups per lane quarter
+  static constexpr int RPP = PT / 8;                       // rows per slicing pass (8 K each)
+  static constexpr int NPASS = kTileRows / RPP;            // passes over a stage's 128 rows
+};
 
 constexpr int pow2_cols(int c) { return c <= 32 ? 32 : (c <= 64 ? 64 : (c <= 128 ? 128 : (c <= 256 ? 256 : 512))); }
 
@@ -127,10 +137,12 @@ __device__ __forceinline__ long long recombine7_exact(const uint32_t* dd, int st
 //         the B pairs with nnlist(k,b) = k', B = U(k'), out M and the diagonal statistics.
 // ngroups: work items of the map (one per group); grid: persistent, <= ngroups.
 template <int WP, int STEP>
-__global__ void __launch_bounds__(kThreads2, 1)
+__global__ void __launch_bounds__(Roles<STEP>::THREADS, 1)
     k_oz_mupdate2(const Problem* __restrict__ probs, WorkMap wm, int which, int ngroups) {
   using L = MU2<WP>;
+  using R = Roles<STEP>;
   constexpr int CW = L::CW, KC = L::KC, NC = L::NC, KSTEPS = L::KSTEPS, NS = L::NS, NACC = L::NACC;
+  constexpr int kEpiWarps = R::EPI, kMmaWarp = R::MMA, kProdThreads = R::PT, kEpiThreads = R::ET;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   unsigned char* sA = base;                                 // NS stages
@@ -211,7 +223,8 @@ __global__ void __launch_bounds__(kThreads2, 1)
       const int ntiles = ntiles_of<WP>(B);
       // ---- B operand of the group: column scales, 7 digit planes
       const int bb = gseq & 1;
-      if (!pwait(&b_empty[bb], ((gseq >> 1) & 1) ^ 1, p)) {
+      // (the first use of each B buffer needs no wait)
+      if (gseq >= 2 && !pwait(&b_empty[bb], ((gseq >> 1) & 1) ^ 1, p)) {
         ok = false;
         break;
       }
@@ -267,18 +280,20 @@ __global__ void __launch_bounds__(kThreads2, 1)
       ++gseq;
       // ---- A operand, tile by tile, one K-step stage at a time
       for (int tile = 0; tile < ntiles && ok; ++tile) {
-        // step 2: the Z rows this thread slices (rows i*16 + pt/8, K index 8 ks + pt%8)
-        const double2* zrow[8];
+        // step 2: the Z rows this thread slices (rows i*RPP + pt/8, K index 8 ks + pt%8)
+        const double2* zrow[R::NPASS];
         if (STEP == 2) {
           // row scales of this tile: computed by step 1's epilogue (zexp)
-          const int row = tile * kTileRows + pt;
-          const int bi = row / WP, rr = row % WP;
-          int e = 0;
-          if (bi < B && rr < W) e = P.zexp[(size_t)P.inv_nnlist[(size_t)g * B + bi] * W + rr];
-          s_rowexp[pt] = e;
+          for (int r0 = pt; r0 < kTileRows; r0 += kProdThreads) {
+            const int row = tile * kTileRows + r0;
+            const int bi = row / WP, rr = row % WP;
+            int e = 0;
+            if (bi < B && rr < W) e = P.zexp[(size_t)P.inv_nnlist[(size_t)g * B + bi] * W + rr];
+            s_rowexp[r0] = e;
+          }
 #pragma unroll
-          for (int i = 0; i < 8; ++i) {
-            const int rw = tile * kTileRows + i * 16 + (pt >> 3);
+          for (int i = 0; i < R::NPASS; ++i) {
+            const int rw = tile * kTileRows + i * R::RPP + (pt >> 3);
             const int b2 = rw / WP, r2 = rw % WP;
             zrow[i] = (b2 < B && r2 < W)
                           ? P.tbuf + (size_t)P.inv_nnlist[(size_t)g * B + b2] * WW + (size_t)r2 * W
@@ -289,14 +304,15 @@ __global__ void __launch_bounds__(kThreads2, 1)
         for (int ks = 0; ks < KSTEPS; ++ks) {
           const int s = sseq % NS;
           const uint32_t use = (uint32_t)(sseq / NS);
-          double2 av[8];
+          double2 av[R::NPASS];
           if (STEP == 2) {
-            // the stage's 8 elements, loaded before the slot is free
+            // the stage's elements, loaded before the slot is free
             const int m = ks * 8 + (pt & 7);
 #pragma unroll
-            for (int i = 0; i < 8; ++i) av[i] = (zrow[i] && m < W) ? zrow[i][m] : make_double2(0.0, 0.0);
+            for (int i = 0; i < R::NPASS; ++i) av[i] = (zrow[i] && m < W) ? zrow[i][m] : make_double2(0.0, 0.0);
           }
-          if (!pwait(&a_empty[s], (use & 1) ^ 1, p)) {
+          // (the first use of each stage slot needs no wait)
+          if (use > 0 && !pwait(&a_empty[s], (use & 1) ^ 1, p)) {
             ok = false;
             break;
           }
@@ -316,10 +332,10 @@ __global__ void __launch_bounds__(kThreads2, 1)
               inflight_par = (inflight_par & ~(1u << s)) | ((use & 1) << s);
             }
           } else {
-            // 128 rows x 8 complex: each thread slices 8 elements into all 7 planes
+            // 128 rows x 8 complex: each thread slices NPASS elements into all 7 planes
 #pragma unroll
-            for (int i = 0; i < 8; ++i) {
-              const int r = i * 16 + (pt >> 3), l = pt & 7;
+            for (int i = 0; i < R::NPASS; ++i) {
+              const int r = i * R::RPP + (pt >> 3), l = pt & 7;
               const double2 a = av[i];
               const int ex = s_rowexp[r];
               int xr[kS], xi[kS];
@@ -365,7 +381,8 @@ __global__ void __launch_bounds__(kThreads2, 1)
         for (int tile = 0; tile < ntiles; ++tile) {
           const int a = useq % NACC;
           const uint32_t ause = (uint32_t)(useq / NACC);
-          if (!mbar_wait_role(smem_u32(&acc_empty[a]), (ause & 1) ^ 1, &s_bad)) {
+          // (the first use of each accumulator set needs no wait)
+          if (ause > 0 && !mbar_wait_role(smem_u32(&acc_empty[a]), (ause & 1) ^ 1, &s_bad)) {
             fail(p);
             ok = false;
             break;
@@ -418,7 +435,7 @@ __global__ void __launch_bounds__(kThreads2, 1)
     const int wq = warp & 3, cg = warp >> 2;            // TMEM lane quarter, column group
     const int r = wq * 32 + lane;                       // tile row = TMEM lane
     const uint32_t lane_base = (uint32_t)(wq * 32) << 16;
-    constexpr int CPG = CW / 4;                         // complex columns per warp
+    constexpr int CPG = CW / R::GROUPS;                 // complex columns per warp
     const int jbeg = cg * CPG;
     int gseq = 0, useq = 0;
     bool ok = true;
@@ -609,8 +626,8 @@ cudaError_t launch2_wp(int step, const Problem* probs, WorkMap wm, int which, in
   const int grid = ngroups < sm_count() ? ngroups : sm_count();
   if (grid <= 0) return cudaSuccess;
   const size_t sm = MU2<WP>::BYTES;
-  if (step == 1) k_oz_mupdate2<WP, 1><<<grid, kThreads2, sm, s>>>(probs, wm, which, ngroups);
-  else k_oz_mupdate2<WP, 2><<<grid, kThreads2, sm, s>>>(probs, wm, which, ngroups);
+  if (step == 1) k_oz_mupdate2<WP, 1><<<grid, Roles<1>::THREADS, sm, s>>>(probs, wm, which, ngroups);
+  else k_oz_mupdate2<WP, 2><<<grid, Roles<2>::THREADS, sm, s>>>(probs, wm, which, ngroups);
   return cudaGetLastError();
 }
 

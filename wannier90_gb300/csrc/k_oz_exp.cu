@@ -298,7 +298,7 @@ __device__ bool oz_cmm(OzCtx& cx, double2* C, const double2* A, const double2* B
 // ---------------------------------------------------------------------------
 constexpr int kS2 = 7;
 
-template <int WP>
+template <int WP, bool SMEM_MATS = false>
 struct Exp2Smem {
   static constexpr int CW = WP < 32 ? WP : 32;      // complex inner indices per K chunk
   static constexpr int KC = 2 * CW;                 // real K per chunk
@@ -314,7 +314,9 @@ struct Exp2Smem {
   static constexpr size_t STAGE_BYTES = STAGED ? (size_t)kS2 * ROWS * STAGE_LD * 4 : 0;
   static constexpr size_t DIGIT_BYTES = (size_t)A_BYTES + (size_t)kS2 * B_BYTES;
   static constexpr size_t REGION = DIGIT_BYTES > STAGE_BYTES ? DIGIT_BYTES : STAGE_BYTES;
-  static constexpr bool MATS_IN_SMEM = WP <= 16;
+  // the six FP64 matrices of the exp chain in shared memory: always for WP <= 16; for
+  // WP = 32 on request (one CTA per SM then, shared-memory latency for every operand read)
+  static constexpr bool MATS_IN_SMEM = WP <= 16 || SMEM_MATS;
   static constexpr size_t MAT_BYTES = (size_t)WP * WP * 16;
   static constexpr size_t NEED = REGION + (MATS_IN_SMEM ? 6 * MAT_BYTES : 0) + 1024;
   // never more CTAs on an SM than its 512 TMEM columns hold: request enough shared
@@ -517,9 +519,9 @@ struct ProdV1 {
   }
 };
 
-template <int WP>
+template <int WP, bool SMEM_MATS = false>
 struct ProdV2 {
-  using E = Exp2Smem<WP>;
+  using E = Exp2Smem<WP, SMEM_MATS>;
   static constexpr int TMEM_COLS = E::TMEM_COLS;
   static constexpr bool MATS_IN_SMEM = E::MATS_IN_SMEM;
   static constexpr size_t REGION = E::REGION, BYTES = E::BYTES;
@@ -529,8 +531,8 @@ struct ProdV2 {
   }
 };
 
-template <int WP>
-using ExpProd = typename std::conditional<(WP <= 64), ProdV2<WP>, ProdV1<WP>>::type;
+template <int WP, bool SMEM_MATS = false>
+using ExpProd = typename std::conditional<(WP <= 64), ProdV2<WP, SMEM_MATS>, ProdV1<WP>>::type;
 
 // make C exactly Hermitian (sign +1) or anti-Hermitian (sign -1) from its upper triangle,
 // as the FP64 path's structured products produce it
@@ -559,9 +561,9 @@ __device__ const double kOzInvFact[17] = {
 }  // namespace
 
 // which = 0: trial step (also forms D = coefG (G or Gp) + coefD D_prev); 1: optimal step
-template <int WP>
+template <int WP, bool SMEM_MATS>
 __global__ void __launch_bounds__(256, 2) k_oz_exp(const Problem* __restrict__ probs, WorkMap wm, int which) {
-  using E = ExpProd<WP>;
+  using E = ExpProd<WP, SMEM_MATS>;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   __shared__ __align__(8) uint64_t mbar;
@@ -724,35 +726,39 @@ __global__ void __launch_bounds__(256, 2) k_oz_exp(const Problem* __restrict__ p
   }
 }
 
-template <int WP>
+template <int WP, bool SM>
 static cudaError_t oz_exp_launch_wp(const Problem* probs, WorkMap wm, int which, int grid, cudaStream_t s) {
-  k_oz_exp<WP><<<grid, 256, ExpProd<WP>::BYTES, s>>>(probs, wm, which);
+  k_oz_exp<WP, SM><<<grid, 256, ExpProd<WP, SM>::BYTES, s>>>(probs, wm, which);
   return cudaGetLastError();
 }
 
-cudaError_t oz_exp_launch(int wp, const Problem* probs, WorkMap wm, int which, int grid, cudaStream_t s) {
+// smem_mats: num_wann 17..32, keep the chain's FP64 matrices in shared memory
+cudaError_t oz_exp_launch(int wp, int smem_mats, const Problem* probs, WorkMap wm, int which, int grid,
+                          cudaStream_t s) {
   switch (wp) {
-    case 8: return oz_exp_launch_wp<8>(probs, wm, which, grid, s);
-    case 16: return oz_exp_launch_wp<16>(probs, wm, which, grid, s);
-    case 32: return oz_exp_launch_wp<32>(probs, wm, which, grid, s);
-    case 64: return oz_exp_launch_wp<64>(probs, wm, which, grid, s);
-    default: return oz_exp_launch_wp<128>(probs, wm, which, grid, s);
+    case 8: return oz_exp_launch_wp<8, false>(probs, wm, which, grid, s);
+    case 16: return oz_exp_launch_wp<16, false>(probs, wm, which, grid, s);
+    case 32:
+      return smem_mats ? oz_exp_launch_wp<32, true>(probs, wm, which, grid, s)
+                       : oz_exp_launch_wp<32, false>(probs, wm, which, grid, s);
+    case 64: return oz_exp_launch_wp<64, false>(probs, wm, which, grid, s);
+    default: return oz_exp_launch_wp<128, false>(probs, wm, which, grid, s);
   }
 }
 
-template <int WP>
+template <int WP, bool SM>
 static cudaError_t oz_exp_attr_wp() {
-  return cudaFuncSetAttribute(k_oz_exp<WP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)ExpProd<WP>::BYTES);
+  return cudaFuncSetAttribute(k_oz_exp<WP, SM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)ExpProd<WP, SM>::BYTES);
 }
 
-cudaError_t oz_exp_set_attributes(int wp) {
+cudaError_t oz_exp_set_attributes(int wp, int smem_mats) {
   switch (wp) {
-    case 8: return oz_exp_attr_wp<8>();
-    case 16: return oz_exp_attr_wp<16>();
-    case 32: return oz_exp_attr_wp<32>();
-    case 64: return oz_exp_attr_wp<64>();
-    default: return oz_exp_attr_wp<128>();
+    case 8: return oz_exp_attr_wp<8, false>();
+    case 16: return oz_exp_attr_wp<16, false>();
+    case 32: return smem_mats ? oz_exp_attr_wp<32, true>() : oz_exp_attr_wp<32, false>();
+    case 64: return oz_exp_attr_wp<64, false>();
+    default: return oz_exp_attr_wp<128, false>();
   }
 }
 
