@@ -1249,8 +1249,10 @@ KNOWN_ITERS = {"dis_fcc8_b48w32": (200, 3053)}
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of the dominant
 # kernel, from the committed ncu captures under profiles/ (name of the summary beside each)
 NCU_TRAFFIC = {
-    # profiles/k_oz_mupdate_fcc10_w32.md: steps 1 + 2 of one M update
-    ("fcc10_w32", "k_m_update"): 584.4e6,
+    # profiles/k_oz_mupdate2_fcc10_w32.md: steps 1 + 2 of one M update
+    ("fcc10_w32", "k_m_update"): 584.1e6,
+    # profiles/k_oz_exp_fcc10_w32.md: one trial-step exp launch
+    ("fcc10_w32", "k_exp_u"): 139.2e6,
 }
 
 if __name__ == "__main__":

@@ -157,6 +157,7 @@ __global__ void __launch_bounds__(Roles<STEP>::THREADS, 1)
   __shared__ volatile int s_bad;
   __shared__ int s_bad_prob;
   __shared__ int s_pflag;
+  __shared__ int s_eflag;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (warp == kMmaWarp) {
@@ -463,12 +464,16 @@ __global__ void __launch_bounds__(Roles<STEP>::THREADS, 1)
           if (valid) erow = P.zexp[(size_t)kb_out * W + rr];
         }
         const size_t kb_in = (size_t)g * B + bi;    // step 1: block (k, b) of this row
-        int okw = 1;
-        if (lane == 0) {
-          okw = mbar_wait_role(smem_u32(&acc_full[a]), ause & 1, &s_bad) ? 1 : 0;
+        // one epilogue thread waits for the accumulators; the others wait at the epilogue
+        // group's named barrier (issuing nothing) and read the outcome
+        if (tid == 0) {
+          const bool okw = mbar_wait_role(smem_u32(&acc_full[a]), ause & 1, &s_bad);
           if (!okw) fail(p);
+          s_eflag = okw ? 0 : 1;
         }
-        okw = __shfl_sync(0xffffffffu, okw, 0);
+        bar_named(2, kEpiThreads);
+        const bool okw = s_eflag == 0;
+        bar_named(2, kEpiThreads);
         if (!okw) {
           ok = false;
           break;

@@ -232,9 +232,10 @@ __global__ void __launch_bounds__(256, 1) k_oz_mupdate(const Problem* __restrict
         }
         if (NCH > 1) slice_b(nc, kc);
         if (presliced) {
-          // bounded wait; on a timeout the error is recorded and the drain wait lets the
-          // copies in flight land before the CTA gives up its shared memory
-          if (!mbar_wait(smem_u32(&mbar_ld), phase_ld)) {
+          // bounded wait, by the MMA-issuing thread alone (the only reader of the copied
+          // planes); on a timeout the error is recorded and the drain wait lets the copies
+          // in flight land before the CTA gives up its shared memory
+          if (tid == 0 && !mbar_wait(smem_u32(&mbar_ld), phase_ld)) {
             s_bad = 1;
             mbar_drain(smem_u32(&mbar_ld), phase_ld);
           }
@@ -275,7 +276,8 @@ __global__ void __launch_bounds__(256, 1) k_oz_mupdate(const Problem* __restrict
           asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
                        :: "r"(smem_u32(&mbar)) : "memory");
         }
-        const bool ok_mine = mbar_wait(smem_u32(&mbar), phase);
+        // one thread waits for the commit (the others wait at the CTA barrier below)
+        const bool ok_mine = (tid != 0) || mbar_wait(smem_u32(&mbar), phase);
         if (!ok_mine) {
           // the MMAs may still run: record the error, then wait (drain limit) for their
           // commit before the CTA reads or frees tensor memory or reuses the operands
