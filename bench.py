@@ -767,10 +767,20 @@ def run_batch(args, wl):
     }
     if "mixed" in arms and "fp64" in arms:
         f64 = arms["fp64"]
-        rel = np.abs(arms["mixed"]["final"] - f64["final"]) / np.maximum(np.abs(f64["final"]), 1e-300)
+        fm, ff = arms["mixed"]["final"], f64["final"]
+        rel = np.abs(fm - ff) / np.maximum(np.abs(ff), 1e-300)
+        worst = int(np.argmax(rel))
+        # the problems are chaotic minimisations run for a fixed 300 iterations: the two
+        # arms' final spreads differ by where each trajectory has got to, not by roundoff
         line["fp64_gpu"] = {"value": n / f64["t_step"], "unit": "solves/s", "ms_per_step": 1e3 * f64["t_step"],
                             "mixed_over_fp64": f64["t_step"] / t_step,
-                            "final_spread_rel_diff": {"median": float(np.median(rel)), "max": float(rel.max())},
+                            "final_spread_rel_diff": {
+                                "median": float(np.median(rel)), "p90": float(np.percentile(rel, 90)),
+                                "max": float(rel.max()),
+                                "worst": {"problem": worst, "num_wann": probs[worst].num_wann,
+                                          "num_kpts": len(probs[worst].kpoints), "mixed": float(fm[worst]),
+                                          "fp64": float(ff[worst])},
+                                "mixed_lower": int(np.sum(fm < ff)), "fp64_lower": int(np.sum(ff < fm))},
                             "clocks": f64["clocks"]}
     print(json.dumps(line, default=float))
     return 0

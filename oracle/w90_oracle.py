@@ -1171,12 +1171,16 @@ def new_u_and_m(cdq, U, M, nnlist, sitesym=None):
     return Unew, Mnew
 
 
-def wann_main(M, U, km, ctl: WannControl, record=True, precond=None, rguide=None, slwf=None, sitesym=None):
+def wann_main(M, U, km, ctl: WannControl, record=True, precond=None, rguide=None, slwf=None, sitesym=None,
+              update_noise=None):
     """Restatement of wann_main.
     ``precond``: the tables of :func:`precond_setup` when ``ctl.precond``;
     ``rguide``: guiding centres [3,W] (Cartesian, Angstrom) when ``ctl.guiding_centres``;
     ``slwf``: :class:`Slwf` for selective localisation (slwf_num < num_wann);
-    ``sitesym``: :class:`Sitesym` for the symmetry-adapted mode (site_symmetry = T).
+    ``sitesym``: :class:`Sitesym` for the symmetry-adapted mode (site_symmetry = T);
+    ``update_noise``: test use only -- a function applied to every updated M (e.g. a
+    seeded relative perturbation modelling an implementation whose M update carries
+    rounding at that level); None for the reference's arithmetic.
     The mode-2 symmetrisation the reference applies to its global cdq array after the
     search direction (:589-591) acts on the previous step's rotation, which
     internal_new_u_and_m overwrites before reading it: it does not enter the run."""
@@ -1272,6 +1276,8 @@ def wann_main(M, U, km, ctl: WannControl, record=True, precond=None, rguide=None
             cdq_t = cdqkeep * (ctl.trial_step / (4.0 * wbtot))        # :605
             U0, M0 = U, M
             U, M = new_u_and_m(cdq_t, U0, M0, nnlist, sitesym)
+            if update_noise is not None:
+                M = update_noise(M)
             trial_spread, rave, r2ave, rave2 = wann_omega(M, km, om_invariant, sheet=sheet, slwf=slwf)
             # internal_optimal_step (:1528-1596)
             fac = trial_spread.om_tot - wann_spread.om_tot
@@ -1298,6 +1304,8 @@ def wann_main(M, U, km, ctl: WannControl, record=True, precond=None, rguide=None
             if not ctl.lfixstep:
                 U, M = U0, M0
             U, M = new_u_and_m(cdq_a, U, M, nnlist, sitesym)
+            if update_noise is not None:
+                M = update_noise(M)
             old_spread = wann_spread.copy()
             wann_spread, rave, r2ave, rave2 = wann_omega(M, km, om_invariant, sheet=sheet, slwf=slwf)
         else:

@@ -92,27 +92,44 @@ def dis_control(d):
                         frozen_states=bool(kn["frozen_states"]))
 
 
-def conv_sensitivity(M0, U0, km, ctl, noise=1e-14, runs=2, slwf=None, grad=False):
+def conv_sensitivity(M0, U0, km, ctl, noise=1e-14, runs=2, slwf=None, grad=False, centres=False, sitesym=None,
+                     per_update=False):
     """Per iteration, the largest change of the oracle's own wann_main spread when M0 is
     perturbed by `noise` (relative, seeded): the part of a printed trajectory that no FP64
-    implementation can reproduce more closely.  grad=True also returns the same for the
-    RMS gradient column."""
+    implementation can reproduce more closely.  per_update=True perturbs every updated M
+    instead (the model of the tensor path, whose M update carries ~1e-13 relative rounding
+    at every iteration).  grad=True also returns the same for the RMS gradient column;
+    centres=True also returns the largest change of any final centre coordinate (per WF,
+    A)."""
     import numpy as np
 
     from oracle import w90_oracle as O
-    base = O.wann_main(M0, U0, km, ctl, slwf=slwf)
+    base = O.wann_main(M0, U0, km, ctl, slwf=slwf, sitesym=sitesym)
     ref = {x.iter: x.spread.om_tot for x in [base.initial] + base.iters}
     gref = {x.iter: x.rms_grad for x in [base.initial] + base.iters}
     sens = {i: 0.0 for i in ref}
     gsens = {i: 0.0 for i in ref}
+    csens = np.zeros(np.asarray(base.centres).shape[1])
     rng = np.random.default_rng(2024)
     for _ in range(runs):
-        r = O.wann_main(M0 * (1 + noise * rng.standard_normal(M0.shape)), U0, km, ctl, slwf=slwf)
+        if per_update:
+            def perturb(M):
+                return M * (1 + noise * rng.standard_normal(M.shape))
+            r = O.wann_main(M0, U0, km, ctl, slwf=slwf, sitesym=sitesym, update_noise=perturb)
+        else:
+            r = O.wann_main(M0 * (1 + noise * rng.standard_normal(M0.shape)), U0, km, ctl, slwf=slwf,
+                            sitesym=sitesym)
         for x in [r.initial] + r.iters:
             if x.iter in sens:
                 sens[x.iter] = max(sens[x.iter], abs(x.spread.om_tot - ref[x.iter]))
                 gsens[x.iter] = max(gsens[x.iter], abs(x.rms_grad - gref[x.iter]))
-    return (sens, gsens) if grad else sens
+        csens = np.maximum(csens, np.abs(np.asarray(r.centres) - np.asarray(base.centres)).max(axis=0))
+    out = (sens,)
+    if grad:
+        out += (gsens,)
+    if centres:
+        out += (csens,)
+    return out if len(out) > 1 else sens
 
 
 def conv_tolerance(sens, it, spread, floor=2e-10, factor=10.0, span=0):

@@ -73,8 +73,8 @@ def test_slwf_golden_example26(tensor):
     assert window >= 2
     _check_rows(out, r, window, s)
     # against the reference's printed lines, over the whole run
-    sens = G.conv_sensitivity(M0, U0, km, ctl, noise=1e-13 if tensor else 1e-14, runs=4 if tensor else 3,
-                              slwf=sl)
+    sens, csens = G.conv_sensitivity(M0, U0, km, ctl, noise=1e-13 if tensor else 1e-14, runs=4 if tensor else 3,
+                                     slwf=sl, centres=True)
     log = out["log"]
     assert len(log) == len(d["conv"]) == len(d["sprd"])
     for row, (it, delta, rms, spread), (iod, od, tot) in zip(log, d["conv"], d["sprd"]):
@@ -83,10 +83,14 @@ def test_slwf_golden_example26(tensor):
                                span=3)
         assert abs(row[3] - spread) < tol, (int(it), row[3], spread, tol)
         assert abs(row[5] - iod) < 6e-8 + tol and abs(row[4] - od) < 6e-8 + tol
-    # final state: the objective WF is pinned; the others are outside the functional
+    # final state: the objective WF is pinned; the others are outside the functional.  The
+    # printed centres carry 6 decimals (5e-7 rounding); after 100 iterations the oracle's own
+    # objective centre moves by up to ~8e-7 A under a 1e-13 perturbation of M0, so the
+    # bound is the rounding plus the same factor times that movement as for the spreads
     fin = d["centres_final"]
     cen = out["centres"].T        # (W, 3)
-    np.testing.assert_allclose(cen[:s], fin[:s, :3], rtol=0, atol=1.01e-6)
+    ctol = max(1.01e-6, 5e-7 + (20.0 if tensor else 10.0) * float(csens[:s].max()))
+    np.testing.assert_allclose(cen[:s], fin[:s, :3], rtol=0, atol=ctol)
     np.testing.assert_allclose(out["spreads"][:s], fin[:s, 3], rtol=0, atol=2e-8)
     np.testing.assert_allclose(cen[s:], fin[s:, :3], rtol=0, atol=2e-5)
     iod_c, om_d, rest, penalty, total_c = d["omega_final_slwf"]

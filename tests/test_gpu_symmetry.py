@@ -77,11 +77,16 @@ def test_symmetry_adapted_golden_example21(tensor):
     log = out["log"]
     assert len(log) == len(d["conv"]) == len(r.iters) + 1
     tol = 2e-9 if tensor else 2e-10
+    # the RMS gradient near the minimum moves with the state at the 1e-6 level: the
+    # oracle's own value at iteration 20 (1.7e-6 printed) spreads over 1.7e-6 .. 4.2e-6
+    # when every M update carries 1e-13 relative noise, the tensor path's rounding level
+    _, gsens = G.conv_sensitivity(M0, U0, out["km"], out["ctl"], noise=1e-13 if tensor else 1e-15,
+                                  runs=4 if tensor else 2, grad=True, sitesym=sym, per_update=True)
     for row, x, (it, delta, rms, spread) in zip(log, [r.initial] + r.iters, d["conv"]):
         assert int(row[0]) == int(it) == x.iter
         assert abs(row[3] - x.spread.om_tot) < tol, (int(it), row[3], x.spread.om_tot)
         assert abs(row[3] - spread) < tol + 6e-11, (int(it), row[3], spread)
-        assert abs(row[2] - rms) < 1e-6 + 1e-3 * rms
+        assert abs(row[2] - rms) < G.grad_tolerance(gsens, it, rms, factor=3.0), (int(it), row[2], rms)
     fin = d["centres_final"]
     np.testing.assert_allclose(out["centres"].T, fin[:, :3], rtol=0, atol=1.01e-6)
     np.testing.assert_allclose(out["spreads"], fin[:, 3], rtol=0, atol=2e-8)

@@ -1,7 +1,8 @@
 """Selective localisation: the algebra the GPU kernels use, checked on the CPU.
 
-k_grad forms the gradient as G_mn = M_mn alpha_n + conj(M_nm) beta_m with per-column and
-per-row coefficients.  With selective localisation (slwf_num = s < num_wann) the reference's
+k_grad forms the gradient as G = (4/K)(P - P^H), P_mn = sum_b M_mn(k,b) alpha_n(k,b), with
+one coefficient per column: every term of the reference's expression is X - X^H of one
+(k,b) block.  With selective localisation (slwf_num = s < num_wann) the reference's
 term-by-term expression (src/wannierise.F90:2431-2509) factors the same way, with two
 coefficient variants per objective index j < s -- one for partners inside the objective
 block, one for partners outside it -- and zero coefficients for j >= s:
@@ -21,7 +22,8 @@ from tests import golden_cases as G
 
 
 def kernel_gradient(M, km, slwf):
-    """The factored gradient, coefficient by coefficient as k_grad computes it."""
+    """The factored gradient, coefficient by coefficient as k_grad computes it:
+    P_mn = sum_b M_mn alpha^{v(m)}_n, then G = (4/K)(P - P^H)."""
     K, B, W, _ = M.shape
     wb, bk = km["wb"], km["bk"]
     diag = np.diagonal(M, axis1=2, axis2=3)
@@ -29,13 +31,12 @@ def kernel_gradient(M, km, slwf):
     rave = -np.einsum("b,kbi,kbn->in", wb, bk, ln) / K       # the spread pass's rave
     s = slwf.num if slwf is not None else W
     lam = slwf.lam if slwf is not None else 0.0
-    G_ = np.zeros((K, W, W), dtype=np.complex128)
+    P_ = np.zeros((K, W, W), dtype=np.complex128)
     for k in range(K):
         for b in range(B):
             w = wb[b]
             brn = bk[k, b] @ rave
             alpha = np.zeros((2, W), dtype=np.complex128)
-            beta = np.zeros((2, W), dtype=np.complex128)
             for j in range(W):
                 d = diag[k, b, j]
                 inv = 1.0 / (d.real ** 2 + d.imag ** 2)
@@ -50,15 +51,12 @@ def kernel_gradient(M, km, slwf):
                 for v, q in enumerate(qs):
                     alpha[v, j] = complex(0.5 * w * d.real + 0.5 * q * inv * d.imag,
                                           -0.5 * w * d.imag + 0.5 * q * inv * d.real)
-                    beta[v, j] = complex(-0.5 * w * d.real - 0.5 * q * inv * d.imag,
-                                         -0.5 * w * d.imag + 0.5 * q * inv * d.real)
             Mb = M[k, b]
             for m in range(W):
-                for n in range(W):
-                    va = 0 if m < s else 1
-                    vb = 0 if n < s else 1
-                    G_[k, m, n] += Mb[m, n] * alpha[va, n] + np.conj(Mb[n, m]) * beta[vb, m]
-    return G_ * (4.0 / K)
+                P_[k, m, :] += Mb[m, :] * alpha[0 if m < s else 1, :]
+    fac = 4.0 / K
+    Ph = np.conj(np.swapaxes(P_, 1, 2))
+    return (P_.real - Ph.real) * fac + 1j * ((P_.imag - Ph.imag) * fac)
 
 
 def kernel_spread(M, km, slwf):
@@ -112,6 +110,8 @@ def test_factored_gradient_equals_reference_terms(s, lam, constrain):
     ref = O.wann_domega(M, km, slwf=sl)
     got = kernel_gradient(M, km, sl)
     np.testing.assert_allclose(got, ref, rtol=0, atol=1e-13 * np.abs(ref).max())
+    # exactly anti-Hermitian, as the reference's X - X^H terms are
+    assert np.array_equal(got, -np.conj(np.swapaxes(got, 1, 2)))
     # the objective block is non-zero, the non-objective block is exactly zero
     assert np.all(got[:, s:, s:] == 0)
     assert np.abs(got[:, :s, :s]).max() > 0

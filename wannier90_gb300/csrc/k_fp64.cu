@@ -349,7 +349,6 @@ __global__ void __launch_bounds__(256) k_omega_p3(const Problem* __restrict__ pr
 // ----------------------------------------------------------------------------
 // k_grad: wann_domega (src/wannierise.F90:2287-2569), both branches, fused with the
 // per-k partial dot products of internal_search_direction (:1424-1431).
-// grid: one CTA per (problem, k, tile_i, tile_j) of 32x32 tiles; 256 threads.
 // rave is the one computed by the preceding spread pass on the same M (the reference
 // recomputes it from the same data, :2378-2393).
 // ----------------------------------------------------------------------------
@@ -383,12 +382,21 @@ __device__ __forceinline__ bool grad_q(const Problem& P, double w, double l, dou
   return true;
 }
 
+// The gradient is anti-Hermitian, and the reference forms it exactly so: every term of
+// wann_domega is X - X^H of one (k,b) block (:2518-2527).  With
+//   alpha_n = wb/2 conj(M_nn) + (i/2) q_n / M_nn      (q_n from grad_q)
+// that sum is G = (4/K)(P - P^H),  P_mn = sum_b M_mn(k,b) alpha^{v(m)}_n(k,b),
+// where the variant v(m) selects q by the partner index m (inside / outside the objective
+// block; one variant without selective localisation).  So one complex FMA per element
+// and b, all reads coalesced down columns; the transpose happens once, in shared memory.
+// Grid: one CTA per (problem, k, ti, tj) of 32 x 32 tiles, 256 threads.  The CTA with
+// ti <= tj forms P over tiles (ti,tj) and (tj,ti) (one tile when ti == tj) and writes
+// G on both; a CTA with ti > tj only clears its partial slots.
+constexpr int kGradBC = 8;   // b values whose coefficients are staged together
+
 __global__ void __launch_bounds__(256) k_grad(const Problem* __restrict__ probs, WorkMap wm) {
-  __shared__ double2 sA[kTile * (kTile + 1)];   // A[j*(33)+i] = M(r0+i, c0+j)
-  __shared__ double2 sT[kTile * (kTile + 1)];   // T[i*(33)+j] = M(c0+j, r0+i)
-  // per-column / per-row coefficients of the factored gradient (see below); variant 0 for
-  // a partner index inside the objective block, 1 outside (equal without SLWF)
-  __shared__ double2 s_alpha[2][kTile], s_beta[2][kTile];
+  __shared__ double2 s_alpha[2][kGradBC][kTile];
+  __shared__ double2 sP[2][kTile * (kTile + 1)];   // sP[t][j*(33)+i]: P tile t, row i, column j
   __shared__ double red[256];
   int local;
   const int p = locate(wm, blockIdx.x, local);
@@ -399,96 +407,100 @@ __global__ void __launch_bounds__(256) k_grad(const Problem* __restrict__ probs,
   const int nt = (W + kTile - 1) / kTile;
   const int k = local / (nt * nt);
   const int tt = local % (nt * nt);
-  const int r0 = (tt % nt) * kTile, c0 = (tt / nt) * kTile;
-  const int nr = min(kTile, W - r0), nc = min(kTile, W - c0);
-  const double* rave = P.centres + (size_t)2 * 4 * W;  // accepted slot
-  const double2* Mk = P.M[st->cur] + (size_t)k * B * W * W;
+  const int ti = tt % nt, tj = tt / nt;
   const int t = threadIdx.x;
+  if (ti > tj) {
+    if (t == 0) {
+      P.gpart[(size_t)local * 2] = 0.0;
+      P.gpart[(size_t)local * 2 + 1] = 0.0;
+    }
+    return;
+  }
+  const double* rave = P.centres + (size_t)2 * 4 * W;  // accepted slot
+  const double2* __restrict__ Mk = P.M[st->cur] + (size_t)k * B * W * W;
   const int S = P.slwf_num > 0 ? P.slwf_num : W;   // objective WFs 0..S-1
-
-  double2 acc[4];
+  const int npass = (ti == tj) ? 1 : 2;
+  for (int pass = 0; pass < npass; ++pass) {
+    // P tile `pass`: rows R0.., columns C0..  (pass 0: (ti,tj); pass 1: (tj,ti))
+    const int R0 = (pass == 0 ? ti : tj) * kTile, C0 = (pass == 0 ? tj : ti) * kTile;
+    const int nr = min(kTile, W - R0), nc = min(kTile, W - C0);
+    double2 acc[4];
+    int vrow[4];
 #pragma unroll
-  for (int q = 0; q < 4; ++q) acc[q] = cmk(0, 0);
-
-  for (int b = 0; b < B; ++b) {
-    const double2* Mb = Mk + (size_t)b * W * W;
-    const double w = P.wb[b];
-    const double* bv = P.bk + ((size_t)k * B + b) * 3;
-    __syncthreads();
-    for (int e = t; e < kTile * kTile; e += 256) {
-      const int i = e % kTile, j = e / kTile;
-      if (i < nr && j < nc) sA[j * (kTile + 1) + i] = Mb[(size_t)(c0 + j) * W + r0 + i];
-      // transposed tile: rows c0.., cols r0..; coalesced over the row index
-      const int jj = e % kTile, ii = e / kTile;
-      if (jj < nc && ii < nr) sT[ii * (kTile + 1) + jj] = Mb[(size_t)(r0 + ii) * W + c0 + jj];
+    for (int q = 0; q < 4; ++q) {
+      acc[q] = cmk(0, 0);
+      const int i = (t + 256 * q) % kTile;
+      vrow[q] = (R0 + i < S) ? 0 : 1;
     }
-    // G_mn += wb/2 (M_mn conj(M_nn) - conj(M_nm) M_mm) + (i/2)(M_mn q_n / M_nn + conj(M_nm) q_m / conj(M_mm))
-    //       = M_mn alpha_n + conj(M_nm) beta_m,
-    // alpha_n =  wb/2 conj(M_nn) + (i/2) q_n / M_nn,   beta_m = -wb/2 M_mm + (i/2) q_m / conj(M_mm)
-    // with q = wb (Im ln M_nn + b.rave_n)  (src/wannierise.F90:2366-2375, :2409-2417, :2499-2527);
-    // selective localisation: q from grad_q, zero coefficients for non-objective indices
-    if (t < kTile) {
-      if (t < nr) {
-        const int m = r0 + t;
-        const double2 d = Mb[(size_t)m * W + m];
-        const double inv = 1.0 / (d.x * d.x + d.y * d.y);
-        const double brn = bv[0] * rave[m] + bv[1] * rave[W + m] + bv[2] * rave[2 * W + m];
-        double qv[2];
-        if (grad_q(P, w, diag_ln_of(P, ((size_t)k * B + b) * W + m, d), brn, bv, m, qv[0], qv[1])) {
-          // conj(1/M_mm) = d * inv ;  (i/2) q conj(1/M_mm) = (i/2) q inv (d.x + i d.y)
-          for (int v = 0; v < 2; ++v)
-            s_beta[v][t] = cmk(-0.5 * w * d.x - 0.5 * qv[v] * inv * d.y, -0.5 * w * d.y + 0.5 * qv[v] * inv * d.x);
-        } else {
-          s_beta[0][t] = s_beta[1][t] = cmk(0.0, 0.0);
+    for (int b0 = 0; b0 < B; b0 += kGradBC) {
+      const int nb = min(kGradBC, B - b0);
+      __syncthreads();   // the previous chunk's coefficients are consumed
+      // coefficients of the chunk: thread (bl, u) for column n = C0 + u of block b0 + bl
+      {
+        const int bl = t / kTile, u = t % kTile;
+        if (bl < nb && u < nc) {
+          const int b = b0 + bl, n = C0 + u;
+          const double w = P.wb[b];
+          const double* bv = P.bk + ((size_t)k * B + b) * 3;
+          const double2 d = Mk[((size_t)b * W + n) * W + n];
+          const double inv = 1.0 / (d.x * d.x + d.y * d.y);
+          const double brn = bv[0] * rave[n] + bv[1] * rave[W + n] + bv[2] * rave[2 * W + n];
+          double qv[2];
+          if (grad_q(P, w, diag_ln_of(P, ((size_t)k * B + b) * W + n, d), brn, bv, n, qv[0], qv[1])) {
+            // 1/M_nn = (d.x - i d.y) inv ;  (i/2) q / M_nn = (q inv / 2)(d.y + i d.x)
+            for (int v = 0; v < 2; ++v)
+              s_alpha[v][bl][u] = cmk(0.5 * w * d.x + 0.5 * qv[v] * inv * d.y, -0.5 * w * d.y + 0.5 * qv[v] * inv * d.x);
+          } else {
+            s_alpha[0][bl][u] = s_alpha[1][bl][u] = cmk(0.0, 0.0);
+          }
         }
       }
-    } else if (t < 2 * kTile) {
-      const int u = t - kTile;
-      if (u < nc) {
-        const int n = c0 + u;
-        const double2 d = Mb[(size_t)n * W + n];
-        const double inv = 1.0 / (d.x * d.x + d.y * d.y);
-        const double brn = bv[0] * rave[n] + bv[1] * rave[W + n] + bv[2] * rave[2 * W + n];
-        double qv[2];
-        if (grad_q(P, w, diag_ln_of(P, ((size_t)k * B + b) * W + n, d), brn, bv, n, qv[0], qv[1])) {
-          // 1/M_nn = (d.x - i d.y) inv ;  (i/2) q / M_nn = (q inv / 2)(d.y + i d.x)
-          for (int v = 0; v < 2; ++v)
-            s_alpha[v][u] = cmk(0.5 * w * d.x + 0.5 * qv[v] * inv * d.y, -0.5 * w * d.y + 0.5 * qv[v] * inv * d.x);
-        } else {
-          s_alpha[0][u] = s_alpha[1][u] = cmk(0.0, 0.0);
+      __syncthreads();
+      // P_mn += M_mn alpha^{v(m)}_n; four b blocks' loads issued together
+#pragma unroll 4
+      for (int bl = 0; bl < nb; ++bl) {
+        const double2* Mb = Mk + (size_t)(b0 + bl) * W * W;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int e = t + 256 * q;
+          const int i = e % kTile, j = e / kTile;
+          if (i < nr && j < nc) cfma(acc[q], Mb[(size_t)(C0 + j) * W + R0 + i], s_alpha[vrow[q]][bl][j]);
         }
       }
     }
-    __syncthreads();
 #pragma unroll
-    for (int qq = 0; qq < 4; ++qq) {
-      const int e = t + 256 * qq;
-      const int i = e % kTile, j = e / kTile;
-      if (i < nr && j < nc) {
-        const double2 mmn = sA[j * (kTile + 1) + i];    // M_mn
-        const double2 mnm = sT[i * (kTile + 1) + j];    // M_nm
-        // variant by the partner index: row m for alpha_n, column n for beta_m
-        cfma(acc[qq], mmn, s_alpha[r0 + i < S ? 0 : 1][j]);
-        cfmac(acc[qq], mnm, s_beta[c0 + j < S ? 0 : 1][i]);
-      }
+    for (int q = 0; q < 4; ++q) {
+      const int e = t + 256 * q;
+      sP[pass][(e / kTile) * (kTile + 1) + e % kTile] = acc[q];
     }
   }
-  // scale, store, partial dot products
+  __syncthreads();
+  // G = fac (P - P^H) on tile (ti,tj) and, off the diagonal, on tile (tj,ti):
+  // G_mn = fac (P_mn - conj(P_nm)); the mirrored element is the exact -conj of it
   const double fac = 4.0 / (double)K;
   double g2 = 0.0, gd = 0.0;
   double2* Gk = P.G + (size_t)k * W * W;
   const double2* Dk = P.D + (size_t)k * W * W;
+  const int other = npass - 1;   // sP index of the transposed tile
+  for (int pass = 0; pass < npass; ++pass) {
+    const int R0 = (pass == 0 ? ti : tj) * kTile, C0 = (pass == 0 ? tj : ti) * kTile;
+    const int nr = min(kTile, W - R0), nc = min(kTile, W - C0);
+    const double2* mine = sP[pass == 0 ? 0 : 1];
+    const double2* tr = sP[pass == 0 ? other : 0];
 #pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    const int e = t + 256 * q;
-    const int i = e % kTile, j = e / kTile;
-    if (i < nr && j < nc) {
-      const double2 g = cscale(acc[q], fac);
-      const size_t off = (size_t)(c0 + j) * W + r0 + i;
-      Gk[off] = g;
-      const double2 d = Dk[off];
-      g2 += g.x * g.x + g.y * g.y;
-      gd += g.x * d.x + g.y * d.y;
+    for (int q = 0; q < 4; ++q) {
+      const int e = t + 256 * q;
+      const int i = e % kTile, j = e / kTile;
+      if (i < nr && j < nc) {
+        const double2 a = mine[j * (kTile + 1) + i];
+        const double2 c = tr[i * (kTile + 1) + j];   // P_nm: row j, column i of the transposed tile
+        const double2 g = cmk(fac * (a.x - c.x), fac * (a.y + c.y));
+        const size_t off = (size_t)(C0 + j) * W + R0 + i;
+        Gk[off] = g;
+        const double2 d = Dk[off];
+        g2 += g.x * g.x + g.y * g.y;
+        gd += g.x * d.x + g.y * d.y;
+      }
     }
   }
   g2 = block_sum(g2, red);

@@ -74,22 +74,46 @@ struct OzCtx {
   int* bad;
 };
 
+// Scale records of the chain's matrices: for every row and column the key of its largest
+// |re| or |im| (0 for none, else the biased exponent + 1; the exponent above that value
+// is key - 1023, as exp_above_bits gives it).  The epilogue that writes a matrix forms its
+// record with shared-memory maxima, so that the products reading the matrix take their
+// scales from shared memory instead of a pass over the operand.
+__device__ __forceinline__ unsigned scale_key(double re, double im) {
+  const unsigned long long ab = max(abs_bits(re), abs_bits(im));
+  return ab ? (unsigned)(ab >> 52) + 1u : 0u;
+}
+__device__ __forceinline__ int key_exp(unsigned key) { return key ? (int)key - 1023 : 0; }
+
+struct Rec {
+  unsigned* row;
+  unsigned* col;
+};
+
 // Power-of-two scales of a product: the exponent above the largest |re| or |im| of every
-// row of A and every column of B.  The 2 WP rows / columns share the CTA's 256 threads
-// (TPI consecutive lanes each, then a max across those lanes), so each thread reads
-// W / TPI entries instead of W; the maximum does not depend on the order.
+// row of A and every column of B, from the operands' records where given (arow / bcol),
+// else by a pass over them.  The 2 WP rows / columns share the CTA's 256 threads (TPI
+// consecutive lanes each, then a max across those lanes), so each thread reads W / TPI
+// entries instead of W; the maximum does not depend on the order.
 template <int WP>
-__device__ __forceinline__ void ab_exponents(OzCtx& cx, const double2* A, const double2* B, int W) {
+__device__ __forceinline__ void ab_exponents(OzCtx& cx, const double2* A, const unsigned* arow,
+                                             const double2* B, const unsigned* bcol, int W) {
   constexpr int ITEMS = 2 * WP;
   constexpr int TPI = ITEMS >= 256 ? 1 : (256 / ITEMS > 32 ? 32 : 256 / ITEMS);
+  if (arow != nullptr && bcol != nullptr) {
+    for (int i = threadIdx.x; i < ITEMS; i += blockDim.x)
+      (i < WP ? cx.rowexp : cx.colexp)[i % WP] = key_exp(i < WP ? arow[i] : bcol[i - WP]);
+    return;
+  }
   for (int base = 0; base < ITEMS * TPI; base += blockDim.x) {
     const int gi = base + (int)threadIdx.x;
     const int idx = gi / TPI, sub = gi % TPI;
     const int r = idx % WP;
+    const bool row_of_a = idx < WP;
+    const unsigned* rec = row_of_a ? arow : bcol;
     unsigned long long mx = 0ull;
-    if (idx < ITEMS && r < W) {
+    if (idx < ITEMS && r < W && rec == nullptr) {
       // eight independent loads per round (the matrices may sit in L2), then the max
-      const bool row_of_a = idx < WP;
       for (int l0 = sub; l0 < W; l0 += 8 * TPI) {
         double2 v[8];
 #pragma unroll
@@ -104,19 +128,93 @@ __device__ __forceinline__ void ab_exponents(OzCtx& cx, const double2* A, const 
 #pragma unroll
     for (int o = 1; o < TPI; o <<= 1)
       mx = max(mx, (unsigned long long)__shfl_xor_sync(0xffffffffu, (long long)mx, o));
-    if (idx < ITEMS && sub == 0) (idx < WP ? cx.rowexp : cx.colexp)[r] = exp_above_bits(mx);
+    if (idx < ITEMS && sub == 0)
+      (row_of_a ? cx.rowexp : cx.colexp)[r] = rec != nullptr ? key_exp(rec[r]) : exp_above_bits(mx);
   }
 }
 
+// Where a product's result goes: `out`, made exactly Hermitian (sym = +1) or
+// anti-Hermitian (sym = -1) from its upper triangle as the FP64 path's structured products
+// produce it, or plain (sym = 0) with an elementwise term added (Add), and its scale
+// record formed in `rec` (rec.row == nullptr: none).
+struct Epi {
+  double2* out;
+  int sym;
+  Rec rec;
+};
+
+// no elementwise term
+struct NoAdd {
+  static constexpr bool kActive = false;
+  __device__ double2 operator()(int) const { return make_double2(0.0, 0.0); }
+};
+
+// block q of the Paterson-Stockmeyer polynomial, added by a Horner step's epilogue
+template <class F>
+struct HornerAdd {
+  static constexpr bool kActive = true;
+  const F* f;
+  int q;
+  __device__ double2 operator()(int e) const { return (*f)(q, e); }
+};
+
+__device__ __forceinline__ void rec_clear(const Rec& r, int n) {
+  if (r.row != nullptr)
+    for (int i = threadIdx.x; i < 2 * n; i += blockDim.x) (i < n ? r.row : r.col)[i % n] = 0u;
+}
+
+__device__ __forceinline__ void rec_add(const Rec& r, int i, int j, double2 v) {
+  if (r.row != nullptr) {
+    const unsigned key = scale_key(v.x, v.y);
+    if (key) {
+      atomicMax(r.row + i, key);
+      atomicMax(r.col + j, key);
+    }
+  }
+}
+
+// Applies an Epi to a product already in C (the product forms whose epilogue does not
+// apply it directly): out[e] from C[e] (its upper triangle when sym != 0) plus add(e),
+// and the record.  out may be C.  All threads call.
+template <int WP, class Add>
+__device__ void epi_apply(const double2* C, const Epi& ep, const Add& add, int W) {
+  if (ep.sym == 0 && !Add::kActive && ep.rec.row == nullptr && ep.out == C) return;
+  rec_clear(ep.rec, WP);
+  __syncthreads();
+#pragma unroll 4
+  for (int e = threadIdx.x; e < W * W; e += blockDim.x) {
+    const int i = e % W, j = e / W;
+    double2 v;
+    bool write = ep.out != C || Add::kActive;
+    if (ep.sym != 0 && i > j) {
+      const double2 u = C[(size_t)i * W + j];
+      v = cmk(ep.sym * u.x, -ep.sym * u.y);
+      write = true;
+    } else if (ep.sym != 0 && i == j) {
+      const double2 d = C[e];
+      v = (ep.sym > 0) ? cmk(d.x, 0.0) : cmk(0.0, d.y);
+      write = true;
+    } else {
+      v = C[e];
+    }
+    if (Add::kActive) v = cadd(v, add(e));
+    if (write) ep.out[e] = v;
+    rec_add(ep.rec, i, j, v);
+  }
+  __syncthreads();
+}
+
 // C = A B for W x W complex column-major matrices (generic pointers; C must not alias
-// A or B).  All threads call; returns false (uniformly) if an MMA wait timed out.
-template <int WP>
-__device__ bool oz_cmm(OzCtx& cx, double2* C, const double2* A, const double2* B, int W) {
+// A or B), then the Epi applied from C.  All threads call; returns false (uniformly) if
+// an MMA wait timed out.
+template <int WP, class Add>
+__device__ bool oz_cmm(OzCtx& cx, double2* C, const double2* A, const unsigned* arow, const double2* B,
+                       const unsigned* bcol, int W, const Epi& ep, const Add& add) {
   using E = ExpSmem<WP>;
   constexpr int CW = E::CW, KC = E::KC, NC = E::NC, NCH = E::NCH;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   // ---- power-of-two scales: rows of A, columns of B (over re and im parts)
-  ab_exponents<WP>(cx, A, B, W);
+  ab_exponents<WP>(cx, A, arow, B, bcol, W);
   __syncthreads();
   const uint32_t idesc = idesc_bf16(NC);
   bool ok = true;
@@ -188,8 +286,8 @@ __device__ bool oz_cmm(OzCtx& cx, double2* C, const double2* A, const double2* B
         asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
                      :: "r"(cx.mbar) : "memory");
       }
-      const bool ok_mine = mbar_wait(cx.mbar, cx.phase);
-      if (!ok_mine) {
+      // one thread waits for the commit (the others wait at the CTA barrier, issuing nothing)
+      if (tid == 0 && !mbar_wait(cx.mbar, cx.phase)) {
         // record the error; drain the MMAs before tensor memory or the operands are reused
         *cx.bad = 1;
         mbar_drain(cx.mbar, cx.phase);
@@ -283,6 +381,7 @@ __device__ bool oz_cmm(OzCtx& cx, double2* C, const double2* A, const double2* B
     __syncthreads();
   }
   __syncthreads();
+  if (ok) epi_apply<WP>(C, ep, add, W);
   return ok;
 }
 
@@ -325,12 +424,16 @@ struct Exp2Smem {
   static constexpr size_t BYTES = NEED > FLOOR ? NEED : FLOOR;
 };
 
-template <int WP>
-__device__ bool oz_cmm2(OzCtx& cx, double2* C, const double2* A, const double2* B, int W) {
+// C = A B, then the Epi.  num_wann <= 32 (staged accumulators): the epilogue applies the
+// Epi itself and writes ep.out only (C unused; ep.out may alias B, whose digits are in
+// shared memory before the MMAs run, but not A); WP = 64: C as in oz_cmm.
+template <int WP, class Add>
+__device__ bool oz_cmm2(OzCtx& cx, double2* C, const double2* A, const unsigned* arow, const double2* B,
+                        const unsigned* bcol, int W, const Epi& ep, const Add& add) {
   using E = Exp2Smem<WP>;
   constexpr int CW = E::CW, KC = E::KC, N = E::N;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  ab_exponents<WP>(cx, A, B, W);
+  ab_exponents<WP>(cx, A, arow, B, bcol, W);
   __syncthreads();
   const uint32_t idesc = idesc_bf16(N);
   // a warp slices 4 rows x 8 consecutive K, i.e. whole 16-byte core-matrix rows
@@ -428,8 +531,8 @@ __device__ bool oz_cmm2(OzCtx& cx, double2* C, const double2* A, const double2* 
       asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
                    :: "r"(cx.mbar) : "memory");
     }
-    const bool ok_mine = mbar_wait(cx.mbar, cx.phase);
-    if (!ok_mine) {
+    // one thread waits for the commit (the others wait at the CTA barrier, issuing nothing)
+    if (tid == 0 && !mbar_wait(cx.mbar, cx.phase)) {
       *cx.bad = 1;
       mbar_drain(cx.mbar, cx.phase);
     }
@@ -451,6 +554,7 @@ __device__ bool oz_cmm2(OzCtx& cx, double2* C, const double2* A, const double2* 
     const uint32_t lane_base = (uint32_t)(wq * 32) << 16;
     constexpr int NH = N / 2;   // columns per warp half
     if (E::STAGED) {
+      rec_clear(ep.rec, WP);     // the operands' scales are in cx already
       uint32_t* stage = (uint32_t*)cx.sA;
       if (wq * 32 < E::ROWS) {
 #pragma unroll 1
@@ -476,10 +580,43 @@ __device__ bool oz_cmm2(OzCtx& cx, double2* C, const double2* A, const double2* 
         }
       }
       __syncthreads();
-      for (int e = tid; e < 2 * W * W; e += blockDim.x) {
-        const int rr = e % W, c = (e / W) % W, part = e / (W * W);
-        const int row = part * WP + rr;
-        recombine(stage + (size_t)row * E::STAGE_LD + c, E::ROWS * E::STAGE_LD, row, c);
+      // both parts of element (rr, c) by one thread
+      auto element = [&](int rr, int c) -> double2 {
+        const int sc = cx.rowexp[rr] + cx.colexp[c] - 62;
+        const double re = recombine7x8(stage + (size_t)rr * E::STAGE_LD + c, E::ROWS * E::STAGE_LD, sc);
+        const double im = recombine7x8(stage + (size_t)(WP + rr) * E::STAGE_LD + c, E::ROWS * E::STAGE_LD, sc);
+        return make_double2(re, im);
+      };
+      if (ep.sym == 0) {
+#pragma unroll 2
+        for (int e = tid; e < W * W; e += blockDim.x) {
+          const int rr = e % W, c = e / W;
+          double2 v = element(rr, c);
+          if (Add::kActive) v = cadd(v, add(e));
+          ep.out[e] = v;
+          rec_add(ep.rec, rr, c, v);
+        }
+      } else {
+        // the upper triangle rr <= c (linear index e = c (c + 1) / 2 + rr), mirrored
+        const int ntri = W * (W + 1) / 2;
+        for (int e = tid; e < ntri; e += blockDim.x) {
+          int c = (int)((sqrtf(8.0f * (float)e + 1.0f) - 1.0f) * 0.5f);
+          while (c * (c + 1) / 2 > e) --c;
+          while ((c + 1) * (c + 2) / 2 <= e) ++c;
+          const int rr = e - c * (c + 1) / 2;
+          double2 v = element(rr, c);
+          if (rr == c) {
+            v = (ep.sym > 0) ? cmk(v.x, 0.0) : cmk(0.0, v.y);
+            ep.out[(size_t)c * W + c] = v;
+            rec_add(ep.rec, c, c, v);
+          } else {
+            ep.out[(size_t)c * W + rr] = v;
+            const double2 m = cmk(ep.sym * v.x, -ep.sym * v.y);
+            ep.out[(size_t)rr * W + c] = m;
+            rec_add(ep.rec, rr, c, v);
+            rec_add(ep.rec, c, rr, m);
+          }
+        }
       }
     } else {
       const int row = wq * 32 + lane;   // all 128 lanes hold rows (ROWS = 128)
@@ -503,6 +640,7 @@ __device__ bool oz_cmm2(OzCtx& cx, double2* C, const double2* A, const double2* 
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
+  if (ok && !E::STAGED) epi_apply<WP>(C, ep, add, W);
   return ok;
 }
 
@@ -514,8 +652,10 @@ struct ProdV1 {
   static constexpr bool MATS_IN_SMEM = E::MATS_IN_SMEM;
   static constexpr size_t REGION = E::REGION, BYTES = E::BYTES;
   static constexpr size_t SB_OFFSET = E::A_BYTES;
-  __device__ static bool mm(OzCtx& cx, double2* C, const double2* A, const double2* B, int W) {
-    return oz_cmm<WP>(cx, C, A, B, W);
+  template <class Add>
+  __device__ static bool mm(OzCtx& cx, double2* C, const double2* A, const unsigned* arow, const double2* B,
+                            const unsigned* bcol, int W, const Epi& ep, const Add& add) {
+    return oz_cmm<WP>(cx, C, A, arow, B, bcol, W, ep, add);
   }
 };
 
@@ -526,30 +666,15 @@ struct ProdV2 {
   static constexpr bool MATS_IN_SMEM = E::MATS_IN_SMEM;
   static constexpr size_t REGION = E::REGION, BYTES = E::BYTES;
   static constexpr size_t SB_OFFSET = E::A_BYTES;
-  __device__ static bool mm(OzCtx& cx, double2* C, const double2* A, const double2* B, int W) {
-    return oz_cmm2<WP>(cx, C, A, B, W);
+  template <class Add>
+  __device__ static bool mm(OzCtx& cx, double2* C, const double2* A, const unsigned* arow, const double2* B,
+                            const unsigned* bcol, int W, const Epi& ep, const Add& add) {
+    return oz_cmm2<WP>(cx, C, A, arow, B, bcol, W, ep, add);
   }
 };
 
 template <int WP, bool SMEM_MATS = false>
 using ExpProd = typename std::conditional<(WP <= 64), ProdV2<WP, SMEM_MATS>, ProdV1<WP>>::type;
-
-// make C exactly Hermitian (sign +1) or anti-Hermitian (sign -1) from its upper triangle,
-// as the FP64 path's structured products produce it
-__device__ void mirror(double2* C, int W, double sign) {
-#pragma unroll 4
-  for (int e = threadIdx.x; e < W * W; e += blockDim.x) {
-    const int i = e % W, j = e / W;
-    if (i > j) {
-      const double2 u = C[(size_t)i * W + j];
-      C[e] = cmk(sign * u.x, -sign * u.y);
-    } else if (i == j) {
-      const double2 d = C[e];
-      C[e] = (sign > 0) ? cmk(d.x, 0.0) : cmk(0.0, d.y);
-    }
-  }
-  __syncthreads();
-}
 
 __device__ const double kOzInvFact[17] = {
     1.0, 1.0, 0.5, 1.6666666666666666e-01, 4.1666666666666664e-02, 8.3333333333333332e-03,
@@ -569,6 +694,7 @@ __global__ void __launch_bounds__(256, 2) k_oz_exp(const Problem* __restrict__ p
   __shared__ __align__(8) uint64_t mbar;
   __shared__ uint32_t tmem_slot;
   __shared__ int s_rowexp[WP], s_colexp[WP];
+  __shared__ unsigned s_key[6][2][WP];
   __shared__ int s_bad;
   __shared__ double red[256];
 
@@ -652,19 +778,26 @@ __global__ void __launch_bounds__(256, 2) k_oz_exp(const Problem* __restrict__ p
       js = j;
     }
   }
+  // scale records of X, Y2, Y3, Y4, R, T (see Rec)
+  Rec rX{s_key[0][0], s_key[0][1]}, rY2{s_key[1][0], s_key[1][1]}, rY3{s_key[2][0], s_key[2][1]},
+      rY4{s_key[3][0], s_key[3][1]}, rR{s_key[4][0], s_key[4][1]}, rT{s_key[5][0], s_key[5][1]};
   const double sc = ldexp(1.0, -js);
-  #pragma unroll 4
-  for (int e = tid; e < WW; e += blockDim.x) X[e] = cscale(X[e], sc);
+  rec_clear(rX, WP);
   __syncthreads();
-  bool ok = E::mm(cx, Y2, X, X, W);
-  if (ok) mirror(Y2, W, 1.0);
-  if (ok) ok = E::mm(cx, Y3, Y2, X, W);
-  if (ok) mirror(Y3, W, -1.0);
-  if (ok && pw >= 4) {
-    ok = E::mm(cx, Y4, Y2, Y2, W);
-    if (ok) mirror(Y4, W, 1.0);
+  #pragma unroll 4
+  for (int e = tid; e < WW; e += blockDim.x) {
+    const double2 v = cscale(X[e], sc);
+    X[e] = v;
+    rec_add(rX, e % W, e / W, v);
   }
+  __syncthreads();
+  const NoAdd none;
+  // powers, exactly Hermitian (even) / anti-Hermitian (odd) as the FP64 path forms them
+  bool ok = E::mm(cx, Y2, X, rX.row, X, rX.col, W, Epi{Y2, 1, rY2}, none);
+  if (ok) ok = E::mm(cx, Y3, Y2, rY2.row, X, rX.col, W, Epi{Y3, -1, rY3}, none);
+  if (ok && pw >= 4) ok = E::mm(cx, Y4, Y2, rY2.row, Y2, rY2.col, W, Epi{Y4, 1, rY4}, none);
   const double2* Yp = (pw == 4) ? Y4 : Y3;
+  const Rec rYp = (pw == 4) ? rY4 : rY3;
   const int nblk = (m + pw) / pw;
   auto blk = [&](int q, int e) -> double2 {
     const int i = e % W, j = e / W;
@@ -683,29 +816,42 @@ __global__ void __launch_bounds__(256, 2) k_oz_exp(const Problem* __restrict__ p
     return v;
   };
   int q = nblk - 1;
+  rec_clear(rR, WP);
+  __syncthreads();
   if (pw * q == m) {
     const double cm = kOzInvFact[m];
     #pragma unroll 4
-    for (int e = tid; e < WW; e += blockDim.x) R[e] = cadd(cscale(Yp[e], cm), blk(q - 1, e));
+    for (int e = tid; e < WW; e += blockDim.x) {
+      const double2 v = cadd(cscale(Yp[e], cm), blk(q - 1, e));
+      R[e] = v;
+      rec_add(rR, e % W, e / W, v);
+    }
     q -= 1;
   } else {
     #pragma unroll 4
-    for (int e = tid; e < WW; e += blockDim.x) R[e] = blk(q, e);
+    for (int e = tid; e < WW; e += blockDim.x) {
+      const double2 v = blk(q, e);
+      R[e] = v;
+      rec_add(rR, e % W, e / W, v);
+    }
   }
   __syncthreads();
+  // Horner steps R <- Yp R + block q (the product's epilogue adds the block)
   for (q = q - 1; q >= 0 && ok; --q) {
-    ok = E::mm(cx, T, Yp, R, W);
-    #pragma unroll 4
-    for (int e = tid; e < WW; e += blockDim.x) R[e] = cadd(T[e], blk(q, e));
-    __syncthreads();
+    const HornerAdd<decltype(blk)> hadd{&blk, q};
+    ok = E::mm(cx, T, Yp, rYp.row, R, rR.col, W, Epi{R, 0, rR}, hadd);
   }
   double2* a = R;
   double2* b = T;
+  Rec ra = rR, rb = rT;
   for (int sq = 0; sq < js && ok; ++sq) {
-    ok = E::mm(cx, b, a, a, W);
+    ok = E::mm(cx, b, a, ra.row, a, ra.col, W, Epi{b, 0, rb}, none);
     double2* tmp = a;
     a = b;
     b = tmp;
+    const Rec rt = ra;
+    ra = rb;
+    rb = rt;
   }
   // dU = exp(s D);  U[cur^1] = U[cur] dU
   double2* dUk = P.dU + (size_t)k * WW;
@@ -713,7 +859,9 @@ __global__ void __launch_bounds__(256, 2) k_oz_exp(const Problem* __restrict__ p
   for (int e = tid; e < WW; e += blockDim.x) dUk[e] = a[e];
   __syncthreads();
   const int cur = st->cur;
-  if (ok) ok = E::mm(cx, P.U[cur ^ 1] + (size_t)k * WW, P.U[cur] + (size_t)k * WW, a, W);
+  double2* Unew = P.U[cur ^ 1] + (size_t)k * WW;
+  if (ok) ok = E::mm(cx, Unew, P.U[cur] + (size_t)k * WW, nullptr, a, ra.col, W, Epi{Unew, 0, Rec{nullptr, nullptr}},
+                     none);
   if (tid == 0) atomicAdd(&st->exp_products, best + 1.0);
   if (!ok && tid == 0) {
     st->error = 2;
