@@ -36,19 +36,23 @@ namespace {
 
 constexpr int kDynBudget = 232448 - 5120;                 // opt-in smem minus static use and slack
 
-// Warp roles per step.  Step 1's A operand arrives by bulk copy, so its producer is light
-// and 16 epilogue warps (4 per TMEM lane quarter) share the recombination; step 2 slices Z
-// in its producer, which gets 8 warps, and 8 epilogue warps remain.
+// Warp roles per step: 16 epilogue warps (4 per TMEM lane quarter) share the exact
+// recombination; the producer is split into an A producer, which fills the ring of K-step
+// stages, and a B producer, which slices the next group's shared operand into the other B
+// buffer meanwhile.  Step 1's A operand arrives by bulk copy (one thread issues it), so its
+// B producer gets 3 warps; step 2 slices Z, so its A producer gets 4 warps and B one.
+// (21-22 warps: at most 6 per SM sub-partition, so at most 80 registers per thread.)
 template <int STEP>
 struct Roles {
-  static constexpr int EPI = STEP == 1 ? 16 : 8;           // epilogue warps 0 .. EPI-1
-  static constexpr int PROD = STEP == 1 ? 4 : 8;           // producer warps EPI .. EPI+PROD-1
-  static constexpr int MMA = EPI + PROD;                   // the MMA-issue warp
+  static constexpr int EPI = 16;                           // epilogue warps 0 .. EPI-1
+  static constexpr int PA = STEP == 1 ? 1 : 4;             // A producer warps EPI ..
+  static constexpr int PB = STEP == 1 ? 3 : 1;             // B producer warps EPI + PA ..
+  static constexpr int MMA = EPI + PA + PB;                // the MMA-issue warp
   static constexpr int THREADS = (MMA + 1) * 32;
-  static constexpr int ET = EPI * 32, PT = PROD * 32;
+  static constexpr int ET = EPI * 32, PAT = PA * 32, PBT = PB * 32;
   static constexpr int GROUPS = EPI / 4;                   // column groups per lane quarter
-  static constexpr int RPP = PT / 8;                       // rows per slicing pass (8 K each)
-  static constexpr int NPASS = kTileRows / RPP;            // passes over a stage's 128 rows
+  static constexpr int AITEMS = 2 * kTileRows;             // step 2: (row, part) slicing items per stage
+  static constexpr int AIPT = (AITEMS + PAT - 1) / PAT;     // ... per A-producer thread
 };
 
 constexpr int pow2_cols(int c) { return c <= 32 ? 32 : (c <= 64 ? 64 : (c <= 128 ? 128 : (c <= 256 ? 256 : 512))); }
@@ -142,7 +146,7 @@ __global__ void __launch_bounds__(Roles<STEP>::THREADS, 1)
   using L = MU2<WP>;
   using R = Roles<STEP>;
   constexpr int CW = L::CW, KC = L::KC, NC = L::NC, KSTEPS = L::KSTEPS, NS = L::NS, NACC = L::NACC;
-  constexpr int kEpiWarps = R::EPI, kMmaWarp = R::MMA, kProdThreads = R::PT, kEpiThreads = R::ET;
+  constexpr int kEpiWarps = R::EPI, kMmaWarp = R::MMA, kEpiThreads = R::ET;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   unsigned char* sA = base;                                 // NS stages
@@ -153,10 +157,9 @@ __global__ void __launch_bounds__(Roles<STEP>::THREADS, 1)
   __shared__ __align__(8) uint64_t drain_bar;
   __shared__ uint32_t tmem_slot;
   __shared__ int s_colexp[2][WP];
-  __shared__ int s_rowexp[kTileRows];     // producer's copy of the current tile's row scales
   __shared__ volatile int s_bad;
   __shared__ int s_bad_prob;
-  __shared__ int s_pflag;
+  __shared__ int s_aflag, s_bflag;
   __shared__ int s_eflag;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -167,11 +170,11 @@ __global__ void __launch_bounds__(Roles<STEP>::THREADS, 1)
   }
   if (tid == 0) {
     for (int s = 0; s < NS; ++s) {
-      mbar_init(&a_full[s], STEP == 1 ? 1u : (uint32_t)kProdThreads);
+      mbar_init(&a_full[s], STEP == 1 ? 1u : (uint32_t)R::PAT);
       mbar_init(&a_empty[s], 1u);
     }
     for (int b = 0; b < 2; ++b) {
-      mbar_init(&b_full[b], (uint32_t)kProdThreads);
+      mbar_init(&b_full[b], (uint32_t)R::PBT);
       mbar_init(&b_empty[b], 1u + (uint32_t)kEpiThreads);
     }
     for (int a = 0; a < NACC; ++a) {
@@ -195,158 +198,100 @@ __global__ void __launch_bounds__(Roles<STEP>::THREADS, 1)
     }
   };
 
-  if (warp >= kEpiWarps && warp < kMmaWarp) {
-    // =========================== producer ===========================
-    const int pt = tid - kEpiThreads;
-    int gseq = 0;          // groups started
+  if (warp >= kEpiWarps && warp < kEpiWarps + R::PA) {
+    // =========================== A producer ===========================
+    const int pa = tid - kEpiThreads;
     int sseq = 0;          // stages filled
     uint32_t inflight = 0, inflight_par = 0;   // step 1: slots with a bulk copy issued, and its parity
-    // producer-wide bounded wait: thread 0 polls, the outcome is shared (uniform branch)
-    auto pwait = [&](uint64_t* bar, uint32_t parity, int p) -> bool {
-      if (pt == 0) {
+    // A-producer-wide bounded wait: thread 0 polls, the outcome is shared (uniform branch);
+    // in step 1 thread 0 is the whole A producer
+    auto await = [&](uint64_t* bar, uint32_t parity, int p) -> bool {
+      if (pa == 0) {
         const bool ok = mbar_wait_role(smem_u32(bar), parity, &s_bad);
         if (!ok) fail(p);
-        s_pflag = ok ? 0 : 1;
+        s_aflag = ok ? 0 : 1;
       }
-      bar_named(1, kProdThreads);
-      const bool ok = s_pflag == 0;
-      bar_named(1, kProdThreads);
+      if (STEP == 1) return s_aflag == 0;
+      bar_named(1, R::PAT);
+      const bool ok = s_aflag == 0;
+      bar_named(1, R::PAT);
       return ok;
     };
-    bool ok = true;
+    bool ok = STEP == 2 || pa == 0;
     for (int item = blockIdx.x; item < ngroups && ok; item += gridDim.x) {
       int g;
       const int p = locate(wm, item, g);
       const Problem& P = probs[p];
       if (!group_active(P, which)) continue;
       const int W = P.W, B = P.B, WW = W * W;
-      const double2* Ug = P.U[P.st->cur ^ 1] + (size_t)g * WW;
       const int ntiles = ntiles_of<WP>(B);
-      // ---- B operand of the group: column scales, 7 digit planes
-      const int bb = gseq & 1;
-      // (the first use of each B buffer needs no wait)
-      if (gseq >= 2 && !pwait(&b_empty[bb], ((gseq >> 1) & 1) ^ 1, p)) {
-        ok = false;
-        break;
-      }
-      {
-        // column scales: 4 threads per column, 8 independent loads each, max over the 4 lanes
-        const int c = pt >> 2, part = pt & 3;
-        unsigned long long mx = 0ull;
-        if (c < WP) {
-          double2 v[8];
-#pragma unroll
-          for (int i = 0; i < 8; ++i) {
-            const int m = part * 8 + i;
-            v[i] = (c < W && m < W) ? Ug[(size_t)c * W + m] : make_double2(0.0, 0.0);
-          }
-#pragma unroll
-          for (int i = 0; i < 8; ++i) mx = max(mx, max(abs_bits(v[i].x), abs_bits(v[i].y)));
-        }
-        mx = max(mx, (unsigned long long)__shfl_xor_sync(0xffffffffu, (long long)mx, 1));
-        mx = max(mx, (unsigned long long)__shfl_xor_sync(0xffffffffu, (long long)mx, 2));
-        if (c < WP && part == 0) s_colexp[bb][c] = exp_above_bits(mx);
-      }
-      bar_named(1, kProdThreads);
-      unsigned char* dB = sB + (size_t)bb * L::B_BYTES;
-      // B^T planes: each complex U(m, c) gives the four real entries of the embedding
-      // [[B_r, B_i], [-B_i, B_r]]; B_r, B_i and -B_i are sliced once each
-      for (int idx = pt; idx < WP * WP; idx += kProdThreads) {
-        const int mm = idx % WP, cc = idx / WP;
-        double br = 0.0, bi = 0.0;
-        if (cc < W && mm < W) {
-          const double2 u = Ug[(size_t)cc * W + mm];
-          br = u.x;
-          bi = (STEP == 1) ? -u.y : u.y;
-        }
-        const int ec = s_colexp[bb][cc];
-        int xr[kS], xi[kS], xn[kS];
-        digits7(scaled_int(br, ec), xr);
-        digits7(scaled_int(bi, ec), xi);
-        digits7(scaled_int(-bi, ec), xn);
-        const int k_re = (mm >> 3) * 16 + (mm & 7), k_im = k_re + 8;   // K positions of Re / Im of m
-        const uint32_t o_rr = kmaj_off(cc, k_re, KC), o_ir = kmaj_off(CW + cc, k_re, KC);
-        const uint32_t o_ri = kmaj_off(cc, k_im, KC), o_ii = kmaj_off(CW + cc, k_im, KC);
-#pragma unroll
-        for (int t = 0; t < kS; ++t) {
-          unsigned char* pl = dB + (size_t)t * L::B_PLANE;
-          *(uint16_t*)(pl + o_rr) = int_to_bf16(xr[t]);   // (K re, N re) =  B_r
-          *(uint16_t*)(pl + o_ir) = int_to_bf16(xi[t]);   // (K re, N im) =  B_i
-          *(uint16_t*)(pl + o_ri) = int_to_bf16(xn[t]);   // (K im, N re) = -B_i
-          *(uint16_t*)(pl + o_ii) = int_to_bf16(xr[t]);   // (K im, N im) =  B_r
-        }
-      }
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      mbar_arrive(&b_full[bb]);
-      ++gseq;
-      // ---- A operand, tile by tile, one K-step stage at a time
       for (int tile = 0; tile < ntiles && ok; ++tile) {
-        // step 2: the Z rows this thread slices (rows i*RPP + pt/8, K index 8 ks + pt%8)
-        const double2* zrow[R::NPASS];
+        // step 2: the Z rows this thread slices -- items it = pa + j PAT: tile row it % 128,
+        // part it / 128, 8 complex of one K-step (one 16-byte core-matrix row per plane)
+        const double2* zrow[R::AIPT];
+        int zex[R::AIPT];
         if (STEP == 2) {
-          // row scales of this tile: computed by step 1's epilogue (zexp)
-          for (int r0 = pt; r0 < kTileRows; r0 += kProdThreads) {
-            const int row = tile * kTileRows + r0;
-            const int bi = row / WP, rr = row % WP;
-            int e = 0;
-            if (bi < B && rr < W) e = P.zexp[(size_t)P.inv_nnlist[(size_t)g * B + bi] * W + rr];
-            s_rowexp[r0] = e;
-          }
 #pragma unroll
-          for (int i = 0; i < R::NPASS; ++i) {
-            const int rw = tile * kTileRows + i * R::RPP + (pt >> 3);
+          for (int j = 0; j < R::AIPT; ++j) {
+            const int it = pa + j * R::PAT;
+            const int rw = tile * kTileRows + it % kTileRows;
             const int b2 = rw / WP, r2 = rw % WP;
-            zrow[i] = (b2 < B && r2 < W)
-                          ? P.tbuf + (size_t)P.inv_nnlist[(size_t)g * B + b2] * WW + (size_t)r2 * W
-                          : nullptr;
+            zrow[j] = nullptr;
+            zex[j] = 0;
+            if (it < R::AITEMS && b2 < B && r2 < W) {
+              const size_t kb = (size_t)P.inv_nnlist[(size_t)g * B + b2];
+              zrow[j] = P.tbuf + kb * WW + (size_t)r2 * W;
+              zex[j] = P.zexp[kb * W + r2];     // the row's scale, computed by step 1's epilogue
+            }
           }
-          bar_named(1, kProdThreads);
         }
         for (int ks = 0; ks < KSTEPS; ++ks) {
           const int s = sseq % NS;
           const uint32_t use = (uint32_t)(sseq / NS);
-          double2 av[R::NPASS];
+          double av[R::AIPT][8];
           if (STEP == 2) {
             // the stage's elements, loaded before the slot is free
-            const int m = ks * 8 + (pt & 7);
 #pragma unroll
-            for (int i = 0; i < R::NPASS; ++i) av[i] = (zrow[i] && m < W) ? zrow[i][m] : make_double2(0.0, 0.0);
+            for (int j = 0; j < R::AIPT; ++j) {
+              const int part = (pa + j * R::PAT) / kTileRows;
+#pragma unroll
+              for (int i = 0; i < 8; ++i) {
+                const int m = ks * 8 + i;
+                av[j][i] = (zrow[j] && m < W) ? ((const double*)(zrow[j] + m))[part] : 0.0;
+              }
+            }
           }
           // (the first use of each stage slot needs no wait)
-          if (use > 0 && !pwait(&a_empty[s], (use & 1) ^ 1, p)) {
+          if (use > 0 && !await(&a_empty[s], (use & 1) ^ 1, p)) {
             ok = false;
             break;
           }
           inflight &= ~(1u << s);    // the MMA consumed the slot's last copy
           unsigned char* dA = sA + (size_t)s * L::STAGE;
           if (STEP == 1) {
-            if (pt == 0) {
-              const unsigned char* src =
-                  P.m0s + ((((size_t)g * ntiles + tile) * KSTEPS) + ks) * (size_t)L::STAGE;
-              asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}"
-                           :: "r"(smem_u32(&a_full[s])), "r"((uint32_t)L::STAGE) : "memory");
-              asm volatile(
-                  "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                  :: "r"(smem_u32(dA)), "l"(src), "r"((uint32_t)L::STAGE), "r"(smem_u32(&a_full[s]))
-                  : "memory");
-              inflight |= 1u << s;
-              inflight_par = (inflight_par & ~(1u << s)) | ((use & 1) << s);
-            }
+            const unsigned char* src =
+                P.m0s + ((((size_t)g * ntiles + tile) * KSTEPS) + ks) * (size_t)L::STAGE;
+            asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}"
+                         :: "r"(smem_u32(&a_full[s])), "r"((uint32_t)L::STAGE) : "memory");
+            asm volatile(
+                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                :: "r"(smem_u32(dA)), "l"(src), "r"((uint32_t)L::STAGE), "r"(smem_u32(&a_full[s]))
+                : "memory");
+            inflight |= 1u << s;
+            inflight_par = (inflight_par & ~(1u << s)) | ((use & 1) << s);
           } else {
-            // 128 rows x 8 complex: each thread slices NPASS elements into all 7 planes
+            // 128 rows x 8 complex: each item is one part of a row's 8 elements, sliced into
+            // all 7 planes (K 0-7 real parts, 8-15 imaginary parts), one 16-byte store each
 #pragma unroll
-            for (int i = 0; i < R::NPASS; ++i) {
-              const int r = i * R::RPP + (pt >> 3), l = pt & 7;
-              const double2 a = av[i];
-              const int ex = s_rowexp[r];
-              int xr[kS], xi[kS];
-              digits7(scaled_int(a.x, ex), xr);
-              digits7(scaled_int(a.y, ex), xi);
-              const uint32_t o = stage_off(r, l);
+            for (int j = 0; j < R::AIPT; ++j) {
+              const int it = pa + j * R::PAT;
+              if (it < R::AITEMS) {
+                uint32_t w[kS][4];
+                pack_digits7(w, av[j], zex[j], false);
+                const uint32_t o = stage_off(it % kTileRows, 8 * (it / kTileRows));
 #pragma unroll
-              for (int t = 0; t < kS; ++t) {
-                *(uint16_t*)(dA + (size_t)t * L::PLANE + o) = int_to_bf16(xr[t]);
-                *(uint16_t*)(dA + (size_t)t * L::PLANE + o + 128) = int_to_bf16(xi[t]);
+                for (int t = 0; t < kS; ++t)
+                  *(uint4*)(dA + (size_t)t * L::PLANE + o) = make_uint4(w[t][0], w[t][1], w[t][2], w[t][3]);
               }
             }
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -354,13 +299,96 @@ __global__ void __launch_bounds__(Roles<STEP>::THREADS, 1)
           }
           ++sseq;
         }
-        if (STEP == 2) bar_named(1, kProdThreads);   // s_rowexp is rewritten for the next tile
       }
     }
     // drain: bulk copies still in flight must land before the CTA frees its shared memory
-    if (STEP == 1 && pt == 0)
+    if (STEP == 1 && pa == 0)
       for (int s = 0; s < NS; ++s)
         if (inflight & (1u << s)) mbar_drain(smem_u32(&a_full[s]), (inflight_par >> s) & 1);
+  } else if (warp >= kEpiWarps + R::PA && warp < kMmaWarp) {
+    // =========================== B producer ===========================
+    const int pb = tid - kEpiThreads - R::PAT;
+    int gseq = 0;          // groups started
+    auto bwait = [&](uint64_t* bar, uint32_t parity, int p) -> bool {
+      if (pb == 0) {
+        const bool ok = mbar_wait_role(smem_u32(bar), parity, &s_bad);
+        if (!ok) fail(p);
+        s_bflag = ok ? 0 : 1;
+      }
+      bar_named(3, R::PBT);
+      const bool ok = s_bflag == 0;
+      bar_named(3, R::PBT);
+      return ok;
+    };
+    for (int item = blockIdx.x; item < ngroups; item += gridDim.x) {
+      int g;
+      const int p = locate(wm, item, g);
+      const Problem& P = probs[p];
+      if (!group_active(P, which)) continue;
+      const int W = P.W, WW = W * W;
+      const double2* Ug = P.U[P.st->cur ^ 1] + (size_t)g * WW;
+      const int bb = gseq & 1;
+      // (the first use of each B buffer needs no wait)
+      if (gseq >= 2 && !bwait(&b_empty[bb], ((gseq >> 1) & 1) ^ 1, p)) break;
+      // column scales: one column per thread, 8 independent loads per round
+      for (int c = pb; c < WP; c += R::PBT) {
+        unsigned long long mx = 0ull;
+        if (c < W)
+          for (int m0 = 0; m0 < W; m0 += 8) {
+            double2 v[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) v[i] = (m0 + i < W) ? Ug[(size_t)c * W + m0 + i] : make_double2(0.0, 0.0);
+#pragma unroll
+            for (int i = 0; i < 8; ++i) mx = max(mx, max(abs_bits(v[i].x), abs_bits(v[i].y)));
+          }
+        s_colexp[bb][c] = exp_above_bits(mx);
+      }
+      bar_named(3, R::PBT);
+      unsigned char* dB = sB + (size_t)bb * L::B_BYTES;
+      // B^T planes: each complex U(m, c) gives the four real entries of the embedding
+      // [[B_r, B_i], [-B_i, B_r]]; B_r, B_i and -B_i are sliced once each.  A thread takes
+      // one part of 8 consecutive m of column c (contiguous in memory; their K positions
+      // form one 16-byte core-matrix row) and stores each plane's row with 16-byte stores:
+      // B_r to (N re, K re) and (N im, K im); B_i to (N im, K re), -B_i to (N re, K im).
+      for (int idx = pb; idx < WP * (WP / 8) * 2; idx += R::PBT) {
+        const int cc = idx % WP, g8 = (idx / WP) % (WP / 8), part = idx / (WP * (WP / 8));
+        const int ec = s_colexp[bb][cc];
+        double v[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          const int mm = g8 * 8 + i;
+          v[i] = 0.0;
+          if (cc < W && mm < W) {
+            const double2 u = Ug[(size_t)cc * W + mm];
+            v[i] = part == 0 ? u.x : ((STEP == 1) ? -u.y : u.y);
+          }
+        }
+        uint32_t w[kS][4];
+        pack_digits7(w, v, ec, false);
+        const int k_re = g8 * 16, k_im = k_re + 8;   // K positions of Re / Im of m = 8 g8 ..
+        if (part == 0) {
+          const uint32_t o_rr = kmaj_off(cc, k_re, KC), o_ii = kmaj_off(CW + cc, k_im, KC);
+#pragma unroll
+          for (int t = 0; t < kS; ++t) {
+            unsigned char* pl = dB + (size_t)t * L::B_PLANE;
+            *(uint4*)(pl + o_rr) = make_uint4(w[t][0], w[t][1], w[t][2], w[t][3]);   // (K re, N re) = B_r
+            *(uint4*)(pl + o_ii) = make_uint4(w[t][0], w[t][1], w[t][2], w[t][3]);   // (K im, N im) = B_r
+          }
+        } else {
+          const uint32_t o_ir = kmaj_off(CW + cc, k_re, KC), o_ri = kmaj_off(cc, k_im, KC);
+#pragma unroll
+          for (int t = 0; t < kS; ++t)   // (K re, N im) = B_i
+            *(uint4*)(dB + (size_t)t * L::B_PLANE + o_ir) = make_uint4(w[t][0], w[t][1], w[t][2], w[t][3]);
+          pack_digits7(w, v, ec, true);
+#pragma unroll
+          for (int t = 0; t < kS; ++t)   // (K im, N re) = -B_i, the digits of the negated values
+            *(uint4*)(dB + (size_t)t * L::B_PLANE + o_ri) = make_uint4(w[t][0], w[t][1], w[t][2], w[t][3]);
+        }
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      mbar_arrive(&b_full[bb]);
+      ++gseq;
+    }
   } else if (warp == kMmaWarp) {
     // =========================== MMA issue ===========================
     if (lane == 0) {
@@ -398,12 +426,17 @@ __global__ void __launch_bounds__(Roles<STEP>::THREADS, 1)
               break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t a0 = smem_u32(sA + (size_t)s * L::STAGE);
+            // descriptors: the base descriptor plus the byte offset / 16 in the address field
+            // (shared-memory addresses stay below 2^18, so the field holds it)
+            const uint64_t da = smem_desc(smem_u32(sA + (size_t)s * L::STAGE), 128, 256);
+            const uint64_t db = smem_desc(b0 + ks * 256, 128, (KC / 8) * 128);
+#pragma unroll
             for (int t = 0; t < kS; ++t) {
-              const uint64_t ad = smem_desc(a0 + t * L::PLANE, 128, 256);
+              const uint64_t ad = da + (uint64_t)((t * L::PLANE) >> 4);
+#pragma unroll
               for (int u = 0; u + t <= kS - 1; ++u) {
                 const int d = t + u;
-                const uint64_t bd = smem_desc(b0 + u * L::B_PLANE + ks * 256, 128, (KC / 8) * 128);
+                const uint64_t bd = db + (uint64_t)((u * L::B_PLANE) >> 4);
                 // the first write of diagonal d in this tile: pair (0, d) of K-step 0
                 const uint32_t accf = (ks == 0 && t == 0) ? 0u : 1u;
                 asm volatile(

@@ -163,6 +163,7 @@ __device__ __forceinline__ void rec_clear(const Rec& r, int n) {
     for (int i = threadIdx.x; i < 2 * n; i += blockDim.x) (i < n ? r.row : r.col)[i % n] = 0u;
 }
 
+// Adds the key of v (at row i, column j) to the record (shared-memory maxima).
 __device__ __forceinline__ void rec_add(const Rec& r, int i, int j, double2 v) {
   if (r.row != nullptr) {
     const unsigned key = scale_key(v.x, v.y);
@@ -424,6 +425,40 @@ struct Exp2Smem {
   static constexpr size_t BYTES = NEED > FLOOR ? NEED : FLOOR;
 };
 
+// Part (0 re, 1 im) of 8 values base[(m0 + i) * stride], i < 8 (zero where m0 + i >= W or
+// !valid): the operand run a thread slices.
+__device__ __forceinline__ void load_run8(double (&v)[8], const double2* base, size_t stride, int m0, int W,
+                                          bool valid, int part) {
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int m = m0 + i;
+    v[i] = 0.0;
+    if (valid && m < W) v[i] = ((const double*)(base + (size_t)m * stride))[part];
+  }
+}
+
+// The seven 8-bit digit planes of the 8 values scaled by 2^(55 - ex), as packed BF16
+// pairs: w[t][i / 2] holds digit t of values i (low half) and i + 1 -- the digits and BF16
+// bits of slicing the values one at a time (digits7x8, int_to_bf16).
+__device__ __forceinline__ void slice_run8(uint32_t (&w)[7][4], const double (&v)[8], int ex) {
+#pragma unroll
+  for (int i = 0; i < 8; i += 2) {
+    float fa[7], fb[7];
+    digits7x8_f(scaled_int55(v[i], ex), fa);
+    digits7x8_f(scaled_int55(v[i + 1], ex), fb);
+#pragma unroll
+    for (int t = 0; t < 7; ++t) w[t][i >> 1] = pack_bf16x2(fa[t], fb[t]);
+  }
+}
+
+// the BF16 bits of -x for both halves of a packed pair of exact small integers: the sign
+// flipped where the value is not zero (int_to_bf16(-0) is +0, as int_to_bf16(0))
+__device__ __forceinline__ uint32_t bf16x2_neg(uint32_t w) {
+  const uint32_t lo = (w & 0x7FFFu) ? 0x8000u : 0u;
+  const uint32_t hi = (w & 0x7FFF0000u) ? 0x80000000u : 0u;
+  return w ^ (lo | hi);
+}
+
 // C = A B, then the Epi.  num_wann <= 32 (staged accumulators): the epilogue applies the
 // Epi itself and writes ep.out only (C unused; ep.out may alias B, whose digits are in
 // shared memory before the MMAs run, but not A); WP = 64: C as in oz_cmm.
@@ -436,88 +471,66 @@ __device__ bool oz_cmm2(OzCtx& cx, double2* C, const double2* A, const unsigned*
   ab_exponents<WP>(cx, A, arow, B, bcol, W);
   __syncthreads();
   const uint32_t idesc = idesc_bf16(N);
-  // a warp slices 4 rows x 8 consecutive K, i.e. whole 16-byte core-matrix rows
-  constexpr int kgroups = CW / 8;
   bool ok = true;
   for (int kc = 0; kc < E::NCHK && ok; ++kc) {
-    // ---- A_emb chunk: complex (r, l) -> rows r (re) and WP + r (im), K l (re) / CW + l (im);
-    // each thread's elements are loaded together first (they may come from L2)
-    constexpr int NA = (WP * CW + 255) / 256;
-    double2 av[NA];
+    // ---- A_emb chunk: complex (r, l) -> rows r (re) and WP + r (im), K l (re) / CW + l (im),
+    // and B_emb chunk as B^T (K-major): row = output column c, K l (re) / CW + l (im).  A
+    // thread slices one part (re or im) of 8 consecutive l of a row of A and of a column of
+    // B (contiguous in memory) -- a whole 16-byte core-matrix row per digit plane -- with
+    // both runs' loads issued before either is sliced.  The A part goes to both places it
+    // occupies (A_r: (re, K re) and (im, K im); A_i: (im, K re) and, negated, (re, K im));
+    // lanes take consecutive rows / columns, so the 16-byte stores do not conflict.
+    {
+      constexpr int LG = CW / 8, NIA = WP * LG * 2, NIB = N * LG * 2;
+      constexpr int NI = NIA > NIB ? NIA : NIB;
+      for (int it = tid; it < NI; it += 256) {
+        const int r = it % WP, lga = (it / WP) % LG, pa = it / (WP * LG);
+        const int c = it % N, lgb = (it / N) % LG, pb = it / (N * LG);
+        double va[8], vb[8];
+        if (it < NIA) load_run8(va, A + r, (size_t)W, kc * CW + lga * 8, W, r < W, pa);
+        if (it < NIB) load_run8(vb, B + (size_t)c * W, (size_t)1, kc * CW + lgb * 8, W, c < W, pb);
+        uint32_t w[kS2][4];
+        if (it < NIA) {
+          slice_run8(w, va, cx.rowexp[r]);
+          const int kq = lga * 8;
+          const uint32_t o1 = pa == 0 ? kmaj_off(r, kq, KC) : kmaj_off(WP + r, kq, KC);
+          const uint32_t o2 = pa == 0 ? kmaj_off(WP + r, CW + kq, KC) : kmaj_off(r, CW + kq, KC);
 #pragma unroll
-    for (int i = 0; i < NA; ++i) {
-      const int e = tid + i * 256;
-      const int ln = e & 31, wi = e >> 5;
-      const int r = (wi / kgroups) * 4 + (ln >> 3), l = (wi % kgroups) * 8 + (ln & 7);
-      const int m = kc * CW + l;
-      av[i] = (e < WP * CW && r < W && m < W) ? A[(size_t)m * W + r] : make_double2(0.0, 0.0);
-    }
+          for (int t = 0; t < kS2; ++t) {
+            unsigned char* sa = cx.sA + (size_t)t * E::A_SLICE;
+            *(uint4*)(sa + o1) = make_uint4(w[t][0], w[t][1], w[t][2], w[t][3]);
+            *(uint4*)(sa + o2) = pa == 0 ? make_uint4(w[t][0], w[t][1], w[t][2], w[t][3])
+                                         : make_uint4(bf16x2_neg(w[t][0]), bf16x2_neg(w[t][1]),
+                                                      bf16x2_neg(w[t][2]), bf16x2_neg(w[t][3]));
+          }
+        }
+        if (it < NIB) {
+          slice_run8(w, vb, cx.colexp[c < WP ? c : 0]);
+          const uint32_t o = kmaj_off(c, pb * CW + lgb * 8, KC);
 #pragma unroll
-    for (int i = 0; i < NA; ++i) {
-      const int e = tid + i * 256;
-      if (e >= WP * CW) break;
-      const int ln = e & 31, wi = e >> 5;
-      const int r = (wi / kgroups) * 4 + (ln >> 3), l = (wi % kgroups) * 8 + (ln & 7);
-      const double2 a = av[i];
-      int xr[kS2], xi[kS2];
-      const int ex = cx.rowexp[r];
-      digits7x8(scaled_int55(a.x, ex), xr);
-      digits7x8(scaled_int55(a.y, ex), xi);
-      const uint32_t o_rr = kmaj_off(r, l, KC), o_ri = kmaj_off(r, l + CW, KC);
-      const uint32_t o_ir = kmaj_off(WP + r, l, KC), o_ii = kmaj_off(WP + r, l + CW, KC);
-#pragma unroll
-      for (int t = 0; t < kS2; ++t) {
-        unsigned char* sa = cx.sA + (size_t)t * E::A_SLICE;
-        *(uint16_t*)(sa + o_rr) = int_to_bf16(xr[t]);    // row re, K re:  A_r
-        *(uint16_t*)(sa + o_ri) = int_to_bf16(-xi[t]);   // row re, K im: -A_i
-        *(uint16_t*)(sa + o_ir) = int_to_bf16(xi[t]);    // row im, K re:  A_i
-        *(uint16_t*)(sa + o_ii) = int_to_bf16(xr[t]);    // row im, K im:  A_r
-      }
-    }
-    // ---- B_emb chunk as B^T (K-major): row = output column c, K l (re) / CW + l (im)
-    constexpr int NB = (N * CW + 255) / 256;
-    double2 bv[NB];
-#pragma unroll
-    for (int i = 0; i < NB; ++i) {
-      const int e = tid + i * 256;
-      const int ln = e & 31, wi = e >> 5;
-      const int c = (wi / kgroups) * 4 + (ln >> 3), l = (wi % kgroups) * 8 + (ln & 7);
-      const int mm = kc * CW + l;
-      bv[i] = (e < N * CW && mm < W && c < W) ? B[(size_t)c * W + mm] : make_double2(0.0, 0.0);
-    }
-#pragma unroll
-    for (int i = 0; i < NB; ++i) {
-      const int e = tid + i * 256;
-      if (e >= N * CW) break;
-      const int ln = e & 31, wi = e >> 5;
-      const int c = (wi / kgroups) * 4 + (ln >> 3), l = (wi % kgroups) * 8 + (ln & 7);
-      const double2 b = bv[i];
-      int xr[kS2], xi[kS2];
-      const int ex = cx.colexp[c < WP ? c : 0];
-      digits7x8(scaled_int55(b.x, ex), xr);
-      digits7x8(scaled_int55(b.y, ex), xi);
-      const uint32_t o_r = kmaj_off(c, l, KC), o_i = kmaj_off(c, l + CW, KC);
-#pragma unroll
-      for (int t = 0; t < kS2; ++t) {
-        unsigned char* sb = cx.sB + (size_t)t * E::B_BYTES;
-        *(uint16_t*)(sb + o_r) = int_to_bf16(xr[t]);
-        *(uint16_t*)(sb + o_i) = int_to_bf16(xi[t]);
+          for (int t = 0; t < kS2; ++t)
+            *(uint4*)(cx.sB + (size_t)t * E::B_BYTES + o) = make_uint4(w[t][0], w[t][1], w[t][2], w[t][3]);
+        }
       }
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
     if (tid == 0) {
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      // descriptors of the slices' K-steps: the base descriptor plus the byte offset / 16 in
+      // its address field (shared-memory addresses stay below 2^18, so the field holds it)
+      const uint64_t da = smem_desc(smem_u32(cx.sA), 128, (KC / 8) * 128);
+      const uint64_t db = smem_desc(smem_u32(cx.sB), 128, (KC / 8) * 128);
+#pragma unroll
       for (int t = 0; t < kS2; ++t) {
+#pragma unroll
         for (int u = 0; u + t <= kS2 - 1; ++u) {
           const uint32_t dtm = cx.tmem + (uint32_t)((t + u) * N);
-          const uint32_t a0 = smem_u32(cx.sA + (size_t)t * E::A_SLICE);
-          const uint32_t b0 = smem_u32(cx.sB + (size_t)u * E::B_BYTES);
           const bool first_pair = (kc == 0) && (t == 0);
 #pragma unroll
           for (int ks = 0; ks < KC / 16; ++ks) {
-            const uint64_t ad = smem_desc(a0 + ks * 256, 128, (KC / 8) * 128);
-            const uint64_t bd = smem_desc(b0 + ks * 256, 128, (KC / 8) * 128);
+            const uint64_t ad = da + (uint64_t)(((size_t)t * E::A_SLICE + ks * 256) >> 4);
+            const uint64_t bd = db + (uint64_t)(((size_t)u * E::B_BYTES + ks * 256) >> 4);
             const uint32_t acc = (first_pair && ks == 0) ? 0u : 1u;
             asm volatile(
                 "{\n\t.reg .pred p;\n\t"
@@ -676,6 +689,26 @@ struct ProdV2 {
 template <int WP, bool SMEM_MATS = false>
 using ExpProd = typename std::conditional<(WP <= 64), ProdV2<WP, SMEM_MATS>, ProdV1<WP>>::type;
 
+// x 2^-j (sc = 2^-j): an exponent subtraction where the result is a normal number (the
+// product is exact there, so the bits are those of x * sc), else the FP64 multiply
+__device__ __forceinline__ double scale_pow2(double x, int j, double sc) {
+  const long long b = __double_as_longlong(x);
+  const int be = (int)((b >> 52) & 0x7FF);
+  if (be > j && be != 0x7FF) return __longlong_as_double(b - ((long long)j << 52));
+  return x * sc;
+}
+
+// The number of halvings that bring v to theta or below (at most 60): the smallest j >= 0
+// with v 2^-j <= theta.  Halving is exact, so this is the count of the loop
+// "while (v > theta && j < 60) { v *= 0.5; ++j; }", found from the exponents in a few steps.
+__device__ __forceinline__ int halvings(double v, double theta) {
+  if (!(v > theta)) return 0;
+  int j = ilogb(v) - ilogb(theta) - 1;
+  j = j < 0 ? 0 : (j > 60 ? 60 : j);
+  while (j < 60 && ldexp(v, -j) > theta) ++j;
+  return j;
+}
+
 __device__ const double kOzInvFact[17] = {
     1.0, 1.0, 0.5, 1.6666666666666666e-01, 4.1666666666666664e-02, 8.3333333333333332e-03,
     1.3888888888888889e-03, 1.9841269841269841e-04, 2.4801587301587302e-05,
@@ -764,12 +797,7 @@ __global__ void __launch_bounds__(256, 2) k_oz_exp(const Problem* __restrict__ p
   int m = 16, pw = 4, js = 0;
   double best = 1e300;
   for (int c = 0; c < 5; ++c) {
-    int j = 0;
-    double v = nrm;
-    while (v > cand_theta[c] && j < 60) {
-      v *= 0.5;
-      ++j;
-    }
+    const int j = halvings(nrm, cand_theta[c]);
     const double cost = cand_cost[c] + j;
     if (cost < best) {
       best = cost;
@@ -786,7 +814,8 @@ __global__ void __launch_bounds__(256, 2) k_oz_exp(const Problem* __restrict__ p
   __syncthreads();
   #pragma unroll 4
   for (int e = tid; e < WW; e += blockDim.x) {
-    const double2 v = cscale(X[e], sc);
+    const double2 x = X[e];
+    const double2 v = make_double2(scale_pow2(x.x, js, sc), scale_pow2(x.y, js, sc));
     X[e] = v;
     rec_add(rX, e % W, e / W, v);
   }
@@ -799,6 +828,9 @@ __global__ void __launch_bounds__(256, 2) k_oz_exp(const Problem* __restrict__ p
   const double2* Yp = (pw == 4) ? Y4 : Y3;
   const Rec rYp = (pw == 4) ? rY4 : rY3;
   const int nblk = (m + pw) / pw;
+  // block q of the polynomial, sum_r c_{pw q + r} X^r (X^0 = I), one FMA per term and part
+  // (the FP64 pipe runs at 1/64 of FP32 on this chip: these elementwise terms are a large
+  // part of the chain's FP64 work)
   auto blk = [&](int q, int e) -> double2 {
     const int i = e % W, j = e / W;
     double2 v = cmk(0.0, 0.0);
@@ -810,7 +842,7 @@ __global__ void __launch_bounds__(256, 2) k_oz_exp(const Problem* __restrict__ p
         if (i == j) v.x += c;
       } else {
         const double2 y = (r == 1) ? X[e] : ((r == 2) ? Y2[e] : Y3[e]);
-        v = cadd(v, cscale(y, c));
+        v = cmk(fma(y.x, c, v.x), fma(y.y, c, v.y));
       }
     }
     return v;
@@ -822,7 +854,8 @@ __global__ void __launch_bounds__(256, 2) k_oz_exp(const Problem* __restrict__ p
     const double cm = kOzInvFact[m];
     #pragma unroll 4
     for (int e = tid; e < WW; e += blockDim.x) {
-      const double2 v = cadd(cscale(Yp[e], cm), blk(q - 1, e));
+      const double2 b = blk(q - 1, e), y = Yp[e];
+      const double2 v = cmk(fma(y.x, cm, b.x), fma(y.y, cm, b.y));
       R[e] = v;
       rec_add(rR, e % W, e / W, v);
     }

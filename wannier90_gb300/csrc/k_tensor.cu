@@ -61,29 +61,28 @@ __device__ __forceinline__ void a_row_exponents(int tile, int W, int* rowexp, AE
 }
 
 // The kS digit planes of A chunk (tile, kc) in the canonical K-major layout, written to
-// dst (shared memory, or the global image the shared-memory copy is taken from): a warp
-// writes 4 consecutive 16-byte core rows.
+// dst (shared memory, or the global image the shared-memory copy is taken from).  A
+// thread slices one part (re / im) of 8 consecutive K of one row -- one 16-byte core row
+// per plane -- and lanes take consecutive rows, so the 16-byte stores do not conflict.
 template <int WP, class AElem>
 __device__ __forceinline__ void a_slice_chunk(unsigned char* dst, int tile, int kc, const int* rowexp,
                                               AElem&& a_elem) {
   using L = TileSmem<WP>;
-  constexpr int CW = L::CW, KC = L::KC;
-  for (int e = threadIdx.x; e < kTileRows * CW; e += blockDim.x) {
-    const int ln = e & 31, wi = e >> 5;
-    constexpr int mgroups = CW / 8;
-    const int r = (wi / mgroups) * 4 + (ln >> 3);
-    const int l = (wi % mgroups) * 8 + (ln & 7);
-    const double2 a = a_elem(tile * kTileRows + r, kc * CW + l);
-    const int ex = rowexp[r];
-    int xr[kS], xi[kS];
-    split_digits<WP>(a.x, ex, xr);
-    split_digits<WP>(a.y, ex, xi);
-    const uint32_t o_re = kmaj_off(r, l, KC), o_im = kmaj_off(r, l + CW, KC);
+  constexpr int CW = L::CW, KC = L::KC, LG = CW / 8;
+  for (int it = threadIdx.x; it < kTileRows * LG * 2; it += blockDim.x) {
+    const int r = it % kTileRows, lg = (it / kTileRows) % LG, part = it / (kTileRows * LG);
+    double v[8];
 #pragma unroll
-    for (int t = 0; t < kS; ++t) {
-      *(uint16_t*)(dst + (size_t)t * L::A_BYTES + o_re) = int_to_bf16(xr[t]);
-      *(uint16_t*)(dst + (size_t)t * L::A_BYTES + o_im) = int_to_bf16(xi[t]);
+    for (int i = 0; i < 8; ++i) {
+      const double2 a = a_elem(tile * kTileRows + r, kc * CW + lg * 8 + i);
+      v[i] = part == 0 ? a.x : a.y;
     }
+    uint32_t w[kS][4];
+    pack_digits7(w, v, rowexp[r], false);
+    const uint32_t o = kmaj_off(r, part * CW + lg * 8, KC);
+#pragma unroll
+    for (int t = 0; t < kS; ++t)
+      *(uint4*)(dst + (size_t)t * L::A_BYTES + o) = make_uint4(w[t][0], w[t][1], w[t][2], w[t][3]);
   }
 }
 
@@ -152,30 +151,34 @@ __global__ void __launch_bounds__(256, 1) k_oz_mupdate(const Problem* __restrict
     if (sub == 0 && c < WP) s_colexp[c] = exp_above_bits(mx);
   }
 
-  // slice the (nc, kc) chunk of B^T (K-major: rows = real N index within the chunk)
+  // slice the (nc, kc) chunk of B^T (K-major: rows = real N index within the chunk): a
+  // thread takes 8 consecutive K of one row n, i.e. one entry of the embedding
+  // [[B_r, B_i], [-B_i, B_r]] for 8 consecutive m of column c (contiguous in memory), and
+  // writes one 16-byte core row per plane
   auto slice_b = [&](int nc, int kc) {
-    for (int e = tid; e < NC * KC; e += blockDim.x) {
-      const int ln = e & 31, wi = e >> 5;
-      constexpr int kgroups = KC / 8;
-      const int n = (wi / kgroups) * 4 + (ln >> 3);
-      const int kk = (wi % kgroups) * 8 + (ln & 7);
-      const bool nre = n < CW, kre = kk < CW;
-      const int cc = nc * CW + (nre ? n : n - CW);    // complex column
-      const int mm = kc * CW + (kre ? kk : kk - CW);  // complex row (K index)
-      double val = 0.0;
-      if (cc < W && mm < W) {
-        const double2 u = Ug[(size_t)cc * W + mm];
-        const double br = u.x, bi = (STEP == 1) ? -u.y : u.y;
-        if (kre && nre) val = br;            // [B_r   B_i]
-        else if (kre && !nre) val = bi;
-        else if (!kre && nre) val = -bi;     // [-B_i  B_r]
-        else val = br;
-      }
-      int x[kS];
-      split_digits<WP>(val, s_colexp[cc < WP ? cc : 0], x);
-      const uint32_t off = kmaj_off(n, kk, KC);
+    constexpr int KG = KC / 8;
+    for (int it = tid; it < NC * KG; it += blockDim.x) {
+      const int n = it % NC, kk0 = (it / NC) * 8;
+      const bool nre = n < CW, kre = kk0 < CW;
+      const int cc = nc * CW + (nre ? n : n - CW);      // complex column
+      const int mm0 = kc * CW + (kre ? kk0 : kk0 - CW); // complex row (K index) of the first
+      double v[8];
 #pragma unroll
-      for (int t = 0; t < kS; ++t) *(uint16_t*)(sB + (size_t)t * L::B_BYTES + off) = int_to_bf16(x[t]);
+      for (int i = 0; i < 8; ++i) {
+        const int mm = mm0 + i;
+        v[i] = 0.0;
+        if (cc < W && mm < W) {
+          const double2 u = Ug[(size_t)cc * W + mm];
+          const double br = u.x, bi = (STEP == 1) ? -u.y : u.y;
+          v[i] = (kre && nre) ? br : (kre ? bi : (nre ? -bi : br));   // [B_r B_i; -B_i B_r]
+        }
+      }
+      uint32_t w[kS][4];
+      pack_digits7(w, v, s_colexp[cc < WP ? cc : 0], false);
+      const uint32_t off = kmaj_off(n, kk0, KC);
+#pragma unroll
+      for (int t = 0; t < kS; ++t)
+        *(uint4*)(sB + (size_t)t * L::B_BYTES + off) = make_uint4(w[t][0], w[t][1], w[t][2], w[t][3]);
     }
   };
 
@@ -251,18 +254,22 @@ __global__ void __launch_bounds__(256, 1) k_oz_mupdate(const Problem* __restrict
         // ---- MMAs: digit pairs (t,u), t+u <= S-1 (0-based) -> accumulator of diagonal t+u
         if (tid == 0) {
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          // descriptors: the base descriptor plus the byte offset / 16 in the address field
+          // (shared-memory addresses stay below 2^18, so the field holds it)
+          const uint64_t da = smem_desc(smem_u32(sA), 128, (KC / 8) * 128);
+          const uint64_t db = smem_desc(smem_u32(sB), 128, (KC / 8) * 128);
+#pragma unroll
           for (int t = 0; t < kS; ++t) {
+#pragma unroll
             for (int u = 0; u + t <= kS - 1; ++u) {
               const int d = t + u;
               const uint32_t dtm = tmem + (uint32_t)(d * NC);
-              const uint32_t a0 = smem_u32(sA + (size_t)t * L::A_BYTES);
-              const uint32_t b0 = smem_u32(sB + (size_t)u * L::B_BYTES);
               // the first write of every diagonal d in this N chunk is pair (0, d) of chunk kc = 0
               const bool first_pair = (kc == 0) && (t == 0);
 #pragma unroll
               for (int ks = 0; ks < KC / 16; ++ks) {
-                const uint64_t ad = smem_desc(a0 + ks * 256, 128, (KC / 8) * 128);
-                const uint64_t bd = smem_desc(b0 + ks * 256, 128, (KC / 8) * 128);
+                const uint64_t ad = da + (uint64_t)(((size_t)t * L::A_BYTES + ks * 256) >> 4);
+                const uint64_t bd = db + (uint64_t)(((size_t)u * L::B_BYTES + ks * 256) >> 4);
                 const uint32_t acc = (first_pair && ks == 0) ? 0u : 1u;
                 asm volatile(
                     "{\n\t.reg .pred p;\n\t"

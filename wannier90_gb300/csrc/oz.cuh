@@ -143,6 +143,56 @@ __device__ __forceinline__ void digits7x8(long long n, int x[7]) {
   x[0] = (int)n;
 }
 
+// The digits of digits7x8 as exact floats (f[t] = x[t]), without the serial recoding:
+// with C = 128 (1 + 2^8 + ... + 2^40), x_{6-t} = byte t of N + C minus 128 (t = 0..5) and
+// x_0 = (N + C) >> 48 (arithmetic).  (Adding 128 at every lower byte position turns the
+// centred digits into the plain bytes of N + C: x_6 = sext8(N mod 2^8) = byte0(N + 128) -
+// 128, and (N - x_6) / 2^8 = (N + 128) >> 8, so the next step repeats on N + 128 shifted.)
+// A byte b becomes the float b - 128 by one OR into 1.5 * 2^23 and one subtraction.
+__device__ __forceinline__ void digits7x8_f(long long n, float f[7]) {
+  const long long m = n + 0x808080808080LL;
+  const uint32_t lo = (uint32_t)m, hi = (uint32_t)((unsigned long long)m >> 32);
+#pragma unroll
+  for (int t = 0; t < 6; ++t) {
+    const uint32_t b = ((t < 4 ? lo >> (8 * t) : hi >> (8 * (t - 4))) & 255u);
+    f[6 - t] = __uint_as_float(0x4B400000u | b) - 12583040.0f;   // 1.5 * 2^23 + 128
+  }
+  f[0] = (float)(int)(m >> 48);
+}
+
+// The same for digits7 (7-bit digits of |N| <= 2^49): C = 64 (1 + 2^7 + ... + 2^35),
+// x_{6-t} = bits 7t..7t+6 of N + C minus 64, x_0 = (N + C) >> 42.
+__device__ __forceinline__ void digits7_f(long long n, float f[7]) {
+  const long long m = n + 0x20408102040LL;
+  const uint32_t lo = (uint32_t)m, hi = (uint32_t)((unsigned long long)m >> 32);
+  const uint32_t mid = __funnelshift_r(lo, hi, 28);   // bits 28..59
+#pragma unroll
+  for (int t = 0; t < 6; ++t) {
+    const uint32_t b = (t < 4 ? lo >> (7 * t) : (t == 4 ? mid : hi >> 3)) & 127u;
+    f[6 - t] = __uint_as_float(0x4B400000u | b) - 12582976.0f;   // 1.5 * 2^23 + 64
+  }
+  f[0] = (float)(int)(m >> 42);
+}
+
+// BF16 bits of two exact floats (values that BF16 holds) packed as (lo, hi) halves
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
+  return __byte_perm(__float_as_uint(lo), __float_as_uint(hi), 0x7632);
+}
+
+// The seven 7-bit digit planes of 8 values scaled by 2^(49 - ex) (negated first when neg),
+// as packed BF16 pairs: w[t][i / 2] holds digit t of values i (low half) and i + 1 -- the
+// digits and BF16 bits of slicing the values one at a time.
+__device__ __forceinline__ void pack_digits7(uint32_t (&w)[kS][4], const double (&v)[8], int ex, bool neg) {
+#pragma unroll
+  for (int i = 0; i < 8; i += 2) {
+    float fa[kS], fb[kS];
+    digits7_f(scaled_int(neg ? -v[i] : v[i], ex), fa);
+    digits7_f(scaled_int(neg ? -v[i + 1] : v[i + 1], ex), fb);
+#pragma unroll
+    for (int t = 0; t < kS; ++t) w[t][i >> 1] = pack_bf16x2(fa[t], fb[t]);
+  }
+}
+
 // exact integer value of an integer-valued float with |f| < 2^24
 __device__ __forceinline__ int float_to_int_exact24(float f) {
   return (fabsf(f) < 4194304.0f) ? float_to_int_exact(f) : __float2int_rn(f);
