@@ -5,9 +5,10 @@ that is not skipped gives up at once; the drain limit that follows a timeout is
 unchanged).  Each kernel must then record device status 2, wait for the MMAs and bulk
 copies it already issued, free its tensor memory and return: the call reports the error,
 and the GPU stays usable -- a normal solve in the same test afterwards gives the expected
-result.  Three routes: the pipelined M update (num_wann <= 32, FP64 exp so that the M
+result.  Four routes: the pipelined M update (num_wann <= 32, FP64 exp so that the M
 update runs first; its producer has issued one bulk copy per stage slot, which the drain
-must let land), the tensor exp (its first product's MMAs are in flight), and the
+must let land) with two accumulator sets (num_wann 8) and with the two half sets of
+num_wann 32, the tensor exp (its first product's MMAs are in flight), and the
 one-CTA-per-group M update (num_wann > 32, its first bulk copy in flight)."""
 import json
 import os
@@ -45,7 +46,7 @@ for W, texp in %(cases)r:
 print(json.dumps(out))
 """
 
-CASES = [(8, 0), (24, 1), (40, 0)]
+CASES = [(8, 0), (24, 0), (24, 1), (40, 0)]
 
 
 def test_timed_out_waits_report_error_and_leave_the_gpu_usable(tmp_path):

@@ -47,6 +47,7 @@ cudaError_t oz2_launch(int wp, int step, const Problem* probs, WorkMap wm, int w
                        cudaStream_t s);
 cudaError_t oz2_set_attributes(int wp);
 cudaError_t oz2_preslice_launch(int wp, const Problem* probs, WorkMap wm, int grid, cudaStream_t s);
+void oz2_ub2_bytes(int wp, int K, size_t* data, size_t* exps);
 cudaError_t oz_launch(int wp, int step, const Problem* probs, WorkMap wm, int which, int grid,
                       cudaStream_t s);
 cudaError_t oz_set_attributes(int wp);
@@ -188,14 +189,14 @@ int choose_tensor_wp(const std::vector<ProblemSpec>& specs) {
 
 struct Sizes {
   size_t M, U, KWW, work, tbuf, diag, offd, gpart, cen, log, logc, nn, bk, wb, st, op1, op2, m0, u0, inv, fr;
-  size_t m0s, m0e, zexp;
+  size_t m0s, m0e, zexp, ub2, ub2e;
   size_t pkr, pr2, pgr, pgp, ppart;
   size_t gbka, gneigh, grg, gsheet, gcsheet;
   size_t slwf;
   size_t symi, symd, symw;
   size_t total() const {
     return 2 * M + 2 * U + 3 * KWW + work + tbuf + 2 * diag + offd + gpart + cen + log + logc + nn + bk + wb + st +
-           op1 + op2 + m0 + u0 + inv + fr + m0s + m0e + zexp + pkr + 2 * pr2 + pgr + pgp + ppart + gbka + gneigh + grg + gsheet +
+           op1 + op2 + m0 + u0 + inv + fr + m0s + m0e + zexp + ub2 + ub2e + pkr + 2 * pr2 + pgr + pgp + ppart + gbka + gneigh + grg + gsheet +
            gcsheet + slwf + symi + 2 * symd + symw;
   }
 };
@@ -218,6 +219,13 @@ Sizes problem_sizes(const ProblemSpec& s, int wp, int* pc_tiles) {
   z.fr = wp ? align_up(K * B * 8) : 0;
   z.m0s = z.m0e = 0;
   z.zexp = (wp && wp <= 32) ? align_up(K * B * W * 4) : 0;
+  z.ub2 = z.ub2e = 0;
+  if (wp && wp <= 32) {
+    size_t d = 0, e = 0;
+    oz2_ub2_bytes(wp, (int)K, &d, &e);
+    z.ub2 = align_up(d);
+    z.ub2e = align_up(e);
+  }
   if (wp) {
     size_t d = 0, e = 0;
     oz_preslice_bytes(wp, (int)K, (int)B, &d, &e);
@@ -377,6 +385,8 @@ int Engine::alloc(std::string& err) {
     P.m0s = z.m0s ? (unsigned char*)take(z.m0s) : nullptr;
     P.m0s_exp = z.m0e ? (int*)take(z.m0e) : nullptr;
     P.zexp = z.zexp ? (int*)take(z.zexp) : nullptr;
+    P.ub2 = z.ub2 ? (unsigned char*)take(z.ub2) : nullptr;
+    P.ub2_exp = z.ub2e ? (int*)take(z.ub2e) : nullptr;
     if (inv) {
       std::vector<int> h_inv((size_t)s.K * s.B), fill(s.K, 0);
       for (int kb = 0; kb < s.K * s.B; ++kb) {

@@ -59,6 +59,7 @@ constexpr int pow2_cols(int c) { return c <= 32 ? 32 : (c <= 64 ? 64 : (c <= 128
 
 template <int WP>
 struct MU2 {
+  static constexpr int kPlanesPerMma = (2 * WP) >= 256 ? 1 : 256 / (2 * WP);   // B planes per MMA (N <= 256)
   static_assert(WP == 8 || WP == 16 || WP == 32, "pipelined M update: num_wann <= 32");
   static constexpr int CW = WP;                    // complex columns (one N chunk)
   static constexpr int KC = 2 * WP;                // real K per tile
@@ -146,6 +147,8 @@ __global__ void __launch_bounds__(Roles<STEP>::THREADS, 1)
   using L = MU2<WP>;
   using R = Roles<STEP>;
   constexpr int CW = L::CW, KC = L::KC, NC = L::NC, KSTEPS = L::KSTEPS, NS = L::NS, NACC = L::NACC;
+  constexpr int kPlanesPerMma = L::kPlanesPerMma;
+
   constexpr int kEpiWarps = R::EPI, kMmaWarp = R::MMA, kEpiThreads = R::ET;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -174,7 +177,7 @@ __global__ void __launch_bounds__(Roles<STEP>::THREADS, 1)
       mbar_init(&a_empty[s], 1u);
     }
     for (int b = 0; b < 2; ++b) {
-      mbar_init(&b_full[b], (uint32_t)R::PBT);
+      mbar_init(&b_full[b], STEP == 1 ? (uint32_t)R::PBT : 1u);
       mbar_init(&b_empty[b], 1u + (uint32_t)kEpiThreads);
     }
     for (int a = 0; a < NACC; ++a) {
@@ -307,8 +310,14 @@ __global__ void __launch_bounds__(Roles<STEP>::THREADS, 1)
         if (inflight & (1u << s)) mbar_drain(smem_u32(&a_full[s]), (inflight_par >> s) & 1);
   } else if (warp >= kEpiWarps + R::PA && warp < kMmaWarp) {
     // =========================== B producer ===========================
+    // Step 1 slices conj(U(k)) into the B buffer and also writes the planes of U(k) as step
+    // 2 uses them (the same three digit decompositions, Re U, Im U and -Im U, with the two
+    // imaginary quadrants exchanged) to the per-k image ub2, with the column exponents
+    // (conjugation keeps the moduli).  Step 2 takes its group's B from that image with one
+    // bulk copy.
     const int pb = tid - kEpiThreads - R::PAT;
     int gseq = 0;          // groups started
+    uint32_t inflight = 0, inflight_par = 0;   // step 2: buffers with a bulk copy issued, and its parity
     auto bwait = [&](uint64_t* bar, uint32_t parity, int p) -> bool {
       if (pb == 0) {
         const bool ok = mbar_wait_role(smem_u32(bar), parity, &s_bad);
@@ -330,6 +339,25 @@ __global__ void __launch_bounds__(Roles<STEP>::THREADS, 1)
       const int bb = gseq & 1;
       // (the first use of each B buffer needs no wait)
       if (gseq >= 2 && !bwait(&b_empty[bb], ((gseq >> 1) & 1) ^ 1, p)) break;
+      unsigned char* dB = sB + (size_t)bb * L::B_BYTES;
+      if constexpr (STEP == 2) {
+        // column scales and planes from step 1's image of U(k')
+        for (int c = pb; c < WP; c += R::PBT) s_colexp[bb][c] = P.ub2_exp[(size_t)g * WP + c];
+        bar_named(3, R::PBT);
+        inflight &= ~(1u << bb);   // the buffer's previous copy was consumed (b_empty)
+        if (pb == 0) {
+          const unsigned char* src = P.ub2 + (size_t)g * L::B_BYTES;
+          asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}"
+                       :: "r"(smem_u32(&b_full[bb])), "r"((uint32_t)L::B_BYTES) : "memory");
+          asm volatile(
+              "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+              :: "r"(smem_u32(dB)), "l"(src), "r"((uint32_t)L::B_BYTES), "r"(smem_u32(&b_full[bb]))
+              : "memory");
+          inflight |= 1u << bb;
+          inflight_par = (inflight_par & ~(1u << bb)) | ((((uint32_t)gseq >> 1) & 1u) << bb);
+        }
+        ++gseq;
+      } else {
       // column scales: one column per thread, 8 independent loads per round
       for (int c = pb; c < WP; c += R::PBT) {
         unsigned long long mx = 0ull;
@@ -342,9 +370,10 @@ __global__ void __launch_bounds__(Roles<STEP>::THREADS, 1)
             for (int i = 0; i < 8; ++i) mx = max(mx, max(abs_bits(v[i].x), abs_bits(v[i].y)));
           }
         s_colexp[bb][c] = exp_above_bits(mx);
+        if (P.ub2_exp) P.ub2_exp[(size_t)g * WP + c] = exp_above_bits(mx);
       }
       bar_named(3, R::PBT);
-      unsigned char* dB = sB + (size_t)bb * L::B_BYTES;
+      unsigned char* gB = P.ub2 ? P.ub2 + (size_t)g * L::B_BYTES : nullptr;   // step 2's image of U(k)
       // B^T planes: each complex U(m, c) gives the four real entries of the embedding
       // [[B_r, B_i], [-B_i, B_r]]; B_r, B_i and -B_i are sliced once each.  A thread takes
       // one part of 8 consecutive m of column c (contiguous in memory; their K positions
@@ -360,7 +389,7 @@ __global__ void __launch_bounds__(Roles<STEP>::THREADS, 1)
           v[i] = 0.0;
           if (cc < W && mm < W) {
             const double2 u = Ug[(size_t)cc * W + mm];
-            v[i] = part == 0 ? u.x : ((STEP == 1) ? -u.y : u.y);
+            v[i] = part == 0 ? u.x : -u.y;     // step 1: B = conj(U)
           }
         }
         uint32_t w[kS][4];
@@ -370,29 +399,46 @@ __global__ void __launch_bounds__(Roles<STEP>::THREADS, 1)
           const uint32_t o_rr = kmaj_off(cc, k_re, KC), o_ii = kmaj_off(CW + cc, k_im, KC);
 #pragma unroll
           for (int t = 0; t < kS; ++t) {
+            const uint4 q = make_uint4(w[t][0], w[t][1], w[t][2], w[t][3]);
             unsigned char* pl = dB + (size_t)t * L::B_PLANE;
-            *(uint4*)(pl + o_rr) = make_uint4(w[t][0], w[t][1], w[t][2], w[t][3]);   // (K re, N re) = B_r
-            *(uint4*)(pl + o_ii) = make_uint4(w[t][0], w[t][1], w[t][2], w[t][3]);   // (K im, N im) = B_r
+            *(uint4*)(pl + o_rr) = q;   // (K re, N re) = B_r
+            *(uint4*)(pl + o_ii) = q;   // (K im, N im) = B_r
+            if (gB) {
+              *(uint4*)(gB + (size_t)t * L::B_PLANE + o_rr) = q;
+              *(uint4*)(gB + (size_t)t * L::B_PLANE + o_ii) = q;
+            }
           }
         } else {
+          // B_i = -Im U (step 1) to (N im, K re) -- for step 2 (B_i = Im U) the same digits
+          // go to (N re, K im) -- and -B_i = Im U to (N re, K im), for step 2 to (N im, K re)
           const uint32_t o_ir = kmaj_off(CW + cc, k_re, KC), o_ri = kmaj_off(cc, k_im, KC);
 #pragma unroll
-          for (int t = 0; t < kS; ++t)   // (K re, N im) = B_i
-            *(uint4*)(dB + (size_t)t * L::B_PLANE + o_ir) = make_uint4(w[t][0], w[t][1], w[t][2], w[t][3]);
+          for (int t = 0; t < kS; ++t) {
+            const uint4 q = make_uint4(w[t][0], w[t][1], w[t][2], w[t][3]);
+            *(uint4*)(dB + (size_t)t * L::B_PLANE + o_ir) = q;
+            if (gB) *(uint4*)(gB + (size_t)t * L::B_PLANE + o_ri) = q;
+          }
           pack_digits7(w, v, ec, true);
 #pragma unroll
-          for (int t = 0; t < kS; ++t)   // (K im, N re) = -B_i, the digits of the negated values
-            *(uint4*)(dB + (size_t)t * L::B_PLANE + o_ri) = make_uint4(w[t][0], w[t][1], w[t][2], w[t][3]);
+          for (int t = 0; t < kS; ++t) {   // the digits of the negated values
+            const uint4 q = make_uint4(w[t][0], w[t][1], w[t][2], w[t][3]);
+            *(uint4*)(dB + (size_t)t * L::B_PLANE + o_ri) = q;
+            if (gB) *(uint4*)(gB + (size_t)t * L::B_PLANE + o_ir) = q;
+          }
         }
       }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       mbar_arrive(&b_full[bb]);
       ++gseq;
+      }
     }
+    // drain (step 2): bulk copies still in flight must land before the CTA frees its memory
+    if (STEP == 2 && pb == 0)
+      for (int b = 0; b < 2; ++b)
+        if (inflight & (1u << b)) mbar_drain(smem_u32(&b_full[b]), (inflight_par >> b) & 1);
   } else if (warp == kMmaWarp) {
     // =========================== MMA issue ===========================
     if (lane == 0) {
-      const uint32_t idesc = idesc_bf16(NC);
       int gseq = 0, sseq = 0, useq = 0;
       bool issued = false, ok = true;
       for (int item = blockIdx.x; item < ngroups && ok; item += gridDim.x) {
@@ -407,7 +453,7 @@ __global__ void __launch_bounds__(Roles<STEP>::THREADS, 1)
           break;
         }
         const uint32_t b0 = smem_u32(sB + (size_t)bb * L::B_BYTES);
-        for (int tile = 0; tile < ntiles; ++tile) {
+        for (int tile = 0; tile < ntiles && ok; ++tile) {
           const int a = useq % NACC;
           const uint32_t ause = (uint32_t)(useq / NACC);
           // (the first use of each accumulator set needs no wait)
@@ -430,20 +476,25 @@ __global__ void __launch_bounds__(Roles<STEP>::THREADS, 1)
             // (shared-memory addresses stay below 2^18, so the field holds it)
             const uint64_t da = smem_desc(smem_u32(sA + (size_t)s * L::STAGE), 128, 256);
             const uint64_t db = smem_desc(b0 + ks * 256, 128, (KC / 8) * 128);
+            // The B planes follow one another as consecutive row groups of one K-major
+            // operand, and diagonal d's accumulator columns follow d - 1's: digit plane t
+            // of A against planes u0 .. u0 + n - 1 of B is one MMA with N = n NC, writing
+            // diagonals t + u0 .. at once (N <= 256).  The integer sums are exact, so the
+            // grouping does not change them.
 #pragma unroll
             for (int t = 0; t < kS; ++t) {
               const uint64_t ad = da + (uint64_t)((t * L::PLANE) >> 4);
 #pragma unroll
-              for (int u = 0; u + t <= kS - 1; ++u) {
-                const int d = t + u;
-                const uint64_t bd = db + (uint64_t)((u * L::B_PLANE) >> 4);
-                // the first write of diagonal d in this tile: pair (0, d) of K-step 0
+              for (int u0 = 0; u0 + t <= kS - 1; u0 += kPlanesPerMma) {
+                const int n = (kS - t - u0) < kPlanesPerMma ? (kS - t - u0) : kPlanesPerMma;
+                const uint64_t bd = db + (uint64_t)((u0 * L::B_PLANE) >> 4);
+                // the first write of every diagonal in this tile: plane 0 of A, K-step 0
                 const uint32_t accf = (ks == 0 && t == 0) ? 0u : 1u;
                 asm volatile(
                     "{\n\t.reg .pred p;\n\t"
                     "setp.ne.b32 p, %4, 0;\n\t"
                     "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
-                    :: "r"(acc + (uint32_t)(d * NC)), "l"(ad), "l"(bd), "r"(idesc), "r"(accf)
+                    :: "r"(acc + (uint32_t)((t + u0) * NC)), "l"(ad), "l"(bd), "r"(idesc_bf16(n * NC)), "r"(accf)
                     : "memory");
               }
             }
@@ -482,7 +533,7 @@ __global__ void __launch_bounds__(Roles<STEP>::THREADS, 1)
       const int cur = P.st->cur;
       const int ntiles = ntiles_of<WP>(B);
       const int bb = gseq & 1;
-      for (int tile = 0; tile < ntiles; ++tile) {
+      for (int tile = 0; tile < ntiles && ok; ++tile) {
         const int a = useq % NACC;
         const uint32_t ause = (uint32_t)(useq / NACC);
         // the row's scale and output block, fetched before the accumulators are ready
@@ -688,6 +739,13 @@ cudaError_t oz2_launch(int wp, int step, const Problem* probs, WorkMap wm, int w
     case 32: return launch2_wp<32>(step, probs, wm, which, ngroups, s);
     default: return cudaErrorInvalidValue;
   }
+}
+
+// bytes of step 2's per-k B image and its column exponents
+void oz2_ub2_bytes(int wp, int K, size_t* data, size_t* exps) {
+  const size_t b_bytes = (size_t)kS * (2 * wp) * (2 * wp) * 2;
+  *data = (size_t)K * b_bytes;
+  *exps = (size_t)K * wp * 4;
 }
 
 cudaError_t oz2_set_attributes(int wp) {

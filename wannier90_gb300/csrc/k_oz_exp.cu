@@ -217,7 +217,6 @@ __device__ bool oz_cmm(OzCtx& cx, double2* C, const double2* A, const unsigned* 
   // ---- power-of-two scales: rows of A, columns of B (over re and im parts)
   ab_exponents<WP>(cx, A, arow, B, bcol, W);
   __syncthreads();
-  const uint32_t idesc = idesc_bf16(NC);
   bool ok = true;
   for (int nc = 0; nc < NCH && ok; ++nc) {
     for (int kc = 0; kc < NCH && ok; ++kc) {
@@ -264,22 +263,30 @@ __device__ bool oz_cmm(OzCtx& cx, double2* C, const double2* A, const unsigned* 
       __syncthreads();
       if (tid == 0) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        // descriptors from a base plus offsets / 16 (shared-memory addresses stay below
+        // 2^18); B's digit planes follow one another as row groups of one K-major operand
+        // and diagonal d's accumulator columns follow d - 1's, so slice t of A against
+        // planes u0 .. u0 + n - 1 of B is one MMA with N = n NC (<= 256)
+        const uint64_t da = smem_desc(smem_u32(cx.sA), 128, (KC / 8) * 128);
+        const uint64_t db = smem_desc(smem_u32(cx.sB), 128, (KC / 8) * 128);
+        constexpr int PPM = 256 / NC;
+#pragma unroll
         for (int t = 0; t < kS8; ++t) {
-          for (int u = 0; u + t <= kS8 - 1; ++u) {
-            const uint32_t dtm = cx.tmem + (uint32_t)((t + u) * NC);
-            const uint32_t a0 = smem_u32(cx.sA + (size_t)t * E::A_SLICE);
-            const uint32_t b0 = smem_u32(cx.sB + (size_t)u * E::B_BYTES);
+#pragma unroll
+          for (int u0 = 0; u0 + t <= kS8 - 1; u0 += PPM) {
+            const int n = (kS8 - t - u0) < PPM ? (kS8 - t - u0) : PPM;
+            const uint32_t dtm = cx.tmem + (uint32_t)((t + u0) * NC);
             const bool first_pair = (kc == 0) && (t == 0);
 #pragma unroll
             for (int ks = 0; ks < KC / 16; ++ks) {
-              const uint64_t ad = smem_desc(a0 + ks * 256, 128, (KC / 8) * 128);
-              const uint64_t bd = smem_desc(b0 + ks * 256, 128, (KC / 8) * 128);
+              const uint64_t ad = da + (uint64_t)(((size_t)t * E::A_SLICE + ks * 256) >> 4);
+              const uint64_t bd = db + (uint64_t)(((size_t)u0 * E::B_BYTES + ks * 256) >> 4);
               const uint32_t acc = (first_pair && ks == 0) ? 0u : 1u;
               asm volatile(
                   "{\n\t.reg .pred p;\n\t"
                   "setp.ne.b32 p, %4, 0;\n\t"
                   "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
-                  :: "r"(dtm), "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+                  :: "r"(dtm), "l"(ad), "l"(bd), "r"(idesc_bf16(n * NC)), "r"(acc)
                   : "memory");
             }
           }
@@ -470,7 +477,6 @@ __device__ bool oz_cmm2(OzCtx& cx, double2* C, const double2* A, const unsigned*
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   ab_exponents<WP>(cx, A, arow, B, bcol, W);
   __syncthreads();
-  const uint32_t idesc = idesc_bf16(N);
   bool ok = true;
   for (int kc = 0; kc < E::NCHK && ok; ++kc) {
     // ---- A_emb chunk: complex (r, l) -> rows r (re) and WP + r (im), K l (re) / CW + l (im),
@@ -521,22 +527,27 @@ __device__ bool oz_cmm2(OzCtx& cx, double2* C, const double2* A, const unsigned*
       // its address field (shared-memory addresses stay below 2^18, so the field holds it)
       const uint64_t da = smem_desc(smem_u32(cx.sA), 128, (KC / 8) * 128);
       const uint64_t db = smem_desc(smem_u32(cx.sB), 128, (KC / 8) * 128);
+      // B's digit planes follow one another as row groups of one K-major operand and
+      // diagonal d's accumulator columns follow d - 1's: slice t of A against planes
+      // u0 .. u0 + n - 1 of B is one MMA with N = n N, writing diagonals t + u0 .. (N <= 256)
+      constexpr int PPM = 256 / N;
 #pragma unroll
       for (int t = 0; t < kS2; ++t) {
 #pragma unroll
-        for (int u = 0; u + t <= kS2 - 1; ++u) {
-          const uint32_t dtm = cx.tmem + (uint32_t)((t + u) * N);
+        for (int u0 = 0; u0 + t <= kS2 - 1; u0 += PPM) {
+          const int n = (kS2 - t - u0) < PPM ? (kS2 - t - u0) : PPM;
+          const uint32_t dtm = cx.tmem + (uint32_t)((t + u0) * N);
           const bool first_pair = (kc == 0) && (t == 0);
 #pragma unroll
           for (int ks = 0; ks < KC / 16; ++ks) {
             const uint64_t ad = da + (uint64_t)(((size_t)t * E::A_SLICE + ks * 256) >> 4);
-            const uint64_t bd = db + (uint64_t)(((size_t)u * E::B_BYTES + ks * 256) >> 4);
+            const uint64_t bd = db + (uint64_t)(((size_t)u0 * E::B_BYTES + ks * 256) >> 4);
             const uint32_t acc = (first_pair && ks == 0) ? 0u : 1u;
             asm volatile(
                 "{\n\t.reg .pred p;\n\t"
                 "setp.ne.b32 p, %4, 0;\n\t"
                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
-                :: "r"(dtm), "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+                :: "r"(dtm), "l"(ad), "l"(bd), "r"(idesc_bf16(n * N)), "r"(acc)
                 : "memory");
           }
         }

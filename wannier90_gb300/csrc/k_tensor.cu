@@ -187,7 +187,6 @@ __global__ void __launch_bounds__(256, 1) k_oz_mupdate(const Problem* __restrict
   __syncthreads();
   if (NCH == 1) slice_b(0, 0);
   const uint32_t tmem = tmem_base_slot;
-  const uint32_t idesc = idesc_bf16(NC);
   uint32_t phase = 0, phase_ld = 0;
 
   // A element (row, complex K index m) of this tile
@@ -258,24 +257,28 @@ __global__ void __launch_bounds__(256, 1) k_oz_mupdate(const Problem* __restrict
           // (shared-memory addresses stay below 2^18, so the field holds it)
           const uint64_t da = smem_desc(smem_u32(sA), 128, (KC / 8) * 128);
           const uint64_t db = smem_desc(smem_u32(sB), 128, (KC / 8) * 128);
+          // B's digit planes follow one another as row groups of one K-major operand and
+          // diagonal d's accumulator columns follow d - 1's: slice t of A against planes
+          // u0 .. u0 + n - 1 of B is one MMA with N = n NC (<= 256), writing diagonals t + u0 ..
+          constexpr int PPM = 256 / NC;
 #pragma unroll
           for (int t = 0; t < kS; ++t) {
 #pragma unroll
-            for (int u = 0; u + t <= kS - 1; ++u) {
-              const int d = t + u;
-              const uint32_t dtm = tmem + (uint32_t)(d * NC);
-              // the first write of every diagonal d in this N chunk is pair (0, d) of chunk kc = 0
+            for (int u0 = 0; u0 + t <= kS - 1; u0 += PPM) {
+              const int n = (kS - t - u0) < PPM ? (kS - t - u0) : PPM;
+              const uint32_t dtm = tmem + (uint32_t)((t + u0) * NC);
+              // the first write of every diagonal in this N chunk: slice 0 of A, chunk kc = 0
               const bool first_pair = (kc == 0) && (t == 0);
 #pragma unroll
               for (int ks = 0; ks < KC / 16; ++ks) {
                 const uint64_t ad = da + (uint64_t)(((size_t)t * L::A_BYTES + ks * 256) >> 4);
-                const uint64_t bd = db + (uint64_t)(((size_t)u * L::B_BYTES + ks * 256) >> 4);
+                const uint64_t bd = db + (uint64_t)(((size_t)u0 * L::B_BYTES + ks * 256) >> 4);
                 const uint32_t acc = (first_pair && ks == 0) ? 0u : 1u;
                 asm volatile(
                     "{\n\t.reg .pred p;\n\t"
                     "setp.ne.b32 p, %4, 0;\n\t"
                     "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
-                    :: "r"(dtm), "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+                    :: "r"(dtm), "l"(ad), "l"(bd), "r"(idesc_bf16(n * NC)), "r"(acc)
                     : "memory");
               }
             }

@@ -132,6 +132,9 @@ struct Problem {
   int* m0s_exp;         // tensor path: the row exponents of those tiles [k][tile][128]
   int* zexp;            // pipelined tensor path: step 2's row exponents [k][b][row of Z(k,b)],
                         // written by step 1's epilogue
+  unsigned char* ub2;   // pipelined tensor path: step 2's B operand -- the digit planes of U(k)
+                        // in the shared-memory layout, per k -- written by step 1's B producer
+  int* ub2_exp;         // ... and the column exponents of U(k) [k][WP]
   double2* U0;          // tensor path: U at entry; U[] then holds R = U0^H U
   const int* inv_nnlist;  // tensor path: [k'][i] = k*B+b with nnlist(k,b) = k'
   double* frob0;        // tensor path: |M0(k,b)|_F^2
