@@ -1268,9 +1268,9 @@ KNOWN_ITERS = {"dis_fcc8_b48w32": (200, 3053)}
 # kernel, from the committed ncu captures under profiles/ (name of the summary beside each)
 NCU_TRAFFIC = {
     # profiles/k_oz_mupdate2_fcc10_w32.md: steps 1 + 2 of one M update
-    ("fcc10_w32", "k_m_update"): 584.1e6,
+    ("fcc10_w32", "k_m_update"): 678.6e6,
     # profiles/k_oz_exp_fcc10_w32.md: one trial-step exp launch
-    ("fcc10_w32", "k_exp_u"): 139.2e6,
+    ("fcc10_w32", "k_exp_u"): 132.0e6,
 }
 
 if __name__ == "__main__":

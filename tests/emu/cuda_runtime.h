@@ -30,6 +30,10 @@ extern dim3 blockDim, gridDim;
 void emu_syncthreads();
 #define __syncthreads() emu_syncthreads()
 template <class T> inline T __ldg(const T* p) { return *p; }
+template <class T> inline T __ldcg(const T* p) { return *(const volatile T*)p; }
+// device-wide ordering and the counter of the spread passes' last-CTA reductions
+inline void __threadfence() { __atomic_thread_fence(__ATOMIC_SEQ_CST); }
+inline unsigned atomicAdd(unsigned* a, unsigned v) { return __atomic_fetch_add(a, v, __ATOMIC_SEQ_CST); }
 // CUDA's integer min / max overloads
 inline int min(int a, int b) { return a < b ? a : b; }
 inline int max(int a, int b) { return a > b ? a : b; }

@@ -119,7 +119,6 @@ int emu_wann_main(int W, int K, int B, const int* nnlist, const double* bk, cons
   auto omega = [&](int slot) {
     launch(nchunk, 256, 0, [&] { k_omega_p1(pp, wmc, slot); });
     launch(nchunk, 256, 0, [&] { k_omega_p2(pp, wmc, slot); });
-    launch(1, 256, 0, [&] { k_omega_p3(pp, slot); });
   };
   // Engine::project
   launch(K, 256, sm4, [&] { k_lowdin(pp, wmk, st_lowdin.data()); });

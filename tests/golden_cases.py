@@ -132,6 +132,30 @@ def conv_sensitivity(M0, U0, km, ctl, noise=1e-14, runs=2, slwf=None, grad=False
     return out if len(out) > 1 else sens
 
 
+def match_centres(a, b, lattice):
+    """One-to-one partners of the centres a[i] among b[j] (greedy by distance, distances
+    modulo lattice translations): (largest distance, [(i, j), ...], distance matrix).  WF
+    labels are arbitrary: two runs that end at the same minimum may order the WFs
+    differently."""
+    import numpy as np
+    inv = np.linalg.inv(lattice)
+    d = np.zeros((len(a), len(b)))
+    for i in range(len(a)):
+        f = (b - a[i]) @ inv
+        f -= np.round(f)
+        d[i] = np.linalg.norm(f @ lattice, axis=1)
+    used_a, used_b, pairs, worst = set(), set(), [], 0.0
+    for flat in np.argsort(d, axis=None):
+        i, j = divmod(int(flat), len(b))
+        if i in used_a or j in used_b:
+            continue
+        used_a.add(i)
+        used_b.add(j)
+        pairs.append((i, j))
+        worst = max(worst, d[i, j])
+    return worst, sorted(pairs), d
+
+
 def conv_tolerance(sens, it, spread, floor=2e-10, factor=10.0, span=0):
     """2e-10 A^2 where the trajectory is insensitive at that level, else `factor` times the
     measured sensitivity (at least the metric's 1e-8 relative).  span > 0 takes the

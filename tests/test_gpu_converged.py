@@ -33,6 +33,7 @@ import numpy as np
 import pytest
 
 from oracle import w90_oracle as O
+from tests import golden_cases as G
 from tests.engine_helpers import run_engine
 from wannier90_gb300 import synth
 
@@ -56,20 +57,7 @@ def _problem(name):
 def _match_centres(a, b, lattice):
     """Largest distance between the centres a[i] and their partners in b (one-to-one,
     greedy by distance), distances taken modulo lattice translations."""
-    inv = np.linalg.inv(lattice)
-    d = np.zeros((len(a), len(b)))
-    for i in range(len(a)):
-        f = (b - a[i]) @ inv
-        f -= np.round(f)
-        d[i] = np.linalg.norm(f @ lattice, axis=1)
-    used_a, used_b, worst = set(), set(), 0.0
-    for flat in np.argsort(d, axis=None):
-        i, j = divmod(int(flat), len(b))
-        if i in used_a or j in used_b:
-            continue
-        used_a.add(i)
-        used_b.add(j)
-        worst = max(worst, d[i, j])
+    worst, _, d = G.match_centres(a, b, lattice)
     return worst, d
 
 

@@ -67,14 +67,21 @@ def test_disentangle_golden(name, tensor):
     # the oracle's own sensitivity to a 1e-14 perturbation of M0 (the GaAs case's middle
     # iterations move by 1e-5 A^2 under it).  The tensor path rounds every product at
     # ~2^-49 of its scales on every iteration, a perturbation renewed at each step: 2e-9,
-    # and twenty times the largest change over four 1e-13 perturbations
+    # and twenty times the largest change over four 1e-13 perturbations.  The final centres:
+    # the printed 6 decimals plus three times the oracle's own spread of them over runs
+    # perturbed as the path rounds (the tensor path: 1e-13 at every M update; the GaAs
+    # case's centres move by up to 4e-7 A under it)
     assert out["wann_ierr"] == 0, out["wann_err"]
     by_iter = {int(row[0]): row for row in out["log"]}
     sens = G.conv_sensitivity(M0, U0, km, ctl, noise=1e-13 if tensor else 1e-14, runs=4 if tensor else 2)
     for it, delta, rms, spread in d["conv"]:
         tol = G.conv_tolerance(sens, it, spread, floor=2e-9 if tensor else 2e-10, factor=20.0 if tensor else 10.0)
         assert abs(by_iter[int(it)][3] - spread) < tol, (int(it), by_iter[int(it)][3], spread, tol)
-    np.testing.assert_allclose(out["centres"].T, d["centres_final"][:, :3], atol=1.01e-6)
+    _, csens = G.conv_sensitivity(M0, U0, km, ctl, noise=1e-13 if tensor else 1e-14, runs=4 if tensor else 2,
+                                  centres=True, per_update=bool(tensor))
+    ctol = 1.01e-6 + 3.0 * csens
+    assert np.all(np.abs(out["centres"].T - d["centres_final"][:, :3]) <= ctol[:, None]), \
+        (out["centres"].T, d["centres_final"][:, :3], ctol)
     np.testing.assert_allclose(out["omega"][[0, 3]], d["omega_final"][[0, 3]], atol=1.01e-9)
     # wann_main wrote only the top-left blocks: the rest of m_local is the raw overlaps
     nb = M.shape[2]
@@ -82,7 +89,7 @@ def test_disentangle_golden(name, tensor):
     mask[:W, :W] = False
     np.testing.assert_array_equal(out["m_after_wann"][:, :, mask], M[:, :, mask])
     r = O.wann_main(M0, U0, km, ctl)
-    np.testing.assert_allclose(out["centres"], r.centres, atol=1e-6)
+    assert np.all(np.abs(out["centres"] - np.asarray(r.centres)) <= 1e-6 + 3.0 * csens[None, :])
 
 
 @pytest.mark.parametrize("case", [

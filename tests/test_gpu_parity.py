@@ -265,10 +265,16 @@ def test_guiding_centres_golden(tensor):
     assert window >= 5
     _check_trajectory(out, r, upto=window)
     # 1000 iterations end short of convergence (conv_window 40): Omega and the centres
-    # are tight, the split of Omega among the WFs still drifts along the trajectory
+    # are tight, the split of Omega among the WFs still drifts along the trajectory.  The
+    # WF labels are not: past the stable window a rounding-level difference can leave
+    # equivalent WFs in another order, so each WF is compared with its partner (the
+    # nearest printed centre, one-to-one)
     fin = d["centres_final"]
-    np.testing.assert_allclose(out["centres"].T, fin[:, :3], atol=2e-6)
-    np.testing.assert_allclose(out["spreads"], fin[:, 3], atol=5e-6 if not tensor else 2e-5)
+    worst, pairs, _ = G.match_centres(out["centres"].T, fin[:, :3], d["real_lattice"])
+    assert worst < 2e-6 * np.sqrt(3.0), worst
+    stol = 5e-6 if not tensor else 2e-5
+    for i, j in pairs:
+        assert abs(out["spreads"][i] - fin[j, 3]) < stol, (i, j, out["spreads"][i], fin[j, 3])
     assert abs(out["omega"][3] - d["omega_final_total"][0]) < 1e-6
 
 

@@ -10,7 +10,7 @@ block, one for partners outside it -- and zero coefficients for j >= s:
     X_j = wb ln_j + (b.r_j)(1 - wb lambda) + wb lambda (b.c_j)      (both indices objective)
     Y_j = wb ln_j + wb (b.r_j)(1 - lambda) + wb lambda (b.c_j)      (partner not objective)
 
-k_omega_p1..p3 form Omega_IOD + Omega_nu from per-index sums over the objective WFs and
+k_omega_p1 and k_omega_p2 form Omega_IOD + Omega_nu from per-index sums over the objective WFs and
 scale Omega_D by (1 - lambda).  This file restates both in NumPy exactly as the kernels
 arrange them and compares with the oracle's direct restatement.
 """
@@ -60,7 +60,7 @@ def kernel_gradient(M, km, slwf):
 
 
 def kernel_spread(M, km, slwf):
-    """Omega terms as k_omega_p1..p3 arrange them (per-index chunk sums, then totals)."""
+    """Omega terms as k_omega_p1 and k_omega_p2 arrange them (per-index chunk sums, then totals)."""
     K, B, W, _ = M.shape
     wb, bk = km["wb"], km["bk"]
     diag = np.diagonal(M, axis1=2, axis2=3)

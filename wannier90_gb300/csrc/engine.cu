@@ -22,7 +22,6 @@ namespace w90g {
 __global__ void k_mdiag(const Problem* probs, WorkMap wm);
 __global__ void k_omega_p1(const Problem* probs, WorkMap wm, int slot);
 __global__ void k_omega_p2(const Problem* probs, WorkMap wm, int slot);
-__global__ void k_omega_p3(const Problem* probs, int slot);
 __global__ void k_grad(const Problem* probs, WorkMap wm);
 __global__ void k_ctrl_search(const Problem* probs);
 __global__ void k_exp_u(const Problem* probs, WorkMap wm, int which);
@@ -634,7 +633,6 @@ void Engine::launch_omega(cudaStream_t s, int slot) {
   const WorkMap wmc{d_offs_chunk_, np};
   k_omega_p1<<<n_chunk_, 256, 0, s>>>(dprobs_, wmc, slot);
   k_omega_p2<<<n_chunk_, 256, 0, s>>>(dprobs_, wmc, slot);
-  k_omega_p3<<<np, 256, 0, s>>>(dprobs_, slot);
 }
 
 // tensor path: keep the entry M and U, iterate on R = U0^H U starting from identity
@@ -728,7 +726,7 @@ int Engine::begin(std::string& err) {
   launch_omega(st, 2);
   k_log_init<<<np, 128, 0, st>>>(dprobs_);
   W90G_CHECK(cudaGetLastError());
-  launches_ += 5;
+  launches_ += 4;
   // capture one iteration into a graph (once per arena layout)
   if (!graph_exec_) {
     cudaStream_t cap;
@@ -749,7 +747,7 @@ int Engine::advance(int n, int* d_flag, std::string& err) {
   cudaStream_t st = stream();
   n = std::min(n, max_iter_ - launched_iters_);
   for (int i = 0; i < n; ++i) W90G_CHECK(cudaGraphLaunch(graph_exec_, st));
-  // grad, search, 2 x (exp, M update, 3 spread passes), step, end (+ 2 precond)
+  // grad, search, 2 x (exp, M update, 2 spread passes), step, end (+ 2 precond)
   launches_ += (10LL + 2 * (tensor_wp_ ? 2 : 1) + (pc_tiles_ ? 2 : 0) + (guide_w_ ? 1 : 0) + (n_ir_ ? 2 : 0)) *
                 std::max(n, 0);
   launched_iters_ += std::max(n, 0);

@@ -3,7 +3,7 @@
 // One iteration of wann_main (src/wannierise.F90:534-816) is the fixed launch sequence
 //   k_grad [-> k_precond(0) -> k_precond(1)] -> k_ctrl_search -> k_exp_u(0) -> k_m_update(0) -> spread(0) -> k_ctrl_step
 //   -> k_exp_u(1) -> k_m_update(1) -> spread(1) -> k_ctrl_end
-// where spread(slot) = k_omega_p1 -> k_omega_p2 -> k_omega_p3.
+// where spread(slot) = k_omega_p1 -> k_omega_p2.
 // All data-dependent decisions of the reference (CG reset, uphill reversal, parabolic
 // line search, convergence) are taken on the device by the k_ctrl_* kernels, so the
 // sequence never needs the host and can be replayed (or graph-captured) blindly:
@@ -112,6 +112,21 @@ __global__ void k_mdiag(const Problem* __restrict__ probs, WorkMap wm) {
 // ----------------------------------------------------------------------------
 constexpr int kOmegaChunk = 64;
 
+// Whether this CTA is the last of the problem's nchunk CTAs to finish (all threads get
+// the answer).  Every CTA makes its partials visible device-wide before it counts itself
+// in; the last one then reads all of them (through L2) and sums them in chunk order, so
+// the totals do not depend on which CTA comes last.
+__device__ __forceinline__ bool last_chunk_cta(unsigned* arrive, int nchunk) {
+  __shared__ int s_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = (atomicAdd(arrive, 1u) == (unsigned)(nchunk - 1));
+  __syncthreads();
+  const bool last = s_last != 0;
+  if (last) __threadfence();
+  return last;
+}
+
 __device__ __forceinline__ bool omega_skip(const CtrlState* st, int slot) {
   if (slot < 2) {
     if (st->done) return true;
@@ -125,7 +140,7 @@ __global__ void __launch_bounds__(256) k_omega_p1(const Problem* __restrict__ pr
   int ch;
   const int p = locate(wm, blockIdx.x, ch);
   const Problem& P = probs[p];
-  const CtrlState* st = P.st;
+  CtrlState* st = P.st;
   if (omega_skip(st, slot)) return;
   const int W = P.W, B = P.B;
   const int KB = P.K * B;
@@ -182,67 +197,79 @@ __global__ void __launch_bounds__(256) k_omega_p1(const Problem* __restrict__ pr
       out[4 * W] = iod;
       out[4 * W + 1] = nu;
     }
-    return;
-  }
-  const bool first = (slot == 2) && st->first_pass;
-  double od = 0.0, oi = 0.0;
-  for (int kb = kb0 + t; kb < kb1; kb += blockDim.x) {
-    const double w = P.wb[kb % B];
-    double o;
-    if (P.tensor && slot < 2) {
-      // tensor path: |M(k,b)|_F^2 is invariant under the unitary rotation, so the
-      // off-diagonal sum is |M0(k,b)|_F^2 minus the diagonal (src/wannierise.F90:2214-2258)
-      double sd = 0.0;
-      for (int m = 0; m < W; ++m) sd += P.diag_abs2[(size_t)kb * W + m];
-      o = P.frob0[kb] - sd;
-    } else {
-      o = P.offd[kb];
+  } else {
+    const bool first = (slot == 2) && st->first_pass;
+    double od = 0.0, oi = 0.0;
+    for (int kb = kb0 + t; kb < kb1; kb += blockDim.x) {
+      const double w = P.wb[kb % B];
+      double o;
+      if (P.tensor && slot < 2) {
+        // tensor path: |M(k,b)|_F^2 is invariant under the unitary rotation, so the
+        // off-diagonal sum is |M0(k,b)|_F^2 minus the diagonal (src/wannierise.F90:2214-2258)
+        double sd = 0.0;
+        for (int m = 0; m < W; ++m) sd += P.diag_abs2[(size_t)kb * W + m];
+        o = P.frob0[kb] - sd;
+      } else {
+        o = P.offd[kb];
+      }
+      od += w * o;
+      if (first) {
+        double sd = 0.0;
+        for (int m = 0; m < W; ++m) sd += P.diag_abs2[(size_t)kb * W + m];
+        oi += w * ((double)W - (o + sd));
+      }
     }
-    od += w * o;
-    if (first) {
-      double sd = 0.0;
-      for (int m = 0; m < W; ++m) sd += P.diag_abs2[(size_t)kb * W + m];
-      oi += w * ((double)W - (o + sd));
+    od = block_sum(od, red);
+    oi = block_sum(oi, red);
+    if (t == 0) {
+      out[4 * W] = od;
+      out[4 * W + 1] = oi;
     }
   }
-  od = block_sum(od, red);
-  oi = block_sum(oi, red);
-  if (t == 0) {
-    out[4 * W] = od;
-    out[4 * W + 1] = oi;
-  }
-}
-
-// rave(3,W) from the pass-1 partials, summed over chunks in index order
-__device__ void omega_rave(const Problem& P, double* s_rave) {
-  const int W = P.W;
+  if (!last_chunk_cta(&st->omega_arrive[0], P.nchunk)) return;
+  // ---- the last CTA: every chunk sum in chunk order on its own thread -- rave (3W) into
+  // the slot's centres, r^2 (W) into its spreads, the Omega_OD and Omega_I totals (2)
+  double* cen = P.centres + (size_t)slot * 4 * W;
   const int stride = 4 * W + 2;
-  for (int i = threadIdx.x; i < 3 * W; i += blockDim.x) {
+  __shared__ double s_rave[3 * 256];
+  __shared__ double s_q[256];
+  for (int i = t; i < 4 * W + 2; i += blockDim.x) {
     double sacc = 0.0;
-    for (int c = 0; c < P.nchunk; ++c) sacc += P.opart1[(size_t)c * stride + i];
-    s_rave[i] = -sacc / (double)P.K;
+    for (int c = 0; c < P.nchunk; ++c) sacc += __ldcg(P.opart1 + (size_t)c * stride + i);
+    if (i < 3 * W) s_rave[i] = -sacc / (double)P.K;
+    else if (i < 4 * W) s_q[i - 3 * W] = sacc;
+    else st->omega_tot[i - 4 * W] = sacc;
   }
   __syncthreads();
+  for (int i = t; i < W; i += blockDim.x) {
+    const double x0 = s_rave[i], x1 = s_rave[W + i], x2 = s_rave[2 * W + i];
+    cen[i] = x0;
+    cen[W + i] = x1;
+    cen[2 * W + i] = x2;
+    cen[3 * W + i] = s_q[i] / (double)P.K - (x0 * x0 + x1 * x1 + x2 * x2);
+  }
+  if (t == 0) st->omega_arrive[0] = 0u;
 }
 
 __global__ void __launch_bounds__(256) k_omega_p2(const Problem* __restrict__ probs, WorkMap wm, int slot) {
   __shared__ double red[256];
-  __shared__ double s_rave[3 * 256];
   int ch;
   const int p = locate(wm, blockIdx.x, ch);
   const Problem& P = probs[p];
-  if (omega_skip(P.st, slot)) return;
-  omega_rave(P, s_rave);
-  const int W = P.W, B = P.B;
-  const int KB = P.K * B;
+  CtrlState* st = P.st;
+  if (omega_skip(st, slot)) return;
+  const int W = P.W, B = P.B, K = P.K;
+  const int KB = K * B;
   const int kb0 = ch * kOmegaChunk, kb1 = min(KB, kb0 + kOmegaChunk);
   const int t = threadIdx.x;
   const int nsub = blockDim.x / W;
   const int n = t % W, sub = t / W;
+  // rave from pass 1's last CTA (the slot's centres)
+  const double* cen = P.centres + (size_t)slot * 4 * W;
   double dd = 0.0;
   // selective localisation: Omega_D over the objective WFs only
   if (sub < nsub && (P.slwf_num == 0 || n < P.slwf_num)) {
-    const double x0 = s_rave[n], x1 = s_rave[W + n], x2 = s_rave[2 * W + n];
+    const double x0 = cen[n], x1 = cen[W + n], x2 = cen[2 * W + n];
     for (int kb = kb0 + sub; kb < kb1; kb += nsub) {
       const double w = P.wb[kb % B];
       const double* bv = P.bk + (size_t)kb * 3;
@@ -252,69 +279,12 @@ __global__ void __launch_bounds__(256) k_omega_p2(const Problem* __restrict__ pr
   }
   dd = block_sum(dd, red);
   if (t == 0) P.opart2[ch] = dd;
-}
-
-__global__ void __launch_bounds__(256) k_omega_p3(const Problem* __restrict__ probs, int slot) {
-  __shared__ double red[256];
-  __shared__ double s_rave[3 * 256];
-  const Problem& P = probs[blockIdx.x];
-  CtrlState* st = P.st;
-  if (omega_skip(st, slot)) return;
-  const int W = P.W, K = P.K;
-  const int stride = 4 * W + 2;
-  const int t = threadIdx.x;
-  double* cen = P.centres + (size_t)slot * 4 * W;
-  // Omega_OD, Omega_I and Omega_D totals over the chunks, on the last three threads
-  __shared__ double s_sum[3];
-  const int u = t - ((int)blockDim.x - 3);
-  auto totals = [&]() {
-    if (u < 0) return;
-    double acc = 0.0;
-    if (u == 2)
-      for (int c = 0; c < P.nchunk; ++c) acc += P.opart2[c];
-    else
-      for (int c = 0; c < P.nchunk; ++c) acc += P.opart1[(size_t)c * stride + 4 * W + u];
-    s_sum[u] = acc;
-  };
-  if (4 * W + 3 <= (int)blockDim.x) {
-    // every chunk sum on its own thread, all at once: rave (3W), r^2 (W), and the three
-    // totals on the last three threads below (each in chunk order)
-    __shared__ double s_q[256];
-    if (t < 3 * W) {
-      double sacc = 0.0;
-      for (int c = 0; c < P.nchunk; ++c) sacc += P.opart1[(size_t)c * stride + t];
-      s_rave[t] = -sacc / (double)P.K;
-    } else if (t < 4 * W) {
-      double q = 0.0;
-      for (int c = 0; c < P.nchunk; ++c) q += P.opart1[(size_t)c * stride + t];
-      s_q[t - 3 * W] = q;
-    } else {
-      totals();
-    }
-    __syncthreads();
-    if (t < W) {
-      const double x0 = s_rave[t], x1 = s_rave[W + t], x2 = s_rave[2 * W + t];
-      cen[t] = x0;
-      cen[W + t] = x1;
-      cen[2 * W + t] = x2;
-      cen[3 * W + t] = s_q[t] / (double)K - (x0 * x0 + x1 * x1 + x2 * x2);
-    }
-  } else {
-    omega_rave(P, s_rave);
-    for (int i = t; i < W; i += blockDim.x) {
-      double q = 0.0;
-      for (int c = 0; c < P.nchunk; ++c) q += P.opart1[(size_t)c * stride + 3 * W + i];
-      const double x0 = s_rave[i], x1 = s_rave[W + i], x2 = s_rave[2 * W + i];
-      cen[i] = x0;
-      cen[W + i] = x1;
-      cen[2 * W + i] = x2;
-      cen[3 * W + i] = q / (double)K - (x0 * x0 + x1 * x1 + x2 * x2);
-    }
-    totals();
-  }
-  __syncthreads();
+  if (!last_chunk_cta(&st->omega_arrive[1], P.nchunk)) return;
+  // ---- the last CTA: the Omega_D total in chunk order, then the spread of the slot
   if (t == 0) {
-    const double od = s_sum[0], oi = s_sum[1], dd = s_sum[2];
+    double acc = 0.0;
+    for (int c = 0; c < P.nchunk; ++c) acc += __ldcg(P.opart2 + c);
+    const double od = st->omega_tot[0], oi = st->omega_tot[1], dsum = acc;
     Spread sp;
     if (P.slwf_num > 0) {
       // Omega_tot = Omega_IOD + Omega_D + Omega_nu (Omega_I is never formed); om_od
@@ -322,7 +292,7 @@ __global__ void __launch_bounds__(256) k_omega_p3(const Problem* __restrict__ pr
       const double iod = od / (double)K;
       sp.om_nu = oi / (double)K + P.slwf_nu0;
       sp.om_i = 0.0;
-      sp.om_d = (1.0 - P.slwf_lambda) * dd / (double)K;
+      sp.om_d = (1.0 - P.slwf_lambda) * dsum / (double)K;
       sp.om_od = iod + sp.om_nu;
       sp.om_tot = iod + sp.om_d + sp.om_nu;
     } else {
@@ -331,7 +301,7 @@ __global__ void __launch_bounds__(256) k_omega_p3(const Problem* __restrict__ pr
         st->first_pass = 0;
       }
       sp.om_i = st->om_invariant;
-      sp.om_d = dd / (double)K;
+      sp.om_d = dsum / (double)K;
       sp.om_od = od / (double)K;
       sp.om_tot = sp.om_i + sp.om_d + sp.om_od;
       sp.om_nu = 0.0;
@@ -342,8 +312,8 @@ __global__ void __launch_bounds__(256) k_omega_p3(const Problem* __restrict__ pr
       st->error = 1;
       st->done = 1;
     }
+    st->omega_arrive[1] = 0u;
   }
-  (void)red;
 }
 
 // ----------------------------------------------------------------------------

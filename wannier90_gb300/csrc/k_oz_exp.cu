@@ -163,7 +163,8 @@ __device__ __forceinline__ void rec_clear(const Rec& r, int n) {
     for (int i = threadIdx.x; i < 2 * n; i += blockDim.x) (i < n ? r.row : r.col)[i % n] = 0u;
 }
 
-// Adds the key of v (at row i, column j) to the record (shared-memory maxima).
+// Adds the key of v (at row i, column j) to the record (shared-memory maxima).  (A warp
+// maximum before one atomic per distinct index measured slower than these atomics.)
 __device__ __forceinline__ void rec_add(const Rec& r, int i, int j, double2 v) {
   if (r.row != nullptr) {
     const unsigned key = scale_key(v.x, v.y);
@@ -638,7 +639,8 @@ __device__ bool oz_cmm2(OzCtx& cx, double2* C, const double2* A, const unsigned*
             const double2 m = cmk(ep.sym * v.x, -ep.sym * v.y);
             ep.out[(size_t)rr * W + c] = m;
             rec_add(ep.rec, rr, c, v);
-            rec_add(ep.rec, c, rr, m);
+            // (a record whose rows and columns share one array already holds the mirror)
+            if (ep.rec.row != ep.rec.col) rec_add(ep.rec, c, rr, m);
           }
         }
       }
@@ -709,15 +711,73 @@ __device__ __forceinline__ double scale_pow2(double x, int j, double sc) {
   return x * sc;
 }
 
-// The number of halvings that bring v to theta or below (at most 60): the smallest j >= 0
-// with v 2^-j <= theta.  Halving is exact, so this is the count of the loop
-// "while (v > theta && j < 60) { v *= 0.5; ++j; }", found from the exponents in a few steps.
+// The number of halvings that bring v >= 0 to theta (a positive normal) or below, at most
+// 60: the count of the loop "while (v > theta && j < 60) { v *= 0.5; ++j; }" (halving is
+// exact), from the bits with integer ops only.  Non-negative doubles order like their bit
+// patterns; with v = mv 2^ev and theta = mt 2^et (mantissas in [1, 2)), v 2^-j <= theta
+// first holds at j = ev - et, or one later where mv > mt.  (0 for nan, where v > theta is
+// false; 60 for inf.)
 __device__ __forceinline__ int halvings(double v, double theta) {
-  if (!(v > theta)) return 0;
-  int j = ilogb(v) - ilogb(theta) - 1;
-  j = j < 0 ? 0 : (j > 60 ? 60 : j);
-  while (j < 60 && ldexp(v, -j) > theta) ++j;
-  return j;
+  constexpr long long kMant = 0x000FFFFFFFFFFFFFLL;
+  const long long vb = __double_as_longlong(v), tb = __double_as_longlong(theta);
+  if (vb <= tb) return 0;
+  if ((vb >> 52) == 0x7FF && (vb & kMant) != 0) return 0;
+  const int j = (int)(vb >> 52) - (int)(tb >> 52) + ((vb & kMant) > (tb & kMant) ? 1 : 0);
+  return j > 60 ? 60 : j;
+}
+
+// Degree m, block size pw and squarings js of exp(X) from its 1-norm, with the cost in
+// products (powers plus Horner steps, plus js): the FP64 path's table (k_exp_u), the
+// cheapest candidate after the halvings that bring the norm under its theta.
+struct ExpPlan {
+  int m, pw, js, cost;
+};
+__device__ const int kPlanM[5] = {4, 6, 8, 12, 16};
+__device__ const int kPlanP[5] = {4, 3, 4, 4, 4};
+__device__ const double kPlanTheta[5] = {1.6e-3, 1.68e-2, 6.6e-2, 0.32, 0.78};
+__device__ const int kPlanCost[5] = {3, 3, 4, 5, 6};
+
+__device__ __noinline__ ExpPlan exp_plan(double nrm) {
+  ExpPlan pl{16, 4, 0, 1 << 30};
+  for (int c = 0; c < 5; ++c) {
+    const int j = halvings(nrm, kPlanTheta[c]);
+    const int cost = kPlanCost[c] + j;
+    if (cost < pl.cost) pl = ExpPlan{kPlanM[c], kPlanP[c], j, cost};
+  }
+  return pl;
+}
+
+// Whether every norm within a relative 2^-14 of nrm gets the same halvings for every
+// candidate -- nrm finite and at least that far from each candidate's boundaries theta
+// 2^(j-1) and theta 2^j -- so that an estimate of the norm to that accuracy picks the plan
+// the exact norm picks.  (nrm < x 2^j compares the bits of nrm with those of x plus j in
+// the exponent field, x 2^j being a normal number here.)
+__device__ __noinline__ bool exp_plan_stable(double nrm) {
+  if (!(nrm < 1e300)) return false;
+  const long long nb = __double_as_longlong(nrm);
+  for (int c = 0; c < 5; ++c) {
+    const double th = kPlanTheta[c];
+    const int j = halvings(nrm, th);
+    const long long lo = __double_as_longlong(th * (1.0 - 0x1p-14)), hi = __double_as_longlong(th * (1.0 + 0x1p-14));
+    if (j < 60 && !(nb < lo + ((long long)j << 52))) return false;
+    if (j > 0 && !(nb > hi + ((long long)(j - 1) << 52))) return false;
+  }
+  return true;
+}
+
+// |re + i im| to a relative 2^-20 with no FP64 instruction: each part truncated to FP32
+// through its bits (0 below 2^-60, +inf above 2^60 or for inf / nan), then FP32 fma and
+// sqrt.  A column sum of these (<= 128 terms, FP32) is within 2^-16 of the FP64 one.
+__device__ __forceinline__ float abs_est(double2 v) {
+  auto f32 = [](double x) -> float {
+    const unsigned long long b = abs_bits(x);
+    const int e = (int)(b >> 52) - 1023;
+    if (e < -60) return 0.0f;
+    if (e > 60) return __int_as_float(0x7f800000);
+    return __uint_as_float(((unsigned)(e + 127) << 23) | (unsigned)((b >> 29) & 0x7FFFFFu));
+  };
+  const float a = f32(v.x), b = f32(v.y);
+  return sqrtf(fmaf(a, a, b * b));
 }
 
 __device__ const double kOzInvFact[17] = {
@@ -768,67 +828,129 @@ __global__ void __launch_bounds__(256, 2) k_oz_exp(const Problem* __restrict__ p
           *T = mats + 5 * WW;
   double2* Dk = P.D + (size_t)k * WW;
   const double s = (which == 0) ? st->s_trial : st->s_second;
-  if (which == 0 && P.sym_nir == 0) {
-    // (in the symmetry-adapted mode k_sym_dir has formed D already)
-    const double cg = st->coefG, cd = st->coefD;
-    const double2* Gk = (st->use_gp ? P.pc_gp : P.G) + (size_t)k * WW;
-    #pragma unroll 4
-    for (int e = tid; e < WW; e += blockDim.x) {
-      const double2 d = cadd(cscale(Gk[e], cg), cscale(Dk[e], cd));
+  // scale records of X, Y2, Y3, Y4, R, T (see Rec).  The powers are exactly Hermitian or
+  // anti-Hermitian (|re| and |im| of element (i, j) are those of (j, i)), so row i and
+  // column i of their records are the same maximum: one array serves both.
+  Rec rX{s_key[0][0], s_key[0][1]}, rY2{s_key[1][0], s_key[1][0]}, rY3{s_key[2][0], s_key[2][0]},
+      rY4{s_key[3][0], s_key[3][0]}, rR{s_key[4][0], s_key[4][1]}, rT{s_key[5][0], s_key[5][1]};
+  rec_clear(rX, WP);
+  // ---- X = s D (the trial step first forms D = coefG G + coefD D_prev; in the
+  // symmetry-adapted mode k_sym_dir has formed D already) and estimates of the moduli
+  // |X_ij| into shared scratch.  num_wann <= 32: X stays in registers (element tid + 256 i
+  // in slot i) until it is scaled below.
+  constexpr bool XREG = WP <= 32;
+  constexpr int NE = XREG ? (WP * WP + 255) / 256 : 1;
+  double2 xr[NE];
+  // the digit region is free before the first product: |X_ij| estimates, then (where the
+  // exact norm is needed, once the estimates are summed) the exact moduli in its place
+  float* absf = (float*)base;
+  double* absx = (double*)base;
+  const bool form_d = (which == 0 && P.sym_nir == 0);
+  const double cg = st->coefG, cd = st->coefD;
+  const double2* Gk = form_d ? (st->use_gp ? P.pc_gp : P.G) + (size_t)k * WW : nullptr;
+  // (each product and the sum rounded on its own, as the oracle forms D: no contraction
+  // into an FMA, whose choice of product would follow the code's shape)
+  auto form_x = [&](int e) -> double2 {
+    double2 d = Dk[e];
+    if (form_d) {
+      const double2 g = Gk[e];
+      d = cmk(__dadd_rn(__dmul_rn(g.x, cg), __dmul_rn(d.x, cd)), __dadd_rn(__dmul_rn(g.y, cg), __dmul_rn(d.y, cd)));
       Dk[e] = d;
-      X[e] = cscale(d, s);
+    }
+    const double2 x = cscale(d, s);
+    absf[e] = abs_est(x);
+    return x;
+  };
+  if (XREG) {
+#pragma unroll
+    for (int i = 0; i < NE; ++i) {
+      const int e = tid + 256 * i;
+      if (e < WW) xr[i] = form_x(e);
     }
   } else {
-    #pragma unroll 4
-    for (int e = tid; e < WW; e += blockDim.x) X[e] = cscale(Dk[e], s);
+#pragma unroll 4
+    for (int e = tid; e < WW; e += 256) X[e] = form_x(e);
   }
   __syncthreads();
   OzCtx cx{base, base + E::SB_OFFSET, tmem_slot, smem_u32(&mbar), 0u, s_rowexp, s_colexp, &s_bad};
 
-  // ---- degree / squarings from the 1-norm (the FP64 path's table; costs in products:
-  // powers X^2, X^3 (, X^4) plus the Horner steps)
-  // 1-norm: the moduli |X_ij| by all threads into shared scratch (the digit region is
-  // free before the first product), then each column summed in row order as before
-  double* absx = (double*)base;
-#pragma unroll 4
-  for (int e = tid; e < WW; e += blockDim.x) absx[e] = sqrt(cabs2(X[e]));
-  __syncthreads();
-  double colmax = 0.0;
-  for (int j = tid; j < W; j += blockDim.x) {
-    double a = 0.0;
-    for (int i = 0; i < W; ++i) a += absx[(size_t)j * W + i];
-    colmax = fmax(colmax, a);
-  }
-  __syncthreads();
-  const double nrm = cta_max(colmax, red);
-  const int cand_m[5] = {4, 6, 8, 12, 16};
-  const int cand_p[5] = {4, 3, 4, 4, 4};
-  const double cand_theta[5] = {1.6e-3, 1.68e-2, 6.6e-2, 0.32, 0.78};
-  const double cand_cost[5] = {3.0, 3.0, 4.0, 5.0, 6.0};
-  int m = 16, pw = 4, js = 0;
-  double best = 1e300;
-  for (int c = 0; c < 5; ++c) {
-    const int j = halvings(nrm, cand_theta[c]);
-    const double cost = cand_cost[c] + j;
-    if (cost < best) {
-      best = cost;
-      m = cand_m[c];
-      pw = cand_p[c];
-      js = j;
+  // ---- degree / squarings from the 1-norm (the FP64 path's table and choice, exp_plan).
+  // The plan depends on the norm only through which side of each theta 2^j it lies, so
+  // the FP32 estimate decides wherever it is clearly inside one interval
+  // (exp_plan_stable); else the exact FP64 norm is formed -- moduli, then each column
+  // summed in row order -- as the FP64 path forms it.  One thread plans, all read it.
+  __shared__ float s_wmax[8];
+  __shared__ int s_plan[5];
+  {
+    float colmax = 0.0f;
+    for (int j = tid; j < W; j += 256) {
+      float a = 0.0f;
+      for (int i = 0; i < W; ++i) a += absf[(size_t)j * W + i];
+      colmax = fmaxf(colmax, a);
     }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) colmax = fmaxf(colmax, __shfl_xor_sync(0xffffffffu, colmax, o));
+    if ((tid & 31) == 0) s_wmax[warp] = colmax;
   }
-  // scale records of X, Y2, Y3, Y4, R, T (see Rec)
-  Rec rX{s_key[0][0], s_key[0][1]}, rY2{s_key[1][0], s_key[1][1]}, rY3{s_key[2][0], s_key[2][1]},
-      rY4{s_key[3][0], s_key[3][1]}, rR{s_key[4][0], s_key[4][1]}, rT{s_key[5][0], s_key[5][1]};
-  const double sc = ldexp(1.0, -js);
-  rec_clear(rX, WP);
   __syncthreads();
-  #pragma unroll 4
-  for (int e = tid; e < WW; e += blockDim.x) {
-    const double2 x = X[e];
+  if (tid == 0) {
+    float nf = 0.0f;
+    for (int w = 0; w < 8; ++w) nf = fmaxf(nf, s_wmax[w]);
+    const bool stable = exp_plan_stable((double)nf);
+    const ExpPlan pl = exp_plan((double)nf);
+    s_plan[0] = pl.m;
+    s_plan[1] = pl.pw;
+    s_plan[2] = pl.js;
+    s_plan[3] = stable ? 0 : 1;
+    s_plan[4] = pl.cost;
+  }
+  __syncthreads();
+  if (s_plan[3]) {
+    auto exact_abs = [&](int e, double2 x) { absx[e] = sqrt(cabs2(x)); };
+    if (XREG) {
+#pragma unroll
+      for (int i = 0; i < NE; ++i) {
+        const int e = tid + 256 * i;
+        if (e < WW) exact_abs(e, xr[i]);
+      }
+    } else {
+      for (int e = tid; e < WW; e += 256) exact_abs(e, X[e]);
+    }
+    __syncthreads();
+    double colmax = 0.0;
+    for (int j = tid; j < W; j += 256) {
+      double a = 0.0;
+      for (int i = 0; i < W; ++i) a += absx[(size_t)j * W + i];
+      colmax = fmax(colmax, a);
+    }
+    __syncthreads();
+    const double nrm = cta_max(colmax, red);
+    if (tid == 0) {
+      const ExpPlan pl = exp_plan(nrm);
+      s_plan[0] = pl.m;
+      s_plan[1] = pl.pw;
+      s_plan[2] = pl.js;
+      s_plan[4] = pl.cost;
+    }
+    __syncthreads();
+  }
+  const int m = s_plan[0], pw = s_plan[1], js = s_plan[2];
+  const double best = (double)s_plan[4];
+  const double sc = ldexp(1.0, -js);
+  auto scale_x = [&](int e, double2 x) {
     const double2 v = make_double2(scale_pow2(x.x, js, sc), scale_pow2(x.y, js, sc));
     X[e] = v;
     rec_add(rX, e % W, e / W, v);
+  };
+  if (XREG) {
+#pragma unroll
+    for (int i = 0; i < NE; ++i) {
+      const int e = tid + 256 * i;
+      if (e < WW) scale_x(e, xr[i]);
+    }
+  } else {
+#pragma unroll 4
+    for (int e = tid; e < WW; e += 256) scale_x(e, X[e]);
   }
   __syncthreads();
   const NoAdd none;

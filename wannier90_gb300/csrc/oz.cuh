@@ -242,7 +242,9 @@ __device__ __forceinline__ double int64_scaled_to_double(long long S, int sc) {
 
 // sum_d D_d 2^(8(6-d)) * 2^sc for the 7 diagonal accumulators of the 8-bit-digit scheme
 // (|D_d| < 2^24): the top four and the bottom three diagonals are combined exactly in
-// int64 (< 2^49 and < 2^41), converted exactly, and added once in FP64 (one rounding)
+// int64 (< 2^49 and < 2^41) and their exact sum (< 2^73, int128) rounded once to FP64 with
+// integer ops -- the bits of converting both parts exactly and adding them in FP64, which
+// is what happens where the result could leave FP64's normal range
 __device__ __forceinline__ double recombine7x8(const uint32_t* dd, int stride, int sc) {
   long long hi = float_to_int_exact24(__uint_as_float(dd[0]));
 #pragma unroll
@@ -250,6 +252,7 @@ __device__ __forceinline__ double recombine7x8(const uint32_t* dd, int stride, i
   long long lo = float_to_int_exact24(__uint_as_float(dd[4 * stride]));
 #pragma unroll
   for (int d = 5; d < 7; ++d) lo = (lo << 8) + float_to_int_exact24(__uint_as_float(dd[d * stride]));
+  if (sc > -900 && sc < 900) return int128_scaled_to_double(((__int128)hi << 24) + (__int128)lo, sc);
   return int64_scaled_to_double(hi, sc + 24) + int64_scaled_to_double(lo, sc);
 }
 

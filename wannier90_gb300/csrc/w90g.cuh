@@ -94,6 +94,11 @@ struct CtrlState {
   Spread wann, old, slot[2];   // slot[0] = trial spread, slot[1] = optimal-step spread
   double history[kMaxConvWindow];
   double exp_products;   // W^3 complex products spent in exp(s D) and U dU (work counter)
+  // spread passes: CTAs of k_omega_p1 / k_omega_p2 that have finished this launch (the
+  // last one reduces the chunk partials and sets the count back to 0), and the Omega_OD,
+  // Omega_I chunk totals that pass 1's last CTA hands to pass 2's
+  unsigned omega_arrive[2];
+  double omega_tot[2];
 };
 
 // wann_control_type subset used on device (src/wannier90_types.F90:170-192)
