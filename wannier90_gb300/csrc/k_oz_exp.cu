@@ -1,6 +1,7 @@
 // Tensor-core rotation step: dU(k) = exp(s D(k)) and U(k) <- U(k) dU(k)
 // (internal_new_u_and_m, src/wannierise.F90:1655-1733) with every W x W complex
-// product on the tcgen05 tensor cores through exact BF16 slicing (see k_tensor.cu).
+// product on the tcgen05 tensor cores through exact slicing into BF16 / FP16 digits
+// (see k_tensor.cu).
 //
 // The matrix function is the FP64 path's (k_exp_u in k_fp64.cu): scaling and squaring
 // of a Taylor polynomial evaluated by Paterson-Stockmeyer, degree and squarings chosen
@@ -10,7 +11,7 @@
 // double any error) needs 56-bit operands: a product is accurate to ~2^-56 of
 // (row scale x column scale), below FP64 GEMM roundoff.  Two product forms:
 //   num_wann <= 64: [C_r; C_i] = [[A_r, -A_i], [A_i, A_r]] [B_r; B_i], 7 signed 8-bit
-//     digits, 28 digit pairs (oz_cmm2);
+//     digits (FP16 operands), 28 digit pairs (oz_cmm2);
 //   num_wann = 65..128: [C_r C_i] = [A_r A_i] [[B_r, B_i], [-B_i, B_r]], 8 signed
 //     7-bit digits, 36 digit pairs (oz_cmm; K = 256 keeps 8-bit digits from being exact).
 //
@@ -399,7 +400,8 @@ __device__ bool oz_cmm(OzCtx& cx, double2* C, const double2* A, const unsigned* 
 //     [C_r; C_i] = [[A_r, -A_i], [A_i, A_r]] [B_r; B_i]
 // i.e. 2W accumulator rows (real parts in rows 0..WP-1, imaginary parts in rows
 // WP..2WP-1), N = W columns, K = 2W; operands split into 7 signed 8-bit digits (56 bits;
-// exact BF16 values) and the 28 digit pairs with t+u <= 6 kept.  Against the first
+// exact FP16 values, built two at a time by a packed FP16 subtraction) and the 28 digit
+// pairs with t+u <= 6 kept.  Against the first
 // form this halves N and TMEM, drops 36 pairs to 28 at the same 56-bit precision, and
 // (FP64 matrices in L2 instead of shared memory) lets two CTAs share an SM.  Exactness:
 // a diagonal holds at most 7 pairs of products <= 2^14 over K <= 128 terms, < 2^24.
@@ -445,27 +447,42 @@ __device__ __forceinline__ void load_run8(double (&v)[8], const double2* base, s
   }
 }
 
-// The seven 8-bit digit planes of the 8 values scaled by 2^(55 - ex), as packed BF16
-// pairs: w[t][i / 2] holds digit t of values i (low half) and i + 1 -- the digits and BF16
-// bits of slicing the values one at a time (digits7x8, int_to_bf16).
-__device__ __forceinline__ void slice_run8(uint32_t (&w)[7][4], const double (&v)[8], int ex) {
+// The seven 8-bit digit planes of the 8 values scaled by 2^(55 - ex), as packed FP16
+// pairs: w[t][i / 2] holds digit t of values i (low half) and i + 1 -- the digits of
+// digits7x8, without its serial recoding.  With C = 128 (1 + 2^8 + ... + 2^40), byte t' of
+// N + C is digit 6 - t' plus 128 (adding 128 at every lower byte position turns the
+// centred digits into the plain bytes of N + C: x_6 = sext8(N mod 2^8) = byte0(N + 128) -
+// 128, and (N - x_6) / 2^8 = (N + 128) >> 8, so the next step repeats on N + 128 shifted),
+// and the top digit is (N + C) >> 48 (arithmetic), so b = digit + 128 lies in [0, 256].
+// With 0x6400 above it, b is the FP16 number 1024 + b: one byte permute, one mask and one
+// packed subtraction of 1152 give two digits.  Exact: FP16 holds the integers to 2048, and
+// the difference of two of them is rounded to itself.
+__device__ __forceinline__ uint32_t f16x2_minus1152(uint32_t x) {
+  uint32_t r;
+  asm("sub.rn.f16x2 %0, %1, %2;" : "=r"(r) : "r"(x), "r"(0x64806480u));
+  return r;
+}
+__device__ __forceinline__ void slice_run8_h(uint32_t (&w)[7][4], const double (&v)[8], int ex) {
 #pragma unroll
   for (int i = 0; i < 8; i += 2) {
-    float fa[7], fb[7];
-    digits7x8_f(scaled_int55(v[i], ex), fa);
-    digits7x8_f(scaled_int55(v[i + 1], ex), fb);
+    const long long ma = scaled_int55(v[i], ex) + 0x808080808080LL;
+    const long long mb = scaled_int55(v[i + 1], ex) + 0x808080808080LL;
+    const uint32_t la = (uint32_t)ma, lb = (uint32_t)mb;
+    const uint32_t ha = (uint32_t)((unsigned long long)ma >> 32), hb = (uint32_t)((unsigned long long)mb >> 32);
 #pragma unroll
-    for (int t = 0; t < 7; ++t) w[t][i >> 1] = pack_bf16x2(fa[t], fb[t]);
+    for (int t = 0; t < 6; ++t) {
+      const uint32_t bt = (uint32_t)(t & 3);
+      const uint32_t sel = bt | (bt << 4) | ((4u + bt) << 8) | ((4u + bt) << 12);
+      const uint32_t p = __byte_perm(t < 4 ? la : ha, t < 4 ? lb : hb, sel);
+      w[6 - t][i >> 1] = f16x2_minus1152((p & 0x00FF00FFu) | 0x64006400u);
+    }
+    const uint32_t ta = (uint32_t)((int)(ma >> 48) + 128), tb = (uint32_t)((int)(mb >> 48) + 128);
+    w[0][i >> 1] = f16x2_minus1152(ta | (tb << 16) | 0x64006400u);
   }
 }
 
-// the BF16 bits of -x for both halves of a packed pair of exact small integers: the sign
-// flipped where the value is not zero (int_to_bf16(-0) is +0, as int_to_bf16(0))
-__device__ __forceinline__ uint32_t bf16x2_neg(uint32_t w) {
-  const uint32_t lo = (w & 0x7FFFu) ? 0x8000u : 0u;
-  const uint32_t hi = (w & 0x7FFF0000u) ? 0x80000000u : 0u;
-  return w ^ (lo | hi);
-}
+// -x for both halves of a packed FP16 pair (a zero becomes -0, the same in every product)
+__device__ __forceinline__ uint32_t f16x2_neg(uint32_t w) { return w ^ 0x80008000u; }
 
 // C = A B, then the Epi.  num_wann <= 32 (staged accumulators): the epilogue applies the
 // Epi itself and writes ep.out only (C unused; ep.out may alias B, whose digits are in
@@ -498,7 +515,7 @@ __device__ bool oz_cmm2(OzCtx& cx, double2* C, const double2* A, const unsigned*
         if (it < NIB) load_run8(vb, B + (size_t)c * W, (size_t)1, kc * CW + lgb * 8, W, c < W, pb);
         uint32_t w[kS2][4];
         if (it < NIA) {
-          slice_run8(w, va, cx.rowexp[r]);
+          slice_run8_h(w, va, cx.rowexp[r]);
           const int kq = lga * 8;
           const uint32_t o1 = pa == 0 ? kmaj_off(r, kq, KC) : kmaj_off(WP + r, kq, KC);
           const uint32_t o2 = pa == 0 ? kmaj_off(WP + r, CW + kq, KC) : kmaj_off(r, CW + kq, KC);
@@ -507,12 +524,12 @@ __device__ bool oz_cmm2(OzCtx& cx, double2* C, const double2* A, const unsigned*
             unsigned char* sa = cx.sA + (size_t)t * E::A_SLICE;
             *(uint4*)(sa + o1) = make_uint4(w[t][0], w[t][1], w[t][2], w[t][3]);
             *(uint4*)(sa + o2) = pa == 0 ? make_uint4(w[t][0], w[t][1], w[t][2], w[t][3])
-                                         : make_uint4(bf16x2_neg(w[t][0]), bf16x2_neg(w[t][1]),
-                                                      bf16x2_neg(w[t][2]), bf16x2_neg(w[t][3]));
+                                         : make_uint4(f16x2_neg(w[t][0]), f16x2_neg(w[t][1]),
+                                                      f16x2_neg(w[t][2]), f16x2_neg(w[t][3]));
           }
         }
         if (it < NIB) {
-          slice_run8(w, vb, cx.colexp[c < WP ? c : 0]);
+          slice_run8_h(w, vb, cx.colexp[c < WP ? c : 0]);
           const uint32_t o = kmaj_off(c, pb * CW + lgb * 8, KC);
 #pragma unroll
           for (int t = 0; t < kS2; ++t)
@@ -548,7 +565,7 @@ __device__ bool oz_cmm2(OzCtx& cx, double2* C, const double2* A, const unsigned*
                 "{\n\t.reg .pred p;\n\t"
                 "setp.ne.b32 p, %4, 0;\n\t"
                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
-                :: "r"(dtm), "l"(ad), "l"(bd), "r"(idesc_bf16(n * N)), "r"(acc)
+                :: "r"(dtm), "l"(ad), "l"(bd), "r"(idesc_f16(n * N)), "r"(acc)
                 : "memory");
           }
         }
@@ -767,7 +784,8 @@ __device__ __noinline__ bool exp_plan_stable(double nrm) {
 
 // |re + i im| to a relative 2^-20 with no FP64 instruction: each part truncated to FP32
 // through its bits (0 below 2^-60, +inf above 2^60 or for inf / nan), then FP32 fma and
-// sqrt.  A column sum of these (<= 128 terms, FP32) is within 2^-16 of the FP64 one.
+// q rsqrt(q) (rsqrtf: 2 ulp).  A column sum of these (<= 128 terms, FP32) is within 2^-16
+// of the FP64 one.  (An infinite estimate gives a nan norm, which is never stable.)
 __device__ __forceinline__ float abs_est(double2 v) {
   auto f32 = [](double x) -> float {
     const unsigned long long b = abs_bits(x);
@@ -777,7 +795,8 @@ __device__ __forceinline__ float abs_est(double2 v) {
     return __uint_as_float(((unsigned)(e + 127) << 23) | (unsigned)((b >> 29) & 0x7FFFFFu));
   };
   const float a = f32(v.x), b = f32(v.y);
-  return sqrtf(fmaf(a, a, b * b));
+  const float q = fmaf(a, a, b * b);
+  return q > 0.0f ? q * rsqrtf(q) : 0.0f;
 }
 
 __device__ const double kOzInvFact[17] = {
@@ -935,7 +954,6 @@ __global__ void __launch_bounds__(256, 2) k_oz_exp(const Problem* __restrict__ p
     __syncthreads();
   }
   const int m = s_plan[0], pw = s_plan[1], js = s_plan[2];
-  const double best = (double)s_plan[4];
   const double sc = ldexp(1.0, -js);
   auto scale_x = [&](int e, double2 x) {
     const double2 v = make_double2(scale_pow2(x.x, js, sc), scale_pow2(x.y, js, sc));
@@ -1028,7 +1046,7 @@ __global__ void __launch_bounds__(256, 2) k_oz_exp(const Problem* __restrict__ p
   double2* Unew = P.U[cur ^ 1] + (size_t)k * WW;
   if (ok) ok = E::mm(cx, Unew, P.U[cur] + (size_t)k * WW, nullptr, a, ra.col, W, Epi{Unew, 0, Rec{nullptr, nullptr}},
                      none);
-  if (tid == 0) atomicAdd(&st->exp_products, best + 1.0);
+  if (tid == 0) atomicAdd(&st->exp_products, (double)s_plan[4] + 1.0);   // the plan's cost, + U dU
   if (!ok && tid == 0) {
     st->error = 2;
     st->done = 1;

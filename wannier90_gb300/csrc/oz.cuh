@@ -34,6 +34,11 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int N) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(kTileRows >> 4) << 24);
 }
 
+// the same with A = B = F16 (the exp kernel's 8-bit digits)
+__host__ __device__ constexpr uint32_t idesc_f16(int N) {
+  return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(kTileRows >> 4) << 24);
+}
+
 // element (row, k) of a K-major tile with K_real columns, in bytes
 __device__ __forceinline__ uint32_t kmaj_off(int row, int k, int kreal) {
   return (uint32_t)((row >> 3) * (kreal >> 3) * 128 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
@@ -143,25 +148,11 @@ __device__ __forceinline__ void digits7x8(long long n, int x[7]) {
   x[0] = (int)n;
 }
 
-// The digits of digits7x8 as exact floats (f[t] = x[t]), without the serial recoding:
-// with C = 128 (1 + 2^8 + ... + 2^40), x_{6-t} = byte t of N + C minus 128 (t = 0..5) and
-// x_0 = (N + C) >> 48 (arithmetic).  (Adding 128 at every lower byte position turns the
-// centred digits into the plain bytes of N + C: x_6 = sext8(N mod 2^8) = byte0(N + 128) -
-// 128, and (N - x_6) / 2^8 = (N + 128) >> 8, so the next step repeats on N + 128 shifted.)
-// A byte b becomes the float b - 128 by one OR into 1.5 * 2^23 and one subtraction.
-__device__ __forceinline__ void digits7x8_f(long long n, float f[7]) {
-  const long long m = n + 0x808080808080LL;
-  const uint32_t lo = (uint32_t)m, hi = (uint32_t)((unsigned long long)m >> 32);
-#pragma unroll
-  for (int t = 0; t < 6; ++t) {
-    const uint32_t b = ((t < 4 ? lo >> (8 * t) : hi >> (8 * (t - 4))) & 255u);
-    f[6 - t] = __uint_as_float(0x4B400000u | b) - 12583040.0f;   // 1.5 * 2^23 + 128
-  }
-  f[0] = (float)(int)(m >> 48);
-}
-
-// The same for digits7 (7-bit digits of |N| <= 2^49): C = 64 (1 + 2^7 + ... + 2^35),
-// x_{6-t} = bits 7t..7t+6 of N + C minus 64, x_0 = (N + C) >> 42.
+// The digits of digits7 (7-bit digits of |N| <= 2^49) as exact floats (f[t] = x[t]),
+// without the serial recoding: with C = 64 (1 + 2^7 + ... + 2^35), x_{6-t} = bits
+// 7t..7t+6 of N + C minus 64 and x_0 = (N + C) >> 42 (arithmetic).  (Adding 64 at every
+// lower digit position turns the centred digits into the plain 7-bit fields of N + C.)  A
+// field b becomes the float b - 64 by one OR into 1.5 * 2^23 and one subtraction.
 __device__ __forceinline__ void digits7_f(long long n, float f[7]) {
   const long long m = n + 0x20408102040LL;
   const uint32_t lo = (uint32_t)m, hi = (uint32_t)((unsigned long long)m >> 32);
@@ -242,9 +233,9 @@ __device__ __forceinline__ double int64_scaled_to_double(long long S, int sc) {
 
 // sum_d D_d 2^(8(6-d)) * 2^sc for the 7 diagonal accumulators of the 8-bit-digit scheme
 // (|D_d| < 2^24): the top four and the bottom three diagonals are combined exactly in
-// int64 (< 2^49 and < 2^41) and their exact sum (< 2^73, int128) rounded once to FP64 with
-// integer ops -- the bits of converting both parts exactly and adding them in FP64, which
-// is what happens where the result could leave FP64's normal range
+// int64 (< 2^49 and < 2^41), converted exactly, and added once in FP64 (one rounding).
+// (Rounding their exact int128 sum with integer ops gives the same bits but measured
+// slower.)
 __device__ __forceinline__ double recombine7x8(const uint32_t* dd, int stride, int sc) {
   long long hi = float_to_int_exact24(__uint_as_float(dd[0]));
 #pragma unroll
@@ -252,7 +243,6 @@ __device__ __forceinline__ double recombine7x8(const uint32_t* dd, int stride, i
   long long lo = float_to_int_exact24(__uint_as_float(dd[4 * stride]));
 #pragma unroll
   for (int d = 5; d < 7; ++d) lo = (lo << 8) + float_to_int_exact24(__uint_as_float(dd[d * stride]));
-  if (sc > -900 && sc < 900) return int128_scaled_to_double(((__int128)hi << 24) + (__int128)lo, sc);
   return int64_scaled_to_double(hi, sc + 24) + int64_scaled_to_double(lo, sc);
 }
 
