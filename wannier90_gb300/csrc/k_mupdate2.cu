@@ -1,6 +1,6 @@
 // Tensor-core M update for num_wann <= 32, pipelined: M(k,b) = U(k)^H M0(k,b) U(k+b).
 //
-// The arithmetic is k_tensor.cu's (real embedding, 7 signed 7-bit BF16 digits per
+// The arithmetic is k_tensor.cu's (real embedding, 7 signed 7-bit FP16 digits per
 // operand, the 28 digit pairs of the 7 diagonals accumulated exactly in FP32 TMEM
 // columns, exact int64 recombination), so results are bitwise those of k_oz_mupdate;
 // only the schedule differs.  One persistent CTA per SM walks the work units
@@ -494,7 +494,7 @@ __global__ void __launch_bounds__(Roles<STEP>::THREADS, 1)
                     "{\n\t.reg .pred p;\n\t"
                     "setp.ne.b32 p, %4, 0;\n\t"
                     "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
-                    :: "r"(acc + (uint32_t)((t + u0) * NC)), "l"(ad), "l"(bd), "r"(idesc_bf16(n * NC)), "r"(accf)
+                    :: "r"(acc + (uint32_t)((t + u0) * NC)), "l"(ad), "l"(bd), "r"(idesc_f16(n * NC)), "r"(accf)
                     : "memory");
               }
             }
@@ -687,8 +687,8 @@ __global__ void __launch_bounds__(256) k_oz_preslice2(const Problem* __restrict_
         const uint32_t o = stage_off(r, l);
 #pragma unroll
         for (int t = 0; t < kS; ++t) {
-          *(uint16_t*)(dst + (size_t)t * L::PLANE + o) = int_to_bf16(xr[t]);
-          *(uint16_t*)(dst + (size_t)t * L::PLANE + o + 128) = int_to_bf16(xi[t]);
+          *(uint16_t*)(dst + (size_t)t * L::PLANE + o) = int_to_f16(xr[t]);
+          *(uint16_t*)(dst + (size_t)t * L::PLANE + o + 128) = int_to_f16(xi[t]);
         }
       }
     }

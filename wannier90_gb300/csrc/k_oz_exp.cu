@@ -457,11 +457,6 @@ __device__ __forceinline__ void load_run8(double (&v)[8], const double2* base, s
 // With 0x6400 above it, b is the FP16 number 1024 + b: one byte permute, one mask and one
 // packed subtraction of 1152 give two digits.  Exact: FP16 holds the integers to 2048, and
 // the difference of two of them is rounded to itself.
-__device__ __forceinline__ uint32_t f16x2_minus1152(uint32_t x) {
-  uint32_t r;
-  asm("sub.rn.f16x2 %0, %1, %2;" : "=r"(r) : "r"(x), "r"(0x64806480u));
-  return r;
-}
 __device__ __forceinline__ void slice_run8_h(uint32_t (&w)[7][4], const double (&v)[8], int ex) {
 #pragma unroll
   for (int i = 0; i < 8; i += 2) {
@@ -474,10 +469,10 @@ __device__ __forceinline__ void slice_run8_h(uint32_t (&w)[7][4], const double (
       const uint32_t bt = (uint32_t)(t & 3);
       const uint32_t sel = bt | (bt << 4) | ((4u + bt) << 8) | ((4u + bt) << 12);
       const uint32_t p = __byte_perm(t < 4 ? la : ha, t < 4 ? lb : hb, sel);
-      w[6 - t][i >> 1] = f16x2_minus1152((p & 0x00FF00FFu) | 0x64006400u);
+      w[6 - t][i >> 1] = f16x2_sub((p & 0x00FF00FFu) | 0x64006400u, 0x64806480u);
     }
     const uint32_t ta = (uint32_t)((int)(ma >> 48) + 128), tb = (uint32_t)((int)(mb >> 48) + 128);
-    w[0][i >> 1] = f16x2_minus1152(ta | (tb << 16) | 0x64006400u);
+    w[0][i >> 1] = f16x2_sub(ta | (tb << 16) | 0x64006400u, 0x64806480u);
   }
 }
 

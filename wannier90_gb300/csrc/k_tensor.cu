@@ -1,11 +1,11 @@
 // Tensor-core M update: M(k,b) = U(k)^H M0(k,b) U(k+b) with FP64-level accuracy from
-// BF16 tcgen05 MMAs (Ozaki-style exact slicing).
+// FP16 tcgen05 MMAs (Ozaki-style exact slicing).
 //
 // Every complex product is computed through its real embedding
 //     [C_r C_i] = [A_r A_i] [[B_r, B_i], [-B_i, B_r]]      (K = N = 2*WP real)
 // Each operand is scaled per row (A) / per column (B) by a power of two and split into
 // S = 7 signed 7-bit digits (x_1 in [-128,128], x_t in [-64,63] for t > 1), each an exact
-// BF16 value.  For every digit pair (t,u) with t+u <= S-1 (0-based) the MMA A^(t) B^(u)
+// FP16 value (built two at a time by a packed FP16 subtraction, pack_digits7).  For every digit pair (t,u) with t+u <= S-1 (0-based) the MMA A^(t) B^(u)
 // over the K = 2*WP reduction is exact in the FP32 accumulator (every partial sum is an
 // integer below 2^22), so the pairs of one diagonal d = t+u share one TMEM accumulator.
 // The epilogue recombines the 7 diagonals exactly in int64 and rounds once to FP64.
@@ -278,7 +278,7 @@ __global__ void __launch_bounds__(256, 1) k_oz_mupdate(const Problem* __restrict
                     "{\n\t.reg .pred p;\n\t"
                     "setp.ne.b32 p, %4, 0;\n\t"
                     "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
-                    :: "r"(dtm), "l"(ad), "l"(bd), "r"(idesc_bf16(n * NC)), "r"(acc)
+                    :: "r"(dtm), "l"(ad), "l"(bd), "r"(idesc_f16(n * NC)), "r"(acc)
                     : "memory");
               }
             }

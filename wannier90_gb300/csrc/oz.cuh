@@ -1,6 +1,6 @@
-// Exact BF16 slicing helpers shared by the tensor-core kernels (M update, exp):
-// power-of-two scales, signed 7-bit digits, tcgen05 descriptors, exact int64
-// recombination.  See k_tensor.cu for the scheme.
+// Exact slicing helpers shared by the tensor-core kernels (M update, exp): power-of-two
+// scales, signed 7- and 8-bit digits as FP16 (BF16 for the exp's 65..128-wide form),
+// tcgen05 descriptors, exact int64 recombination.  See k_tensor.cu for the scheme.
 #pragma once
 #include <cuda_bf16.h>
 
@@ -30,6 +30,7 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint3
 }
 
 // instruction descriptor, kind::f16: D = F32, A = B = BF16, both K-major, N, M = 128
+// (one MMA never mixes BF16 and FP16 operands)
 __host__ __device__ constexpr uint32_t idesc_bf16(int N) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(kTileRows >> 4) << 24);
 }
@@ -148,39 +149,47 @@ __device__ __forceinline__ void digits7x8(long long n, int x[7]) {
   x[0] = (int)n;
 }
 
-// The digits of digits7 (7-bit digits of |N| <= 2^49) as exact floats (f[t] = x[t]),
-// without the serial recoding: with C = 64 (1 + 2^7 + ... + 2^35), x_{6-t} = bits
-// 7t..7t+6 of N + C minus 64 and x_0 = (N + C) >> 42 (arithmetic).  (Adding 64 at every
-// lower digit position turns the centred digits into the plain 7-bit fields of N + C.)  A
-// field b becomes the float b - 64 by one OR into 1.5 * 2^23 and one subtraction.
-__device__ __forceinline__ void digits7_f(long long n, float f[7]) {
-  const long long m = n + 0x20408102040LL;
-  const uint32_t lo = (uint32_t)m, hi = (uint32_t)((unsigned long long)m >> 32);
-  const uint32_t mid = __funnelshift_r(lo, hi, 28);   // bits 28..59
-#pragma unroll
-  for (int t = 0; t < 6; ++t) {
-    const uint32_t b = (t < 4 ? lo >> (7 * t) : (t == 4 ? mid : hi >> 3)) & 127u;
-    f[6 - t] = __uint_as_float(0x4B400000u | b) - 12582976.0f;   // 1.5 * 2^23 + 64
-  }
-  f[0] = (float)(int)(m >> 42);
+// x - c for both halves of a packed FP16 pair (c packed likewise)
+__device__ __forceinline__ uint32_t f16x2_sub(uint32_t x, uint32_t c) {
+  uint32_t r;
+  asm("sub.rn.f16x2 %0, %1, %2;" : "=r"(r) : "r"(x), "r"(c));
+  return r;
 }
 
-// BF16 bits of two exact floats (values that BF16 holds) packed as (lo, hi) halves
-__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
-  return __byte_perm(__float_as_uint(lo), __float_as_uint(hi), 0x7632);
+// FP16 bits of a small integer (|x| <= 2048: exact)
+__device__ __forceinline__ uint16_t int_to_f16(int x) {
+  uint16_t r;
+  asm("cvt.rn.f16.s32 %0, %1;" : "=h"(r) : "r"(x));
+  return r;
 }
 
 // The seven 7-bit digit planes of 8 values scaled by 2^(49 - ex) (negated first when neg),
-// as packed BF16 pairs: w[t][i / 2] holds digit t of values i (low half) and i + 1 -- the
-// digits and BF16 bits of slicing the values one at a time.
+// as packed FP16 pairs: w[t][i / 2] holds digit t of values i (low half) and i + 1 -- the
+// digits of digits7, without its serial recoding.  With C = 64 (1 + 2^7 + ... + 2^35), bits
+// 7t'..7t'+6 of N + C are digit 6 - t' plus 64 (adding 64 at every lower digit position
+// turns the centred digits into the plain 7-bit fields of N + C), and the top digit is
+// (N + C) >> 42 (arithmetic), in [-128, 128].  Two values' 14-bit windows side by side in
+// one word (one byte permute) give two fields of both per mask; with 0x6400 above it a
+// field b is the FP16 number 1024 + b, so one packed subtraction of 1088 (top digit: of
+// 1152, after adding 128) leaves the digits.  Exact: FP16 holds the integers to 2048, and
+// the difference of two of them is rounded to itself.
 __device__ __forceinline__ void pack_digits7(uint32_t (&w)[kS][4], const double (&v)[8], int ex, bool neg) {
 #pragma unroll
   for (int i = 0; i < 8; i += 2) {
-    float fa[kS], fb[kS];
-    digits7_f(scaled_int(neg ? -v[i] : v[i], ex), fa);
-    digits7_f(scaled_int(neg ? -v[i + 1] : v[i + 1], ex), fb);
+    const long long ma = scaled_int(neg ? -v[i] : v[i], ex) + 0x20408102040LL;
+    const long long mb = scaled_int(neg ? -v[i + 1] : v[i + 1], ex) + 0x20408102040LL;
+    const uint32_t la = (uint32_t)ma, lb = (uint32_t)mb;
+    const uint32_t ha = (uint32_t)((unsigned long long)ma >> 32), hb = (uint32_t)((unsigned long long)mb >> 32);
+    // bits 0-13, 14-27 and 28-41 of a (low half) and b (high half)
+    const uint32_t q[3] = {__byte_perm(la, lb, 0x5410), __byte_perm(la >> 14, lb >> 14, 0x5410),
+                           __byte_perm(__funnelshift_r(la, ha, 28), __funnelshift_r(lb, hb, 28), 0x5410)};
 #pragma unroll
-    for (int t = 0; t < kS; ++t) w[t][i >> 1] = pack_bf16x2(fa[t], fb[t]);
+    for (int j = 0; j < 3; ++j) {
+      w[6 - 2 * j][i >> 1] = f16x2_sub((q[j] & 0x007F007Fu) | 0x64006400u, 0x64406440u);
+      w[5 - 2 * j][i >> 1] = f16x2_sub(((q[j] >> 7) & 0x007F007Fu) | 0x64006400u, 0x64406440u);
+    }
+    const uint32_t ta = (uint32_t)((int)(ma >> 42) + 128), tb = (uint32_t)((int)(mb >> 42) + 128);
+    w[0][i >> 1] = f16x2_sub(ta | (tb << 16) | 0x64006400u, 0x64806480u);
   }
 }
 
