@@ -35,7 +35,8 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int N) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(kTileRows >> 4) << 24);
 }
 
-// the same with A = B = F16 (the exp kernel's 8-bit digits)
+// the same with A = B = F16 (the FP16 digit planes of the M update and of the exp's
+// second product form)
 __host__ __device__ constexpr uint32_t idesc_f16(int N) {
   return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(kTileRows >> 4) << 24);
 }
