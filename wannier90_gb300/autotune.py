@@ -19,8 +19,8 @@ The padded tile width (8 / 16 / 32 / 64 / 128) follows from num_wann.  For each 
 tuner times a few iterations of a seeded tight-binding probe (sc lattice, 4x4x4 k-mesh,
 nntot 6) in every candidate on the current GPU and keeps the fastest; all candidates
 give the same minimum (the tensor ones bitwise the same M update).  Results are cached
-per process and, optionally, in a JSON file.  The batched and served forms ask
-:func:`options` per problem.
+per process; :func:`table` also writes them to a JSON file.  The batched and served forms
+ask :func:`options` per problem.
 """
 from __future__ import annotations
 
